@@ -1,0 +1,241 @@
+"""Input decks for the collocation-BEM path: quad8 surface meshes and nodal
+boundary conditions, in the form MultiFEBE's input pipeline hands to its region
+builders (one BE region, ordinary boundaries, continuous quad8 elements).
+
+A deck is what a MultiFEBE ``.dat`` + ``.msh`` pair describes for this path:
+node coordinates, element connectivity (quad8 node order of
+lib/fbem/src/resources_shape_functions/xi_quad8.rc, element normal T1 x T2
+pointing out of the region), and per node and direction the boundary condition
+type (0: displacement known, 1: traction known) with its value
+(``[conditions over nodes]``, docs/manual/manual.tex:2010-2036).
+
+Element order is face by face and row by row; DOF numbering follows from it
+(first appearance of a node over elements, see
+src/build_auxiliary_variables_mechanics_static.f90:60-140).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Deck:
+    name: str
+    nodes: np.ndarray          # (nn, 3) float64
+    conn: np.ndarray           # (ne, 8) int32, 0-based
+    ctype: np.ndarray          # (nn, 3) int32: 0 displacement known, 1 traction known
+    cvalue: np.ndarray         # (nn, 3) complex128
+    boundary_of_element: np.ndarray = field(default=None)  # (ne,) face id (informational)
+
+    @property
+    def n_nodes(self) -> int:
+        return int(self.nodes.shape[0])
+
+    @property
+    def n_elements(self) -> int:
+        return int(self.conn.shape[0])
+
+    @property
+    def n_dof(self) -> int:
+        return 3 * self.n_nodes
+
+
+# faces of an axis-aligned box: (axis, side, u, v) with u x v the outward normal
+_BOX_FACES = [
+    (2, 0, 1, 0),  # z = 0, normal -z: u = +y, v = +x
+    (2, 1, 0, 1),  # z = L, normal +z
+    (0, 0, 2, 1),  # x = 0, normal -x: u = +z, v = +y
+    (0, 1, 1, 2),  # x = L, normal +x
+    (1, 0, 0, 2),  # y = 0, normal -y
+    (1, 1, 2, 0),  # y = L, normal +y
+]
+
+
+def _quad8_from_corner(p1, du, dv):
+    """Integer half-step coordinates of the 8 nodes of the quad whose corner 1 is
+    p1 and whose sides are du (xi1) and dv (xi2)."""
+    p1 = np.asarray(p1)
+    du = np.asarray(du)
+    dv = np.asarray(dv)
+    return [p1, p1 + du, p1 + du + dv, p1 + dv,
+            p1 + du // 2, p1 + du + dv // 2, p1 + dv + du // 2, p1 + dv // 2]
+
+
+def box(dims=(1.0, 1.0, 1.0), divs=(4, 4, 4), split_faces=False, name="box"):
+    """Closed quad8 surface of the box [0,Lx]x[0,Ly]x[0,Lz].
+
+    split_faces=False: one closed boundary with shared nodes (18 n^2 + 2 nodes
+    for an n x n x n cube). split_faces=True: six boundaries with their own nodes
+    (duplicated along the box edges), the layout of the reference tutorials.
+    """
+    dims = np.asarray(dims, dtype=np.float64)
+    divs = np.asarray(divs, dtype=np.int64)
+    key_to_node = {}
+    coords = []
+    conn = []
+    face_of = []
+    for fid, (axis, side, ua, va) in enumerate(_BOX_FACES):
+        nu, nv = int(divs[ua]), int(divs[va])
+        for b in range(nv):
+            for a in range(nu):
+                p1 = np.zeros(3, dtype=np.int64)
+                p1[axis] = side * 2 * divs[axis]
+                p1[ua] = 2 * a
+                p1[va] = 2 * b
+                du = np.zeros(3, dtype=np.int64)
+                dv = np.zeros(3, dtype=np.int64)
+                du[ua] = 2
+                dv[va] = 2
+                el = []
+                for p in _quad8_from_corner(p1, du, dv):
+                    key = (fid if split_faces else -1, int(p[0]), int(p[1]), int(p[2]))
+                    if key not in key_to_node:
+                        key_to_node[key] = len(coords)
+                        coords.append(p * dims / (2 * divs))
+                    el.append(key_to_node[key])
+                conn.append(el)
+                face_of.append(fid)
+    nodes = np.array(coords, dtype=np.float64)
+    conn = np.array(conn, dtype=np.int32)
+    nn = nodes.shape[0]
+    ctype = np.ones((nn, 3), dtype=np.int32)
+    cvalue = np.zeros((nn, 3), dtype=np.complex128)
+    return Deck(name, nodes, conn, ctype, cvalue, np.array(face_of, dtype=np.int32))
+
+
+def cube_clamped_top_traction(n, L=1.0, traction=(0.0, 0.0, -1.0), name=None):
+    """Unit cube, n x n quad8 per face, one closed boundary with shared nodes.
+    Bottom-face nodes (z=0, edges included): u = 0. Top-face nodes (z=L, edges
+    included): t = traction. All other nodes traction-free."""
+    d = box((L, L, L), (n, n, n), split_faces=False, name=name or f"cube{n}")
+    z = d.nodes[:, 2]
+    tol = 1e-12 * L
+    top = np.abs(z - L) <= tol
+    bot = np.abs(z) <= tol
+    d.ctype[:] = 1
+    d.cvalue[:] = 0.0
+    d.cvalue[top] = np.asarray(traction, dtype=np.complex128)
+    d.ctype[bot] = 0
+    d.cvalue[bot] = 0.0
+    return d
+
+
+def cube_confined_kat(n, L=1.0, P=1.0):
+    """Confined cube of docs/examples/ME-ST-EL-002 (rollers on five faces,
+    traction P on x=L), six boundaries with duplicated edge nodes as in the
+    tutorial deck t2.dat. Exact field: u1 = (1+nu)(1-2nu)/(E(1-nu)) P x1."""
+    d = box((L, L, L), (n, n, n), split_faces=True, name=f"kat_s{n}")
+    d.ctype[:] = 1
+    d.cvalue[:] = 0.0
+    for e in range(d.n_elements):
+        axis, side, _, _ = _BOX_FACES[int(d.boundary_of_element[e])]
+        for s in d.conn[e]:
+            if axis == 0 and side == 1:
+                d.ctype[s] = 1
+                d.cvalue[s] = (P, 0.0, 0.0)
+            else:
+                d.ctype[s, axis] = 0
+                d.cvalue[s, axis] = 0.0
+    return d
+
+
+def slab(nxy=16, nz=1, dims=(1.0, 1.0, 0.02), traction_top=(0.0, 0.0, -1.0)):
+    """Thin slab: nxy x nxy quad8 on each large face, nxy x nz on each edge face.
+    Face x=0 clamped (u=0 on its nodes, edges included); top face (z=Lz)
+    loaded with traction_top; all other nodes traction-free."""
+    d = box(dims, (nxy, nxy, nz), split_faces=False, name=f"slab{nxy}x{nz}")
+    tol = 1e-12
+    x = d.nodes[:, 0]
+    z = d.nodes[:, 2]
+    d.ctype[:] = 1
+    d.cvalue[:] = 0.0
+    top = np.abs(z - dims[2]) <= tol
+    d.cvalue[top] = np.asarray(traction_top, dtype=np.complex128)
+    clamp = np.abs(x) <= tol
+    d.ctype[clamp] = 0
+    d.cvalue[clamp] = 0.0
+    return d
+
+
+def surface_patch(half=10.0, n=40, load_half=1.0, traction=(0.0, 0.0, -1.0)):
+    """Open square patch [-half,half]^2 of the free surface z=0 (normal +z, out
+    of the half-space z<0), n x n quad8 elements, traction on the nodes with
+    |x|,|y| <= load_half, traction-free elsewhere. Rim nodes lie on the mesh
+    boundary and get the SBIE-MCA formulation."""
+    h = 2.0 * half / n
+    key_to_node = {}
+    coords = []
+    conn = []
+    for b in range(n):
+        for a in range(n):
+            p1 = np.array([2 * a, 2 * b, 0])
+            el = []
+            for p in _quad8_from_corner(p1, np.array([2, 0, 0]), np.array([0, 2, 0])):
+                key = (int(p[0]), int(p[1]))
+                if key not in key_to_node:
+                    key_to_node[key] = len(coords)
+                    coords.append([-half + 0.5 * h * p[0], -half + 0.5 * h * p[1], 0.0])
+                el.append(key_to_node[key])
+            conn.append(el)
+    nodes = np.array(coords, dtype=np.float64)
+    conn = np.array(conn, dtype=np.int32)
+    nn = nodes.shape[0]
+    ctype = np.ones((nn, 3), dtype=np.int32)
+    cvalue = np.zeros((nn, 3), dtype=np.complex128)
+    tol = 1e-9
+    loaded = (np.abs(nodes[:, 0]) <= load_half + tol) & (np.abs(nodes[:, 1]) <= load_half + tol)
+    cvalue[loaded] = np.asarray(traction, dtype=np.complex128)
+    return Deck(f"patch{n}", nodes, conn, ctype, cvalue, np.zeros(len(conn), dtype=np.int32))
+
+
+# ----------------------------------------------------------------------------
+# Materials
+# ----------------------------------------------------------------------------
+
+def elastic(E=1.0, nu=0.25):
+    """Static elastic region: (mu, nu) as the staela builder reads them."""
+    return {"mu": E / (2.0 * (1.0 + nu)), "nu": nu}
+
+
+def viscoelastic(E=1.0, nu=0.25, rho=1.0, xi=0.05):
+    """Viscoelastic region as src/read_regions.f90:938-948 builds it: complex
+    mu* = mu (1 + 2 i xi), lambda* = 2 mu* nu / (1 - 2 nu), complex-typed nu."""
+    mu = E / (2.0 * (1.0 + nu))
+    muc = mu * (1.0 + 2.0j * xi)
+    lam = 2.0 * muc * nu / (1.0 - 2.0 * nu)
+    cs = np.sqrt(mu / rho)
+    return {"mu": muc, "lambda": lam, "nu": complex(nu), "rho": rho, "mu_real": mu, "c_s": cs}
+
+
+def omega_from_a0(a0, mat, L=1.0):
+    """Dimensionless frequency a0 = omega L / c_s with the undamped c_s."""
+    return np.asarray(a0, dtype=np.float64) * mat["c_s"] / L
+
+
+# ----------------------------------------------------------------------------
+# The five workloads of the benchmark definition
+# ----------------------------------------------------------------------------
+
+def workload(cfg: int):
+    """Deck, material and frequencies (None for static) of workload cfg (1..5)."""
+    if cfg == 1:
+        return cube_clamped_top_traction(4), elastic(1.0, 0.25), None
+    if cfg == 2:
+        m = viscoelastic(1.0, 0.25, 1.0, 0.05)
+        return cube_clamped_top_traction(8), m, omega_from_a0(np.linspace(0.1, 2.0, 20), m)
+    if cfg == 3:
+        m = viscoelastic(1.0, 0.33, 1.0, 0.05)
+        return surface_patch(10.0, 40, 1.0), m, omega_from_a0([0.5], m)
+    if cfg == 5:
+        m = viscoelastic(1.0, 0.3, 1.0, 0.02)
+        return slab(16, 1), m, omega_from_a0([0.2, 1.0], m)
+    raise ValueError(cfg)
+
+
+def batch_workload():
+    """Workload 4: cubes n in {4,5,6,7,8,10} per face x 8 frequencies."""
+    m = viscoelastic(1.0, 0.25, 1.0, 0.05)
+    om = omega_from_a0(np.linspace(0.2, 1.6, 8), m)
+    return [(cube_clamped_top_traction(n), m, om) for n in (4, 5, 6, 7, 8, 10)]

@@ -1,0 +1,186 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
+arm load this module. The oracle restates MultiFEBE's collocation BEM path
+(see orc.h) and solves the assembled systems with LAPACK getrf/getrs through
+scipy (OpenBLAS), as src/solve_lse_r.f90:137,189 and src/solve_lse_c.f90:124,176 do.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liborc.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_long)
+
+
+def build(force=False):
+    if force or not os.path.exists(LIB) or any(
+            os.path.getmtime(os.path.join(HERE, f)) > os.path.getmtime(LIB)
+            for f in os.listdir(HERE) if f.endswith((".cpp", ".h"))):
+        subprocess.check_call(["make", "-s", "-C", HERE])
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.orc_problem_new.restype = ctypes.c_void_p
+        L.orc_problem_new.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip, _ip, _dp, ctypes.c_double, ctypes.c_int,
+                                      ctypes.c_int, _ip, ctypes.c_double]
+        L.orc_problem_free.argtypes = [ctypes.c_void_p]
+        L.orc_n_dof.argtypes = [ctypes.c_void_p]
+        L.orc_n_colloc.argtypes = [ctypes.c_void_p]
+        L.orc_dof_map.argtypes = [ctypes.c_void_p, _ip, _ip]
+        L.orc_element_data.argtypes = [ctypes.c_void_p, _dp, _ip, _dp]
+        L.orc_colloc.argtypes = [ctypes.c_void_p, _dp, _ip]
+        L.orc_node_geometry.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, ctypes.c_char_p]
+        L.orc_assemble_staela.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _dp, _dp, ctypes.c_int,
+                                          _lp]
+        L.orc_assemble_harela_nu.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 8 + [_dp, _dp, ctypes.c_int, _lp]
+        L.orc_pair_staela.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                      _dp, _dp]
+        L.orc_pair_harela.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6 + [_dp, _dp]
+        L.orc_harela_parameters.argtypes = [ctypes.c_double] * 6 + [_dp]
+        L.orc_gauss_tables.argtypes = [_dp] * 4
+        L.orc_qs_parameters.argtypes = [ctypes.c_double, _dp]
+        L.orc_qs_estimate.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp]
+        L.orc_zexp.argtypes = [ctypes.c_double, ctypes.c_double, _dp]
+        L.orc_nearest_quad8.argtypes = [_dp, ctypes.c_double, _dp, _dp, _dp, _dp, _ip]
+        L.orc_freeterm.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp]
+        _lib = L
+    return _lib
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+# settings defaults, src/read_settings.f90:86,101,143-145,164
+DEFAULTS = dict(qsi_re=1e-6, ns_max=16, ps_gln=(2, 3, 4, 5, 6, 7, 8, 9), geo_tol=1e-6)
+
+
+class Problem:
+    """One BE region of a deck prepared as the reference's build_data* and
+    build_auxiliary_variables_* leave it."""
+
+    def __init__(self, deck, **settings):
+        s = dict(DEFAULTS)
+        s.update(settings)
+        self.deck = deck
+        L = lib()
+        X = np.ascontiguousarray(deck.nodes, dtype=np.float64)
+        conn = np.ascontiguousarray(deck.conn, dtype=np.int32)
+        ct = np.ascontiguousarray(deck.ctype, dtype=np.int32)
+        cv = np.ascontiguousarray(deck.cvalue, dtype=np.complex128).view(np.float64)
+        gl = np.array(s["ps_gln"], dtype=np.int32)
+        self._h = L.orc_problem_new(deck.n_nodes, _p(X), deck.n_elements, _p(conn, _ip), _p(ct, _ip), _p(cv),
+                                    s["qsi_re"], s["ns_max"], len(gl), _p(gl, _ip), s["geo_tol"])
+        self.n = L.orc_n_dof(self._h)
+        self.settings = s
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_problem_free(self._h)
+            self._h = None
+
+    def dof_map(self):
+        nn = self.deck.n_nodes
+        dof = np.zeros(3 * nn, dtype=np.int32)
+        order = np.zeros(nn, dtype=np.int32)
+        lib().orc_dof_map(self._h, _p(dof, _ip), _p(order, _ip))
+        return dof.reshape(nn, 3), order
+
+    def element_data(self):
+        ne = self.deck.n_elements
+        cl = np.zeros(ne)
+        gf = np.zeros(ne, dtype=np.int32)
+        ball = np.zeros((ne, 4))
+        lib().orc_element_data(self._h, _p(cl), _p(gf, _ip), _p(ball))
+        return cl, gf, ball
+
+    def colloc(self):
+        m = lib().orc_n_colloc(self._h)
+        x = np.zeros((m, 3))
+        info = np.zeros((m, 4), dtype=np.int32)
+        lib().orc_colloc(self._h, _p(x), _p(info, _ip))
+        return x, info
+
+    def assemble_staela(self, mu, nu, nthreads=0):
+        n = self.n
+        A = np.zeros((n, n), dtype=np.float64, order="F")
+        b = np.zeros(n, dtype=np.float64)
+        st = np.zeros(6, dtype=np.int64)
+        rc = lib().orc_assemble_staela(self._h, mu, nu, _p(A), _p(b), nthreads, _p(st, _lp))
+        if rc != 0:
+            raise RuntimeError("oracle: invalid normals/tangents configuration at a free-term node")
+        self.stats = st
+        return A, b
+
+    def assemble_harela(self, mat, omega, nthreads=0):
+        n = self.n
+        A = np.zeros((n, n), dtype=np.complex128, order="F")
+        b = np.zeros(n, dtype=np.complex128)
+        st = np.zeros(6, dtype=np.int64)
+        lam, mu, nu = complex(mat["lambda"]), complex(mat["mu"]), complex(mat["nu"])
+        rc = lib().orc_assemble_harela_nu(self._h, lam.real, lam.imag, mu.real, mu.imag, float(mat["rho"]),
+                                          float(omega), nu.real, nu.imag, _p(A), _p(b), nthreads, _p(st, _lp))
+        if rc != 0:
+            raise RuntimeError("oracle: invalid normals/tangents configuration at a free-term node")
+        self.stats = st
+        return A, b
+
+    def pair_staela(self, ci, e, mu, nu):
+        h = np.zeros((8, 3, 3))
+        g = np.zeros((8, 3, 3))
+        cls = lib().orc_pair_staela(self._h, ci, e, mu, nu, _p(h), _p(g))
+        return cls, h, g
+
+    def pair_harela(self, ci, e, mat, omega):
+        h = np.zeros((8, 3, 3), dtype=np.complex128)
+        g = np.zeros((8, 3, 3), dtype=np.complex128)
+        lam, mu = complex(mat["lambda"]), complex(mat["mu"])
+        cls = lib().orc_pair_harela(self._h, ci, e, lam.real, lam.imag, mu.real, mu.imag, float(mat["rho"]),
+                                    float(omega), _p(h), _p(g))
+        return cls, h, g
+
+    def solution(self, x):
+        """Nodal (u, t) from the solved unknown vector: the variable of each
+        (node, direction) DOF is u if the traction is known, t otherwise
+        (src/assign_solution_mechanics_static.f90:130-150)."""
+        d = self.deck
+        dof, _ = self.dof_map()
+        u = np.zeros((d.n_nodes, 3), dtype=x.dtype)
+        t = np.zeros((d.n_nodes, 3), dtype=x.dtype)
+        known_u = d.ctype == 0
+        u[known_u] = d.cvalue[known_u].astype(x.dtype) if np.iscomplexobj(x) else d.cvalue[known_u].real
+        t[~known_u] = d.cvalue[~known_u].astype(x.dtype) if np.iscomplexobj(x) else d.cvalue[~known_u].real
+        vals = x[dof]
+        u[~known_u] = vals[~known_u]
+        t[known_u] = vals[known_u]
+        return u, t
+
+
+def lu_solve(A, b, threads=None):
+    """getrf + getrs (partial pivoting) through scipy's OpenBLAS."""
+    import scipy.linalg as sl
+    lu, piv = sl.lu_factor(A, overwrite_a=False, check_finite=False)
+    return sl.lu_solve((lu, piv), b, check_finite=False)
+
+
+def gauss_tables():
+    a = [np.zeros(32 * 32) for _ in range(4)]
+    lib().orc_gauss_tables(*[_p(x) for x in a])
+    return [x.reshape(32, 32) for x in a]  # [rule-1, point-1]

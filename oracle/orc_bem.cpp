@@ -1,0 +1,1123 @@
+// Oracle (test infrastructure only): staela / harela SBIE element integration,
+// free terms, the region builders' collocation loops and the equation scatter,
+// plus the C entry points the Python tests load with ctypes.
+#include "orc.h"
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <algorithm>
+#include <omp.h>
+
+namespace orc {
+
+// ---------------------------------------------------------------------------
+// Element prepared for integration: fbem_bem_element subset
+// (lib/fbem/src/bem_general.f90:51-107) for continuous quad8 elements, with the
+// precalculated datasets of init_precalculated_datasets (bem_general.f90:163-759).
+// phi^p == phi^s here (same quad8 functional interpolation, delta=0).
+// ---------------------------------------------------------------------------
+struct Elem {
+  double x[8][3];
+  double cl;
+  int gln_far;
+  double bc[3], br;
+  int n_ps;
+  int ps_gln[16], ps_ngp[16], ps_off[16];
+  int ps_gln_max;
+  std::vector<double> px, pn, pphijw;  // [off+kip][3], [3], [8]
+};
+
+static void init_precalculated(Elem& e, int n_ps, const int* ps_gln) {
+  e.n_ps = n_ps;
+  int off = 0;
+  e.ps_gln_max = 0;
+  for (int i = 0; i < n_ps; ++i) {
+    e.ps_gln[i] = ps_gln[i];
+    e.ps_ngp[i] = ps_gln[i] * ps_gln[i];
+    e.ps_off[i] = off;
+    off += e.ps_ngp[i];
+    if (ps_gln[i] > e.ps_gln_max) e.ps_gln_max = ps_gln[i];
+  }
+  e.px.assign(off * 3, 0.0);
+  e.pn.assign(off * 3, 0.0);
+  e.pphijw.assign(off * 8, 0.0);
+  for (int i = 0; i < n_ps; ++i) {
+    int g = e.ps_gln[i];
+    for (int k1 = 1; k1 <= g; ++k1)
+      for (int k2 = 1; k2 <= g; ++k2) {
+        int kt = e.ps_off[i] + (k2 - 1) + (k1 - 1) * g;
+        double xi[2] = {gl11_xi(k1, g), gl11_xi(k2, g)};
+        double w1 = gl11_w(k1, g), w2 = gl11_w(k2, g);
+        double phi[8], d1[8], d2[8];
+        phi_quad8(xi, phi);
+        dphi_quad8(xi, d1, d2);
+        double xp[3] = {0, 0, 0}, T1[3] = {0, 0, 0}, T2[3] = {0, 0, 0};
+        for (int k = 0; k < 8; ++k)
+          for (int c = 0; c < 3; ++c) {
+            xp[c] = xp[c] + phi[k] * e.x[k][c];
+            T1[c] = T1[c] + d1[k] * e.x[k][c];
+            T2[c] = T2[c] + d2[k] * e.x[k][c];
+          }
+        double N[3] = {T1[1] * T2[2] - T1[2] * T2[1], T1[2] * T2[0] - T1[0] * T2[2],
+                       T1[0] * T2[1] - T1[1] * T2[0]};
+        double j = std::sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+        for (int c = 0; c < 3; ++c) {
+          e.px[kt * 3 + c] = xp[c];
+          e.pn[kt * 3 + c] = N[c] / j;
+        }
+        for (int k = 0; k < 8; ++k) e.pphijw[kt * 8 + k] = phi[k] * j * w1 * w2;
+      }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Harmonic parameters: fbem_bem_harela3d_calculate_parameters
+// (bem_harela3d.f90:143-287), u*/t* coefficient subset.
+// ---------------------------------------------------------------------------
+struct HarPar {
+  cplx k1, k2, c1, c2;
+  cplx psi[6], chi[6], T1[10], T2[9], T3[9];
+  cplx cte_u, cte_t;
+};
+static HarPar harela_parameters(cplx lambda, cplx mu, double rho, double omega) {
+  HarPar p;
+  const cplx I(0.0, 1.0);
+  cplx c1 = std::sqrt((lambda + 2.0 * mu) / rho);
+  cplx c2 = std::sqrt(mu / rho);
+  cplx k1 = omega / c1, k2 = omega / c2;
+  p.c1 = c1; p.c2 = c2; p.k1 = k1; p.k2 = k2;
+  cplx c1p2 = c1 * c1, c2p2 = c2 * c2, c1p3 = c1p2 * c1, c1p4 = c1p2 * c1p2;
+  cplx k2p2 = k2 * k2;
+  cplx ik1 = I * k1, ik2 = I * k2;
+  cplx ik1p2 = ik1 * ik1, ik2p2 = ik2 * ik2;
+  cplx r = c2p2 / c1p2;
+  double om2 = omega * omega;
+  p.psi[0] = 0.5 * (1.0 + r);
+  p.psi[1] = -1.0 / 3.0 * (2.0 / c2 + c2p2 / c1p3) * I * omega;
+  p.psi[2] = I * k1 / k2p2;
+  p.psi[3] = 1.0 / ik2;
+  p.psi[4] = 1.0 / k2p2;
+  p.psi[5] = -1.0 / k2p2;
+  p.chi[0] = -0.5 * (1.0 - r);
+  p.chi[1] = -r;
+  p.chi[2] = -3.0 * r / ik1;
+  p.chi[3] = 3.0 / ik2;
+  p.chi[4] = -3.0 * r / ik1p2;
+  p.chi[5] = 3.0 / ik2p2;
+  p.T1[0] = 3.0 * (r - 1.0);
+  p.T1[1] = -0.25 * (1.0 / c2p2 - c2p2 / c1p4) * om2;
+  p.T1[2] = -2.0 * I * k1 * r;
+  p.T1[3] = 2.0 * I * k2;
+  p.T1[4] = -12.0 * r;
+  p.T1[5] = 12.0;
+  p.T1[6] = -r * 30.0 / ik1;
+  p.T1[7] = 30.0 / ik2;
+  p.T1[8] = -r * 30.0 / ik1p2;
+  p.T1[9] = 30.0 / ik2p2;
+  p.T2[0] = -r;
+  p.T2[1] = -0.25 * (1.0 / c2p2 + c2p2 / c1p4) * om2;
+  p.T2[2] = -I * k2;
+  p.T2[3] = 2.0 * r;
+  p.T2[4] = -3.0;
+  p.T2[5] = r * 6.0 / ik1;
+  p.T2[6] = -6.0 / ik2;
+  p.T2[7] = r * 6.0 / ik1p2;
+  p.T2[8] = -6.0 / ik2p2;
+  p.T3[0] = r;
+  p.T3[1] = 0.25 * (3.0 * c2p2 / c1p4 - 2.0 / c1p2 + 1.0 / c2p2) * om2;
+  p.T3[2] = (2.0 * r - 1.0) * I * k1;
+  p.T3[3] = 4.0 * r - 1.0;
+  p.T3[4] = -2.0;
+  p.T3[5] = r * 6.0 / ik1;
+  p.T3[6] = -6.0 / ik2;
+  p.T3[7] = r * 6.0 / ik1p2;
+  p.T3[8] = -6.0 / ik2p2;
+  p.cte_u = c_1_4pi / mu;
+  p.cte_t = cplx(c_1_4pi, 0.0);
+  return p;
+}
+
+// Per integration point evaluation of the fundamental solutions without their
+// constants. Static: bem_staela3d.f90:622-633; harmonic: bem_harela3d.f90:654-688.
+struct StaelaK {
+  typedef double T;
+  double cteu1, cteu2, ctet1, ctet2;
+  StaelaK(double mu, double nu) {
+    cteu1 = 1.0 / (16.0 * c_pi * mu * (1.0 - nu));
+    cteu2 = 3.0 - 4.0 * nu;
+    ctet1 = -1.0 / (8.0 * c_pi * (1.0 - nu));
+    ctet2 = 1.0 - 2.0 * nu;
+  }
+  T cu() const { return cteu1; }
+  T ct() const { return ctet1; }
+  inline void eval(const double rv[3], const double n[3], T fu[3][3], T ft[3][3]) const {
+    double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    double d1r = 1.0 / r, d1r2 = d1r * d1r;
+    double drdx[3] = {rv[0] * d1r, rv[1] * d1r, rv[2] * d1r};
+    double drdn = drdx[0] * n[0] + drdx[1] * n[1] + drdx[2] * n[2];
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        double dk = (il == ik) ? 1.0 : 0.0;
+        fu[il][ik] = d1r * (cteu2 * dk + drdx[il] * drdx[ik]);
+        ft[il][ik] = d1r2 * ((ctet2 * dk + 3.0 * drdx[il] * drdx[ik]) * drdn +
+                             ctet2 * (n[il] * drdx[ik] - n[ik] * drdx[il]));
+      }
+  }
+};
+struct HarelaK {
+  typedef cplx T;
+  HarPar p;
+  explicit HarelaK(const HarPar& pp) : p(pp) {}
+  T cu() const { return p.cte_u; }
+  T ct() const { return p.cte_t; }
+  inline void coeffs(double r, cplx& psi, cplx& chi, cplx& TT1, cplx& TT2, cplx& TT3, double& d1r1,
+                     double& d1r2, bool full) const {
+    d1r1 = 1.0 / r;
+    d1r2 = d1r1 * d1r1;
+    double d1r3 = d1r2 * d1r1, d1r4 = d1r3 * d1r1;
+    const cplx I(0.0, 1.0);
+    cplx z[2] = {-I * p.k1 * r, -I * p.k2 * r};
+    cplx E[7][2];
+    zexp_decomposed(2, z, E);
+    for (int j = 0; j < 2; ++j) {
+      E[2][j] = E[2][j] * d1r1;
+      E[3][j] = E[3][j] * d1r2;
+      E[4][j] = E[4][j] * d1r3;
+      E[5][j] = E[5][j] * d1r4;
+    }
+    psi = p.psi[0] * d1r1 + p.psi[1] + E[2][1] + p.psi[2] * E[3][0] + p.psi[3] * E[3][1] + p.psi[4] * E[4][0] +
+          p.psi[5] * E[4][1];
+    chi = p.chi[0] * d1r1 + p.chi[1] * E[2][0] + E[2][1] + p.chi[2] * E[3][0] + p.chi[3] * E[3][1] +
+          p.chi[4] * E[4][0] + p.chi[5] * E[4][1];
+    if (full) {
+      TT1 = p.T1[0] * d1r2 + p.T1[1] + p.T1[2] * E[2][0] + p.T1[3] * E[2][1] + p.T1[4] * E[3][0] +
+            p.T1[5] * E[3][1] + p.T1[6] * E[4][0] + p.T1[7] * E[4][1] + p.T1[8] * E[5][0] + p.T1[9] * E[5][1];
+      TT2 = p.T2[0] * d1r2 + p.T2[1] + p.T2[2] * E[2][1] + p.T2[3] * E[3][0] + p.T2[4] * E[3][1] +
+            p.T2[5] * E[4][0] + p.T2[6] * E[4][1] + p.T2[7] * E[5][0] + p.T2[8] * E[5][1];
+      TT3 = p.T3[0] * d1r2 + p.T3[1] + p.T3[2] * E[2][0] + p.T3[3] * E[3][0] + p.T3[4] * E[3][1] +
+            p.T3[5] * E[4][0] + p.T3[6] * E[4][1] + p.T3[7] * E[5][0] + p.T3[8] * E[5][1];
+    } else {  // regular parts only (bem_harela3d.f90 sbie_int)
+      TT1 = p.T1[1] + p.T1[2] * E[2][0] + p.T1[3] * E[2][1] + p.T1[4] * E[3][0] + p.T1[5] * E[3][1] +
+            p.T1[6] * E[4][0] + p.T1[7] * E[4][1] + p.T1[8] * E[5][0] + p.T1[9] * E[5][1];
+      TT2 = p.T2[1] + p.T2[2] * E[2][1] + p.T2[3] * E[3][0] + p.T2[4] * E[3][1] + p.T2[5] * E[4][0] +
+            p.T2[6] * E[4][1] + p.T2[7] * E[5][0] + p.T2[8] * E[5][1];
+      TT3 = p.T3[1] + p.T3[2] * E[2][0] + p.T3[3] * E[3][0] + p.T3[4] * E[3][1] + p.T3[5] * E[4][0] +
+            p.T3[6] * E[4][1] + p.T3[7] * E[5][0] + p.T3[8] * E[5][1];
+    }
+  }
+  inline void eval(const double rv[3], const double n[3], T fu[3][3], T ft[3][3]) const {
+    double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    cplx psi, chi, TT1, TT2, TT3;
+    double d1r1, d1r2;
+    coeffs(r, psi, chi, TT1, TT2, TT3, d1r1, d1r2, true);
+    double drdx[3] = {rv[0] * d1r1, rv[1] * d1r1, rv[2] * d1r1};
+    double drdn = drdx[0] * n[0] + drdx[1] * n[1] + drdx[2] * n[2];
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        double dk = (il == ik) ? 1.0 : 0.0;
+        fu[il][ik] = psi * dk - chi * drdx[il] * drdx[ik];
+        ft[il][ik] = TT1 * drdx[il] * drdx[ik] * drdn + TT2 * (drdn * dk + drdx[ik] * n[il]) + TT3 * drdx[il] * n[ik];
+      }
+  }
+};
+
+template <class K>
+struct HG {
+  typename K::T h[8][3][3], g[8][3][3];
+  void zero() {
+    for (int a = 0; a < 8; ++a)
+      for (int b = 0; b < 3; ++b)
+        for (int c = 0; c < 3; ++c) h[a][b][c] = g[a][b][c] = 0.0;
+  }
+};
+
+// sbie_ext_pre: bem_staela3d.f90:592-650 / bem_harela3d.f90:628-700
+template <class K>
+static void ext_pre(const K& k, int ps, const Elem& e, bool reverse, const double x_i[3], HG<K>& out) {
+  out.zero();
+  for (int kip = 0; kip < e.ps_ngp[ps]; ++kip) {
+    int kt = e.ps_off[ps] + kip;
+    const double* x = &e.px[kt * 3];
+    const double* n = &e.pn[kt * 3];
+    const double* pj = &e.pphijw[kt * 8];
+    double rv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] - x_i[2]};
+    typename K::T fu[3][3], ft[3][3];
+    k.eval(rv, n, fu, ft);
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik)
+        for (int a = 0; a < 8; ++a) {
+          out.h[a][il][ik] = out.h[a][il][ik] + ft[il][ik] * pj[a];
+          out.g[a][il][ik] = out.g[a][il][ik] + fu[il][ik] * pj[a];
+        }
+  }
+  for (int a = 0; a < 8; ++a)
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        out.h[a][il][ik] = k.ct() * out.h[a][il][ik];
+        out.g[a][il][ik] = k.cu() * out.g[a][il][ik];
+        if (reverse) out.h[a][il][ik] = -out.h[a][il][ik];
+      }
+}
+
+// sbie_ext_st (quadrilateral branch): bem_staela3d.f90:654-969 / bem_harela3d.f90:702-1048
+template <class K>
+static void ext_st(const K& k, const Elem& e, bool reverse, const double xi_s[4][2], const double x_i[3],
+                   const double barxip[2], double barr, int gln, HG<K>& out) {
+  out.zero();
+  Telles tp1 = telles11(barxip[0], barr), tp2 = telles11(barxip[1], barr);
+  for (int k1 = 1; k1 <= gln; ++k1) {
+    double g1 = gl11_xi(k1, gln), w1 = gl11_w(k1, gln);
+    double xip1, jt1;
+    telles_xi_jac(tp1, g1, xip1, jt1);
+    for (int k2 = 1; k2 <= gln; ++k2) {
+      double g2 = gl11_xi(k2, gln), w2 = gl11_w(k2, gln);
+      double xip2, jt2;
+      telles_xi_jac(tp2, g2, xip2, jt2);
+      double xip[2] = {xip1, xip2};
+      double sp[4], sd1[4], sd2[4];
+      phi_quad4(xip, sp);
+      dphi_quad4(xip, sd1, sd2);
+      double xi[2] = {0, 0}, dx1[2] = {0, 0}, dx2[2] = {0, 0};
+      for (int q = 0; q < 4; ++q)
+        for (int c = 0; c < 2; ++c) {
+          xi[c] = xi[c] + sp[q] * xi_s[q][c];
+          dx1[c] = dx1[c] + sd1[q] * xi_s[q][c];
+          dx2[c] = dx2[c] + sd2[q] * xi_s[q][c];
+        }
+      double js = dx1[0] * dx2[1] - dx1[1] * dx2[0];
+      double phi[8], d1[8], d2[8];
+      phi_quad8(xi, phi);
+      dphi_quad8(xi, d1, d2);
+      double x[3] = {0, 0, 0}, T1[3] = {0, 0, 0}, T2[3] = {0, 0, 0};
+      for (int q = 0; q < 8; ++q)
+        for (int c = 0; c < 3; ++c) {
+          x[c] = x[c] + phi[q] * e.x[q][c];
+          T1[c] = T1[c] + d1[q] * e.x[q][c];
+          T2[c] = T2[c] + d2[q] * e.x[q][c];
+        }
+      double N[3] = {T1[1] * T2[2] - T1[2] * T2[1], T1[2] * T2[0] - T1[0] * T2[2],
+                     T1[0] * T2[1] - T1[1] * T2[0]};
+      double jg = std::sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+      double n[3] = {N[0] / jg, N[1] / jg, N[2] / jg};
+      double rv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] - x_i[2]};
+      double jw = jg * js * jt1 * jt2 * w1 * w2;
+      double pj[8];
+      for (int q = 0; q < 8; ++q) pj[q] = phi[q] * jw;
+      typename K::T fu[3][3], ft[3][3];
+      k.eval(rv, n, fu, ft);
+      for (int il = 0; il < 3; ++il)
+        for (int ik = 0; ik < 3; ++ik)
+          for (int a = 0; a < 8; ++a) {
+            out.h[a][il][ik] = out.h[a][il][ik] + ft[il][ik] * pj[a];
+            out.g[a][il][ik] = out.g[a][il][ik] + fu[il][ik] * pj[a];
+          }
+    }
+  }
+  for (int a = 0; a < 8; ++a)
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        out.h[a][il][ik] = k.ct() * out.h[a][il][ik];
+        out.g[a][il][ik] = k.cu() * out.g[a][il][ik];
+        if (reverse) out.h[a][il][ik] = -out.h[a][il][ik];
+      }
+}
+
+struct AdpStats { long leaves = 0, points = 0, maxdepth_hits = 0; };
+
+// sbie_ext_adp: bem_staela3d.f90:973-1096 / bem_harela3d.f90:1050-1172
+template <class K>
+static void ext_adp(const K& k, const Elem& e, bool reverse, double xi_s[4][2], const double x_i[3],
+                    const QsParams& qsp, int ks, int ns, HG<K>& acc, AdpStats* st) {
+  double barxip[2], rmin, d;
+  int method;
+  if (ks == 1) {
+    acc.zero();
+    xi_s[0][0] = -1; xi_s[0][1] = -1;
+    xi_s[1][0] = 1;  xi_s[1][1] = -1;
+    xi_s[2][0] = 1;  xi_s[2][1] = 1;
+    xi_s[3][0] = -1; xi_s[3][1] = 1;
+    nearest_element_point_quad8(e.x, e.cl, x_i, barxip, &rmin, &d, &method);
+  } else {
+    double x_s[8][3];
+    subdivision_coords_quad8(e.x, xi_s, x_s);
+    double cl = characteristic_length_quad8(x_s, 1e-12);
+    nearest_element_point_quad8(x_s, cl, x_i, barxip, &rmin, &d, &method);
+  }
+  int gln_near = qs_n_estimation_telles(2, 5, qsp, d, barxip);
+  bool subdivide = false;
+  if (ks == ns) {
+    if (gln_near == 0) { gln_near = 30; if (st) st->maxdepth_hits++; }
+  } else if (gln_near == 0) {
+    subdivide = true;
+  }
+  if (subdivide) {
+    double t[4][2];
+    double c[2] = {0.25 * (xi_s[0][0] + xi_s[1][0] + xi_s[2][0] + xi_s[3][0]),
+                   0.25 * (xi_s[0][1] + xi_s[1][1] + xi_s[2][1] + xi_s[3][1])};
+    for (int q = 0; q < 2; ++q) {
+      t[0][q] = xi_s[0][q]; t[1][q] = 0.5 * (xi_s[0][q] + xi_s[1][q]); t[2][q] = c[q]; t[3][q] = 0.5 * (xi_s[0][q] + xi_s[3][q]);
+    }
+    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st);
+    for (int q = 0; q < 2; ++q) {
+      t[0][q] = 0.5 * (xi_s[0][q] + xi_s[1][q]); t[1][q] = xi_s[1][q]; t[2][q] = 0.5 * (xi_s[1][q] + xi_s[2][q]); t[3][q] = c[q];
+    }
+    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st);
+    for (int q = 0; q < 2; ++q) {
+      t[0][q] = c[q]; t[1][q] = 0.5 * (xi_s[1][q] + xi_s[2][q]); t[2][q] = xi_s[2][q]; t[3][q] = 0.5 * (xi_s[2][q] + xi_s[3][q]);
+    }
+    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st);
+    for (int q = 0; q < 2; ++q) {
+      t[0][q] = 0.5 * (xi_s[0][q] + xi_s[3][q]); t[1][q] = c[q]; t[2][q] = 0.5 * (xi_s[2][q] + xi_s[3][q]); t[3][q] = xi_s[3][q];
+    }
+    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st);
+  } else {
+    double barr = telles_barr_any(d);
+    int gln = std::max(gln_near, e.gln_far);
+    HG<K> tmp;
+    ext_st(k, e, reverse, xi_s, x_i, barxip, barr, gln, tmp);
+    if (st) { st->leaves++; st->points += (long)gln * gln; }
+    for (int a = 0; a < 8; ++a)
+      for (int il = 0; il < 3; ++il)
+        for (int ik = 0; ik < 3; ++ik) {
+          acc.h[a][il][ik] = acc.h[a][il][ik] + tmp.h[a][il][ik];
+          acc.g[a][il][ik] = acc.g[a][il][ik] + tmp.g[a][il][ik];
+        }
+  }
+}
+
+// fbem_bem_staela3d_sbie_int_li (bem_staela3d.f90:2245-2376), line3 edge
+static void int_li(const double xn[3][3], double xi_s[2], const double x_i[3], int ngp_min, const QsParams& qsp,
+                   int ks, int ns, double hli[3][3]) {
+  double x_s[3][3];
+  if (ks == 1) {
+    xi_s[0] = -1.0;
+    xi_s[1] = 1.0;
+    std::memcpy(x_s, xn, sizeof(x_s));
+  } else {
+    subdivision_coords_line3(xn, xi_s, x_s);
+  }
+  double cl = characteristic_length_line3(x_s, 1e-12);
+  double barxip, rmin, d;
+  int method;
+  nearest_element_point_line3(x_s, cl, x_i, &barxip, &rmin, &d, &method);
+  int gln_near = qs_n_estimation_telles(1, 1, qsp, d, &barxip);
+  bool subdivide = false;
+  if (ks == ns) {
+    if (gln_near == 0) gln_near = 30;
+  } else if (gln_near == 0) {
+    subdivide = true;
+  }
+  if (subdivide) {
+    double t[2];
+    t[0] = xi_s[0]; t[1] = 0.5 * (xi_s[0] + xi_s[1]);
+    int_li(xn, t, x_i, ngp_min, qsp, ks + 1, ns, hli);
+    t[0] = 0.5 * (xi_s[0] + xi_s[1]); t[1] = xi_s[1];
+    int_li(xn, t, x_i, ngp_min, qsp, ks + 1, ns, hli);
+  } else {
+    double ht[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    int gln = std::max(gln_near, ngp_min);
+    double barr = telles_barr_any(d);
+    Telles tp = telles11(barxip, barr);
+    for (int kip = 1; kip <= gln; ++kip) {
+      double gm = gl11_xi(kip, gln), w = gl11_w(kip, gln);
+      double xip, jt;
+      telles_xi_jac(tp, gm, xip, jt);
+      double xi = 0.5 * (1.0 - xip) * xi_s[0] + 0.5 * (1.0 + xip) * xi_s[1];
+      double js = 0.5 * (xi_s[1] - xi_s[0]);
+      double phi[3], dphi[3];
+      phi_line3(xi, phi);
+      dphi_line3(xi, dphi);
+      double x[3] = {0, 0, 0}, T[3] = {0, 0, 0};
+      for (int q = 0; q < 3; ++q)
+        for (int c = 0; c < 3; ++c) {
+          x[c] = x[c] + phi[q] * xn[q][c];
+          T[c] = T[c] + dphi[q] * xn[q][c];
+        }
+      double jg = std::sqrt(T[0] * T[0] + T[1] * T[1] + T[2] * T[2]);
+      double t[3] = {T[0] / jg, T[1] / jg, T[2] / jg};
+      double rv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] - x_i[2]};
+      double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+      double dr1 = 1.0 / r;
+      double jw = jg * js * jt * w;
+      ht[0][1] = ht[0][1] - dr1 * t[2] * jw;
+      ht[0][2] = ht[0][2] + dr1 * t[1] * jw;
+      ht[1][2] = ht[1][2] - dr1 * t[0] * jw;
+    }
+    ht[1][0] = -ht[0][1];
+    ht[2][0] = -ht[0][2];
+    ht[2][1] = -ht[1][2];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) hli[a][b] = hli[a][b] + ht[a][b];
+  }
+}
+
+// Shared surface-integral driver of sbie_int: bem_staela3d.f90:1100-1381 and
+// bem_harela3d.f90:1174-1472 (polar coordinates, CPV regularisation, line
+// integrals for the strongly singular part).
+template <class K>
+static void sbie_int(const K& k, const Elem& e, bool reverse, const double xi_i[2], HG<K>& out);
+
+template <>
+void sbie_int<StaelaK>(const StaelaK& k, const Elem& e, bool reverse, const double xi_i[2], HG<StaelaK>& out);
+template <>
+void sbie_int<HarelaK>(const HarelaK& k, const Elem& e, bool reverse, const double xi_i[2], HG<HarelaK>& out);
+
+static void line_integrals(const Elem& e, const double x_i[3], int nsub, const int* st, double hli[3][3]) {
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) hli[a][b] = 0.0;
+  QsParams qsp;
+  qs_calculate_parameters(1e-15, qsp);
+  for (int ke = 1; ke <= 4; ++ke) {
+    bool integ = false;
+    for (int s = 0; s < nsub; ++s)
+      if (st[s] == 2 * ke - 1 || st[s] == 2 * ke) { integ = true; break; }
+    if (!integ) continue;
+    double xe[3][3];
+    for (int q = 0; q < 3; ++q)
+      for (int c = 0; c < 3; ++c) xe[q][c] = e.x[quad8_edge_node[ke - 1][q]][c];
+    double xs[2];
+    int_li(xe, xs, x_i, 5, qsp, 1, 16, hli);
+  }
+}
+
+template <class K, class PointFn>
+static void polar_loop(const Elem& e, const double xi_i[2], const double x_i[3], PointFn fn, int* nsub_out,
+                       int st_out[8]) {
+  int nsub, st[8];
+  double th[8][2], thp[8][2];
+  polar_setup_quad(xi_i, &nsub, st, th, thp);
+  for (int s = 0; s < nsub; ++s) {
+    double ti = th[s][0], tf = th[s][1], tpi = thp[s][0], tpf = thp[s][1];
+    const int ngp_rho = 15;
+    int ngp_theta = 5 + (int)std::lround(25.0 * (tf - ti) / c_pi_2);
+    for (int kt = 1; kt <= ngp_theta; ++kt) {
+      double tpp = gl01_xi(kt, ngp_theta), wa = gl01_w(kt, ngp_theta);
+      double jtp = (tpf - tpi);
+      double tp = jtp * tpp + tpi;
+      double theta, rhoij;
+      polar_angular_quad(xi_i, st[s], tp, &theta, &rhoij);
+      double ct = std::cos(theta), sn = std::sin(theta);
+      for (int kr = 1; kr <= ngp_rho; ++kr) {
+        double rhop = gl01_xi(kr, ngp_rho), wr = gl01_w(kr, ngp_rho);
+        double rho = rhoij * rhop;
+        double xi[2] = {xi_i[0] + rho * ct, xi_i[1] + rho * sn};
+        double phi[8], d1[8], d2[8];
+        phi_quad8(xi, phi);
+        dphi_quad8(xi, d1, d2);
+        double x[3] = {0, 0, 0}, T1[3] = {0, 0, 0}, T2[3] = {0, 0, 0};
+        for (int q = 0; q < 8; ++q)
+          for (int c = 0; c < 3; ++c) {
+            x[c] = x[c] + phi[q] * e.x[q][c];
+            T1[c] = T1[c] + d1[q] * e.x[q][c];
+            T2[c] = T2[c] + d2[q] * e.x[q][c];
+          }
+        double N[3] = {T1[1] * T2[2] - T1[2] * T2[1], T1[2] * T2[0] - T1[0] * T2[2],
+                       T1[0] * T2[1] - T1[1] * T2[0]};
+        double jg = std::sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+        double n[3] = {N[0] / jg, N[1] / jg, N[2] / jg};
+        double rv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] - x_i[2]};
+        double jw = jg * rho * jtp * wa * wr;
+        fn(rv, n, phi, jw);
+      }
+    }
+  }
+  *nsub_out = nsub;
+  for (int s = 0; s < nsub; ++s) st_out[s] = st[s];
+}
+
+template <>
+void sbie_int<StaelaK>(const StaelaK& k, const Elem& e, bool reverse, const double xi_i[2], HG<StaelaK>& out) {
+  out.zero();
+  double phii[8];
+  phi_quad8(xi_i, phii);
+  double x_i[3] = {0, 0, 0};
+  for (int q = 0; q < 8; ++q)
+    for (int c = 0; c < 3; ++c) x_i[c] = x_i[c] + phii[q] * e.x[q][c];
+  int nsub, st[8];
+  auto fn = [&](const double rv[3], const double n[3], const double phi[8], double jw) {
+    double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    double d1r = 1.0 / r, d1r2 = d1r * d1r;
+    double drdx[3] = {rv[0] * d1r, rv[1] * d1r, rv[2] * d1r};
+    double drdn = drdx[0] * n[0] + drdx[1] * n[1] + drdx[2] * n[2];
+    double pj[8];
+    for (int q = 0; q < 8; ++q) pj[q] = phi[q] * jw;
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        double dk = (il == ik) ? 1.0 : 0.0;
+        double fu = d1r * (k.cteu2 * dk + drdx[il] * drdx[ik]);
+        double ft = d1r2 * drdn * (k.ctet2 * dk + 3.0 * drdx[il] * drdx[ik]);
+        for (int a = 0; a < 8; ++a) {
+          out.h[a][il][ik] = out.h[a][il][ik] + ft * pj[a];
+          out.g[a][il][ik] = out.g[a][il][ik] + fu * pj[a];
+        }
+        ft = d1r2 * k.ctet2 * (n[il] * drdx[ik] - n[ik] * drdx[il]);
+        for (int a = 0; a < 8; ++a) out.h[a][il][ik] = out.h[a][il][ik] + ft * (phi[a] - phii[a]) * jw;
+      }
+  };
+  polar_loop<StaelaK>(e, xi_i, x_i, fn, &nsub, st);
+  double hli[3][3];
+  line_integrals(e, x_i, nsub, st, hli);
+  for (int il = 0; il < 3; ++il)
+    for (int ik = 0; ik < 3; ++ik)
+      for (int a = 0; a < 8; ++a) out.h[a][il][ik] = out.h[a][il][ik] + phii[a] * k.ctet2 * hli[il][ik];
+  for (int a = 0; a < 8; ++a)
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        out.h[a][il][ik] = k.ctet1 * out.h[a][il][ik];
+        out.g[a][il][ik] = k.cteu1 * out.g[a][il][ik];
+        if (reverse) out.h[a][il][ik] = -out.h[a][il][ik];
+      }
+}
+
+template <>
+void sbie_int<HarelaK>(const HarelaK& k, const Elem& e, bool reverse, const double xi_i[2], HG<HarelaK>& out) {
+  out.zero();
+  double phii[8];
+  phi_quad8(xi_i, phii);
+  double x_i[3] = {0, 0, 0};
+  for (int q = 0; q < 8; ++q)
+    for (int c = 0; c < 3; ++c) x_i[c] = x_i[c] + phii[q] * e.x[q][c];
+  int nsub, st[8];
+  const HarPar& p = k.p;
+  auto fn = [&](const double rv[3], const double n[3], const double phi[8], double jw) {
+    double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    cplx psi, chi, TT1, TT2, TT3;
+    double dr1, dr2;
+    k.coeffs(r, psi, chi, TT1, TT2, TT3, dr1, dr2, false);
+    double drdx[3] = {rv[0] * dr1, rv[1] * dr1, rv[2] * dr1};
+    double drdn = drdx[0] * n[0] + drdx[1] * n[1] + drdx[2] * n[2];
+    double pj[8];
+    for (int q = 0; q < 8; ++q) pj[q] = phi[q] * jw;
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        double dk = (il == ik) ? 1.0 : 0.0;
+        cplx fu = psi * dk - chi * drdx[il] * drdx[ik];
+        cplx ft = (TT1 + p.T1[0] * dr2) * drdx[il] * drdx[ik] * drdn + (TT2 + p.T2[0] * dr2) * drdn * dk +
+                  TT2 * drdx[ik] * n[il] + TT3 * drdx[il] * n[ik];
+        for (int a = 0; a < 8; ++a) {
+          out.h[a][il][ik] = out.h[a][il][ik] + ft * pj[a];
+          out.g[a][il][ik] = out.g[a][il][ik] + fu * pj[a];
+        }
+        ft = p.T2[0] * dr2 * (n[il] * drdx[ik] - n[ik] * drdx[il]);
+        for (int a = 0; a < 8; ++a) out.h[a][il][ik] = out.h[a][il][ik] + ft * (phi[a] - phii[a]) * jw;
+      }
+  };
+  polar_loop<HarelaK>(e, xi_i, x_i, fn, &nsub, st);
+  double hli[3][3];
+  line_integrals(e, x_i, nsub, st, hli);
+  for (int il = 0; il < 3; ++il)
+    for (int ik = 0; ik < 3; ++ik)
+      for (int a = 0; a < 8; ++a) out.h[a][il][ik] = out.h[a][il][ik] + phii[a] * p.T2[0] * hli[il][ik];
+  for (int a = 0; a < 8; ++a)
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        out.h[a][il][ik] = p.cte_t * out.h[a][il][ik];
+        out.g[a][il][ik] = p.cte_u * out.g[a][il][ik];
+        if (reverse) out.h[a][il][ik] = -out.h[a][il][ik];
+      }
+}
+
+// Pair classes reported for tests: precalculated rule index 0..n_ps-1,
+// CLS_ADP for adaptive subdivision, CLS_SING for interior integration.
+enum { CLS_ADP = 100, CLS_SING = 101 };
+
+// sbie_auto: bem_staela3d.f90:524-589 / bem_harela3d.f90:1474-1538
+template <class K>
+static int sbie_auto(const K& k, const Elem& e, bool reverse, const double x_i[3], const QsParams& qsp, int ns,
+                     HG<K>& out, AdpStats* st) {
+  double r[3] = {e.bc[0] - x_i[0], e.bc[1] - x_i[1], e.bc[2] - x_i[2]};
+  double rmin = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) - e.br;
+  double barxi[2], d;
+  int delta;
+  if (rmin > 4.0 * e.br) {
+    delta = 0;
+    barxi[0] = barxi[1] = 0.0;
+    d = rmin / e.cl;
+  } else {
+    int method;
+    nearest_element_point_quad8(e.x, e.cl, x_i, barxi, &rmin, &d, &method);
+    delta = (d <= 1e-12) ? 1 : 0;
+  }
+  if (delta == 1) {
+    sbie_int<K>(k, e, reverse, barxi, out);
+    return CLS_SING;
+  }
+  int gln_near = qs_n_estimation_standard(2, 5, qsp, d, barxi);
+  int gln = std::max(e.gln_far, gln_near);
+  if (gln <= e.ps_gln_max && gln_near > 0) {
+    int ps = 0;
+    for (int i = 0; i < e.n_ps; ++i)
+      if (e.ps_gln[i] >= gln) { ps = i; break; }
+    ext_pre<K>(k, ps, e, reverse, x_i, out);
+    return ps;
+  }
+  double xi_s[4][2];
+  ext_adp<K>(k, e, reverse, xi_s, x_i, qsp, 1, ns, out, st);
+  return CLS_ADP;
+}
+
+// ---------------------------------------------------------------------------
+// Free term: V. Mantic's formula, bem_staela3d.f90:228-405 (real nu) and
+// bem_harela3d.f90:365-542 (complex nu): identical algorithm.
+// Returns false when the normals/tangents configuration is invalid (the
+// reference stops there).
+// ---------------------------------------------------------------------------
+template <typename T>
+static bool freeterm(int ne, const double* n, const double* t, double tol, T nu, T c[3][3]) {
+  double ltol = (tol < 1e-12 || tol > 1e-3) ? 1e-6 : tol;
+  std::vector<double> ln(3 * (ne + 2)), lt(3 * (ne + 2)), lti(3 * ne);
+  auto LN = [&](int k, int c) -> double& { return ln[3 * k + c]; };
+  auto LT = [&](int k, int c) -> double& { return lt[3 * k + c]; };
+  for (int ki = 1; ki <= ne; ++ki)
+    for (int c = 0; c < 3; ++c) { LN(ki, c) = n[3 * (ki - 1) + c]; LT(ki, c) = t[3 * (ki - 1) + c]; }
+  std::vector<int> tc(ne + 1);
+  std::vector<double> theta(ne + 1);
+  for (int ki = 1; ki <= ne - 1; ++ki) {
+    double e1[3] = {LT(ki, 0), LT(ki, 1), LT(ki, 2)}, e3[3] = {LN(ki, 0), LN(ki, 1), LN(ki, 2)};
+    double e2[3] = {e3[1] * e1[2] - e3[2] * e1[1], e3[2] * e1[0] - e3[0] * e1[2], e3[0] * e1[1] - e3[1] * e1[0]};
+    for (int kj = 1; kj <= ne; ++kj) {
+      lti[3 * (kj - 1) + 0] = e1[0] * LT(kj, 0) + e1[1] * LT(kj, 1) + e1[2] * LT(kj, 2);
+      lti[3 * (kj - 1) + 1] = e2[0] * LT(kj, 0) + e2[1] * LT(kj, 1) + e2[2] * LT(kj, 2);
+      lti[3 * (kj - 1) + 2] = e3[0] * LT(kj, 0) + e3[1] * LT(kj, 1) + e3[2] * LT(kj, 2);
+    }
+    int nc = 0;
+    for (int kj = ki + 1; kj <= ne; ++kj)
+      if (std::fabs(lti[3 * (kj - 1) + 2]) <= ltol) tc[++nc] = kj;
+    if (nc == 0) return false;
+    for (int kj = 1; kj <= nc; ++kj) {
+      int j = tc[kj];
+      theta[j] = std::atan2(lti[3 * (j - 1) + 1], lti[3 * (j - 1) + 0]);
+      if (theta[j] < 0.0) theta[j] = theta[j] + 2.0 * c_pi;
+    }
+    double mt = theta[tc[1]];
+    int mk = tc[1];
+    for (int kj = 2; kj <= nc; ++kj)
+      if (theta[tc[kj]] < mt) { mt = theta[tc[kj]]; mk = tc[kj]; }
+    for (int c = 0; c < 3; ++c) {
+      std::swap(LT(ki + 1, c), LT(mk, c));
+      std::swap(LN(ki + 1, c), LN(mk, c));
+    }
+  }
+  for (int c = 0; c < 3; ++c) {
+    LN(0, c) = LN(ne, c); LT(0, c) = LT(ne, c);
+    LN(ne + 1, c) = LN(1, c); LT(ne + 1, c) = LT(1, c);
+  }
+  double sum_a = 0.0;
+  for (int ki = 1; ki <= ne; ++ki) {
+    double nx[3] = {LN(ki - 1, 1) * LN(ki, 2) - LN(ki - 1, 2) * LN(ki, 1),
+                    LN(ki - 1, 2) * LN(ki, 0) - LN(ki - 1, 0) * LN(ki, 2),
+                    LN(ki - 1, 0) * LN(ki, 1) - LN(ki - 1, 1) * LN(ki, 0)};
+    double s = nx[0] * LT(ki, 0) + nx[1] * LT(ki, 1) + nx[2] * LT(ki, 2);
+    if (s < 0.0) s = -1.0;
+    if (s > 0.0) s = 1.0;
+    double ndn = LN(ki - 1, 0) * LN(ki, 0) + LN(ki - 1, 1) * LN(ki, 1) + LN(ki - 1, 2) * LN(ki, 2);
+    if (ndn > 1.0) ndn = 1.0;
+    sum_a = sum_a + s * std::acos(ndn);
+  }
+  double cp = 1.0 / (4.0 * c_pi) * (2.0 * c_pi + sum_a);
+  double sb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int ki = 1; ki <= ne; ++ki) {
+    double rmr[3] = {LT(ki + 1, 0) - LT(ki, 0), LT(ki + 1, 1) - LT(ki, 1), LT(ki + 1, 2) - LT(ki, 2)};
+    double rx[3] = {rmr[1] * LN(ki, 2) - rmr[2] * LN(ki, 1), rmr[2] * LN(ki, 0) - rmr[0] * LN(ki, 2),
+                    rmr[0] * LN(ki, 1) - rmr[1] * LN(ki, 0)};
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) sb[a][b] = sb[a][b] + rx[a] * LN(ki, b);
+  }
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      c[a][b] = -1.0 / (8.0 * c_pi * (1.0 - nu)) * sb[a][b];
+      if (a == b) c[a][b] = c[a][b] + cp;
+    }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Problem: the host-side data the Fortran keeps in problem_variables for one
+// ordinary BE boundary of continuous quad8 elements in a full-space region.
+// ---------------------------------------------------------------------------
+struct Colloc {
+  double x[3];
+  int node;     // collocation node (rows)
+  int kind;     // 0 SBIE (nodal), 1 SBIE MCA
+  int elem, kn; // element/local node it was taken from
+  double xi[2];
+};
+
+struct Problem {
+  int nn, ne;
+  std::vector<double> X;     // 3*nn
+  std::vector<int> conn;     // 8*ne
+  std::vector<int> ctype;    // 3*nn
+  std::vector<cplx> cvalue;  // 3*nn
+  double qsi_re, geo_tol;
+  int ns_max, n_ps;
+  int ps_gln[16];
+  QsParams qsp;
+  std::vector<Elem> el;
+  std::vector<int> node_order;                   // DOF order
+  std::vector<int> dof;                          // nn*3 -> 0-based DOF index
+  std::vector<std::vector<std::pair<int, int>>> node_el;  // (element, local)
+  std::vector<char> in_boundary;
+  std::vector<double> delta_mca;                 // 8*ne
+  std::vector<double> n_gn, tbp_gn, tbm_gn;      // 8*ne*3
+  std::vector<Colloc> cps;
+  std::vector<std::vector<int>> node_cps;        // collocation points per node
+  int ndof;
+};
+
+static void build(Problem& P) {
+  const int nn = P.nn, ne = P.ne;
+  P.el.resize(ne);
+  for (int e = 0; e < ne; ++e) {
+    Elem& E = P.el[e];
+    for (int k = 0; k < 8; ++k)
+      for (int c = 0; c < 3; ++c) E.x[k][c] = P.X[3 * P.conn[8 * e + k] + c];
+    // build_data_of_be_elements.f90:52-96
+    E.cl = characteristic_length_quad8(E.x, 1e-9);
+    bool ok;
+    int n1 = qs_phijac_ngp_2d_quad8(E.x, P.qsi_re, &ok);
+    int n2 = qs_phijac_ngp_2d_quad8(E.x, P.qsi_re, &ok);
+    E.gln_far = std::max(n1, n2);
+    element_ball_quad8(E.x, E.gln_far, E.bc, &E.br);
+    init_precalculated(E, P.n_ps, P.ps_gln);
+  }
+  // node -> elements (increasing element order)
+  P.node_el.assign(nn, {});
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 8; ++k) P.node_el[P.conn[8 * e + k]].push_back({e, k});
+  // mesh boundary (data_structures.f90:1433-1495): edges with one element
+  std::map<std::pair<int, int>, int> edge_count;
+  for (int e = 0; e < ne; ++e)
+    for (int ke = 0; ke < 4; ++ke) {
+      int a = P.conn[8 * e + quad8_edge_node[ke][0]], b = P.conn[8 * e + quad8_edge_node[ke][1]];
+      edge_count[{std::min(a, b), std::max(a, b)}]++;
+    }
+  P.in_boundary.assign(nn, 0);
+  for (int e = 0; e < ne; ++e)
+    for (int ke = 0; ke < 4; ++ke) {
+      int a = P.conn[8 * e + quad8_edge_node[ke][0]], b = P.conn[8 * e + quad8_edge_node[ke][1]];
+      if (edge_count[{std::min(a, b), std::max(a, b)}] == 1)
+        for (int q = 0; q < 3; ++q) P.in_boundary[P.conn[8 * e + quad8_edge_node[ke][q]]] = 1;
+    }
+  // assign_default_bem_formulation.f90:76-93
+  P.delta_mca.assign(8 * ne, 0.0);
+  for (int s = 0; s < nn; ++s)
+    if (P.in_boundary[s])
+      for (auto& pr : P.node_el[s]) P.delta_mca[8 * pr.first + pr.second] = 0.05;
+  // geometrical node normals/tangents (build_data_at_geometrical_nodes.f90:177-222)
+  P.n_gn.assign(8 * ne * 3, 0.0);
+  P.tbp_gn.assign(8 * ne * 3, 0.0);
+  P.tbm_gn.assign(8 * ne * 3, 0.0);
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 8; ++k) {
+      double d1[8], d2[8];
+      dphi_quad8(quad8_xi_nodes[k], d1, d2);
+      double T1[3] = {0, 0, 0}, T2[3] = {0, 0, 0};
+      for (int i = 0; i < 8; ++i)
+        for (int c = 0; c < 3; ++c) { T1[c] = T1[c] + d1[i] * P.el[e].x[i][c]; T2[c] = T2[c] + d2[i] * P.el[e].x[i][c]; }
+      double N[3] = {T1[1] * T2[2] - T1[2] * T2[1], T1[2] * T2[0] - T1[0] * T2[2], T1[0] * T2[1] - T1[1] * T2[0]};
+      double tmp = std::sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+      for (int c = 0; c < 3; ++c) P.n_gn[(8 * e + k) * 3 + c] = N[c] / tmp;
+      double n1 = std::sqrt(T1[0] * T1[0] + T1[1] * T1[1] + T1[2] * T1[2]);
+      double n2 = std::sqrt(T2[0] * T2[0] + T2[1] * T2[1] + T2[2] * T2[2]);
+      double t1[3] = {T1[0] / n1, T1[1] / n1, T1[2] / n1}, t2[3] = {T2[0] / n2, T2[1] / n2, T2[2] / n2};
+      // geometry.f90:833-873 quadrilateral branch
+      static const int sp[8][2] = {{1, 2}, {2, -1}, {-1, -2}, {-2, 1}, {1, -1}, {2, -2}, {-1, 1}, {-2, 2}};
+      for (int c = 0; c < 3; ++c) {
+        int a = sp[k][0], b = sp[k][1];
+        double va = (std::abs(a) == 1 ? t1[c] : t2[c]) * (a > 0 ? 1.0 : -1.0);
+        double vb = (std::abs(b) == 1 ? t1[c] : t2[c]) * (b > 0 ? 1.0 : -1.0);
+        P.tbp_gn[(8 * e + k) * 3 + c] = va;
+        P.tbm_gn[(8 * e + k) * 3 + c] = vb;
+      }
+    }
+  // DOF numbering, build_auxiliary_variables_mechanics_static.f90:60-140
+  P.dof.assign(3 * nn, -1);
+  std::vector<char> used(nn, 0);
+  int row = 0;
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 8; ++k) {
+      int s = P.conn[8 * e + k];
+      if (used[s]) continue;
+      used[s] = 1;
+      P.node_order.push_back(s);
+      for (int c = 0; c < 3; ++c) P.dof[3 * s + c] = row++;
+    }
+  P.ndof = row;
+  // collocation points in the collocation loop order (build_lse_mechanics_bem_staela.f90:761-1034)
+  std::vector<char> coll(nn, 0);
+  P.node_cps.assign(nn, {});
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 8; ++k) {
+      int s = P.conn[8 * e + k];
+      Colloc cp;
+      cp.node = s; cp.elem = e; cp.kn = k;
+      double xi[2] = {quad8_xi_nodes[k][0], quad8_xi_nodes[k][1]};
+      if (!P.in_boundary[s]) {
+        if (coll[s]) continue;
+        coll[s] = 1;
+        cp.kind = 0;
+      } else {
+        // fbem_move_xi1xi2_from_edge (geometry.f90:5631-5659)
+        double dl = P.delta_mca[8 * e + k];
+        if (check_xi1xi2_edge_quad(xi)) { xi[0] = xi[0] * (1.0 - dl); xi[1] = xi[1] * (1.0 - dl); }
+        cp.kind = 1;
+      }
+      cp.xi[0] = xi[0]; cp.xi[1] = xi[1];
+      double phi[8];
+      phi_quad8(xi, phi);
+      double x[3] = {0, 0, 0};
+      for (int q = 0; q < 8; ++q)
+        for (int c = 0; c < 3; ++c) x[c] = x[c] + phi[q] * P.el[e].x[q][c];
+      for (int c = 0; c < 3; ++c) cp.x[c] = x[c];
+      P.node_cps[s].push_back((int)P.cps.size());
+      P.cps.push_back(cp);
+    }
+}
+
+// Scatter one (collocation node, integration element) block into the row
+// buffer of that node: assemble_bem_staela_equation.f90:69-98 and
+// assemble_bem_harela_equation.f90:78-113 (ordinary BE boundary).
+template <typename T>
+static void scatter(const Problem& P, int e, const T h[8][3][3], const T g[8][3][3], T* rowbuf /*3*ndof*/,
+                    T* brow /*3*/) {
+  for (int il = 0; il < 3; ++il)
+    for (int ik = 0; ik < 3; ++ik)
+      for (int kn = 0; kn < 8; ++kn) {
+        int s = P.conn[8 * e + kn];
+        int col = P.dof[3 * s + ik];
+        T cv = (T)0;
+        if constexpr (std::is_same<T, double>::value) cv = P.cvalue[3 * s + ik].real();
+        else cv = P.cvalue[3 * s + ik];
+        if (P.ctype[3 * s + ik] == 0) {
+          rowbuf[il * P.ndof + col] = rowbuf[il * P.ndof + col] - g[kn][il][ik];
+          brow[il] = brow[il] - h[kn][il][ik] * cv;
+        } else {
+          rowbuf[il * P.ndof + col] = rowbuf[il * P.ndof + col] + h[kn][il][ik];
+          brow[il] = brow[il] + g[kn][il][ik] * cv;
+        }
+      }
+}
+
+// Free-term contribution for collocation node s (first element of the
+// collocation order carries it), build_lse_mechanics_bem_staela.f90:152-549.
+template <class K>
+static bool free_terms_for_node(const Problem& P, int s, typename K::T nu, typename K::T* rowbuf, typename K::T* brow) {
+  typedef typename K::T T;
+  for (int ci : P.node_cps[s]) {
+    const Colloc& cp = P.cps[ci];
+    HG<K> hg;
+    hg.zero();
+    if (cp.kind == 0) {
+      int nce = (int)P.node_el[s].size();
+      std::vector<double> nset(3 * nce), tset(3 * nce);
+      for (int j = 0; j < nce; ++j) {
+        int e = P.node_el[s][j].first, k = P.node_el[s][j].second;
+        for (int c = 0; c < 3; ++c) {
+          nset[3 * j + c] = P.n_gn[(8 * e + k) * 3 + c];
+          tset[3 * j + c] = P.tbp_gn[(8 * e + k) * 3 + c];
+        }
+      }
+      T C[3][3];
+      if (!freeterm<T>(nce, nset.data(), tset.data(), P.geo_tol, nu, C)) return false;
+      for (int il = 0; il < 3; ++il)
+        for (int ik = 0; ik < 3; ++ik) hg.h[cp.kn][il][ik] = hg.h[cp.kn][il][ik] + C[il][ik];
+    } else {
+      double pphi[8];
+      phi_quad8(cp.xi, pphi);
+      for (int il = 0; il < 3; ++il)
+        for (int a = 0; a < 8; ++a) hg.h[a][il][il] = hg.h[a][il][il] + 0.5 * pphi[a];
+    }
+    scatter<T>(P, cp.elem, hg.h, hg.g, rowbuf, brow);
+  }
+  return true;
+}
+
+template <class K>
+static int assemble(const Problem& P, const K& k, typename K::T nu, typename K::T* A, typename K::T* b, int nthreads,
+                    long* stats) {
+  typedef typename K::T T;
+  const int n = P.ndof;
+  int nord = (int)P.node_order.size();
+  int bad = 0;
+  long s_leaves = 0, s_points = 0, s_maxd = 0, s_sing = 0, s_adp = 0, s_pre = 0;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel reduction(+ : bad, s_leaves, s_points, s_maxd, s_sing, s_adp, s_pre)
+  {
+    std::vector<T> rowbuf(3 * (size_t)n);
+    AdpStats st;
+#pragma omp for schedule(dynamic, 1)
+    for (int oi = 0; oi < nord; ++oi) {
+      int s = P.node_order[oi];
+      std::fill(rowbuf.begin(), rowbuf.end(), (T)0);
+      T brow[3] = {(T)0, (T)0, (T)0};
+      for (int e = 0; e < P.ne; ++e) {
+        for (int ci : P.node_cps[s]) {
+          HG<K> hg;
+          int cls = sbie_auto<K>(k, P.el[e], false, P.cps[ci].x, P.qsp, P.ns_max, hg, &st);
+          if (cls == CLS_SING) s_sing++;
+          else if (cls == CLS_ADP) s_adp++;
+          else s_pre++;
+          scatter<T>(P, e, hg.h, hg.g, rowbuf.data(), brow);
+        }
+      }
+      if (!free_terms_for_node<K>(P, s, nu, rowbuf.data(), brow)) bad++;
+      for (int il = 0; il < 3; ++il) {
+        int r = P.dof[3 * s + il];
+        for (int c = 0; c < n; ++c) A[(size_t)c * n + r] = A[(size_t)c * n + r] + rowbuf[(size_t)il * n + c];
+        b[r] = b[r] + brow[il];
+      }
+    }
+    s_leaves += st.leaves;
+    s_points += st.points;
+    s_maxd += st.maxdepth_hits;
+  }
+  if (stats) {
+    stats[0] = s_pre; stats[1] = s_adp; stats[2] = s_sing; stats[3] = s_leaves; stats[4] = s_points; stats[5] = s_maxd;
+  }
+  return bad ? -1 : 0;
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+void* orc_problem_new(int nn, const double* X, int ne, const int* conn, const int* ctype, const double* cvalue,
+                      double qsi_re, int ns_max, int n_ps, const int* ps_gln, double geo_tol) {
+  Problem* P = new Problem();
+  P->nn = nn; P->ne = ne;
+  P->X.assign(X, X + 3 * nn);
+  P->conn.assign(conn, conn + 8 * ne);
+  P->ctype.assign(ctype, ctype + 3 * nn);
+  P->cvalue.resize(3 * nn);
+  for (int i = 0; i < 3 * nn; ++i) P->cvalue[i] = cplx(cvalue[2 * i], cvalue[2 * i + 1]);
+  P->qsi_re = qsi_re; P->ns_max = ns_max; P->n_ps = n_ps; P->geo_tol = geo_tol;
+  for (int i = 0; i < n_ps; ++i) P->ps_gln[i] = ps_gln[i];
+  qs_calculate_parameters(qsi_re, P->qsp);
+  build(*P);
+  return P;
+}
+void orc_problem_free(void* h) { delete (Problem*)h; }
+int orc_n_dof(void* h) { return ((Problem*)h)->ndof; }
+int orc_n_colloc(void* h) { return (int)((Problem*)h)->cps.size(); }
+
+void orc_dof_map(void* h, int* dof /*3*nn*/, int* order /*nn*/) {
+  Problem* P = (Problem*)h;
+  for (int i = 0; i < 3 * P->nn; ++i) dof[i] = P->dof[i];
+  for (size_t i = 0; i < P->node_order.size(); ++i) order[i] = P->node_order[i];
+}
+void orc_element_data(void* h, double* cl, int* gln_far, double* ball /*4*ne*/) {
+  Problem* P = (Problem*)h;
+  for (int e = 0; e < P->ne; ++e) {
+    cl[e] = P->el[e].cl;
+    gln_far[e] = P->el[e].gln_far;
+    for (int c = 0; c < 3; ++c) ball[4 * e + c] = P->el[e].bc[c];
+    ball[4 * e + 3] = P->el[e].br;
+  }
+}
+void orc_colloc(void* h, double* x /*3*ncp*/, int* info /*4*ncp: node, kind, elem, kn*/) {
+  Problem* P = (Problem*)h;
+  for (size_t i = 0; i < P->cps.size(); ++i) {
+    for (int c = 0; c < 3; ++c) x[3 * i + c] = P->cps[i].x[c];
+    info[4 * i + 0] = P->cps[i].node;
+    info[4 * i + 1] = P->cps[i].kind;
+    info[4 * i + 2] = P->cps[i].elem;
+    info[4 * i + 3] = P->cps[i].kn;
+  }
+}
+void orc_node_geometry(void* h, double* n_gn, double* tbp, double* tbm, char* in_boundary) {
+  Problem* P = (Problem*)h;
+  std::memcpy(n_gn, P->n_gn.data(), sizeof(double) * P->n_gn.size());
+  std::memcpy(tbp, P->tbp_gn.data(), sizeof(double) * P->tbp_gn.size());
+  std::memcpy(tbm, P->tbm_gn.data(), sizeof(double) * P->tbm_gn.size());
+  std::memcpy(in_boundary, P->in_boundary.data(), P->in_boundary.size());
+}
+
+int orc_assemble_staela(void* h, double mu, double nu, double* A, double* b, int nthreads, long* stats) {
+  Problem* P = (Problem*)h;
+  StaelaK k(mu, nu);
+  return assemble<StaelaK>(*P, k, nu, A, b, nthreads, stats);
+}
+// Harmonic assembly; nu is the region's complex-typed Poisson ratio (property_c(3)).
+int orc_assemble_harela_nu(void* h, double lre, double lim, double mre, double mim, double rho, double omega,
+                           double nure, double nuim, double* A, double* b, int nthreads, long* stats) {
+  Problem* P = (Problem*)h;
+  HarelaK k(harela_parameters(cplx(lre, lim), cplx(mre, mim), rho, omega));
+  return assemble<HarelaK>(*P, k, cplx(nure, nuim), (cplx*)A, (cplx*)b, nthreads, stats);
+}
+
+// One (collocation point, element) pair; h,g laid out [kn][il][ik].
+int orc_pair_staela(void* hp, int ci, int e, double mu, double nu, double* h, double* g) {
+  Problem* P = (Problem*)hp;
+  StaelaK k(mu, nu);
+  HG<StaelaK> hg;
+  int cls = sbie_auto<StaelaK>(k, P->el[e], false, P->cps[ci].x, P->qsp, P->ns_max, hg, nullptr);
+  std::memcpy(h, hg.h, sizeof(hg.h));
+  std::memcpy(g, hg.g, sizeof(hg.g));
+  return cls;
+}
+int orc_pair_harela(void* hp, int ci, int e, double lre, double lim, double mre, double mim, double rho,
+                    double omega, double* h, double* g) {
+  Problem* P = (Problem*)hp;
+  HarelaK k(harela_parameters(cplx(lre, lim), cplx(mre, mim), rho, omega));
+  HG<HarelaK> hg;
+  int cls = sbie_auto<HarelaK>(k, P->el[e], false, P->cps[ci].x, P->qsp, P->ns_max, hg, nullptr);
+  std::memcpy(h, hg.h, sizeof(hg.h));
+  std::memcpy(g, hg.g, sizeof(hg.g));
+  return cls;
+}
+// Harmonic parameter block for tests: k1,k2,c1,c2,psi(6),chi(6),T1(10),T2(9),T3(9),cte_u,cte_t (complex)
+void orc_harela_parameters(double lre, double lim, double mre, double mim, double rho, double omega, double* out) {
+  HarPar p = harela_parameters(cplx(lre, lim), cplx(mre, mim), rho, omega);
+  cplx* o = (cplx*)out;
+  int i = 0;
+  o[i++] = p.k1; o[i++] = p.k2; o[i++] = p.c1; o[i++] = p.c2;
+  for (int j = 0; j < 6; ++j) o[i++] = p.psi[j];
+  for (int j = 0; j < 6; ++j) o[i++] = p.chi[j];
+  for (int j = 0; j < 10; ++j) o[i++] = p.T1[j];
+  for (int j = 0; j < 9; ++j) o[i++] = p.T2[j];
+  for (int j = 0; j < 9; ++j) o[i++] = p.T3[j];
+  o[i++] = p.cte_u; o[i++] = p.cte_t;
+}
+
+void orc_gauss_tables(double* gl11x, double* gl11w, double* gl01x, double* gl01w) {
+  const GaussTables& g = gauss();
+  std::memcpy(gl11x, g.gl11_xi, sizeof(g.gl11_xi));
+  std::memcpy(gl11w, g.gl11_w, sizeof(g.gl11_w));
+  std::memcpy(gl01x, g.gl01_xi, sizeof(g.gl01_xi));
+  std::memcpy(gl01w, g.gl01_w, sizeof(g.gl01_w));
+}
+void orc_qs_parameters(double re, double* out /*10*24*/) {
+  QsParams p;
+  qs_calculate_parameters(re, p);
+  const double* arrs[10] = {&p.dmin[0][0], &p.dmax[0][0], &p.alpha0[0][0], &p.alpha1[0][0], &p.beta1[0][0],
+                            &p.t_dmin[0][0], &p.t_dmax[0][0], &p.t_alpha0[0][0], &p.t_alpha1[0][0], &p.t_beta1[0][0]};
+  for (int a = 0; a < 10; ++a)
+    for (int i = 0; i < 24; ++i) out[24 * a + i] = arrs[a][i];
+}
+int orc_qs_estimate(int telles, int dim, int f, double re, double d, const double* barxi) {
+  QsParams p;
+  qs_calculate_parameters(re, p);
+  return telles ? qs_n_estimation_telles(dim, f, p, d, barxi) : qs_n_estimation_standard(dim, f, p, d, barxi);
+}
+void orc_zexp(double zr, double zi, double* E /*7 complex*/) {
+  cplx z(zr, zi), e[7][2];
+  zexp_decomposed(1, &z, e);
+  for (int k = 0; k < 7; ++k) { E[2 * k] = e[k][0].real(); E[2 * k + 1] = e[k][0].imag(); }
+}
+void orc_nearest_quad8(const double* x /*8x3*/, double cl, const double* p, double* barxi, double* rmin, double* d,
+                       int* method) {
+  double xx[8][3];
+  std::memcpy(xx, x, sizeof(xx));
+  nearest_element_point_quad8(xx, cl, p, barxi, rmin, d, method);
+}
+int orc_freeterm(int ne, const double* n, const double* t, double tol, double nu, double* c) {
+  double C[3][3];
+  bool ok = freeterm<double>(ne, n, t, tol, nu, C);
+  std::memcpy(c, C, sizeof(C));
+  return ok ? 0 : -1;
+}
+
+}  // extern "C"
