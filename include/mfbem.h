@@ -1,0 +1,164 @@
+/*
+ * mfbem.h - C-ABI of the GB300 collocation-BEM library (drop-in for the
+ * element integration + dense solve path of MultiFEBE 2.0.1).
+ *
+ * The entry points replace, one to one, the reference routines that fill and
+ * solve the dense BEM system:
+ *
+ *   mfbem_assemble_staela  <- subroutine build_lse_mechanics_bem_staela(kr)
+ *                             src/build_lse_mechanics_bem_staela.f90:22 (called from
+ *                             src/build_lse_mechanics_static.f90:62)
+ *   mfbem_assemble_harela  <- subroutine build_lse_mechanics_bem_harela(kf,kr)
+ *                             src/build_lse_mechanics_bem_harela.f90:22 (called from
+ *                             src/build_lse_mechanics_harmonic.f90:88)
+ *   mfbem_solve_r          <- subroutine solve_lse_r(n_dof,A,ipiv,Aodim,Ao,equed,r,c,n_rhs,b,
+ *                             factorize,scaling,condition,refine), src/solve_lse_r.f90:25
+ *   mfbem_solve_c          <- subroutine solve_lse_c(...), src/solve_lse_c.f90:25
+ *   mfbem_mesh_upload      <- the module state those builders read (problem_variables:
+ *                             element(:), node(:), qsi_parameters, precalset_gln,
+ *                             src/problem_variables.f90:73-109), snapshotted once per mesh
+ *   mfbem_sweep_harela     <- the frequency loop of src/multifebe.f90:107-119
+ *                             (build_lse_mechanics_harmonic + solve_lse_c per frequency),
+ *                             batched on the device; no reference counterpart as one call
+ *
+ * Conventions (those of the reference's Fortran globals):
+ *   - all indices that name nodes, elements, rows or columns are 1-based;
+ *   - matrices are column-major with leading dimension lda >= n_dof;
+ *   - complex numbers are interleaved (re, im) doubles, i.e. complex(real64);
+ *   - the builders ADD into A and b (the caller zeroes them, as
+ *     src/build_lse_mechanics_static.f90:52-53 does), unless MFBEM_OVERWRITE;
+ *   - return value 0 on success, > 0 LAPACK-style info (index of the first
+ *     zero pivot), < 0 an MFBEM_E* error; mfbem_last_error() describes it.
+ *
+ * Threading: calls are synchronous, made from one host thread, not re-entrant
+ * per handle. A handle owns device memory for one mesh and its work buffers.
+ */
+#ifndef MFBEM_H
+#define MFBEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MFBEM_OK 0
+#define MFBEM_EARG (-1)        /* invalid argument */
+#define MFBEM_ECUDA (-2)       /* CUDA runtime failure / no device */
+#define MFBEM_ENOMEM (-3)      /* device allocation failed */
+#define MFBEM_ETIMEOUT (-4)    /* a bounded device wait gave up */
+#define MFBEM_EGEOMETRY (-5)   /* invalid normals/tangents at a free-term node
+                                  (the reference stops: bem_staela3d.f90:296-303) */
+#define MFBEM_ENOCONV (-6)     /* iterative refinement did not reach the tolerance */
+#define MFBEM_EUNSUPPORTED (-7)
+
+/* flags */
+#define MFBEM_DEVICE_PTRS 0x1  /* A, b (and x) are device pointers */
+#define MFBEM_OVERWRITE 0x2    /* overwrite A and b instead of adding into them */
+
+/* Mesh snapshot of one BE region with ordinary boundaries of continuous quad8
+ * elements, in the layout of the reference's derived types. */
+typedef struct mfbem_mesh_desc {
+  int32_t n_nodes;
+  int32_t n_elements;
+  int32_t n_dof;                 /* row-1 after build_auxiliary_variables_* */
+  /* element(se): x_gn(3,8), node(8) (1-based), csize, n_phi, bball_centre(3),
+     bball_radius, and the reversion flag of its boundary in the region */
+  const double* x_gn;            /* [n_elements][8][3] */
+  const int32_t* element_node;   /* [n_elements][8] */
+  const double* csize;           /* [n_elements] */
+  const int32_t* n_phi;          /* [n_elements] */
+  const double* bball;           /* [n_elements][4]: centre x,y,z, radius */
+  const int32_t* reversion;      /* [n_elements] 0/1, may be NULL (all 0) */
+  /* element(se)%n_gn(3,8) and %tbp_gn(3,8): unit normal and forward element
+     boundary tangent at each node (free-term inputs) */
+  const double* n_gn;            /* [n_elements][8][3] */
+  const double* tbp_gn;          /* [n_elements][8][3] */
+  /* node(sn): row(3,1), col(6,1) (0 where unused), ctype(3,1), cvalue(3,1,1)
+     (complex, the real part is used by the static path), and the SBIE
+     formulation (0 nodal SBIE, 1 SBIE with MCA) */
+  const int32_t* row;            /* [n_nodes][3] */
+  const int32_t* col;            /* [n_nodes][6] */
+  const int32_t* ctype;          /* [n_nodes][3]: 0 u known, 1 t known */
+  const double* cvalue;          /* [n_nodes][3][2] */
+  const int32_t* sbie;           /* [n_nodes] */
+  /* element(se)%xi_i_sbie_mca(2,8) and %x_i_sbie_mca(3,8) (read for MCA nodes) */
+  const double* xi_i_sbie_mca;   /* [n_elements][8][2] */
+  const double* x_i_sbie_mca;    /* [n_elements][8][3] */
+  /* settings (src/read_settings.f90): qsi_relative_error, qsi_ns_max,
+     precalset_gln(1:n_precalsets), geometric_tolerance */
+  double qsi_relative_error;
+  int32_t qsi_ns_max;
+  int32_t n_precalsets;
+  const int32_t* precalset_gln;
+  double geometric_tolerance;
+} mfbem_mesh_desc;
+
+typedef struct mfbem_handle mfbem_handle;
+
+/* Per-call accounting written by the assemble / sweep entry points. */
+typedef struct mfbem_stats {
+  int64_t pairs_regular, pairs_adaptive, pairs_singular;
+  int64_t points_regular, points_adaptive, points_singular;
+  int32_t adaptive_leaves;
+  int32_t refinement_iterations; /* sweep: total over frequencies */
+  double max_backward_error;     /* sweep: max over frequencies of ||b-Ax||/(||A|| ||x||) */
+  double ms_assemble, ms_factor, ms_solve;
+} mfbem_stats;
+
+/* mesh lifetime */
+int mfbem_mesh_upload(const mfbem_mesh_desc* desc, mfbem_handle** out);
+int mfbem_mesh_release(mfbem_handle* h);
+
+/* build_lse_mechanics_bem_staela: A (n_dof x n_dof, real) and b (n_dof). */
+int mfbem_assemble_staela(mfbem_handle* h, double mu, double nu, double* A, int32_t lda, double* b,
+                          int32_t flags);
+
+/* build_lse_mechanics_bem_harela for one frequency omega (rad/s): lambda, mu
+   and nu complex (region property_c(6), property_c(2), property_c(3)), rho
+   real. A and b complex(real64). */
+int mfbem_assemble_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
+                          const double nu[2], double omega, double* A, int32_t lda, double* b, int32_t flags);
+
+/* solve_lse_r / solve_lse_c: LU with partial pivoting (getrf) and the
+   triangular solves (getrs) for n_rhs right-hand sides, in FP64 on the GPU.
+   On return A holds the LU factors and ipiv the 1-based pivots, exactly as
+   LAPACK leaves them, so a later call with factorize = 0 reuses them.
+   scaling / condition / refine must be 0 (the reference defaults,
+   src/read_settings.f90); other values return MFBEM_EUNSUPPORTED. */
+int mfbem_solve_r(int32_t n, double* A, int32_t* ipiv, int32_t aodim, double* Ao, char* equed, double* r,
+                  double* c, int32_t n_rhs, double* b, int32_t factorize, int32_t scaling, int32_t condition,
+                  int32_t refine);
+int mfbem_solve_c(int32_t n, double* A, int32_t* ipiv, int32_t aodim, double* Ao, char* equed, double* r,
+                  double* c, int32_t n_rhs, double* b, int32_t factorize, int32_t scaling, int32_t condition,
+                  int32_t refine);
+
+/* Harmonic sweep on the device: for each of n_freq frequencies, assemble the
+   FP64 system (same integration as mfbem_assemble_harela), factorise and solve.
+   precision 0: plain FP64 LU (the drop-in method).
+   precision 1: complex64 LU with FP64 iterative refinement to rel_tol in the
+                backward error (the FP64 residual r = b - A x is evaluated with
+                the FP64 matrix).
+   x_out receives n_dof complex values per frequency (column f at f*n_dof).
+   The right-hand side is the one assembled from the prescribed values. */
+int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho, const double nu[2],
+                       int32_t n_freq, const double* omega, int32_t precision, double rel_tol, double* x_out,
+                       int32_t flags, mfbem_stats* stats);
+
+/* Same for a static problem (one solve). */
+int mfbem_solve_staela(mfbem_handle* h, double mu, double nu, int32_t precision, double rel_tol, double* x_out,
+                       int32_t flags, mfbem_stats* stats);
+
+/* Statistics of the last assemble / sweep on this handle. */
+int mfbem_last_stats(mfbem_handle* h, mfbem_stats* stats);
+
+/* Error message of the last failing call on this thread ("" if none). */
+const char* mfbem_last_error(void);
+
+/* Library build identification: "<version> sm_103a". */
+const char* mfbem_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MFBEM_H */

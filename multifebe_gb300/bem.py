@@ -1,0 +1,176 @@
+"""Host-side mirror of the reference's region-builder / solver interface for the
+collocation-BEM path (the calls MultiFEBE's Fortran makes, from Python).
+
+    region = BemRegion(deck)                         # build_data* + mesh upload
+    A, b = region.build_lse_staela(mu, nu)           # build_lse_mechanics_bem_staela
+    A, b = region.build_lse_harela(material, omega)  # build_lse_mechanics_bem_harela
+    x = solve_lse(A, b)                              # solve_lse_r / solve_lse_c (FP64 LU on the GPU)
+    X = region.sweep_harela(material, omegas, precision="mixed")   # batched device sweep
+    u, t = region.solution(x)                        # assign_solution_*
+
+Every compute call goes through the native library (CUDA kernels for sm_103a);
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._abi import check
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+# src/read_settings.f90 defaults
+DEFAULT_SETTINGS = dict(qsi_relative_error=1e-6, qsi_ns_max=16, precalset_gln=(2, 3, 4, 5, 6, 7, 8, 9),
+                        geometric_tolerance=1e-6)
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+class BemRegion:
+    """One BE region (ordinary boundaries, continuous quad8) on the GPU."""
+
+    def __init__(self, deck, **settings):
+        s = dict(DEFAULT_SETTINGS)
+        s.update(settings)
+        self.deck = deck
+        self.settings = s
+        L = _abi.load()
+        self._X = np.ascontiguousarray(deck.nodes, dtype=np.float64)
+        self._conn = np.ascontiguousarray(deck.conn, dtype=np.int32)
+        self._ct = np.ascontiguousarray(deck.ctype, dtype=np.int32)
+        self._cv = np.ascontiguousarray(deck.cvalue, dtype=np.complex128)
+        self._gl = np.ascontiguousarray(s["precalset_gln"], dtype=np.int32)
+        self._prep = L.mfbem_prep_create(deck.n_nodes, _p(self._X), deck.n_elements, _p(self._conn, _ip),
+                                         _p(self._ct, _ip), _p(self._cv.view(np.float64)), s["qsi_relative_error"],
+                                         s["qsi_ns_max"], len(self._gl), _p(self._gl, _ip),
+                                         s["geometric_tolerance"])
+        self.desc = L.mfbem_prep_desc(self._prep)
+        self.n = int(self.desc.contents.n_dof)
+        self._h = ctypes.c_void_p()
+        check(L.mfbem_mesh_upload(self.desc, ctypes.byref(self._h)))
+
+    def close(self):
+        L = _abi.load()
+        if getattr(self, "_h", None) is not None and self._h.value:
+            L.mfbem_mesh_release(self._h)
+            self._h = ctypes.c_void_p()
+        if getattr(self, "_prep", None):
+            L.mfbem_prep_free(self._prep)
+            self._prep = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------------- data
+    def dof_map(self):
+        nn = self.deck.n_nodes
+        dof = np.zeros(3 * nn, dtype=np.int32)
+        order = np.zeros(nn, dtype=np.int32)
+        _abi.load().mfbem_prep_dof(self._prep, _p(dof, _ip), _p(order, _ip))
+        return dof.reshape(nn, 3), order
+
+    def element_data(self):
+        d = self.desc.contents
+        ne = self.deck.n_elements
+        cl = np.ctypeslib.as_array(d.csize, shape=(ne,)).copy()
+        gf = np.ctypeslib.as_array(d.n_phi, shape=(ne,)).copy()
+        ball = np.ctypeslib.as_array(d.bball, shape=(ne * 4,)).reshape(ne, 4).copy()
+        return cl, gf, ball
+
+    def stats(self):
+        s = _abi.Stats()
+        check(_abi.load().mfbem_last_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+    # ---------------------------------------------------------------- builders
+    def build_lse_staela(self, mu, nu, A=None, b=None):
+        n = self.n
+        if A is None:
+            A = np.zeros((n, n), dtype=np.float64, order="F")
+        if b is None:
+            b = np.zeros(n, dtype=np.float64)
+        assert A.flags.f_contiguous and A.dtype == np.float64 and b.dtype == np.float64
+        check(_abi.load().mfbem_assemble_staela(self._h, float(mu), float(nu), _p(A), A.shape[0], _p(b), 0))
+        return A, b
+
+    def build_lse_harela(self, mat, omega, A=None, b=None):
+        n = self.n
+        if A is None:
+            A = np.zeros((n, n), dtype=np.complex128, order="F")
+        if b is None:
+            b = np.zeros(n, dtype=np.complex128)
+        assert A.flags.f_contiguous and A.dtype == np.complex128 and b.dtype == np.complex128
+        lam = np.array([complex(mat["lambda"]).real, complex(mat["lambda"]).imag])
+        mu = np.array([complex(mat["mu"]).real, complex(mat["mu"]).imag])
+        nu = np.array([complex(mat["nu"]).real, complex(mat["nu"]).imag])
+        check(_abi.load().mfbem_assemble_harela(self._h, _p(lam), _p(mu), float(mat["rho"]), _p(nu), float(omega),
+                                                _p(A), A.shape[0], _p(b), 0))
+        return A, b
+
+    # ---------------------------------------------------------------- device pipelines
+    def sweep_harela(self, mat, omegas, precision="plain", rel_tol=1e-12):
+        """Assemble + factorise + solve every frequency on the device.
+        precision 'plain': FP64 LU; 'mixed': complex64 LU + FP64 refinement."""
+        om = np.ascontiguousarray(omegas, dtype=np.float64)
+        nf = om.size
+        X = np.zeros((nf, self.n), dtype=np.complex128)
+        lam = np.array([complex(mat["lambda"]).real, complex(mat["lambda"]).imag])
+        mu = np.array([complex(mat["mu"]).real, complex(mat["mu"]).imag])
+        nu = np.array([complex(mat["nu"]).real, complex(mat["nu"]).imag])
+        st = _abi.Stats()
+        prec = {"plain": 0, "mixed": 1}[precision]
+        check(_abi.load().mfbem_sweep_harela(self._h, _p(lam), _p(mu), float(mat["rho"]), _p(nu), nf, _p(om), prec,
+                                             rel_tol, _p(X), 0, ctypes.byref(st)))
+        self.last_stats = st.as_dict()
+        return X
+
+    def solve_staela(self, mu, nu, precision="plain", rel_tol=1e-12):
+        x = np.zeros(self.n, dtype=np.float64)
+        st = _abi.Stats()
+        prec = {"plain": 0, "mixed": 1}[precision]
+        check(_abi.load().mfbem_solve_staela(self._h, float(mu), float(nu), prec, rel_tol, _p(x), 0,
+                                             ctypes.byref(st)))
+        self.last_stats = st.as_dict()
+        return x
+
+    def solution(self, x):
+        """Nodal (u, t): the unknown of each (node, direction) is u when the
+        traction is prescribed and t otherwise (src/assign_solution_mechanics_static.f90:130-150)."""
+        d = self.deck
+        dof, _ = self.dof_map()
+        cplx = np.iscomplexobj(x)
+        dt = np.complex128 if cplx else np.float64
+        cv = d.cvalue if cplx else d.cvalue.real
+        known_u = d.ctype == 0
+        u = np.where(known_u, cv, 0).astype(dt)
+        t = np.where(~known_u, cv, 0).astype(dt)
+        vals = x[dof]
+        u[~known_u] = vals[~known_u]
+        t[known_u] = vals[known_u]
+        return u, t
+
+
+def solve_lse(A, b, ipiv=None, factorize=True):
+    """solve_lse_r / solve_lse_c with LAPACK semantics: A (Fortran order) is
+    overwritten by its LU factors, ipiv by the 1-based pivots, b by x."""
+    L = _abi.load()
+    n = A.shape[0]
+    assert A.flags.f_contiguous
+    if ipiv is None:
+        ipiv = np.zeros(n, dtype=np.int32)
+    bb = b if b.ndim == 2 else b.reshape(n, 1)
+    nrhs = bb.shape[1]
+    assert bb.flags.f_contiguous
+    fn = L.mfbem_solve_c if np.iscomplexobj(A) else L.mfbem_solve_r
+    rc = fn(n, _p(A), _p(ipiv, _ip), 1, None, None, None, None, nrhs, _p(bb), 1 if factorize else 0, 0, 0, 0)
+    check(rc)
+    return b, ipiv

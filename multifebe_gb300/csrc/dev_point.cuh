@@ -1,0 +1,194 @@
+// Per-integration-point evaluation of the fundamental solutions (without their
+// constant factors), device side.
+//   static (Kelvin):      lib/fbem/src/bem_staela3d.f90:622-633
+//   time-harmonic (Stokes): lib/fbem/src/bem_harela3d.f90:654-688, with the
+//   decomposed exponential E_n(z) of lib/fbem/src/numerical.f90:1258-1331
+#pragma once
+#include "dev_complex.cuh"
+
+namespace mfb {
+
+struct StaelaP {
+  double cteu1, cteu2, ctet1, ctet2;
+};
+
+// u* / t* coefficient block of fbem_bem_harela3d_parameters (bem_harela3d.f90:118-134)
+struct HarParD {
+  cd k1, k2;
+  cd psi[6], chi[6];
+  cd T1[10], T2[9], T3[9];
+  cd cte_u, cte_t;
+};
+
+__host__ __device__ inline StaelaP staela_params(double mu, double nu) {
+  StaelaP p;
+  p.cteu1 = 1.0 / (16.0 * kPi * mu * (1.0 - nu));
+  p.cteu2 = 3.0 - 4.0 * nu;
+  p.ctet1 = -1.0 / (8.0 * kPi * (1.0 - nu));
+  p.ctet2 = 1.0 - 2.0 * nu;
+  return p;
+}
+
+// fbem_bem_harela3d_calculate_parameters (bem_harela3d.f90:143-287), u*/t* part
+__host__ __device__ inline HarParD harela_params(cd lambda, cd mu, double rho, double omega) {
+  HarParD p;
+  const cd I = mk(0.0, 1.0);
+  cd c1 = csqrt_((lambda + 2.0 * mu) / rho);
+  cd c2 = csqrt_(mu / rho);
+  cd k1 = omega / c1, k2 = omega / c2;
+  p.k1 = k1;
+  p.k2 = k2;
+  cd c1p2 = c1 * c1, c2p2 = c2 * c2, c1p3 = c1p2 * c1, c1p4 = c1p2 * c1p2;
+  cd k2p2 = k2 * k2;
+  cd ik1 = I * k1, ik2 = I * k2, ik1p2 = ik1 * ik1, ik2p2 = ik2 * ik2;
+  cd r = c2p2 / c1p2;
+  double om2 = omega * omega;
+  p.psi[0] = 0.5 * (1.0 + r);
+  p.psi[1] = (-1.0 / 3.0 * (2.0 / c2 + c2p2 / c1p3)) * I * omega;
+  p.psi[2] = I * k1 / k2p2;
+  p.psi[3] = 1.0 / ik2;
+  p.psi[4] = 1.0 / k2p2;
+  p.psi[5] = -1.0 / k2p2;
+  p.chi[0] = -0.5 * (1.0 - r);
+  p.chi[1] = -r;
+  p.chi[2] = -3.0 * r / ik1;
+  p.chi[3] = 3.0 / ik2;
+  p.chi[4] = -3.0 * r / ik1p2;
+  p.chi[5] = 3.0 / ik2p2;
+  p.T1[0] = 3.0 * (r - 1.0);
+  p.T1[1] = -0.25 * (1.0 / c2p2 - c2p2 / c1p4) * om2;
+  p.T1[2] = -2.0 * I * k1 * r;
+  p.T1[3] = 2.0 * I * k2;
+  p.T1[4] = -12.0 * r;
+  p.T1[5] = mk(12.0);
+  p.T1[6] = -r * 30.0 / ik1;
+  p.T1[7] = 30.0 / ik2;
+  p.T1[8] = -r * 30.0 / ik1p2;
+  p.T1[9] = 30.0 / ik2p2;
+  p.T2[0] = -r;
+  p.T2[1] = -0.25 * (1.0 / c2p2 + c2p2 / c1p4) * om2;
+  p.T2[2] = -I * k2;
+  p.T2[3] = 2.0 * r;
+  p.T2[4] = mk(-3.0);
+  p.T2[5] = r * 6.0 / ik1;
+  p.T2[6] = -6.0 / ik2;
+  p.T2[7] = r * 6.0 / ik1p2;
+  p.T2[8] = -6.0 / ik2p2;
+  p.T3[0] = r;
+  p.T3[1] = 0.25 * (3.0 * c2p2 / c1p4 - 2.0 / c1p2 + 1.0 / c2p2) * om2;
+  p.T3[2] = (2.0 * r - 1.0) * I * k1;
+  p.T3[3] = 4.0 * r - 1.0;
+  p.T3[4] = mk(-2.0);
+  p.T3[5] = r * 6.0 / ik1;
+  p.T3[6] = -6.0 / ik2;
+  p.T3[7] = r * 6.0 / ik1p2;
+  p.T3[8] = -6.0 / ik2p2;
+  p.cte_u = k1_4Pi / mu;
+  p.cte_t = mk(k1_4Pi);
+  return p;
+}
+
+// E_2..E_5 of z (numerical.f90:1258-1331): E_n(z) = e^z - sum_{k<n} z^k/k!.
+// For |z|<=1 the reference sums the series tail from k=n+6 down to 6; the same
+// terms are summed here in nested (Horner) form.
+__device__ __forceinline__ void zexp_2to5(cd z, cd& E2, cd& E3, cd& E4, cd& E5) {
+  double az = cabs_(z);
+  cd z2 = z * z, z3 = z2 * z, z4 = z3 * z;
+  if (az <= 1.0) {
+    int n = 1;
+    if (az > 1e-6) {
+      double v = pow(10.0, 1.176 + 0.175 * log10(az));
+      n = (int)floor(v + 0.5);
+    }
+    int N = n + 6;
+    cd t = mk(1.0);
+    for (int k = N; k >= 7; --k) t = 1.0 + t * z * (1.0 / (double)k);
+    cd z5 = z4 * z, z6 = z5 * z;
+    cd e6 = (z6 * (1.0 / 720.0)) * t;
+    E5 = e6 + z5 * (1.0 / 120.0);
+    E4 = E5 + z4 * (1.0 / 24.0);
+    E3 = E4 + z3 * (1.0 / 6.0);
+    E2 = E3 + z2 * 0.5;
+  } else {
+    cd e0 = cexp_(z);
+    cd e1 = e0 - 1.0;
+    E2 = e1 - z;
+    E3 = E2 - 0.5 * z2;
+    E4 = E3 - (1.0 / 6.0) * z3;
+    E5 = E4 - (1.0 / 24.0) * z4;
+  }
+}
+
+// Regular-point harmonic fundamental solutions: fu[3*il+ik] = u*_{il,ik}/cte_u,
+// ft[...] = t*_{il,ik}/cte_t.  With full == false the 1/r^2 terms of TT1..TT3
+// are dropped (bem_harela3d.f90 sbie_int); the caller adds them back.
+__device__ __forceinline__ void harela_coeffs(const HarParD& p, double r, cd& psi, cd& chi, cd& TT1, cd& TT2,
+                                              cd& TT3, double& d1r1, double& d1r2, bool full) {
+  d1r1 = 1.0 / r;
+  d1r2 = d1r1 * d1r1;
+  double d1r3 = d1r2 * d1r1, d1r4 = d1r3 * d1r1;
+  cd z1 = mk(p.k1.im * r, -p.k1.re * r);  // -i k1 r
+  cd z2 = mk(p.k2.im * r, -p.k2.re * r);
+  cd a2, a3, a4, a5, b2, b3, b4, b5;
+  zexp_2to5(z1, a2, a3, a4, a5);
+  zexp_2to5(z2, b2, b3, b4, b5);
+  a2 = a2 * d1r1; b2 = b2 * d1r1;
+  a3 = a3 * d1r2; b3 = b3 * d1r2;
+  a4 = a4 * d1r3; b4 = b4 * d1r3;
+  a5 = a5 * d1r4; b5 = b5 * d1r4;
+  psi = p.psi[0] * d1r1 + p.psi[1] + b2 + p.psi[2] * a3 + p.psi[3] * b3 + p.psi[4] * a4 + p.psi[5] * b4;
+  chi = p.chi[0] * d1r1 + p.chi[1] * a2 + b2 + p.chi[2] * a3 + p.chi[3] * b3 + p.chi[4] * a4 + p.chi[5] * b4;
+  TT1 = p.T1[1] + p.T1[2] * a2 + p.T1[3] * b2 + p.T1[4] * a3 + p.T1[5] * b3 + p.T1[6] * a4 + p.T1[7] * b4 +
+        p.T1[8] * a5 + p.T1[9] * b5;
+  TT2 = p.T2[1] + p.T2[2] * b2 + p.T2[3] * a3 + p.T2[4] * b3 + p.T2[5] * a4 + p.T2[6] * b4 + p.T2[7] * a5 +
+        p.T2[8] * b5;
+  TT3 = p.T3[1] + p.T3[2] * a2 + p.T3[3] * a3 + p.T3[4] * b3 + p.T3[5] * a4 + p.T3[6] * b4 + p.T3[7] * a5 +
+        p.T3[8] * b5;
+  if (full) {
+    TT1 = TT1 + p.T1[0] * d1r2;
+    TT2 = TT2 + p.T2[0] * d1r2;
+    TT3 = TT3 + p.T3[0] * d1r2;
+  }
+}
+
+__device__ __forceinline__ void harela_point(const HarParD& p, const double rv[3], const double n[3], cd fu[9],
+                                             cd ft[9]) {
+  double r = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+  cd psi, chi, TT1, TT2, TT3;
+  double d1r1, d1r2;
+  harela_coeffs(p, r, psi, chi, TT1, TT2, TT3, d1r1, d1r2, true);
+  double dr[3] = {rv[0] * d1r1, rv[1] * d1r1, rv[2] * d1r1};
+  double drdn = dr[0] * n[0] + dr[1] * n[1] + dr[2] * n[2];
+#pragma unroll
+  for (int il = 0; il < 3; ++il)
+#pragma unroll
+    for (int ik = 0; ik < 3; ++ik) {
+      double rr = dr[il] * dr[ik];
+      cd u = -(chi * rr);
+      cd t = TT1 * (rr * drdn) + TT2 * (dr[ik] * n[il]) + TT3 * (dr[il] * n[ik]);
+      if (il == ik) {
+        u = u + psi;
+        t = t + TT2 * drdn;
+      }
+      fu[3 * il + ik] = u;
+      ft[3 * il + ik] = t;
+    }
+}
+
+__device__ __forceinline__ void staela_point(const StaelaP& k, const double rv[3], const double n[3], double fu[9],
+                                             double ft[9]) {
+  double r = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+  double d1r = 1.0 / r, d1r2 = d1r * d1r;
+  double dr[3] = {rv[0] * d1r, rv[1] * d1r, rv[2] * d1r};
+  double drdn = dr[0] * n[0] + dr[1] * n[1] + dr[2] * n[2];
+#pragma unroll
+  for (int il = 0; il < 3; ++il)
+#pragma unroll
+    for (int ik = 0; ik < 3; ++ik) {
+      double dk = (il == ik) ? 1.0 : 0.0;
+      fu[3 * il + ik] = d1r * (k.cteu2 * dk + dr[il] * dr[ik]);
+      ft[3 * il + ik] = d1r2 * ((k.ctet2 * dk + 3.0 * dr[il] * dr[ik]) * drdn + k.ctet2 * (n[il] * dr[ik] - n[ik] * dr[il]));
+    }
+}
+
+}  // namespace mfb

@@ -1,0 +1,504 @@
+// C-ABI of the GB300 collocation-BEM library (see include/mfbem.h): handle
+// management, the once-per-mesh device precompute, per-frequency assembly,
+// and the dense solves. Single translation unit for all device code.
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mfbem.h"
+#include "bem_common.h"
+#include "dev_complex.cuh"
+#include "dev_point.cuh"
+#include "mfbem_dev.h"
+#include "mfbem_host.h"
+#include "mfbem_precompute.cuh"
+#include "mfbem_assemble.cuh"
+#include "mfbem_lu.cuh"
+
+namespace mfb {
+static thread_local std::string g_err;
+void set_error(const std::string& s) { g_err = s; }
+int fail(int code, const std::string& s) {
+  g_err = s;
+  return code;
+}
+}  // namespace mfb
+
+using namespace mfb;
+
+#define CK(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) return fail(MFBEM_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+#define CKB(call)                                                                                  \
+  do {                                                                                             \
+    cublasStatus_t s_ = (call);                                                                    \
+    if (s_ != CUBLAS_STATUS_SUCCESS) return fail(MFBEM_ECUDA, std::string(#call) + ": cublas status " + std::to_string((int)s_)); \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct mfbem_handle {
+  DMesh m;
+  std::vector<void*> owned;
+  QsCurves* d_qs = nullptr;
+  QsCurves* d_q15 = nullptr;
+  int ndof = 0, ne = 0, nn = 0;
+  cudaStream_t st = nullptr;
+  cublasHandle_t blas = nullptr;
+  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu;
+  mfbem_stats stats{};
+  long long pts_reg = 0, pts_adp = 0, pts_sing = 0;
+  int* d_err = nullptr;
+};
+
+static int dalloc(mfbem_handle* h, void** p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) return fail(MFBEM_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  h->owned.push_back(*p);
+  return 0;
+}
+template <typename T>
+static int dupload(mfbem_handle* h, T** dst, const T* src, size_t n) {
+  int rc = dalloc(h, (void**)dst, n * sizeof(T));
+  if (rc) return rc;
+  if (n) CK(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+  return 0;
+}
+static int ensure(DevBuf& b, size_t bytes) {
+  if (b.bytes >= bytes) return 0;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e != cudaSuccess) return fail(MFBEM_ENOMEM, std::string("cudaMalloc(work): ") + cudaGetErrorString(e));
+  b.bytes = bytes;
+  return 0;
+}
+
+static bool g_tables_ready = false;
+static int init_tables() {
+  if (g_tables_ready) return 0;
+  const GLTables& t = host_gauss_tables();
+  CK(cudaMemcpyToSymbol(c_gl, &t, sizeof(GLTables)));
+  g_tables_ready = true;
+  return 0;
+}
+
+static inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+extern "C" const char* mfbem_last_error(void) { return g_err.c_str(); }
+extern "C" const char* mfbem_version(void) { return "mfbem-gb300 0.1 sm_103a"; }
+
+// ---------------------------------------------------------------------------
+// upload + once-per-mesh precompute
+// ---------------------------------------------------------------------------
+extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
+  g_err.clear();
+  if (!d || !out) return fail(MFBEM_EARG, "null argument");
+  *out = nullptr;
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) return fail(MFBEM_ECUDA, "no CUDA device");
+  const int nn = d->n_nodes, ne = d->n_elements, ndof = d->n_dof;
+  if (nn <= 0 || ne <= 0 || ndof != 3 * nn) return fail(MFBEM_EARG, "n_dof must be 3*n_nodes for one BE region");
+  if (d->n_precalsets < 1 || d->n_precalsets > 16) return fail(MFBEM_EARG, "n_precalsets out of range [1,16]");
+  if (d->qsi_ns_max < 1 || d->qsi_ns_max > 17) return fail(MFBEM_EUNSUPPORTED, "qsi_ns_max must be in [1,17]");
+  for (int i = 0; i < d->n_precalsets; ++i)
+    if (d->precalset_gln[i] < 1 || d->precalset_gln[i] > 32 || (i && d->precalset_gln[i] <= d->precalset_gln[i - 1]))
+      return fail(MFBEM_EARG, "precalset_gln must be increasing in [1,32]");
+  int rc = init_tables();
+  if (rc) return rc;
+  mfbem_handle* h = new mfbem_handle();
+  h->ndof = ndof;
+  h->ne = ne;
+  h->nn = nn;
+  DMesh& m = h->m;
+  std::memset(&m, 0, sizeof(m));
+  m.ne = ne;
+  m.ndn = nn;
+  m.ndof = ndof;
+  m.nps = d->n_precalsets;
+  m.ns_max = d->qsi_ns_max;
+  m.ptot = 0;
+  m.ps_gln_max = 0;
+  for (int i = 0; i < m.nps; ++i) {
+    m.ps_gln[i] = d->precalset_gln[i];
+    m.ps_off[i] = m.ptot;
+    m.ptot += d->precalset_gln[i] * d->precalset_gln[i];
+    m.ps_gln_max = std::max(m.ps_gln_max, d->precalset_gln[i]);
+  }
+  m.geo_tol = d->geometric_tolerance;
+  // --- host bookkeeping (topology only)
+  std::vector<int> dn_of(nn, -1);
+  for (int s = 0; s < nn; ++s) {
+    int r1 = d->row[3 * s];
+    if (r1 < 1 || (r1 - 1) % 3 != 0 || d->row[3 * s + 1] != r1 + 1 || d->row[3 * s + 2] != r1 + 2 || r1 + 2 > ndof) {
+      delete h;
+      return fail(MFBEM_EARG, "node rows must be node-wise consecutive triples");
+    }
+    dn_of[s] = (r1 - 1) / 3;
+    for (int k = 0; k < 3; ++k) {
+      int ct = d->ctype[3 * s + k];
+      int c = ct == 0 ? d->col[6 * s + 3 + k] : d->col[6 * s + k];
+      if ((ct != 0 && ct != 1) || c != r1 + k) {
+        delete h;
+        return fail(MFBEM_EUNSUPPORTED, "only ctype 0/1 with col == row (ordinary BE boundary) is supported");
+      }
+    }
+  }
+  std::vector<int> edof(8 * (size_t)ne), rev(ne, 0);
+  for (int e = 0; e < ne; ++e) {
+    for (int k = 0; k < 8; ++k) {
+      int s = d->element_node[8 * e + k] - 1;
+      if (s < 0 || s >= nn) { delete h; return fail(MFBEM_EARG, "element_node out of range"); }
+      edof[8 * e + k] = 3 * dn_of[s];
+    }
+    if (d->reversion) rev[e] = d->reversion[e] ? 1 : 0;
+  }
+  std::vector<int> dct(ndof);
+  std::vector<double> dcv(2 * (size_t)ndof);
+  for (int s = 0; s < nn; ++s)
+    for (int k = 0; k < 3; ++k) {
+      int dof = 3 * dn_of[s] + k;
+      dct[dof] = d->ctype[3 * s + k];
+      dcv[2 * dof] = d->cvalue[6 * s + 2 * k];
+      dcv[2 * dof + 1] = d->cvalue[6 * s + 2 * k + 1];
+    }
+  // collocation points in the builders' collocation order
+  struct CP { double x[3], xi[2]; int dn, kind, e, kn; };
+  std::vector<CP> cps;
+  std::vector<char> col(nn, 0);
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 8; ++k) {
+      int s = d->element_node[8 * e + k] - 1;
+      CP c;
+      c.dn = dn_of[s];
+      c.e = e;
+      c.kn = k;
+      if (d->sbie[s] == 0) {
+        if (col[s]) continue;
+        col[s] = 1;
+        c.kind = 0;
+        for (int q = 0; q < 3; ++q) c.x[q] = d->x_gn[24 * (size_t)e + 3 * k + q];
+        c.xi[0] = q8xi(k, 0);
+        c.xi[1] = q8xi(k, 1);
+      } else {
+        c.kind = 1;
+        for (int q = 0; q < 3; ++q) c.x[q] = d->x_i_sbie_mca[24 * (size_t)e + 3 * k + q];
+        c.xi[0] = d->xi_i_sbie_mca[16 * (size_t)e + 2 * k];
+        c.xi[1] = d->xi_i_sbie_mca[16 * (size_t)e + 2 * k + 1];
+      }
+      cps.push_back(c);
+    }
+  std::stable_sort(cps.begin(), cps.end(), [](const CP& a, const CP& b) { return a.dn < b.dn; });
+  const int ncp = (int)cps.size();
+  m.ncp = ncp;
+  std::vector<int> dn_cp(nn + 1, 0);
+  for (auto& c : cps) dn_cp[c.dn + 1]++;
+  for (int i = 0; i < nn; ++i) dn_cp[i + 1] += dn_cp[i];
+  std::vector<double> cpx(3 * (size_t)ncp), cpxi(2 * (size_t)ncp);
+  std::vector<int> cp_dn(ncp), cp_kind(ncp), cp_e(ncp), cp_kn(ncp);
+  // node -> incident (element, local) in element order
+  std::vector<std::vector<int>> inc(nn);
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 8; ++k) inc[d->element_node[8 * e + k] - 1].push_back(8 * e + k);
+  std::vector<int> node_of_dn(nn);
+  for (int s = 0; s < nn; ++s) node_of_dn[dn_of[s]] = s;
+  std::vector<int> inc_start(ncp + 1, 0), inc_el;
+  for (int i = 0; i < ncp; ++i) {
+    const CP& c = cps[i];
+    for (int q = 0; q < 3; ++q) cpx[3 * i + q] = c.x[q];
+    cpxi[2 * i] = c.xi[0];
+    cpxi[2 * i + 1] = c.xi[1];
+    cp_dn[i] = c.dn;
+    cp_kind[i] = c.kind;
+    cp_e[i] = c.e;
+    cp_kn[i] = c.kn;
+    if (c.kind == 0)
+      for (int v : inc[node_of_dn[c.dn]]) inc_el.push_back(v);
+    inc_start[i + 1] = (int)inc_el.size();
+  }
+  // --- device arrays
+  double *ex, *cl, *ball, *dcvd, *cpxd, *cpxid, *ngn, *tbp;
+  int *gln, *revd, *edofd, *dctd, *cpdn, *cpk, *cpe, *cpkn, *dncp, *incs, *ince;
+  if ((rc = dupload(h, &ex, d->x_gn, 24 * (size_t)ne)) || (rc = dupload(h, &cl, d->csize, (size_t)ne)) ||
+      (rc = dupload(h, &gln, d->n_phi, (size_t)ne)) || (rc = dupload(h, &ball, d->bball, 4 * (size_t)ne)) ||
+      (rc = dupload(h, &revd, rev.data(), rev.size())) || (rc = dupload(h, &edofd, edof.data(), edof.size())) ||
+      (rc = dupload(h, &dctd, dct.data(), dct.size())) || (rc = dupload(h, &dcvd, dcv.data(), dcv.size())) ||
+      (rc = dupload(h, &cpxd, cpx.data(), cpx.size())) || (rc = dupload(h, &cpxid, cpxi.data(), cpxi.size())) ||
+      (rc = dupload(h, &cpdn, cp_dn.data(), cp_dn.size())) || (rc = dupload(h, &cpk, cp_kind.data(), cp_kind.size())) ||
+      (rc = dupload(h, &cpe, cp_e.data(), cp_e.size())) || (rc = dupload(h, &cpkn, cp_kn.data(), cp_kn.size())) ||
+      (rc = dupload(h, &dncp, dn_cp.data(), dn_cp.size())) || (rc = dupload(h, &incs, inc_start.data(), inc_start.size())) ||
+      (rc = dupload(h, &ince, inc_el.data(), inc_el.size())) || (rc = dupload(h, &ngn, d->n_gn, 24 * (size_t)ne)) ||
+      (rc = dupload(h, &tbp, d->tbp_gn, 24 * (size_t)ne))) {
+    mfbem_mesh_release(h);
+    return rc;
+  }
+  m.ex = ex; m.cl = cl; m.gln_far = gln; m.ball = ball; m.rev = revd; m.edof = edofd;
+  m.dct = dctd; m.dcv = dcvd; m.cpx = cpxd; m.cp_xi = cpxid; m.cp_dn = cpdn; m.cp_kind = cpk;
+  m.cp_elem = cpe; m.cp_kn = cpkn; m.dn_cp = dncp; m.inc_start = incs; m.inc_el = ince;
+  m.n_gn = ngn; m.tbp_gn = tbp;
+  QsCurves q = qs_curves(d->qsi_relative_error), q15 = qs_curves(1e-15);
+  if ((rc = dupload(h, &h->d_qs, &q, 1)) || (rc = dupload(h, &h->d_q15, &q15, 1)) ||
+      (rc = dalloc(h, (void**)&m.px, 3 * sizeof(double) * (size_t)ne * m.ptot)) ||
+      (rc = dalloc(h, (void**)&m.pn, 3 * sizeof(double) * (size_t)ne * m.ptot)) ||
+      (rc = dalloc(h, (void**)&m.pphi, 8 * sizeof(double) * (size_t)ne * m.ptot)) ||
+      (rc = dalloc(h, (void**)&m.cls, (size_t)ncp * ne)) ||
+      (rc = dalloc(h, (void**)&m.ft, sizeof(double) * FT_D * (size_t)ncp)) ||
+      (rc = dalloc(h, (void**)&m.ft_ok, sizeof(int) * (size_t)ncp)) ||
+      (rc = dalloc(h, (void**)&h->d_err, sizeof(int)))) {
+    mfbem_mesh_release(h);
+    return rc;
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  k_datasets<<<ne, 128>>>(m);
+  k_classify<<<std::min(nblk((long long)ncp * ne, 256), 152u * 16u), 256>>>(m, h->d_qs);
+  // counts and list offsets
+  int *nreg, *nadp, *nsing;
+  long long* npts;
+  if ((rc = dalloc(h, (void**)&nreg, sizeof(int) * ncp)) || (rc = dalloc(h, (void**)&nadp, sizeof(int) * ncp)) ||
+      (rc = dalloc(h, (void**)&nsing, sizeof(int) * ncp)) || (rc = dalloc(h, (void**)&npts, sizeof(long long) * ncp)) ||
+      (rc = dalloc(h, (void**)&m.reg_start, sizeof(int) * (ncp + 1))) ||
+      (rc = dalloc(h, (void**)&m.adp_start, sizeof(int) * (ncp + 1))) ||
+      (rc = dalloc(h, (void**)&m.sing_start, sizeof(int) * (ncp + 1)))) {
+    mfbem_mesh_release(h);
+    return rc;
+  }
+  long long* pts_base;
+  if ((rc = dalloc(h, (void**)&pts_base, sizeof(long long) * (ncp + 1)))) { mfbem_mesh_release(h); return rc; }
+  k_count<<<nblk(ncp, 8), 256>>>(m, nreg, nadp, nsing, npts);
+  k_scan<int, int><<<1, 1024>>>(nreg, m.reg_start, ncp);
+  k_scan<int, int><<<1, 1024>>>(nadp, m.adp_start, ncp);
+  k_scan<int, int><<<1, 1024>>>(nsing, m.sing_start, ncp);
+  k_scan<long long, long long><<<1, 1024>>>(npts, pts_base, ncp);
+  CK(cudaGetLastError());
+  int tot[3];
+  long long totp;
+  CK(cudaMemcpy(&tot[0], m.reg_start + ncp, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&tot[1], m.adp_start + ncp, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&tot[2], m.sing_start + ncp, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&totp, pts_base + ncp, sizeof(long long), cudaMemcpyDeviceToHost));
+  m.nreg = tot[0];
+  m.nadp = tot[1];
+  m.nsing = tot[2];
+  int *adp_cp, *sing_cp;
+  if ((rc = dalloc(h, (void**)&m.reg_pair, sizeof(int) * (m.nreg + 1))) ||
+      (rc = dalloc(h, (void**)&m.reg_pt, sizeof(long long) * (m.nreg + 1))) ||
+      (rc = dalloc(h, (void**)&m.adp_e, sizeof(int) * (m.nadp + 1))) ||
+      (rc = dalloc(h, (void**)&adp_cp, sizeof(int) * (m.nadp + 1))) ||
+      (rc = dalloc(h, (void**)&m.sing_e, sizeof(int) * (m.nsing + 1))) ||
+      (rc = dalloc(h, (void**)&sing_cp, sizeof(int) * (m.nsing + 1)))) {
+    mfbem_mesh_release(h);
+    return rc;
+  }
+  k_fill<<<nblk(ncp, 8), 256>>>(m, pts_base, adp_cp, sing_cp);
+  CK(cudaMemcpy(m.reg_pt + m.nreg, &totp, sizeof(long long), cudaMemcpyHostToDevice));
+  h->pts_reg = totp;
+  // adaptive subdivision leaves
+  int* nl;
+  if ((rc = dalloc(h, (void**)&nl, sizeof(int) * (m.nadp + 1))) ||
+      (rc = dalloc(h, (void**)&m.adp_leaf, sizeof(int) * (m.nadp + 1)))) {
+    mfbem_mesh_release(h);
+    return rc;
+  }
+  if (m.nadp > 0) k_adp_count<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, adp_cp, nl);
+  k_scan<int, int><<<1, 1024>>>(nl, m.adp_leaf, (int)m.nadp);
+  int nleaf = 0;
+  CK(cudaMemcpy(&nleaf, m.adp_leaf + m.nadp, sizeof(int), cudaMemcpyDeviceToHost));
+  m.nleaf = nleaf;
+  long long* lpts;
+  if ((rc = dalloc(h, (void**)&m.leaf, sizeof(double) * LEAF_D * (m.nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&m.leaf_gln, sizeof(int) * (m.nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&m.leaf_pair, sizeof(int) * (m.nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&m.leaf_pt, sizeof(long long) * (m.nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&lpts, sizeof(long long) * (m.nleaf + 1)))) {
+    mfbem_mesh_release(h);
+    return rc;
+  }
+  if (m.nadp > 0) k_adp_fill<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, adp_cp);
+  if (m.nleaf > 0) k_leaf_points<<<nblk(m.nleaf, 256), 256>>>(m, lpts);
+  k_scan<long long, long long><<<1, 1024>>>(lpts, m.leaf_pt, (int)m.nleaf);
+  CK(cudaMemcpy(&h->pts_adp, m.leaf_pt + m.nleaf, sizeof(long long), cudaMemcpyDeviceToHost));
+  // singular pairs
+  long long* spts;
+  if ((rc = dalloc(h, (void**)&m.sing_d, sizeof(double) * SING_D * (m.nsing + 1))) ||
+      (rc = dalloc(h, (void**)&m.sing_i, sizeof(int) * SING_I * (m.nsing + 1))) ||
+      (rc = dalloc(h, (void**)&m.sing_pt, sizeof(long long) * (m.nsing + 1))) ||
+      (rc = dalloc(h, (void**)&spts, sizeof(long long) * (m.nsing + 1)))) {
+    mfbem_mesh_release(h);
+    return rc;
+  }
+  if (m.nsing > 0) k_sing_prep<<<nblk(m.nsing, 64), 64>>>(m, h->d_q15, sing_cp, spts);
+  k_scan<long long, long long><<<1, 1024>>>(spts, m.sing_pt, (int)m.nsing);
+  CK(cudaMemcpy(&h->pts_sing, m.sing_pt + m.nsing, sizeof(long long), cudaMemcpyDeviceToHost));
+  k_ft_prep<<<nblk(ncp, 128), 128>>>(m);
+  CK(cudaGetLastError());
+  CK(cudaDeviceSynchronize());
+  auto t1 = std::chrono::steady_clock::now();
+  h->stats.pairs_regular = m.nreg;
+  h->stats.pairs_adaptive = m.nadp;
+  h->stats.pairs_singular = m.nsing;
+  h->stats.points_regular = h->pts_reg;
+  h->stats.points_adaptive = h->pts_adp;
+  h->stats.points_singular = h->pts_sing;
+  h->stats.adaptive_leaves = (int)m.nleaf;
+  h->stats.ms_assemble = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+  if (cublasCreate(&h->blas) != CUBLAS_STATUS_SUCCESS) { mfbem_mesh_release(h); return fail(MFBEM_ECUDA, "cublasCreate"); }
+  cublasSetStream(h->blas, h->st);
+  *out = h;
+  return 0;
+}
+
+extern "C" int mfbem_mesh_release(mfbem_handle* h) {
+  if (!h) return MFBEM_EARG;
+  cudaDeviceSynchronize();
+  for (void* p : h->owned) cudaFree(p);
+  for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu})
+    if (b->p) cudaFree(b->p);
+  if (h->blas) cublasDestroy(h->blas);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return 0;
+}
+
+extern "C" int mfbem_last_stats(mfbem_handle* h, mfbem_stats* s) {
+  if (!h || !s) return fail(MFBEM_EARG, "null argument");
+  *s = h->stats;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// assembly into device buffers (nf systems: A at A + f*astride, b at b + f*bstride)
+// ---------------------------------------------------------------------------
+__global__ void k_harpar(const double* in /*nf x {lre,lim,mre,mim,rho,omega}*/, int nf, HarParD* out) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const double* q = in + 6 * f;
+  out[f] = harela_params(mk(q[0], q[1]), mk(q[2], q[3]), q[4], q[5]);
+}
+
+template <class POL>
+static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, int nf, double* A, size_t lda,
+                           size_t astride, double* b, size_t bstride) {
+  const DMesh& m = h->m;
+  constexpr int WPB = 4;
+  long long nw = (long long)m.ndn * nf;
+  unsigned g = nblk(nw, WPB);
+  CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
+  if (m.nreg > 0) k_reg<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
+  if (m.nadp > 0) k_adp<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
+  // the singular kernel keeps two combo sets per point: 2 warps per block
+  if (m.nsing > 0) k_sing<POL, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
+  k_free<POL><<<nblk(nw, 128), 128, 0, h->st>>>(m, pol, d_nu, nf, A, lda, astride, b, bstride, h->d_err);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+static int check_err(mfbem_handle* h) {
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (e) return fail(MFBEM_EGEOMETRY, "the normals/tangents configuration at a free-term node is not valid");
+  return 0;
+}
+
+// host <-> device copies of a column-major lda-strided matrix
+static int copy_mat(void* dst, size_t dpitch, const void* src, size_t spitch, size_t rows_bytes, size_t cols,
+                    cudaMemcpyKind kind, cudaStream_t st) {
+  CK(cudaMemcpy2DAsync(dst, dpitch, src, spitch, rows_bytes, cols, kind, st));
+  return 0;
+}
+
+template <bool CPLX>
+static int assemble_common(mfbem_handle* h, const void* polp, const double* nu_host, double* A, int lda, double* b,
+                           int flags) {
+  const int n = h->ndof;
+  if (lda < n) return fail(MFBEM_EARG, "lda < n_dof");
+  const size_t es = CPLX ? 16 : 8;
+  int rc;
+  if ((rc = ensure(h->nu, 2 * sizeof(double)))) return rc;
+  CK(cudaMemcpyAsync(h->nu.p, nu_host, 2 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  double *dA, *db;
+  size_t dlda;
+  const bool dev = flags & MFBEM_DEVICE_PTRS;
+  if (dev) {
+    dA = A;
+    db = b;
+    dlda = lda;
+    if (flags & MFBEM_OVERWRITE) {
+      CK(cudaMemset2DAsync(dA, (size_t)lda * es, 0, n * es, n, h->st));
+      CK(cudaMemsetAsync(db, 0, n * es, h->st));
+    }
+  } else {
+    if ((rc = ensure(h->A, (size_t)n * n * es)) || (rc = ensure(h->b, n * es))) return rc;
+    dA = (double*)h->A.p;
+    db = (double*)h->b.p;
+    dlda = n;
+    if (flags & MFBEM_OVERWRITE) {
+      CK(cudaMemsetAsync(dA, 0, (size_t)n * n * es, h->st));
+      CK(cudaMemsetAsync(db, 0, n * es, h->st));
+    } else {
+      if ((rc = copy_mat(dA, n * es, A, (size_t)lda * es, n * es, n, cudaMemcpyHostToDevice, h->st))) return rc;
+      CK(cudaMemcpyAsync(db, b, n * es, cudaMemcpyHostToDevice, h->st));
+    }
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, h->st);
+  if (CPLX) rc = launch_assembly(h, *(const PolHarmonic*)polp, (const double*)h->nu.p, 1, dA, dlda, 0, db, 0);
+  else rc = launch_assembly(h, *(const PolStatic*)polp, (const double*)h->nu.p, 1, dA, dlda, 0, db, 0);
+  cudaEventRecord(e1, h->st);
+  if (rc) return rc;
+  if (!dev) {
+    if ((rc = copy_mat(A, (size_t)lda * es, dA, n * es, n * es, n, cudaMemcpyDeviceToHost, h->st))) return rc;
+    CK(cudaMemcpyAsync(b, db, n * es, cudaMemcpyDeviceToHost, h->st));
+  }
+  rc = check_err(h);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  h->stats.ms_assemble = ms;
+  return rc;
+}
+
+extern "C" int mfbem_assemble_staela(mfbem_handle* h, double mu, double nu, double* A, int32_t lda, double* b,
+                                     int32_t flags) {
+  g_err.clear();
+  if (!h || !A || !b) return fail(MFBEM_EARG, "null argument");
+  PolStatic pol;
+  pol.k = staela_params(mu, nu);
+  double nuv[2] = {nu, 0.0};
+  return assemble_common<false>(h, &pol, nuv, A, lda, b, flags);
+}
+
+extern "C" int mfbem_assemble_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
+                                     const double nu[2], double omega, double* A, int32_t lda, double* b,
+                                     int32_t flags) {
+  g_err.clear();
+  if (!h || !A || !b || !lambda || !mu || !nu) return fail(MFBEM_EARG, "null argument");
+  int rc;
+  if ((rc = ensure(h->par, sizeof(HarParD) + 64))) return rc;
+  double q[6] = {lambda[0], lambda[1], mu[0], mu[1], rho, omega};
+  double* dq = (double*)((char*)h->par.p + sizeof(HarParD));
+  CK(cudaMemcpyAsync(dq, q, sizeof(q), cudaMemcpyHostToDevice, h->st));
+  k_harpar<<<1, 32, 0, h->st>>>(dq, 1, (HarParD*)h->par.p);
+  PolHarmonic pol;
+  pol.p = (const HarParD*)h->par.p;
+  return assemble_common<true>(h, &pol, nu, A, lda, b, flags);
+}
+
+#include "mfbem_solve.cuh"

@@ -1,0 +1,84 @@
+// Device-resident mesh snapshot and work lists, shared by the kernels
+// (mfbem_kernels.cu) and the C-ABI layer (mfbem_abi.cpp).
+//
+// HBM layout (all arrays structure-of-arrays, 0-based):
+//   elements   ex[ne][8][3], cl, gln_far, ball[ne][4], rev, edof[ne][8]
+//              (DOF index of direction 1 of each element node = row base)
+//   DOFs       dct[ndof] (0 u known / 1 t known), dcv[ndof] complex value
+//   colloc.    points sorted by DOF-order node ("dnode"): cpx[ncp][3], cp_dn,
+//              cp_kind (0 nodal SBIE / 1 SBIE-MCA), cp_elem, cp_kn, cp_xi[2];
+//              dn_cp[ndn+1] = range of points of each dnode (its 3 rows)
+//   datasets   px/pn[ne][ptot][3], pphi[ne][ptot][8]: x, unit normal and
+//              phi*J*w at the Gauss points of every precalculated rule
+//   pair class cls[ncp][ne]: rule index, CLS_ADP or CLS_SING
+//   lists      per collocation point, in element order: regular pairs
+//              (e | rule << 24) with exclusive point offsets, adaptive pairs
+//              with their subdivision leaves, singular pairs with their polar
+//              layout and static line integrals
+#pragma once
+#include <cstdint>
+
+namespace mfb {
+
+enum : uint8_t { CLS_ADP = 254, CLS_SING = 255 };
+
+constexpr int LEAF_D = 16;  // xs[4][2], telles1 {a,b,c,d}, telles2 {a,b,c,d}
+constexpr int SING_D = 56;  // xi_i[2], x_i[3], phi_i[8], hli[9], th[8][2], thp[8][2], pad
+constexpr int SING_I = 28;  // nsub, st[8], ngp_theta[8], off[9] (combo offsets), total, pad
+constexpr int FT_D = 10;    // cp (solid-angle part) and sum_b[3][3] of the free term
+
+struct DMesh {
+  int ne, ndn, ncp, ndof, nps, ptot, ns_max;
+  int ps_gln[16], ps_off[16];
+  int ps_gln_max;
+  // elements
+  const double* ex;
+  const double* cl;
+  const int* gln_far;
+  const double* ball;
+  const int* rev;
+  const int* edof;
+  // dofs
+  const int* dct;
+  const double* dcv;
+  // collocation points
+  const double* cpx;
+  const int* cp_dn;
+  const int* cp_kind;
+  const int* cp_elem;
+  const int* cp_kn;
+  const double* cp_xi;
+  const int* dn_cp;
+  // free-term inputs: incidences of SBIE collocation nodes (element, local node)
+  const int* inc_start;  // [ncp+1]
+  const int* inc_el;     // element*8 + local
+  const double* n_gn;    // [ne][8][3]
+  const double* tbp_gn;  // [ne][8][3]
+  double geo_tol;
+  // datasets
+  double* px;
+  double* pn;
+  double* pphi;
+  // classes and lists
+  uint8_t* cls;
+  int* reg_start;        // [ncp+1]
+  int* reg_pair;         // e | rule<<24
+  long long* reg_pt;     // [nreg+1] exclusive prefix of points
+  int* adp_start;        // [ncp+1]
+  int* adp_e;
+  int* adp_leaf;         // [nadp+1]
+  double* leaf;          // [nleaf][LEAF_D]
+  int* leaf_gln;
+  int* leaf_pair;        // adaptive pair index of each leaf
+  long long* leaf_pt;    // [nleaf+1]
+  int* sing_start;       // [ncp+1]
+  int* sing_e;
+  double* sing_d;        // [nsing][SING_D]
+  int* sing_i;           // [nsing][SING_I]
+  long long* sing_pt;    // [nsing+1]
+  double* ft;            // [ncp][FT_D]
+  int* ft_ok;            // [ncp] 1 ok, 0 invalid configuration
+  long long nreg, nadp, nleaf, nsing;
+};
+
+}  // namespace mfb

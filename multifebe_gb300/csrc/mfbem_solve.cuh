@@ -1,0 +1,484 @@
+// Dense solves behind mfbem_solve_{r,c}, mfbem_sweep_harela and
+// mfbem_solve_staela (included into mfbem_abi.cu).
+#pragma once
+
+// ---------------------------------------------------------------------------
+// GEMM dispatch for the trailing update A22 -= L21 U12 (plain library GEMM)
+// ---------------------------------------------------------------------------
+static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const double* A, int lda, long long sA,
+                              const double* B, int ldb, long long sB, double* C, int ldc, long long sC, int batch) {
+  const double al = -1.0, be = 1.0;
+  return cublasDgemmStridedBatched(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, lda, sA, B, ldb, sB, &be, C, ldc,
+                                   sC, batch);
+}
+static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const float* A, int lda, long long sA,
+                              const float* B, int ldb, long long sB, float* C, int ldc, long long sC, int batch) {
+  const float al = -1.0f, be = 1.0f;
+  return cublasSgemmStridedBatched(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, lda, sA, B, ldb, sB, &be, C, ldc,
+                                   sC, batch);
+}
+static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const double2* A, int lda, long long sA,
+                              const double2* B, int ldb, long long sB, double2* C, int ldc, long long sC, int batch) {
+  const cuDoubleComplex al = make_cuDoubleComplex(-1.0, 0.0), be = make_cuDoubleComplex(1.0, 0.0);
+  return cublasZgemmStridedBatched(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, (const cuDoubleComplex*)A, lda, sA,
+                                   (const cuDoubleComplex*)B, ldb, sB, &be, (cuDoubleComplex*)C, ldc, sC, batch);
+}
+static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const float2* A, int lda, long long sA,
+                              const float2* B, int ldb, long long sB, float2* C, int ldc, long long sC, int batch) {
+  const cuComplex al = make_cuComplex(-1.0f, 0.0f), be = make_cuComplex(1.0f, 0.0f);
+  return cublasCgemmStridedBatched(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, (const cuComplex*)A, lda, sA,
+                                   (const cuComplex*)B, ldb, sB, &be, (cuComplex*)C, ldc, sC, batch);
+}
+
+template <typename S> struct IsF64 { static const bool v = false; };
+template <> struct IsF64<double> { static const bool v = true; };
+template <> struct IsF64<double2> { static const bool v = true; };
+
+// Blocked right-looking getrf for a batch of n x n matrices (stride sA).
+template <typename S>
+static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA, int lda, int n, int batch,
+                         int* ipiv, int* info) {
+  // panel width: the L11 block of the TRSM lives in shared memory (<= 16 KB)
+  const int nb = 32;
+  CK(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
+  // FP64: spread the panel's rank-1 updates over many SMs (one SM's FP64 rate
+  // would serialise the panel); FP32: one CTA per matrix and panel.
+  const bool multi = IsF64<S>::v;
+  int G = std::max(1, std::min(64, (n / 128) * 2 / std::max(1, batch) + 1));
+  for (int k = 0; k < n; k += nb) {
+    const int kb = std::min(nb, n - k);
+    if (multi) {
+      for (int j = k; j < k + kb; ++j) {
+        k_pcol_pivot<S, 256><<<batch, 256, 0, st>>>(A, sA, lda, n, k, kb, j, ipiv, info);
+        int rows = n - j - 1;
+        int g = std::max(1, std::min(G, (rows + 255) / 256));
+        k_pcol_update<S, 256><<<dim3(g, batch), 256, 0, st>>>(A, sA, lda, n, k, kb, j);
+      }
+    } else {
+      k_panel_cta<S, 512><<<batch, 512, 0, st>>>(A, sA, lda, n, k, kb, ipiv, info);
+    }
+    int nout = n - kb;
+    if (nout > 0) k_laswp<S><<<dim3(nblk(nout, 128), batch), 128, 0, st>>>(A, sA, lda, n, k, kb, ipiv);
+    if (k + kb < n) {
+      int nc = n - k - kb;
+      k_trsm_llu<S><<<dim3(nblk(nc, 64), batch), 64, kb * kb * sizeof(S), st>>>(A, sA, lda, n, k, kb);
+      CKB(gemm_sb(hb, nc, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)(k + kb) * lda, lda, sA,
+                  A + (k + kb) + (size_t)(k + kb) * lda, lda, sA, batch));
+    }
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// getrs (no transpose) for one right-hand side per batch entry.
+// A: batch stride sA (0 = shared factors), ipiv stride sP, b stride sb.
+template <typename S>
+__global__ void k_rhs_swap2(S* b, long long sb, int n, const int* ipiv, long long sP, int nbatch) {
+  int bi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bi >= nbatch) return;
+  S* x = b + sb * bi;
+  const int* piv = ipiv + sP * bi;
+  for (int j = 0; j < n; ++j) {
+    int p = piv[j] - 1;
+    if (p != j) {
+      S t = x[j];
+      x[j] = x[p];
+      x[p] = t;
+    }
+  }
+}
+template <typename S>
+static int getrs_batched(cudaStream_t st, const S* A, long long sA, int lda, int n, const int* ipiv, long long sP,
+                         S* b, long long sb, int batch) {
+  const int TB = 128;
+  k_rhs_swap2<S><<<nblk(batch, 64), 64, 0, st>>>(b, sb, n, ipiv, sP, batch);
+  for (int r0 = 0; r0 < n; r0 += TB) {
+    int w = std::min(TB, n - r0);
+    k_trsv_diag<S, true><<<batch, TB, 0, st>>>(A, sA, lda, b, sb, r0, w);
+    if (r0 + w < n) k_trsv_update<S><<<dim3(nblk(n - r0 - w, 256), batch), 256, 0, st>>>(A, sA, lda, b, sb, r0, w, r0 + w, n);
+  }
+  int last = ((n - 1) / TB) * TB;
+  for (int r0 = last; r0 >= 0; r0 -= TB) {
+    int w = std::min(TB, n - r0);
+    k_trsv_diag<S, false><<<batch, TB, 0, st>>>(A, sA, lda, b, sb, r0, w);
+    if (r0 > 0) k_trsv_update<S><<<dim3(nblk(r0, 256), batch), 256, 0, st>>>(A, sA, lda, b, sb, r0, w, 0, r0);
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// mfbem_solve_{r,c}: LAPACK-semantics drop-in (host arrays in and out)
+// ---------------------------------------------------------------------------
+struct SolveCtx {
+  cudaStream_t st = nullptr;
+  cublasHandle_t hb = nullptr;
+  DevBuf A, b, ipiv, info;
+};
+static SolveCtx* g_solve = nullptr;
+static int solve_ctx(SolveCtx** out) {
+  if (!g_solve) {
+    int nd = 0;
+    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) return fail(MFBEM_ECUDA, "no CUDA device");
+    int rc = init_tables();
+    if (rc) return rc;
+    SolveCtx* c = new SolveCtx();
+    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    if (cublasCreate(&c->hb) != CUBLAS_STATUS_SUCCESS) return fail(MFBEM_ECUDA, "cublasCreate");
+    cublasSetStream(c->hb, c->st);
+    g_solve = c;
+  }
+  *out = g_solve;
+  return 0;
+}
+
+template <typename S>
+static int solve_dropin(int32_t n, double* A, int32_t* ipiv, int32_t n_rhs, double* b, int32_t factorize,
+                        int32_t scaling, int32_t condition, int32_t refine) {
+  g_err.clear();
+  if (n <= 0 || !A || !ipiv || !b || n_rhs < 0) return fail(MFBEM_EARG, "invalid argument");
+  if (scaling || condition || refine)
+    return fail(MFBEM_EUNSUPPORTED, "lse_scaling / lse_condition / lse_refine are not supported by this path");
+  SolveCtx* c;
+  int rc = solve_ctx(&c);
+  if (rc) return rc;
+  const size_t es = sizeof(S);
+  if ((rc = ensure(c->A, (size_t)n * n * es)) || (rc = ensure(c->b, (size_t)n * std::max(1, n_rhs) * es)) ||
+      (rc = ensure(c->ipiv, sizeof(int) * n)) || (rc = ensure(c->info, sizeof(int) * 4)))
+    return rc;
+  S* dA = (S*)c->A.p;
+  int* dp = (int*)c->ipiv.p;
+  int* di = (int*)c->info.p;
+  CK(cudaMemcpyAsync(dA, A, (size_t)n * n * es, cudaMemcpyHostToDevice, c->st));
+  int info = 0;
+  if (factorize) {
+    if ((rc = getrf_batched<S>(c->hb, c->st, dA, 0, n, n, 1, dp, di))) return rc;
+    CK(cudaMemcpyAsync(A, dA, (size_t)n * n * es, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(ipiv, dp, sizeof(int) * n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(&info, di, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    if (info > 0) return fail(info, "singular matrix: zero pivot U(info,info)");
+  } else {
+    CK(cudaMemcpyAsync(dp, ipiv, sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
+  }
+  if (n_rhs > 0) {
+    CK(cudaMemcpyAsync(c->b.p, b, (size_t)n * n_rhs * es, cudaMemcpyHostToDevice, c->st));
+    if ((rc = getrs_batched<S>(c->st, dA, 0, n, n, dp, 0, (S*)c->b.p, n, n_rhs))) return rc;
+    CK(cudaMemcpyAsync(b, c->b.p, (size_t)n * n_rhs * es, cudaMemcpyDeviceToHost, c->st));
+  }
+  CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+extern "C" int mfbem_solve_r(int32_t n, double* A, int32_t* ipiv, int32_t, double*, char*, double*, double*,
+                             int32_t n_rhs, double* b, int32_t factorize, int32_t scaling, int32_t condition,
+                             int32_t refine) {
+  return solve_dropin<double>(n, A, ipiv, n_rhs, b, factorize, scaling, condition, refine);
+}
+extern "C" int mfbem_solve_c(int32_t n, double* A, int32_t* ipiv, int32_t, double*, char*, double*, double*,
+                             int32_t n_rhs, double* b, int32_t factorize, int32_t scaling, int32_t condition,
+                             int32_t refine) {
+  return solve_dropin<double2>(n, A, ipiv, n_rhs, b, factorize, scaling, condition, refine);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision: FP32 factors + FP64 iterative refinement on the FP64 system.
+// ---------------------------------------------------------------------------
+template <typename SD, typename SF>
+__global__ void k_demote(const SD* a, SF* out, long long n);
+template <>
+__global__ void k_demote<double2, float2>(const double2* a, float2* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+template <>
+__global__ void k_demote<double, float>(const double* a, float* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)a[i];
+}
+__device__ __forceinline__ double amag(double a) { return fabs(a); }
+__device__ __forceinline__ double amag(double2 a) { return hypot(a.x, a.y); }
+__device__ __forceinline__ double amag(float a) { return fabsf(a); }
+__device__ __forceinline__ double amag(float2 a) { return hypotf(a.x, a.y); }
+
+// infinity norm of each batch's matrix: row sums of |a_ij|, then max
+template <typename S>
+__global__ void k_rowabs(const S* A, long long sA, int lda, int n, double* rows) {
+  int b = blockIdx.y;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const S* M = A + sA * b;
+  double s = 0.0;
+  for (int j = 0; j < n; ++j) s += amag(M[(size_t)j * lda + i]);
+  rows[(size_t)n * b + i] = s;
+}
+template <typename S>
+__global__ void k_vecmax(const S* v, long long sv, int n, double* out, int slot, int nslots) {
+  int b = blockIdx.x;
+  const S* x = v + sv * b;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, amag(x[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ double sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x / 32] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)blockDim.x / 32; ++w) m = fmax(m, sm[w]);
+    m = fmax(m, sm[0]);
+    out[(size_t)nslots * b + slot] = m;
+  }
+}
+// scaled demotion of the residual: r32 = r / ||r||
+template <typename SD, typename SF>
+__global__ void k_scale_demote(const SD* r, long long sr, SF* out, long long so, int n, const double* nrm,
+                               int nslots, int slot);
+template <>
+__global__ void k_scale_demote<double2, float2>(const double2* r, long long sr, float2* out, long long so, int n,
+                                                const double* nrm, int nslots, int slot) {
+  int b = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = nrm[(size_t)nslots * b + slot];
+  double inv = s > 0.0 ? 1.0 / s : 0.0;
+  double2 v = r[sr * b + i];
+  out[so * b + i] = make_float2((float)(v.x * inv), (float)(v.y * inv));
+}
+template <>
+__global__ void k_scale_demote<double, float>(const double* r, long long sr, float* out, long long so, int n,
+                                              const double* nrm, int nslots, int slot) {
+  int b = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = nrm[(size_t)nslots * b + slot];
+  double inv = s > 0.0 ? 1.0 / s : 0.0;
+  out[so * b + i] = (float)(r[sr * b + i] * inv);
+}
+// x += ||r|| d  (FP64 update with the FP32 correction)
+template <typename SD, typename SF>
+__global__ void k_update(SD* x, long long sx, const SF* d, long long sd, int n, const double* nrm, int nslots,
+                         int slot, const int* active);
+template <>
+__global__ void k_update<double2, float2>(double2* x, long long sx, const float2* d, long long sd, int n,
+                                          const double* nrm, int nslots, int slot, const int* active) {
+  int b = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !active[b]) return;
+  double s = nrm[(size_t)nslots * b + slot];
+  float2 v = d[sd * b + i];
+  double2 xo = x[sx * b + i];
+  x[sx * b + i] = make_double2(xo.x + s * (double)v.x, xo.y + s * (double)v.y);
+}
+template <>
+__global__ void k_update<double, float>(double* x, long long sx, const float* d, long long sd, int n,
+                                        const double* nrm, int nslots, int slot, const int* active) {
+  int b = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !active[b]) return;
+  double s = nrm[(size_t)nslots * b + slot];
+  x[sx * b + i] += s * (double)d[sd * b + i];
+}
+template <typename SD>
+__global__ void k_copy_vec(const SD* a, SD* b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = a[i];
+}
+
+static cublasStatus_t gemv_res(cublasHandle_t hb, int n, const double* A, int lda, long long sA, const double* x,
+                               long long sx, double* r, long long sr, int batch) {
+  const double al = -1.0, be = 1.0;
+  return cublasDgemvStridedBatched(hb, CUBLAS_OP_N, n, n, &al, A, lda, sA, x, 1, sx, &be, r, 1, sr, batch);
+}
+static cublasStatus_t gemv_res(cublasHandle_t hb, int n, const double2* A, int lda, long long sA, const double2* x,
+                               long long sx, double2* r, long long sr, int batch) {
+  const cuDoubleComplex al = make_cuDoubleComplex(-1.0, 0.0), be = make_cuDoubleComplex(1.0, 0.0);
+  return cublasZgemvStridedBatched(hb, CUBLAS_OP_N, n, n, &al, (const cuDoubleComplex*)A, lda, sA,
+                                   (const cuDoubleComplex*)x, 1, sx, &be, (cuDoubleComplex*)r, 1, sr, batch);
+}
+
+// Solve the batch of FP64 systems (A_f, b_f) in place of x. precision 0: FP64
+// LU; 1: FP32 LU + FP64 refinement. Work memory from the handle.
+template <typename SD, typename SF>
+static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD* x, int precision, double tol,
+                       mfbem_stats* stats) {
+  int rc;
+  cudaStream_t st = h->st;
+  const long long nn = (long long)n * n;
+  if ((rc = ensure(h->ipiv, sizeof(int) * (size_t)n * batch)) || (rc = ensure(h->info, sizeof(int) * (batch + 4))))
+    return rc;
+  int* ipiv = (int*)h->ipiv.p;
+  int* info = (int*)h->info.p;
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  cudaEventRecord(e0, st);
+  std::vector<int> hinfo(batch);
+  if (precision == 0) {
+    if ((rc = getrf_batched<SD>(h->blas, st, A, nn, n, n, batch, ipiv, info))) return rc;
+    cudaEventRecord(e1, st);
+    k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(b, x, (long long)n * batch);
+    if ((rc = getrs_batched<SD>(st, A, nn, n, n, ipiv, n, x, n, batch))) return rc;
+    cudaEventRecord(e2, st);
+    CK(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    stats->refinement_iterations = 0;
+  } else {
+    // FP32 copy of A, factor
+    if ((rc = ensure(h->A32, sizeof(SF) * nn * batch)) || (rc = ensure(h->r, sizeof(SD) * (size_t)n * batch)) ||
+        (rc = ensure(h->work, sizeof(SF) * (size_t)n * batch + sizeof(double) * ((size_t)n * batch + 8 * batch) + 4 * batch)))
+      return rc;
+    SF* A32 = (SF*)h->A32.p;
+    SD* r = (SD*)h->r.p;
+    SF* d32 = (SF*)h->work.p;
+    double* nrm = (double*)((char*)h->work.p + sizeof(SF) * (size_t)n * batch);  // [batch][4]: |r|,|x|,|b|,|A|
+    double* rows = nrm + 8 * batch;
+    int* active = (int*)(rows + (size_t)n * batch);
+    k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, A32, nn * batch);
+    k_rowabs<SD><<<dim3(nblk(n, 128), batch), 128, 0, st>>>(A, nn, n, n, rows);
+    k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, nrm, 3, 8);
+    k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, nrm, 2, 8);
+    if ((rc = getrf_batched<SF>(h->blas, st, A32, nn, n, n, batch, ipiv, info))) return rc;
+    cudaEventRecord(e1, st);
+    // x = 0, r = b, then iterate x += LU^{-1} r
+    CK(cudaMemsetAsync(x, 0, sizeof(SD) * (size_t)n * batch, st));
+    std::vector<int> hact(batch, 1);
+    std::vector<double> hn(8 * batch);
+    int it = 0;
+    double maxbe = 0.0;
+    const int maxit = 30;
+    for (; it <= maxit; ++it) {
+      k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(b, r, (long long)n * batch);
+      if (it > 0) CKB(gemv_res(h->blas, n, A, n, nn, x, n, r, n, batch));
+      k_vecmax<SD><<<batch, 256, 0, st>>>(r, n, n, nrm, 0, 8);
+      k_vecmax<SD><<<batch, 256, 0, st>>>(x, n, n, nrm, 1, 8);
+      CK(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 8 * batch, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      bool any = false;
+      maxbe = 0.0;
+      for (int bi = 0; bi < batch; ++bi) {
+        double be = hn[8 * bi + 0] / (hn[8 * bi + 3] * hn[8 * bi + 1] + hn[8 * bi + 2]);
+        if (it == 0) be = 1.0;
+        maxbe = std::max(maxbe, be);
+        hact[bi] = (be > tol) ? 1 : 0;
+        any = any || hact[bi];
+      }
+      if (!any || it == maxit) break;
+      CK(cudaMemcpyAsync(active, hact.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, st));
+      k_scale_demote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(r, n, d32, n, n, nrm, 8, 0);
+      if ((rc = getrs_batched<SF>(st, A32, nn, n, n, ipiv, n, d32, n, batch))) return rc;
+      k_update<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(x, n, d32, n, n, nrm, 8, 0, active);
+    }
+    cudaEventRecord(e2, st);
+    CK(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    stats->refinement_iterations += it;
+    stats->max_backward_error = std::max(stats->max_backward_error, maxbe);
+    if (maxbe > tol) {
+      cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+      return fail(MFBEM_ENOCONV, "iterative refinement did not reach the requested backward error");
+    }
+  }
+  float ms1 = 0, ms2 = 0;
+  cudaEventElapsedTime(&ms1, e0, e1);
+  cudaEventElapsedTime(&ms2, e1, e2);
+  stats->ms_factor += ms1;
+  stats->ms_solve += ms2;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  for (int bi = 0; bi < batch; ++bi)
+    if (hinfo[bi] > 0) return fail(hinfo[bi], "singular matrix: zero pivot");
+  return 0;
+}
+
+extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
+                                  const double nu[2], int32_t n_freq, const double* omega, int32_t precision,
+                                  double rel_tol, double* x_out, int32_t flags, mfbem_stats* stats) {
+  g_err.clear();
+  if (!h || !lambda || !mu || !nu || !omega || !x_out || n_freq < 1) return fail(MFBEM_EARG, "invalid argument");
+  if (precision != 0 && precision != 1) return fail(MFBEM_EARG, "precision must be 0 or 1");
+  const int n = h->ndof;
+  const long long nn = (long long)n * n;
+  int rc;
+  mfbem_stats s = h->stats;
+  s.refinement_iterations = 0;
+  s.max_backward_error = 0.0;
+  s.ms_factor = s.ms_solve = 0.0;
+  if ((rc = ensure(h->A, sizeof(double2) * nn * n_freq)) || (rc = ensure(h->b, sizeof(double2) * (size_t)n * n_freq)) ||
+      (rc = ensure(h->x, sizeof(double2) * (size_t)n * n_freq)) ||
+      (rc = ensure(h->par, (sizeof(HarParD) + 6 * sizeof(double)) * n_freq + 2 * sizeof(double) * n_freq)))
+    return rc;
+  HarParD* dpar = (HarParD*)h->par.p;
+  double* dq = (double*)(dpar + n_freq);
+  double* dnu = dq + 6 * n_freq;
+  std::vector<double> q(6 * (size_t)n_freq), nuv(2 * (size_t)n_freq);
+  for (int f = 0; f < n_freq; ++f) {
+    double v[6] = {lambda[0], lambda[1], mu[0], mu[1], rho, omega[f]};
+    for (int j = 0; j < 6; ++j) q[6 * f + j] = v[j];
+    nuv[2 * f] = nu[0];
+    nuv[2 * f + 1] = nu[1];
+  }
+  CK(cudaMemcpyAsync(dq, q.data(), sizeof(double) * q.size(), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(dnu, nuv.data(), sizeof(double) * nuv.size(), cudaMemcpyHostToDevice, h->st));
+  k_harpar<<<nblk(n_freq, 32), 32, 0, h->st>>>(dq, n_freq, dpar);
+  double2* A = (double2*)h->A.p;
+  double2* b = (double2*)h->b.p;
+  double2* x = (flags & MFBEM_DEVICE_PTRS) ? (double2*)x_out : (double2*)h->x.p;
+  CK(cudaMemsetAsync(A, 0, sizeof(double2) * nn * n_freq, h->st));
+  CK(cudaMemsetAsync(b, 0, sizeof(double2) * (size_t)n * n_freq, h->st));
+  cudaEvent_t a0, a1;
+  cudaEventCreate(&a0);
+  cudaEventCreate(&a1);
+  cudaEventRecord(a0, h->st);
+  PolHarmonic pol;
+  pol.p = dpar;
+  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n))) return rc;
+  cudaEventRecord(a1, h->st);
+  if ((rc = check_err(h))) return rc;
+  float ams = 0;
+  cudaEventElapsedTime(&ams, a0, a1);
+  cudaEventDestroy(a0);
+  cudaEventDestroy(a1);
+  s.ms_assemble = ams;
+  rc = solve_batch<double2, float2>(h, A, n, n_freq, b, x, precision, rel_tol, &s);
+  if (rc && rc != MFBEM_ENOCONV) return rc;
+  if (!(flags & MFBEM_DEVICE_PTRS)) {
+    CK(cudaMemcpyAsync(x_out, x, sizeof(double2) * (size_t)n * n_freq, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  h->stats = s;
+  if (stats) *stats = s;
+  return rc;
+}
+
+extern "C" int mfbem_solve_staela(mfbem_handle* h, double mu, double nu, int32_t precision, double rel_tol,
+                                  double* x_out, int32_t flags, mfbem_stats* stats) {
+  g_err.clear();
+  if (!h || !x_out) return fail(MFBEM_EARG, "invalid argument");
+  const int n = h->ndof;
+  const long long nn = (long long)n * n;
+  int rc;
+  mfbem_stats s = h->stats;
+  s.refinement_iterations = 0;
+  s.max_backward_error = 0.0;
+  s.ms_factor = s.ms_solve = 0.0;
+  if ((rc = ensure(h->A, sizeof(double) * nn)) || (rc = ensure(h->b, sizeof(double) * n)) ||
+      (rc = ensure(h->x, sizeof(double) * n)) || (rc = ensure(h->nu, 2 * sizeof(double))))
+    return rc;
+  double nuv[2] = {nu, 0.0};
+  CK(cudaMemcpyAsync(h->nu.p, nuv, sizeof(nuv), cudaMemcpyHostToDevice, h->st));
+  double* A = (double*)h->A.p;
+  double* b = (double*)h->b.p;
+  double* x = (flags & MFBEM_DEVICE_PTRS) ? x_out : (double*)h->x.p;
+  CK(cudaMemsetAsync(A, 0, sizeof(double) * nn, h->st));
+  CK(cudaMemsetAsync(b, 0, sizeof(double) * n, h->st));
+  PolStatic pol;
+  pol.k = staela_params(mu, nu);
+  if ((rc = launch_assembly(h, pol, (const double*)h->nu.p, 1, A, n, 0, b, 0))) return rc;
+  if ((rc = check_err(h))) return rc;
+  rc = solve_batch<double, float>(h, A, n, 1, b, x, precision, rel_tol, &s);
+  if (rc && rc != MFBEM_ENOCONV) return rc;
+  if (!(flags & MFBEM_DEVICE_PTRS)) {
+    CK(cudaMemcpyAsync(x_out, x, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  h->stats = s;
+  if (stats) *stats = s;
+  return rc;
+}
