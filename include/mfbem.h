@@ -104,6 +104,10 @@ typedef struct mfbem_stats {
   int32_t refinement_iterations; /* sweep: total over frequencies */
   double max_backward_error;     /* sweep: max over frequencies of ||b-Ax||/(||A|| ||x||) */
   double ms_assemble, ms_factor, ms_solve;
+  /* device time of the assembly kernels of the last call (CUDA events on the
+     library's stream): regular, adaptive, singular pairs and free terms */
+  double ms_regular, ms_adaptive, ms_singular, ms_free;
+  int64_t kernel_launches;       /* this library's kernels launched by the call */
 } mfbem_stats;
 
 /* mesh lifetime */

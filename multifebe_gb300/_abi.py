@@ -55,6 +55,8 @@ class Stats(ctypes.Structure):
         ("points_regular", ctypes.c_int64), ("points_adaptive", ctypes.c_int64), ("points_singular", ctypes.c_int64),
         ("adaptive_leaves", c_int32), ("refinement_iterations", c_int32), ("max_backward_error", c_double),
         ("ms_assemble", c_double), ("ms_factor", c_double), ("ms_solve", c_double),
+        ("ms_regular", c_double), ("ms_adaptive", c_double), ("ms_singular", c_double), ("ms_free", c_double),
+        ("kernel_launches", ctypes.c_int64),
     ]
 
     def as_dict(self):

@@ -23,6 +23,8 @@
 
 namespace mfb {
 static thread_local std::string g_err;
+// kernels of this library launched so far (reported per call in mfbem_stats)
+static long long g_launches = 0;
 void set_error(const std::string& s) { g_err = s; }
 int fail(int code, const std::string& s) {
   g_err = s;
@@ -262,8 +264,8 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
     return rc;
   }
   auto t0 = std::chrono::steady_clock::now();
-  k_datasets<<<ne, 128>>>(m);
-  k_classify<<<std::min(nblk((long long)ncp * ne, 256), 152u * 16u), 256>>>(m, h->d_qs);
+  k_datasets<<<ne, 128>>>(m); ++g_launches;
+  k_classify<<<std::min(nblk((long long)ncp * ne, 256), 152u * 16u), 256>>>(m, h->d_qs); ++g_launches;
   // counts and list offsets
   int *nreg, *nadp, *nsing;
   long long* npts;
@@ -277,11 +279,11 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   }
   long long* pts_base;
   if ((rc = dalloc(h, (void**)&pts_base, sizeof(long long) * (ncp + 1)))) { mfbem_mesh_release(h); return rc; }
-  k_count<<<nblk(ncp, 8), 256>>>(m, nreg, nadp, nsing, npts);
-  k_scan<int, int><<<1, 1024>>>(nreg, m.reg_start, ncp);
-  k_scan<int, int><<<1, 1024>>>(nadp, m.adp_start, ncp);
-  k_scan<int, int><<<1, 1024>>>(nsing, m.sing_start, ncp);
-  k_scan<long long, long long><<<1, 1024>>>(npts, pts_base, ncp);
+  k_count<<<nblk(ncp, 8), 256>>>(m, nreg, nadp, nsing, npts); ++g_launches;
+  k_scan<int, int><<<1, 1024>>>(nreg, m.reg_start, ncp); ++g_launches;
+  k_scan<int, int><<<1, 1024>>>(nadp, m.adp_start, ncp); ++g_launches;
+  k_scan<int, int><<<1, 1024>>>(nsing, m.sing_start, ncp); ++g_launches;
+  k_scan<long long, long long><<<1, 1024>>>(npts, pts_base, ncp); ++g_launches;
   CK(cudaGetLastError());
   int tot[3];
   long long totp;
@@ -302,7 +304,7 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
     mfbem_mesh_release(h);
     return rc;
   }
-  k_fill<<<nblk(ncp, 8), 256>>>(m, pts_base, adp_cp, sing_cp);
+  k_fill<<<nblk(ncp, 8), 256>>>(m, pts_base, adp_cp, sing_cp); ++g_launches;
   CK(cudaMemcpy(m.reg_pt + m.nreg, &totp, sizeof(long long), cudaMemcpyHostToDevice));
   h->pts_reg = totp;
   // adaptive subdivision leaves
@@ -312,8 +314,8 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
     mfbem_mesh_release(h);
     return rc;
   }
-  if (m.nadp > 0) k_adp_count<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, adp_cp, nl);
-  k_scan<int, int><<<1, 1024>>>(nl, m.adp_leaf, (int)m.nadp);
+  if (m.nadp > 0) k_adp_count<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, adp_cp, nl); ++g_launches;
+  k_scan<int, int><<<1, 1024>>>(nl, m.adp_leaf, (int)m.nadp); ++g_launches;
   int nleaf = 0;
   CK(cudaMemcpy(&nleaf, m.adp_leaf + m.nadp, sizeof(int), cudaMemcpyDeviceToHost));
   m.nleaf = nleaf;
@@ -326,9 +328,9 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
     mfbem_mesh_release(h);
     return rc;
   }
-  if (m.nadp > 0) k_adp_fill<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, adp_cp);
-  if (m.nleaf > 0) k_leaf_points<<<nblk(m.nleaf, 256), 256>>>(m, lpts);
-  k_scan<long long, long long><<<1, 1024>>>(lpts, m.leaf_pt, (int)m.nleaf);
+  if (m.nadp > 0) k_adp_fill<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, adp_cp); ++g_launches;
+  if (m.nleaf > 0) k_leaf_points<<<nblk(m.nleaf, 256), 256>>>(m, lpts); ++g_launches;
+  k_scan<long long, long long><<<1, 1024>>>(lpts, m.leaf_pt, (int)m.nleaf); ++g_launches;
   CK(cudaMemcpy(&h->pts_adp, m.leaf_pt + m.nleaf, sizeof(long long), cudaMemcpyDeviceToHost));
   // singular pairs
   long long* spts;
@@ -339,10 +341,10 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
     mfbem_mesh_release(h);
     return rc;
   }
-  if (m.nsing > 0) k_sing_prep<<<nblk(m.nsing, 64), 64>>>(m, h->d_q15, sing_cp, spts);
-  k_scan<long long, long long><<<1, 1024>>>(spts, m.sing_pt, (int)m.nsing);
+  if (m.nsing > 0) k_sing_prep<<<nblk(m.nsing, 64), 64>>>(m, h->d_q15, sing_cp, spts); ++g_launches;
+  k_scan<long long, long long><<<1, 1024>>>(spts, m.sing_pt, (int)m.nsing); ++g_launches;
   CK(cudaMemcpy(&h->pts_sing, m.sing_pt + m.nsing, sizeof(long long), cudaMemcpyDeviceToHost));
-  k_ft_prep<<<nblk(ncp, 128), 128>>>(m);
+  k_ft_prep<<<nblk(ncp, 128), 128>>>(m); ++g_launches;
   CK(cudaGetLastError());
   CK(cudaDeviceSynchronize());
   auto t1 = std::chrono::steady_clock::now();
@@ -389,19 +391,47 @@ __global__ void k_harpar(const double* in /*nf x {lre,lim,mre,mim,rho,omega}*/, 
   out[f] = harela_params(mk(q[0], q[1]), mk(q[2], q[3]), q[4], q[5]);
 }
 
+// Assembly kernels in a fixed order (regular, adaptive, singular, free terms);
+// per-kernel device times are recorded with events on the library's stream.
+struct AsmTimes {
+  cudaEvent_t ev[5];
+  bool live = false;
+  AsmTimes() {
+    for (auto& e : ev) cudaEventCreate(&e);
+    live = true;
+  }
+  ~AsmTimes() {
+    if (live)
+      for (auto& e : ev) cudaEventDestroy(e);
+  }
+  void read(mfbem_stats* s) {
+    float t[4] = {0, 0, 0, 0};
+    for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]);
+    s->ms_regular = t[0];
+    s->ms_adaptive = t[1];
+    s->ms_singular = t[2];
+    s->ms_free = t[3];
+  }
+};
+
 template <class POL>
 static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, int nf, double* A, size_t lda,
-                           size_t astride, double* b, size_t bstride) {
+                           size_t astride, double* b, size_t bstride, AsmTimes* tm = nullptr) {
   const DMesh& m = h->m;
   constexpr int WPB = 4;
   long long nw = (long long)m.ndn * nf;
   unsigned g = nblk(nw, WPB);
   CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
-  if (m.nreg > 0) k_reg<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
-  if (m.nadp > 0) k_adp<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
+  if (tm) cudaEventRecord(tm->ev[0], h->st);
+  if (m.nreg > 0) { k_reg<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride); ++g_launches; }
+  if (tm) cudaEventRecord(tm->ev[1], h->st);
+  if (m.nadp > 0) { k_adp<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride); ++g_launches; }
+  if (tm) cudaEventRecord(tm->ev[2], h->st);
   // the singular kernel keeps two combo sets per point: 2 warps per block
-  if (m.nsing > 0) k_sing<POL, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
-  k_free<POL><<<nblk(nw, 128), 128, 0, h->st>>>(m, pol, d_nu, nf, A, lda, astride, b, bstride, h->d_err);
+  if (m.nsing > 0) { k_sing<POL, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride); ++g_launches; }
+  if (tm) cudaEventRecord(tm->ev[3], h->st);
+  k_free<POL><<<nblk(nw, 128), 128, 0, h->st>>>(m, pol, d_nu, nf, A, lda, astride, b, bstride, h->d_err); ++g_launches;
+  if (tm) cudaEventRecord(tm->ev[4], h->st);
   CK(cudaGetLastError());
   return 0;
 }
@@ -458,8 +488,10 @@ static int assemble_common(mfbem_handle* h, const void* polp, const double* nu_h
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, h->st);
-  if (CPLX) rc = launch_assembly(h, *(const PolHarmonic*)polp, (const double*)h->nu.p, 1, dA, dlda, 0, db, 0);
-  else rc = launch_assembly(h, *(const PolStatic*)polp, (const double*)h->nu.p, 1, dA, dlda, 0, db, 0);
+  AsmTimes tm;
+  long long l0 = g_launches;
+  if (CPLX) rc = launch_assembly(h, *(const PolHarmonic*)polp, (const double*)h->nu.p, 1, dA, dlda, 0, db, 0, &tm);
+  else rc = launch_assembly(h, *(const PolStatic*)polp, (const double*)h->nu.p, 1, dA, dlda, 0, db, 0, &tm);
   cudaEventRecord(e1, h->st);
   if (rc) return rc;
   if (!dev) {
@@ -472,6 +504,8 @@ static int assemble_common(mfbem_handle* h, const void* polp, const double* nu_h
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   h->stats.ms_assemble = ms;
+  tm.read(&h->stats);
+  h->stats.kernel_launches = g_launches - l0;
   return rc;
 }
 
@@ -495,7 +529,7 @@ extern "C" int mfbem_assemble_harela(mfbem_handle* h, const double lambda[2], co
   double q[6] = {lambda[0], lambda[1], mu[0], mu[1], rho, omega};
   double* dq = (double*)((char*)h->par.p + sizeof(HarParD));
   CK(cudaMemcpyAsync(dq, q, sizeof(q), cudaMemcpyHostToDevice, h->st));
-  k_harpar<<<1, 32, 0, h->st>>>(dq, 1, (HarParD*)h->par.p);
+  k_harpar<<<1, 32, 0, h->st>>>(dq, 1, (HarParD*)h->par.p); ++g_launches;
   PolHarmonic pol;
   pol.p = (const HarParD*)h->par.p;
   return assemble_common<true>(h, &pol, nu, A, lda, b, flags);

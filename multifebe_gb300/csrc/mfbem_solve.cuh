@@ -49,19 +49,19 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
     const int kb = std::min(nb, n - k);
     if (multi) {
       for (int j = k; j < k + kb; ++j) {
-        k_pcol_pivot<S, 256><<<batch, 256, 0, st>>>(A, sA, lda, n, k, kb, j, ipiv, info);
+        k_pcol_pivot<S, 256><<<batch, 256, 0, st>>>(A, sA, lda, n, k, kb, j, ipiv, info); ++g_launches;
         int rows = n - j - 1;
         int g = std::max(1, std::min(G, (rows + 255) / 256));
-        k_pcol_update<S, 256><<<dim3(g, batch), 256, 0, st>>>(A, sA, lda, n, k, kb, j);
+        k_pcol_update<S, 256><<<dim3(g, batch), 256, 0, st>>>(A, sA, lda, n, k, kb, j); ++g_launches;
       }
     } else {
-      k_panel_cta<S, 512><<<batch, 512, 0, st>>>(A, sA, lda, n, k, kb, ipiv, info);
+      k_panel_cta<S, 512><<<batch, 512, 0, st>>>(A, sA, lda, n, k, kb, ipiv, info); ++g_launches;
     }
     int nout = n - kb;
-    if (nout > 0) k_laswp<S><<<dim3(nblk(nout, 128), batch), 128, 0, st>>>(A, sA, lda, n, k, kb, ipiv);
+    if (nout > 0) k_laswp<S><<<dim3(nblk(nout, 128), batch), 128, 0, st>>>(A, sA, lda, n, k, kb, ipiv); ++g_launches;
     if (k + kb < n) {
       int nc = n - k - kb;
-      k_trsm_llu<S><<<dim3(nblk(nc, 64), batch), 64, kb * kb * sizeof(S), st>>>(A, sA, lda, n, k, kb);
+      k_trsm_llu<S><<<dim3(nblk(nc, 64), batch), 64, kb * kb * sizeof(S), st>>>(A, sA, lda, n, k, kb); ++g_launches;
       CKB(gemm_sb(hb, nc, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)(k + kb) * lda, lda, sA,
                   A + (k + kb) + (size_t)(k + kb) * lda, lda, sA, batch));
     }
@@ -91,17 +91,17 @@ template <typename S>
 static int getrs_batched(cudaStream_t st, const S* A, long long sA, int lda, int n, const int* ipiv, long long sP,
                          S* b, long long sb, int batch) {
   const int TB = 128;
-  k_rhs_swap2<S><<<nblk(batch, 64), 64, 0, st>>>(b, sb, n, ipiv, sP, batch);
+  k_rhs_swap2<S><<<nblk(batch, 64), 64, 0, st>>>(b, sb, n, ipiv, sP, batch); ++g_launches;
   for (int r0 = 0; r0 < n; r0 += TB) {
     int w = std::min(TB, n - r0);
-    k_trsv_diag<S, true><<<batch, TB, 0, st>>>(A, sA, lda, b, sb, r0, w);
-    if (r0 + w < n) k_trsv_update<S><<<dim3(nblk(n - r0 - w, 256), batch), 256, 0, st>>>(A, sA, lda, b, sb, r0, w, r0 + w, n);
+    k_trsv_diag<S, true><<<batch, TB, 0, st>>>(A, sA, lda, b, sb, r0, w); ++g_launches;
+    if (r0 + w < n) k_trsv_update<S><<<dim3(nblk(n - r0 - w, 256), batch), 256, 0, st>>>(A, sA, lda, b, sb, r0, w, r0 + w, n); ++g_launches;
   }
   int last = ((n - 1) / TB) * TB;
   for (int r0 = last; r0 >= 0; r0 -= TB) {
     int w = std::min(TB, n - r0);
-    k_trsv_diag<S, false><<<batch, TB, 0, st>>>(A, sA, lda, b, sb, r0, w);
-    if (r0 > 0) k_trsv_update<S><<<dim3(nblk(r0, 256), batch), 256, 0, st>>>(A, sA, lda, b, sb, r0, w, 0, r0);
+    k_trsv_diag<S, false><<<batch, TB, 0, st>>>(A, sA, lda, b, sb, r0, w); ++g_launches;
+    if (r0 > 0) k_trsv_update<S><<<dim3(nblk(r0, 256), batch), 256, 0, st>>>(A, sA, lda, b, sb, r0, w, 0, r0); ++g_launches;
   }
   CK(cudaGetLastError());
   return 0;
@@ -312,7 +312,7 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
   if (precision == 0) {
     if ((rc = getrf_batched<SD>(h->blas, st, A, nn, n, n, batch, ipiv, info))) return rc;
     cudaEventRecord(e1, st);
-    k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(b, x, (long long)n * batch);
+    k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(b, x, (long long)n * batch); ++g_launches;
     if ((rc = getrs_batched<SD>(st, A, nn, n, n, ipiv, n, x, n, batch))) return rc;
     cudaEventRecord(e2, st);
     CK(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
@@ -329,10 +329,10 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     double* nrm = (double*)((char*)h->work.p + sizeof(SF) * (size_t)n * batch);  // [batch][4]: |r|,|x|,|b|,|A|
     double* rows = nrm + 8 * batch;
     int* active = (int*)(rows + (size_t)n * batch);
-    k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, A32, nn * batch);
-    k_rowabs<SD><<<dim3(nblk(n, 128), batch), 128, 0, st>>>(A, nn, n, n, rows);
-    k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, nrm, 3, 8);
-    k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, nrm, 2, 8);
+    k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, A32, nn * batch); ++g_launches;
+    k_rowabs<SD><<<dim3(nblk(n, 128), batch), 128, 0, st>>>(A, nn, n, n, rows); ++g_launches;
+    k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, nrm, 3, 8); ++g_launches;
+    k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, nrm, 2, 8); ++g_launches;
     if ((rc = getrf_batched<SF>(h->blas, st, A32, nn, n, n, batch, ipiv, info))) return rc;
     cudaEventRecord(e1, st);
     // x = 0, r = b, then iterate x += LU^{-1} r
@@ -343,10 +343,10 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     double maxbe = 0.0;
     const int maxit = 30;
     for (; it <= maxit; ++it) {
-      k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(b, r, (long long)n * batch);
+      k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(b, r, (long long)n * batch); ++g_launches;
       if (it > 0) CKB(gemv_res(h->blas, n, A, n, nn, x, n, r, n, batch));
-      k_vecmax<SD><<<batch, 256, 0, st>>>(r, n, n, nrm, 0, 8);
-      k_vecmax<SD><<<batch, 256, 0, st>>>(x, n, n, nrm, 1, 8);
+      k_vecmax<SD><<<batch, 256, 0, st>>>(r, n, n, nrm, 0, 8); ++g_launches;
+      k_vecmax<SD><<<batch, 256, 0, st>>>(x, n, n, nrm, 1, 8); ++g_launches;
       CK(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 8 * batch, cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
       bool any = false;
@@ -360,9 +360,9 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
       }
       if (!any || it == maxit) break;
       CK(cudaMemcpyAsync(active, hact.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, st));
-      k_scale_demote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(r, n, d32, n, n, nrm, 8, 0);
+      k_scale_demote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(r, n, d32, n, n, nrm, 8, 0); ++g_launches;
       if ((rc = getrs_batched<SF>(st, A32, nn, n, n, ipiv, n, d32, n, batch))) return rc;
-      k_update<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(x, n, d32, n, n, nrm, 8, 0, active);
+      k_update<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(x, n, d32, n, n, nrm, 8, 0, active); ++g_launches;
     }
     cudaEventRecord(e2, st);
     CK(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
@@ -416,7 +416,7 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   }
   CK(cudaMemcpyAsync(dq, q.data(), sizeof(double) * q.size(), cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(dnu, nuv.data(), sizeof(double) * nuv.size(), cudaMemcpyHostToDevice, h->st));
-  k_harpar<<<nblk(n_freq, 32), 32, 0, h->st>>>(dq, n_freq, dpar);
+  k_harpar<<<nblk(n_freq, 32), 32, 0, h->st>>>(dq, n_freq, dpar); ++g_launches;
   double2* A = (double2*)h->A.p;
   double2* b = (double2*)h->b.p;
   double2* x = (flags & MFBEM_DEVICE_PTRS) ? (double2*)x_out : (double2*)h->x.p;
@@ -428,7 +428,9 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   cudaEventRecord(a0, h->st);
   PolHarmonic pol;
   pol.p = dpar;
-  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n))) return rc;
+  AsmTimes tm;
+  long long l0 = g_launches;
+  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n, &tm))) return rc;
   cudaEventRecord(a1, h->st);
   if ((rc = check_err(h))) return rc;
   float ams = 0;
@@ -436,7 +438,9 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   cudaEventDestroy(a0);
   cudaEventDestroy(a1);
   s.ms_assemble = ams;
+  tm.read(&s);
   rc = solve_batch<double2, float2>(h, A, n, n_freq, b, x, precision, rel_tol, &s);
+  s.kernel_launches = g_launches - l0;
   if (rc && rc != MFBEM_ENOCONV) return rc;
   if (!(flags & MFBEM_DEVICE_PTRS)) {
     CK(cudaMemcpyAsync(x_out, x, sizeof(double2) * (size_t)n * n_freq, cudaMemcpyDeviceToHost, h->st));
@@ -470,9 +474,13 @@ extern "C" int mfbem_solve_staela(mfbem_handle* h, double mu, double nu, int32_t
   CK(cudaMemsetAsync(b, 0, sizeof(double) * n, h->st));
   PolStatic pol;
   pol.k = staela_params(mu, nu);
-  if ((rc = launch_assembly(h, pol, (const double*)h->nu.p, 1, A, n, 0, b, 0))) return rc;
+  AsmTimes tm;
+  long long l0 = g_launches;
+  if ((rc = launch_assembly(h, pol, (const double*)h->nu.p, 1, A, n, 0, b, 0, &tm))) return rc;
   if ((rc = check_err(h))) return rc;
+  tm.read(&s);
   rc = solve_batch<double, float>(h, A, n, 1, b, x, precision, rel_tol, &s);
+  s.kernel_launches = g_launches - l0;
   if (rc && rc != MFBEM_ENOCONV) return rc;
   if (!(flags & MFBEM_DEVICE_PTRS)) {
     CK(cudaMemcpyAsync(x_out, x, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));

@@ -1,0 +1,153 @@
+"""GPU path against the CPU oracle, through the C-ABI (mfbem_* entry points).
+
+Tolerances (max-norm relative):
+  assembled A, b     <= 1e-11 (the near-singular integrands amplify FP64
+                     rounding differences between an FMA device and the oracle)
+  solutions          <= 1e-10 on well-conditioned systems; <= cond(A) * 1e-12
+                     in general (the FP64 method's own sensitivity)
+  pair classes       identical counts of regular / adaptive / singular pairs,
+                     adaptive leaves and quadrature points
+"""
+import numpy as np
+import pytest
+
+from multifebe_gb300 import meshgen as M, BemRegion, solve_lse, MfbemError
+from multifebe_gb300 import _abi
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+STATIC = [("cube4", lambda: M.cube_clamped_top_traction(4)), ("kat2", lambda: M.cube_confined_kat(2))]
+HARMONIC = [("cube4", lambda: M.cube_clamped_top_traction(4)), ("patch8", lambda: M.surface_patch(10.0, 8, 1.0)),
+            ("slab4", lambda: M.slab(4, 1))]
+
+
+@pytest.mark.parametrize("name,mk", STATIC, ids=[s[0] for s in STATIC])
+def test_assemble_staela_matches_oracle(oracle, name, mk):
+    d = mk()
+    R = BemRegion(d)
+    P = oracle.Problem(d)
+    mat = M.elastic(1.0, 0.25)
+    A, b = R.build_lse_staela(mat["mu"], mat["nu"])
+    Ao, bo = P.assemble_staela(mat["mu"], mat["nu"])
+    st = R.stats()
+    assert (st["pairs_regular"], st["pairs_adaptive"], st["pairs_singular"]) == tuple(P.stats[:3])
+    assert st["adaptive_leaves"] == P.stats[3] and st["points_adaptive"] == P.stats[4]
+    assert rel(A, Ao) < 1e-11 and rel(b, bo) < 1e-11
+    # accumulate semantics: a second call adds the same contribution
+    A2, b2 = R.build_lse_staela(mat["mu"], mat["nu"], A.copy(order="F"), b.copy())
+    assert rel(A2, 2 * A) < 1e-15 and rel(b2, 2 * b) < 1e-15
+    R.close()
+
+
+@pytest.mark.parametrize("name,mk", HARMONIC, ids=[s[0] for s in HARMONIC])
+def test_assemble_harela_matches_oracle(oracle, name, mk):
+    d = mk()
+    R = BemRegion(d)
+    P = oracle.Problem(d)
+    mat = M.viscoelastic(1.0, 0.3, 1.0, 0.05)
+    for a0 in (0.2, 1.5):
+        om = float(M.omega_from_a0(a0, mat))
+        A, b = R.build_lse_harela(mat, om)
+        Ao, bo = P.assemble_harela(mat, om)
+        assert rel(A, Ao) < 1e-11, (a0, rel(A, Ao))
+        assert rel(b, bo) < 1e-11
+        st = R.stats()
+        assert (st["pairs_regular"], st["pairs_adaptive"], st["pairs_singular"]) == tuple(P.stats[:3])
+    R.close()
+
+
+def test_assembly_is_deterministic():
+    d = M.slab(4, 1)
+    R = BemRegion(d)
+    mat = M.viscoelastic(1.0, 0.3, 1.0, 0.05)
+    A1, b1 = R.build_lse_harela(mat, 0.7)
+    A2, b2 = R.build_lse_harela(mat, 0.7)
+    assert np.array_equal(A1, A2) and np.array_equal(b1, b2)
+    R.close()
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_solve_lse_lapack_semantics(cplx):
+    """mfbem_solve_{r,c}: A overwritten by getrf's LU, 1-based ipiv, b by x;
+    factorize=0 reuses the factors."""
+    import scipy.linalg as sl
+    rng = np.random.default_rng(3)
+    n = 300
+    A = rng.standard_normal((n, n)) + (1j * rng.standard_normal((n, n)) if cplx else 0)
+    A = np.asfortranarray(A)
+    b = np.asfortranarray(rng.standard_normal((n, 2)) + (1j * rng.standard_normal((n, 2)) if cplx else 0))
+    lu, piv = sl.lu_factor(A)
+    xr = sl.lu_solve((lu, piv), b)
+    A1, b1 = A.copy(order="F"), b.copy(order="F")
+    _, ipiv = solve_lse(A1, b1)
+    assert np.array_equal(ipiv - 1, piv)
+    assert rel(A1, lu) < 1e-12
+    assert rel(b1, xr) < 1e-11
+    b2 = b.copy(order="F")
+    solve_lse(A1, b2, ipiv=ipiv, factorize=False)
+    assert rel(b2, xr) < 1e-11
+
+
+def test_solve_lse_singular_matrix_reports_info():
+    n = 64
+    A = np.asfortranarray(np.eye(n))
+    A[:, 10] = 0.0
+    b = np.ones((n, 1), order="F")
+    with pytest.raises(MfbemError) as e:
+        solve_lse(A, b)
+    assert e.value.code == 11
+
+
+def test_solve_lse_unsupported_options_are_errors():
+    L = _abi.load()
+    n = 8
+    A = np.asfortranarray(np.eye(n))
+    b = np.ones(n)
+    ip = np.zeros(n, dtype=np.int32)
+    rc = L.mfbem_solve_r(n, A.ctypes.data_as(_abi._dp), ip.ctypes.data_as(_abi._ip), 1, None, None, None, None, 1,
+                         b.ctypes.data_as(_abi._dp), 1, 1, 0, 0)
+    assert rc == _abi.MFBEM_EUNSUPPORTED
+
+
+def test_kat_confined_cube_on_gpu():
+    """docs/examples/ME-ST-EL-002 closed form through the device path."""
+    d = M.cube_confined_kat(2)
+    R = BemRegion(d, qsi_relative_error=1e-10)
+    mat = M.elastic(1.0, 0.25)
+    x = R.solve_staela(mat["mu"], mat["nu"])
+    u, _ = R.solution(x)
+    assert np.abs(u[:, 0] - (1.25 * 0.5 / 0.75) * d.nodes[:, 0]).max() < 2e-9
+    assert np.abs(u[:, 1:]).max() < 2e-9
+    R.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("plain", 1e-10), ("mixed", 1e-8)])
+def test_sweep_matches_oracle_solution(oracle, precision, tol):
+    d = M.cube_clamped_top_traction(4)
+    mat = M.viscoelastic(1.0, 0.25, 1.0, 0.05)
+    om = M.omega_from_a0(np.linspace(0.1, 2.0, 5), mat)
+    R = BemRegion(d)
+    P = oracle.Problem(d)
+    X = R.sweep_harela(mat, om, precision=precision)
+    for i, w in enumerate(om):
+        Ao, bo = P.assemble_harela(mat, w)
+        xo = oracle.lu_solve(Ao, bo)
+        assert rel(X[i], xo) < tol, (precision, i, rel(X[i], xo))
+    if precision == "mixed":
+        assert R.last_stats["max_backward_error"] <= 1e-12
+    R.close()
+
+
+def test_static_solve_mixed_matches_plain():
+    d = M.cube_clamped_top_traction(4)
+    R = BemRegion(d)
+    mat = M.elastic(1.0, 0.25)
+    xp = R.solve_staela(mat["mu"], mat["nu"], precision="plain")
+    xm = R.solve_staela(mat["mu"], mat["nu"], precision="mixed")
+    assert rel(xm, xp) < 1e-9
+    R.close()

@@ -1,0 +1,76 @@
+"""Caller-side mesh preparation and the C-ABI library (CPU only): the arrays
+the Fortran host would pass are bit-identical to the oracle's, and the shared
+library exports every entry point include/mfbem.h declares."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from multifebe_gb300 import meshgen as M, _abi
+from multifebe_gb300.bem import BemRegion
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _prep(d):
+    L = _abi.load()
+    X = np.ascontiguousarray(d.nodes)
+    conn = np.ascontiguousarray(d.conn, dtype=np.int32)
+    ct = np.ascontiguousarray(d.ctype, dtype=np.int32)
+    cv = np.ascontiguousarray(d.cvalue)
+    gl = np.array([2, 3, 4, 5, 6, 7, 8, 9], dtype=np.int32)
+    pp = L.mfbem_prep_create(d.n_nodes, X.ctypes.data_as(_abi._dp), d.n_elements, conn.ctypes.data_as(_abi._ip),
+                             ct.ctypes.data_as(_abi._ip), cv.view(np.float64).ctypes.data_as(_abi._dp), 1e-6, 16, 8,
+                             gl.ctypes.data_as(_abi._ip), 1e-6)
+    return L, pp, (X, conn, ct, cv, gl)
+
+
+@pytest.mark.parametrize("deck", [M.cube_clamped_top_traction(4), M.cube_confined_kat(2), M.surface_patch(10.0, 8, 1.0),
+                                  M.slab(4, 1)], ids=lambda d: d.name)
+def test_prep_matches_oracle_bit_exact(oracle, deck):
+    L, pp, keep = _prep(deck)
+    try:
+        desc = L.mfbem_prep_desc(pp).contents
+        ne = deck.n_elements
+        cl = np.ctypeslib.as_array(desc.csize, shape=(ne,))
+        gf = np.ctypeslib.as_array(desc.n_phi, shape=(ne,))
+        ball = np.ctypeslib.as_array(desc.bball, shape=(4 * ne,)).reshape(ne, 4)
+        P = oracle.Problem(deck)
+        ocl, ogf, oball = P.element_data()
+        assert np.array_equal(cl, ocl) and np.array_equal(gf, ogf) and np.array_equal(ball, oball)
+        dof = np.zeros(3 * deck.n_nodes, dtype=np.int32)
+        order = np.zeros(deck.n_nodes, dtype=np.int32)
+        L.mfbem_prep_dof(pp, dof.ctypes.data_as(_abi._ip), order.ctypes.data_as(_abi._ip))
+        odof, oorder = P.dof_map()
+        assert np.array_equal(dof.reshape(-1, 3), odof) and np.array_equal(order, oorder)
+        # 1-based rows / columns as node%row, node%col
+        row = np.ctypeslib.as_array(desc.row, shape=(3 * deck.n_nodes,)).reshape(-1, 3)
+        assert np.array_equal(row - 1, odof)
+        # MCA collocation points = oracle's collocation points of kind 1
+        x, info = P.colloc()
+        xm = np.ctypeslib.as_array(desc.x_i_sbie_mca, shape=(24 * ne,)).reshape(ne, 8, 3)
+        for i in np.nonzero(info[:, 1] == 1)[0]:
+            assert np.array_equal(xm[info[i, 2], info[i, 3]], x[i])
+    finally:
+        L.mfbem_prep_free(pp)
+
+
+def test_library_exports_every_declared_symbol():
+    L = _abi.load()
+    hdr = open(os.path.join(ROOT, "include", "mfbem.h")).read()
+    declared = set(re.findall(r"\b(mfbem_[a-z_]+)\s*\(", hdr))
+    assert declared == set(_abi.ABI_SYMBOLS)
+    for s in sorted(declared) + _abi.PREP_SYMBOLS:
+        assert hasattr(L, s), s
+    assert b"sm_103a" in L.mfbem_version()
+
+
+def test_no_device_is_an_error_status_not_a_crash():
+    from conftest import have_gpu
+    if have_gpu():
+        pytest.skip("a GPU is present")
+    with pytest.raises(_abi.MfbemError) as e:
+        BemRegion(M.cube_clamped_top_traction(2))
+    assert e.value.code == _abi.MFBEM_ECUDA
