@@ -219,6 +219,18 @@ def run_gpu(args):
     return 0
 
 
+def profile_case(nf):
+    """Small fixed case for ncu captures: the benchmark mesh, nf frequencies,
+    two mixed-precision sweeps."""
+    from multifebe_gb300 import meshgen as M, BemRegion
+    deck, mat, om = M.workload(2)
+    R = BemRegion(deck)
+    for _ in range(2):
+        R.sweep_harela(mat, om[:nf], precision="mixed")
+    print(json.dumps(R.last_stats))
+    return 0
+
+
 def _desc_bytes(d, deck):
     ne, nn = deck.n_elements, deck.n_nodes
     return int(ne * (24 + 1 + 4 + 24 + 24 + 16 + 24) * 8 + ne * (8 + 1 + 1) * 4 + nn * (3 + 6 + 3 + 1) * 4 + nn * 6 * 8)
@@ -230,7 +242,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--profile-case", type=int, default=0,
+                    help="profiling helper: run the benchmark mesh for this many frequencies twice, print stats, exit")
     args = ap.parse_args()
+    if args.profile_case:
+        return profile_case(args.profile_case)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
