@@ -153,6 +153,23 @@ int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const double mu[
 int mfbem_solve_staela(mfbem_handle* h, double mu, double nu, int32_t precision, double rel_tol, double* x_out,
                        int32_t flags, mfbem_stats* stats);
 
+/* No-allocation variant of mfbem_solve_c. No counterpart in the reference.
+   For callers that cannot allocate device memory: hosts whose device memory
+   is owned by another runtime's pool allocator, or that run under a hard cap
+   on device allocations. Same arguments and results as mfbem_solve_c with
+   scaling = condition = refine = 0 (host arrays; A receives the LU factors,
+   ipiv the 1-based pivots, b the solutions; factorize = 0 reuses A/ipiv).
+   The device working set is a fixed file-scope array of about 16 MiB that
+   every GPU loading the library holds until the process exits; the call
+   makes no cudaMalloc/cudaFree and uses no allocating library. Limits:
+   n <= MFBEM_STATIC_MAX_N, n_rhs <= MFBEM_STATIC_MAX_RHS, else MFBEM_EARG.
+   The first call on a device resolves the array's device address with that
+   device current: make it before any stream capture. Every call shares the
+   array; calls that overlap on the GPU (several host threads) race. */
+#define MFBEM_STATIC_MAX_N 1024
+#define MFBEM_STATIC_MAX_RHS 4
+int mfbem_solve_c_static(int32_t n, double* A, int32_t* ipiv, int32_t n_rhs, double* b, int32_t factorize);
+
 /* Statistics of the last assemble / sweep on this handle. */
 int mfbem_last_stats(mfbem_handle* h, mfbem_stats* stats);
 

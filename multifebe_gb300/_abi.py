@@ -32,7 +32,7 @@ MFBEM_OVERWRITE = 0x2
 ABI_SYMBOLS = [
     "mfbem_mesh_upload", "mfbem_mesh_release", "mfbem_assemble_staela", "mfbem_assemble_harela",
     "mfbem_solve_r", "mfbem_solve_c", "mfbem_sweep_harela", "mfbem_solve_staela", "mfbem_last_stats",
-    "mfbem_last_error", "mfbem_version",
+    "mfbem_last_error", "mfbem_version", "mfbem_solve_c_static",
 ]
 PREP_SYMBOLS = ["mfbem_prep_create", "mfbem_prep_desc", "mfbem_prep_free", "mfbem_prep_dof"]
 
@@ -94,6 +94,7 @@ def load():
                                      ctypes.POINTER(Stats)]
     L.mfbem_solve_staela.argtypes = [vp, c_double, c_double, c_int32, c_double, _dp, c_int32, ctypes.POINTER(Stats)]
     L.mfbem_last_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.mfbem_solve_c_static.argtypes = [c_int32, _dp, _ip, c_int32, _dp, c_int32]
     L.mfbem_last_error.restype = ctypes.c_char_p
     L.mfbem_version.restype = ctypes.c_char_p
     L.mfbem_prep_create.restype = vp

@@ -57,6 +57,8 @@ def build(force=False, verbose=False):
         "mfbem_abi.o": [nvcc, ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", *inc,
                         "-Xptxas", "-v" if verbose else "-O3",
                         "-c", os.path.join(SRC, "mfbem_abi.cu"), "-o", os.path.join(OUT, "mfbem_abi.o")],
+        "mfbem_noalloc.o": [nvcc, ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", *inc,
+                            "-c", os.path.join(SRC, "mfbem_noalloc.cu"), "-o", os.path.join(OUT, "mfbem_noalloc.o")],
     }
 
     def run(cmd):
