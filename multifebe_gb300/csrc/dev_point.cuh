@@ -12,12 +12,43 @@ struct StaelaP {
   double cteu1, cteu2, ctet1, ctet2;
 };
 
+// Number of series terms of numerical.f90:1286-1290 for 1e-6 < |z| <= 1:
+// n = nint(10^(1.176 + 0.175 log10|z|)), a step function of |z|. Its steps sit
+// at |z| = ((k + 1/2) / 10^1.176)^(1/0.175); the table holds their squares
+// (filled on the host by zexp_thresholds()), so the device decides n with four
+// comparisons on |z|^2 instead of evaluating log10 and pow in FP64.
+struct ZexpSteps {
+  double t2[16];  // t2[k-1]: |z|^2 at which n becomes k+1 (k = 1..14), t2[14] = +inf
+};
+__host__ inline ZexpSteps zexp_thresholds() {
+  ZexpSteps s;
+  const double c = pow(10.0, 1.176);
+  for (int k = 1; k <= 14; ++k) {
+    double t = pow((k + 0.5) / c, 1.0 / 0.175);
+    s.t2[k - 1] = t * t;
+  }
+  s.t2[14] = s.t2[15] = 1e300;
+  return s;
+}
+__device__ __forceinline__ int zexp_nterms(const ZexpSteps& s, double az2) {
+  if (az2 <= 1e-12) return 1;
+  // smallest k with az2 < t2[k-1] gives n = k (n = 15 above the last step)
+  int lo = 0, hi = 15;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (az2 < s.t2[mid]) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo + 1;
+}
+
 // u* / t* coefficient block of fbem_bem_harela3d_parameters (bem_harela3d.f90:118-134)
 struct HarParD {
   cd k1, k2;
   cd psi[6], chi[6];
   cd T1[10], T2[9], T3[9];
   cd cte_u, cte_t;
+  ZexpSteps steps;
 };
 
 __host__ __device__ inline StaelaP staela_params(double mu, double nu) {
@@ -91,16 +122,11 @@ __host__ __device__ inline HarParD harela_params(cd lambda, cd mu, double rho, d
 // E_2..E_5 of z (numerical.f90:1258-1331): E_n(z) = e^z - sum_{k<n} z^k/k!.
 // For |z|<=1 the reference sums the series tail from k=n+6 down to 6; the same
 // terms are summed here in nested (Horner) form.
-__device__ __forceinline__ void zexp_2to5(cd z, cd& E2, cd& E3, cd& E4, cd& E5) {
-  double az = cabs_(z);
+__device__ __forceinline__ void zexp_2to5(const ZexpSteps& steps, cd z, cd& E2, cd& E3, cd& E4, cd& E5) {
+  double az2 = z.re * z.re + z.im * z.im;
   cd z2 = z * z, z3 = z2 * z, z4 = z3 * z;
-  if (az <= 1.0) {
-    int n = 1;
-    if (az > 1e-6) {
-      double v = pow(10.0, 1.176 + 0.175 * log10(az));
-      n = (int)floor(v + 0.5);
-    }
-    int N = n + 6;
+  if (az2 <= 1.0) {
+    int N = zexp_nterms(steps, az2) + 6;
     cd t = mk(1.0);
     for (int k = N; k >= 7; --k) t = 1.0 + t * z * (1.0 / (double)k);
     cd z5 = z4 * z, z6 = z5 * z;
@@ -130,8 +156,8 @@ __device__ __forceinline__ void harela_coeffs(const HarParD& p, double r, cd& ps
   cd z1 = mk(p.k1.im * r, -p.k1.re * r);  // -i k1 r
   cd z2 = mk(p.k2.im * r, -p.k2.re * r);
   cd a2, a3, a4, a5, b2, b3, b4, b5;
-  zexp_2to5(z1, a2, a3, a4, a5);
-  zexp_2to5(z2, b2, b3, b4, b5);
+  zexp_2to5(p.steps, z1, a2, a3, a4, a5);
+  zexp_2to5(p.steps, z2, b2, b3, b4, b5);
   a2 = a2 * d1r1; b2 = b2 * d1r1;
   a3 = a3 * d1r2; b3 = b3 * d1r2;
   a4 = a4 * d1r3; b4 = b4 * d1r3;

@@ -345,6 +345,20 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   k_scan<long long, long long><<<1, 1024>>>(spts, m.sing_pt, (int)m.nsing); ++g_launches;
   CK(cudaMemcpy(&h->pts_sing, m.sing_pt + m.nsing, sizeof(long long), cudaMemcpyDeviceToHost));
   k_ft_prep<<<nblk(ncp, 128), 128>>>(m); ++g_launches;
+  // hoist the singular / adaptive point geometry out of the frequency loop when
+  // it fits a modest share of the device (22 / 14 doubles per point)
+  m.adp_cp = adp_cp;
+  m.nsing_pts = h->pts_sing;
+  m.nleaf_pts = h->pts_adp;
+  const size_t geo_budget = (size_t)8 << 30;
+  if (m.nsing_pts > 0 && (size_t)m.nsing_pts * 22 * sizeof(double) <= geo_budget) {
+    if ((rc = dalloc(h, (void**)&m.sing_geo, (size_t)m.nsing_pts * 22 * sizeof(double)))) { mfbem_mesh_release(h); return rc; }
+    k_sing_geo<<<nblk(m.nsing_pts, 128), 128>>>(m); ++g_launches;
+  }
+  if (m.nleaf_pts > 0 && (size_t)m.nleaf_pts * 14 * sizeof(double) <= geo_budget) {
+    if ((rc = dalloc(h, (void**)&m.leaf_geo, (size_t)m.nleaf_pts * 14 * sizeof(double)))) { mfbem_mesh_release(h); return rc; }
+    k_leaf_geo<<<nblk(m.nleaf_pts, 128), 128>>>(m); ++g_launches;
+  }
   CK(cudaGetLastError());
   CK(cudaDeviceSynchronize());
   auto t1 = std::chrono::steady_clock::now();
@@ -384,11 +398,14 @@ extern "C" int mfbem_last_stats(mfbem_handle* h, mfbem_stats* s) {
 // ---------------------------------------------------------------------------
 // assembly into device buffers (nf systems: A at A + f*astride, b at b + f*bstride)
 // ---------------------------------------------------------------------------
-__global__ void k_harpar(const double* in /*nf x {lre,lim,mre,mim,rho,omega}*/, int nf, HarParD* out) {
+__global__ void k_harpar(const double* in /*nf x {lre,lim,mre,mim,rho,omega}*/, int nf, HarParD* out,
+                         ZexpSteps steps) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   const double* q = in + 6 * f;
-  out[f] = harela_params(mk(q[0], q[1]), mk(q[2], q[3]), q[4], q[5]);
+  HarParD p = harela_params(mk(q[0], q[1]), mk(q[2], q[3]), q[4], q[5]);
+  p.steps = steps;
+  out[f] = p;
 }
 
 // Assembly kernels in a fixed order (regular, adaptive, singular, free terms);
@@ -529,7 +546,7 @@ extern "C" int mfbem_assemble_harela(mfbem_handle* h, const double lambda[2], co
   double q[6] = {lambda[0], lambda[1], mu[0], mu[1], rho, omega};
   double* dq = (double*)((char*)h->par.p + sizeof(HarParD));
   CK(cudaMemcpyAsync(dq, q, sizeof(q), cudaMemcpyHostToDevice, h->st));
-  k_harpar<<<1, 32, 0, h->st>>>(dq, 1, (HarParD*)h->par.p); ++g_launches;
+  k_harpar<<<1, 32, 0, h->st>>>(dq, 1, (HarParD*)h->par.p, zexp_thresholds()); ++g_launches;
   PolHarmonic pol;
   pol.p = (const HarParD*)h->par.p;
   return assemble_common<true>(h, &pol, nu, A, lda, b, flags);

@@ -100,38 +100,47 @@ struct PolHarmonic {
   }
 };
 
-// Shared flush: scale, reverse, scatter one pair's 144 outputs of this lane set.
+// Outputs of one pair handled by the lanes of a warp: o = lane + 32 j, j < 4.
+// o < 72: h(kn, il, ik), kn = o / 9; o >= 72: g(kn, s) with s one of the six
+// (il <= ik) components (u* is symmetric, so g(kn, il, ik) = g(kn, ik, il)).
+constexpr int kOut = 120;
+constexpr int kAcc = 4;
+__device__ __forceinline__ int sym_il(int s) { return s < 3 ? 0 : (s < 5 ? 1 : 2); }
+__device__ __forceinline__ int sym_ik(int s) { return s < 3 ? s : (s < 5 ? s - 2 : 2); }
+
+// Shared flush: scale, reverse, scatter one pair's outputs of this lane set.
 template <class POL>
 __device__ __forceinline__ void flush_pair(const DMesh& m, const POL& pol, int f, int dn, int e,
-                                           typename POL::T acc[5], double* A, size_t lda, size_t astride,
+                                           typename POL::T acc[kAcc], double* A, size_t lda, size_t astride,
                                            double* b, size_t bstride, const double* hli_phi /* or null */) {
   typedef typename POL::T T;
   const int lane = threadIdx.x & 31;
   T bc[3] = {VT<T>::zero(), VT<T>::zero(), VT<T>::zero()};
   const bool rev = m.rev[e] != 0;
   double* Af = A + astride * f;
-  for (int j = 0; j < 5; ++j) {
+  for (int j = 0; j < kAcc; ++j) {
     int o = lane + 32 * j;
-    if (o >= 144) break;
-    int hg = o / 72, r = o % 72, kn = r / 9, il = (r % 9) / 3, ik = r % 3;
+    if (o >= kOut) break;
     T v = acc[j];
-    if (hg == 0) {
+    if (o < 72) {
+      int kn = o / 9, il = (o % 9) / 3, ik = o % 3;
       if (hli_phi) v = v + hli_phi[9 + kn] * pol.cpv(f) * hli_phi[3 * il + ik];
       v = v * pol.cte_t(f);
       if (rev) v = -v;
+      int dof = m.edof[8 * e + kn] + ik;
+      size_t row = 3 * (size_t)dn + il;
+      if (m.dct[dof] == 1) addA(Af, (size_t)dof * lda + row, v);
+      else bc[il] = bc[il] - v * cval(m.dcv, dof, v);
     } else {
+      int q = o - 72, kn = q / 6, sidx = q % 6, il = sym_il(sidx), ik = sym_ik(sidx);
       v = v * pol.cte_u(f);
-    }
-    int dof = m.edof[8 * e + kn] + ik;
-    int ct = m.dct[dof];
-    size_t row = 3 * (size_t)dn + il;
-    T cv = cval(m.dcv, dof, v);
-    if (hg == 0) {
-      if (ct == 1) addA(Af, (size_t)dof * lda + row, v);
-      else bc[il] = bc[il] - v * cv;
-    } else {
-      if (ct == 0) addA(Af, (size_t)dof * lda + row, -v);
-      else bc[il] = bc[il] + v * cv;
+      for (int t = 0; t < (il == ik ? 1 : 2); ++t) {
+        int r_ = t ? ik : il, c_ = t ? il : ik;
+        int dof = m.edof[8 * e + kn] + c_;
+        size_t row = 3 * (size_t)dn + r_;
+        if (m.dct[dof] == 0) addA(Af, (size_t)dof * lda + row, -v);
+        else bc[r_] = bc[r_] + v * cval(m.dcv, dof, v);
+      }
     }
   }
   for (int il = 0; il < 3; ++il)
@@ -145,16 +154,21 @@ __device__ __forceinline__ void flush_pair(const DMesh& m, const POL& pol, int f
 
 template <typename T>
 struct alignas(16) Combo {
-  T fu[9], ft[9];
+  T fu[6], ft[9];
   double w[8];
   int pair;
 };
 template <typename T>
 struct alignas(16) ComboS {
-  T fu[9], ft[9], fc[9];
+  T fu[6], ft[9], fc[9];
   double w[8], wd[8];
   int pair;
 };
+// keep the six independent components of the symmetric u*
+template <typename T>
+__device__ __forceinline__ void store_u6(T* dst, const T fu[9]) {
+  dst[0] = fu[0]; dst[1] = fu[1]; dst[2] = fu[2]; dst[3] = fu[4]; dst[4] = fu[5]; dst[5] = fu[8];
+}
 
 __device__ __forceinline__ int find_le(const long long* a, int lo, int hi, long long v) {
   // largest j in [lo, hi) with a[j] <= v
@@ -167,14 +181,21 @@ __device__ __forceinline__ int find_le(const long long* a, int lo, int hi, long 
 }
 
 template <typename T>
-__device__ __forceinline__ void accumulate(T acc[5], const T* fu, const T* ft, const double* w) {
+__device__ __forceinline__ void accumulate(T acc[kAcc], const T* fu6, const T* ft, const double* w) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int j = 0; j < 5; ++j) {
+  for (int j = 0; j < kAcc; ++j) {
     int o = lane + 32 * j;
-    if (o < 144) {
-      int hg = o / 72, r = o % 72, kn = r / 9, q = r % 9;
-      T v = hg == 0 ? ft[q] : fu[q];
+    if (o < kOut) {
+      T v;
+      int kn;
+      if (o < 72) {
+        kn = o / 9;
+        v = ft[o % 9];
+      } else {
+        kn = (o - 72) / 6;
+        v = fu6[(o - 72) % 6];
+      }
       acc[j] = acc[j] + v * w[kn];
     }
   }
@@ -197,8 +218,8 @@ __global__ void __launch_bounds__(WPB * 32) k_reg(DMesh m, POL pol, int nf, doub
     const double* xi = m.cpx + 3 * (size_t)cp;
     const long long P0 = m.reg_pt[s0], Q = m.reg_pt[s1] - P0;
     int cur = -1;
-    T acc[5];
-    for (int j = 0; j < 5; ++j) acc[j] = VT<T>::zero();
+    T acc[kAcc];
+    for (int j = 0; j < kAcc; ++j) acc[j] = VT<T>::zero();
     for (long long base = 0; base < Q; base += 32) {
       long long c = base + lane;
       if (c < Q) {
@@ -208,7 +229,9 @@ __global__ void __launch_bounds__(WPB * 32) k_reg(DMesh m, POL pol, int nf, doub
         size_t pt = (size_t)e * m.ptot + m.ps_off[ps] + (size_t)(P0 + c - m.reg_pt[jp]);
         double rv[3] = {m.px[3 * pt] - xi[0], m.px[3 * pt + 1] - xi[1], m.px[3 * pt + 2] - xi[2]};
         double n[3] = {m.pn[3 * pt], m.pn[3 * pt + 1], m.pn[3 * pt + 2]};
-        pol.point(f, rv, n, S[lane].fu, S[lane].ft);
+        T fu9[9];
+        pol.point(f, rv, n, fu9, S[lane].ft);
+        store_u6(S[lane].fu, fu9);
         for (int k = 0; k < 8; ++k) S[lane].w[k] = m.pphi[8 * pt + k];
         S[lane].pair = jp;
       }
@@ -219,7 +242,7 @@ __global__ void __launch_bounds__(WPB * 32) k_reg(DMesh m, POL pol, int nf, doub
         if (jp != cur) {
           if (cur >= 0) flush_pair(m, pol, f, dn, m.reg_pair[cur] & 0xFFFFFF, acc, A, lda, astride, b, bstride, nullptr);
           cur = jp;
-          for (int j = 0; j < 5; ++j) acc[j] = VT<T>::zero();
+          for (int j = 0; j < kAcc; ++j) acc[j] = VT<T>::zero();
         }
         accumulate(acc, S[t].fu, S[t].ft, S[t].w);
       }
@@ -230,6 +253,45 @@ __global__ void __launch_bounds__(WPB * 32) k_reg(DMesh m, POL pol, int nf, doub
 }
 
 // ---------------------------------------------------------------- adaptive pairs
+// Geometry of point k of leaf l (adaptive pair a): Telles maps, sub-square to
+// element coordinates, element geometry (sbie_ext_st, bem_staela3d.f90:654-969).
+__device__ __forceinline__ void leaf_point(const DMesh& m, int l, int a, int k, const double* xi, double rv[3],
+                                           double n[3], double w[8]) {
+  int e = m.adp_e[a];
+  int g = m.leaf_gln[l];
+  int k1 = k / g + 1, k2 = k % g + 1;
+  const double* L = m.leaf + (size_t)l * LEAF_D;
+  Telles t1{L[8], L[9], L[10], L[11]}, t2{L[12], L[13], L[14], L[15]};
+  double xp1, jt1, xp2, jt2;
+  telles_map(t1, gl11x(k1, g), xp1, jt1);
+  telles_map(t2, gl11x(k2, g), xp2, jt2);
+  double sp[4], sd1[4], sd2[4];
+  phi_q4(xp1, xp2, sp);
+  dphi_q4(xp1, xp2, sd1, sd2);
+  double xa = 0, xb = 0, a11 = 0, a12 = 0, a21 = 0, a22 = 0;
+  for (int q = 0; q < 4; ++q) {
+    xa = xa + sp[q] * L[2 * q];
+    xb = xb + sp[q] * L[2 * q + 1];
+    a11 = a11 + sd1[q] * L[2 * q];
+    a12 = a12 + sd1[q] * L[2 * q + 1];
+    a21 = a21 + sd2[q] * L[2 * q];
+    a22 = a22 + sd2[q] * L[2 * q + 1];
+  }
+  double js = a11 * a22 - a12 * a21;
+  double xq[3], T1[3], T2[3], phi[8], N[3];
+  geom_q8(m.ex + 24 * (size_t)e, xa, xb, xq, T1, T2, phi);
+  cross3(T1, T2, N);
+  double jg = norm3(N);
+  n[0] = N[0] / jg;
+  n[1] = N[1] / jg;
+  n[2] = N[2] / jg;
+  rv[0] = xq[0] - xi[0];
+  rv[1] = xq[1] - xi[1];
+  rv[2] = xq[2] - xi[2];
+  double jw = jg * js * jt1 * jt2 * gl11w(k1, g) * gl11w(k2, g);
+  for (int q = 0; q < 8; ++q) w[q] = phi[q] * jw;
+}
+
 template <class POL, int WPB>
 __global__ void __launch_bounds__(WPB * 32) k_adp(DMesh m, POL pol, int nf, double* A, size_t lda, size_t astride,
                                                   double* b, size_t bstride) {
@@ -247,44 +309,30 @@ __global__ void __launch_bounds__(WPB * 32) k_adp(DMesh m, POL pol, int nf, doub
     const double* xi = m.cpx + 3 * (size_t)cp;
     const long long P0 = m.leaf_pt[l0], Q = m.leaf_pt[l1] - P0;
     int cur = -1;
-    T acc[5];
-    for (int j = 0; j < 5; ++j) acc[j] = VT<T>::zero();
+    T acc[kAcc];
+    for (int j = 0; j < kAcc; ++j) acc[j] = VT<T>::zero();
     for (long long base = 0; base < Q; base += 32) {
       long long c = base + lane;
       if (c < Q) {
         int l = find_le(m.leaf_pt, l0, l1, P0 + c);
         int a = m.leaf_pair[l];
-        int e = m.adp_e[a];
-        int g = m.leaf_gln[l];
-        int k = (int)(P0 + c - m.leaf_pt[l]);
-        int k1 = k / g + 1, k2 = k % g + 1;
-        const double* L = m.leaf + (size_t)l * LEAF_D;
-        Telles t1{L[8], L[9], L[10], L[11]}, t2{L[12], L[13], L[14], L[15]};
-        double xp1, jt1, xp2, jt2;
-        telles_map(t1, gl11x(k1, g), xp1, jt1);
-        telles_map(t2, gl11x(k2, g), xp2, jt2);
-        double sp[4], sd1[4], sd2[4];
-        phi_q4(xp1, xp2, sp);
-        dphi_q4(xp1, xp2, sd1, sd2);
-        double xa = 0, xb = 0, a11 = 0, a12 = 0, a21 = 0, a22 = 0;
-        for (int q = 0; q < 4; ++q) {
-          xa = xa + sp[q] * L[2 * q];
-          xb = xb + sp[q] * L[2 * q + 1];
-          a11 = a11 + sd1[q] * L[2 * q];
-          a12 = a12 + sd1[q] * L[2 * q + 1];
-          a21 = a21 + sd2[q] * L[2 * q];
-          a22 = a22 + sd2[q] * L[2 * q + 1];
+        if (m.leaf_geo) {
+          const long long g = P0 + c, np = m.nleaf_pts;
+          const double* G = m.leaf_geo;
+          double rv[3] = {G[g], G[np + g], G[2 * np + g]};
+          double n[3] = {G[3 * np + g], G[4 * np + g], G[5 * np + g]};
+          T fu9[9];
+          pol.point(f, rv, n, fu9, S[lane].ft);
+          store_u6(S[lane].fu, fu9);
+          for (int q = 0; q < 8; ++q) S[lane].w[q] = G[(6 + q) * np + g];
+        } else {
+          double rv[3], n[3], w[8];
+          leaf_point(m, l, a, (int)(P0 + c - m.leaf_pt[l]), xi, rv, n, w);
+          T fu9[9];
+          pol.point(f, rv, n, fu9, S[lane].ft);
+          store_u6(S[lane].fu, fu9);
+          for (int q = 0; q < 8; ++q) S[lane].w[q] = w[q];
         }
-        double js = a11 * a22 - a12 * a21;
-        double xq[3], T1[3], T2[3], phi[8], N[3];
-        geom_q8(m.ex + 24 * (size_t)e, xa, xb, xq, T1, T2, phi);
-        cross3(T1, T2, N);
-        double jg = norm3(N);
-        double n[3] = {N[0] / jg, N[1] / jg, N[2] / jg};
-        double rv[3] = {xq[0] - xi[0], xq[1] - xi[1], xq[2] - xi[2]};
-        double jw = jg * js * jt1 * jt2 * gl11w(k1, g) * gl11w(k2, g);
-        pol.point(f, rv, n, S[lane].fu, S[lane].ft);
-        for (int q = 0; q < 8; ++q) S[lane].w[q] = phi[q] * jw;
         S[lane].pair = a;
       }
       __syncwarp();
@@ -294,7 +342,7 @@ __global__ void __launch_bounds__(WPB * 32) k_adp(DMesh m, POL pol, int nf, doub
         if (a != cur) {
           if (cur >= 0) flush_pair(m, pol, f, dn, m.adp_e[cur], acc, A, lda, astride, b, bstride, nullptr);
           cur = a;
-          for (int j = 0; j < 5; ++j) acc[j] = VT<T>::zero();
+          for (int j = 0; j < kAcc; ++j) acc[j] = VT<T>::zero();
         }
         accumulate(acc, S[t].fu, S[t].ft, S[t].w);
       }
@@ -305,6 +353,76 @@ __global__ void __launch_bounds__(WPB * 32) k_adp(DMesh m, POL pol, int nf, doub
 }
 
 // ---------------------------------------------------------------- singular pairs
+// Geometry of polar point k of singular pair q (sbie_int, bem_staela3d.f90:1100-1381).
+__device__ __forceinline__ void sing_point(const DMesh& m, int q, int k, double rv[3], double n[3], double w[8],
+                                           double wd[8]) {
+  const double* D = m.sing_d + (size_t)q * SING_D;
+  const int* I = m.sing_i + (size_t)q * SING_I;
+  int s = 0;
+  while (s + 1 < I[0] && I[17 + s + 1] <= k) ++s;
+  int kk = k - I[17 + s];
+  int ngt = I[9 + s];
+  int kt = kk / 15 + 1, kr = kk % 15 + 1;
+  double xi_i[2] = {D[0], D[1]};
+  double tpi = D[38 + 2 * s], tpf = D[39 + 2 * s];
+  double tpp = gl01x(kt, ngt), wa = gl01w(kt, ngt);
+  double jtp = tpf - tpi;
+  double tp = jtp * tpp + tpi;
+  double theta, rhoij;
+  polar_angular(xi_i, I[1 + s], tp, &theta, &rhoij);
+  double sn, cs;
+  sincos(theta, &sn, &cs);
+  double rho = rhoij * gl01x(kr, 15);
+  double xq[3], T1[3], T2[3], phi[8], N[3];
+  int e = m.sing_e[q];
+  geom_q8(m.ex + 24 * (size_t)e, xi_i[0] + rho * cs, xi_i[1] + rho * sn, xq, T1, T2, phi);
+  cross3(T1, T2, N);
+  double jg = norm3(N);
+  n[0] = N[0] / jg;
+  n[1] = N[1] / jg;
+  n[2] = N[2] / jg;
+  rv[0] = xq[0] - D[2];
+  rv[1] = xq[1] - D[3];
+  rv[2] = xq[2] - D[4];
+  double jw = jg * rho * jtp * wa * gl01w(kr, 15);
+  for (int p = 0; p < 8; ++p) {
+    w[p] = phi[p] * jw;
+    wd[p] = (phi[p] - D[5 + p]) * jw;
+  }
+}
+
+// once per mesh: the singular and adaptive-leaf point geometry for all frequencies
+__global__ void k_sing_geo(DMesh m) {
+  long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= m.nsing_pts) return;
+  int q = find_le(m.sing_pt, 0, (int)m.nsing, g);
+  double rv[3], n[3], w[8], wd[8];
+  sing_point(m, q, (int)(g - m.sing_pt[q]), rv, n, w, wd);
+  const long long np = m.nsing_pts;
+  for (int c = 0; c < 3; ++c) {
+    m.sing_geo[c * np + g] = rv[c];
+    m.sing_geo[(3 + c) * np + g] = n[c];
+  }
+  for (int p = 0; p < 8; ++p) {
+    m.sing_geo[(6 + p) * np + g] = w[p];
+    m.sing_geo[(14 + p) * np + g] = wd[p];
+  }
+}
+__global__ void k_leaf_geo(DMesh m) {
+  long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= m.nleaf_pts) return;
+  int l = find_le(m.leaf_pt, 0, (int)m.nleaf, g);
+  int a = m.leaf_pair[l];
+  double rv[3], n[3], w[8];
+  leaf_point(m, l, a, (int)(g - m.leaf_pt[l]), m.cpx + 3 * (size_t)m.adp_cp[a], rv, n, w);
+  const long long np = m.nleaf_pts;
+  for (int c = 0; c < 3; ++c) {
+    m.leaf_geo[c * np + g] = rv[c];
+    m.leaf_geo[(3 + c) * np + g] = n[c];
+  }
+  for (int p = 0; p < 8; ++p) m.leaf_geo[(6 + p) * np + g] = w[p];
+}
+
 template <class POL, int WPB>
 __global__ void __launch_bounds__(WPB * 32) k_sing(DMesh m, POL pol, int nf, double* A, size_t lda, size_t astride,
                                                    double* b, size_t bstride) {
@@ -321,43 +439,28 @@ __global__ void __launch_bounds__(WPB * 32) k_sing(DMesh m, POL pol, int nf, dou
     if (q0 == q1) continue;
     const long long P0 = m.sing_pt[q0], Q = m.sing_pt[q1] - P0;
     int cur = -1;
-    T acc[5], acd[5];
-    for (int j = 0; j < 5; ++j) acc[j] = acd[j] = VT<T>::zero();
+    T acc[kAcc], acd[kAcc];
+    for (int j = 0; j < kAcc; ++j) acc[j] = acd[j] = VT<T>::zero();
     for (long long base = 0; base < Q; base += 32) {
       long long c = base + lane;
       if (c < Q) {
         int q = find_le(m.sing_pt, q0, q1, P0 + c);
-        const double* D = m.sing_d + (size_t)q * SING_D;
-        const int* I = m.sing_i + (size_t)q * SING_I;
-        int k = (int)(P0 + c - m.sing_pt[q]);
-        int s = 0;
-        while (s + 1 < I[0] && I[17 + s + 1] <= k) ++s;
-        int kk = k - I[17 + s];
-        int ngt = I[9 + s];
-        int kt = kk / 15 + 1, kr = kk % 15 + 1;
-        double xi_i[2] = {D[0], D[1]};
-        double tpi = D[38 + 2 * s], tpf = D[39 + 2 * s];
-        double tpp = gl01x(kt, ngt), wa = gl01w(kt, ngt);
-        double jtp = tpf - tpi;
-        double tp = jtp * tpp + tpi;
-        double theta, rhoij;
-        polar_angular(xi_i, I[1 + s], tp, &theta, &rhoij);
-        double sn, cs;
-        sincos(theta, &sn, &cs);
-        double rho = rhoij * gl01x(kr, 15);
-        double xq[3], T1[3], T2[3], phi[8], N[3];
-        int e = m.sing_e[q];
-        geom_q8(m.ex + 24 * (size_t)e, xi_i[0] + rho * cs, xi_i[1] + rho * sn, xq, T1, T2, phi);
-        cross3(T1, T2, N);
-        double jg = norm3(N);
-        double n[3] = {N[0] / jg, N[1] / jg, N[2] / jg};
-        double rv[3] = {xq[0] - D[2], xq[1] - D[3], xq[2] - D[4]};
-        double jw = jg * rho * jtp * wa * gl01w(kr, 15);
-        pol.point_sing(f, rv, n, S[lane].fu, S[lane].ft, S[lane].fc);
-        for (int p = 0; p < 8; ++p) {
-          S[lane].w[p] = phi[p] * jw;
-          S[lane].wd[p] = (phi[p] - D[5 + p]) * jw;
+        double rv[3], n[3];
+        if (m.sing_geo) {
+          const long long g = P0 + c, np = m.nsing_pts;
+          const double* G = m.sing_geo;
+          rv[0] = G[g]; rv[1] = G[np + g]; rv[2] = G[2 * np + g];
+          n[0] = G[3 * np + g]; n[1] = G[4 * np + g]; n[2] = G[5 * np + g];
+          for (int p = 0; p < 8; ++p) {
+            S[lane].w[p] = G[(6 + p) * np + g];
+            S[lane].wd[p] = G[(14 + p) * np + g];
+          }
+        } else {
+          sing_point(m, q, (int)(P0 + c - m.sing_pt[q]), rv, n, S[lane].w, S[lane].wd);
         }
+        T fu9[9];
+        pol.point_sing(f, rv, n, fu9, S[lane].ft, S[lane].fc);
+        store_u6(S[lane].fu, fu9);
         S[lane].pair = q;
       }
       __syncwarp();
@@ -366,11 +469,11 @@ __global__ void __launch_bounds__(WPB * 32) k_sing(DMesh m, POL pol, int nf, dou
         int q = S[t].pair;
         if (q != cur) {
           if (cur >= 0) {
-            for (int j = 0; j < 5; ++j) acc[j] = acc[j] + acd[j];
+            for (int j = 0; j < kAcc; ++j) acc[j] = acc[j] + acd[j];
             flush_pair(m, pol, f, dn, m.sing_e[cur], acc, A, lda, astride, b, bstride, hp[w]);
           }
           cur = q;
-          for (int j = 0; j < 5; ++j) acc[j] = acd[j] = VT<T>::zero();
+          for (int j = 0; j < kAcc; ++j) acc[j] = acd[j] = VT<T>::zero();
           if (lane < 17) {
             const double* D = m.sing_d + (size_t)q * SING_D;
             hp[w][lane] = lane < 9 ? D[13 + lane] : D[5 + lane - 9];
@@ -391,7 +494,7 @@ __global__ void __launch_bounds__(WPB * 32) k_sing(DMesh m, POL pol, int nf, dou
       __syncwarp();
     }
     if (cur >= 0) {
-      for (int j = 0; j < 5; ++j) acc[j] = acc[j] + acd[j];
+      for (int j = 0; j < kAcc; ++j) acc[j] = acc[j] + acd[j];
       flush_pair(m, pol, f, dn, m.sing_e[cur], acc, A, lda, astride, b, bstride, hp[w]);
     }
   }

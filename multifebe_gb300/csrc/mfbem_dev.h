@@ -76,6 +76,12 @@ struct DMesh {
   double* sing_d;        // [nsing][SING_D]
   int* sing_i;           // [nsing][SING_I]
   long long* sing_pt;    // [nsing+1]
+  // frequency-independent geometry of every singular / adaptive-leaf
+  // quadrature point, component-major [component][point] (null: recompute)
+  double* sing_geo;      // 22 components: x - x_i (3), unit normal (3), phi*jw (8), (phi - phi_i)*jw (8)
+  double* leaf_geo;      // 14 components: x - x_i (3), unit normal (3), phi*jw (8)
+  int* adp_cp;           // collocation point of each adaptive pair
+  long long nsing_pts, nleaf_pts;
   double* ft;            // [ncp][FT_D]
   int* ft_ok;            // [ncp] 1 ok, 0 invalid configuration
   long long nreg, nadp, nleaf, nsing;

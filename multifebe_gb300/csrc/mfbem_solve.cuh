@@ -416,7 +416,7 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   }
   CK(cudaMemcpyAsync(dq, q.data(), sizeof(double) * q.size(), cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(dnu, nuv.data(), sizeof(double) * nuv.size(), cudaMemcpyHostToDevice, h->st));
-  k_harpar<<<nblk(n_freq, 32), 32, 0, h->st>>>(dq, n_freq, dpar); ++g_launches;
+  k_harpar<<<nblk(n_freq, 32), 32, 0, h->st>>>(dq, n_freq, dpar, zexp_thresholds()); ++g_launches;
   double2* A = (double2*)h->A.p;
   double2* b = (double2*)h->b.p;
   double2* x = (flags & MFBEM_DEVICE_PTRS) ? (double2*)x_out : (double2*)h->x.p;
