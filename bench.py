@@ -200,6 +200,8 @@ def run_gpu(args):
                        "rel_err_vs_fp64": relerr, "max_backward_error": st["max_backward_error"],
                        "l2": "inputs larger than L2 (20 x 192 MB systems per step)",
                        "ms_assemble": st["ms_assemble"], "ms_factor": st["ms_factor"], "ms_solve": st["ms_solve"],
+                       "ms_regular": st["ms_regular"], "ms_singular": st["ms_singular"],
+                       "ms_adaptive": st["ms_adaptive"], "ms_free": st["ms_free"],
                        "parallelism": f"replicas x{ws}"},
             "e2e": {"value": ws * nf / e2e_step, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

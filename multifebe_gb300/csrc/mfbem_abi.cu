@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -58,7 +59,7 @@ struct mfbem_handle {
   int ndof = 0, ne = 0, nn = 0;
   cudaStream_t st = nullptr;
   cublasHandle_t blas = nullptr;
-  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu;
+  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f;
   mfbem_stats stats{};
   long long pts_reg = 0, pts_adp = 0, pts_sing = 0;
   int* d_err = nullptr;
@@ -381,7 +382,8 @@ extern "C" int mfbem_mesh_release(mfbem_handle* h) {
   if (!h) return MFBEM_EARG;
   cudaDeviceSynchronize();
   for (void* p : h->owned) cudaFree(p);
-  for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu})
+  for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu, &h->parf,
+                    &h->pphi_f})
     if (b->p) cudaFree(b->p);
   if (h->blas) cublasDestroy(h->blas);
   if (h->st) cudaStreamDestroy(h->st);
@@ -433,14 +435,26 @@ struct AsmTimes {
 
 template <class POL>
 static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, int nf, double* A, size_t lda,
-                           size_t astride, double* b, size_t bstride, AsmTimes* tm = nullptr) {
+                           size_t astride, double* b, size_t bstride, AsmTimes* tm = nullptr,
+                           const HarParF* pf = nullptr, const ff* pphi_f = nullptr) {
   const DMesh& m = h->m;
   constexpr int WPB = 4;
   long long nw = (long long)m.ndn * nf;
   unsigned g = nblk(nw, WPB);
   CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
   if (tm) cudaEventRecord(tm->ev[0], h->st);
-  if (m.nreg > 0) { k_reg<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride); ++g_launches; }
+  if (m.nreg > 0) {
+    if constexpr (std::is_same<POL, PolHarmonic>::value) {
+      if (pf && pphi_f) {
+        k_reg_mixed<WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, pf, pphi_f, nf, A, lda, astride, b, bstride);
+      } else {
+        k_reg<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
+      }
+    } else {
+      k_reg<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
+    }
+    ++g_launches;
+  }
   if (tm) cudaEventRecord(tm->ev[1], h->st);
   if (m.nadp > 0) { k_adp<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride); ++g_launches; }
   if (tm) cudaEventRecord(tm->ev[2], h->st);

@@ -17,6 +17,7 @@
 #include "dev_complex.cuh"
 #include "dev_point.cuh"
 #include "mfbem_dev.h"
+#include "dev_df64.cuh"
 
 namespace mfb {
 
@@ -552,6 +553,188 @@ __global__ void k_free(DMesh m, POL pol, const double* nu /* complex, per freque
     }
   }
   for (int il = 0; il < 3; ++il) addA(bf, 3 * (size_t)dn + il, bc[il]);
+}
+
+// ============================================================================
+// Mixed-precision regular pairs (time-harmonic). The exponential decomposition
+// E_n and the geometry stay in binary64; the linear combinations forming psi,
+// chi, TT1..TT3, the fundamental solutions and the quadrature sums run in
+// double-float arithmetic (dev_df64.cuh) on the FP32 pipe. Used by the mixed
+// sweep only: regular (far-field) pairs have smooth integrands, and double-float
+// keeps them at ~1e-14 relative; singular and quasi-singular pairs stay FP64.
+// ============================================================================
+
+struct HarParF {
+  cf psi[6], chi[6], T1[10], T2[9], T3[9];
+};
+__global__ void k_harpar_f(const HarParD* p, HarParF* out, int nf) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  HarParF o;
+  for (int i = 0; i < 6; ++i) o.psi[i] = cf_from(p[f].psi[i].re, p[f].psi[i].im);
+  for (int i = 0; i < 6; ++i) o.chi[i] = cf_from(p[f].chi[i].re, p[f].chi[i].im);
+  for (int i = 0; i < 10; ++i) o.T1[i] = cf_from(p[f].T1[i].re, p[f].T1[i].im);
+  for (int i = 0; i < 9; ++i) o.T2[i] = cf_from(p[f].T2[i].re, p[f].T2[i].im);
+  for (int i = 0; i < 9; ++i) o.T3[i] = cf_from(p[f].T3[i].re, p[f].T3[i].im);
+  out[f] = o;
+}
+// phi*J*w of the element datasets as double-float, once per mesh
+__global__ void k_pphi_f(const double* pphi, ff* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = ff_from(pphi[i]);
+}
+
+__device__ __forceinline__ cf cfc(const cd& v) { return cf_from(v.re, v.im); }
+
+// u*, t* (without constants) at one regular point, df64 combination stage
+__device__ __forceinline__ void harela_point_f(const HarParD& p, const HarParF& q, const double rv[3], const double n[3],
+                                               cf fu6[6], cf ft[9]) {
+  double r = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+  double d1r1 = 1.0 / r, d1r2 = d1r1 * d1r1, d1r3 = d1r2 * d1r1, d1r4 = d1r3 * d1r1;
+  cd z1 = mk(p.k1.im * r, -p.k1.re * r), z2 = mk(p.k2.im * r, -p.k2.re * r);
+  cd a2, a3, a4, a5, b2, b3, b4, b5;
+  zexp_2to5(p.steps, z1, a2, a3, a4, a5);
+  zexp_2to5(p.steps, z2, b2, b3, b4, b5);
+  cf A2 = cfc(a2 * d1r1), A3 = cfc(a3 * d1r2), A4 = cfc(a4 * d1r3), A5 = cfc(a5 * d1r4);
+  cf B2 = cfc(b2 * d1r1), B3 = cfc(b3 * d1r2), B4 = cfc(b4 * d1r3), B5 = cfc(b5 * d1r4);
+  ff D1 = ff_from(d1r1), D2 = ff_from(d1r2);
+  cf psi = cf_add(cf_add(cf_scale(q.psi[0], D1), q.psi[1]), B2);
+  psi = cf_fma(q.psi[2], A3, psi);
+  psi = cf_fma(q.psi[3], B3, psi);
+  psi = cf_fma(q.psi[4], A4, psi);
+  psi = cf_fma(q.psi[5], B4, psi);
+  cf chi = cf_add(cf_add(cf_scale(q.chi[0], D1), B2), cf_mul(q.chi[1], A2));
+  chi = cf_fma(q.chi[2], A3, chi);
+  chi = cf_fma(q.chi[3], B3, chi);
+  chi = cf_fma(q.chi[4], A4, chi);
+  chi = cf_fma(q.chi[5], B4, chi);
+  cf T1 = cf_add(cf_scale(q.T1[0], D2), q.T1[1]);
+  T1 = cf_fma(q.T1[2], A2, T1);
+  T1 = cf_fma(q.T1[3], B2, T1);
+  T1 = cf_fma(q.T1[4], A3, T1);
+  T1 = cf_fma(q.T1[5], B3, T1);
+  T1 = cf_fma(q.T1[6], A4, T1);
+  T1 = cf_fma(q.T1[7], B4, T1);
+  T1 = cf_fma(q.T1[8], A5, T1);
+  T1 = cf_fma(q.T1[9], B5, T1);
+  cf T2 = cf_add(cf_scale(q.T2[0], D2), q.T2[1]);
+  T2 = cf_fma(q.T2[2], B2, T2);
+  T2 = cf_fma(q.T2[3], A3, T2);
+  T2 = cf_fma(q.T2[4], B3, T2);
+  T2 = cf_fma(q.T2[5], A4, T2);
+  T2 = cf_fma(q.T2[6], B4, T2);
+  T2 = cf_fma(q.T2[7], A5, T2);
+  T2 = cf_fma(q.T2[8], B5, T2);
+  cf T3 = cf_add(cf_scale(q.T3[0], D2), q.T3[1]);
+  T3 = cf_fma(q.T3[2], A2, T3);
+  T3 = cf_fma(q.T3[3], A3, T3);
+  T3 = cf_fma(q.T3[4], B3, T3);
+  T3 = cf_fma(q.T3[5], A4, T3);
+  T3 = cf_fma(q.T3[6], B4, T3);
+  T3 = cf_fma(q.T3[7], A5, T3);
+  T3 = cf_fma(q.T3[8], B5, T3);
+  double drd[3] = {rv[0] * d1r1, rv[1] * d1r1, rv[2] * d1r1};
+  double drdn_d = drd[0] * n[0] + drd[1] * n[1] + drd[2] * n[2];
+  ff dr[3] = {ff_from(drd[0]), ff_from(drd[1]), ff_from(drd[2])};
+  ff nn[3] = {ff_from(n[0]), ff_from(n[1]), ff_from(n[2])};
+  ff drdn = ff_from(drdn_d);
+  cf T2dn = cf_scale(T2, drdn);
+  int s = 0;
+#pragma unroll
+  for (int il = 0; il < 3; ++il)
+#pragma unroll
+    for (int ik = 0; ik < 3; ++ik) {
+      ff rr = ff_mul(dr[il], dr[ik]);
+      cf t = cf_scale(T1, ff_mul(rr, drdn));
+      t = cf_fma_r(T2, ff_mul(dr[ik], nn[il]), t);
+      t = cf_fma_r(T3, ff_mul(dr[il], nn[ik]), t);
+      if (il == ik) t = cf_add(t, T2dn);
+      ft[3 * il + ik] = t;
+      if (ik >= il) {
+        cf u = cf_neg(cf_scale(chi, rr));
+        if (il == ik) u = cf_add(u, psi);
+        fu6[s++] = u;
+      }
+    }
+}
+
+struct alignas(16) ComboF {
+  cf fu[6], ft[9];
+  ff w[8];
+  int pair;
+};
+
+template <int WPB>
+__global__ void __launch_bounds__(WPB * 32) k_reg_mixed(DMesh m, PolHarmonic pol, const HarParF* pf, const ff* pphi_f,
+                                                        int nf, double* A, size_t lda, size_t astride, double* b,
+                                                        size_t bstride) {
+  __shared__ ComboF sm[WPB][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x / 32;
+  const long long gw = blockIdx.x * (long long)WPB + w;
+  if (gw >= (long long)m.ndn * nf) return;
+  const int dn = (int)(gw % m.ndn), f = (int)(gw / m.ndn);
+  ComboF* S = sm[w];
+  const HarParD& P = pol.p[f];
+  const HarParF& Q = pf[f];
+  for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
+    const int s0 = m.reg_start[cp], s1 = m.reg_start[cp + 1];
+    if (s0 == s1) continue;
+    const double* xi = m.cpx + 3 * (size_t)cp;
+    const long long P0 = m.reg_pt[s0], Qn = m.reg_pt[s1] - P0;
+    int cur = -1;
+    cf acc[kAcc];
+    for (int j = 0; j < kAcc; ++j) acc[j] = cf_zero();
+    for (long long base = 0; base < Qn; base += 32) {
+      long long c = base + lane;
+      if (c < Qn) {
+        int jp = find_le(m.reg_pt, s0, s1, P0 + c);
+        int pr = m.reg_pair[jp];
+        int e = pr & 0xFFFFFF, ps = pr >> 24;
+        size_t pt = (size_t)e * m.ptot + m.ps_off[ps] + (size_t)(P0 + c - m.reg_pt[jp]);
+        double rv[3] = {m.px[3 * pt] - xi[0], m.px[3 * pt + 1] - xi[1], m.px[3 * pt + 2] - xi[2]};
+        double n[3] = {m.pn[3 * pt], m.pn[3 * pt + 1], m.pn[3 * pt + 2]};
+        harela_point_f(P, Q, rv, n, S[lane].fu, S[lane].ft);
+        for (int k = 0; k < 8; ++k) S[lane].w[k] = pphi_f[8 * pt + k];
+        S[lane].pair = jp;
+      }
+      __syncwarp();
+      int nt = (int)min((long long)32, Qn - base);
+      for (int t = 0; t < nt; ++t) {
+        int jp = S[t].pair;
+        if (jp != cur) {
+          if (cur >= 0) {
+            cd a[kAcc];
+            for (int j = 0; j < kAcc; ++j) a[j] = mk(ff_to(acc[j].re), ff_to(acc[j].im));
+            flush_pair(m, pol, f, dn, m.reg_pair[cur] & 0xFFFFFF, a, A, lda, astride, b, bstride, nullptr);
+          }
+          cur = jp;
+          for (int j = 0; j < kAcc; ++j) acc[j] = cf_zero();
+        }
+#pragma unroll
+        for (int j = 0; j < kAcc; ++j) {
+          int o = lane + 32 * j;
+          if (o < kOut) {
+            cf v;
+            int kn;
+            if (o < 72) {
+              kn = o / 9;
+              v = S[t].ft[o % 9];
+            } else {
+              kn = (o - 72) / 6;
+              v = S[t].fu[(o - 72) % 6];
+            }
+            acc[j] = cf_fma_r(v, S[t].w[kn], acc[j]);
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (cur >= 0) {
+      cd a[kAcc];
+      for (int j = 0; j < kAcc; ++j) a[j] = mk(ff_to(acc[j].re), ff_to(acc[j].im));
+      flush_pair(m, pol, f, dn, m.reg_pair[cur] & 0xFFFFFF, a, A, lda, astride, b, bstride, nullptr);
+    }
+  }
 }
 
 }  // namespace mfb

@@ -430,7 +430,22 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   pol.p = dpar;
   AsmTimes tm;
   long long l0 = g_launches;
-  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n, &tm))) return rc;
+  const HarParF* pf = nullptr;
+  const ff* pphi_f = nullptr;
+  if (precision == 1) {
+    // mixed: regular pairs in double-float (df64 datasets made once per mesh)
+    const long long npp = 8LL * h->m.ne * h->m.ptot;
+    if (h->pphi_f.bytes < sizeof(ff) * npp) {
+      if ((rc = ensure(h->pphi_f, sizeof(ff) * npp))) return rc;
+      k_pphi_f<<<std::min(nblk(npp, 256), 152u * 16u), 256, 0, h->st>>>(h->m.pphi, (ff*)h->pphi_f.p, npp); ++g_launches;
+    }
+    if ((rc = ensure(h->parf, sizeof(HarParF) * n_freq))) return rc;
+    k_harpar_f<<<nblk(n_freq, 32), 32, 0, h->st>>>(dpar, (HarParF*)h->parf.p, n_freq); ++g_launches;
+    pf = (const HarParF*)h->parf.p;
+    pphi_f = (const ff*)h->pphi_f.p;
+  }
+  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n, &tm, pf, pphi_f)))
+    return rc;
   cudaEventRecord(a1, h->st);
   if ((rc = check_err(h))) return rc;
   float ams = 0;
