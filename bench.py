@@ -32,6 +32,19 @@ sys.path.insert(0, ROOT)
 
 METRIC = "harmonic BEM assemble+solve solves/sec vs plain FP64 GPU at rel-err ≤1e-8"
 WORKLOAD = "harela cube 8x8 quad8 per face, 3462 complex DOF, 20 frequencies a0=0.1..2.0"
+WORKLOAD_P = "harela surface patch 40x40 quad8 (20x20), 14883 complex DOF, a0=0.5"
+
+# Algorithmic work of the regular-pair assembly kernel (the dominant kernel):
+# bytes = the complex system A (n^2) and b (n) written once per frequency;
+# flops = FLOPS_PER_REGULAR_POINT real flops per regular quadrature point of the
+# time-harmonic kernel, counted on the binary64 formulation: distance and
+# powers 13, E_2..E_5 for both wavenumbers 272, psi/chi/TT1..TT3 320, 1/r
+# scalings and dr 24, u*/t* components 168, 120 complex accumulations 480.
+FLOPS_PER_REGULAR_POINT = 1280
+# DRAM bytes per frequency of that kernel from ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch of the 2-frequency profile case divided
+# by 2; profiles/k_reg_mixed_cube8.md).
+REG_TRAFFIC_PER_FREQ = None
 
 
 def _dist():
@@ -188,11 +201,18 @@ def run_gpu(args):
 
     if rank != 0:
         return 0
-    # accuracy of the timed path against FP64 (plain device LU, itself pinned to the oracle in tests)
-    Xp = R.sweep_harela(mat, om, precision="plain")
+    # the plain FP64 GPU path on the same sweep (FP64 assembly + FP64 LU), and
+    # the accuracy of the timed path against it (the plain path is itself
+    # pinned to the oracle in the tests)
     Xm = R.sweep_harela(mat, om, precision="mixed")
+    Xp = R.sweep_harela(mat, om, precision="plain")
+    plain_ms = []
+    for _ in range(max(1, args.steps // 2)):
+        Xp = R.sweep_harela(mat, om, precision="plain")
+        sp = R.last_stats
+        plain_ms.append(sp["ms_assemble"] + sp["ms_factor"] + sp["ms_solve"])
+    plain_step = statistics.mean(plain_ms)
     relerr = max(np.abs(Xm[i] - Xp[i]).max() / np.abs(Xp[i]).max() for i in range(nf))
-    plain_ms = R.last_stats["ms_factor"]
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "complex128 assembly / complex64 LU + FP64 refinement", "data": "synthetic",
@@ -205,7 +225,13 @@ def run_gpu(args):
                        "parallelism": f"replicas x{ws}"},
             "e2e": {"value": ws * nf / e2e_step, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches, "clocks": clk}
+            "gpu_launches": launches, "clocks": clk,
+            "plain_fp64_gpu": {"value": nf / (plain_step / 1e3), "unit": "solves/s", "ms_per_step": plain_step,
+                               "ms_factor": sp["ms_factor"], "ms_assemble": sp["ms_assemble"],
+                               "speedup_of_mixed": (nf / (per_step_ms / 1e3)) / (nf / (plain_step / 1e3))}}
+    line["roofline"] = roofline(st, n, nf)
+    if args.precision_form:
+        line["precision_form"] = precision_form()
     # cpu baseline: oracle on one frequency (bounded sample)
     try:
         t, cores = cpu_baseline_sample(deck, mat, om[len(om) // 2])
@@ -214,11 +240,58 @@ def run_gpu(args):
     except Exception as ex:  # the oracle must build on the host; report why not
         line["cpu_baseline"] = {"value": None, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"unavailable: {ex}"}
-    rf = os.environ.get("MFBEM_ROOFLINE_JSON")
-    if rf and os.path.exists(rf):
-        line["roofline"] = json.load(open(rf))
     print(json.dumps(line), flush=True)
     return 0
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def roofline(st, n, nf):
+    """Roofline of the dominant kernel (regular-pair assembly, one launch for
+    all nf frequencies), timed by CUDA events on the library's stream."""
+    pk, src = _peaks()
+    t = st["ms_regular"] / 1e3
+    alg_bytes = nf * (n * n + n) * 16
+    achieved = alg_bytes / t / 1e9
+    pts = st["points_regular"] * nf
+    tfl = pts * FLOPS_PER_REGULAR_POINT / t / 1e12
+    return {"kernel": "k_reg_mixed (regular pairs, all frequencies)", "bound": "hbm", "achieved": achieved,
+            "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "peak_source": src,
+            "traffic": (REG_TRAFFIC_PER_FREQ * nf) if REG_TRAFFIC_PER_FREQ else None,
+            "algorithmic_bytes": alg_bytes, "ms": st["ms_regular"],
+            "compute": {"points": pts, "flops_per_point": FLOPS_PER_REGULAR_POINT, "achieved_tflops": tfl,
+                        "note": "SIMT-compute bound (double-float on the FP32 pipe, binary64 for x - x_i); "
+                                "HBM and tensor pipes are not the limit of this kernel"}}
+
+
+def precision_form():
+    """The 14883-DOF surface patch at a0=0.5: one mixed solve against one plain
+    FP64 solve on the GPU, and their difference."""
+    from multifebe_gb300 import meshgen as M, BemRegion
+    deck, mat, om = M.workload(3)
+    R = BemRegion(deck)
+    Xm = R.sweep_harela(mat, om, precision="mixed")
+    Xm = R.sweep_harela(mat, om, precision="mixed")
+    sm = dict(R.last_stats)
+    Xp = R.sweep_harela(mat, om, precision="plain")
+    sp = dict(R.last_stats)
+    R.close()
+    tm = sm["ms_assemble"] + sm["ms_factor"] + sm["ms_solve"]
+    tp = sp["ms_assemble"] + sp["ms_factor"] + sp["ms_solve"]
+    return {"workload": WORKLOAD_P, "n_dof": int(Xm.shape[1]),
+            "mixed": {"value": 1e3 / tm, "unit": "solves/s", "ms_assemble": sm["ms_assemble"],
+                      "ms_factor": sm["ms_factor"], "ms_solve": sm["ms_solve"],
+                      "refinement_iterations": sm["refinement_iterations"],
+                      "max_backward_error": sm["max_backward_error"]},
+            "plain_fp64": {"value": 1e3 / tp, "unit": "solves/s", "ms_assemble": sp["ms_assemble"],
+                           "ms_factor": sp["ms_factor"], "ms_solve": sp["ms_solve"]},
+            "speedup_of_mixed": tp / tm,
+            "rel_err_mixed_vs_fp64": float(np.abs(Xm - Xp).max() / np.abs(Xp).max())}
 
 
 def profile_case(nf):
@@ -244,6 +317,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-precision-form", dest="precision_form", action="store_false",
+                    help="skip the 14883-DOF surface-patch mixed/plain comparison")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="profiling helper: run the benchmark mesh for this many frequencies twice, print stats, exit")
     args = ap.parse_args()

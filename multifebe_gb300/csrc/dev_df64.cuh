@@ -73,13 +73,17 @@ namespace mfb {
 // ---------------------------------------------------------------------------
 // Elementary functions in df64, written from their Taylor series with
 // Cody-Waite argument reduction (W. J. Cody and W. Waite, "Software Manual for
-// the Elementary Functions", 1980): exp on |r| <= ln2/2, sin/cos on |t| <= pi/4.
-// Constants are split into hi + lo binary32 pairs on the host (DfConst).
+// the Elementary Functions", 1980): e^x = 2^k e^r with |r| <= ln2/2, and
+// sin/cos of t = x - q pi/2 with |t| <= pi/4. The reduction constants are held
+// as three binary32 parts (72 bits), so the reduced argument keeps full df64
+// accuracy for |q| up to 2^20. Constants are split on the host (df_constants_host).
 // ---------------------------------------------------------------------------
 struct DfConst {
-  ff inv_fact[24];  // 1/k!
-  ff inv[24];       // 1/k
-  ff ln2, pio2;     // ln 2, pi/2
+  ff inv_fact[20];  // 1/k!
+  ff inv[24];       // 1/k (inv[0] unused)
+  ff sin_c[9];      // (-1)^k / (2k+1)!, k = 0..8
+  ff cos_c[10];     // (-1)^k / (2k)!,   k = 0..9
+  float ln2[3], pio2[3];
 };
 #ifdef __CUDACC__
 __constant__ DfConst c_df;
@@ -91,62 +95,89 @@ inline DfConst df_constants_host() {
     float l = (float)(x - (long double)h);
     return ff{h, l};
   };
+  auto split3 = [](long double x, float* o) {
+    o[0] = (float)x;
+    long double r = x - (long double)o[0];
+    o[1] = (float)r;
+    o[2] = (float)(r - (long double)o[1]);
+  };
   long double f = 1.0L;
-  for (int k = 0; k < 24; ++k) {
+  for (int k = 0; k < 20; ++k) {
     if (k > 0) f *= (long double)k;
     c.inv_fact[k] = split(1.0L / f);
-    c.inv[k] = k > 0 ? split(1.0L / (long double)k) : ff{0.0f, 0.0f};
   }
-  c.ln2 = split(0.693147180559945309417232121458176568L);
-  c.pio2 = split(1.570796326794896619231321691639751442L);
+  for (int k = 0; k < 24; ++k) c.inv[k] = k > 0 ? split(1.0L / (long double)k) : ff{0.0f, 0.0f};
+  long double g = 1.0L;  // (2k)!
+  for (int k = 0; k < 10; ++k) {
+    if (k > 0) g *= (long double)(2 * k - 1) * (long double)(2 * k);
+    c.cos_c[k] = split((k & 1 ? -1.0L : 1.0L) / g);
+    if (k < 9) c.sin_c[k] = split((k & 1 ? -1.0L : 1.0L) / (g * (long double)(2 * k + 1)));
+  }
+  split3(0.693147180559945309417232121458176568L, c.ln2);
+  split3(1.570796326794896619231321691639751442L, c.pio2);
   return c;
 }
 
-// e^x for |x| <= ~40
-__device__ __forceinline__ ff ff_exp(ff x) {
-  const float k = rintf(__fmul_rn(x.hi, 1.44269504088896340736f));
-  ff r = ff_sub(x, ff_mul(ff{k, 0.0f}, c_df.ln2));
-  // sum_{i<=13} r^i / i!
-  ff p = c_df.inv_fact[13];
-#pragma unroll
-  for (int i = 12; i >= 0; --i) p = ff_fma(p, r, c_df.inv_fact[i]);
-  const int ki = (int)k;
-  return ff{ldexpf(p.hi, ki), ldexpf(p.lo, ki)};
+#ifdef __CUDACC__
+// x - q (c0 + c1 + c2) with q an integer-valued float (|q| < 2^20)
+__device__ __forceinline__ ff ff_reduce(ff x, float q, const float c[3]) {
+  float p0 = __fmul_rn(q, c[0]), e0 = __fmaf_rn(q, c[0], -p0);  // q c0 = p0 + e0 exactly
+  float p1 = __fmul_rn(q, c[1]), e1 = __fmaf_rn(q, c[1], -p1);
+  ff t = ff_sub(x, ff{p0, e0});
+  t = ff_sub(t, ff{p1, e1});
+  return ff_sub(t, ff{__fmul_rn(q, c[2]), 0.0f});
 }
-// sin x, cos x for |x| <= ~1e4
+// sqrt(a), a > 0: one Newton correction of the binary32 root
+__device__ __forceinline__ ff ff_sqrt(ff a) {
+  float x = __fsqrt_rn(a.hi);
+  float p = __fmul_rn(x, x), e = __fmaf_rn(x, x, -p);
+  ff d = ff_sub(a, ff{p, e});
+  float c = __fdiv_rn(d.hi, __fmul_rn(2.0f, x));
+  float h = __fadd_rn(x, c);
+  return ff{h, __fsub_rn(c, __fsub_rn(h, x))};
+}
+// 1 / b: one Newton correction of the binary32 reciprocal
+__device__ __forceinline__ ff ff_rcp(ff b) {
+  float y = __frcp_rn(b.hi);
+  ff e = ff_sub(ff{1.0f, 0.0f}, ff_mul(b, ff{y, 0.0f}));
+  float c = __fmul_rn(e.hi, y);
+  float h = __fadd_rn(y, c);
+  return ff{h, __fsub_rn(c, __fsub_rn(h, y))};
+}
+// e^x for -87 <= x <= 80 (0 below -87, x clamped to 80 above)
+__device__ __forceinline__ ff ff_exp(ff x) {
+  if (x.hi < -87.0f) return ff{0.0f, 0.0f};
+  if (x.hi > 80.0f) x = ff{80.0f, 0.0f};
+  const float k = rintf(__fmul_rn(x.hi, 1.44269504088896340736f));
+  ff r = ff_reduce(x, k, c_df.ln2);
+  // sum_{i<=13} r^i / i!, |r| <= 0.35: truncation below 2e-18
+  ff p = c_df.inv_fact[13];
+#pragma unroll 1
+  for (int i = 12; i >= 0; --i) p = ff_fma(p, r, c_df.inv_fact[i]);
+  // 2^k as a binary32 (k in [-126, 116] for -87 <= x <= 80): exact scaling
+  const float s2 = __int_as_float(((int)k + 127) << 23);
+  return ff{__fmul_rn(p.hi, s2), __fmul_rn(p.lo, s2)};
+}
+// sin x, cos x for |x| < 1e6
 __device__ __forceinline__ void ff_sincos(ff x, ff* s, ff* c) {
   const float q = rintf(__fmul_rn(x.hi, 0.636619772367581343076f));
-  ff t = ff_sub(x, ff_mul(ff{q, 0.0f}, c_df.pio2));
+  ff t = ff_reduce(x, q, c_df.pio2);
   ff t2 = ff_mul(t, t);
-  // sin t = t (1 - t^2/3! + ... - t^18/19!)
-  ff ps = ff_neg(c_df.inv_fact[19]);
-  ps = ff_fma(ps, t2, c_df.inv_fact[17]);
-  ps = ff_fma(ps, t2, ff_neg(c_df.inv_fact[15]));
-  ps = ff_fma(ps, t2, c_df.inv_fact[13]);
-  ps = ff_fma(ps, t2, ff_neg(c_df.inv_fact[11]));
-  ps = ff_fma(ps, t2, c_df.inv_fact[9]);
-  ps = ff_fma(ps, t2, ff_neg(c_df.inv_fact[7]));
-  ps = ff_fma(ps, t2, c_df.inv_fact[5]);
-  ps = ff_fma(ps, t2, ff_neg(c_df.inv_fact[3]));
-  ps = ff_fma(ps, t2, c_df.inv_fact[1]);
-  ff sn = ff_mul(ps, t);
-  // cos t = 1 - t^2/2! + t^4/4! - ... + t^18/18!
-  ff pc = c_df.inv_fact[18];
-  pc = ff_fma(pc, t2, ff_neg(c_df.inv_fact[16]));
-  pc = ff_fma(pc, t2, c_df.inv_fact[14]);
-  pc = ff_fma(pc, t2, ff_neg(c_df.inv_fact[12]));
-  pc = ff_fma(pc, t2, c_df.inv_fact[10]);
-  pc = ff_fma(pc, t2, ff_neg(c_df.inv_fact[8]));
-  pc = ff_fma(pc, t2, c_df.inv_fact[6]);
-  pc = ff_fma(pc, t2, ff_neg(c_df.inv_fact[4]));
-  pc = ff_fma(pc, t2, c_df.inv_fact[2]);
-  pc = ff_fma(pc, t2, ff_neg(c_df.inv_fact[0]));
-  ff cs = ff_neg(pc);
+  // |t| <= pi/4: sin to t^17, cos to t^18 (truncation below 1e-19)
+  ff ps = c_df.sin_c[8], pc = c_df.cos_c[9];
+#pragma unroll 1
+  for (int k = 7; k >= 0; --k) {
+    ps = ff_fma(ps, t2, c_df.sin_c[k]);
+    pc = ff_fma(pc, t2, c_df.cos_c[k + 1]);
+  }
+  pc = ff_fma(pc, t2, c_df.cos_c[0]);
+  const ff sn = ff_mul(ps, t), cs = pc;
   const int qi = ((int)q) & 3;
   if (qi == 0) { *s = sn; *c = cs; }
   else if (qi == 1) { *s = cs; *c = ff_neg(sn); }
   else if (qi == 2) { *s = ff_neg(sn); *c = ff_neg(cs); }
   else { *s = ff_neg(cs); *c = sn; }
 }
+#endif
 
 }  // namespace mfb

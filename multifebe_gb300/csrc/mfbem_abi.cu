@@ -59,7 +59,7 @@ struct mfbem_handle {
   int ndof = 0, ne = 0, nn = 0;
   cudaStream_t st = nullptr;
   cublasHandle_t blas = nullptr;
-  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f;
+  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, Af;
   mfbem_stats stats{};
   long long pts_reg = 0, pts_adp = 0, pts_sing = 0;
   int* d_err = nullptr;
@@ -95,6 +95,8 @@ static int init_tables() {
   if (g_tables_ready) return 0;
   const GLTables& t = host_gauss_tables();
   CK(cudaMemcpyToSymbol(c_gl, &t, sizeof(GLTables)));
+  const DfConst dc = df_constants_host();
+  CK(cudaMemcpyToSymbol(c_df, &dc, sizeof(DfConst)));
   g_tables_ready = true;
   return 0;
 }
@@ -383,7 +385,7 @@ extern "C" int mfbem_mesh_release(mfbem_handle* h) {
   cudaDeviceSynchronize();
   for (void* p : h->owned) cudaFree(p);
   for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu, &h->parf,
-                    &h->pphi_f})
+                    &h->pphi_f, &h->Af})
     if (b->p) cudaFree(b->p);
   if (h->blas) cublasDestroy(h->blas);
   if (h->st) cudaStreamDestroy(h->st);
@@ -436,7 +438,7 @@ struct AsmTimes {
 template <class POL>
 static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, int nf, double* A, size_t lda,
                            size_t astride, double* b, size_t bstride, AsmTimes* tm = nullptr,
-                           const HarParF* pf = nullptr, const ff* pphi_f = nullptr) {
+                           const HarParF* pf = nullptr, const ff* dsf = nullptr, float4* Af = nullptr) {
   const DMesh& m = h->m;
   constexpr int WPB = 4;
   long long nw = (long long)m.ndn * nf;
@@ -445,8 +447,8 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
   if (tm) cudaEventRecord(tm->ev[0], h->st);
   if (m.nreg > 0) {
     if constexpr (std::is_same<POL, PolHarmonic>::value) {
-      if (pf && pphi_f) {
-        k_reg_mixed<WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, pf, pphi_f, nf, A, lda, astride, b, bstride);
+      if (pf && dsf && Af) {
+        k_reg_mixed<WPB><<<g, WPB * 32, 0, h->st>>>(m, pf, dsf, nf, Af, lda, astride / 2, b, bstride);
       } else {
         k_reg<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
       }
@@ -462,6 +464,11 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
   if (m.nsing > 0) { k_sing<POL, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride); ++g_launches; }
   if (tm) cudaEventRecord(tm->ev[3], h->st);
   k_free<POL><<<nblk(nw, 128), 128, 0, h->st>>>(m, pol, d_nu, nf, A, lda, astride, b, bstride, h->d_err); ++g_launches;
+  if (Af && m.nreg > 0) {
+    // mixed: fold the df64 regular-pair sums into the binary64 systems
+    const long long ne_ = (long long)(astride / 2) * nf;
+    k_add_ff<<<152 * 16, 256, 0, h->st>>>((double2*)A, Af, ne_); ++g_launches;
+  }
   if (tm) cudaEventRecord(tm->ev[4], h->st);
   CK(cudaGetLastError());
   return 0;
@@ -564,6 +571,50 @@ extern "C" int mfbem_assemble_harela(mfbem_handle* h, const double lambda[2], co
   PolHarmonic pol;
   pol.p = (const HarParD*)h->par.p;
   return assemble_common<true>(h, &pol, nu, A, lda, b, flags);
+}
+
+// ---------------------------------------------------------------------------
+// Test hook (not part of the reference interface): E_2..E_5 of n values z by
+// the binary64 path (zexp_2to5) and the double-float path (zexp_2to5_ff).
+// z: [n][2]; e64, e32: [n][4][2] (E2..E5, re/im).
+// ---------------------------------------------------------------------------
+__global__ void k_zexp_check(const double* z, int n, ZexpSteps steps, double* e64, double* eff) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  cd zz = mk(z[2 * i], z[2 * i + 1]);
+  cd E[4];
+  zexp_2to5(steps, zz, E[0], E[1], E[2], E[3]);
+  float t2[16];
+  for (int k = 0; k < 16; ++k) t2[k] = (float)steps.t2[k];
+  cf F[4];
+  zexp_2to5_ff(t2, cf_from(zz.re, zz.im), F[0], F[1], F[2], F[3]);
+  for (int k = 0; k < 4; ++k) {
+    e64[8 * i + 2 * k] = E[k].re;
+    e64[8 * i + 2 * k + 1] = E[k].im;
+    eff[8 * i + 2 * k] = ff_to(F[k].re);
+    eff[8 * i + 2 * k + 1] = ff_to(F[k].im);
+  }
+}
+extern "C" int mfbem_internal_zexp(int32_t n, const double* z, double* e64, double* eff) {
+  g_err.clear();
+  if (n <= 0 || !z || !e64 || !eff) return fail(MFBEM_EARG, "invalid argument");
+  int rc = init_tables();
+  if (rc) return rc;
+  DevBuf dz, d1, d2;
+  if ((rc = ensure(dz, 16 * (size_t)n)) || (rc = ensure(d1, 64 * (size_t)n)) || (rc = ensure(d2, 64 * (size_t)n)))
+    return rc;
+  cudaError_t e = cudaMemcpy(dz.p, z, 16 * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_zexp_check<<<nblk(n, 128), 128>>>((const double*)dz.p, n, zexp_thresholds(), (double*)d1.p, (double*)d2.p); ++g_launches;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(e64, d1.p, 64 * (size_t)n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(eff, d2.p, 64 * (size_t)n, cudaMemcpyDeviceToHost);
+  cudaFree(dz.p);
+  cudaFree(d1.p);
+  cudaFree(d2.p);
+  if (e != cudaSuccess) return fail(MFBEM_ECUDA, std::string("zexp check: ") + cudaGetErrorString(e));
+  return 0;
 }
 
 #include "mfbem_solve.cuh"

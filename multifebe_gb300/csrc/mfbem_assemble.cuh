@@ -556,106 +556,155 @@ __global__ void k_free(DMesh m, POL pol, const double* nu /* complex, per freque
 }
 
 // ============================================================================
-// Mixed-precision regular pairs (time-harmonic). The exponential decomposition
-// E_n and the geometry stay in binary64; the linear combinations forming psi,
-// chi, TT1..TT3, the fundamental solutions and the quadrature sums run in
-// double-float arithmetic (dev_df64.cuh) on the FP32 pipe. Used by the mixed
-// sweep only: regular (far-field) pairs have smooth integrands, and double-float
-// keeps them at ~1e-14 relative; singular and quasi-singular pairs stay FP64.
+// Mixed-precision regular pairs (time-harmonic). Only x - x_i is formed in
+// binary64; the distance, the decomposed exponentials E_n of both wavenumbers,
+// the linear combinations forming psi, chi, TT1..TT3, the fundamental solutions
+// and the quadrature sums run in double-float arithmetic (dev_df64.cuh) on the
+// FP32 pipe. Used by the mixed sweep only: regular (far-field) pairs have smooth
+// integrands, and double-float keeps them at ~1e-14 relative; singular and
+// quasi-singular pairs stay FP64.
 // ============================================================================
 
+// Coefficients of one frequency in double-float. The five combinations
+// X = psi, chi, TT1, TT2, TT3 of bem_harela3d.f90:654-688 are written as
+//   X = c0[X] r^-p + c1[X] + sum_{w=1,2} sum_{n=2..5} cm[w][n-2][X] E_n(-i k_w r) r^-(n-1)
+// (p = 1 for psi and chi, 2 for TT1..TT3); cm holds the reference's psi(6),
+// chi(6), T1(10), T2(9), T3(9) at the places of the terms they multiply and
+// zero elsewhere, so one loop over (w, n) evaluates all five.
 struct HarParF {
-  cf psi[6], chi[6], T1[10], T2[9], T3[9];
+  cf k1, k2, cte_u, cte_t;
+  cf c0[5], c1[5];
+  cf cm[2][4][5];
+  float t2[16];  // E_n series-length steps on |z|^2 (ZexpSteps as binary32)
 };
 __global__ void k_harpar_f(const HarParD* p, HarParF* out, int nf) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
+  const HarParD& P = p[f];
   HarParF o;
-  for (int i = 0; i < 6; ++i) o.psi[i] = cf_from(p[f].psi[i].re, p[f].psi[i].im);
-  for (int i = 0; i < 6; ++i) o.chi[i] = cf_from(p[f].chi[i].re, p[f].chi[i].im);
-  for (int i = 0; i < 10; ++i) o.T1[i] = cf_from(p[f].T1[i].re, p[f].T1[i].im);
-  for (int i = 0; i < 9; ++i) o.T2[i] = cf_from(p[f].T2[i].re, p[f].T2[i].im);
-  for (int i = 0; i < 9; ++i) o.T3[i] = cf_from(p[f].T3[i].re, p[f].T3[i].im);
+  auto c = [](const cd& v) { return cf_from(v.re, v.im); };
+  const cf Z = cf_zero(), ONE = cf{ff{1.0f, 0.0f}, ff_zero()};
+  o.k1 = c(P.k1);
+  o.k2 = c(P.k2);
+  o.cte_u = c(P.cte_u);
+  o.cte_t = c(P.cte_t);
+  // targets 0 psi, 1 chi, 2 TT1, 3 TT2, 4 TT3
+  o.c0[0] = c(P.psi[0]); o.c0[1] = c(P.chi[0]); o.c0[2] = c(P.T1[0]); o.c0[3] = c(P.T2[0]); o.c0[4] = c(P.T3[0]);
+  o.c1[0] = c(P.psi[1]); o.c1[1] = Z;           o.c1[2] = c(P.T1[1]); o.c1[3] = c(P.T2[1]); o.c1[4] = c(P.T3[1]);
+  // wavenumber k1 (w = 0), n = 2..5
+  const cf k1t[4][5] = {{Z, c(P.chi[1]), c(P.T1[2]), Z, c(P.T3[2])},
+                        {c(P.psi[2]), c(P.chi[2]), c(P.T1[4]), c(P.T2[3]), c(P.T3[3])},
+                        {c(P.psi[4]), c(P.chi[4]), c(P.T1[6]), c(P.T2[5]), c(P.T3[5])},
+                        {Z, Z, c(P.T1[8]), c(P.T2[7]), c(P.T3[7])}};
+  // wavenumber k2 (w = 1)
+  const cf k2t[4][5] = {{ONE, ONE, c(P.T1[3]), c(P.T2[2]), Z},
+                        {c(P.psi[3]), c(P.chi[3]), c(P.T1[5]), c(P.T2[4]), c(P.T3[4])},
+                        {c(P.psi[5]), c(P.chi[5]), c(P.T1[7]), c(P.T2[6]), c(P.T3[6])},
+                        {Z, Z, c(P.T1[9]), c(P.T2[8]), c(P.T3[8])}};
+  for (int n = 0; n < 4; ++n)
+    for (int t = 0; t < 5; ++t) {
+      o.cm[0][n][t] = k1t[n][t];
+      o.cm[1][n][t] = k2t[n][t];
+    }
+  for (int i = 0; i < 16; ++i) o.t2[i] = (float)P.steps.t2[i];
   out[f] = o;
 }
-// phi*J*w of the element datasets as double-float, once per mesh
+// binary64 dataset arrays (phi*J*w, unit normals) as double-float, once per mesh
 __global__ void k_pphi_f(const double* pphi, ff* out, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     out[i] = ff_from(pphi[i]);
 }
 
-__device__ __forceinline__ cf cfc(const cd& v) { return cf_from(v.re, v.im); }
+__device__ __forceinline__ int zexp_nterms_f(const float* t2, float az2) {
+  if (az2 <= 1e-12f) return 1;
+  int lo = 0, hi = 15;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (az2 < t2[mid]) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo + 1;
+}
 
-// u*, t* (without constants) at one regular point, df64 combination stage
-__device__ __forceinline__ void harela_point_f(const HarParD& p, const HarParF& q, const double rv[3], const double n[3],
-                                               cf fu6[6], cf ft[9]) {
-  double r = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
-  double d1r1 = 1.0 / r, d1r2 = d1r1 * d1r1, d1r3 = d1r2 * d1r1, d1r4 = d1r3 * d1r1;
-  cd z1 = mk(p.k1.im * r, -p.k1.re * r), z2 = mk(p.k2.im * r, -p.k2.re * r);
-  cd a2, a3, a4, a5, b2, b3, b4, b5;
-  zexp_2to5(p.steps, z1, a2, a3, a4, a5);
-  zexp_2to5(p.steps, z2, b2, b3, b4, b5);
-  cf A2 = cfc(a2 * d1r1), A3 = cfc(a3 * d1r2), A4 = cfc(a4 * d1r3), A5 = cfc(a5 * d1r4);
-  cf B2 = cfc(b2 * d1r1), B3 = cfc(b3 * d1r2), B4 = cfc(b4 * d1r3), B5 = cfc(b5 * d1r4);
-  ff D1 = ff_from(d1r1), D2 = ff_from(d1r2);
-  cf psi = cf_add(cf_add(cf_scale(q.psi[0], D1), q.psi[1]), B2);
-  psi = cf_fma(q.psi[2], A3, psi);
-  psi = cf_fma(q.psi[3], B3, psi);
-  psi = cf_fma(q.psi[4], A4, psi);
-  psi = cf_fma(q.psi[5], B4, psi);
-  cf chi = cf_add(cf_add(cf_scale(q.chi[0], D1), B2), cf_mul(q.chi[1], A2));
-  chi = cf_fma(q.chi[2], A3, chi);
-  chi = cf_fma(q.chi[3], B3, chi);
-  chi = cf_fma(q.chi[4], A4, chi);
-  chi = cf_fma(q.chi[5], B4, chi);
-  cf T1 = cf_add(cf_scale(q.T1[0], D2), q.T1[1]);
-  T1 = cf_fma(q.T1[2], A2, T1);
-  T1 = cf_fma(q.T1[3], B2, T1);
-  T1 = cf_fma(q.T1[4], A3, T1);
-  T1 = cf_fma(q.T1[5], B3, T1);
-  T1 = cf_fma(q.T1[6], A4, T1);
-  T1 = cf_fma(q.T1[7], B4, T1);
-  T1 = cf_fma(q.T1[8], A5, T1);
-  T1 = cf_fma(q.T1[9], B5, T1);
-  cf T2 = cf_add(cf_scale(q.T2[0], D2), q.T2[1]);
-  T2 = cf_fma(q.T2[2], B2, T2);
-  T2 = cf_fma(q.T2[3], A3, T2);
-  T2 = cf_fma(q.T2[4], B3, T2);
-  T2 = cf_fma(q.T2[5], A4, T2);
-  T2 = cf_fma(q.T2[6], B4, T2);
-  T2 = cf_fma(q.T2[7], A5, T2);
-  T2 = cf_fma(q.T2[8], B5, T2);
-  cf T3 = cf_add(cf_scale(q.T3[0], D2), q.T3[1]);
-  T3 = cf_fma(q.T3[2], A2, T3);
-  T3 = cf_fma(q.T3[3], A3, T3);
-  T3 = cf_fma(q.T3[4], B3, T3);
-  T3 = cf_fma(q.T3[5], A4, T3);
-  T3 = cf_fma(q.T3[6], B4, T3);
-  T3 = cf_fma(q.T3[7], A5, T3);
-  T3 = cf_fma(q.T3[8], B5, T3);
-  double drd[3] = {rv[0] * d1r1, rv[1] * d1r1, rv[2] * d1r1};
-  double drdn_d = drd[0] * n[0] + drd[1] * n[1] + drd[2] * n[2];
-  ff dr[3] = {ff_from(drd[0]), ff_from(drd[1]), ff_from(drd[2])};
-  ff nn[3] = {ff_from(n[0]), ff_from(n[1]), ff_from(n[2])};
-  ff drdn = ff_from(drdn_d);
-  cf T2dn = cf_scale(T2, drdn);
-  int s = 0;
-#pragma unroll
-  for (int il = 0; il < 3; ++il)
-#pragma unroll
-    for (int ik = 0; ik < 3; ++ik) {
-      ff rr = ff_mul(dr[il], dr[ik]);
-      cf t = cf_scale(T1, ff_mul(rr, drdn));
-      t = cf_fma_r(T2, ff_mul(dr[ik], nn[il]), t);
-      t = cf_fma_r(T3, ff_mul(dr[il], nn[ik]), t);
-      if (il == ik) t = cf_add(t, T2dn);
-      ft[3 * il + ik] = t;
-      if (ik >= il) {
-        cf u = cf_neg(cf_scale(chi, rr));
-        if (il == ik) u = cf_add(u, psi);
-        fu6[s++] = u;
-      }
+// E_2..E_5 of z in double-float: the series tail of numerical.f90:1286-1301 for
+// |z| <= 1 (same number of terms), e^z minus its leading terms above.
+__device__ __forceinline__ void zexp_2to5_ff(const float* t2, cf z, cf& E2, cf& E3, cf& E4, cf& E5) {
+  const float az2 = __fmaf_rn(z.re.hi, z.re.hi, __fmul_rn(z.im.hi, z.im.hi));
+  cf z2 = cf_mul(z, z), z3 = cf_mul(z2, z), z4 = cf_mul(z3, z);
+  if (az2 <= 1.0f) {
+    const int N = zexp_nterms_f(t2, az2) + 6;
+    cf t = cf{ff{1.0f, 0.0f}, ff_zero()};
+#pragma unroll 1
+    for (int k = N; k >= 7; --k) {
+      t = cf_scale(cf_mul(t, z), c_df.inv[k]);
+      t.re = ff_add(t.re, ff{1.0f, 0.0f});
     }
+    cf z5 = cf_mul(z4, z), z6 = cf_mul(z5, z);
+    cf e6 = cf_mul(cf_scale(z6, c_df.inv_fact[6]), t);
+    E5 = cf_add(e6, cf_scale(z5, c_df.inv_fact[5]));
+    E4 = cf_add(E5, cf_scale(z4, c_df.inv_fact[4]));
+    E3 = cf_add(E4, cf_scale(z3, c_df.inv_fact[3]));
+    E2 = cf_add(E3, cf_scale(z2, c_df.inv_fact[2]));
+  } else {
+    ff ex = ff_exp(z.re), sn, cs;
+    ff_sincos(z.im, &sn, &cs);
+    cf e0 = cf{ff_mul(ex, cs), ff_mul(ex, sn)};
+    e0.re = ff_sub(e0.re, ff{1.0f, 0.0f});
+    E2 = cf_add(e0, cf_neg(z));
+    E3 = cf_add(E2, cf_neg(cf_scale(z2, c_df.inv_fact[2])));
+    E4 = cf_add(E3, cf_neg(cf_scale(z3, c_df.inv_fact[3])));
+    E5 = cf_add(E4, cf_neg(cf_scale(z4, c_df.inv_fact[4])));
+  }
+}
+
+__device__ __forceinline__ ff sel3(const ff v[3], int i) { return i == 0 ? v[0] : (i == 1 ? v[1] : v[2]); }
+__device__ __forceinline__ cf sel4(cf a, cf b, cf c, cf d, int i) { return i == 0 ? a : (i == 1 ? b : (i == 2 ? c : d)); }
+
+// u*, t* (without constants) at one regular point (bem_harela3d.f90:654-688),
+// all in double-float, written to fu6 (the six il <= ik components of u*) and
+// ft (9). Loops are kept rolled: the kernel is bound by instruction fetch when
+// this function is fully unrolled.
+__device__ __forceinline__ void harela_point_ff(const HarParF& q, const ff rv[3], const ff n[3], cf* fu6, cf* ft) {
+  const ff r2 = ff_add(ff_add(ff_mul(rv[0], rv[0]), ff_mul(rv[1], rv[1])), ff_mul(rv[2], rv[2]));
+  const ff r = ff_sqrt(r2);
+  const ff d1r1 = ff_rcp(r), d1r2 = ff_mul(d1r1, d1r1);
+  cf X[5];
+#pragma unroll
+  for (int t = 0; t < 5; ++t) X[t] = cf_add(cf_scale(q.c0[t], t < 2 ? d1r1 : d1r2), q.c1[t]);
+#pragma unroll 1
+  for (int w = 0; w < 2; ++w) {
+    const cf k = w ? q.k2 : q.k1;
+    const cf z = cf{ff_mul(k.im, r), ff_neg(ff_mul(k.re, r))};  // -i k r
+    cf e2, e3, e4, e5;
+    zexp_2to5_ff(q.t2, z, e2, e3, e4, e5);
+    ff rp = d1r1;
+#pragma unroll 1
+    for (int nn = 0; nn < 4; ++nn) {
+      const cf src = cf_scale(sel4(e2, e3, e4, e5, nn), rp);
+#pragma unroll
+      for (int t = 0; t < 5; ++t) X[t] = cf_fma(q.cm[w][nn][t], src, X[t]);
+      rp = ff_mul(rp, d1r1);
+    }
+  }
+  const cf psi = X[0], chi = X[1], T1 = X[2], T2 = X[3], T3 = X[4];
+  const ff dr[3] = {ff_mul(rv[0], d1r1), ff_mul(rv[1], d1r1), ff_mul(rv[2], d1r1)};
+  const ff drdn = ff_add(ff_add(ff_mul(dr[0], n[0]), ff_mul(dr[1], n[1])), ff_mul(dr[2], n[2]));
+#pragma unroll 1
+  for (int c = 0; c < 9; ++c) {
+    const int il = c / 3, ik = c - 3 * il;
+    const ff dri = sel3(dr, il), drk = sel3(dr, ik), ni = sel3(n, il), nk = sel3(n, ik);
+    const ff rr = ff_mul(dri, drk);
+    const ff s1 = il == ik ? ff_add(ff_mul(drk, ni), drdn) : ff_mul(drk, ni);
+    cf t = cf_scale(T1, ff_mul(rr, drdn));
+    t = cf_fma_r(T2, s1, t);
+    t = cf_fma_r(T3, ff_mul(dri, nk), t);
+    ft[c] = t;
+    if (ik >= il) {
+      cf u = cf_neg(cf_scale(chi, rr));
+      if (il == ik) u = cf_add(u, psi);
+      fu6[ik + (il == 1 ? 2 : (il == 2 ? 3 : 0))] = u;
+    }
+  }
 }
 
 struct alignas(16) ComboF {
@@ -664,18 +713,72 @@ struct alignas(16) ComboF {
   int pair;
 };
 
+__device__ __forceinline__ cf cf_sub(cf a, cf b) { return cf_add(a, cf_neg(b)); }
+__device__ __forceinline__ cf cval_f(const ff* dcv_f, int dof) { return cf{dcv_f[2 * (size_t)dof], dcv_f[2 * (size_t)dof + 1]}; }
+// df64 complex entry {re.hi, re.lo, im.hi, im.lo} += v
+__device__ __forceinline__ void addAf(float4* Af, size_t idx, cf v) {
+  float4 a = Af[idx];
+  ff re = ff_add(ff{a.x, a.y}, v.re), im = ff_add(ff{a.z, a.w}, v.im);
+  Af[idx] = make_float4(re.hi, re.lo, im.hi, im.lo);
+}
+__device__ __forceinline__ void add3(cf bc[3], int i, cf v) {
+  if (i == 0) bc[0] = cf_add(bc[0], v);
+  else if (i == 1) bc[1] = cf_add(bc[1], v);
+  else bc[2] = cf_add(bc[2], v);
+}
+
+// scale, reverse and scatter this lane's outputs of one pair (the scatter of
+// flush_pair in double-float): A entries into the df64 buffer Af, prescribed
+// values into the lane's b partial sums bc
+__device__ __forceinline__ void flush_pair_ff(const DMesh& m, const HarParF& q, const ff* dcv_f, int dn, int e,
+                                              const cf acc[kAcc], float4* Af, size_t lda, cf bc[3]) {
+  const int lane = threadIdx.x & 31;
+  const bool rev = m.rev[e] != 0;
+#pragma unroll 1
+  for (int j = 0; j < kAcc; ++j) {
+    const int o = lane + 32 * j;
+    if (o >= kOut) break;
+    const cf aj = sel4(acc[0], acc[1], acc[2], acc[3], j);
+    if (o < 72) {
+      const int kn = o / 9, il = (o % 9) / 3, ik = o % 3;
+      cf v = cf_mul(aj, q.cte_t);
+      if (rev) v = cf_neg(v);
+      const int dof = m.edof[8 * e + kn] + ik;
+      if (m.dct[dof] == 1) addAf(Af, (size_t)dof * lda + 3 * (size_t)dn + il, v);
+      else add3(bc, il, cf_neg(cf_mul(v, cval_f(dcv_f, dof))));
+    } else {
+      const int qq = o - 72, kn = qq / 6, sidx = qq % 6, il = sym_il(sidx), ik = sym_ik(sidx);
+      const cf v = cf_mul(aj, q.cte_u);
+      for (int t = 0; t < (il == ik ? 1 : 2); ++t) {
+        const int r_ = t ? ik : il, c_ = t ? il : ik;
+        const int dof = m.edof[8 * e + kn] + c_;
+        if (m.dct[dof] == 0) addAf(Af, (size_t)dof * lda + 3 * (size_t)dn + r_, cf_neg(v));
+        else add3(bc, r_, cf_mul(v, cval_f(dcv_f, dof)));
+      }
+    }
+  }
+}
+
+// Regular pairs of the mixed sweep. Af: df64 accumulation buffer with the
+// entry layout of A (entry stride astride_e per frequency), added into the
+// binary64 A by k_add_ff after the other assembly kernels. dsf: df64 copies of
+// phi*J*w [ne][ptot][8], unit normals [ne][ptot][3] and prescribed values [ndof][2].
 template <int WPB>
-__global__ void __launch_bounds__(WPB * 32) k_reg_mixed(DMesh m, PolHarmonic pol, const HarParF* pf, const ff* pphi_f,
-                                                        int nf, double* A, size_t lda, size_t astride, double* b,
-                                                        size_t bstride) {
+__global__ void __launch_bounds__(WPB * 32, 4) k_reg_mixed(DMesh m, const HarParF* pf, const ff* dsf, int nf,
+                                                           float4* Af, size_t lda, size_t astride_e, double* b,
+                                                           size_t bstride) {
   __shared__ ComboF sm[WPB][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x / 32;
   const long long gw = blockIdx.x * (long long)WPB + w;
   if (gw >= (long long)m.ndn * nf) return;
   const int dn = (int)(gw % m.ndn), f = (int)(gw / m.ndn);
   ComboF* S = sm[w];
-  const HarParD& P = pol.p[f];
   const HarParF& Q = pf[f];
+  const ff* pphi_f = dsf;
+  const ff* pn_f = dsf + 8LL * m.ne * m.ptot;
+  const ff* dcv_f = pn_f + 3LL * m.ne * m.ptot;
+  float4* Aff = Af + astride_e * f;
+  cf bc[3] = {cf_zero(), cf_zero(), cf_zero()};
   for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
     const int s0 = m.reg_start[cp], s1 = m.reg_start[cp + 1];
     if (s0 == s1) continue;
@@ -685,55 +788,81 @@ __global__ void __launch_bounds__(WPB * 32) k_reg_mixed(DMesh m, PolHarmonic pol
     cf acc[kAcc];
     for (int j = 0; j < kAcc; ++j) acc[j] = cf_zero();
     for (long long base = 0; base < Qn; base += 32) {
-      long long c = base + lane;
+      const long long c = base + lane;
       if (c < Qn) {
-        int jp = find_le(m.reg_pt, s0, s1, P0 + c);
-        int pr = m.reg_pair[jp];
-        int e = pr & 0xFFFFFF, ps = pr >> 24;
-        size_t pt = (size_t)e * m.ptot + m.ps_off[ps] + (size_t)(P0 + c - m.reg_pt[jp]);
-        double rv[3] = {m.px[3 * pt] - xi[0], m.px[3 * pt + 1] - xi[1], m.px[3 * pt + 2] - xi[2]};
-        double n[3] = {m.pn[3 * pt], m.pn[3 * pt + 1], m.pn[3 * pt + 2]};
-        harela_point_f(P, Q, rv, n, S[lane].fu, S[lane].ft);
+        const int jp = find_le(m.reg_pt, s0, s1, P0 + c);
+        const int pr = m.reg_pair[jp];
+        const int e = pr & 0xFFFFFF, ps = pr >> 24;
+        const size_t pt = (size_t)e * m.ptot + m.ps_off[ps] + (size_t)(P0 + c - m.reg_pt[jp]);
+        ff rv[3] = {ff_from(m.px[3 * pt] - xi[0]), ff_from(m.px[3 * pt + 1] - xi[1]), ff_from(m.px[3 * pt + 2] - xi[2])};
+        ff n[3] = {pn_f[3 * pt], pn_f[3 * pt + 1], pn_f[3 * pt + 2]};
+        harela_point_ff(Q, rv, n, S[lane].fu, S[lane].ft);
         for (int k = 0; k < 8; ++k) S[lane].w[k] = pphi_f[8 * pt + k];
         S[lane].pair = jp;
       }
       __syncwarp();
-      int nt = (int)min((long long)32, Qn - base);
-      for (int t = 0; t < nt; ++t) {
-        int jp = S[t].pair;
+      const int nt = (int)min((long long)32, Qn - base);
+      // one extra step after the last point flushes the last pair (single call site)
+      const int tend = (base + 32 >= Qn) ? nt + 1 : nt;
+#pragma unroll 1
+      for (int t = 0; t < tend; ++t) {
+        const int jp = t < nt ? S[t].pair : -1;
         if (jp != cur) {
-          if (cur >= 0) {
-            cd a[kAcc];
-            for (int j = 0; j < kAcc; ++j) a[j] = mk(ff_to(acc[j].re), ff_to(acc[j].im));
-            flush_pair(m, pol, f, dn, m.reg_pair[cur] & 0xFFFFFF, a, A, lda, astride, b, bstride, nullptr);
-          }
+          if (cur >= 0) flush_pair_ff(m, Q, dcv_f, dn, m.reg_pair[cur] & 0xFFFFFF, acc, Aff, lda, bc);
           cur = jp;
           for (int j = 0; j < kAcc; ++j) acc[j] = cf_zero();
         }
+        if (t < nt) {
 #pragma unroll
-        for (int j = 0; j < kAcc; ++j) {
-          int o = lane + 32 * j;
-          if (o < kOut) {
-            cf v;
-            int kn;
-            if (o < 72) {
-              kn = o / 9;
-              v = S[t].ft[o % 9];
-            } else {
-              kn = (o - 72) / 6;
-              v = S[t].fu[(o - 72) % 6];
+          for (int j = 0; j < kAcc; ++j) {
+            const int o = lane + 32 * j;
+            if (o < kOut) {
+              cf v;
+              int kn;
+              if (o < 72) {
+                kn = o / 9;
+                v = S[t].ft[o % 9];
+              } else {
+                kn = (o - 72) / 6;
+                v = S[t].fu[(o - 72) % 6];
+              }
+              acc[j] = cf_fma_r(v, S[t].w[kn], acc[j]);
             }
-            acc[j] = cf_fma_r(v, S[t].w[kn], acc[j]);
           }
         }
       }
       __syncwarp();
     }
-    if (cur >= 0) {
-      cd a[kAcc];
-      for (int j = 0; j < kAcc; ++j) a[j] = mk(ff_to(acc[j].re), ff_to(acc[j].im));
-      flush_pair(m, pol, f, dn, m.reg_pair[cur] & 0xFFFFFF, a, A, lda, astride, b, bstride, nullptr);
+  }
+  // b: one warp reduction per DOF node
+  double* bf = b + bstride * f;
+#pragma unroll 1
+  for (int il = 0; il < 3; ++il) {
+    cf v = il == 0 ? bc[0] : (il == 1 ? bc[1] : bc[2]);
+#pragma unroll 1
+    for (int o = 16; o > 0; o >>= 1) {
+      cf u;
+      u.re.hi = __shfl_xor_sync(0xffffffffu, v.re.hi, o);
+      u.re.lo = __shfl_xor_sync(0xffffffffu, v.re.lo, o);
+      u.im.hi = __shfl_xor_sync(0xffffffffu, v.im.hi, o);
+      u.im.lo = __shfl_xor_sync(0xffffffffu, v.im.lo, o);
+      v = cf_add(v, u);
     }
+    if (lane == 0) {
+      bf[2 * (3 * (size_t)dn + il)] += ff_to(v.re);
+      bf[2 * (3 * (size_t)dn + il) + 1] += ff_to(v.im);
+    }
+  }
+}
+
+// A += Af (df64 entries to binary64), n complex entries
+__global__ void k_add_ff(double2* A, const float4* Af, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float4 a = Af[i];
+    double2 x = A[i];
+    x.x += (double)a.x + (double)a.y;
+    x.y += (double)a.z + (double)a.w;
+    A[i] = x;
   }
 }
 

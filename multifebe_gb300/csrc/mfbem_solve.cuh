@@ -420,31 +420,40 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   double2* A = (double2*)h->A.p;
   double2* b = (double2*)h->b.p;
   double2* x = (flags & MFBEM_DEVICE_PTRS) ? (double2*)x_out : (double2*)h->x.p;
-  CK(cudaMemsetAsync(A, 0, sizeof(double2) * nn * n_freq, h->st));
-  CK(cudaMemsetAsync(b, 0, sizeof(double2) * (size_t)n * n_freq, h->st));
+  // the assembly time covers zeroing the systems too
   cudaEvent_t a0, a1;
   cudaEventCreate(&a0);
   cudaEventCreate(&a1);
   cudaEventRecord(a0, h->st);
+  CK(cudaMemsetAsync(A, 0, sizeof(double2) * nn * n_freq, h->st));
+  CK(cudaMemsetAsync(b, 0, sizeof(double2) * (size_t)n * n_freq, h->st));
   PolHarmonic pol;
   pol.p = dpar;
   AsmTimes tm;
   long long l0 = g_launches;
   const HarParF* pf = nullptr;
-  const ff* pphi_f = nullptr;
+  const ff* dsf = nullptr;
+  float4* Af = nullptr;
   if (precision == 1) {
-    // mixed: regular pairs in double-float (df64 datasets made once per mesh)
-    const long long npp = 8LL * h->m.ne * h->m.ptot;
-    if (h->pphi_f.bytes < sizeof(ff) * npp) {
-      if ((rc = ensure(h->pphi_f, sizeof(ff) * npp))) return rc;
-      k_pphi_f<<<std::min(nblk(npp, 256), 152u * 16u), 256, 0, h->st>>>(h->m.pphi, (ff*)h->pphi_f.p, npp); ++g_launches;
+    // mixed: regular pairs in double-float (df64 datasets made once per mesh:
+    // phi*J*w [ne][ptot][8], unit normals [ne][ptot][3], prescribed values [ndof][2])
+    const long long npp = 8LL * h->m.ne * h->m.ptot, nnp = 3LL * h->m.ne * h->m.ptot, ncv = 2LL * n;
+    if (h->pphi_f.bytes < sizeof(ff) * (npp + nnp + ncv)) {
+      if ((rc = ensure(h->pphi_f, sizeof(ff) * (npp + nnp + ncv)))) return rc;
+      ff* d = (ff*)h->pphi_f.p;
+      k_pphi_f<<<std::min(nblk(npp, 256), 152u * 16u), 256, 0, h->st>>>(h->m.pphi, d, npp); ++g_launches;
+      k_pphi_f<<<std::min(nblk(nnp, 256), 152u * 16u), 256, 0, h->st>>>(h->m.pn, d + npp, nnp); ++g_launches;
+      k_pphi_f<<<std::min(nblk(ncv, 256), 152u * 16u), 256, 0, h->st>>>(h->m.dcv, d + npp + nnp, ncv); ++g_launches;
     }
     if ((rc = ensure(h->parf, sizeof(HarParF) * n_freq))) return rc;
+    if ((rc = ensure(h->Af, sizeof(float4) * nn * n_freq))) return rc;
     k_harpar_f<<<nblk(n_freq, 32), 32, 0, h->st>>>(dpar, (HarParF*)h->parf.p, n_freq); ++g_launches;
     pf = (const HarParF*)h->parf.p;
-    pphi_f = (const ff*)h->pphi_f.p;
+    dsf = (const ff*)h->pphi_f.p;
+    Af = (float4*)h->Af.p;
+    CK(cudaMemsetAsync(Af, 0, sizeof(float4) * nn * n_freq, h->st));
   }
-  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n, &tm, pf, pphi_f)))
+  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n, &tm, pf, dsf, Af)))
     return rc;
   cudaEventRecord(a1, h->st);
   if ((rc = check_err(h))) return rc;
