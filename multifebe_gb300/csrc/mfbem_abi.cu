@@ -59,7 +59,7 @@ struct mfbem_handle {
   int ndof = 0, ne = 0, nn = 0;
   cudaStream_t st = nullptr;
   cublasHandle_t blas = nullptr;
-  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, Af;
+  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, Af, geo_f;
   mfbem_stats stats{};
   long long pts_reg = 0, pts_adp = 0, pts_sing = 0;
   int* d_err = nullptr;
@@ -385,7 +385,7 @@ extern "C" int mfbem_mesh_release(mfbem_handle* h) {
   cudaDeviceSynchronize();
   for (void* p : h->owned) cudaFree(p);
   for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu, &h->parf,
-                    &h->pphi_f, &h->Af})
+                    &h->pphi_f, &h->Af, &h->geo_f})
     if (b->p) cudaFree(b->p);
   if (h->blas) cublasDestroy(h->blas);
   if (h->st) cudaStreamDestroy(h->st);
@@ -438,7 +438,8 @@ struct AsmTimes {
 template <class POL>
 static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, int nf, double* A, size_t lda,
                            size_t astride, double* b, size_t bstride, AsmTimes* tm = nullptr,
-                           const HarParF* pf = nullptr, const ff* dsf = nullptr, float4* Af = nullptr) {
+                           const HarParF* pf = nullptr, const ff* dsf = nullptr, float4* Af = nullptr,
+                           const ff* sgf = nullptr, const ff* lgf = nullptr) {
   const DMesh& m = h->m;
   constexpr int WPB = 4;
   long long nw = (long long)m.ndn * nf;
@@ -448,7 +449,7 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
   if (m.nreg > 0) {
     if constexpr (std::is_same<POL, PolHarmonic>::value) {
       if (pf && dsf && Af) {
-        k_reg_mixed<WPB><<<g, WPB * 32, 0, h->st>>>(m, pf, dsf, nf, Af, lda, astride / 2, b, bstride);
+        k_mixed<MIX_REG, WPB><<<g, WPB * 32, 0, h->st>>>(m, pf, dsf, nullptr, nf, Af, lda, astride / 2, b, bstride);
       } else {
         k_reg<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
       }
@@ -458,13 +459,21 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
     ++g_launches;
   }
   if (tm) cudaEventRecord(tm->ev[1], h->st);
-  if (m.nadp > 0) { k_adp<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride); ++g_launches; }
+  if (m.nadp > 0) {
+    if (Af && lgf) k_mixed<MIX_ADP, WPB><<<g, WPB * 32, 0, h->st>>>(m, pf, dsf, lgf, nf, Af, lda, astride / 2, b, bstride);
+    else k_adp<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
+    ++g_launches;
+  }
   if (tm) cudaEventRecord(tm->ev[2], h->st);
-  // the singular kernel keeps two combo sets per point: 2 warps per block
-  if (m.nsing > 0) { k_sing<POL, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride); ++g_launches; }
+  // the singular kernels keep two combo sets per point: 2 warps per block
+  if (m.nsing > 0) {
+    if (Af && sgf) k_mixed<MIX_SING, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pf, dsf, sgf, nf, Af, lda, astride / 2, b, bstride);
+    else k_sing<POL, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
+    ++g_launches;
+  }
   if (tm) cudaEventRecord(tm->ev[3], h->st);
   k_free<POL><<<nblk(nw, 128), 128, 0, h->st>>>(m, pol, d_nu, nf, A, lda, astride, b, bstride, h->d_err); ++g_launches;
-  if (Af && m.nreg > 0) {
+  if (Af) {
     // mixed: fold the df64 regular-pair sums into the binary64 systems
     const long long ne_ = (long long)(astride / 2) * nf;
     k_add_ff<<<152 * 16, 256, 0, h->st>>>((double2*)A, Af, ne_); ++g_launches;

@@ -707,9 +707,15 @@ __device__ __forceinline__ void harela_point_ff(const HarParF& q, const ff rv[3]
   }
 }
 
-struct alignas(16) ComboF {
+template <bool SING> struct alignas(16) ComboF;
+template <> struct alignas(16) ComboF<false> {
   cf fu[6], ft[9];
   ff w[8];
+  int pair;
+};
+template <> struct alignas(16) ComboF<true> {
+  cf fu[6], ft[9], fc[9];
+  ff w[8], wd[8];
   int pair;
 };
 
@@ -729,18 +735,21 @@ __device__ __forceinline__ void add3(cf bc[3], int i, cf v) {
 
 // scale, reverse and scatter this lane's outputs of one pair (the scatter of
 // flush_pair in double-float): A entries into the df64 buffer Af, prescribed
-// values into the lane's b partial sums bc
+// values into the lane's b partial sums bc. hp (singular pairs only): static
+// line integrals hli[9] and phi_i[8] of the pair; their CPV part
+// T2[0] hli(il,ik) phi_i(kn) is added to the h outputs.
 __device__ __forceinline__ void flush_pair_ff(const DMesh& m, const HarParF& q, const ff* dcv_f, int dn, int e,
-                                              const cf acc[kAcc], float4* Af, size_t lda, cf bc[3]) {
+                                              const cf acc[kAcc], float4* Af, size_t lda, cf bc[3], const ff* hp) {
   const int lane = threadIdx.x & 31;
   const bool rev = m.rev[e] != 0;
 #pragma unroll 1
   for (int j = 0; j < kAcc; ++j) {
     const int o = lane + 32 * j;
     if (o >= kOut) break;
-    const cf aj = sel4(acc[0], acc[1], acc[2], acc[3], j);
+    cf aj = sel4(acc[0], acc[1], acc[2], acc[3], j);
     if (o < 72) {
       const int kn = o / 9, il = (o % 9) / 3, ik = o % 3;
+      if (hp) aj = cf_add(aj, cf_scale(q.c0[3], ff_mul(hp[9 + kn], hp[3 * il + ik])));
       cf v = cf_mul(aj, q.cte_t);
       if (rev) v = cf_neg(v);
       const int dof = m.edof[8 * e + kn] + ik;
@@ -759,20 +768,82 @@ __device__ __forceinline__ void flush_pair_ff(const DMesh& m, const HarParF& q, 
   }
 }
 
-// Regular pairs of the mixed sweep. Af: df64 accumulation buffer with the
-// entry layout of A (entry stride astride_e per frequency), added into the
-// binary64 A by k_add_ff after the other assembly kernels. dsf: df64 copies of
-// phi*J*w [ne][ptot][8], unit normals [ne][ptot][3] and prescribed values [ndof][2].
-template <int WPB>
-__global__ void __launch_bounds__(WPB * 32, 4) k_reg_mixed(DMesh m, const HarParF* pf, const ff* dsf, int nf,
-                                                           float4* Af, size_t lda, size_t astride_e, double* b,
-                                                           size_t bstride) {
-  __shared__ ComboF sm[WPB][32];
+// Singular (polar) points: the regular parts of u*, t* and the CPV integrand
+// (PolHarmonic::point_sing) in double-float. TT2, TT3 without their 1/r^2
+// terms; those form fc = T2[0]/r^2 (n_il dr_ik - n_ik dr_il), integrated with
+// (phi - phi_i) J w.
+__device__ __forceinline__ void harela_point_sing_ff(const HarParF& q, const ff rv[3], const ff n[3], cf* fu6, cf* ft,
+                                                     cf* fc) {
+  const ff r2 = ff_add(ff_add(ff_mul(rv[0], rv[0]), ff_mul(rv[1], rv[1])), ff_mul(rv[2], rv[2]));
+  const ff r = ff_sqrt(r2);
+  const ff d1r1 = ff_rcp(r), d1r2 = ff_mul(d1r1, d1r1);
+  cf X[5];
+#pragma unroll
+  for (int t = 0; t < 5; ++t) X[t] = t < 3 ? cf_add(cf_scale(q.c0[t], t < 2 ? d1r1 : d1r2), q.c1[t]) : q.c1[t];
+#pragma unroll 1
+  for (int w = 0; w < 2; ++w) {
+    const cf k = w ? q.k2 : q.k1;
+    const cf z = cf{ff_mul(k.im, r), ff_neg(ff_mul(k.re, r))};
+    cf e2, e3, e4, e5;
+    zexp_2to5_ff(q.t2, z, e2, e3, e4, e5);
+    ff rp = d1r1;
+#pragma unroll 1
+    for (int nn = 0; nn < 4; ++nn) {
+      const cf src = cf_scale(sel4(e2, e3, e4, e5, nn), rp);
+#pragma unroll
+      for (int t = 0; t < 5; ++t) X[t] = cf_fma(q.cm[w][nn][t], src, X[t]);
+      rp = ff_mul(rp, d1r1);
+    }
+  }
+  const cf psi = X[0], chi = X[1], T1 = X[2], T2 = X[3], T3 = X[4];
+  const cf c2 = cf_scale(q.c0[3], d1r2);
+  const cf T2f = cf_add(T2, c2);
+  const ff dr[3] = {ff_mul(rv[0], d1r1), ff_mul(rv[1], d1r1), ff_mul(rv[2], d1r1)};
+  const ff drdn = ff_add(ff_add(ff_mul(dr[0], n[0]), ff_mul(dr[1], n[1])), ff_mul(dr[2], n[2]));
+#pragma unroll 1
+  for (int c = 0; c < 9; ++c) {
+    const int il = c / 3, ik = c - 3 * il;
+    const ff dri = sel3(dr, il), drk = sel3(dr, ik), ni = sel3(n, il), nk = sel3(n, ik);
+    const ff rr = ff_mul(dri, drk);
+    const ff a = ff_mul(drk, ni), bq = ff_mul(dri, nk);
+    cf t = cf_scale(T1, ff_mul(rr, drdn));
+    t = cf_fma_r(T2, a, t);
+    t = cf_fma_r(T3, bq, t);
+    if (il == ik) t = cf_fma_r(T2f, drdn, t);
+    ft[c] = t;
+    fc[c] = cf_scale(c2, ff_sub(a, bq));
+    if (ik >= il) {
+      cf u = cf_neg(cf_scale(chi, rr));
+      if (il == ik) u = cf_add(u, psi);
+      fu6[ik + (il == 1 ? 2 : (il == 2 ? 3 : 0))] = u;
+    }
+  }
+}
+
+// Pair lists walked by the mixed kernels: regular pairs (precalculated element
+// datasets), adaptive pairs (subdivision leaves) and singular pairs (polar points).
+enum MixKind { MIX_REG = 0, MIX_ADP = 1, MIX_SING = 2 };
+
+// Mixed-precision pair kernels (time-harmonic): one warp per (DOF node,
+// frequency), the two-phase scheme of k_reg, all arithmetic after x - x_i in
+// double-float. Af: df64 accumulation buffer with the entry layout of A (entry
+// stride astride_e per frequency), added into the binary64 A by k_add_ff after
+// the other assembly kernels. dsf: df64 copies of phi*J*w [ne][ptot][8], unit
+// normals [ne][ptot][3] and prescribed values [ndof][2]; gf: df64 copy of the
+// frequency-independent point geometry (leaf_geo for adaptive, sing_geo for
+// singular pairs), component-major.
+template <int KIND, int WPB>
+__global__ void __launch_bounds__(WPB * 32, 4) k_mixed(DMesh m, const HarParF* pf, const ff* dsf, const ff* gf, int nf,
+                                                       float4* Af, size_t lda, size_t astride_e, double* b,
+                                                       size_t bstride) {
+  constexpr bool SG = KIND == MIX_SING;
+  __shared__ ComboF<SG> sm[WPB][32];
+  __shared__ ff hps[WPB][SG ? 17 : 1];
   const int lane = threadIdx.x & 31, w = threadIdx.x / 32;
   const long long gw = blockIdx.x * (long long)WPB + w;
   if (gw >= (long long)m.ndn * nf) return;
   const int dn = (int)(gw % m.ndn), f = (int)(gw / m.ndn);
-  ComboF* S = sm[w];
+  ComboF<SG>* S = sm[w];
   const HarParF& Q = pf[f];
   const ff* pphi_f = dsf;
   const ff* pn_f = dsf + 8LL * m.ne * m.ptot;
@@ -780,25 +851,53 @@ __global__ void __launch_bounds__(WPB * 32, 4) k_reg_mixed(DMesh m, const HarPar
   float4* Aff = Af + astride_e * f;
   cf bc[3] = {cf_zero(), cf_zero(), cf_zero()};
   for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
-    const int s0 = m.reg_start[cp], s1 = m.reg_start[cp + 1];
+    int s0, s1;
+    const long long* pts;
+    if (KIND == MIX_REG) {
+      s0 = m.reg_start[cp]; s1 = m.reg_start[cp + 1]; pts = m.reg_pt;
+    } else if (KIND == MIX_ADP) {
+      const int a0 = m.adp_start[cp], a1 = m.adp_start[cp + 1];
+      if (a0 == a1) continue;
+      s0 = m.adp_leaf[a0]; s1 = m.adp_leaf[a1]; pts = m.leaf_pt;
+    } else {
+      s0 = m.sing_start[cp]; s1 = m.sing_start[cp + 1]; pts = m.sing_pt;
+    }
     if (s0 == s1) continue;
     const double* xi = m.cpx + 3 * (size_t)cp;
-    const long long P0 = m.reg_pt[s0], Qn = m.reg_pt[s1] - P0;
+    const long long P0 = pts[s0], Qn = pts[s1] - P0;
     int cur = -1;
     cf acc[kAcc];
     for (int j = 0; j < kAcc; ++j) acc[j] = cf_zero();
     for (long long base = 0; base < Qn; base += 32) {
       const long long c = base + lane;
       if (c < Qn) {
-        const int jp = find_le(m.reg_pt, s0, s1, P0 + c);
-        const int pr = m.reg_pair[jp];
-        const int e = pr & 0xFFFFFF, ps = pr >> 24;
-        const size_t pt = (size_t)e * m.ptot + m.ps_off[ps] + (size_t)(P0 + c - m.reg_pt[jp]);
-        ff rv[3] = {ff_from(m.px[3 * pt] - xi[0]), ff_from(m.px[3 * pt + 1] - xi[1]), ff_from(m.px[3 * pt + 2] - xi[2])};
-        ff n[3] = {pn_f[3 * pt], pn_f[3 * pt + 1], pn_f[3 * pt + 2]};
-        harela_point_ff(Q, rv, n, S[lane].fu, S[lane].ft);
-        for (int k = 0; k < 8; ++k) S[lane].w[k] = pphi_f[8 * pt + k];
-        S[lane].pair = jp;
+        const int jl = find_le(pts, s0, s1, P0 + c);
+        ff rv[3], n[3];
+        if (KIND == MIX_REG) {
+          const int pr = m.reg_pair[jl];
+          const int e = pr & 0xFFFFFF, ps = pr >> 24;
+          const size_t pt = (size_t)e * m.ptot + m.ps_off[ps] + (size_t)(P0 + c - m.reg_pt[jl]);
+          rv[0] = ff_from(m.px[3 * pt] - xi[0]);
+          rv[1] = ff_from(m.px[3 * pt + 1] - xi[1]);
+          rv[2] = ff_from(m.px[3 * pt + 2] - xi[2]);
+          n[0] = pn_f[3 * pt]; n[1] = pn_f[3 * pt + 1]; n[2] = pn_f[3 * pt + 2];
+          for (int k = 0; k < 8; ++k) S[lane].w[k] = pphi_f[8 * pt + k];
+          S[lane].pair = jl;
+        } else {
+          const long long g = P0 + c, np = SG ? m.nsing_pts : m.nleaf_pts;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            rv[k] = gf[k * np + g];
+            n[k] = gf[(3 + k) * np + g];
+          }
+          for (int k = 0; k < 8; ++k) S[lane].w[k] = gf[(6 + k) * np + g];
+          if constexpr (SG) {
+            for (int k = 0; k < 8; ++k) S[lane].wd[k] = gf[(14 + k) * np + g];
+          }
+          S[lane].pair = SG ? jl : m.leaf_pair[jl];
+        }
+        if constexpr (SG) harela_point_sing_ff(Q, rv, n, S[lane].fu, S[lane].ft, S[lane].fc);
+        else harela_point_ff(Q, rv, n, S[lane].fu, S[lane].ft);
       }
       __syncwarp();
       const int nt = (int)min((long long)32, Qn - base);
@@ -808,25 +907,34 @@ __global__ void __launch_bounds__(WPB * 32, 4) k_reg_mixed(DMesh m, const HarPar
       for (int t = 0; t < tend; ++t) {
         const int jp = t < nt ? S[t].pair : -1;
         if (jp != cur) {
-          if (cur >= 0) flush_pair_ff(m, Q, dcv_f, dn, m.reg_pair[cur] & 0xFFFFFF, acc, Aff, lda, bc);
+          if (cur >= 0) {
+            const int e = KIND == MIX_REG ? (m.reg_pair[cur] & 0xFFFFFF) : (KIND == MIX_ADP ? m.adp_e[cur] : m.sing_e[cur]);
+            flush_pair_ff(m, Q, dcv_f, dn, e, acc, Aff, lda, bc, SG ? hps[w] : nullptr);
+          }
           cur = jp;
           for (int j = 0; j < kAcc; ++j) acc[j] = cf_zero();
+          if constexpr (SG) {
+            __syncwarp();
+            if (jp >= 0 && lane < 17) {
+              const double* D = m.sing_d + (size_t)jp * SING_D;
+              hps[w][lane] = ff_from(lane < 9 ? D[13 + lane] : D[5 + lane - 9]);
+            }
+            __syncwarp();
+          }
         }
         if (t < nt) {
 #pragma unroll
           for (int j = 0; j < kAcc; ++j) {
             const int o = lane + 32 * j;
             if (o < kOut) {
-              cf v;
-              int kn;
               if (o < 72) {
-                kn = o / 9;
-                v = S[t].ft[o % 9];
+                const int kn = o / 9, cc = o % 9;
+                acc[j] = cf_fma_r(S[t].ft[cc], S[t].w[kn], acc[j]);
+                if constexpr (SG) acc[j] = cf_fma_r(S[t].fc[cc], S[t].wd[kn], acc[j]);
               } else {
-                kn = (o - 72) / 6;
-                v = S[t].fu[(o - 72) % 6];
+                const int kn = (o - 72) / 6;
+                acc[j] = cf_fma_r(S[t].fu[(o - 72) % 6], S[t].w[kn], acc[j]);
               }
-              acc[j] = cf_fma_r(v, S[t].w[kn], acc[j]);
             }
           }
         }

@@ -434,6 +434,7 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   const HarParF* pf = nullptr;
   const ff* dsf = nullptr;
   float4* Af = nullptr;
+  const ff *sgf = nullptr, *lgf = nullptr;
   if (precision == 1) {
     // mixed: regular pairs in double-float (df64 datasets made once per mesh:
     // phi*J*w [ne][ptot][8], unit normals [ne][ptot][3], prescribed values [ndof][2])
@@ -445,6 +446,16 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
       k_pphi_f<<<std::min(nblk(nnp, 256), 152u * 16u), 256, 0, h->st>>>(h->m.pn, d + npp, nnp); ++g_launches;
       k_pphi_f<<<std::min(nblk(ncv, 256), 152u * 16u), 256, 0, h->st>>>(h->m.dcv, d + npp + nnp, ncv); ++g_launches;
     }
+    // df64 copies of the hoisted singular / adaptive point geometry
+    const long long ngs = h->m.sing_geo ? 22LL * h->m.nsing_pts : 0, ngl = h->m.leaf_geo ? 14LL * h->m.nleaf_pts : 0;
+    if (ngs + ngl > 0 && h->geo_f.bytes < sizeof(ff) * (ngs + ngl)) {
+      if ((rc = ensure(h->geo_f, sizeof(ff) * (ngs + ngl)))) return rc;
+      ff* d = (ff*)h->geo_f.p;
+      if (ngs) { k_pphi_f<<<std::min(nblk(ngs, 256), 152u * 16u), 256, 0, h->st>>>(h->m.sing_geo, d, ngs); ++g_launches; }
+      if (ngl) { k_pphi_f<<<std::min(nblk(ngl, 256), 152u * 16u), 256, 0, h->st>>>(h->m.leaf_geo, d + ngs, ngl); ++g_launches; }
+    }
+    sgf = ngs ? (const ff*)h->geo_f.p : nullptr;
+    lgf = ngl ? (const ff*)h->geo_f.p + ngs : nullptr;
     if ((rc = ensure(h->parf, sizeof(HarParF) * n_freq))) return rc;
     if ((rc = ensure(h->Af, sizeof(float4) * nn * n_freq))) return rc;
     k_harpar_f<<<nblk(n_freq, 32), 32, 0, h->st>>>(dpar, (HarParF*)h->parf.p, n_freq); ++g_launches;
@@ -453,7 +464,7 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
     Af = (float4*)h->Af.p;
     CK(cudaMemsetAsync(Af, 0, sizeof(float4) * nn * n_freq, h->st));
   }
-  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n, &tm, pf, dsf, Af)))
+  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n, &tm, pf, dsf, Af, sgf, lgf)))
     return rc;
   cudaEventRecord(a1, h->st);
   if ((rc = check_err(h))) return rc;
