@@ -306,6 +306,16 @@ def profile_case(nf):
     return 0
 
 
+def profile_patch(precision):
+    """ncu case for the 14883-DOF surface patch: one sweep at a0=0.5."""
+    from multifebe_gb300 import meshgen as M, BemRegion
+    deck, mat, om = M.workload(3)
+    R = BemRegion(deck)
+    R.sweep_harela(mat, om, precision=precision)
+    print(json.dumps(R.last_stats))
+    return 0
+
+
 def _desc_bytes(d, deck):
     ne, nn = deck.n_elements, deck.n_nodes
     return int(ne * (24 + 1 + 4 + 24 + 24 + 16 + 24) * 8 + ne * (8 + 1 + 1) * 4 + nn * (3 + 6 + 3 + 1) * 4 + nn * 6 * 8)
@@ -321,9 +331,13 @@ def main():
                     help="skip the 14883-DOF surface-patch mixed/plain comparison")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="profiling helper: run the benchmark mesh for this many frequencies twice, print stats, exit")
+    ap.add_argument("--profile-patch", default="", choices=["", "mixed", "plain"],
+                    help="profiling helper: one sweep of the 14883-DOF surface patch, print stats, exit")
     args = ap.parse_args()
     if args.profile_case:
         return profile_case(args.profile_case)
+    if args.profile_patch:
+        return profile_patch(args.profile_patch)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

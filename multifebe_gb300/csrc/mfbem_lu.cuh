@@ -211,6 +211,167 @@ __global__ void __launch_bounds__(NT) k_pcol_update(S* A, long long strideA, int
   }
 }
 
+// ---------------------------------------------------------------------------
+// Cooperative panel factorisation: the panel columns [k, k+kb) of each matrix
+// are split by rows over G CTAs (row chunk of `chunk` rows each) and held in
+// shared memory for the whole panel; per column one barrier among the matrix's
+// G CTAs exchanges the chunk-local pivot candidates. Launched with
+// cudaLaunchCooperativeKernel, so all CTAs are co-resident; every barrier wait
+// is bounded (about a second), after which the kernel sets *err and returns.
+//
+// Per column j (global row/column jj = k + j):
+//   every CTA   argmax |A(i,jj)| (LAPACK's |re|+|im| for complex) over its rows
+//               i >= jj, publishes (value, row, the row's kb panel values); the
+//               owner of row jj publishes that row too (slot jj % 2)
+//   barrier
+//   every CTA   picks the winner (largest value, smallest row on ties), swaps
+//               the two rows inside its chunk where it owns them, then scales
+//               column jj below the diagonal and updates columns jj+1.. of its rows
+// Counters ctr[matrix] count barrier arrivals over the whole factorisation
+// (zeroed once per getrf), so the target of column jj is (jj + 1) * G.
+// ---------------------------------------------------------------------------
+constexpr long long kCoopSpin = 1LL << 24;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <typename S, int NT>
+__global__ void __launch_bounds__(NT) k_panel_coop(S* A, long long strideA, int lda, int n, int k, int kb, int G,
+                                                   int chunk, int b0, int* ipiv, int* info, unsigned* ctr, S* xrow,
+                                                   typename Sc<S>::R* xval, int* xidx, int* err) {
+  typedef typename Sc<S>::R R;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  S* pan = reinterpret_cast<S*>(smraw);  // [kb][chunk]
+  S* prow = pan + (size_t)kb * chunk;     // [kb] pivot row
+  __shared__ R sv[NT / 32];
+  __shared__ int si[NT / 32], sg[NT / 32];
+  __shared__ int s_ok, s_p, s_g;
+  const int mat = b0 + blockIdx.x / G, g = blockIdx.x % G;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x / 32;
+  S* M = A + strideA * mat;
+  int* piv = ipiv + (size_t)n * mat;
+  const int r0 = k + g * chunk, r1 = min(n, r0 + chunk), nr = max(0, r1 - r0);
+  // exchange slots of this matrix: [2][G][kb] rows, [2][G] values / indices, then
+  // [2][kb] for the current diagonal row (stored at candidate index G)
+  S* XR = xrow + (size_t)(mat) * 2 * (G + 1) * kb;
+  R* XV = xval + (size_t)(mat) * 2 * G;
+  int* XI = xidx + (size_t)(mat) * 2 * G;
+  for (int t = threadIdx.x; t < kb * nr; t += NT) {
+    const int c = t / nr, i = t - c * nr;
+    pan[(size_t)c * chunk + i] = M[(size_t)(k + c) * lda + r0 + i];
+  }
+  __syncthreads();
+  for (int j = 0; j < kb; ++j) {
+    const int jj = k + j, slot = jj & 1;
+    // chunk-local candidate
+    R best = -1;
+    int bi = -1;
+    for (int i = max(jj, r0) - r0 + threadIdx.x; i < nr; i += NT) {
+      const R v = Sc<S>::abs1(pan[(size_t)j * chunk + i]);
+      if (v > best) { best = v; bi = r0 + i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi >= 0 && (bi < 0 || oi < bi))) { best = ov; bi = oi; }
+    }
+    if (lane == 0) { sv[wid] = best; si[wid] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      R b_ = sv[0];
+      int i_ = si[0];
+      for (int w = 1; w < NT / 32; ++w)
+        if (sv[w] > b_ || (sv[w] == b_ && si[w] >= 0 && (i_ < 0 || si[w] < i_))) { b_ = sv[w]; i_ = si[w]; }
+      XV[slot * G + g] = b_;
+      XI[slot * G + g] = i_;
+      s_p = i_;
+    }
+    __syncthreads();
+    const int myc = s_p;
+    if (myc >= 0 && (int)threadIdx.x < kb)
+      XR[((size_t)slot * (G + 1) + g) * kb + threadIdx.x] = pan[(size_t)threadIdx.x * chunk + (myc - r0)];
+    if (jj >= r0 && jj < r1 && (int)threadIdx.x < kb)
+      XR[((size_t)slot * (G + 1) + G) * kb + threadIdx.x] = pan[(size_t)threadIdx.x * chunk + (jj - r0)];
+    // barrier among the G CTAs of this matrix
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(ctr + mat, 1u);
+      const unsigned target = (unsigned)(jj + 1) * (unsigned)G;
+      long long it = 0;
+      int ok = 1;
+      while (ld_acquire_u32(ctr + mat) < target) {
+        if (++it > kCoopSpin) { ok = 0; atomicExch(err, 1); break; }
+        __nanosleep(32);
+      }
+      __threadfence();
+      s_ok = ok;
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    // winner over the G candidates (parallel loads, block argmax)
+    {
+      R b_ = -1;
+      int i_ = -1, g_ = 0;
+      for (int q = threadIdx.x; q < G; q += NT) {
+        const R v = __ldcg(XV + slot * G + q);
+        const int ix = __ldcg(XI + slot * G + q);
+        if (ix >= 0 && (v > b_ || (v == b_ && ix < i_))) { b_ = v; i_ = ix; g_ = q; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const R ov = __shfl_xor_sync(0xffffffffu, b_, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, i_, o);
+        const int og = __shfl_xor_sync(0xffffffffu, g_, o);
+        if (oi >= 0 && (ov > b_ || (ov == b_ && (i_ < 0 || oi < i_)))) { b_ = ov; i_ = oi; g_ = og; }
+      }
+      if (lane == 0) { sv[wid] = b_; si[wid] = i_; sg[wid] = g_; }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        R bb = sv[0];
+        int ii = si[0], gg = sg[0];
+        for (int w = 1; w < NT / 32; ++w)
+          if (si[w] >= 0 && (sv[w] > bb || (sv[w] == bb && (ii < 0 || si[w] < ii)))) { bb = sv[w]; ii = si[w]; gg = sg[w]; }
+        s_p = ii;
+        s_g = gg;
+      }
+      __syncthreads();
+    }
+    const int p = s_p;
+    if ((int)threadIdx.x < kb)
+      prow[threadIdx.x] = __ldcg(XR + ((size_t)slot * (G + 1) + s_g) * kb + threadIdx.x);
+    __syncthreads();
+    if (g == 0 && threadIdx.x == 0) {
+      piv[jj] = p + 1;
+      if (Sc<S>::iszero(prow[j]) && info[mat] == 0) info[mat] = jj + 1;
+    }
+    if (p != jj) {
+      // row p <- old row jj, row jj <- pivot row, where this CTA owns them
+      if (p >= r0 && p < r1 && (int)threadIdx.x < kb)
+        pan[(size_t)threadIdx.x * chunk + (p - r0)] = __ldcg(XR + ((size_t)slot * (G + 1) + G) * kb + threadIdx.x);
+      if (jj >= r0 && jj < r1 && (int)threadIdx.x < kb) pan[(size_t)threadIdx.x * chunk + (jj - r0)] = prow[threadIdx.x];
+    }
+    __syncthreads();
+    const S dj = prow[j];
+    if (!Sc<S>::iszero(dj)) {
+      const S rcp = Sc<S>::rcp(dj);
+      for (int i = max(jj + 1, r0) - r0 + threadIdx.x; i < nr; i += NT) {
+        const S l = Sc<S>::mul(pan[(size_t)j * chunk + i], rcp);
+        pan[(size_t)j * chunk + i] = l;
+        for (int c = j + 1; c < kb; ++c)
+          pan[(size_t)c * chunk + i] = Sc<S>::sub(pan[(size_t)c * chunk + i], Sc<S>::mul(l, prow[c]));
+      }
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < kb * nr; t += NT) {
+    const int c = t / nr, i = t - c * nr;
+    M[(size_t)(k + c) * lda + r0 + i] = pan[(size_t)c * chunk + i];
+  }
+}
+
 // Apply the panel interchanges (rows k..k+nb-1 with ipiv) to the columns
 // outside the panel: one thread per column.
 template <typename S>
@@ -255,6 +416,96 @@ __global__ void k_trsm_llu(S* A, long long strideA, int lda, int n, int k, int n
   for (int jj = 0; jj < w; ++jj)
     for (int i = jj + 1; i < w; ++i) x[i] = Sc<S>::sub(x[i], Sc<S>::mul(L[jj * w + i], x[jj]));
   for (int i = 0; i < w; ++i) Ac[i] = x[i];
+}
+
+// U12 = L11^{-1} A12 for the columns [c0, c1) (L11 unit lower, w x w at (k,k),
+// w <= 32). A CTA of trsm_cols<S>() threads stages a 32-row tile of as many
+// columns (coalesced along each column), thread t solves column t in shared
+// memory, and the tile is written back.
+template <typename S> __host__ __device__ constexpr int trsm_cols() { return sizeof(S) > 8 ? 32 : 64; }
+template <typename S>
+__global__ void __launch_bounds__(trsm_cols<S>()) k_trsm_cols(S* A, long long strideA, int lda, int k, int w, int c0,
+                                                              int c1) {
+  constexpr int NC = trsm_cols<S>();
+  const int bidx = blockIdx.y;
+  S* M = A + strideA * bidx;
+  __shared__ S L[32 * 32];
+  __shared__ S T[NC * 33];  // [column][row], padded
+  const int cb = c0 + blockIdx.x * NC;
+  const int ncol = min(NC, c1 - cb);
+  for (int t = threadIdx.x; t < w * w; t += NC) {
+    const int i = t % w, jj = t / w;
+    L[t] = M[(size_t)(k + jj) * lda + k + i];
+  }
+  // the 32 rows of one column are contiguous
+  for (int t = threadIdx.x; t < 32 * ncol; t += NC) {
+    const int i = t & 31, c = t >> 5;
+    if (i < w) T[c * 33 + i] = M[(size_t)(cb + c) * lda + k + i];
+  }
+  __syncthreads();
+  const int c = threadIdx.x;
+  if (c < ncol) {
+    S* x = T + c * 33;
+    for (int jj = 0; jj < w; ++jj) {
+      const S xj = x[jj];
+      for (int i = jj + 1; i < w; ++i) x[i] = Sc<S>::sub(x[i], Sc<S>::mul(L[jj * w + i], xj));
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < 32 * ncol; t += NC) {
+    const int i = t & 31, cc = t >> 5;
+    if (i < w) M[(size_t)(cb + cc) * lda + k + i] = T[cc * 33 + i];
+  }
+}
+
+// Diagonal block solve of getrs by one warp: the w x w block (w <= 64) staged
+// in shared memory, lane l holding rows l and l + 32 of the block; the solved
+// component is broadcast by a shuffle, no block-wide barrier per row.
+// LOWER: unit lower forward substitution; else upper backward substitution.
+template <typename S> __device__ __forceinline__ S shfl_s(S v, int src);
+template <> __device__ __forceinline__ float2 shfl_s(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+template <> __device__ __forceinline__ double2 shfl_s(double2 v, int src) {
+  return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+template <> __device__ __forceinline__ float shfl_s(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+template <> __device__ __forceinline__ double shfl_s(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+template <typename S, bool LOWER>
+__global__ void __launch_bounds__(128) k_trsv_diag64(const S* A, long long strideA, int lda, S* b, long long strideb,
+                                                     int r0, int w) {
+  const int bidx = blockIdx.x;
+  const S* M = A + strideA * bidx;
+  S* xg = b + strideb * bidx;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  S* D = reinterpret_cast<S*>(smraw);  // [col][row], w x w, padded to 65 rows
+  for (int t = threadIdx.x; t < w * 64; t += 128) {
+    const int i = t & 63, j = t >> 6;
+    if (i < w) D[j * 65 + i] = M[(size_t)(r0 + j) * lda + r0 + i];
+  }
+  __syncthreads();
+  if (threadIdx.x >= 32) return;
+  const int l = threadIdx.x;
+  S x0 = l < w ? xg[r0 + l] : Sc<S>::zero();
+  S x1 = l + 32 < w ? xg[r0 + l + 32] : Sc<S>::zero();
+  if (LOWER) {
+    for (int j = 0; j < w; ++j) {
+      const S xj = shfl_s(j < 32 ? x0 : x1, j & 31);
+      if (l > j && l < w) x0 = Sc<S>::sub(x0, Sc<S>::mul(D[j * 65 + l], xj));
+      if (l + 32 > j && l + 32 < w) x1 = Sc<S>::sub(x1, Sc<S>::mul(D[j * 65 + l + 32], xj));
+    }
+  } else {
+    for (int j = w - 1; j >= 0; --j) {
+      if (j < 32) { if (l == j) x0 = Sc<S>::div(x0, D[j * 65 + j]); }
+      else { if (l + 32 == j) x1 = Sc<S>::div(x1, D[j * 65 + j]); }
+      const S xj = shfl_s(j < 32 ? x0 : x1, j & 31);
+      if (l < j) x0 = Sc<S>::sub(x0, Sc<S>::mul(D[j * 65 + l], xj));
+      if (l + 32 < j) x1 = Sc<S>::sub(x1, Sc<S>::mul(D[j * 65 + l + 32], xj));
+    }
+  }
+  if (l < w) xg[r0 + l] = x0;
+  if (l + 32 < w) xg[r0 + l + 32] = x1;
 }
 
 // ---------------------------------------------------------------------------

@@ -34,6 +34,51 @@ template <typename S> struct IsF64 { static const bool v = false; };
 template <> struct IsF64<double> { static const bool v = true; };
 template <> struct IsF64<double2> { static const bool v = true; };
 
+// Workspace of the cooperative panel (barrier counters, candidate exchange, error flag)
+static DevBuf g_lu_ws;
+
+// Plan of the cooperative panel for n x n matrices in a batch: G CTAs per
+// matrix (panel rows split in G chunks held in shared memory, at most
+// kCoopBytes per CTA so that two CTAs share an SM), launched in groups of
+// `group` matrices whose CTAs are all co-resident. Returns false when the
+// device cannot hold one matrix's CTAs at once (the caller then uses the
+// per-column panel).
+struct CoopPlan {
+  int G = 0, group = 0;
+  size_t smem = 0;
+};
+template <typename S>
+static bool coop_plan(int n, int nb, int batch, CoopPlan* pl) {
+  constexpr size_t kCoopBytes = 96 * 1024;
+  int dev = 0, nsm = 0, coop = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (!coop || nsm <= 0) return false;
+  const size_t es = sizeof(S);
+  const int gmin = (int)(((size_t)n * nb * es + kCoopBytes - 1) / kCoopBytes);
+  // about one CTA per SM in total (barrier cost grows with G), at least 64 rows each
+  int G = std::max(gmin, std::min((n + 63) / 64, std::max(1, nsm / std::max(1, batch))));
+  G = std::max(1, std::min(G, n));
+  const int chunk = (n + G - 1) / G;
+  const size_t smem = ((size_t)nb * chunk + nb) * es;
+  if (cudaFuncSetAttribute(k_panel_coop<S, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  int bps = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_panel_coop<S, 256>, 256, smem) != cudaSuccess || bps < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  const int cap = bps * nsm;
+  if (G > cap) return false;
+  pl->G = G;
+  pl->group = std::max(1, std::min(batch, cap / G));
+  pl->smem = smem;
+  return true;
+}
+
 // Blocked right-looking getrf for a batch of n x n matrices (stride sA).
 template <typename S>
 static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA, int lda, int n, int batch,
@@ -41,32 +86,95 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
   // panel width: the L11 block of the TRSM lives in shared memory (<= 16 KB)
   const int nb = 32;
   CK(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
-  // FP64: spread the panel's rank-1 updates over many SMs (one SM's FP64 rate
-  // would serialise the panel); FP32: one CTA per matrix and panel.
+  typedef typename Sc<S>::R R;
+  CoopPlan pl;
+  const bool coop = coop_plan<S>(n, nb, batch, &pl);
+  unsigned* ctr = nullptr;
+  S* xrow = nullptr;
+  R* xval = nullptr;
+  int *xidx = nullptr, *derr = nullptr;
+  if (coop) {
+    const size_t nctr = (size_t)batch, nrow = (size_t)batch * 2 * (pl.G + 1) * nb, nval = (size_t)batch * 2 * pl.G;
+    size_t off_row = ((nctr + 1) * sizeof(unsigned) + 255) / 256 * 256;
+    size_t off_val = off_row + (nrow * sizeof(S) + 255) / 256 * 256;
+    size_t off_idx = off_val + (nval * sizeof(R) + 255) / 256 * 256;
+    size_t total = off_idx + nval * sizeof(int);
+    int rc = ensure(g_lu_ws, total);
+    if (rc) return rc;
+    char* w = (char*)g_lu_ws.p;
+    ctr = (unsigned*)w;
+    derr = (int*)(ctr + nctr);
+    xrow = (S*)(w + off_row);
+    xval = (R*)(w + off_val);
+    xidx = (int*)(w + off_idx);
+    CK(cudaMemsetAsync(w, 0, (nctr + 1) * sizeof(unsigned), st));
+  }
+  // FP64 without the cooperative panel: spread the panel's rank-1 updates over
+  // many SMs per column (one SM's FP64 rate would serialise the panel); FP32:
+  // one CTA per matrix and panel.
   const bool multi = IsF64<S>::v;
   int G = std::max(1, std::min(64, (n / 128) * 2 / std::max(1, batch) + 1));
-  for (int k = 0; k < n; k += nb) {
-    const int kb = std::min(nb, n - k);
-    if (multi) {
-      for (int j = k; j < k + kb; ++j) {
-        k_pcol_pivot<S, 256><<<batch, 256, 0, st>>>(A, sA, lda, n, k, kb, j, ipiv, info); ++g_launches;
-        int rows = n - j - 1;
-        int g = std::max(1, std::min(G, (rows + 255) / 256));
-        k_pcol_update<S, 256><<<dim3(g, batch), 256, 0, st>>>(A, sA, lda, n, k, kb, j); ++g_launches;
+  // Two-level blocking: outer blocks of NBO columns are factorised with inner
+  // panels of nb columns (updates restricted to the outer block), then one
+  // trailing GEMM of depth NBO updates the rest of the matrix.
+  const int NBO = 128;
+  for (int K = 0; K < n; K += NBO) {
+    const int KE = std::min(n, K + NBO);
+    for (int k = K; k < KE; k += nb) {
+      const int kb = std::min(nb, KE - k);
+      if (coop) {
+        const int chunk = (n - k + pl.G - 1) / pl.G;
+        for (int b0 = 0; b0 < batch; b0 += pl.group) {
+          const int nbm = std::min(pl.group, batch - b0);
+          int Gp = pl.G, ck = chunk, kk = k, kbb = kb, nn_ = n, ldaa = lda, bb0 = b0;
+          long long sAA = sA;
+          void* args[] = {&A, &sAA, &ldaa, &nn_, &kk, &kbb, &Gp, &ck, &bb0, &ipiv, &info, &ctr, &xrow, &xval, &xidx, &derr};
+          CK(cudaLaunchCooperativeKernel((const void*)k_panel_coop<S, 256>, dim3(pl.G * nbm), dim3(256), args,
+                                         ((size_t)kb * chunk + kb) * sizeof(S), st));
+          ++g_launches;
+        }
+      } else if (multi) {
+        for (int j = k; j < k + kb; ++j) {
+          k_pcol_pivot<S, 256><<<batch, 256, 0, st>>>(A, sA, lda, n, k, kb, j, ipiv, info); ++g_launches;
+          int rows = n - j - 1;
+          int g = std::max(1, std::min(G, (rows + 255) / 256));
+          k_pcol_update<S, 256><<<dim3(g, batch), 256, 0, st>>>(A, sA, lda, n, k, kb, j); ++g_launches;
+        }
+      } else {
+        k_panel_cta<S, 512><<<batch, 512, 0, st>>>(A, sA, lda, n, k, kb, ipiv, info); ++g_launches;
       }
-    } else {
-      k_panel_cta<S, 512><<<batch, 512, 0, st>>>(A, sA, lda, n, k, kb, ipiv, info); ++g_launches;
+      int nout = n - kb;
+      if (nout > 0) { k_laswp<S><<<dim3(nblk(nout, 128), batch), 128, 0, st>>>(A, sA, lda, n, k, kb, ipiv); ++g_launches; }
+      if (k + kb < KE) {
+        // inside the outer block: U12 and the update of columns [k+kb, KE)
+        const int nc = KE - k - kb;
+        k_trsm_cols<S><<<dim3(nblk(nc, trsm_cols<S>()), batch), trsm_cols<S>(), 0, st>>>(A, sA, lda, k, kb, k + kb, KE); ++g_launches;
+        CKB(gemm_sb(hb, n - k - kb, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)(k + kb) * lda, lda,
+                    sA, A + (k + kb) + (size_t)(k + kb) * lda, lda, sA, batch));
+      }
     }
-    int nout = n - kb;
-    if (nout > 0) k_laswp<S><<<dim3(nblk(nout, 128), batch), 128, 0, st>>>(A, sA, lda, n, k, kb, ipiv); ++g_launches;
-    if (k + kb < n) {
-      int nc = n - k - kb;
-      k_trsm_llu<S><<<dim3(nblk(nc, 64), batch), 64, kb * kb * sizeof(S), st>>>(A, sA, lda, n, k, kb); ++g_launches;
-      CKB(gemm_sb(hb, nc, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)(k + kb) * lda, lda, sA,
-                  A + (k + kb) + (size_t)(k + kb) * lda, lda, sA, batch));
+    if (KE < n) {
+      // U12 of the outer block (rows [K, KE), columns [KE, n)), blocked by nb
+      const int nc = n - KE;
+      for (int k = K; k < KE; k += nb) {
+        const int kb = std::min(nb, KE - k);
+        k_trsm_cols<S><<<dim3(nblk(nc, trsm_cols<S>()), batch), trsm_cols<S>(), 0, st>>>(A, sA, lda, k, kb, KE, n); ++g_launches;
+        if (k + kb < KE)
+          CKB(gemm_sb(hb, KE - k - kb, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)KE * lda, lda, sA,
+                      A + (k + kb) + (size_t)KE * lda, lda, sA, batch));
+      }
+      // trailing update of depth KE - K
+      CKB(gemm_sb(hb, nc, nc, KE - K, A + KE + (size_t)K * lda, lda, sA, A + K + (size_t)KE * lda, lda, sA,
+                  A + KE + (size_t)KE * lda, lda, sA, batch));
     }
   }
   CK(cudaGetLastError());
+  if (coop) {
+    int e = 0;
+    CK(cudaMemcpyAsync(&e, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (e) return fail(MFBEM_ETIMEOUT, "LU panel: a barrier wait timed out");
+  }
   return 0;
 }
 
@@ -90,18 +198,27 @@ __global__ void k_rhs_swap2(S* b, long long sb, int n, const int* ipiv, long lon
 template <typename S>
 static int getrs_batched(cudaStream_t st, const S* A, long long sA, int lda, int n, const int* ipiv, long long sP,
                          S* b, long long sb, int batch) {
-  const int TB = 128;
+  // diagonal blocks of TB rows solved by one warp (k_trsv_diag64), the rows
+  // below / above updated by a GEMV over the solved block
+  const int TB = 64;
+  const size_t dsm = (size_t)TB * 65 * sizeof(S);
+  static bool attr = false;
+  if (!attr) {
+    CK(cudaFuncSetAttribute(k_trsv_diag64<S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+    CK(cudaFuncSetAttribute(k_trsv_diag64<S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+    attr = true;
+  }
   k_rhs_swap2<S><<<nblk(batch, 64), 64, 0, st>>>(b, sb, n, ipiv, sP, batch); ++g_launches;
   for (int r0 = 0; r0 < n; r0 += TB) {
     int w = std::min(TB, n - r0);
-    k_trsv_diag<S, true><<<batch, TB, 0, st>>>(A, sA, lda, b, sb, r0, w); ++g_launches;
-    if (r0 + w < n) k_trsv_update<S><<<dim3(nblk(n - r0 - w, 256), batch), 256, 0, st>>>(A, sA, lda, b, sb, r0, w, r0 + w, n); ++g_launches;
+    k_trsv_diag64<S, true><<<batch, 128, dsm, st>>>(A, sA, lda, b, sb, r0, w); ++g_launches;
+    if (r0 + w < n) { k_trsv_update<S><<<dim3(nblk(n - r0 - w, 256), batch), 256, 0, st>>>(A, sA, lda, b, sb, r0, w, r0 + w, n); ++g_launches; }
   }
   int last = ((n - 1) / TB) * TB;
   for (int r0 = last; r0 >= 0; r0 -= TB) {
     int w = std::min(TB, n - r0);
-    k_trsv_diag<S, false><<<batch, TB, 0, st>>>(A, sA, lda, b, sb, r0, w); ++g_launches;
-    if (r0 > 0) k_trsv_update<S><<<dim3(nblk(r0, 256), batch), 256, 0, st>>>(A, sA, lda, b, sb, r0, w, 0, r0); ++g_launches;
+    k_trsv_diag64<S, false><<<batch, 128, dsm, st>>>(A, sA, lda, b, sb, r0, w); ++g_launches;
+    if (r0 > 0) { k_trsv_update<S><<<dim3(nblk(r0, 256), batch), 256, 0, st>>>(A, sA, lda, b, sb, r0, w, 0, r0); ++g_launches; }
   }
   CK(cudaGetLastError());
   return 0;
@@ -200,6 +317,46 @@ __device__ __forceinline__ double amag(double a) { return fabs(a); }
 __device__ __forceinline__ double amag(double2 a) { return hypot(a.x, a.y); }
 __device__ __forceinline__ double amag(float a) { return fabsf(a); }
 __device__ __forceinline__ double amag(float2 a) { return hypotf(a.x, a.y); }
+
+// FP32 copy of the FP64 systems and their row sums of |a_ij| (for the
+// infinity norm), in one pass: a CTA covers 256 rows x 128 columns, coalesced
+// along the rows; the moduli are taken in binary32 (the norm only scales the
+// stopping test) and the partial sums are added atomically.
+template <typename SD, typename SF>
+__global__ void __launch_bounds__(256) k_demote_rowabs(const SD* A, SF* A32, long long sA, int lda, int n, double* rows);
+template <>
+__global__ void __launch_bounds__(256) k_demote_rowabs<double2, float2>(const double2* A, float2* A32, long long sA,
+                                                                        int lda, int n, double* rows) {
+  const int b = blockIdx.z, i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= n) return;
+  const int j0 = blockIdx.y * 128, j1 = min(n, j0 + 128);
+  const double2* M = A + sA * b;
+  float2* M32 = A32 + sA * b;
+  float s = 0.0f;
+  for (int j = j0; j < j1; ++j) {
+    const double2 v = M[(size_t)j * lda + i];
+    const float2 f = make_float2((float)v.x, (float)v.y);
+    M32[(size_t)j * lda + i] = f;
+    s += hypotf(f.x, f.y);
+  }
+  atomicAdd(rows + (size_t)n * b + i, (double)s);
+}
+template <>
+__global__ void __launch_bounds__(256) k_demote_rowabs<double, float>(const double* A, float* A32, long long sA,
+                                                                      int lda, int n, double* rows) {
+  const int b = blockIdx.z, i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= n) return;
+  const int j0 = blockIdx.y * 128, j1 = min(n, j0 + 128);
+  const double* M = A + sA * b;
+  float* M32 = A32 + sA * b;
+  float s = 0.0f;
+  for (int j = j0; j < j1; ++j) {
+    const float f = (float)M[(size_t)j * lda + i];
+    M32[(size_t)j * lda + i] = f;
+    s += fabsf(f);
+  }
+  atomicAdd(rows + (size_t)n * b + i, (double)s);
+}
 
 // infinity norm of each batch's matrix: row sums of |a_ij|, then max
 template <typename S>
@@ -329,8 +486,8 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     double* nrm = (double*)((char*)h->work.p + sizeof(SF) * (size_t)n * batch);  // [batch][4]: |r|,|x|,|b|,|A|
     double* rows = nrm + 8 * batch;
     int* active = (int*)(rows + (size_t)n * batch);
-    k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, A32, nn * batch); ++g_launches;
-    k_rowabs<SD><<<dim3(nblk(n, 128), batch), 128, 0, st>>>(A, nn, n, n, rows); ++g_launches;
+    CK(cudaMemsetAsync(rows, 0, sizeof(double) * (size_t)n * batch, st));
+    k_demote_rowabs<SD, SF><<<dim3(nblk(n, 256), nblk(n, 128), batch), 256, 0, st>>>(A, A32, nn, n, n, rows); ++g_launches;
     k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, nrm, 3, 8); ++g_launches;
     k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, nrm, 2, 8); ++g_launches;
     if ((rc = getrf_batched<SF>(h->blas, st, A32, nn, n, n, batch, ipiv, info))) return rc;
