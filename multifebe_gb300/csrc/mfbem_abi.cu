@@ -376,20 +376,6 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
   if (cublasCreate(&h->blas) != CUBLAS_STATUS_SUCCESS) { mfbem_mesh_release(h); return fail(MFBEM_ECUDA, "cublasCreate"); }
   cublasSetStream(h->blas, h->st);
-  {
-    // single-precision GEMMs of the mixed LU (the trailing updates): SIMT FP32
-    // by default; MFBEM_FP32_GEMM=bf16x9 (or bf16x9-auto) lets cuBLAS emulate
-    // FP32 on the tensor cores with the BF16x9 split (measured slower for the
-    // batched rank-32/128 complex updates of the sweep). Double-precision
-    // GEMMs are unaffected.
-    const char* e = getenv("MFBEM_FP32_GEMM");
-    const std::string mode = e ? e : "simt";
-    if (mode != "simt") {
-      cublasSetMathMode(h->blas, CUBLAS_FP32_EMULATED_BF16X9_MATH);
-      cublasSetEmulationStrategy(h->blas, mode == "bf16x9-auto" ? CUBLAS_EMULATION_STRATEGY_PERFORMANT
-                                                                : CUBLAS_EMULATION_STRATEGY_EAGER);
-    }
-  }
   *out = h;
   return 0;
 }

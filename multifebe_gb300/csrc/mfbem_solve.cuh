@@ -5,6 +5,17 @@
 // ---------------------------------------------------------------------------
 // GEMM dispatch for the trailing update A22 -= L21 U12 (plain library GEMM)
 // ---------------------------------------------------------------------------
+// Compute type of the single-precision trailing updates of the mixed LU:
+// 0 SIMT FP32, 1 TF32 tensor cores (the factors are then a TF32-accurate
+// preconditioner; refinement in FP64 restores the accuracy and escalates to
+// SIMT FP32 when it stalls), 2 cuBLAS's BF16x9 FP32 emulation. Default TF32;
+// MFBEM_FP32_GEMM=simt|tf32|bf16x9 overrides.
+static int g_c32_mode = 1;
+static int c32_default() {
+  const char* e = getenv("MFBEM_FP32_GEMM");
+  const std::string v = e ? e : "tf32";
+  return v == "simt" ? 0 : (v == "bf16x9" ? 2 : 1);
+}
 static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const double* A, int lda, long long sA,
                               const double* B, int ldb, long long sB, double* C, int ldc, long long sC, int batch) {
   const double al = -1.0, be = 1.0;
@@ -14,6 +25,11 @@ static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const doub
 static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const float* A, int lda, long long sA,
                               const float* B, int ldb, long long sB, float* C, int ldc, long long sC, int batch) {
   const float al = -1.0f, be = 1.0f;
+  if (g_c32_mode > 0)
+    return cublasGemmStridedBatchedEx(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, CUDA_R_32F, lda, sA, B, CUDA_R_32F,
+                                      ldb, sB, &be, C, CUDA_R_32F, ldc, sC, batch,
+                                      g_c32_mode == 1 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F_EMULATED_16BFX9,
+                                      CUBLAS_GEMM_DEFAULT);
   return cublasSgemmStridedBatched(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, lda, sA, B, ldb, sB, &be, C, ldc,
                                    sC, batch);
 }
@@ -26,6 +42,12 @@ static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const doub
 static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const float2* A, int lda, long long sA,
                               const float2* B, int ldb, long long sB, float2* C, int ldc, long long sC, int batch) {
   const cuComplex al = make_cuComplex(-1.0f, 0.0f), be = make_cuComplex(1.0f, 0.0f);
+  const int mode = g_c32_mode;
+  if (mode > 0)
+    return cublasGemmStridedBatchedEx(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, CUDA_C_32F, lda, sA, B, CUDA_C_32F,
+                                      ldb, sB, &be, C, CUDA_C_32F, ldc, sC, batch,
+                                      mode == 1 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F_EMULATED_16BFX9,
+                                      CUBLAS_GEMM_DEFAULT);
   return cublasCgemmStridedBatched(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, (const cuComplex*)A, lda, sA,
                                    (const cuComplex*)B, ldb, sB, &be, (cuComplex*)C, ldc, sC, batch);
 }
@@ -490,37 +512,66 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     k_demote_rowabs<SD, SF><<<dim3(nblk(n, 256), nblk(n, 128), batch), 256, 0, st>>>(A, A32, nn, n, n, rows); ++g_launches;
     k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, nrm, 3, 8); ++g_launches;
     k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, nrm, 2, 8); ++g_launches;
+    g_c32_mode = c32_default();
     if ((rc = getrf_batched<SF>(h->blas, st, A32, nn, n, n, batch, ipiv, info))) return rc;
     cudaEventRecord(e1, st);
     // x = 0, r = b, then iterate x += LU^{-1} r
     CK(cudaMemsetAsync(x, 0, sizeof(SD) * (size_t)n * batch, st));
     std::vector<int> hact(batch, 1);
-    std::vector<double> hn(8 * batch);
-    int it = 0;
+    std::vector<double> hn(8 * batch), prev(batch, 1.0);
+    int it = 0, itot = 0, stall = 0;
     double maxbe = 0.0;
     const int maxit = 30;
-    for (; it <= maxit; ++it) {
+    float ms_refactor = 0.0f;
+    for (;; ++it, ++itot) {
       k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(b, r, (long long)n * batch); ++g_launches;
-      if (it > 0) CKB(gemv_res(h->blas, n, A, n, nn, x, n, r, n, batch));
+      if (itot > 0) CKB(gemv_res(h->blas, n, A, n, nn, x, n, r, n, batch));
       k_vecmax<SD><<<batch, 256, 0, st>>>(r, n, n, nrm, 0, 8); ++g_launches;
       k_vecmax<SD><<<batch, 256, 0, st>>>(x, n, n, nrm, 1, 8); ++g_launches;
       CK(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 8 * batch, cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      bool any = false;
+      bool any = false, slow = false;
       maxbe = 0.0;
       for (int bi = 0; bi < batch; ++bi) {
         double be = hn[8 * bi + 0] / (hn[8 * bi + 3] * hn[8 * bi + 1] + hn[8 * bi + 2]);
-        if (it == 0) be = 1.0;
+        if (itot == 0) be = 1.0;
         maxbe = std::max(maxbe, be);
         hact[bi] = (be > tol) ? 1 : 0;
         any = any || hact[bi];
+        // contraction slower than 1/4 per step after the first correction
+        if (hact[bi] && it >= 2 && be > 0.25 * prev[bi]) slow = true;
+        prev[bi] = be;
       }
-      if (!any || it == maxit) break;
+      if (!any || itot >= maxit) break;
+      stall = slow ? stall + 1 : 0;
+      if (stall >= 2 && g_c32_mode != 0) {
+        // the tensor-core factors are too coarse for this system: refactor
+        // with SIMT FP32 updates and continue from the current x
+        cudaEvent_t f0, f1;
+        cudaEventCreate(&f0);
+        cudaEventCreate(&f1);
+        cudaEventRecord(f0, st);
+        g_c32_mode = 0;
+        k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, A32, nn * batch); ++g_launches;
+        if ((rc = getrf_batched<SF>(h->blas, st, A32, nn, n, n, batch, ipiv, info))) return rc;
+        cudaEventRecord(f1, st);
+        cudaEventSynchronize(f1);
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, f0, f1);
+        ms_refactor += t;
+        cudaEventDestroy(f0);
+        cudaEventDestroy(f1);
+        stall = 0;
+        it = 0;
+      }
       CK(cudaMemcpyAsync(active, hact.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, st));
       k_scale_demote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(r, n, d32, n, n, nrm, 8, 0); ++g_launches;
       if ((rc = getrs_batched<SF>(st, A32, nn, n, n, ipiv, n, d32, n, batch))) return rc;
       k_update<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(x, n, d32, n, n, nrm, 8, 0, active); ++g_launches;
     }
+    it = itot;
+    stats->ms_factor += ms_refactor;
+    stats->ms_solve -= ms_refactor;
     cudaEventRecord(e2, st);
     CK(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));

@@ -183,3 +183,26 @@ def test_zexp_double_float_matches_fp64():
     scale = np.maximum.reduce([np.exp(z[~small].real), np.ones_like(a), a, a ** 2 / 2, a ** 3 / 6, a ** 4 / 24])
     ra = np.abs(F[~small] - E[~small]).max(1) / scale
     assert ra.max() < 2e-13, (ra.max(), z[~small][ra.argmax()])
+
+
+@pytest.mark.parametrize("gemm", ["simt", "tf32"])
+@pytest.mark.parametrize("name,mk", [("cube4", lambda: M.cube_clamped_top_traction(4)), ("slab4", lambda: M.slab(4, 1)),
+                                     ("patch8", lambda: M.surface_patch(10.0, 8, 1.0))],
+                         ids=["cube4", "slab4", "patch8"])
+def test_mixed_sweep_trailing_update_modes(oracle, monkeypatch, gemm, name, mk):
+    """Mixed sweep with SIMT FP32 and TF32 tensor-core trailing updates: both
+    reach the FP64 oracle solution to 1e-8 (TF32 factors are refined in FP64,
+    and escalate to SIMT FP32 when refinement stalls)."""
+    monkeypatch.setenv("MFBEM_FP32_GEMM", gemm)
+    d = mk()
+    mat = M.viscoelastic(1.0, 0.3, 1.0, 0.05)
+    om = M.omega_from_a0([0.3, 1.2], mat)
+    R = BemRegion(d)
+    P = oracle.Problem(d)
+    X = R.sweep_harela(mat, om, precision="mixed")
+    for i, w in enumerate(om):
+        Ao, bo = P.assemble_harela(mat, w)
+        xo = oracle.lu_solve(Ao, bo)
+        assert rel(X[i], xo) < 1e-8, (gemm, name, i, rel(X[i], xo))
+    assert R.last_stats["max_backward_error"] <= 1e-12
+    R.close()
