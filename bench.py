@@ -136,11 +136,17 @@ def run_reference(args):
 def run_gpu(args):
     ws, rank = _dist()
     if ws > 1:
+        # one GPU per rank, selected before the library initialises CUDA
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", str(rank)))
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    from multifebe_gb300 import meshgen as M, BemRegion, _abi
+    from multifebe_gb300 import meshgen as M, BemRegion, _abi, shard
     from multifebe_gb300.bem import _p
     deck, mat, om = M.workload(2)
+    if ws > 1:
+        # weak scaling: a 20*N-frequency sweep over a0 in [0.1, 2.0], 20 per rank
+        om_all = M.omega_from_a0(shard.weak_scaled_frequencies(0.1, 2.0, len(om), ws), mat)
+        om = om_all[shard.frequency_shard(len(om_all), rank, ws)]
     nf = len(om)
     R = BemRegion(deck)
     n = R.n
