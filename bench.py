@@ -42,9 +42,10 @@ WORKLOAD_P = "harela surface patch 40x40 quad8 (20x20), 14883 complex DOF, a0=0.
 # scalings and dr 24, u*/t* components 168, 120 complex accumulations 480.
 FLOPS_PER_REGULAR_POINT = 1280
 # DRAM bytes per frequency of that kernel from ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum of one launch of the 2-frequency profile case divided
-# by 2; profiles/k_reg_mixed_cube8.md).
-REG_TRAFFIC_PER_FREQ = None
+# dram__bytes_write.sum of one launch of the 2-frequency profile case, 454.1 +
+# 408.1 MB, divided by 2; profiles/k_mixed_cube8x2freq.md). Traffic grows in
+# proportion to the frequencies (one system per frequency).
+REG_TRAFFIC_PER_FREQ = 431.1e6
 
 
 def _dist():
