@@ -108,6 +108,8 @@ typedef struct mfbem_stats {
      library's stream): regular, adaptive, singular pairs and free terms */
   double ms_regular, ms_adaptive, ms_singular, ms_free;
   int64_t kernel_launches;       /* this library's kernels launched by the call */
+  int32_t gmres_iterations;      /* mixed: inner GMRES steps of GMRES-based refinement (0: classical only) */
+  int32_t refactorizations;      /* mixed: FP32 refactorisations after TF32 factors stalled the refinement */
 } mfbem_stats;
 
 /* mesh lifetime */
@@ -142,7 +144,12 @@ int mfbem_solve_c(int32_t n, double* A, int32_t* ipiv, int32_t aodim, double* Ao
    precision 0: plain FP64 LU (the drop-in method).
    precision 1: complex64 LU with FP64 iterative refinement to rel_tol in the
                 backward error (the FP64 residual r = b - A x is evaluated with
-                the FP64 matrix).
+                the FP64 matrix): classical refinement, switching to
+                GMRES-based refinement (FP64 GMRES preconditioned by the LU
+                factors) when it stalls; the trailing updates of the LU run on
+                the TF32 tensor cores and are redone in SIMT FP32 when even
+                GMRES-based refinement does not converge.
+   precision 2: as 1, with GMRES-based refinement from the start.
    x_out receives n_dof complex values per frequency (column f at f*n_dof).
    The right-hand side is the one assembled from the prescribed values. */
 int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho, const double nu[2],

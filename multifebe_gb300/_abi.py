@@ -56,7 +56,7 @@ class Stats(ctypes.Structure):
         ("adaptive_leaves", c_int32), ("refinement_iterations", c_int32), ("max_backward_error", c_double),
         ("ms_assemble", c_double), ("ms_factor", c_double), ("ms_solve", c_double),
         ("ms_regular", c_double), ("ms_adaptive", c_double), ("ms_singular", c_double), ("ms_free", c_double),
-        ("kernel_launches", ctypes.c_int64),
+        ("kernel_launches", ctypes.c_int64), ("gmres_iterations", c_int32), ("refactorizations", c_int32),
     ]
 
     def as_dict(self):

@@ -28,6 +28,10 @@ DEFAULT_SETTINGS = dict(qsi_relative_error=1e-6, qsi_ns_max=16, precalset_gln=(2
                         geometric_tolerance=1e-6)
 
 
+# precision argument of mfbem_sweep_harela / mfbem_solve_staela
+PRECISION = {"plain": 0, "mixed": 1, "mixed-gmres": 2}
+
+
 def _p(a, t=_dp):
     return a.ctypes.data_as(t)
 
@@ -119,7 +123,9 @@ class BemRegion:
     # ---------------------------------------------------------------- device pipelines
     def sweep_harela(self, mat, omegas, precision="plain", rel_tol=1e-12):
         """Assemble + factorise + solve every frequency on the device.
-        precision 'plain': FP64 LU; 'mixed': complex64 LU + FP64 refinement."""
+        precision 'plain': FP64 LU; 'mixed': complex64 LU + FP64 refinement
+        (classical, then GMRES-based when it stalls); 'mixed-gmres': complex64
+        LU + GMRES-based refinement from the start."""
         om = np.ascontiguousarray(omegas, dtype=np.float64)
         nf = om.size
         X = np.zeros((nf, self.n), dtype=np.complex128)
@@ -127,7 +133,7 @@ class BemRegion:
         mu = np.array([complex(mat["mu"]).real, complex(mat["mu"]).imag])
         nu = np.array([complex(mat["nu"]).real, complex(mat["nu"]).imag])
         st = _abi.Stats()
-        prec = {"plain": 0, "mixed": 1}[precision]
+        prec = PRECISION[precision]
         check(_abi.load().mfbem_sweep_harela(self._h, _p(lam), _p(mu), float(mat["rho"]), _p(nu), nf, _p(om), prec,
                                              rel_tol, _p(X), 0, ctypes.byref(st)))
         self.last_stats = st.as_dict()
@@ -136,7 +142,7 @@ class BemRegion:
     def solve_staela(self, mu, nu, precision="plain", rel_tol=1e-12):
         x = np.zeros(self.n, dtype=np.float64)
         st = _abi.Stats()
-        prec = {"plain": 0, "mixed": 1}[precision]
+        prec = PRECISION[precision]
         check(_abi.load().mfbem_solve_staela(self._h, float(mu), float(nu), prec, rel_tol, _p(x), 0,
                                              ctypes.byref(st)))
         self.last_stats = st.as_dict()

@@ -7,6 +7,8 @@
 #include <algorithm>
 #include <type_traits>
 #include <chrono>
+#include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -59,7 +61,7 @@ struct mfbem_handle {
   int ndof = 0, ne = 0, nn = 0;
   cudaStream_t st = nullptr;
   cublasHandle_t blas = nullptr;
-  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, Af, geo_f;
+  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, Af, geo_f, gm;
   mfbem_stats stats{};
   long long pts_reg = 0, pts_adp = 0, pts_sing = 0;
   int* d_err = nullptr;
@@ -385,7 +387,7 @@ extern "C" int mfbem_mesh_release(mfbem_handle* h) {
   cudaDeviceSynchronize();
   for (void* p : h->owned) cudaFree(p);
   for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu, &h->parf,
-                    &h->pphi_f, &h->Af, &h->geo_f})
+                    &h->pphi_f, &h->Af, &h->geo_f, &h->gm})
     if (b->p) cudaFree(b->p);
   if (h->blas) cublasDestroy(h->blas);
   if (h->st) cudaStreamDestroy(h->st);

@@ -470,6 +470,325 @@ static cublasStatus_t gemv_res(cublasHandle_t hb, int n, const double2* A, int l
                                    (const cuDoubleComplex*)x, 1, sx, &be, (cuDoubleComplex*)r, 1, sr, batch);
 }
 
+// y = A x
+static cublasStatus_t gemv_apply(cublasHandle_t hb, int n, const double* A, int lda, long long sA, const double* x,
+                                 long long sx, double* y, long long sy, int batch) {
+  const double al = 1.0, be = 0.0;
+  return cublasDgemvStridedBatched(hb, CUBLAS_OP_N, n, n, &al, A, lda, sA, x, 1, sx, &be, y, 1, sy, batch);
+}
+static cublasStatus_t gemv_apply(cublasHandle_t hb, int n, const double2* A, int lda, long long sA, const double2* x,
+                                 long long sx, double2* y, long long sy, int batch) {
+  const cuDoubleComplex al = make_cuDoubleComplex(1.0, 0.0), be = make_cuDoubleComplex(0.0, 0.0);
+  return cublasZgemvStridedBatched(hb, CUBLAS_OP_N, n, n, &al, (const cuDoubleComplex*)A, lda, sA,
+                                   (const cuDoubleComplex*)x, 1, sx, &be, (cuDoubleComplex*)y, 1, sy, batch);
+}
+
+// ---------------------------------------------------------------------------
+// GMRES-based iterative refinement (Carson & Higham, SIAM J. Sci. Comput. 40(2),
+// 2018): each correction d solves A d = r by GMRES in FP64, left-preconditioned
+// with the FP32 (or TF32-updated) LU factors, M^-1 A d = M^-1 r. Batched over
+// the systems of a sweep; the small Hessenberg least-squares problems run on
+// the host with Givens rotations; orthogonalisation is classical Gram-Schmidt
+// applied twice.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 cdot_term(double2 a, double2 b) {  // conj(a) * b
+  return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double cdot_term(double a, double b) { return a * b; }
+__device__ __forceinline__ double2 add2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double add2(double a, double b) { return a + b; }
+__device__ __forceinline__ double2 shfl_dn(double2 v, int o) {
+  return make_double2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o));
+}
+__device__ __forceinline__ double shfl_dn(double v, int o) { return __shfl_down_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double2 zmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double zmul(double a, double b) { return a * b; }
+
+// out[b][i] = V_i^H w (i < nv), V_i = V + b*sVb + i*n, w = W + b*sW
+template <typename SD>
+__global__ void k_bdot(const SD* V, long long sVb, int nv, const SD* W, long long sW, int n, SD* out, int ldo) {
+  const int i = blockIdx.x, b = blockIdx.y;
+  const SD* v = V + sVb * b + (long long)i * n;
+  const SD* w = W + sW * b;
+  SD acc = Sc<SD>::zero();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) acc = add2(acc, cdot_term(v[k], w[k]));
+  for (int o = 16; o > 0; o >>= 1) acc = add2(acc, shfl_dn(acc, o));
+  __shared__ SD sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x / 32] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    SD t = sm[0];
+    for (int q = 1; q < (int)blockDim.x / 32; ++q) t = add2(t, sm[q]);
+    out[(size_t)ldo * b + i] = t;
+  }
+}
+__device__ __forceinline__ double2 rscal(double2 a, double f) { return make_double2(a.x * f, a.y * f); }
+__device__ __forceinline__ double rscal(double a, double f) { return a * f; }
+
+// w[b] += sign * sum_{i<nv} V_i c[b][i]  (sign -1: Gram-Schmidt; +1: x += V y)
+template <typename SD>
+__global__ void k_bcomb(SD* W, long long sW, const SD* V, long long sVb, int nv, const SD* c, int ldc, int n,
+                        double sign, const int* active) {
+  const int b = blockIdx.y, k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n || (active && !active[b])) return;
+  const SD* v = V + sVb * b + k;
+  SD acc = Sc<SD>::zero();
+  for (int i = 0; i < nv; ++i) acc = add2(acc, zmul(v[(long long)i * n], c[(size_t)ldc * b + i]));
+  W[sW * b + k] = add2(W[sW * b + k], rscal(acc, sign));
+}
+// out[b] = in[b] * s[b] (s real)
+template <typename SD>
+__global__ void k_bscale(const SD* in, long long sIn, SD* out, long long sOut, int n, const double* s) {
+  const int b = blockIdx.y, k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  out[sOut * b + k] = rscal(in[sIn * b + k], s[b]);
+}
+// FP64 out = nrm[b] * (FP64) in32  (promotion of a preconditioner application)
+template <typename SD, typename SF>
+__global__ void k_promote(const SF* in, long long sIn, SD* out, long long sOut, int n, const double* nrm, int nslots,
+                          int slot);
+template <>
+__global__ void k_promote<double2, float2>(const float2* in, long long sIn, double2* out, long long sOut, int n,
+                                           const double* nrm, int nslots, int slot) {
+  const int b = blockIdx.y, k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double s = nrm[(size_t)nslots * b + slot];
+  const float2 v = in[sIn * b + k];
+  out[sOut * b + k] = make_double2(s * (double)v.x, s * (double)v.y);
+}
+template <>
+__global__ void k_promote<double, float>(const float* in, long long sIn, double* out, long long sOut, int n,
+                                         const double* nrm, int nslots, int slot) {
+  const int b = blockIdx.y, k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  out[sOut * b + k] = nrm[(size_t)nslots * b + slot] * (double)in[sIn * b + k];
+}
+
+// State of the mixed solve of one batch.
+template <typename SD, typename SF>
+struct MixCtx {
+  mfbem_handle* h;
+  SD* A;
+  SF* A32;
+  int* ipiv;
+  int n, batch;
+  const SD* b;
+  SD *x, *r;
+  SF* d32;
+  double* nrm;
+  int* active;
+  double tol;
+  int it = 0, inner = 0, refactor = 0;
+  double maxbe = 0.0;
+  std::vector<double> be;
+};
+
+// r = b - A x, backward errors ||r|| / (||A|| ||x|| + ||b||) (infinity norms);
+// active[b] = not yet converged. Returns whether all converged.
+template <typename SD, typename SF>
+static int residual_check(MixCtx<SD, SF>& c, bool first, bool* all) {
+  cudaStream_t st = c.h->st;
+  const int n = c.n, batch = c.batch;
+  const long long nn = (long long)n * n;
+  k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(c.b, c.r, (long long)n * batch); ++g_launches;
+  if (!first) CKB(gemv_res(c.h->blas, n, c.A, n, nn, c.x, n, c.r, n, batch));
+  k_vecmax<SD><<<batch, 256, 0, st>>>(c.r, n, n, c.nrm, 0, 8); ++g_launches;
+  k_vecmax<SD><<<batch, 256, 0, st>>>(c.x, n, n, c.nrm, 1, 8); ++g_launches;
+  std::vector<double> hn(8 * (size_t)batch);
+  CK(cudaMemcpyAsync(hn.data(), c.nrm, sizeof(double) * 8 * batch, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  c.be.assign(batch, 1.0);
+  std::vector<int> hact(batch);
+  c.maxbe = 0.0;
+  bool any = false;
+  for (int bi = 0; bi < batch; ++bi) {
+    double be = first ? 1.0 : hn[8 * bi + 0] / (hn[8 * bi + 3] * hn[8 * bi + 1] + hn[8 * bi + 2]);
+    c.be[bi] = be;
+    c.maxbe = std::max(c.maxbe, be);
+    hact[bi] = be > c.tol ? 1 : 0;
+    any = any || hact[bi];
+  }
+  CK(cudaMemcpyAsync(c.active, hact.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, st));
+  *all = !any;
+  return 0;
+}
+
+// out = M^-1 u for every system (FP64 in and out, FP32 factors): scale by
+// ||u||_inf, demote, getrs, promote
+template <typename SD, typename SF>
+static int precond(MixCtx<SD, SF>& c, const SD* u, SD* out) {
+  cudaStream_t st = c.h->st;
+  const int n = c.n, batch = c.batch;
+  const long long nn = (long long)n * n;
+  k_vecmax<SD><<<batch, 256, 0, st>>>(u, n, n, c.nrm, 4, 8); ++g_launches;
+  k_scale_demote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(u, n, c.d32, n, n, c.nrm, 8, 4); ++g_launches;
+  int rc = getrs_batched<SF>(st, c.A32, nn, n, n, c.ipiv, n, c.d32, n, batch);
+  if (rc) return rc;
+  k_promote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(c.d32, n, out, n, n, c.nrm, 8, 4); ++g_launches;
+  return 0;
+}
+
+// Classical refinement x += M^-1 (b - A x). *conv = 1 when every system reaches
+// tol; returns early (conv 0) when the contraction per step is slower than 1/4
+// twice in a row, or after 30 steps.
+template <typename SD, typename SF>
+static int refine_classical(MixCtx<SD, SF>& c, int* conv) {
+  cudaStream_t st = c.h->st;
+  const int n = c.n, batch = c.batch;
+  const long long nn = (long long)n * n;
+  std::vector<double> prev(batch, 1.0);
+  int stall = 0;
+  *conv = 0;
+  for (int it = 0;; ++it) {
+    bool all;
+    int rc = residual_check(c, c.it == 0, &all);
+    if (rc) return rc;
+    if (all) { *conv = 1; return 0; }
+    bool slow = false;
+    for (int bi = 0; bi < batch; ++bi)
+      if (c.be[bi] > c.tol && it >= 2 && c.be[bi] > 0.25 * prev[bi]) slow = true;
+    prev = c.be;
+    stall = slow ? stall + 1 : 0;
+    if (stall >= 2 || it >= 30) return 0;
+    k_scale_demote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(c.r, n, c.d32, n, n, c.nrm, 8, 0); ++g_launches;
+    if ((rc = getrs_batched<SF>(st, c.A32, nn, n, n, c.ipiv, n, c.d32, n, batch))) return rc;
+    k_update<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(c.x, n, c.d32, n, n, c.nrm, 8, 0, c.active); ++g_launches;
+    ++c.it;
+  }
+}
+
+// GMRES-IR: up to 10 outer corrections, each a GMRES(m) solve of
+// M^-1 A d = M^-1 r to 1e-6 relative (preconditioned residual).
+template <typename SD, typename SF>
+static int refine_gmres(MixCtx<SD, SF>& c, int* conv) {
+  typedef std::complex<double> C;
+  cudaStream_t st = c.h->st;
+  const int n = c.n, batch = c.batch, m = 20;
+  const long long nn = (long long)n * n;
+  int rc;
+  // work: V [batch][m+1][n], w [batch][n], coefficients [batch][m+1], scales [batch]
+  const size_t vbytes = sizeof(SD) * (size_t)batch * (m + 1) * n, wbytes = sizeof(SD) * (size_t)batch * n;
+  const size_t cbytes = sizeof(SD) * (size_t)batch * (m + 1), sbytes = sizeof(double) * batch;
+  if ((rc = ensure(c.h->gm, vbytes + wbytes + 2 * cbytes + sbytes + 64))) return rc;
+  SD* V = (SD*)c.h->gm.p;
+  SD* w = (SD*)((char*)V + vbytes);
+  SD* hc = (SD*)((char*)w + wbytes);
+  SD* hc2 = (SD*)((char*)hc + cbytes);
+  double* sc = (double*)((char*)hc2 + cbytes);
+  const long long sV = (long long)(m + 1) * n;
+  std::vector<SD> hh(batch * (size_t)(m + 1)), hh2(batch * (size_t)(m + 1));
+  std::vector<double> hs(batch);
+  auto toC = [](const SD& v) -> C {
+    if constexpr (std::is_same<SD, double2>::value) return C(v.x, v.y);
+    else return C(v, 0.0);
+  };
+  auto fromC = [](const C& v) -> SD {
+    if constexpr (std::is_same<SD, double2>::value) return make_double2(v.real(), v.imag());
+    else return v.real();
+  };
+  *conv = 0;
+  for (int outer = 0; outer < 10; ++outer) {
+    bool all;
+    if ((rc = residual_check(c, c.it == 0 && outer == 0, &all))) return rc;
+    if (all) { *conv = 1; return 0; }
+    ++c.it;
+    // z = M^-1 r -> V_0 = z / beta
+    if ((rc = precond(c, c.r, w))) return rc;
+    k_bdot<SD><<<dim3(1, batch), 256, 0, st>>>(w, n, 1, w, n, n, hc, m + 1); ++g_launches;
+    CK(cudaMemcpyAsync(hh.data(), hc, cbytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<double> beta(batch);
+    std::vector<int> kb(batch, 0), done(batch, 0);
+    std::vector<std::vector<C>> H(batch, std::vector<C>((size_t)(m + 1) * m)), g(batch, std::vector<C>(m + 1));
+    std::vector<std::vector<double>> cs(batch, std::vector<double>(m));
+    std::vector<std::vector<C>> sn(batch, std::vector<C>(m));
+    for (int bi = 0; bi < batch; ++bi) {
+      beta[bi] = std::sqrt(std::max(0.0, toC(hh[(size_t)(m + 1) * bi]).real()));
+      done[bi] = !(c.be[bi] > c.tol) || beta[bi] == 0.0;
+      hs[bi] = beta[bi] > 0.0 ? 1.0 / beta[bi] : 0.0;
+      g[bi][0] = beta[bi];
+    }
+    CK(cudaMemcpyAsync(sc, hs.data(), sbytes, cudaMemcpyHostToDevice, st));
+    k_bscale<SD><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(w, n, V, sV, n, sc); ++g_launches;
+    int j = 0;
+    for (; j < m; ++j) {
+      // w = M^-1 A V_j
+      CKB(gemv_apply(c.h->blas, n, c.A, n, nn, V + (long long)j * n, sV, c.r, n, batch));
+      if ((rc = precond(c, c.r, w))) return rc;
+      // classical Gram-Schmidt, twice
+      k_bdot<SD><<<dim3(j + 1, batch), 256, 0, st>>>(V, sV, j + 1, w, n, n, hc, m + 1); ++g_launches;
+      k_bcomb<SD><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(w, n, V, sV, j + 1, hc, m + 1, n, -1.0, nullptr); ++g_launches;
+      k_bdot<SD><<<dim3(j + 1, batch), 256, 0, st>>>(V, sV, j + 1, w, n, n, hc2, m + 1); ++g_launches;
+      k_bcomb<SD><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(w, n, V, sV, j + 1, hc2, m + 1, n, -1.0, nullptr); ++g_launches;
+      CK(cudaMemcpyAsync(hh.data(), hc, cbytes, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(hh2.data(), hc2, cbytes, cudaMemcpyDeviceToHost, st));
+      k_bdot<SD><<<dim3(1, batch), 256, 0, st>>>(w, n, 1, w, n, n, hc, m + 1); ++g_launches;
+      std::vector<SD> nw(batch * (size_t)(m + 1));
+      CK(cudaMemcpyAsync(nw.data(), hc, cbytes, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      bool all_done = true;
+      for (int bi = 0; bi < batch; ++bi) {
+        const double hn1 = std::sqrt(std::max(0.0, toC(nw[(size_t)(m + 1) * bi]).real()));
+        hs[bi] = 0.0;
+        if (done[bi]) continue;
+        C* Hc = &H[bi][(size_t)(m + 1) * j];
+        for (int i = 0; i <= j; ++i)
+          Hc[i] = toC(hh[(size_t)(m + 1) * bi + i]) + toC(hh2[(size_t)(m + 1) * bi + i]);
+        Hc[j + 1] = hn1;
+        for (int i = 0; i < j; ++i) {  // previous rotations
+          const C a = Hc[i], bq = Hc[i + 1];
+          Hc[i] = cs[bi][i] * a + sn[bi][i] * bq;
+          Hc[i + 1] = -std::conj(sn[bi][i]) * a + cs[bi][i] * bq;
+        }
+        const C a = Hc[j];
+        const double bq = std::abs(Hc[j + 1]), aa = std::abs(a), t = std::hypot(aa, bq);
+        if (t == 0.0) { cs[bi][j] = 1.0; sn[bi][j] = 0.0; }
+        else if (aa == 0.0) { cs[bi][j] = 0.0; sn[bi][j] = 1.0; Hc[j] = bq; }
+        else {
+          const C ph = a / aa;
+          cs[bi][j] = aa / t;
+          sn[bi][j] = ph * std::conj(Hc[j + 1]) / t;
+          Hc[j] = ph * t;
+        }
+        Hc[j + 1] = 0.0;
+        g[bi][j + 1] = -std::conj(sn[bi][j]) * g[bi][j];
+        g[bi][j] = cs[bi][j] * g[bi][j];
+        kb[bi] = j + 1;
+        ++c.inner;
+        if (std::abs(g[bi][j + 1]) <= 1e-6 * beta[bi] || hn1 == 0.0) done[bi] = 1;
+        else hs[bi] = 1.0 / hn1;
+        all_done = all_done && done[bi];
+      }
+      if (all_done || j + 1 == m) { ++j; break; }
+      CK(cudaMemcpyAsync(sc, hs.data(), sbytes, cudaMemcpyHostToDevice, st));
+      k_bscale<SD><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(w, n, V + (long long)(j + 1) * n, sV, n, sc); ++g_launches;
+    }
+    // y = H^-1 g (upper triangular, kb x kb), x += V y
+    std::vector<SD> yv(batch * (size_t)(m + 1));
+    for (int bi = 0; bi < batch; ++bi) {
+      const int k = kb[bi];
+      std::vector<C> y(k);
+      for (int i = k - 1; i >= 0; --i) {
+        C sum = g[bi][i];
+        for (int q = i + 1; q < k; ++q) sum -= H[bi][(size_t)(m + 1) * q + i] * y[q];
+        y[i] = sum / H[bi][(size_t)(m + 1) * i + i];
+      }
+      for (int i = 0; i <= m; ++i) yv[(size_t)(m + 1) * bi + i] = fromC(i < k ? y[i] : C(0.0));
+    }
+    CK(cudaMemcpyAsync(hc, yv.data(), cbytes, cudaMemcpyHostToDevice, st));
+    int kmax = 0;
+    for (int bi = 0; bi < batch; ++bi) kmax = std::max(kmax, kb[bi]);
+    if (kmax > 0) {
+      k_bcomb<SD><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(c.x, n, V, sV, kmax, hc, m + 1, n, 1.0, c.active);
+      ++g_launches;
+    }
+  }
+  bool all;
+  if ((rc = residual_check(c, false, &all))) return rc;
+  *conv = all ? 1 : 0;
+  return 0;
+}
+
 // Solve the batch of FP64 systems (A_f, b_f) in place of x. precision 0: FP64
 // LU; 1: FP32 LU + FP64 refinement. Work memory from the handle.
 template <typename SD, typename SF>
@@ -502,82 +821,68 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     if ((rc = ensure(h->A32, sizeof(SF) * nn * batch)) || (rc = ensure(h->r, sizeof(SD) * (size_t)n * batch)) ||
         (rc = ensure(h->work, sizeof(SF) * (size_t)n * batch + sizeof(double) * ((size_t)n * batch + 8 * batch) + 4 * batch)))
       return rc;
-    SF* A32 = (SF*)h->A32.p;
-    SD* r = (SD*)h->r.p;
-    SF* d32 = (SF*)h->work.p;
-    double* nrm = (double*)((char*)h->work.p + sizeof(SF) * (size_t)n * batch);  // [batch][4]: |r|,|x|,|b|,|A|
-    double* rows = nrm + 8 * batch;
-    int* active = (int*)(rows + (size_t)n * batch);
+    MixCtx<SD, SF> c;
+    c.h = h;
+    c.A = A;
+    c.A32 = (SF*)h->A32.p;
+    c.ipiv = ipiv;
+    c.n = n;
+    c.batch = batch;
+    c.b = b;
+    c.x = x;
+    c.r = (SD*)h->r.p;
+    c.d32 = (SF*)h->work.p;
+    c.nrm = (double*)((char*)h->work.p + sizeof(SF) * (size_t)n * batch);  // [batch][8]: |r|,|x|,|b|,|A|,precond scale
+    double* rows = c.nrm + 8 * batch;
+    c.active = (int*)(rows + (size_t)n * batch);
+    c.tol = tol;
     CK(cudaMemsetAsync(rows, 0, sizeof(double) * (size_t)n * batch, st));
-    k_demote_rowabs<SD, SF><<<dim3(nblk(n, 256), nblk(n, 128), batch), 256, 0, st>>>(A, A32, nn, n, n, rows); ++g_launches;
-    k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, nrm, 3, 8); ++g_launches;
-    k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, nrm, 2, 8); ++g_launches;
+    k_demote_rowabs<SD, SF><<<dim3(nblk(n, 256), nblk(n, 128), batch), 256, 0, st>>>(A, c.A32, nn, n, n, rows); ++g_launches;
+    k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, c.nrm, 3, 8); ++g_launches;
+    k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, c.nrm, 2, 8); ++g_launches;
     g_c32_mode = c32_default();
-    if ((rc = getrf_batched<SF>(h->blas, st, A32, nn, n, n, batch, ipiv, info))) return rc;
+    if ((rc = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info))) return rc;
     cudaEventRecord(e1, st);
-    // x = 0, r = b, then iterate x += LU^{-1} r
     CK(cudaMemsetAsync(x, 0, sizeof(SD) * (size_t)n * batch, st));
-    std::vector<int> hact(batch, 1);
-    std::vector<double> hn(8 * batch), prev(batch, 1.0);
-    int it = 0, itot = 0, stall = 0;
-    double maxbe = 0.0;
-    const int maxit = 30;
-    float ms_refactor = 0.0f;
-    for (;; ++it, ++itot) {
-      k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(b, r, (long long)n * batch); ++g_launches;
-      if (itot > 0) CKB(gemv_res(h->blas, n, A, n, nn, x, n, r, n, batch));
-      k_vecmax<SD><<<batch, 256, 0, st>>>(r, n, n, nrm, 0, 8); ++g_launches;
-      k_vecmax<SD><<<batch, 256, 0, st>>>(x, n, n, nrm, 1, 8); ++g_launches;
-      CK(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * 8 * batch, cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      bool any = false, slow = false;
-      maxbe = 0.0;
-      for (int bi = 0; bi < batch; ++bi) {
-        double be = hn[8 * bi + 0] / (hn[8 * bi + 3] * hn[8 * bi + 1] + hn[8 * bi + 2]);
-        if (itot == 0) be = 1.0;
-        maxbe = std::max(maxbe, be);
-        hact[bi] = (be > tol) ? 1 : 0;
-        any = any || hact[bi];
-        // contraction slower than 1/4 per step after the first correction
-        if (hact[bi] && it >= 2 && be > 0.25 * prev[bi]) slow = true;
-        prev[bi] = be;
-      }
-      if (!any || itot >= maxit) break;
-      stall = slow ? stall + 1 : 0;
-      if (stall >= 2 && g_c32_mode != 0) {
-        // the tensor-core factors are too coarse for this system: refactor
-        // with SIMT FP32 updates and continue from the current x
-        cudaEvent_t f0, f1;
-        cudaEventCreate(&f0);
-        cudaEventCreate(&f1);
-        cudaEventRecord(f0, st);
-        g_c32_mode = 0;
-        k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, A32, nn * batch); ++g_launches;
-        if ((rc = getrf_batched<SF>(h->blas, st, A32, nn, n, n, batch, ipiv, info))) return rc;
-        cudaEventRecord(f1, st);
-        cudaEventSynchronize(f1);
-        float t = 0.0f;
-        cudaEventElapsedTime(&t, f0, f1);
-        ms_refactor += t;
-        cudaEventDestroy(f0);
-        cudaEventDestroy(f1);
-        stall = 0;
-        it = 0;
-      }
-      CK(cudaMemcpyAsync(active, hact.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, st));
-      k_scale_demote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(r, n, d32, n, n, nrm, 8, 0); ++g_launches;
-      if ((rc = getrs_batched<SF>(st, A32, nn, n, n, ipiv, n, d32, n, batch))) return rc;
-      k_update<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(x, n, d32, n, n, nrm, 8, 0, active); ++g_launches;
+    // refinement: classical (precision 1) until it converges or stalls, then
+    // GMRES-IR with the same factors (precision 2 starts there); if that fails
+    // too and the factors came from TF32 updates, refactorise with SIMT FP32
+    // and run GMRES-IR again
+    const bool gm_env = getenv("MFBEM_REFINE") && std::string(getenv("MFBEM_REFINE")) == "gmres";
+    int conv = 0;
+    if (precision == 1 && !gm_env) {
+      if ((rc = refine_classical(c, &conv))) return rc;
     }
-    it = itot;
-    stats->ms_factor += ms_refactor;
-    stats->ms_solve -= ms_refactor;
+    if (!conv) {
+      if ((rc = refine_gmres(c, &conv))) return rc;
+    }
+    if (!conv && g_c32_mode != 0) {
+      cudaEvent_t f0, f1;
+      cudaEventCreate(&f0);
+      cudaEventCreate(&f1);
+      cudaEventRecord(f0, st);
+      g_c32_mode = 0;
+      ++c.refactor;
+      k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, c.A32, nn * batch); ++g_launches;
+      if ((rc = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info))) return rc;
+      cudaEventRecord(f1, st);
+      cudaEventSynchronize(f1);
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, f0, f1);
+      cudaEventDestroy(f0);
+      cudaEventDestroy(f1);
+      stats->ms_factor += t;
+      stats->ms_solve -= t;
+      if ((rc = refine_gmres(c, &conv))) return rc;
+    }
     cudaEventRecord(e2, st);
     CK(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    stats->refinement_iterations += it;
-    stats->max_backward_error = std::max(stats->max_backward_error, maxbe);
-    if (maxbe > tol) {
+    stats->refinement_iterations += c.it;
+    stats->gmres_iterations += c.inner;
+    stats->refactorizations += c.refactor;
+    stats->max_backward_error = std::max(stats->max_backward_error, c.maxbe);
+    if (!conv) {
       cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
       return fail(MFBEM_ENOCONV, "iterative refinement did not reach the requested backward error");
     }
@@ -600,12 +905,14 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
                                   double rel_tol, double* x_out, int32_t flags, mfbem_stats* stats) {
   g_err.clear();
   if (!h || !lambda || !mu || !nu || !omega || !x_out || n_freq < 1) return fail(MFBEM_EARG, "invalid argument");
-  if (precision != 0 && precision != 1) return fail(MFBEM_EARG, "precision must be 0 or 1");
+  if (precision < 0 || precision > 2) return fail(MFBEM_EARG, "precision must be 0, 1 or 2");
   const int n = h->ndof;
   const long long nn = (long long)n * n;
   int rc;
   mfbem_stats s = h->stats;
   s.refinement_iterations = 0;
+  s.gmres_iterations = 0;
+  s.refactorizations = 0;
   s.max_backward_error = 0.0;
   s.ms_factor = s.ms_solve = 0.0;
   if ((rc = ensure(h->A, sizeof(double2) * nn * n_freq)) || (rc = ensure(h->b, sizeof(double2) * (size_t)n * n_freq)) ||
@@ -643,7 +950,7 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   const ff* dsf = nullptr;
   float4* Af = nullptr;
   const ff *sgf = nullptr, *lgf = nullptr;
-  if (precision == 1) {
+  if (precision >= 1) {
     // mixed: regular pairs in double-float (df64 datasets made once per mesh:
     // phi*J*w [ne][ptot][8], unit normals [ne][ptot][3], prescribed values [ndof][2])
     const long long npp = 8LL * h->m.ne * h->m.ptot, nnp = 3LL * h->m.ne * h->m.ptot, ncv = 2LL * n;
@@ -698,11 +1005,14 @@ extern "C" int mfbem_solve_staela(mfbem_handle* h, double mu, double nu, int32_t
                                   double* x_out, int32_t flags, mfbem_stats* stats) {
   g_err.clear();
   if (!h || !x_out) return fail(MFBEM_EARG, "invalid argument");
+  if (precision < 0 || precision > 2) return fail(MFBEM_EARG, "precision must be 0, 1 or 2");
   const int n = h->ndof;
   const long long nn = (long long)n * n;
   int rc;
   mfbem_stats s = h->stats;
   s.refinement_iterations = 0;
+  s.gmres_iterations = 0;
+  s.refactorizations = 0;
   s.max_backward_error = 0.0;
   s.ms_factor = s.ms_solve = 0.0;
   if ((rc = ensure(h->A, sizeof(double) * nn)) || (rc = ensure(h->b, sizeof(double) * n)) ||

@@ -206,3 +206,37 @@ def test_mixed_sweep_trailing_update_modes(oracle, monkeypatch, gemm, name, mk):
         assert rel(X[i], xo) < 1e-8, (gemm, name, i, rel(X[i], xo))
     assert R.last_stats["max_backward_error"] <= 1e-12
     R.close()
+
+
+@pytest.mark.parametrize("gemm", ["simt", "tf32"])
+@pytest.mark.parametrize("name,mk", [("cube4", lambda: M.cube_clamped_top_traction(4)), ("slab4", lambda: M.slab(4, 1))],
+                         ids=["cube4", "slab4"])
+def test_mixed_sweep_gmres_refinement(oracle, monkeypatch, gemm, name, mk):
+    """GMRES-based refinement (precision 'mixed-gmres'): FP64 GMRES on the
+    correction equation, left-preconditioned by the FP32 / TF32 LU factors,
+    reaches the FP64 oracle solution to 1e-8."""
+    monkeypatch.setenv("MFBEM_FP32_GEMM", gemm)
+    d = mk()
+    mat = M.viscoelastic(1.0, 0.3, 1.0, 0.05)
+    om = M.omega_from_a0([0.3, 1.2], mat)
+    R = BemRegion(d)
+    P = oracle.Problem(d)
+    X = R.sweep_harela(mat, om, precision="mixed-gmres")
+    st = R.last_stats
+    assert st["gmres_iterations"] > 0 and st["max_backward_error"] <= 1e-12
+    for i, w in enumerate(om):
+        Ao, bo = P.assemble_harela(mat, w)
+        xo = oracle.lu_solve(Ao, bo)
+        assert rel(X[i], xo) < 1e-8, (gemm, name, i, rel(X[i], xo))
+    R.close()
+
+
+def test_static_solve_gmres_refinement(oracle):
+    d = M.cube_clamped_top_traction(4)
+    mat = M.elastic(1.0, 0.25)
+    R = BemRegion(d)
+    xp = R.solve_staela(mat["mu"], mat["nu"], precision="plain")
+    xg = R.solve_staela(mat["mu"], mat["nu"], precision="mixed-gmres")
+    assert R.last_stats["gmres_iterations"] > 0
+    assert rel(xg, xp) < 1e-10
+    R.close()
