@@ -186,6 +186,45 @@ const char* mfbem_last_error(void);
 /* Library build identification: "<version> sm_103a". */
 const char* mfbem_version(void);
 
+/* ---------------------------------------------------------------------------
+ * Learned quadrature of quasi-singular pairs. No counterpart in the reference:
+ * an extension that replaces sbie_ext_adp's adaptive subdivision
+ * (lib/fbem/src/bem_staela3d.f90:973-1096) by a rule an MLP predicts to be
+ * accurate enough, keeping the reference rule where no candidate qualifies.
+ * Candidates (index c): c < 7, the reference adaptive rule at
+ * qsi_relative_error 10^-(3+c); c >= 7, graded subdivision of depth
+ * D = (c-7)/9 toward the nearest point (3D + 1 leaves) with a Telles-mapped
+ * g x g Gauss rule per leaf, g = {3,4,6,8,10,12,16,20,30}[(c-7)%9]. Network:
+ * 8 features -> 3 x 64 tanh -> 52 predicted log10 relative errors, FP32
+ * weights (mfbem_mlp_size() floats).
+ * ------------------------------------------------------------------------- */
+
+/* Labels of n (element, point) pairs generated by the caller: elem [n][8][3]
+   quad8 node coordinates, pts [n][3]; kernel 0 static (nu = 0.3), 1 harmonic
+   (E = 1, nu = 0.3, rho = 1, xi = 0.02, omega set by kcl[n] = |k2| x size).
+   Outputs: feat [n][8] network inputs, logerr [n][52] log10 relative error of
+   every candidate against the converged rule (D = 9, g = 30; errors below
+   1e-10 are reported as 1e-10), cost [n][52] its quadrature points (-1 and
+   error 10 for a reference-rule candidate beyond 128 leaves), valid [n]
+   (converged rule checked to 1e-10 against D = 9, g = 24). */
+int mfbem_qlearn_label(int32_t n, const double* elem, const double* pts, int32_t kernel, const double* kcl,
+                       float* feat, float* logerr, int32_t* cost, int32_t* valid);
+int32_t mfbem_mlp_size(void);
+/* network outputs [n][52] for features [n][8] */
+int mfbem_mlp_forward(const float* w, int32_t n, const float* feat, float* out);
+/* mean squared error over valid samples and outputs, and its gradient [mfbem_mlp_size()] */
+int mfbem_mlp_loss_grad(const float* w, int32_t n, const float* feat, const float* y, const int32_t* valid,
+                        float* loss, float* grad);
+/* Adam training in place on device-drawn mini-batches; loss_hist [steps] may be NULL */
+int mfbem_mlp_train(float* w, int32_t n, const float* feat, const float* y, const int32_t* valid, int32_t steps,
+                    int32_t batch, float lr, uint64_t seed, float* loss_hist);
+/* Rebuild a mesh's quasi-singular pair rules from the network w (NULL: the
+   reference rule everywhere): per pair the cheapest candidate whose predicted
+   log10 error is <= log10_tol, else the reference rule. kernel / kcl are the
+   network inputs for the wavenumber (0 / 0 for the static kernel). */
+int mfbem_set_learned_quadrature(mfbem_handle* h, const float* w, double log10_tol, int32_t kernel, double kcl,
+                                 int32_t* n_learned);
+
 #ifdef __cplusplus
 }
 #endif

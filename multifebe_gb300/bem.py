@@ -139,6 +139,20 @@ class BemRegion:
         self.last_stats = st.as_dict()
         return X
 
+    def set_learned_quadrature(self, weights=None, log10_tol=-6.0, kernel=0, kcl=0.0):
+        """Rebuild the quasi-singular (adaptive) pairs' rules: with `weights`
+        (a trained qlearn network) each pair takes the cheapest rule whose
+        predicted log10 relative error is <= log10_tol, or keeps the reference
+        adaptive rule when none qualifies; weights=None restores the reference
+        rule everywhere. Returns the number of pairs on a learned rule."""
+        from . import qlearn
+        L = qlearn._lib()
+        nl = ctypes.c_int32(0)
+        w = None if weights is None else np.ascontiguousarray(weights, np.float32)
+        check(L.mfbem_set_learned_quadrature(self._h, None if w is None else w.ctypes.data, float(log10_tol),
+                                             int(kernel), float(kcl), ctypes.byref(nl)))
+        return int(nl.value)
+
     def solve_staela(self, mu, nu, precision="plain", rel_tol=1e-12):
         x = np.zeros(self.n, dtype=np.float64)
         st = _abi.Stats()

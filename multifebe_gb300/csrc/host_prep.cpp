@@ -238,3 +238,9 @@ extern "C" void mfbem_prep_dof(const mfbem_prep* p, int32_t* dof, int32_t* order
   for (size_t i = 0; i < p->dof.size(); ++i) dof[i] = p->dof[i];
   for (size_t i = 0; i < p->order.size(); ++i) order[i] = p->order[i];
 }
+
+// element far-field order (phijac_ngp) for callers outside this file
+int mfb::host_phijac_ngp_q8(const double* x, double error_height) {
+  bool ok;
+  return phijac_ngp_q8(x, error_height, &ok);
+}

@@ -629,3 +629,270 @@ extern "C" int mfbem_internal_zexp(int32_t n, const double* z, double* e64, doub
 }
 
 #include "mfbem_solve.cuh"
+#include "mfbem_learned.cuh"
+
+// ---------------------------------------------------------------------------
+// Learned quadrature of near-singular pairs (no counterpart in the reference)
+// ---------------------------------------------------------------------------
+// tolerance curves of the reference-rule candidates (1e-3 .. 1e-9)
+static std::vector<QsCurves> ql_tol_curves() {
+  std::vector<QsCurves> q(QL_NT);
+  for (int r = 0; r < QL_NT; ++r) q[r] = qs_curves(std::pow(10.0, -3.0 - r));
+  return q;
+}
+
+extern "C" int mfbem_qlearn_label(int32_t n, const double* elem, const double* pts, int32_t kernel, const double* kcl,
+                                  float* feat, float* logerr, int32_t* cost, int32_t* valid) {
+  g_err.clear();
+  if (n <= 0 || !elem || !pts || !feat || !logerr || !cost || !valid || (kernel && !kcl) || kernel < 0 || kernel > 1)
+    return fail(MFBEM_EARG, "invalid argument");
+  int rc = init_tables();
+  if (rc) return rc;
+  std::vector<double> cl(n);
+  std::vector<int> gf(n);
+  for (int s = 0; s < n; ++s) {
+    const double* x = elem + 24 * (size_t)s;
+    cl[s] = clen_q8(x, 1e-9);
+    gf[s] = host_phijac_ngp_q8(x, 1e-6);
+  }
+  std::vector<HarParD> par;
+  if (kernel) {
+    // viscoelastic material E = 1, nu = 0.3, rho = 1, xi = 0.02; omega from |k2| cl
+    const double E = 1.0, nu = 0.3, rho = 1.0, xi = 0.02;
+    const cd mu = mk(E / (2.0 * (1.0 + nu)), 2.0 * xi * E / (2.0 * (1.0 + nu)));
+    const cd lam = mu * (2.0 * nu / (1.0 - 2.0 * nu));
+    const cd c2 = csqrt_(mu / rho);
+    const double ac2 = sqrt(c2.re * c2.re + c2.im * c2.im);
+    par.resize(n);
+    for (int s = 0; s < n; ++s) {
+      par[s] = harela_params(lam, mu, rho, kcl[s] * ac2 / cl[s]);
+      par[s].steps = zexp_thresholds();
+    }
+  }
+  const std::vector<QsCurves> q = ql_tol_curves();
+  DevBuf b_ex, b_pt, b_cl, b_gf, b_k, b_par, b_q, b_scr, b_f, b_le, b_c, b_v;
+  auto cleanup = [&]() {
+    for (DevBuf* b : {&b_ex, &b_pt, &b_cl, &b_gf, &b_k, &b_par, &b_q, &b_scr, &b_f, &b_le, &b_c, &b_v})
+      if (b->p) cudaFree(b->p);
+  };
+  if ((rc = ensure(b_ex, 24 * sizeof(double) * n)) || (rc = ensure(b_pt, 3 * sizeof(double) * n)) ||
+      (rc = ensure(b_cl, sizeof(double) * n)) || (rc = ensure(b_gf, sizeof(int) * n)) ||
+      (rc = ensure(b_k, sizeof(double) * n)) || (rc = ensure(b_par, sizeof(HarParD) * (kernel ? n : 1))) ||
+      (rc = ensure(b_q, sizeof(QsCurves) * QL_NT)) || (rc = ensure(b_scr, sizeof(double) * LEAF_D * QL_MAXREF * (size_t)n)) ||
+      (rc = ensure(b_f, sizeof(float) * QL_NF * n)) || (rc = ensure(b_le, sizeof(float) * QL_NC * n)) ||
+      (rc = ensure(b_c, sizeof(int) * QL_NC * n)) || (rc = ensure(b_v, sizeof(int) * n))) {
+    cleanup();
+    return rc;
+  }
+  cudaError_t e = cudaMemcpy(b_ex.p, elem, 24 * sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b_pt.p, pts, 3 * sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b_cl.p, cl.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b_gf.p, gf.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && kernel) e = cudaMemcpy(b_k.p, kcl, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && kernel) e = cudaMemcpy(b_par.p, par.data(), sizeof(HarParD) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b_q.p, q.data(), sizeof(QsCurves) * QL_NT, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    constexpr int WPB = 2;
+    if (kernel)
+      k_ql_label<WPB, true><<<nblk(n, WPB), WPB * 32>>>(n, (double*)b_ex.p, (double*)b_pt.p, (double*)b_cl.p,
+                                                        (int*)b_gf.p, (double*)b_k.p, (HarParD*)b_par.p,
+                                                        (QsCurves*)b_q.p, 16, (double*)b_scr.p, (float*)b_f.p,
+                                                        (float*)b_le.p, (int*)b_c.p, (int*)b_v.p);
+    else
+      k_ql_label<WPB, false><<<nblk(n, WPB), WPB * 32>>>(n, (double*)b_ex.p, (double*)b_pt.p, (double*)b_cl.p,
+                                                         (int*)b_gf.p, (double*)b_k.p, (HarParD*)b_par.p,
+                                                         (QsCurves*)b_q.p, 16, (double*)b_scr.p, (float*)b_f.p,
+                                                         (float*)b_le.p, (int*)b_c.p, (int*)b_v.p);
+    ++g_launches;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(feat, b_f.p, sizeof(float) * QL_NF * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(logerr, b_le.p, sizeof(float) * QL_NC * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(cost, b_c.p, sizeof(int) * QL_NC * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(valid, b_v.p, sizeof(int) * n, cudaMemcpyDeviceToHost);
+  cleanup();
+  if (e != cudaSuccess) return fail(MFBEM_ECUDA, std::string("qlearn label: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+extern "C" int32_t mfbem_mlp_size(void) { return QL_NW; }
+extern "C" const int32_t* mfbem_mlp_orders(void) { return h_ql_g; }
+
+// MLP loss and gradient over the whole set (forward + backward kernels), or the
+// forward outputs only (grad == NULL). y, valid may be NULL for forward only.
+static int mlp_run(const float* w, int n, const float* feat, const float* y, const int* valid, float* loss,
+                   float* grad, float* out) {
+  int rc;
+  const bool bwd = grad != nullptr;
+  DevBuf bw, bf, by, bv, bg, bl, bo;
+  auto cleanup = [&]() {
+    for (DevBuf* b : {&bw, &bf, &by, &bv, &bg, &bl, &bo})
+      if (b->p) cudaFree(b->p);
+  };
+  if ((rc = ensure(bw, sizeof(float) * QL_NW)) || (rc = ensure(bf, sizeof(float) * QL_NF * (size_t)n)) ||
+      (rc = ensure(by, sizeof(float) * QL_NC * (size_t)n)) || (rc = ensure(bv, sizeof(int) * (size_t)n)) ||
+      (rc = ensure(bg, sizeof(float) * QL_NW)) || (rc = ensure(bl, sizeof(float))) ||
+      (rc = ensure(bo, sizeof(float) * QL_NC * (size_t)n))) {
+    cleanup();
+    return rc;
+  }
+  std::vector<int> ones;
+  if (!valid) { ones.assign(n, 1); valid = ones.data(); }
+  cudaError_t e = cudaFuncSetAttribute(k_mlp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ql_smem_bytes());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ql_smem_bytes());
+  if (e == cudaSuccess) e = cudaMemcpy(bw.p, w, sizeof(float) * QL_NW, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(bf.p, feat, sizeof(float) * QL_NF * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && y) e = cudaMemcpy(by.p, y, sizeof(float) * QL_NC * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(bv.p, valid, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(bg.p, 0, sizeof(float) * QL_NW);
+  if (e == cudaSuccess) e = cudaMemset(bl.p, 0, sizeof(float));
+  if (e == cudaSuccess) {
+    const float inv = 1.0f / ((float)n * QL_NC);
+    if (bwd)
+      k_mlp<true><<<nblk(n, QL_BT), QL_BT, ql_smem_bytes()>>>((float*)bw.p, (float*)bf.p, (float*)by.p, (int*)bv.p,
+                                                             n, nullptr, n, inv, (float*)bo.p, (float*)bg.p, (float*)bl.p);
+    else
+      k_mlp<false><<<nblk(n, QL_BT), QL_BT, ql_smem_bytes()>>>((float*)bw.p, (float*)bf.p, nullptr, nullptr, n,
+                                                              nullptr, n, inv, (float*)bo.p, nullptr, nullptr);
+    ++g_launches;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && out) e = cudaMemcpy(out, bo.p, sizeof(float) * QL_NC * (size_t)n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && bwd) e = cudaMemcpy(grad, bg.p, sizeof(float) * QL_NW, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && bwd && loss) e = cudaMemcpy(loss, bl.p, sizeof(float), cudaMemcpyDeviceToHost);
+  cleanup();
+  if (e != cudaSuccess) return fail(MFBEM_ECUDA, std::string("mlp: ") + cudaGetErrorString(e));
+  return 0;
+}
+extern "C" int mfbem_mlp_forward(const float* w, int32_t n, const float* feat, float* out) {
+  g_err.clear();
+  if (!w || n <= 0 || !feat || !out) return fail(MFBEM_EARG, "invalid argument");
+  return mlp_run(w, n, feat, nullptr, nullptr, nullptr, nullptr, out);
+}
+extern "C" int mfbem_mlp_loss_grad(const float* w, int32_t n, const float* feat, const float* y, const int32_t* valid,
+                                   float* loss, float* grad) {
+  g_err.clear();
+  if (!w || n <= 0 || !feat || !y || !loss || !grad) return fail(MFBEM_EARG, "invalid argument");
+  return mlp_run(w, n, feat, y, valid, loss, grad, nullptr);
+}
+
+// Train in place with Adam on mini-batches drawn on the device; loss_hist[s]
+// receives the mini-batch loss of step s (may be NULL).
+extern "C" int mfbem_mlp_train(float* w, int32_t n, const float* feat, const float* y, const int32_t* valid,
+                               int32_t steps, int32_t batch, float lr, uint64_t seed, float* loss_hist) {
+  g_err.clear();
+  if (!w || n <= 0 || !feat || !y || steps <= 0 || batch <= 0) return fail(MFBEM_EARG, "invalid argument");
+  int rc;
+  DevBuf bw, bf, by, bv, bg, bm, bvv, bl, bi;
+  auto cleanup = [&]() {
+    for (DevBuf* b : {&bw, &bf, &by, &bv, &bg, &bm, &bvv, &bl, &bi})
+      if (b->p) cudaFree(b->p);
+  };
+  if ((rc = ensure(bw, sizeof(float) * QL_NW)) || (rc = ensure(bf, sizeof(float) * QL_NF * (size_t)n)) ||
+      (rc = ensure(by, sizeof(float) * QL_NC * (size_t)n)) || (rc = ensure(bv, sizeof(int) * (size_t)n)) ||
+      (rc = ensure(bg, sizeof(float) * QL_NW)) || (rc = ensure(bm, sizeof(float) * QL_NW)) ||
+      (rc = ensure(bvv, sizeof(float) * QL_NW)) || (rc = ensure(bl, sizeof(float) * steps)) ||
+      (rc = ensure(bi, sizeof(int) * (size_t)batch))) {
+    cleanup();
+    return rc;
+  }
+  std::vector<int> ones;
+  if (!valid) { ones.assign(n, 1); valid = ones.data(); }
+  cudaError_t e = cudaFuncSetAttribute(k_mlp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ql_smem_bytes());
+  if (e == cudaSuccess) e = cudaMemcpy(bw.p, w, sizeof(float) * QL_NW, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(bf.p, feat, sizeof(float) * QL_NF * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(by.p, y, sizeof(float) * QL_NC * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(bv.p, valid, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(bm.p, 0, sizeof(float) * QL_NW);
+  if (e == cudaSuccess) e = cudaMemset(bvv.p, 0, sizeof(float) * QL_NW);
+  if (e == cudaSuccess) e = cudaMemset(bl.p, 0, sizeof(float) * steps);
+  const float inv = 1.0f / ((float)batch * QL_NC);
+  for (int t = 0; t < steps && e == cudaSuccess; ++t) {
+    k_ql_batch<<<nblk(batch, 256), 256>>>((int*)bi.p, batch, n, (unsigned long long)seed, t); ++g_launches;
+    cudaMemsetAsync(bg.p, 0, sizeof(float) * QL_NW);
+    k_mlp<true><<<nblk(batch, QL_BT), QL_BT, ql_smem_bytes()>>>((float*)bw.p, (float*)bf.p, (float*)by.p, (int*)bv.p,
+                                                               n, (int*)bi.p, batch, inv, nullptr, (float*)bg.p,
+                                                               (float*)bl.p + t);
+    ++g_launches;
+    k_adam<<<nblk(QL_NW, 256), 256>>>((float*)bw.p, (float*)bg.p, (float*)bm.p, (float*)bvv.p, QL_NW, lr, 0.9f, 0.999f,
+                                      1e-8f, t + 1);
+    ++g_launches;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(w, bw.p, sizeof(float) * QL_NW, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && loss_hist) e = cudaMemcpy(loss_hist, bl.p, sizeof(float) * steps, cudaMemcpyDeviceToHost);
+  cleanup();
+  if (e != cudaSuccess) return fail(MFBEM_ECUDA, std::string("mlp train: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+// Rebuild the adaptive leaves of a mesh with the learned rule choice (w) or
+// the reference rule (w == NULL). log10_tol: the largest admissible predicted
+// log10 relative error; kernel / kcl: kernel type and wavenumber x element
+// size fed to the network. n_learned (optional): pairs that took a learned rule.
+extern "C" int mfbem_set_learned_quadrature(mfbem_handle* h, const float* w, double log10_tol, int32_t kernel,
+                                            double kcl, int32_t* n_learned) {
+  g_err.clear();
+  if (!h || kernel < 0 || kernel > 1) return fail(MFBEM_EARG, "invalid argument");
+  DMesh& m = h->m;
+  if (n_learned) *n_learned = 0;
+  if (m.nadp == 0) return 0;
+  int rc;
+  float* dw = nullptr;
+  int *choice, *nl;
+  if ((rc = dalloc(h, (void**)&choice, sizeof(int) * (m.nadp + 1))) || (rc = dalloc(h, (void**)&nl, sizeof(int) * (m.nadp + 1))))
+    return rc;
+  QsCurves* qt;
+  {
+    const std::vector<QsCurves> q = ql_tol_curves();
+    if ((rc = dalloc(h, (void**)&qt, sizeof(QsCurves) * QL_NT))) return rc;
+    CK(cudaMemcpy(qt, q.data(), sizeof(QsCurves) * QL_NT, cudaMemcpyHostToDevice));
+  }
+  if (w) {
+    if ((rc = dalloc(h, (void**)&dw, sizeof(float) * QL_NW))) return rc;
+    CK(cudaMemcpy(dw, w, sizeof(float) * QL_NW, cudaMemcpyHostToDevice));
+    k_ql_choose<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, qt, dw, (float)log10_tol, kernel, kcl, choice, nl); ++g_launches;
+  } else {
+    // reference rule for every pair
+    CK(cudaMemset(choice, 0xff, sizeof(int) * (m.nadp + 1)));
+    k_adp_count<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, m.adp_cp, nl); ++g_launches;
+  }
+  k_scan<int, int><<<1, 1024>>>(nl, m.adp_leaf, (int)m.nadp); ++g_launches;
+  int nleaf = 0;
+  CK(cudaMemcpy(&nleaf, m.adp_leaf + m.nadp, sizeof(int), cudaMemcpyDeviceToHost));
+  long long* lpts;
+  if ((rc = dalloc(h, (void**)&m.leaf, sizeof(double) * LEAF_D * (nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&m.leaf_gln, sizeof(int) * (nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&m.leaf_pair, sizeof(int) * (nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&m.leaf_pt, sizeof(long long) * (nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&lpts, sizeof(long long) * (nleaf + 1))))
+    return rc;
+  m.nleaf = nleaf;
+  k_ql_fill<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, qt, choice); ++g_launches;
+  if (m.nleaf > 0) { k_leaf_points<<<nblk(m.nleaf, 256), 256>>>(m, lpts); ++g_launches; }
+  k_scan<long long, long long><<<1, 1024>>>(lpts, m.leaf_pt, (int)m.nleaf); ++g_launches;
+  CK(cudaMemcpy(&h->pts_adp, m.leaf_pt + m.nleaf, sizeof(long long), cudaMemcpyDeviceToHost));
+  m.nleaf_pts = h->pts_adp;
+  m.leaf_geo = nullptr;
+  const size_t geo_budget = (size_t)8 << 30;
+  if (m.nleaf_pts > 0 && (size_t)m.nleaf_pts * 14 * sizeof(double) <= geo_budget) {
+    if ((rc = dalloc(h, (void**)&m.leaf_geo, (size_t)m.nleaf_pts * 14 * sizeof(double)))) return rc;
+    k_leaf_geo<<<nblk(m.nleaf_pts, 128), 128>>>(m); ++g_launches;
+  }
+  // the df64 copy of the hoisted geometry is rebuilt by the next mixed sweep
+  if (h->geo_f.p) cudaFree(h->geo_f.p);
+  h->geo_f.p = nullptr;
+  h->geo_f.bytes = 0;
+  CK(cudaGetLastError());
+  CK(cudaDeviceSynchronize());
+  if (n_learned && w) {
+    std::vector<int> c(m.nadp);
+    CK(cudaMemcpy(c.data(), choice, sizeof(int) * m.nadp, cudaMemcpyDeviceToHost));
+    int k = 0;
+    for (int v : c) k += v >= 0;
+    *n_learned = k;
+  }
+  h->stats.adaptive_leaves = (int)m.nleaf;
+  h->stats.points_adaptive = h->pts_adp;
+  return 0;
+}

@@ -10,6 +10,8 @@ namespace mfb {
 
 const GLTables& host_gauss_tables();
 QsCurves qs_curves(double relative_error);
+// fbem_qs_phijac_ngp_2d of a quad8 element (host_prep.cpp)
+int host_phijac_ngp_q8(const double* x, double error_height);
 
 // thread-local error string behind mfbem_last_error()
 void set_error(const std::string& s);

@@ -170,7 +170,7 @@ struct AdpNode {
 };
 template <bool WRITE>
 __device__ int adp_traverse(const DMesh& m, const QsCurves& qs, int e, const double* xi, double* leaf_out,
-                            int* gln_out, int* pair_out, int pair_id) {
+                            int* gln_out, int* pair_out, int pair_id, long long* npts = nullptr) {
   AdpNode st[52];
   int top = 0;
   const double* x = m.ex + 24 * (size_t)e;
@@ -225,6 +225,10 @@ __device__ int adp_traverse(const DMesh& m, const QsCurves& qs, int e, const dou
         L[12] = t2.a; L[13] = t2.b; L[14] = t2.c; L[15] = t2.d;
         gln_out[nleaf] = gln;
         pair_out[nleaf] = pair_id;
+      }
+      if (npts) {
+        const long long g = max(gn, m.gln_far[e]);
+        *npts += g * g;
       }
       ++nleaf;
     }
