@@ -239,6 +239,8 @@ def run_gpu(args):
     line["roofline"] = roofline(st, n, nf)
     if args.precision_form:
         line["precision_form"] = precision_form()
+    if args.learned:
+        line["learned_quadrature"] = learned_quadrature()
     # cpu baseline: oracle on one frequency (bounded sample)
     try:
         t, cores = cpu_baseline_sample(deck, mat, om[len(om) // 2])
@@ -274,6 +276,48 @@ def roofline(st, n, nf):
             "compute": {"points": pts, "flops_per_point": FLOPS_PER_REGULAR_POINT, "achieved_tflops": tfl,
                         "note": "SIMT-compute bound (double-float on the FP32 pipe, binary64 for x - x_i); "
                                 "HBM and tensor pipes are not the limit of this kernel"}}
+
+
+def learned_quadrature():
+    """The thin slab (16x16 + 16x1 quad8 per face, 5190 DOF, a0 0.2 and 1.0):
+    the network is trained on 8000 seeded random pairs labelled on the GPU, then
+    the slab's quasi-singular pairs take the learned rules (log10 tolerance -7).
+    Reported beside the reference adaptive rule: the assembly error against the
+    converged assembly (qsi_relative_error 1e-10) at a0 = 1.0, the adaptive-pair
+    quadrature points and kernel time, and the mixed sweep's solves/s."""
+    import time as _t
+    from multifebe_gb300 import meshgen as M, BemRegion, qlearn as Q
+    t0 = _t.perf_counter()
+    e, p, k, kc = Q.random_pairs(8000, seed=21, kernel=0)
+    F, Y, C, V = Q.label_pairs(e, p, k, kc)
+    t1 = _t.perf_counter()
+    w = Q.init_weights(2)
+    hist = Q.train(w, F, Y, V, steps=3000, batch=2048, lr=2e-3, seed=6)
+    t2 = _t.perf_counter()
+    deck, mat, om = M.workload(5)
+    Rc = BemRegion(deck, qsi_relative_error=1e-10)
+    Ac, _ = Rc.build_lse_harela(mat, float(om[-1]))
+    Rc.close()
+    R = BemRegion(deck)
+    out = {"workload": "harela slab 1x1x0.02, 16x16 + 16x1 quad8 per face, 5190 complex DOF, a0 0.2 and 1.0",
+           "training": {"pairs": 8000, "valid": int(V.sum()), "label_s": t1 - t0, "train_s": t2 - t1,
+                        "steps": 3000, "loss_first": float(hist[:10].mean()), "loss_last": float(hist[-100:].mean())}}
+    scale = float(np.abs(Ac).max())
+    for name, tol in (("reference", None), ("learned", -7.0), ("learned_tol_1e-6.5", -6.5)):
+        nl = R.set_learned_quadrature(w if tol is not None else None, log10_tol=tol or -7.0)
+        A, _ = R.build_lse_harela(mat, float(om[-1]))
+        err = float(np.abs(A - Ac).max() / scale)
+        R.sweep_harela(mat, om, precision="mixed")
+        R.sweep_harela(mat, om, precision="mixed")
+        st = R.last_stats
+        out[name] = {"pairs_learned": nl, "points_adaptive": st["points_adaptive"],
+                     "ms_adaptive_sweep": st["ms_adaptive"], "assembly_rel_err_vs_converged": err,
+                     "sweep_solves_per_s": len(om) / ((st["ms_assemble"] + st["ms_factor"] + st["ms_solve"]) / 1e3),
+                     "sweep_ms": {k: st[k] for k in ("ms_assemble", "ms_factor", "ms_solve")},
+                     "refinement": {k: st[k] for k in ("refinement_iterations", "gmres_iterations", "refactorizations",
+                                                       "max_backward_error")}}
+    R.close()
+    return out
 
 
 def precision_form():
@@ -336,6 +380,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-precision-form", dest="precision_form", action="store_false",
                     help="skip the 14883-DOF surface-patch mixed/plain comparison")
+    ap.add_argument("--no-learned", dest="learned", action="store_false",
+                    help="skip the learned-quadrature measurement on the thin slab")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="profiling helper: run the benchmark mesh for this many frequencies twice, print stats, exit")
     ap.add_argument("--profile-patch", default="", choices=["", "mixed", "plain"],
