@@ -144,12 +144,13 @@ int mfbem_solve_c(int32_t n, double* A, int32_t* ipiv, int32_t aodim, double* Ao
    precision 0: plain FP64 LU (the drop-in method).
    precision 1: complex64 LU with FP64 iterative refinement to rel_tol in the
                 backward error (the FP64 residual r = b - A x is evaluated with
-                the FP64 matrix): classical refinement, switching to
-                GMRES-based refinement (FP64 GMRES preconditioned by the LU
-                factors) when it stalls; the trailing updates of the LU run on
-                the TF32 tensor cores and are redone in SIMT FP32 when even
-                GMRES-based refinement does not converge.
-   precision 2: as 1, with GMRES-based refinement from the start.
+                the FP64 matrix). The LU's trailing updates run on the TF32
+                tensor cores; classical refinement x += LU^-1 r follows; if it
+                stalls, the LU is redone with SIMT FP32 updates and refined
+                again, and GMRES-based refinement (FP64 GMRES preconditioned by
+                the LU factors) is the last resort.
+   precision 2: GMRES-based refinement from the start (refactorised with SIMT
+                FP32 updates if it does not converge with the TF32 factors).
    x_out receives n_dof complex values per frequency (column f at f*n_dof).
    The right-hand side is the one assembled from the prescribed values. */
 int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho, const double nu[2],

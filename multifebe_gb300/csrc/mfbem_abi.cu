@@ -59,6 +59,9 @@ struct mfbem_handle {
   QsCurves* d_qs = nullptr;
   QsCurves* d_q15 = nullptr;
   int ndof = 0, ne = 0, nn = 0;
+  // mixed solves: TF32 trailing updates stalled the refinement on this mesh
+  // once, so later solves factorise with SIMT FP32 updates from the start
+  bool tf32_stalled = false;
   cudaStream_t st = nullptr;
   cublasHandle_t blas = nullptr;
   DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, Af, geo_f, gm;

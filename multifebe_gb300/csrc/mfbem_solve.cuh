@@ -841,30 +841,27 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, c.nrm, 3, 8); ++g_launches;
     k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, c.nrm, 2, 8); ++g_launches;
     g_c32_mode = c32_default();
+    if (g_c32_mode == 1 && h->tf32_stalled) g_c32_mode = 0;
     if ((rc = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info))) return rc;
     cudaEventRecord(e1, st);
     CK(cudaMemsetAsync(x, 0, sizeof(SD) * (size_t)n * batch, st));
-    // refinement: classical (precision 1) until it converges or stalls, then
-    // GMRES-IR with the same factors (precision 2 starts there); if that fails
-    // too and the factors came from TF32 updates, refactorise with SIMT FP32
-    // and run GMRES-IR again
-    const bool gm_env = getenv("MFBEM_REFINE") && std::string(getenv("MFBEM_REFINE")) == "gmres";
+    // refinement: precision 1, classical refinement until it converges or
+    // stalls; if the factors came from TF32 updates, refactorise with SIMT FP32
+    // (one factorisation costs about ten triangular-solve pairs, less than the
+    // GMRES steps TF32 factors need on ill-conditioned systems) and refine
+    // again; GMRES-IR last. Precision 2: GMRES-IR first, refactorisation if it fails.
+    const bool gm_first = precision == 2 || (getenv("MFBEM_REFINE") && std::string(getenv("MFBEM_REFINE")) == "gmres");
     int conv = 0;
-    if (precision == 1 && !gm_env) {
-      if ((rc = refine_classical(c, &conv))) return rc;
-    }
-    if (!conv) {
-      if ((rc = refine_gmres(c, &conv))) return rc;
-    }
-    if (!conv && g_c32_mode != 0) {
+    auto refactor = [&]() -> int {
       cudaEvent_t f0, f1;
       cudaEventCreate(&f0);
       cudaEventCreate(&f1);
       cudaEventRecord(f0, st);
       g_c32_mode = 0;
+      h->tf32_stalled = true;
       ++c.refactor;
       k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, c.A32, nn * batch); ++g_launches;
-      if ((rc = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info))) return rc;
+      int r = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info);
       cudaEventRecord(f1, st);
       cudaEventSynchronize(f1);
       float t = 0.0f;
@@ -873,7 +870,23 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
       cudaEventDestroy(f1);
       stats->ms_factor += t;
       stats->ms_solve -= t;
+      return r;
+    };
+    if (gm_first) {
       if ((rc = refine_gmres(c, &conv))) return rc;
+      if (!conv && g_c32_mode != 0) {
+        if ((rc = refactor())) return rc;
+        if ((rc = refine_gmres(c, &conv))) return rc;
+      }
+    } else {
+      if ((rc = refine_classical(c, &conv))) return rc;
+      if (!conv && g_c32_mode != 0) {
+        if ((rc = refactor())) return rc;
+        if ((rc = refine_classical(c, &conv))) return rc;
+      }
+      if (!conv) {
+        if ((rc = refine_gmres(c, &conv))) return rc;
+      }
     }
     cudaEventRecord(e2, st);
     CK(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
