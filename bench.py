@@ -3,15 +3,23 @@ time-harmonic elastodynamic quad8 cube, 8x8 elements per face (384 elements,
 1154 nodes, 3462 complex DOF), E=1, nu=0.25, rho=1, xi=0.05, 20 frequencies
 a0 = 0.1..2.0, bottom face clamped, uniform harmonic t_z=-1 on the top face.
 
-One step = one full frequency sweep on the device: FP64 assembly of the 20
-systems, complex64 LU with FP64 iterative refinement to a 1e-12 backward error
-(the 'mixed' path; its solutions agree with the FP64 oracle to <= 1e-8), i.e.
-20 solves. value: device time (CUDA events inside the library) with the mesh
-resident in HBM. e2e: the same sweep through the public C-ABI from host
-buffers: mesh upload (H2D) + sweep + solution download (D2H) every step.
+One step = one full frequency sweep on the device = 20 solves, mixed precision:
+double-float assembly of the 20 systems (binary64 results), complex64 LU with
+TF32 tensor-core trailing updates, FP64 iterative refinement to a 1e-12
+backward error (solutions within 1e-8 of the FP64 oracle's). value: device time
+(CUDA events inside the library) with the mesh resident in HBM; inputs (20 x
+192 MB systems) exceed L2. e2e: the same sweep through the public C-ABI from
+host buffers: mesh upload (H2D) + sweep + solution download (D2H) every step.
+
+Beside the headline: the plain FP64 GPU path on the same sweep
+(plain_fp64_gpu), the 14883-DOF surface patch with mixed vs plain FP64
+(precision_form), the learned quadrature on the thin slab (learned_quadrature),
+the roofline of the dominant kernel and the CPU oracle timed on the host cores.
 
 --impl reference times the reference-equivalent CPU path (the oracle: OpenMP
 assembly on all host cores + OpenBLAS getrf/getrs) on one frequency per step.
+Under torchrun (N > 1) the sweep is sharded: 20 frequencies per rank of a
+20*N-frequency sweep (weak scaling), no device collective.
 """
 from __future__ import annotations
 
@@ -41,6 +49,9 @@ WORKLOAD_P = "harela surface patch 40x40 quad8 (20x20), 14883 complex DOF, a0=0.
 # powers 13, E_2..E_5 for both wavenumbers 272, psi/chi/TT1..TT3 320, 1/r
 # scalings and dr 24, u*/t* components 168, 120 complex accumulations 480.
 FLOPS_PER_REGULAR_POINT = 1280
+# GB300 FP64 rate (nominal; not in the measured peaks): the binary64
+# formulation of the same kernel could at best run at this rate
+FP64_NOMINAL_TFLOPS = 1.25
 # DRAM bytes per frequency of that kernel from ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch of the 2-frequency profile case, 454.1 +
 # 408.1 MB, divided by 2; profiles/k_mixed_cube8x2freq.md). Traffic grows in
@@ -269,13 +280,17 @@ def roofline(st, n, nf):
     achieved = alg_bytes / t / 1e9
     pts = st["points_regular"] * nf
     tfl = pts * FLOPS_PER_REGULAR_POINT / t / 1e12
-    return {"kernel": "k_reg_mixed (regular pairs, all frequencies)", "bound": "hbm", "achieved": achieved,
+    return {"kernel": "k_mixed<MIX_REG> (regular pairs, double-float, all frequencies in one launch)",
+            "bound": "hbm", "achieved": achieved,
             "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "peak_source": src,
             "traffic": (REG_TRAFFIC_PER_FREQ * nf) if REG_TRAFFIC_PER_FREQ else None,
             "algorithmic_bytes": alg_bytes, "ms": st["ms_regular"],
             "compute": {"points": pts, "flops_per_point": FLOPS_PER_REGULAR_POINT, "achieved_tflops": tfl,
-                        "note": "SIMT-compute bound (double-float on the FP32 pipe, binary64 for x - x_i); "
-                                "HBM and tensor pipes are not the limit of this kernel"}}
+                        "fp64_nominal_peak_tflops": FP64_NOMINAL_TFLOPS,
+                        "frac_of_fp64_nominal": tfl / FP64_NOMINAL_TFLOPS,
+                        "note": "SIMT-issue bound (double-float on the FP32 pipe, binary64 only for x - x_i): "
+                                "FP64-equivalent flops above the GPU's whole FP64 rate; HBM and tensor pipes "
+                                "are not the limit of this kernel"}}
 
 
 def learned_quadrature():
