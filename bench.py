@@ -14,7 +14,8 @@ host buffers: mesh upload (H2D) + sweep + solution download (D2H) every step.
 Beside the headline: the plain FP64 GPU path on the same sweep
 (plain_fp64_gpu), the 14883-DOF surface patch with mixed vs plain FP64
 (precision_form), the learned quadrature on the thin slab (learned_quadrature),
-the roofline of the dominant kernel and the CPU oracle timed on the host cores.
+48 uneven problems in one batched call (batching_form), the roofline of the
+dominant kernel and the CPU oracle timed on the host cores.
 
 --impl reference times the reference-equivalent CPU path (the oracle: OpenMP
 assembly on all host cores + OpenBLAS getrf/getrs) on one frequency per step.
@@ -252,6 +253,8 @@ def run_gpu(args):
         line["precision_form"] = precision_form()
     if args.learned:
         line["learned_quadrature"] = learned_quadrature()
+    if args.batching:
+        line["batching_form"] = batching_form()
     # cpu baseline: oracle on one frequency (bounded sample)
     try:
         t, cores = cpu_baseline_sample(deck, mat, om[len(om) // 2])
@@ -291,6 +294,41 @@ def roofline(st, n, nf):
                         "note": "SIMT-issue bound (double-float on the FP32 pipe, binary64 only for x - x_i): "
                                 "FP64-equivalent flops above the GPU's whole FP64 rate; HBM and tensor pipes "
                                 "are not the limit of this kernel"}}
+
+
+def batching_form():
+    """48 uneven problems: the cube at n x n elements per face, n in
+    {4,5,6,7,8,10} (870 .. 5406 DOF), 8 frequencies a0 = 0.2..1.6 each, mixed
+    precision. One call for all meshes (concurrent sweeps) against the same
+    sweeps one after another (wall clock, host API), and every problem's
+    difference to the plain FP64 GPU solution (itself pinned to the oracle)."""
+    import time as _t
+    from multifebe_gb300 import meshgen as M, BemRegion, sweep_harela_batch
+    work = M.batch_workload()
+    regions = [BemRegion(d) for d, _, _ in work]
+    mats = [m for _, m, _ in work]
+    oms = [o for _, _, o in work]
+    nsol = sum(len(o) for o in oms)
+    for _ in range(2):  # warm-up: kernels, autotuner classes
+        sweep_harela_batch(regions, mats, oms, precision="mixed")
+    t0 = _t.perf_counter()
+    Xb, _ = sweep_harela_batch(regions, mats, oms, precision="mixed")
+    t_batch = _t.perf_counter() - t0
+    t0 = _t.perf_counter()
+    for r, m, o in zip(regions, mats, oms):
+        r.sweep_harela(m, o, precision="mixed")
+    t_seq = _t.perf_counter() - t0
+    errs = []
+    for r, m, o, x in zip(regions, mats, oms, Xb):
+        xp = r.sweep_harela(m, o, precision="plain")
+        errs += [float(np.abs(x[i] - xp[i]).max() / np.abs(xp[i]).max()) for i in range(len(o))]
+    for r in regions:
+        r.close()
+    return {"workload": "harela cubes n x n quad8 per face, n in {4,5,6,7,8,10} (870..5406 DOF), 8 frequencies "
+                        "a0=0.2..1.6 each: 48 problems", "problems": nsol,
+            "batched": {"value": nsol / t_batch, "unit": "solves/s", "wall_s": t_batch},
+            "one_after_another": {"value": nsol / t_seq, "unit": "solves/s", "wall_s": t_seq},
+            "max_rel_err_vs_fp64": max(errs), "n_dof": [r_.n for r_ in regions]}
 
 
 def learned_quadrature():
@@ -397,6 +435,8 @@ def main():
                     help="skip the 14883-DOF surface-patch mixed/plain comparison")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip the learned-quadrature measurement on the thin slab")
+    ap.add_argument("--no-batching", dest="batching", action="store_false",
+                    help="skip the 48-problem batch of uneven meshes")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="profiling helper: run the benchmark mesh for this many frequencies twice, print stats, exit")
     ap.add_argument("--profile-patch", default="", choices=["", "mixed", "plain"],

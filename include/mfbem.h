@@ -187,6 +187,17 @@ const char* mfbem_last_error(void);
 /* Library build identification: "<version> sm_103a". */
 const char* mfbem_version(void);
 
+/* Batch of harmonic sweeps over meshes of uneven size (no counterpart in the
+   reference; the reference solves one problem at a time). Mesh i has its own
+   material (lambda[2i], mu[2i], nu[2i] complex, rho[i]), n_freq[i]
+   frequencies omega[i][...] and solution array x_out[i] (as
+   mfbem_sweep_harela); the sweeps run concurrently on the GPU (one host
+   thread, stream and cuBLAS handle per mesh). stats: [n_mesh] or NULL. */
+int mfbem_sweep_harela_batch(int32_t n_mesh, mfbem_handle* const* hs, const double* lambda, const double* mu,
+                             const double* rho, const double* nu, const int32_t* n_freq, const double* const* omega,
+                             int32_t precision, double rel_tol, double* const* x_out, int32_t flags,
+                             mfbem_stats* stats);
+
 /* ---------------------------------------------------------------------------
  * Learned quadrature of quasi-singular pairs. No counterpart in the reference:
  * an extension that replaces sbie_ext_adp's adaptive subdivision

@@ -34,7 +34,7 @@ ABI_SYMBOLS = [
     "mfbem_solve_r", "mfbem_solve_c", "mfbem_sweep_harela", "mfbem_solve_staela", "mfbem_last_stats",
     "mfbem_last_error", "mfbem_version", "mfbem_solve_c_static",
     "mfbem_qlearn_label", "mfbem_mlp_size", "mfbem_mlp_forward", "mfbem_mlp_loss_grad", "mfbem_mlp_train",
-    "mfbem_set_learned_quadrature",
+    "mfbem_set_learned_quadrature", "mfbem_sweep_harela_batch",
 ]
 PREP_SYMBOLS = ["mfbem_prep_create", "mfbem_prep_desc", "mfbem_prep_free", "mfbem_prep_dof"]
 

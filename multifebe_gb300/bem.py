@@ -194,3 +194,31 @@ def solve_lse(A, b, ipiv=None, factorize=True):
     rc = fn(n, _p(A), _p(ipiv, _ip), 1, None, None, None, None, nrhs, _p(bb), 1 if factorize else 0, 0, 0, 0)
     check(rc)
     return b, ipiv
+
+
+def sweep_harela_batch(regions, materials, omegas, precision="mixed", rel_tol=1e-12):
+    """Sweeps of several meshes (uneven sizes allowed) in one call: every
+    mesh's sweep runs concurrently on the GPU (its own stream). Returns the
+    list of solution arrays [n_freq_i, n_i] and the per-mesh stats."""
+    k = len(regions)
+    vp = ctypes.c_void_p
+    L = _abi.load()
+    if not getattr(L, "_batch_set", False):
+        L.mfbem_sweep_harela_batch.argtypes = [ctypes.c_int32, vp, vp, vp, vp, vp, vp, vp, ctypes.c_int32,
+                                               ctypes.c_double, vp, ctypes.c_int32, vp]
+        L._batch_set = True
+    mats = materials if isinstance(materials, (list, tuple)) else [materials] * k
+    oms = [np.ascontiguousarray(o, dtype=np.float64) for o in omegas]
+    lam = np.array([[complex(m["lambda"]).real, complex(m["lambda"]).imag] for m in mats])
+    mu = np.array([[complex(m["mu"]).real, complex(m["mu"]).imag] for m in mats])
+    nu = np.array([[complex(m["nu"]).real, complex(m["nu"]).imag] for m in mats])
+    rho = np.array([float(m["rho"]) for m in mats])
+    nf = np.array([len(o) for o in oms], dtype=np.int32)
+    X = [np.zeros((len(o), r.n), dtype=np.complex128) for o, r in zip(oms, regions)]
+    hs = (vp * k)(*[r._h.value for r in regions])
+    op = (vp * k)(*[o.ctypes.data for o in oms])
+    xp = (vp * k)(*[x.ctypes.data for x in X])
+    st = (_abi.Stats * k)()
+    check(L.mfbem_sweep_harela_batch(k, hs, lam.ctypes.data, mu.ctypes.data, rho.ctypes.data, nu.ctypes.data,
+                                     nf.ctypes.data, op, PRECISION[precision], rel_tol, xp, 0, st))
+    return X, [s.as_dict() for s in st]

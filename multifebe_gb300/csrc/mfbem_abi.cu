@@ -9,6 +9,9 @@
 #include <chrono>
 #include <cmath>
 #include <complex>
+#include <map>
+#include <mutex>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -26,8 +29,9 @@
 
 namespace mfb {
 static thread_local std::string g_err;
-// kernels of this library launched so far (reported per call in mfbem_stats)
-static long long g_launches = 0;
+// kernels of this library launched so far by the calling thread (reported
+// per call in mfbem_stats; per thread so concurrent sweeps count their own)
+static thread_local long long g_launches = 0;
 void set_error(const std::string& s) { g_err = s; }
 int fail(int code, const std::string& s) {
   g_err = s;
@@ -96,7 +100,9 @@ static int ensure(DevBuf& b, size_t bytes) {
 }
 
 static bool g_tables_ready = false;
+static std::mutex g_tables_mu;
 static int init_tables() {
+  std::lock_guard<std::mutex> lk(g_tables_mu);
   if (g_tables_ready) return 0;
   const GLTables& t = host_gauss_tables();
   CK(cudaMemcpyToSymbol(c_gl, &t, sizeof(GLTables)));
@@ -635,6 +641,43 @@ extern "C" int mfbem_internal_zexp(int32_t n, const double* z, double* e64, doub
 #include "mfbem_learned.cuh"
 
 // ---------------------------------------------------------------------------
+// Batch of harmonic sweeps over meshes of uneven size (no counterpart in the
+// reference): every mesh's sweep runs on its own host thread, stream and
+// cuBLAS handle, so small problems share the GPU instead of running one
+// after another. Per mesh i: material lambda[2i..], mu[2i..], rho[i],
+// nu[2i..], n_freq[i] frequencies omega[i][...], solutions x_out[i].
+// ---------------------------------------------------------------------------
+extern "C" int mfbem_sweep_harela_batch(int32_t n_mesh, mfbem_handle* const* hs, const double* lambda,
+                                        const double* mu, const double* rho, const double* nu, const int32_t* n_freq,
+                                        const double* const* omega, int32_t precision, double rel_tol,
+                                        double* const* x_out, int32_t flags, mfbem_stats* stats) {
+  g_err.clear();
+  if (n_mesh <= 0 || !hs || !lambda || !mu || !rho || !nu || !n_freq || !omega || !x_out)
+    return fail(MFBEM_EARG, "invalid argument");
+  std::vector<int> rc(n_mesh, 0);
+  std::vector<std::string> msg(n_mesh);
+  std::vector<mfbem_stats> st(n_mesh);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::vector<std::thread> th;
+  th.reserve(n_mesh);
+  for (int i = 0; i < n_mesh; ++i)
+    th.emplace_back([&, i]() {
+      cudaSetDevice(dev);
+      g_concurrent = n_mesh > 1;
+      rc[i] = mfbem_sweep_harela(hs[i], lambda + 2 * i, mu + 2 * i, rho[i], nu + 2 * i, n_freq[i], omega[i], precision,
+                                 rel_tol, x_out[i], flags, &st[i]);
+      if (rc[i]) msg[i] = g_err;
+    });
+  for (auto& t : th) t.join();
+  if (stats)
+    for (int i = 0; i < n_mesh; ++i) stats[i] = st[i];
+  for (int i = 0; i < n_mesh; ++i)
+    if (rc[i]) return fail(rc[i], "mesh " + std::to_string(i) + ": " + msg[i]);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
 // Learned quadrature of near-singular pairs (no counterpart in the reference)
 // ---------------------------------------------------------------------------
 // tolerance curves of the reference-rule candidates (1e-3 .. 1e-9)
@@ -741,8 +784,8 @@ static int mlp_run(const float* w, int n, const float* feat, const float* y, con
   }
   std::vector<int> ones;
   if (!valid) { ones.assign(n, 1); valid = ones.data(); }
-  cudaError_t e = cudaFuncSetAttribute(k_mlp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ql_smem_bytes());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ql_smem_bytes());
+  cudaError_t e = (raise_smem_limit((const void*)k_mlp<true>) || raise_smem_limit((const void*)k_mlp<false>))
+                      ? cudaErrorInvalidValue : cudaSuccess;
   if (e == cudaSuccess) e = cudaMemcpy(bw.p, w, sizeof(float) * QL_NW, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(bf.p, feat, sizeof(float) * QL_NF * (size_t)n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && y) e = cudaMemcpy(by.p, y, sizeof(float) * QL_NC * (size_t)n, cudaMemcpyHostToDevice);
@@ -801,7 +844,7 @@ extern "C" int mfbem_mlp_train(float* w, int32_t n, const float* feat, const flo
   }
   std::vector<int> ones;
   if (!valid) { ones.assign(n, 1); valid = ones.data(); }
-  cudaError_t e = cudaFuncSetAttribute(k_mlp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ql_smem_bytes());
+  cudaError_t e = raise_smem_limit((const void*)k_mlp<true>) ? cudaErrorInvalidValue : cudaSuccess;
   if (e == cudaSuccess) e = cudaMemcpy(bw.p, w, sizeof(float) * QL_NW, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(bf.p, feat, sizeof(float) * QL_NF * (size_t)n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(by.p, y, sizeof(float) * QL_NC * (size_t)n, cudaMemcpyHostToDevice);

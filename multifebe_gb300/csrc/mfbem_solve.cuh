@@ -10,7 +10,7 @@
 // preconditioner; refinement in FP64 restores the accuracy and escalates to
 // SIMT FP32 when it stalls), 2 cuBLAS's BF16x9 FP32 emulation. Default TF32;
 // MFBEM_FP32_GEMM=simt|tf32|bf16x9 overrides.
-static int g_c32_mode = 1;
+static thread_local int g_c32_mode = 1;
 static int c32_default() {
   const char* e = getenv("MFBEM_FP32_GEMM");
   const std::string v = e ? e : "tf32";
@@ -56,8 +56,38 @@ template <typename S> struct IsF64 { static const bool v = false; };
 template <> struct IsF64<double> { static const bool v = true; };
 template <> struct IsF64<double2> { static const bool v = true; };
 
-// Workspace of the cooperative panel (barrier counters, candidate exchange, error flag)
-static DevBuf g_lu_ws;
+// Workspace of the cooperative panel (barrier counters, candidate exchange,
+// error flag); per host thread, so concurrent sweeps do not share it
+static thread_local DevBuf g_lu_ws;
+// Concurrent sweeps (mfbem_sweep_harela_batch): a cooperative panel launch
+// waits on its own CTAs only, and two of them sharing the SMs could each hold
+// part of the machine; so under concurrency the panels run one at a time
+// (mutex held until the panel kernel has finished).
+static std::mutex g_coop_mu;
+static thread_local bool g_concurrent = false;
+
+// The dynamic shared-memory limit is a process-wide attribute of a kernel:
+// raise it once to the device's opt-in maximum (a per-call value would race
+// between concurrent sweeps with different sizes).
+static int raise_smem_limit(const void* f) {
+  static std::mutex mu;
+  static std::vector<const void*> done;
+  std::lock_guard<std::mutex> lk(mu);
+  for (const void* d : done)
+    if (d == f) return 0;
+  int dev = 0, mx = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa;
+  cudaFuncGetAttributes(&fa, f);
+  const int lim = mx - (int)fa.sharedSizeBytes;
+  if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  done.push_back(f);
+  return 0;
+}
 
 // Plan of the cooperative panel for n x n matrices in a batch: G CTAs per
 // matrix (panel rows split in G chunks held in shared memory, at most
@@ -84,10 +114,7 @@ static bool coop_plan(int n, int nb, int batch, CoopPlan* pl) {
   G = std::max(1, std::min(G, n));
   const int chunk = (n + G - 1) / G;
   const size_t smem = ((size_t)nb * chunk + nb) * es;
-  if (cudaFuncSetAttribute(k_panel_coop<S, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
+  if (raise_smem_limit((const void*)k_panel_coop<S, 256>)) return false;
   int bps = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_panel_coop<S, 256>, 256, smem) != cudaSuccess || bps < 1) {
     cudaGetLastError();
@@ -104,7 +131,7 @@ static bool coop_plan(int n, int nb, int batch, CoopPlan* pl) {
 // Blocked right-looking getrf for a batch of n x n matrices (stride sA).
 template <typename S>
 static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA, int lda, int n, int batch,
-                         int* ipiv, int* info) {
+                         int* ipiv, int* info, int nbo = 128) {
   // panel width: the L11 block of the TRSM lives in shared memory (<= 16 KB)
   const int nb = 32;
   CK(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
@@ -139,7 +166,7 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
   // Two-level blocking: outer blocks of NBO columns are factorised with inner
   // panels of nb columns (updates restricted to the outer block), then one
   // trailing GEMM of depth NBO updates the rest of the matrix.
-  const int NBO = 128;
+  const int NBO = std::max(nb, nbo);
   for (int K = 0; K < n; K += NBO) {
     const int KE = std::min(n, K + NBO);
     for (int k = K; k < KE; k += nb) {
@@ -151,9 +178,12 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
           int Gp = pl.G, ck = chunk, kk = k, kbb = kb, nn_ = n, ldaa = lda, bb0 = b0;
           long long sAA = sA;
           void* args[] = {&A, &sAA, &ldaa, &nn_, &kk, &kbb, &Gp, &ck, &bb0, &ipiv, &info, &ctr, &xrow, &xval, &xidx, &derr};
+          std::unique_lock<std::mutex> lk(g_coop_mu, std::defer_lock);
+          if (g_concurrent) lk.lock();
           CK(cudaLaunchCooperativeKernel((const void*)k_panel_coop<S, 256>, dim3(pl.G * nbm), dim3(256), args,
                                          ((size_t)kb * chunk + kb) * sizeof(S), st));
           ++g_launches;
+          if (g_concurrent) CK(cudaStreamSynchronize(st));
         }
       } else if (multi) {
         for (int j = k; j < k + kb; ++j) {
@@ -200,6 +230,77 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner of the mixed LU's outer block width (64, 128 or 256 columns: the
+// depth of the trailing GEMMs against the number of panel steps), per scalar
+// type, size class (n rounded up to 512), batch and GEMM compute type. The
+// first factorisation of a class times the candidates on a seeded random
+// batch of that size (partial pivoting; the operation count is what is timed)
+// and caches the fastest.
+// MFBEM_AUTOTUNE=0 keeps 128.
+// ---------------------------------------------------------------------------
+template <typename S> __device__ __forceinline__ S rnd_val(unsigned long long h);
+template <> __device__ __forceinline__ float rnd_val<float>(unsigned long long h) {
+  return (float)((h >> 40) & 0xFFFFFF) / 16777216.0f - 0.5f;
+}
+template <> __device__ __forceinline__ float2 rnd_val<float2>(unsigned long long h) {
+  return make_float2((float)((h >> 40) & 0xFFFFFF) / 16777216.0f - 0.5f, (float)((h >> 8) & 0xFFFFFF) / 16777216.0f - 0.5f);
+}
+template <typename S>
+__global__ void k_tune_fill(S* A, long long total) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    unsigned long long z = (unsigned long long)i * 0x9E3779B97F4A7C15ULL + 0x632BE59BD9B4E019ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    A[i] = rnd_val<S>(z);
+  }
+}
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, int>, int> g_tune;
+template <typename S>
+static int tuned_nbo(cublasHandle_t hb, cudaStream_t st, int n, int batch, int* ipiv, int* info, int* out) {
+  *out = 128;
+  const char* e = getenv("MFBEM_AUTOTUNE");
+  if (e && std::string(e) == "0") return 0;
+  const auto key = std::make_tuple((int)sizeof(S), (n + 511) / 512, batch, g_c32_mode);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) { *out = it->second; return 0; }
+  }
+  const long long nn = (long long)n * n;
+  S* T = nullptr;
+  if (cudaMalloc(&T, sizeof(S) * nn * batch) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;  // no room to tune: keep the default
+  }
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  const int cand[3] = {64, 128, 256};
+  float best = 1e30f;
+  int bn = 128, rc = 0;
+  for (int c = 0; c < 3 && !rc; ++c) {
+    k_tune_fill<S><<<152 * 8, 256, 0, st>>>(T, nn * batch); ++g_launches;
+    cudaEventRecord(t0, st);
+    rc = getrf_batched<S>(hb, st, T, nn, n, n, batch, ipiv, info, cand[c]);
+    cudaEventRecord(t1, st);
+    cudaEventSynchronize(t1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    if (!rc && ms < best) { best = ms; bn = cand[c]; }
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(T);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = bn;
+  *out = bn;
+  return 0;
+}
+
 // getrs (no transpose) for one right-hand side per batch entry.
 // A: batch stride sA (0 = shared factors), ipiv stride sP, b stride sb.
 template <typename S>
@@ -217,6 +318,41 @@ __global__ void k_rhs_swap2(S* b, long long sb, int n, const int* ipiv, long lon
     }
   }
 }
+// The row interchanges of getrs as one permutation: a single thread per
+// matrix replays the n swaps on an index array in shared memory, then the
+// right-hand sides are gathered in parallel.
+__global__ void k_perm(const int* ipiv, long long sP, int n, int* perm) {
+  extern __shared__ int pm[];
+  const int bi = blockIdx.x;
+  const int* piv = ipiv + sP * bi;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) pm[i] = i;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int j = 0; j < n; ++j) {
+      const int p = piv[j] - 1;
+      if (p != j) {
+        const int t = pm[j];
+        pm[j] = pm[p];
+        pm[p] = t;
+      }
+    }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[(size_t)n * bi + i] = pm[i];
+}
+template <typename S>
+__global__ void k_gather_perm(const S* x, long long sx, const int* perm, int n, S* out) {
+  const int bi = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[(size_t)n * bi + i] = x[sx * bi + perm[(size_t)n * bi + i]];
+}
+template <typename S>
+__global__ void k_scatter_back(const S* tmp, int n, S* x, long long sx) {
+  const int bi = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x[sx * bi + i] = tmp[(size_t)n * bi + i];
+}
+static thread_local DevBuf g_rs_ws;
+
 template <typename S>
 static int getrs_batched(cudaStream_t st, const S* A, long long sA, int lda, int n, const int* ipiv, long long sP,
                          S* b, long long sb, int batch) {
@@ -224,13 +360,22 @@ static int getrs_batched(cudaStream_t st, const S* A, long long sA, int lda, int
   // below / above updated by a GEMV over the solved block
   const int TB = 64;
   const size_t dsm = (size_t)TB * 65 * sizeof(S);
-  static bool attr = false;
-  if (!attr) {
-    CK(cudaFuncSetAttribute(k_trsv_diag64<S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
-    CK(cudaFuncSetAttribute(k_trsv_diag64<S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
-    attr = true;
+  if (raise_smem_limit((const void*)k_trsv_diag64<S, true>) || raise_smem_limit((const void*)k_trsv_diag64<S, false>))
+    return fail(MFBEM_ECUDA, "shared-memory limit of the triangular solve");
+  const size_t psm = (size_t)n * sizeof(int);
+  bool gathered = false;
+  if (psm <= 200 * 1024) {
+    int rc = ensure(g_rs_ws, (size_t)batch * n * (sizeof(int) + sizeof(S)) + 256);
+    if (rc) return rc;
+    if (psm > 48 * 1024 && raise_smem_limit((const void*)k_perm)) return fail(MFBEM_ECUDA, "shared-memory limit of the row permutation");
+    int* perm = (int*)g_rs_ws.p;
+    S* tmp = (S*)((char*)g_rs_ws.p + ((size_t)batch * n * sizeof(int) + 255) / 256 * 256);
+    k_perm<<<batch, 256, psm, st>>>(ipiv, sP, n, perm); ++g_launches;
+    k_gather_perm<S><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(b, sb, perm, n, tmp); ++g_launches;
+    k_scatter_back<S><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(tmp, n, b, sb); ++g_launches;
+    gathered = true;
   }
-  k_rhs_swap2<S><<<nblk(batch, 64), 64, 0, st>>>(b, sb, n, ipiv, sP, batch); ++g_launches;
+  if (!gathered) { k_rhs_swap2<S><<<nblk(batch, 64), 64, 0, st>>>(b, sb, n, ipiv, sP, batch); ++g_launches; }
   for (int r0 = 0; r0 < n; r0 += TB) {
     int w = std::min(TB, n - r0);
     k_trsv_diag64<S, true><<<batch, 128, dsm, st>>>(A, sA, lda, b, sb, r0, w); ++g_launches;
@@ -805,6 +950,14 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventCreate(&e2);
+  // mixed: the outer block width of this size class (a first use runs the
+  // autotuner, outside the timed factorisation)
+  int nbo = 128;
+  if (precision != 0) {
+    g_c32_mode = c32_default();
+    if (g_c32_mode == 1 && h->tf32_stalled) g_c32_mode = 0;
+    if ((rc = tuned_nbo<SF>(h->blas, st, n, batch, ipiv, info, &nbo))) return rc;
+  }
   cudaEventRecord(e0, st);
   std::vector<int> hinfo(batch);
   if (precision == 0) {
@@ -840,9 +993,7 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     k_demote_rowabs<SD, SF><<<dim3(nblk(n, 256), nblk(n, 128), batch), 256, 0, st>>>(A, c.A32, nn, n, n, rows); ++g_launches;
     k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, c.nrm, 3, 8); ++g_launches;
     k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, c.nrm, 2, 8); ++g_launches;
-    g_c32_mode = c32_default();
-    if (g_c32_mode == 1 && h->tf32_stalled) g_c32_mode = 0;
-    if ((rc = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info))) return rc;
+    if ((rc = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info, nbo))) return rc;
     cudaEventRecord(e1, st);
     CK(cudaMemsetAsync(x, 0, sizeof(SD) * (size_t)n * batch, st));
     // refinement: precision 1, classical refinement until it converges or
@@ -861,7 +1012,9 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
       h->tf32_stalled = true;
       ++c.refactor;
       k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, c.A32, nn * batch); ++g_launches;
-      int r = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info);
+      int nb2 = 128;
+      int r = tuned_nbo<SF>(h->blas, st, n, batch, ipiv, info, &nb2);
+      if (!r) r = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info, nb2);
       cudaEventRecord(f1, st);
       cudaEventSynchronize(f1);
       float t = 0.0f;
