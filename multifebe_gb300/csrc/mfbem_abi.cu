@@ -26,6 +26,7 @@
 #include "mfbem_precompute.cuh"
 #include "mfbem_assemble.cuh"
 #include "mfbem_lu.cuh"
+#include "mfbem_tc.cuh"
 
 namespace mfb {
 static thread_local std::string g_err;
@@ -639,6 +640,43 @@ extern "C" int mfbem_internal_zexp(int32_t n, const double* z, double* e64, doub
 
 #include "mfbem_solve.cuh"
 #include "mfbem_learned.cuh"
+
+// Test hook (not part of the reference interface): C -= A B for complex64
+// column-major A (m x k), B (k x n), C (m x n) with the tcgen05 3xTF32 kernel.
+extern "C" int mfbem_internal_tc_cgemm(int32_t m, int32_t n, int32_t k, const float* A, const float* B, float* C) {
+  g_err.clear();
+  if (m <= 0 || n <= 0 || k < 0 || !A || !B || !C) return fail(MFBEM_EARG, "invalid argument");
+  int rc;
+  DevBuf dA, dB, dC, dE;
+  auto cleanup = [&]() {
+    for (DevBuf* b : {&dA, &dB, &dC, &dE})
+      if (b->p) cudaFree(b->p);
+  };
+  const size_t sa = 8 * (size_t)m * std::max(k, 1), sb = 8 * (size_t)std::max(k, 1) * n, sc = 8 * (size_t)m * n;
+  if ((rc = ensure(dA, sa)) || (rc = ensure(dB, sb)) || (rc = ensure(dC, sc)) || (rc = ensure(dE, sizeof(int)))) {
+    cleanup();
+    return rc;
+  }
+  cudaError_t e = raise_smem_limit((const void*)k_tc_cgemm) ? cudaErrorInvalidValue : cudaSuccess;
+  if (e == cudaSuccess && k > 0) e = cudaMemcpy(dA.p, A, 8 * (size_t)m * k, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && k > 0) e = cudaMemcpy(dB.p, B, 8 * (size_t)k * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dC.p, C, sc, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(dE.p, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    dim3 g(nblk(m, TC_BM / 2), nblk(n, TC_BN), 1);
+    k_tc_cgemm<<<g, 128, TC_SMEM>>>((const float2*)dA.p, m, 0, (const float2*)dB.p, std::max(k, 1), 0, (float2*)dC.p,
+                                    m, 0, m, n, k, (int*)dE.p);
+    ++g_launches;
+    e = cudaGetLastError();
+  }
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(C, dC.p, sc, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, dE.p, sizeof(int), cudaMemcpyDeviceToHost);
+  cleanup();
+  if (e != cudaSuccess) return fail(MFBEM_ECUDA, std::string("tc cgemm: ") + cudaGetErrorString(e));
+  if (herr) return fail(MFBEM_ETIMEOUT, "tc cgemm: an MMA completion wait timed out");
+  return 0;
+}
 
 // ---------------------------------------------------------------------------
 // Batch of harmonic sweeps over meshes of uneven size (no counterpart in the

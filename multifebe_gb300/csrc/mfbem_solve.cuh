@@ -14,8 +14,11 @@ static thread_local int g_c32_mode = 1;
 static int c32_default() {
   const char* e = getenv("MFBEM_FP32_GEMM");
   const std::string v = e ? e : "tf32";
-  return v == "simt" ? 0 : (v == "bf16x9" ? 2 : 1);
+  return v == "simt" ? 0 : (v == "bf16x9" ? 2 : (v == "tc3" ? 3 : 1));
 }
+// mode 3: this library's tcgen05 3xTF32 kernel (mfbem_tc.cuh) for the complex
+// updates; its timeout flag, per host thread
+static thread_local DevBuf g_tc_err;
 static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const double* A, int lda, long long sA,
                               const double* B, int ldb, long long sB, double* C, int ldc, long long sC, int batch) {
   const double al = -1.0, be = 1.0;
@@ -25,7 +28,7 @@ static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const doub
 static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const float* A, int lda, long long sA,
                               const float* B, int ldb, long long sB, float* C, int ldc, long long sC, int batch) {
   const float al = -1.0f, be = 1.0f;
-  if (g_c32_mode > 0)
+  if (g_c32_mode > 0 && g_c32_mode < 3)
     return cublasGemmStridedBatchedEx(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, CUDA_R_32F, lda, sA, B, CUDA_R_32F,
                                       ldb, sB, &be, C, CUDA_R_32F, ldc, sC, batch,
                                       g_c32_mode == 1 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F_EMULATED_16BFX9,
@@ -43,7 +46,15 @@ static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const floa
                               const float2* B, int ldb, long long sB, float2* C, int ldc, long long sC, int batch) {
   const cuComplex al = make_cuComplex(-1.0f, 0.0f), be = make_cuComplex(1.0f, 0.0f);
   const int mode = g_c32_mode;
-  if (mode > 0)
+  if (mode == 3 && g_tc_err.p) {
+    cudaStream_t st = nullptr;
+    cublasGetStream(hb, &st);
+    dim3 g((unsigned)((m + TC_BM / 2 - 1) / (TC_BM / 2)), (unsigned)((n + TC_BN - 1) / TC_BN), (unsigned)batch);
+    k_tc_cgemm<<<g, 128, TC_SMEM, st>>>(A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, (int*)g_tc_err.p);
+    ++g_launches;
+    return cudaGetLastError() == cudaSuccess ? CUBLAS_STATUS_SUCCESS : CUBLAS_STATUS_EXECUTION_FAILED;
+  }
+  if (mode > 0 && mode < 3)
     return cublasGemmStridedBatchedEx(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, CUDA_C_32F, lda, sA, B, CUDA_C_32F,
                                       ldb, sB, &be, C, CUDA_C_32F, ldc, sC, batch,
                                       mode == 1 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F_EMULATED_16BFX9,
@@ -136,6 +147,13 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
   const int nb = 32;
   CK(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
   typedef typename Sc<S>::R R;
+  const bool tc = g_c32_mode == 3 && std::is_same<S, float2>::value;
+  if (tc) {
+    int rc = ensure(g_tc_err, sizeof(int));
+    if (rc) return rc;
+    if (raise_smem_limit((const void*)k_tc_cgemm)) return fail(MFBEM_ECUDA, "shared-memory limit of the tcgen05 GEMM");
+    CK(cudaMemsetAsync(g_tc_err.p, 0, sizeof(int), st));
+  }
   CoopPlan pl;
   const bool coop = coop_plan<S>(n, nb, batch, &pl);
   unsigned* ctr = nullptr;
@@ -226,6 +244,12 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
     CK(cudaMemcpyAsync(&e, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (e) return fail(MFBEM_ETIMEOUT, "LU panel: a barrier wait timed out");
+  }
+  if (tc) {
+    int e = 0;
+    CK(cudaMemcpyAsync(&e, g_tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (e) return fail(MFBEM_ETIMEOUT, "LU trailing update: a tensor-core completion wait timed out");
   }
   return 0;
 }
@@ -726,7 +750,14 @@ struct MixCtx {
   int it = 0, inner = 0, refactor = 0;
   double maxbe = 0.0;
   std::vector<double> be;
+  // classical refinement: ||d|| / ||x|| of each system's last correction
+  // (infinity norms; +inf before the first), and ||r|| it was scaled by
+  std::vector<double> dx, rprev;
 };
+// forward criterion of the classical refinement: the last correction is at
+// most this fraction of x (with the backward-error test it bounds the forward
+// error on ill-conditioned systems, where a small backward error alone does not)
+constexpr double kFwdTol = 1e-10;
 
 // r = b - A x, backward errors ||r|| / (||A|| ||x|| + ||b||) (infinity norms);
 // active[b] = not yet converged. Returns whether all converged.
@@ -743,6 +774,8 @@ static int residual_check(MixCtx<SD, SF>& c, bool first, bool* all) {
   CK(cudaMemcpyAsync(hn.data(), c.nrm, sizeof(double) * 8 * batch, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   c.be.assign(batch, 1.0);
+  if ((int)c.dx.size() != batch) c.dx.assign(batch, 1e300);
+  if ((int)c.rprev.size() != batch) c.rprev.assign(batch, 0.0);
   std::vector<int> hact(batch);
   c.maxbe = 0.0;
   bool any = false;
@@ -750,8 +783,9 @@ static int residual_check(MixCtx<SD, SF>& c, bool first, bool* all) {
     double be = first ? 1.0 : hn[8 * bi + 0] / (hn[8 * bi + 3] * hn[8 * bi + 1] + hn[8 * bi + 2]);
     c.be[bi] = be;
     c.maxbe = std::max(c.maxbe, be);
-    hact[bi] = be > c.tol ? 1 : 0;
+    hact[bi] = (be > c.tol || c.dx[bi] > kFwdTol) ? 1 : 0;
     any = any || hact[bi];
+    c.rprev[bi] = hn[8 * bi + 0];
   }
   CK(cudaMemcpyAsync(c.active, hact.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, st));
   *all = !any;
@@ -798,6 +832,15 @@ static int refine_classical(MixCtx<SD, SF>& c, int* conv) {
     k_scale_demote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(c.r, n, c.d32, n, n, c.nrm, 8, 0); ++g_launches;
     if ((rc = getrs_batched<SF>(st, c.A32, nn, n, n, c.ipiv, n, c.d32, n, batch))) return rc;
     k_update<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(c.x, n, c.d32, n, n, c.nrm, 8, 0, c.active); ++g_launches;
+    // size of this correction relative to the updated x (for the forward criterion)
+    k_vecmax<SF><<<batch, 256, 0, st>>>(c.d32, n, n, c.nrm, 5, 8); ++g_launches;
+    k_vecmax<SD><<<batch, 256, 0, st>>>(c.x, n, n, c.nrm, 6, 8); ++g_launches;
+    std::vector<double> hn(8 * (size_t)batch);
+    CK(cudaMemcpyAsync(hn.data(), c.nrm, sizeof(double) * 8 * batch, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int bi = 0; bi < batch; ++bi)
+      if (c.be[bi] > c.tol || c.dx[bi] > kFwdTol)
+        c.dx[bi] = c.rprev[bi] * hn[8 * bi + 5] / std::max(hn[8 * bi + 6], 1e-300);
     ++c.it;
   }
 }
@@ -832,6 +875,7 @@ static int refine_gmres(MixCtx<SD, SF>& c, int* conv) {
     else return v.real();
   };
   *conv = 0;
+  c.dx.assign(batch, 0.0);  // GMRES-IR stops on the backward error alone
   for (int outer = 0; outer < 10; ++outer) {
     bool all;
     if ((rc = residual_check(c, c.it == 0 && outer == 0, &all))) return rc;

@@ -1,0 +1,214 @@
+// Complex64 GEMM update C -= A B on the 5th-generation tensor cores (tcgen05,
+// kind::tf32) with the 3xTF32 split (A_hi B_hi + A_hi B_lo + A_lo B_hi, each
+// operand x = hi + lo with hi = tf32(x)), i.e. FP32-level accuracy: the
+// trailing update of the mixed LU. Included into mfbem_abi.cu.
+//
+// The complex product is one real GEMM of the realified operands:
+//   C~ (2m x n)  = C viewed as real, column j = [re C0j, im C0j, re C1j, ...]
+//   B~ (2k x n)  = B viewed as real (same memory)
+//   A~ (2m x 2k) : A~(2i,2l) = re a_il, A~(2i+1,2l) = im a_il,
+//                  A~(2i,2l+1) = -im a_il, A~(2i+1,2l+1) = re a_il
+// so C~ -= A~ B~ is C -= A B. A CTA (4 warps) computes a 128 x 128 tile of C~
+// (64 complex rows x 128 columns): per chunk of 32 real K it stages A~ and B~
+// (hi and lo parts) in shared memory in the canonical K-major layout without
+// swizzle (8-row x 16-byte core matrices, 128 B apart along K, 1024 B apart
+// along M/N), thread 0 issues 4 K-steps x 3 products of
+// tcgen05.mma.cta_group::1.kind::tf32 (M 128, N 128, K 8) into a 128-column
+// TMEM accumulator and commits to an mbarrier; after the last chunk every
+// warp reads its 32 TMEM lanes (tcgen05.ld 32x32b) and subtracts from C.
+// Every wait is bounded: on a timeout the kernel sets *err, waits (bounded)
+// for its MMAs, frees its TMEM and returns.
+#pragma once
+#include <cstdint>
+
+namespace mfb {
+
+constexpr int TC_BM = 128;  // real rows of C~ per CTA (64 complex rows)
+constexpr int TC_BN = 128;  // columns per CTA
+constexpr int TC_BK = 32;   // real K per chunk (16 complex)
+constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 4;  // one operand tile (16 KB); B tile is TC_BN x TC_BK
+constexpr int TC_SMEM = 4 * TC_TILE_BYTES + 64;    // A hi/lo, B hi/lo, mbarrier, TMEM address
+constexpr long long TC_SPIN = 1LL << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint32_t f2tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+// offset in bytes of element (row r, k) of a K-major no-swizzle tile with
+// 8 x 16 B core matrices, LBO 128 B (K), SBO 1024 B (rows)
+__device__ __forceinline__ uint32_t tc_off(int r, int k) {
+  return (uint32_t)((r >> 3) * 1024 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+// shared memory descriptor: start address, LBO, SBO (>> 4), version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)(128 >> 4) << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+// instruction descriptor, kind::tf32: D f32, A and B tf32, both K-major, N, M
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+  for (long long it = 0; it < TC_SPIN; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// C (m x n complex, ldc) -= A (m x k, lda) B (k x n, ldb), batch in blockIdx.z
+__global__ void __launch_bounds__(128, 1) k_tc_cgemm(const float2* A, int lda, long long sA, const float2* B, int ldb,
+                                                     long long sB, float2* C, int ldc, long long sC, int m, int n,
+                                                     int k, int* err) {
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  unsigned char* Ahi = tsm;
+  unsigned char* Alo = tsm + TC_TILE_BYTES;
+  unsigned char* Bhi = tsm + 2 * TC_TILE_BYTES;
+  unsigned char* Blo = tsm + 3 * TC_TILE_BYTES;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(tsm + 4 * TC_TILE_BYTES);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + 4 * TC_TILE_BYTES + 16);
+  __shared__ int s_ok;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int bz = blockIdx.z;
+  const float2* Ab = A + sA * bz;
+  const float2* Bb = B + sB * bz;
+  float2* Cb = C + sC * bz;
+  const int i0 = blockIdx.x * (TC_BM / 2);  // first complex row
+  const int j0 = blockIdx.y * TC_BN;        // first column
+  const uint32_t mb = smem_u32(mbar);
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_ok = 1;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(TC_BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc_idesc(TC_BM, TC_BN);
+  const int nchunk = (k + TC_BK / 2 - 1) / (TC_BK / 2);
+  int phase = 0;
+  for (int ch = 0; ch < nchunk && s_ok; ++ch) {
+    const int l0 = ch * (TC_BK / 2);
+    // A~ tile: 64 complex rows x 16 complex columns -> 128 x 32 reals
+    for (int e = t; e < 64 * 16; e += 128) {
+      const int ii = e & 63, ll = e >> 6;
+      const int i = i0 + ii, l = l0 + ll;
+      float2 a = make_float2(0.0f, 0.0f);
+      if (i < m && l < k) a = Ab[(size_t)l * lda + i];
+      const float v[4] = {a.x, a.y, -a.y, a.x};  // (2ii,2ll) (2ii+1,2ll) (2ii,2ll+1) (2ii+1,2ll+1)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = 2 * ii + (q & 1), kk = 2 * ll + (q >> 1);
+        const uint32_t hi = f2tf32(v[q]);
+        const uint32_t lo = f2tf32(v[q] - __uint_as_float(hi));
+        const uint32_t o = tc_off(r, kk);
+        *reinterpret_cast<uint32_t*>(Ahi + o) = hi;
+        *reinterpret_cast<uint32_t*>(Alo + o) = lo;
+      }
+    }
+    // B~ tile: 16 complex rows x 128 columns -> K-major (row = column j, k = 2 l + c)
+    for (int e = t; e < 16 * TC_BN; e += 128) {
+      const int ll = e & 15, jj = e >> 4;
+      const int l = l0 + ll, j = j0 + jj;
+      float2 b = make_float2(0.0f, 0.0f);
+      if (l < k && j < n) b = Bb[(size_t)j * ldb + l];
+      const float v[2] = {b.x, b.y};
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const uint32_t hi = f2tf32(v[c]);
+        const uint32_t lo = f2tf32(v[c] - __uint_as_float(hi));
+        const uint32_t o = tc_off(jj, 2 * ll + c);
+        *reinterpret_cast<uint32_t*>(Bhi + o) = hi;
+        *reinterpret_cast<uint32_t*>(Blo + o) = lo;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (t == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t ah = smem_u32(Ahi), al = smem_u32(Alo), bh = smem_u32(Bhi), bl = smem_u32(Blo);
+#pragma unroll
+      for (int ks = 0; ks < TC_BK / 8; ++ks) {
+        const uint32_t ko = ks * 256;  // 8 tf32 = two core matrices along K
+        const uint64_t dah = tc_desc(ah + ko), dal = tc_desc(al + ko), dbh = tc_desc(bh + ko), dbl = tc_desc(bl + ko);
+        const uint32_t acc0 = (ch > 0 || ks > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                tmem),
+            "l"(dah), "l"(dbh), "r"(idesc), "r"(acc0)
+            : "memory");
+        asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(tmem), "l"(dah), "l"(dbl),
+                     "r"(idesc)
+                     : "memory");
+        asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(tmem), "l"(dal), "l"(dbh),
+                     "r"(idesc)
+                     : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
+                   : "memory");
+    }
+    // the tiles are reused by the next chunk: wait for this chunk's MMAs
+    if (!tc_wait(mb, (uint32_t)phase)) {
+      if (t == 0) atomicExch(err, 1);
+      s_ok = 0;
+    }
+    phase ^= 1;
+    __syncthreads();
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (s_ok && nchunk > 0) {
+    // epilogue: warp w reads TMEM lanes 32w..32w+31 (rows of C~), 32 columns at a time
+    const int r = 32 * warp + lane;  // real row of the tile
+    const int i = i0 + (r >> 1), comp = r & 1;
+    for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+      uint32_t v[32];
+      const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+          "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+            "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+            "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+          : "r"(ta)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (i < m) {
+        float* cr = reinterpret_cast<float*>(Cb);
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          const int j = j0 + c0 + q;
+          if (j < n) cr[2 * ((size_t)j * ldc + i) + comp] -= __uint_as_float(v[q]);
+        }
+      }
+    }
+  } else if (!s_ok && threadIdx.x == 0) {
+    // give in-flight MMAs a bounded chance to finish before the TMEM is freed
+    tc_wait(mb, (uint32_t)phase);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN) : "memory");
+}
+
+}  // namespace mfb

@@ -185,14 +185,15 @@ def test_zexp_double_float_matches_fp64():
     assert ra.max() < 2e-13, (ra.max(), z[~small][ra.argmax()])
 
 
-@pytest.mark.parametrize("gemm", ["simt", "tf32"])
+@pytest.mark.parametrize("gemm", ["simt", "tf32", "tc3"])
 @pytest.mark.parametrize("name,mk", [("cube4", lambda: M.cube_clamped_top_traction(4)), ("slab4", lambda: M.slab(4, 1)),
                                      ("patch8", lambda: M.surface_patch(10.0, 8, 1.0))],
                          ids=["cube4", "slab4", "patch8"])
 def test_mixed_sweep_trailing_update_modes(oracle, monkeypatch, gemm, name, mk):
-    """Mixed sweep with SIMT FP32 and TF32 tensor-core trailing updates: both
-    reach the FP64 oracle solution to 1e-8 (TF32 factors are refined in FP64,
-    and escalate to SIMT FP32 when refinement stalls)."""
+    """Mixed sweep with SIMT FP32, cuBLAS TF32 and this library's tcgen05
+    3xTF32 trailing updates: all reach the FP64 oracle solution to 1e-8 (TF32
+    factors are refined in FP64 and escalate to SIMT FP32 when refinement
+    stalls)."""
     monkeypatch.setenv("MFBEM_FP32_GEMM", gemm)
     d = mk()
     mat = M.viscoelastic(1.0, 0.3, 1.0, 0.05)
