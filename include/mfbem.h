@@ -144,13 +144,14 @@ int mfbem_solve_c(int32_t n, double* A, int32_t* ipiv, int32_t aodim, double* Ao
    precision 0: plain FP64 LU (the drop-in method).
    precision 1: complex64 LU with FP64 iterative refinement to rel_tol in the
                 backward error (the FP64 residual r = b - A x is evaluated with
-                the FP64 matrix). The LU's trailing updates run on the TF32
-                tensor cores; classical refinement x += LU^-1 r follows; if it
-                stalls, the LU is redone with SIMT FP32 updates and refined
-                again, and GMRES-based refinement (FP64 GMRES preconditioned by
-                the LU factors) is the last resort.
-   precision 2: GMRES-based refinement from the start (refactorised with SIMT
-                FP32 updates if it does not converge with the TF32 factors).
+                the FP64 matrix) and until the last correction is below 1e-10
+                of x. The LU's trailing updates run on the tensor cores
+                (tcgen05, 3xTF32: FP32-accurate factors); classical refinement
+                x += LU^-1 r follows, GMRES-based refinement (FP64 GMRES
+                preconditioned by the LU factors) when it stalls. With
+                MFBEM_FP32_GEMM=tf32 (single-pass TF32 updates) a stall first
+                redoes the LU with SIMT FP32 updates.
+   precision 2: GMRES-based refinement from the start.
    x_out receives n_dof complex values per frequency (column f at f*n_dof).
    The right-hand side is the one assembled from the prescribed values. */
 int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho, const double nu[2],

@@ -642,14 +642,17 @@ extern "C" int mfbem_internal_zexp(int32_t n, const double* z, double* e64, doub
 #include "mfbem_learned.cuh"
 
 // Test hook (not part of the reference interface): C -= A B for complex64
-// column-major A (m x k), B (k x n), C (m x n) with the tcgen05 3xTF32 kernel.
-extern "C" int mfbem_internal_tc_cgemm(int32_t m, int32_t n, int32_t k, const float* A, const float* B, float* C) {
+// column-major A (m x k), B (k x n), C (m x n) with the tcgen05 3xTF32
+// kernels: pre-split tiles + bulk-copy pipeline (staged = 0) or the
+// self-staging kernel (staged = 1).
+extern "C" int mfbem_internal_tc_cgemm(int32_t m, int32_t n, int32_t k, const float* A, const float* B, float* C,
+                                       int32_t staged) {
   g_err.clear();
   if (m <= 0 || n <= 0 || k < 0 || !A || !B || !C) return fail(MFBEM_EARG, "invalid argument");
   int rc;
-  DevBuf dA, dB, dC, dE;
+  DevBuf dA, dB, dC, dE, ws;
   auto cleanup = [&]() {
-    for (DevBuf* b : {&dA, &dB, &dC, &dE})
+    for (DevBuf* b : {&dA, &dB, &dC, &dE, &ws})
       if (b->p) cudaFree(b->p);
   };
   const size_t sa = 8 * (size_t)m * std::max(k, 1), sb = 8 * (size_t)std::max(k, 1) * n, sc = 8 * (size_t)m * n;
@@ -663,10 +666,16 @@ extern "C" int mfbem_internal_tc_cgemm(int32_t m, int32_t n, int32_t k, const fl
   if (e == cudaSuccess) e = cudaMemcpy(dC.p, C, sc, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(dE.p, 0, sizeof(int));
   if (e == cudaSuccess) {
-    dim3 g(nblk(m, TC_BM / 2), nblk(n, TC_BN), 1);
-    k_tc_cgemm<<<g, 128, TC_SMEM>>>((const float2*)dA.p, m, 0, (const float2*)dB.p, std::max(k, 1), 0, (float2*)dC.p,
-                                    m, 0, m, n, k, (int*)dE.p);
-    ++g_launches;
+    if (staged) {
+      dim3 g(nblk(m, TC_BM / 2), nblk(n, TC_BN), 1);
+      k_tc_cgemm<<<g, 128, TC_SMEM>>>((const float2*)dA.p, m, 0, (const float2*)dB.p, std::max(k, 1), 0,
+                                      (float2*)dC.p, m, 0, m, n, k, (int*)dE.p);
+      ++g_launches;
+    } else if ((rc = tc_cgemm_run(0, (const float2*)dA.p, m, 0, (const float2*)dB.p, std::max(k, 1), 0,
+                                  (float2*)dC.p, m, 0, m, n, k, 1, ws, (int*)dE.p))) {
+      cleanup();
+      return rc;
+    }
     e = cudaGetLastError();
   }
   int herr = 0;

@@ -2,23 +2,72 @@
 // mfbem_solve_staela (included into mfbem_abi.cu).
 #pragma once
 
+// The dynamic shared-memory limit is a process-wide attribute of a kernel:
+// raise it once to the device's opt-in maximum (a per-call value would race
+// between concurrent sweeps with different sizes).
+static int raise_smem_limit(const void* f) {
+  static std::mutex mu;
+  static std::vector<const void*> done;
+  std::lock_guard<std::mutex> lk(mu);
+  for (const void* d : done)
+    if (d == f) return 0;
+  int dev = 0, mx = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa;
+  cudaFuncGetAttributes(&fa, f);
+  const int lim = mx - (int)fa.sharedSizeBytes;
+  if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  done.push_back(f);
+  return 0;
+}
+
 // ---------------------------------------------------------------------------
 // GEMM dispatch for the trailing update A22 -= L21 U12 (plain library GEMM)
 // ---------------------------------------------------------------------------
 // Compute type of the single-precision trailing updates of the mixed LU:
-// 0 SIMT FP32, 1 TF32 tensor cores (the factors are then a TF32-accurate
-// preconditioner; refinement in FP64 restores the accuracy and escalates to
-// SIMT FP32 when it stalls), 2 cuBLAS's BF16x9 FP32 emulation. Default TF32;
-// MFBEM_FP32_GEMM=simt|tf32|bf16x9 overrides.
-static thread_local int g_c32_mode = 1;
+// 0 SIMT FP32 (cuBLAS), 1 cuBLAS TF32 tensor cores (TF32-accurate factors;
+// refinement in FP64 restores the accuracy and escalates to SIMT FP32 when it
+// stalls), 2 cuBLAS's BF16x9 FP32 emulation, 3 this library's tcgen05 3xTF32
+// kernels (FP32-accurate factors at tensor-core speed; complex updates only,
+// real ones use SIMT FP32). Default 3; MFBEM_FP32_GEMM=simt|tf32|bf16x9|tc3 overrides.
+static thread_local int g_c32_mode = 3;
 static int c32_default() {
   const char* e = getenv("MFBEM_FP32_GEMM");
-  const std::string v = e ? e : "tf32";
-  return v == "simt" ? 0 : (v == "bf16x9" ? 2 : (v == "tc3" ? 3 : 1));
+  const std::string v = e ? e : "tc3";
+  return v == "simt" ? 0 : (v == "bf16x9" ? 2 : (v == "tf32" ? 1 : 3));
 }
-// mode 3: this library's tcgen05 3xTF32 kernel (mfbem_tc.cuh) for the complex
-// updates; its timeout flag, per host thread
-static thread_local DevBuf g_tc_err;
+// mode 3: this library's tcgen05 3xTF32 kernels (mfbem_tc.cuh) for the complex
+// trailing updates; their timeout flag and pre-split operand tiles, per host thread
+static thread_local DevBuf g_tc_err, g_tc_ws;
+
+// C -= A B (complex64, batched): split A and B into pre-tiled hi / lo TF32
+// words once, then the bulk-copy / tcgen05 pipeline per 128 x 128 tile of C~.
+static int tc_cgemm_run(cudaStream_t st, const float2* A, int lda, long long sA, const float2* B, int ldb,
+                        long long sB, float2* C, int ldc, long long sC, int m, int n, int k, int batch, DevBuf& ws,
+                        int* err) {
+  const int nmt = (m + TC_BM / 2 - 1) / (TC_BM / 2), nnt = (n + TC_BN - 1) / TC_BN, nkc = (k + TQ / 2 - 1) / (TQ / 2);
+  if (nmt == 0 || nnt == 0 || nkc == 0) return 0;
+  const size_t wa = (size_t)batch * nmt * nkc * TQ_TW, wb = (size_t)batch * nnt * nkc * TQ_TW;
+  int rc = ensure(ws, sizeof(uint32_t) * 2 * (wa + wb));
+  if (rc) return rc;
+  if (raise_smem_limit((const void*)k_tc_cgemm_bulk)) return fail(MFBEM_ECUDA, "shared-memory limit of the tcgen05 GEMM");
+  uint32_t* ahi = (uint32_t*)ws.p;
+  uint32_t* alo = ahi + wa;
+  uint32_t* bhi = alo + wa;
+  uint32_t* blo = bhi + wb;
+  k_tc_prep_a<<<(unsigned)std::min<size_t>((wa + 255) / 256, 152 * 32), 256, 0, st>>>(A, lda, sA, m, k, nmt, nkc, batch, ahi, alo);
+  ++g_launches;
+  k_tc_prep_b<<<(unsigned)std::min<size_t>((wb + 255) / 256, 152 * 32), 256, 0, st>>>(B, ldb, sB, k, n, nnt, nkc, batch, bhi, blo);
+  ++g_launches;
+  k_tc_cgemm_bulk<<<dim3(nmt, nnt, batch), 128, TC_SMEM2, st>>>(ahi, alo, bhi, blo, nmt, nnt, nkc, C, ldc, sC, m, n, err);
+  ++g_launches;
+  CK(cudaGetLastError());
+  return 0;
+}
 static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const double* A, int lda, long long sA,
                               const double* B, int ldb, long long sB, double* C, int ldc, long long sC, int batch) {
   const double al = -1.0, be = 1.0;
@@ -46,13 +95,14 @@ static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const floa
                               const float2* B, int ldb, long long sB, float2* C, int ldc, long long sC, int batch) {
   const cuComplex al = make_cuComplex(-1.0f, 0.0f), be = make_cuComplex(1.0f, 0.0f);
   const int mode = g_c32_mode;
-  if (mode == 3 && g_tc_err.p) {
+  if (mode == 3 && g_tc_err.p && k > 32) {
+    // the depth-NBO trailing updates on this library's tcgen05 kernels (the
+    // depth-32 updates inside an outer block stay on SIMT FP32 below)
     cudaStream_t st = nullptr;
     cublasGetStream(hb, &st);
-    dim3 g((unsigned)((m + TC_BM / 2 - 1) / (TC_BM / 2)), (unsigned)((n + TC_BN - 1) / TC_BN), (unsigned)batch);
-    k_tc_cgemm<<<g, 128, TC_SMEM, st>>>(A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, (int*)g_tc_err.p);
-    ++g_launches;
-    return cudaGetLastError() == cudaSuccess ? CUBLAS_STATUS_SUCCESS : CUBLAS_STATUS_EXECUTION_FAILED;
+    return tc_cgemm_run(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch, g_tc_ws, (int*)g_tc_err.p)
+               ? CUBLAS_STATUS_EXECUTION_FAILED
+               : CUBLAS_STATUS_SUCCESS;
   }
   if (mode > 0 && mode < 3)
     return cublasGemmStridedBatchedEx(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, CUDA_C_32F, lda, sA, B, CUDA_C_32F,
@@ -76,29 +126,6 @@ static thread_local DevBuf g_lu_ws;
 // (mutex held until the panel kernel has finished).
 static std::mutex g_coop_mu;
 static thread_local bool g_concurrent = false;
-
-// The dynamic shared-memory limit is a process-wide attribute of a kernel:
-// raise it once to the device's opt-in maximum (a per-call value would race
-// between concurrent sweeps with different sizes).
-static int raise_smem_limit(const void* f) {
-  static std::mutex mu;
-  static std::vector<const void*> done;
-  std::lock_guard<std::mutex> lk(mu);
-  for (const void* d : done)
-    if (d == f) return 0;
-  int dev = 0, mx = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  cudaFuncAttributes fa;
-  cudaFuncGetAttributes(&fa, f);
-  const int lim = mx - (int)fa.sharedSizeBytes;
-  if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess) {
-    cudaGetLastError();
-    return -1;
-  }
-  done.push_back(f);
-  return 0;
-}
 
 // Plan of the cooperative panel for n x n matrices in a batch: G CTAs per
 // matrix (panel rows split in G chunks held in shared memory, at most
@@ -151,7 +178,6 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
   if (tc) {
     int rc = ensure(g_tc_err, sizeof(int));
     if (rc) return rc;
-    if (raise_smem_limit((const void*)k_tc_cgemm)) return fail(MFBEM_ECUDA, "shared-memory limit of the tcgen05 GEMM");
     CK(cudaMemsetAsync(g_tc_err.p, 0, sizeof(int), st));
   }
   CoopPlan pl;
@@ -1071,13 +1097,13 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     };
     if (gm_first) {
       if ((rc = refine_gmres(c, &conv))) return rc;
-      if (!conv && g_c32_mode != 0) {
+      if (!conv && (g_c32_mode == 1 || g_c32_mode == 2)) {
         if ((rc = refactor())) return rc;
         if ((rc = refine_gmres(c, &conv))) return rc;
       }
     } else {
       if ((rc = refine_classical(c, &conv))) return rc;
-      if (!conv && g_c32_mode != 0) {
+      if (!conv && (g_c32_mode == 1 || g_c32_mode == 2)) {
         if ((rc = refactor())) return rc;
         if ((rc = refine_classical(c, &conv))) return rc;
       }

@@ -28,6 +28,7 @@ constexpr int TC_BN = 128;  // columns per CTA
 constexpr int TC_BK = 32;   // real K per chunk (16 complex)
 constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 4;  // one operand tile (16 KB); B tile is TC_BN x TC_BK
 constexpr int TC_SMEM = 4 * TC_TILE_BYTES + 64;    // A hi/lo, B hi/lo, mbarrier, TMEM address
+constexpr int TC_STAGE_BYTES = 4 * TC_TILE_BYTES;  // one pipeline stage: A hi/lo, B hi/lo
 constexpr long long TC_SPIN = 1LL << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -108,38 +109,32 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm(const float2* A, int lda, l
   int phase = 0;
   for (int ch = 0; ch < nchunk && s_ok; ++ch) {
     const int l0 = ch * (TC_BK / 2);
-    // A~ tile: 64 complex rows x 16 complex columns -> 128 x 32 reals
-    for (int e = t; e < 64 * 16; e += 128) {
-      const int ii = e & 63, ll = e >> 6;
-      const int i = i0 + ii, l = l0 + ll;
+    // Staging walks the tiles in shared-memory word order (32 consecutive
+    // words = one 8 x 16 B core matrix), so the stores of a warp are
+    // conflict-free; word w: core matrix w / 32 (8 along K per 8-row group),
+    // row (w % 32) / 4 inside it, K offset w % 4.
+    // A~ tile: 128 rows x 32 K; element (r, kk) comes from a(i0 + r/2, l0 + kk/2)
+    for (int w = t; w < TC_BM * TC_BK; w += 128) {
+      const int cm = w >> 5, r = ((cm >> 3) << 3) + ((w & 31) >> 2), kk = ((cm & 7) << 2) + (w & 3);
+      const int i = i0 + (r >> 1), l = l0 + (kk >> 1);
       float2 a = make_float2(0.0f, 0.0f);
       if (i < m && l < k) a = Ab[(size_t)l * lda + i];
-      const float v[4] = {a.x, a.y, -a.y, a.x};  // (2ii,2ll) (2ii+1,2ll) (2ii,2ll+1) (2ii+1,2ll+1)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int r = 2 * ii + (q & 1), kk = 2 * ll + (q >> 1);
-        const uint32_t hi = f2tf32(v[q]);
-        const uint32_t lo = f2tf32(v[q] - __uint_as_float(hi));
-        const uint32_t o = tc_off(r, kk);
-        *reinterpret_cast<uint32_t*>(Ahi + o) = hi;
-        *reinterpret_cast<uint32_t*>(Alo + o) = lo;
-      }
+      // (r even, kk even) re, (r odd, kk even) im, (r even, kk odd) -im, (r odd, kk odd) re
+      const float v = (kk & 1) ? ((r & 1) ? a.x : -a.y) : ((r & 1) ? a.y : a.x);
+      const uint32_t hi = f2tf32(v), lo = f2tf32(v - __uint_as_float(hi));
+      reinterpret_cast<uint32_t*>(Ahi)[w] = hi;
+      reinterpret_cast<uint32_t*>(Alo)[w] = lo;
     }
-    // B~ tile: 16 complex rows x 128 columns -> K-major (row = column j, k = 2 l + c)
-    for (int e = t; e < 16 * TC_BN; e += 128) {
-      const int ll = e & 15, jj = e >> 4;
-      const int l = l0 + ll, j = j0 + jj;
+    // B~ tile: 128 rows (columns j) x 32 K; element (jj, kk) is component kk&1 of b(l0 + kk/2, j0 + jj)
+    for (int w = t; w < TC_BN * TC_BK; w += 128) {
+      const int cm = w >> 5, jj = ((cm >> 3) << 3) + ((w & 31) >> 2), kk = ((cm & 7) << 2) + (w & 3);
+      const int l = l0 + (kk >> 1), j = j0 + jj;
       float2 b = make_float2(0.0f, 0.0f);
       if (l < k && j < n) b = Bb[(size_t)j * ldb + l];
-      const float v[2] = {b.x, b.y};
-#pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        const uint32_t hi = f2tf32(v[c]);
-        const uint32_t lo = f2tf32(v[c] - __uint_as_float(hi));
-        const uint32_t o = tc_off(jj, 2 * ll + c);
-        *reinterpret_cast<uint32_t*>(Bhi + o) = hi;
-        *reinterpret_cast<uint32_t*>(Blo + o) = lo;
-      }
+      const float v = (kk & 1) ? b.y : b.x;
+      const uint32_t hi = f2tf32(v), lo = f2tf32(v - __uint_as_float(hi));
+      reinterpret_cast<uint32_t*>(Bhi)[w] = hi;
+      reinterpret_cast<uint32_t*>(Blo)[w] = lo;
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
@@ -193,17 +188,246 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm(const float2* A, int lda, l
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       if (i < m) {
+        // all loads first, then the stores (a load / store pair per element
+        // would serialise 32 global round trips)
         float* cr = reinterpret_cast<float*>(Cb);
+        float cv[32];
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
           const int j = j0 + c0 + q;
-          if (j < n) cr[2 * ((size_t)j * ldc + i) + comp] -= __uint_as_float(v[q]);
+          cv[q] = j < n ? cr[2 * ((size_t)j * ldc + i) + comp] : 0.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          const int j = j0 + c0 + q;
+          if (j < n) cr[2 * ((size_t)j * ldc + i) + comp] = cv[q] - __uint_as_float(v[q]);
         }
       }
     }
   } else if (!s_ok && threadIdx.x == 0) {
     // give in-flight MMAs a bounded chance to finish before the TMEM is freed
     tc_wait(mb, (uint32_t)phase);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Pre-split operands + bulk-copy pipeline. The staging above converts every
+// element in every CTA that uses it; the LU's trailing update reuses the same
+// L panel (A) and U block (B) across all tiles, so they are split into
+// hi / lo TF32 once per update and written pre-tiled in the exact shared-
+// memory word order (one 16 KB tile per (row tile, K chunk) / (column tile,
+// K chunk)); the GEMM kernel then only streams tiles with cp.async.bulk into
+// two stages (mbarrier expect-tx) while the tensor cores work on the other.
+// ---------------------------------------------------------------------------
+// Tiles of the pipelined kernel: K chunk of TQ real K (16): 128 x 16 words,
+// core matrices 128 B apart along K and TQ / 4 * 128 B apart along rows.
+constexpr int TQ = 16;
+constexpr int TQ_TW = TC_BM * TQ;                  // words per tile (2048)
+constexpr int TQ_TILE_BYTES = TQ_TW * 4;           // 8 KB
+constexpr int TQ_STAGE_BYTES = 4 * TQ_TILE_BYTES;  // A hi/lo, B hi/lo
+constexpr int TQ_SBO = TQ / 4 * 128;               // 512 B
+constexpr int TC_SMEM2 = 2 * TQ_STAGE_BYTES + 64;
+
+__device__ __forceinline__ uint64_t tq_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)(128 >> 4) << 16;
+  d |= (uint64_t)(TQ_SBO >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+// word w of a tile <-> element (row, k): core matrix w / 32 (TQ/4 along K per
+// 8-row group), row (w % 32) / 4 inside it, K offset w % 4
+__device__ __forceinline__ void tq_rk(int w, int& r, int& kk) {
+  const int cm = w >> 5;
+  r = (cm / (TQ / 4)) * 8 + ((w & 31) >> 2);
+  kk = (cm % (TQ / 4)) * 4 + (w & 3);
+}
+
+// A~ tiles: [batch][row tile][K chunk][word]
+__global__ void k_tc_prep_a(const float2* A, int lda, long long sA, int m, int k, int nmt, int nkc, int batch,
+                            uint32_t* hi, uint32_t* lo) {
+  const long long total = (long long)batch * nmt * nkc * TQ_TW;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+    const int w = (int)(g % TQ_TW);
+    long long tl = g / TQ_TW;
+    const int kc = (int)(tl % nkc);
+    tl /= nkc;
+    const int mt = (int)(tl % nmt);
+    const int b = (int)(tl / nmt);
+    int r, kk;
+    tq_rk(w, r, kk);
+    const int i = mt * (TC_BM / 2) + (r >> 1), l = kc * (TQ / 2) + (kk >> 1);
+    float2 a = make_float2(0.0f, 0.0f);
+    if (i < m && l < k) a = A[sA * b + (size_t)l * lda + i];
+    const float v = (kk & 1) ? ((r & 1) ? a.x : -a.y) : ((r & 1) ? a.y : a.x);
+    const uint32_t h = f2tf32(v);
+    hi[g] = h;
+    lo[g] = f2tf32(v - __uint_as_float(h));
+  }
+}
+// B~ tiles: [batch][column tile][K chunk][word]; element (jj, kk) is component kk&1 of b(l, j)
+__global__ void k_tc_prep_b(const float2* B, int ldb, long long sB, int k, int n, int nnt, int nkc, int batch,
+                            uint32_t* hi, uint32_t* lo) {
+  const long long total = (long long)batch * nnt * nkc * TQ_TW;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+    const int w = (int)(g % TQ_TW);
+    long long tl = g / TQ_TW;
+    const int kc = (int)(tl % nkc);
+    tl /= nkc;
+    const int nt = (int)(tl % nnt);
+    const int b = (int)(tl / nnt);
+    int jj, kk;
+    tq_rk(w, jj, kk);
+    const int j = nt * TC_BN + jj, l = kc * (TQ / 2) + (kk >> 1);
+    float2 bv = make_float2(0.0f, 0.0f);
+    if (l < k && j < n) bv = B[sB * b + (size_t)j * ldb + l];
+    const float v = (kk & 1) ? bv.y : bv.x;
+    const uint32_t h = f2tf32(v);
+    hi[g] = h;
+    lo[g] = f2tf32(v - __uint_as_float(h));
+  }
+}
+
+__device__ __forceinline__ void tc_bulk(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_expect(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+// C -= A B from pre-split tiles: CTA (row tile, column tile, batch); thread 0
+// runs the copy / MMA pipeline (stage s: 4 x 8 KB tiles, "full" barrier fb[s]
+// completed by the bulk copies, "free" barrier mb[s] by the MMA commit), all
+// four warps run the epilogue; 64 KB of shared memory, so three CTAs share an
+// SM and one's epilogue overlaps another's MMAs.
+__global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, const uint32_t* Alo,
+                                                          const uint32_t* Bhi, const uint32_t* Blo, int nmt, int nnt,
+                                                          int nkc, float2* C, int ldc, long long sC, int m, int n,
+                                                          int* err) {
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tsm + 2 * TQ_STAGE_BYTES);  // fb[2], mb[2]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + 2 * TQ_STAGE_BYTES + 32);
+  __shared__ int s_ok;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int mt = blockIdx.x, nt = blockIdx.y, bz = blockIdx.z;
+  const size_t ta0 = ((size_t)bz * nmt + mt) * nkc * TQ_TW;  // first A tile of this row tile
+  const size_t tb0 = ((size_t)bz * nnt + nt) * nkc * TQ_TW;
+  const uint32_t fb[2] = {smem_u32(bars), smem_u32(bars + 1)}, mb[2] = {smem_u32(bars + 2), smem_u32(bars + 3)};
+  const uint32_t st0 = smem_u32(tsm);
+  if (t == 0) {
+    for (int q = 0; q < 2; ++q) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fb[q]) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb[q]) : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_ok = 1;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(TC_BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc_idesc(TC_BM, TC_BN);
+  int issued = 0;  // chunks whose MMAs were issued
+  if (t == 0) {
+    auto load = [&](int kc, int sidx) {
+      const uint32_t d = st0 + sidx * TQ_STAGE_BYTES;
+      tc_expect(fb[sidx], (uint32_t)TQ_STAGE_BYTES);
+      tc_bulk(d, Ahi + ta0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
+      tc_bulk(d + TQ_TILE_BYTES, Alo + ta0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
+      tc_bulk(d + 2 * TQ_TILE_BYTES, Bhi + tb0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
+      tc_bulk(d + 3 * TQ_TILE_BYTES, Blo + tb0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
+    };
+    bool ok = true;
+    if (nkc > 0) load(0, 0);
+    for (int kc = 0; kc < nkc && ok; ++kc) {
+      const int s = kc & 1;
+      if (kc + 1 < nkc) {
+        // stage s^1 was read by the MMAs of chunk kc - 1
+        if (kc >= 1 && !tc_wait(mb[s ^ 1], (uint32_t)(((kc - 1) >> 1) & 1))) { ok = false; break; }
+        load(kc + 1, s ^ 1);
+      }
+      if (!tc_wait(fb[s], (uint32_t)((kc >> 1) & 1))) { ok = false; break; }
+      const uint32_t ah = st0 + s * TQ_STAGE_BYTES, al = ah + TQ_TILE_BYTES, bh = ah + 2 * TQ_TILE_BYTES,
+                     bl = ah + 3 * TQ_TILE_BYTES;
+#pragma unroll
+      for (int ks = 0; ks < TQ / 8; ++ks) {
+        const uint32_t ko = ks * 256;  // 8 tf32 = two core matrices along K
+        const uint64_t dah = tq_desc(ah + ko), dal = tq_desc(al + ko), dbh = tq_desc(bh + ko), dbl = tq_desc(bl + ko);
+        const uint32_t acc0 = (kc > 0 || ks > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                tmem),
+            "l"(dah), "l"(dbh), "r"(idesc), "r"(acc0)
+            : "memory");
+        asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(tmem), "l"(dah), "l"(dbl),
+                     "r"(idesc)
+                     : "memory");
+        asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(tmem), "l"(dal), "l"(dbh),
+                     "r"(idesc)
+                     : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb[s])
+                   : "memory");
+      issued = kc + 1;
+    }
+    // the last commit covers every earlier MMA
+    if (ok && issued > 0 && !tc_wait(mb[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1))) ok = false;
+    if (!ok) {
+      atomicExch(err, 1);
+      s_ok = 0;
+      // bounded chance for the copies and MMAs in flight before the TMEM is freed
+      if (issued > 0) tc_wait(mb[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1));
+    }
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (s_ok && nkc > 0) {
+    const int r = 32 * warp + lane;
+    const int i = mt * (TC_BM / 2) + (r >> 1), comp = r & 1;
+    float2* Cb = C + sC * bz;
+    for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+      uint32_t v[32];
+      const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+          "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+            "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+            "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+          : "r"(ta)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (i < m) {
+        // all loads first, then the stores (a load / store pair per element
+        // would serialise 32 global round trips)
+        float* cr = reinterpret_cast<float*>(Cb);
+        float cv[32];
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          const int j = nt * TC_BN + c0 + q;
+          cv[q] = j < n ? cr[2 * ((size_t)j * ldc + i) + comp] : 0.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          const int j = nt * TC_BN + c0 + q;
+          if (j < n) cr[2 * ((size_t)j * ldc + i) + comp] = cv[q] - __uint_as_float(v[q]);
+        }
+      }
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
