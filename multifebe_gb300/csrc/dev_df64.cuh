@@ -66,6 +66,40 @@ __device__ __forceinline__ cf cf_fma(cf a, cf b, cf c) { return cf_add(cf_mul(a,
 // c + a * s, s real
 __device__ __forceinline__ cf cf_fma_r(cf a, ff s, cf c) { return cf{ff_fma(a.re, s, c.re), ff_fma(a.im, s, c.im)}; }
 
+// Accumulators for long sums of products: (hi, lo) kept unnormalised, each
+// product's rounding error (Dekker's exact product) and the addition's error
+// (Knuth's TwoSum) gathered in lo -- the compensated dot product of Ogita,
+// Rump and Oishi (SIAM J. Sci. Comput. 26(6), 2005) with double-float inputs;
+// 12 operations per real multiply-add instead of 17. Normalise before use.
+__device__ __forceinline__ void acc_mac(ff& acc, ff a, ff b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const float s = __fadd_rn(acc.hi, p);
+  const float bp = __fsub_rn(s, acc.hi);
+  const float t = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+  acc.hi = s;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(t, e));
+}
+// acc += a * b (complex)
+__device__ __forceinline__ void acc_cmac(cf& acc, cf a, cf b) {
+  acc_mac(acc.re, a.re, b.re);
+  acc_mac(acc.re, ff_neg(a.im), b.im);
+  acc_mac(acc.im, a.re, b.im);
+  acc_mac(acc.im, a.im, b.re);
+}
+// acc += a * s (s real)
+__device__ __forceinline__ void acc_cmac_r(cf& acc, cf a, ff s) {
+  acc_mac(acc.re, a.re, s);
+  acc_mac(acc.im, a.im, s);
+}
+__device__ __forceinline__ ff ff_norm(ff a) {
+  const float h = __fadd_rn(a.hi, a.lo);
+  return ff{h, __fsub_rn(a.lo, __fsub_rn(h, a.hi))};
+}
+__device__ __forceinline__ cf cf_norm(cf a) { return cf{ff_norm(a.re), ff_norm(a.im)}; }
+
 }  // namespace mfb
 
 namespace mfb {

@@ -575,7 +575,8 @@ struct HarParF {
   cf k1, k2, cte_u, cte_t;
   cf c0[5], c1[5];
   cf cm[2][4][5];
-  float t2[16];  // E_n series-length steps on |z|^2 (ZexpSteps as binary32)
+  unsigned nz[2][4];  // bit t set: cm[w][n][t] is not structurally zero
+  float t2[16];       // E_n series-length steps on |z|^2 (ZexpSteps as binary32)
 };
 __global__ void k_harpar_f(const HarParD* p, HarParF* out, int nf) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -601,11 +602,15 @@ __global__ void k_harpar_f(const HarParD* p, HarParF* out, int nf) {
                         {c(P.psi[3]), c(P.chi[3]), c(P.T1[5]), c(P.T2[4]), c(P.T3[4])},
                         {c(P.psi[5]), c(P.chi[5]), c(P.T1[7]), c(P.T2[6]), c(P.T3[6])},
                         {Z, Z, c(P.T1[9]), c(P.T2[8]), c(P.T3[8])}};
-  for (int n = 0; n < 4; ++n)
+  for (int n = 0; n < 4; ++n) {
+    o.nz[0][n] = o.nz[1][n] = 0u;
     for (int t = 0; t < 5; ++t) {
       o.cm[0][n][t] = k1t[n][t];
       o.cm[1][n][t] = k2t[n][t];
+      if (k1t[n][t].re.hi != 0.0f || k1t[n][t].im.hi != 0.0f) o.nz[0][n] |= 1u << t;
+      if (k2t[n][t].re.hi != 0.0f || k2t[n][t].im.hi != 0.0f) o.nz[1][n] |= 1u << t;
     }
+  }
   for (int i = 0; i < 16; ++i) o.t2[i] = (float)P.steps.t2[i];
   out[f] = o;
 }
@@ -681,12 +686,14 @@ __device__ __forceinline__ void harela_point_ff(const HarParF& q, const ff rv[3]
 #pragma unroll 1
     for (int nn = 0; nn < 4; ++nn) {
       const cf src = cf_scale(sel4(e2, e3, e4, e5, nn), rp);
+      const unsigned nzm = q.nz[w][nn];
 #pragma unroll
-      for (int t = 0; t < 5; ++t) X[t] = cf_fma(q.cm[w][nn][t], src, X[t]);
+      for (int t = 0; t < 5; ++t)
+        if (nzm & (1u << t)) acc_cmac(X[t], q.cm[w][nn][t], src);
       rp = ff_mul(rp, d1r1);
     }
   }
-  const cf psi = X[0], chi = X[1], T1 = X[2], T2 = X[3], T3 = X[4];
+  const cf psi = cf_norm(X[0]), chi = cf_norm(X[1]), T1 = cf_norm(X[2]), T2 = cf_norm(X[3]), T3 = cf_norm(X[4]);
   const ff dr[3] = {ff_mul(rv[0], d1r1), ff_mul(rv[1], d1r1), ff_mul(rv[2], d1r1)};
   const ff drdn = ff_add(ff_add(ff_mul(dr[0], n[0]), ff_mul(dr[1], n[1])), ff_mul(dr[2], n[2]));
 #pragma unroll 1
@@ -746,7 +753,7 @@ __device__ __forceinline__ void flush_pair_ff(const DMesh& m, const HarParF& q, 
   for (int j = 0; j < kAcc; ++j) {
     const int o = lane + 32 * j;
     if (o >= kOut) break;
-    cf aj = sel4(acc[0], acc[1], acc[2], acc[3], j);
+    cf aj = cf_norm(sel4(acc[0], acc[1], acc[2], acc[3], j));
     if (o < 72) {
       const int kn = o / 9, il = (o % 9) / 3, ik = o % 3;
       if (hp) aj = cf_add(aj, cf_scale(q.c0[3], ff_mul(hp[9 + kn], hp[3 * il + ik])));
@@ -790,12 +797,14 @@ __device__ __forceinline__ void harela_point_sing_ff(const HarParF& q, const ff 
 #pragma unroll 1
     for (int nn = 0; nn < 4; ++nn) {
       const cf src = cf_scale(sel4(e2, e3, e4, e5, nn), rp);
+      const unsigned nzm = q.nz[w][nn];
 #pragma unroll
-      for (int t = 0; t < 5; ++t) X[t] = cf_fma(q.cm[w][nn][t], src, X[t]);
+      for (int t = 0; t < 5; ++t)
+        if (nzm & (1u << t)) acc_cmac(X[t], q.cm[w][nn][t], src);
       rp = ff_mul(rp, d1r1);
     }
   }
-  const cf psi = X[0], chi = X[1], T1 = X[2], T2 = X[3], T3 = X[4];
+  const cf psi = cf_norm(X[0]), chi = cf_norm(X[1]), T1 = cf_norm(X[2]), T2 = cf_norm(X[3]), T3 = cf_norm(X[4]);
   const cf c2 = cf_scale(q.c0[3], d1r2);
   const cf T2f = cf_add(T2, c2);
   const ff dr[3] = {ff_mul(rv[0], d1r1), ff_mul(rv[1], d1r1), ff_mul(rv[2], d1r1)};
