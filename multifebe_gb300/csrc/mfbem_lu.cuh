@@ -12,6 +12,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "dev_complex.cuh"
+#include <cooperative_groups.h>
 
 namespace mfb {
 
@@ -370,6 +371,119 @@ __global__ void __launch_bounds__(NT) k_panel_coop(S* A, long long strideA, int 
     const int c = t / nr, i = t - c * nr;
     M[(size_t)(k + c) * lda + r0 + i] = pan[(size_t)c * chunk + i];
   }
+}
+
+// ---------------------------------------------------------------------------
+// Cluster panel: the same algorithm as k_panel_coop with the G CTAs of a
+// matrix forming one thread-block cluster (cluster rank = row chunk): the
+// per-column exchange goes through distributed shared memory and the
+// hardware cluster barrier instead of global memory and a spin on a counter.
+// Candidate slots are double-buffered by column parity, so one cluster
+// barrier per column suffices: a slot written at column j + 2 is read by
+// everyone before the barrier of column j + 1.
+// ---------------------------------------------------------------------------
+template <typename S, int NT>
+__global__ void __launch_bounds__(NT) k_panel_cluster(S* A, long long strideA, int lda, int n, int k, int kb,
+                                                      int chunk, int* ipiv, int* info) {
+  namespace cg = cooperative_groups;
+  typedef typename Sc<S>::R R;
+  cg::cluster_group cl = cg::this_cluster();
+  const int G = (int)cl.num_blocks(), g = (int)cl.block_rank();
+  extern __shared__ __align__(16) unsigned char smraw[];
+  S* pan = reinterpret_cast<S*>(smraw);  // [kb][chunk]
+  S* prow = pan + (size_t)kb * chunk;     // [kb] pivot row
+  S* xrow = prow + 32;                    // [2][2][32]: slot parity x {candidate row, row jj}
+  R* xval = reinterpret_cast<R*>(xrow + 2 * 2 * 32);  // [2]
+  int* xidx = reinterpret_cast<int*>(xval + 2);        // [2]
+  __shared__ R sv[NT / 32];
+  __shared__ int si[NT / 32];
+  __shared__ int s_p, s_g, s_own;
+  const int mat = blockIdx.x / G;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x / 32;
+  S* M = A + strideA * mat;
+  int* piv = ipiv + (size_t)n * mat;
+  const int r0 = k + g * chunk, r1 = min(n, r0 + chunk), nr = max(0, r1 - r0);
+  for (int t = threadIdx.x; t < kb * nr; t += NT) {
+    const int c = t / nr, i = t - c * nr;
+    pan[(size_t)c * chunk + i] = M[(size_t)(k + c) * lda + r0 + i];
+  }
+  __syncthreads();
+  for (int j = 0; j < kb; ++j) {
+    const int jj = k + j, slot = j & 1;
+    R best = -1;
+    int bi = -1;
+    for (int i = max(jj, r0) - r0 + threadIdx.x; i < nr; i += NT) {
+      const R v = Sc<S>::abs1(pan[(size_t)j * chunk + i]);
+      if (v > best) { best = v; bi = r0 + i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi >= 0 && (bi < 0 || oi < bi))) { best = ov; bi = oi; }
+    }
+    if (lane == 0) { sv[wid] = best; si[wid] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      R b_ = sv[0];
+      int i_ = si[0];
+      for (int w = 1; w < NT / 32; ++w)
+        if (sv[w] > b_ || (sv[w] == b_ && si[w] >= 0 && (i_ < 0 || si[w] < i_))) { b_ = sv[w]; i_ = si[w]; }
+      xval[slot] = b_;
+      xidx[slot] = i_;
+      s_p = i_;
+    }
+    __syncthreads();
+    const int myc = s_p;
+    if ((int)threadIdx.x < kb) {
+      if (myc >= 0) xrow[(slot * 2 + 0) * 32 + threadIdx.x] = pan[(size_t)threadIdx.x * chunk + (myc - r0)];
+      if (jj >= r0 && jj < r1) xrow[(slot * 2 + 1) * 32 + threadIdx.x] = pan[(size_t)threadIdx.x * chunk + (jj - r0)];
+    }
+    cl.sync();
+    // winner over the cluster's candidates (distributed shared memory)
+    if (threadIdx.x == 0) {
+      R b_ = -1;
+      int i_ = -1, g_ = 0;
+      for (int q = 0; q < G; ++q) {
+        const R v = cl.map_shared_rank(xval, q)[slot];
+        const int ix = cl.map_shared_rank(xidx, q)[slot];
+        if (ix >= 0 && (v > b_ || (v == b_ && ix < i_))) { b_ = v; i_ = ix; g_ = q; }
+      }
+      s_p = i_;
+      s_g = g_;
+      s_own = (jj - k) / chunk;  // rank owning row jj
+    }
+    __syncthreads();
+    const int p = s_p;
+    if ((int)threadIdx.x < kb) prow[threadIdx.x] = cl.map_shared_rank(xrow, s_g)[(slot * 2 + 0) * 32 + threadIdx.x];
+    __syncthreads();
+    if (g == 0 && threadIdx.x == 0) {
+      piv[jj] = p + 1;
+      if (Sc<S>::iszero(prow[j]) && info[mat] == 0) info[mat] = jj + 1;
+    }
+    if (p != jj) {
+      if (p >= r0 && p < r1 && (int)threadIdx.x < kb)
+        pan[(size_t)threadIdx.x * chunk + (p - r0)] = cl.map_shared_rank(xrow, s_own)[(slot * 2 + 1) * 32 + threadIdx.x];
+      if (jj >= r0 && jj < r1 && (int)threadIdx.x < kb) pan[(size_t)threadIdx.x * chunk + (jj - r0)] = prow[threadIdx.x];
+    }
+    __syncthreads();
+    const S dj = prow[j];
+    if (!Sc<S>::iszero(dj)) {
+      const S rcp = Sc<S>::rcp(dj);
+      for (int i = max(jj + 1, r0) - r0 + threadIdx.x; i < nr; i += NT) {
+        const S l = Sc<S>::mul(pan[(size_t)j * chunk + i], rcp);
+        pan[(size_t)j * chunk + i] = l;
+        for (int c = j + 1; c < kb; ++c)
+          pan[(size_t)c * chunk + i] = Sc<S>::sub(pan[(size_t)c * chunk + i], Sc<S>::mul(l, prow[c]));
+      }
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < kb * nr; t += NT) {
+    const int c = t / nr, i = t - c * nr;
+    M[(size_t)(k + c) * lda + r0 + i] = pan[(size_t)c * chunk + i];
+  }
+  // no CTA may exit while others can still read its shared memory
+  cl.sync();
 }
 
 // Apply the panel interchanges (rows k..k+nb-1 with ipiv) to the columns

@@ -180,8 +180,34 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
     if (rc) return rc;
     CK(cudaMemsetAsync(g_tc_err.p, 0, sizeof(int), st));
   }
+  // cluster panel: 8 CTAs per matrix in a thread-block cluster when a matrix's
+  // panel rows fit their shared memory (about 200 KB each)
+  constexpr int GC = 8;
+  auto cl_smem = [&](int rows) {
+    const int ch = (rows + GC - 1) / GC;
+    return ((size_t)nb * ch + 32 + 4 * 32) * sizeof(S) + 2 * sizeof(R) + 2 * sizeof(int) + 16;
+  };
+  bool use_cl = cl_smem(n) <= 200 * 1024 && !raise_smem_limit((const void*)k_panel_cluster<S, 256>);
+  if (use_cl) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = GC;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(GC * batch);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = cl_smem(n);
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, (void*)k_panel_cluster<S, 256>, &cfg) != cudaSuccess || ncl < 1) {
+      cudaGetLastError();
+      use_cl = false;
+    }
+  }
   CoopPlan pl;
-  const bool coop = coop_plan<S>(n, nb, batch, &pl);
+  const bool coop = !use_cl && coop_plan<S>(n, nb, batch, &pl);
   unsigned* ctr = nullptr;
   S* xrow = nullptr;
   R* xval = nullptr;
@@ -215,7 +241,23 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
     const int KE = std::min(n, K + NBO);
     for (int k = K; k < KE; k += nb) {
       const int kb = std::min(nb, KE - k);
-      if (coop) {
+      if (use_cl) {
+        const int chunk = (n - k + GC - 1) / GC;
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = GC;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(GC * batch);
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = cl_smem(n - k);
+        cfg.stream = st;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        CK(cudaLaunchKernelEx(&cfg, k_panel_cluster<S, 256>, A, sA, lda, n, k, kb, chunk, ipiv, info));
+        ++g_launches;
+      } else if (coop) {
         const int chunk = (n - k + pl.G - 1) / pl.G;
         for (int b0 = 0; b0 < batch; b0 += pl.group) {
           const int nbm = std::min(pl.group, batch - b0);
