@@ -126,18 +126,35 @@ int mfbem_assemble_staela(mfbem_handle* h, double mu, double nu, double* A, int3
 int mfbem_assemble_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
                           const double nu[2], double omega, double* A, int32_t lda, double* b, int32_t flags);
 
-/* solve_lse_r / solve_lse_c: LU with partial pivoting (getrf) and the
-   triangular solves (getrs) for n_rhs right-hand sides, in FP64 on the GPU.
-   On return A holds the LU factors and ipiv the 1-based pivots, exactly as
-   LAPACK leaves them, so a later call with factorize = 0 reuses them.
-   scaling / condition / refine must be 0 (the reference defaults,
-   src/read_settings.f90); other values return MFBEM_EUNSUPPORTED. */
+/* solve_lse_r / solve_lse_c with LAPACK semantics, on the GPU in FP64, every
+   option of the reference:
+     scaling    (factorize) ?geequ + ?laqge: A equilibrated in place, r and c
+                receive the row / column factors and *equed 'N', 'R', 'C' or
+                'B'; (no factorize) equed, r and c from an earlier call are used.
+                b is scaled by r before the solve (equed R/B), x by c after
+                it (equed C/B). A zero row i / column j of A returns i / n + j.
+     factorize  getrf: on return A holds the LU factors and ipiv the 1-based
+                pivots, exactly as LAPACK leaves them; 0 reuses them.
+     condition  (factorize) ?gecon: reciprocal one-norm condition estimate of
+                the (scaled) matrix, read with mfbem_solve_report.
+     refine     ?gerfs: at most five refinement steps with the residual of
+                the unfactorised matrix; ferr / berr read with
+                mfbem_solve_report.
+   With condition or refine, aodim must be n and Ao (n x n) receives the
+   unfactorised (scaled) matrix when factorize is set; a later call with
+   factorize = 0 and refine reads it back, as src/solve_lse_r.f90:70-78,
+   199-206 do. A singular matrix returns info > 0 (zero pivot U(info,info)). */
 int mfbem_solve_r(int32_t n, double* A, int32_t* ipiv, int32_t aodim, double* Ao, char* equed, double* r,
                   double* c, int32_t n_rhs, double* b, int32_t factorize, int32_t scaling, int32_t condition,
                   int32_t refine);
 int mfbem_solve_c(int32_t n, double* A, int32_t* ipiv, int32_t aodim, double* Ao, char* equed, double* r,
                   double* c, int32_t n_rhs, double* b, int32_t factorize, int32_t scaling, int32_t condition,
                   int32_t refine);
+/* Diagnostics of the last mfbem_solve_r / mfbem_solve_c on the calling
+   thread, which the reference prints at verbose level 2: rcond (NaN unless
+   condition was set with factorize) and per right-hand side the forward-error
+   bound ferr and the componentwise backward error berr (NaN unless refine). */
+int mfbem_solve_report(double* rcond, int32_t n_rhs, double* ferr, double* berr);
 
 /* Harmonic sweep on the device: for each of n_freq frequencies, assemble the
    FP64 system (same integration as mfbem_assemble_harela), factorise and solve.

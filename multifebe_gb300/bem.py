@@ -33,7 +33,7 @@ PRECISION = {"plain": 0, "mixed": 1, "mixed-gmres": 2}
 
 
 def _p(a, t=_dp):
-    return a.ctypes.data_as(t)
+    return None if a is None else a.ctypes.data_as(t)
 
 
 class BemRegion:
@@ -179,9 +179,27 @@ class BemRegion:
         return u, t
 
 
-def solve_lse(A, b, ipiv=None, factorize=True):
+class LseState:
+    """The caller-owned arrays solve_lse_{r,c} keep between calls (Ao, equed,
+    r, c: src/problem_variables.f90 Ao_r/Ao_c, scal_equed, scal_r, scal_c)
+    and the diagnostics the reference prints (rcond, ferr, berr)."""
+
+    def __init__(self):
+        self.Ao = None
+        self.equed = "N"
+        self.r = None
+        self.c = None
+        self.rcond = float("nan")
+        self.ferr = None
+        self.berr = None
+
+
+def solve_lse(A, b, ipiv=None, factorize=True, scaling=False, condition=False, refine=False, state=None):
     """solve_lse_r / solve_lse_c with LAPACK semantics: A (Fortran order) is
-    overwritten by its LU factors, ipiv by the 1-based pivots, b by x."""
+    overwritten by its (equilibrated) LU factors, ipiv by the 1-based pivots,
+    b by x. scaling / condition / refine are the reference's lse_scaling,
+    lse_condition and lse_refine; their arrays live in `state` (an LseState),
+    which a later call with factorize=False must be given again."""
     L = _abi.load()
     n = A.shape[0]
     assert A.flags.f_contiguous
@@ -190,9 +208,34 @@ def solve_lse(A, b, ipiv=None, factorize=True):
     bb = b if b.ndim == 2 else b.reshape(n, 1)
     nrhs = bb.shape[1]
     assert bb.flags.f_contiguous
+    if (scaling or condition or refine) and state is None:
+        raise ValueError("scaling / condition / refine need an LseState")
+    st = state
+    Ao = eq = r = c = None
+    aodim = 1
+    if condition or refine:
+        if st.Ao is None or st.Ao.shape != A.shape or st.Ao.dtype != A.dtype:
+            if not factorize:
+                raise ValueError("refine without factorize needs the state of the factorising call")
+            st.Ao = np.zeros_like(A, order="F")
+        Ao, aodim = st.Ao, n
+    if scaling:
+        if st.r is None or st.r.shape != (n,):
+            st.r, st.c = np.zeros(n), np.zeros(n)
+        eq = ctypes.create_string_buffer(st.equed.encode(), 2)
+        r, c = st.r, st.c
     fn = L.mfbem_solve_c if np.iscomplexobj(A) else L.mfbem_solve_r
-    rc = fn(n, _p(A), _p(ipiv, _ip), 1, None, None, None, None, nrhs, _p(bb), 1 if factorize else 0, 0, 0, 0)
+    rc = fn(n, _p(A), _p(ipiv, _ip), aodim, _p(Ao), eq, _p(r), _p(c), nrhs, _p(bb), 1 if factorize else 0,
+            int(bool(scaling)), int(bool(condition)), int(bool(refine)))
     check(rc)
+    if st is not None:
+        if scaling:
+            st.equed = eq.value.decode()
+        rcond = ctypes.c_double()
+        fe, be = np.zeros(nrhs), np.zeros(nrhs)
+        check(L.mfbem_solve_report(ctypes.byref(rcond), nrhs, _p(fe), _p(be)))
+        st.rcond = rcond.value
+        st.ferr, st.berr = (fe, be) if refine else (None, None)
     return b, ipiv
 
 

@@ -29,6 +29,9 @@ template <> struct Sc<double> {
   __device__ static double div(double a, double b) { return a / b; }
   __device__ static double rcp(double a) { return 1.0 / a; }
   __device__ static bool iszero(double a) { return a == 0.0; }
+  __device__ static double conj(double a) { return a; }
+  __device__ static double from(double v) { return v; }
+  __device__ static double re(double a) { return a; }
 };
 template <> struct Sc<float> {
   typedef float R;
@@ -41,6 +44,9 @@ template <> struct Sc<float> {
   __device__ static float div(float a, float b) { return a / b; }
   __device__ static float rcp(float a) { return 1.0f / a; }
   __device__ static bool iszero(float a) { return a == 0.0f; }
+  __device__ static float conj(float a) { return a; }
+  __device__ static float from(double v) { return (float)v; }
+  __device__ static float re(float a) { return a; }
 };
 template <> struct Sc<double2> {
   typedef double R;
@@ -57,6 +63,9 @@ template <> struct Sc<double2> {
   }
   __device__ static double2 rcp(double2 a) { return div(one(), a); }
   __device__ static bool iszero(double2 a) { return a.x == 0.0 && a.y == 0.0; }
+  __device__ static double2 conj(double2 a) { return make_double2(a.x, -a.y); }
+  __device__ static double2 from(double v) { return make_double2(v, 0.0); }
+  __device__ static double re(double2 a) { return a.x; }
 };
 template <> struct Sc<float2> {
   typedef float R;
@@ -76,6 +85,9 @@ template <> struct Sc<float2> {
   }
   __device__ static float2 rcp(float2 a) { return div(one(), a); }
   __device__ static bool iszero(float2 a) { return a.x == 0.f && a.y == 0.f; }
+  __device__ static float2 conj(float2 a) { return make_float2(a.x, -a.y); }
+  __device__ static float2 from(double v) { return make_float2((float)v, 0.f); }
+  __device__ static float re(float2 a) { return a.x; }
 };
 
 // ---------------------------------------------------------------------------

@@ -483,79 +483,6 @@ static int getrs_batched(cudaStream_t st, const S* A, long long sA, int lda, int
   return 0;
 }
 
-// ---------------------------------------------------------------------------
-// mfbem_solve_{r,c}: LAPACK-semantics drop-in (host arrays in and out)
-// ---------------------------------------------------------------------------
-struct SolveCtx {
-  cudaStream_t st = nullptr;
-  cublasHandle_t hb = nullptr;
-  DevBuf A, b, ipiv, info;
-};
-static SolveCtx* g_solve = nullptr;
-static int solve_ctx(SolveCtx** out) {
-  if (!g_solve) {
-    int nd = 0;
-    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) return fail(MFBEM_ECUDA, "no CUDA device");
-    int rc = init_tables();
-    if (rc) return rc;
-    SolveCtx* c = new SolveCtx();
-    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
-    if (cublasCreate(&c->hb) != CUBLAS_STATUS_SUCCESS) return fail(MFBEM_ECUDA, "cublasCreate");
-    cublasSetStream(c->hb, c->st);
-    g_solve = c;
-  }
-  *out = g_solve;
-  return 0;
-}
-
-template <typename S>
-static int solve_dropin(int32_t n, double* A, int32_t* ipiv, int32_t n_rhs, double* b, int32_t factorize,
-                        int32_t scaling, int32_t condition, int32_t refine) {
-  g_err.clear();
-  if (n <= 0 || !A || !ipiv || !b || n_rhs < 0) return fail(MFBEM_EARG, "invalid argument");
-  if (scaling || condition || refine)
-    return fail(MFBEM_EUNSUPPORTED, "lse_scaling / lse_condition / lse_refine are not supported by this path");
-  SolveCtx* c;
-  int rc = solve_ctx(&c);
-  if (rc) return rc;
-  const size_t es = sizeof(S);
-  if ((rc = ensure(c->A, (size_t)n * n * es)) || (rc = ensure(c->b, (size_t)n * std::max(1, n_rhs) * es)) ||
-      (rc = ensure(c->ipiv, sizeof(int) * n)) || (rc = ensure(c->info, sizeof(int) * 4)))
-    return rc;
-  S* dA = (S*)c->A.p;
-  int* dp = (int*)c->ipiv.p;
-  int* di = (int*)c->info.p;
-  CK(cudaMemcpyAsync(dA, A, (size_t)n * n * es, cudaMemcpyHostToDevice, c->st));
-  int info = 0;
-  if (factorize) {
-    if ((rc = getrf_batched<S>(c->hb, c->st, dA, 0, n, n, 1, dp, di))) return rc;
-    CK(cudaMemcpyAsync(A, dA, (size_t)n * n * es, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaMemcpyAsync(ipiv, dp, sizeof(int) * n, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaMemcpyAsync(&info, di, sizeof(int), cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
-    if (info > 0) return fail(info, "singular matrix: zero pivot U(info,info)");
-  } else {
-    CK(cudaMemcpyAsync(dp, ipiv, sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
-  }
-  if (n_rhs > 0) {
-    CK(cudaMemcpyAsync(c->b.p, b, (size_t)n * n_rhs * es, cudaMemcpyHostToDevice, c->st));
-    if ((rc = getrs_batched<S>(c->st, dA, 0, n, n, dp, 0, (S*)c->b.p, n, n_rhs))) return rc;
-    CK(cudaMemcpyAsync(b, c->b.p, (size_t)n * n_rhs * es, cudaMemcpyDeviceToHost, c->st));
-  }
-  CK(cudaStreamSynchronize(c->st));
-  return 0;
-}
-
-extern "C" int mfbem_solve_r(int32_t n, double* A, int32_t* ipiv, int32_t, double*, char*, double*, double*,
-                             int32_t n_rhs, double* b, int32_t factorize, int32_t scaling, int32_t condition,
-                             int32_t refine) {
-  return solve_dropin<double>(n, A, ipiv, n_rhs, b, factorize, scaling, condition, refine);
-}
-extern "C" int mfbem_solve_c(int32_t n, double* A, int32_t* ipiv, int32_t, double*, char*, double*, double*,
-                             int32_t n_rhs, double* b, int32_t factorize, int32_t scaling, int32_t condition,
-                             int32_t refine) {
-  return solve_dropin<double2>(n, A, ipiv, n_rhs, b, factorize, scaling, condition, refine);
-}
 
 // ---------------------------------------------------------------------------
 // Mixed precision: FP32 factors + FP64 iterative refinement on the FP64 system.
@@ -719,6 +646,8 @@ static cublasStatus_t gemv_apply(cublasHandle_t hb, int n, const double2* A, int
   return cublasZgemvStridedBatched(hb, CUBLAS_OP_N, n, n, &al, (const cuDoubleComplex*)A, lda, sA,
                                    (const cuDoubleComplex*)x, 1, sx, &be, (cuDoubleComplex*)y, 1, sy, batch);
 }
+
+#include "mfbem_lse.cuh"
 
 // ---------------------------------------------------------------------------
 // GMRES-based iterative refinement (Carson & Higham, SIAM J. Sci. Comput. 40(2),

@@ -103,17 +103,6 @@ def test_solve_lse_singular_matrix_reports_info():
     assert e.value.code == 11
 
 
-def test_solve_lse_unsupported_options_are_errors():
-    L = _abi.load()
-    n = 8
-    A = np.asfortranarray(np.eye(n))
-    b = np.ones(n)
-    ip = np.zeros(n, dtype=np.int32)
-    rc = L.mfbem_solve_r(n, A.ctypes.data_as(_abi._dp), ip.ctypes.data_as(_abi._ip), 1, None, None, None, None, 1,
-                         b.ctypes.data_as(_abi._dp), 1, 1, 0, 0)
-    assert rc == _abi.MFBEM_EUNSUPPORTED
-
-
 def test_kat_confined_cube_on_gpu():
     """docs/examples/ME-ST-EL-002 closed form through the device path."""
     d = M.cube_confined_kat(2)
