@@ -150,6 +150,29 @@ int mfbem_solve_r(int32_t n, double* A, int32_t* ipiv, int32_t aodim, double* Ao
 int mfbem_solve_c(int32_t n, double* A, int32_t* ipiv, int32_t aodim, double* Ao, char* equed, double* r,
                   double* c, int32_t n_rhs, double* b, int32_t factorize, int32_t scaling, int32_t condition,
                   int32_t refine);
+/* Internal points: calculate_internal_points_mechanics_bem_staela /
+   _harela (src/calculate_internal_points_mechanics_static.f90:188-502,
+   src/calculate_internal_points_mechanics_bem_harela.f90:22-505), after the
+   solve. From the nodal solution u_nodes, t_nodes [n_nodes][3] (node%value
+   (1:3) and (4:6): real for staela, complex for harela), for n_ip points
+   x_ip [n_ip][3] inside the region:
+     u_ip     [n_ip][3]      displacement (value(1:3, 0))
+     sigma_ip [n_ip][3][3]   sigma_ip[ip][kc][il] = stress sigma(il, kc),
+                             the traction on the plane of normal e_kc
+                             (value(1:3, kc), column-major like the reference)
+   with the SBIE kernels for u and the HBIE kernels (d*, s*) for sigma, the
+   same classification (precalculated / adaptive rules, 1/r^7 estimate for
+   the HBIE). A point at a boundary node (distance < 1e-12 csize of the node's
+   first element) returns the node's displacement and zero stress, as the
+   reference does; a point on an element away from its nodes returns
+   MFBEM_EUNSUPPORTED. Ordinary boundaries; no symmetry planes, body loads or
+   incident field. FP64 on the device. */
+int mfbem_internal_points_staela(mfbem_handle* h, double mu, double nu, int32_t n_ip, const double* x_ip,
+                                 const double* u_nodes, const double* t_nodes, double* u_ip, double* sigma_ip);
+int mfbem_internal_points_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
+                                 double omega, int32_t n_ip, const double* x_ip, const double* u_nodes,
+                                 const double* t_nodes, double* u_ip, double* sigma_ip);
+
 /* Diagnostics of the last mfbem_solve_r / mfbem_solve_c on the calling
    thread, which the reference prints at verbose level 2: rcond (NaN unless
    condition was set with factorize) and per right-hand side the forward-error

@@ -31,7 +31,8 @@ MFBEM_OVERWRITE = 0x2
 # every symbol include/mfbem.h declares
 ABI_SYMBOLS = [
     "mfbem_mesh_upload", "mfbem_mesh_release", "mfbem_assemble_staela", "mfbem_assemble_harela",
-    "mfbem_solve_r", "mfbem_solve_c", "mfbem_solve_report", "mfbem_sweep_harela", "mfbem_solve_staela", "mfbem_last_stats",
+    "mfbem_solve_r", "mfbem_solve_c", "mfbem_solve_report", "mfbem_internal_points_staela",
+    "mfbem_internal_points_harela", "mfbem_sweep_harela", "mfbem_solve_staela", "mfbem_last_stats",
     "mfbem_last_error", "mfbem_version", "mfbem_solve_c_static",
     "mfbem_qlearn_label", "mfbem_mlp_size", "mfbem_mlp_forward", "mfbem_mlp_loss_grad", "mfbem_mlp_train",
     "mfbem_set_learned_quadrature", "mfbem_sweep_harela_batch",
@@ -93,6 +94,8 @@ def load():
     L.mfbem_solve_r.argtypes = solve_args
     L.mfbem_solve_c.argtypes = solve_args
     L.mfbem_solve_report.argtypes = [_dp, c_int32, _dp, _dp]
+    L.mfbem_internal_points_staela.argtypes = [vp, c_double, c_double, c_int32, _dp, _dp, _dp, _dp, _dp]
+    L.mfbem_internal_points_harela.argtypes = [vp, _dp, _dp, c_double, c_double, c_int32, _dp, _dp, _dp, _dp, _dp]
     L.mfbem_sweep_harela.argtypes = [vp, _dp, _dp, c_double, _dp, c_int32, _dp, c_int32, c_double, _dp, c_int32,
                                      ctypes.POINTER(Stats)]
     L.mfbem_solve_staela.argtypes = [vp, c_double, c_double, c_int32, c_double, _dp, c_int32, ctypes.POINTER(Stats)]

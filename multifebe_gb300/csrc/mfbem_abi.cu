@@ -25,6 +25,7 @@
 #include "mfbem_host.h"
 #include "mfbem_precompute.cuh"
 #include "mfbem_assemble.cuh"
+#include "mfbem_internal.cuh"
 #include "mfbem_lu.cuh"
 #include "mfbem_tc.cuh"
 
@@ -73,6 +74,11 @@ struct mfbem_handle {
   mfbem_stats stats{};
   long long pts_reg = 0, pts_adp = 0, pts_sing = 0;
   int* d_err = nullptr;
+  // internal points: element -> node (0-based), node position and the csize
+  // of the node's first element (-1: node of no element)
+  int* enode = nullptr;
+  double* nodex = nullptr;
+  double* nodecl = nullptr;
 };
 
 static int dalloc(mfbem_handle* h, void** p, size_t bytes) {
@@ -261,6 +267,24 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
       (rc = dupload(h, &tbp, d->tbp_gn, 24 * (size_t)ne))) {
     mfbem_mesh_release(h);
     return rc;
+  }
+  {
+    std::vector<int> en(8 * (size_t)ne);
+    std::vector<double> nx(3 * (size_t)nn, 0.0), ncl(nn, -1.0);
+    for (int e = 0; e < ne; ++e)
+      for (int k = 0; k < 8; ++k) {
+        const int s = d->element_node[8 * e + k] - 1;
+        en[8 * e + k] = s;
+        if (ncl[s] < 0.0) {
+          ncl[s] = d->csize[e];
+          for (int q = 0; q < 3; ++q) nx[3 * s + q] = d->x_gn[24 * (size_t)e + 3 * k + q];
+        }
+      }
+    if ((rc = dupload(h, &h->enode, en.data(), en.size())) || (rc = dupload(h, &h->nodex, nx.data(), nx.size())) ||
+        (rc = dupload(h, &h->nodecl, ncl.data(), ncl.size()))) {
+      mfbem_mesh_release(h);
+      return rc;
+    }
   }
   m.ex = ex; m.cl = cl; m.gln_far = gln; m.ball = ball; m.rev = revd; m.edof = edofd;
   m.dct = dctd; m.dcv = dcvd; m.cpx = cpxd; m.cp_xi = cpxid; m.cp_dn = cpdn; m.cp_kind = cpk;
@@ -592,6 +616,130 @@ extern "C" int mfbem_assemble_harela(mfbem_handle* h, const double lambda[2], co
   PolHarmonic pol;
   pol.p = (const HarParD*)h->par.p;
   return assemble_common<true>(h, &pol, nu, A, lda, b, flags);
+}
+
+// ---------------------------------------------------------------------------
+// Internal points (calculate_internal_points_mechanics_bem_{staela,harela})
+// ---------------------------------------------------------------------------
+struct TmpBufs {
+  std::vector<void*> v;
+  ~TmpBufs() {
+    for (void* p : v) cudaFree(p);
+  }
+  int get(void** p, size_t bytes) {
+    if (cudaMalloc(p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(MFBEM_ENOMEM, "cudaMalloc (internal points)");
+    }
+    v.push_back(*p);
+    return 0;
+  }
+};
+
+template <class POL>
+static int internal_points_run(mfbem_handle* h, const POL& pol, int nf, int32_t n_ip, const double* x_ip,
+                               const double* u_nodes, const double* t_nodes, double* u_ip, double* sigma_ip) {
+  typedef typename POL::T T;
+  const DMesh& m = h->m;
+  const int nn = h->nn, ne = h->ne;
+  TmpBufs tb;
+  IpArgs a{};
+  a.nip = n_ip;
+  a.nf = nf;
+  a.nn = nn;
+  a.enode = h->enode;
+  a.nodex = h->nodex;
+  a.nodecl = h->nodecl;
+  const size_t vb = sizeof(T) * 3 * (size_t)nn * nf, ob = sizeof(T) * 12 * (size_t)n_ip * nf;
+  int rc;
+  if ((rc = tb.get((void**)&a.xip, sizeof(double) * 3 * (size_t)n_ip)) || (rc = tb.get((void**)&a.uval, vb)) ||
+      (rc = tb.get((void**)&a.tval, vb)) || (rc = tb.get((void**)&a.cls_s, (size_t)n_ip * ne)) ||
+      (rc = tb.get((void**)&a.cls_h, (size_t)n_ip * ne)) || (rc = tb.get((void**)&a.onnode, sizeof(int) * n_ip)) ||
+      (rc = tb.get((void**)&a.npair, sizeof(int) * n_ip)) || (rc = tb.get((void**)&a.poff, sizeof(int) * (n_ip + 1))) ||
+      (rc = tb.get((void**)&a.err, sizeof(int))) || (rc = tb.get(&a.out, ob)))
+    return rc;
+  cudaStream_t st = h->st;
+  CK(cudaMemcpyAsync((void*)a.xip, x_ip, sizeof(double) * 3 * (size_t)n_ip, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync((void*)a.uval, u_nodes, vb, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync((void*)a.tval, t_nodes, vb, cudaMemcpyHostToDevice, st));
+  const int big = INT_MAX;
+  CK(cudaMemcpyAsync(a.err, &big, sizeof(int), cudaMemcpyHostToDevice, st));
+  k_ip_onnode<<<nblk(n_ip, 128), 128, 0, st>>>(a); ++g_launches;
+  k_ip_classify<<<std::min(nblk((long long)n_ip * ne, 256), 152u * 16u), 256, 0, st>>>(m, a, h->d_qs); ++g_launches;
+  k_ip_count<<<nblk(n_ip, 8), 256, 0, st>>>(m, a); ++g_launches;
+  k_scan<int, int><<<1, 1024, 0, st>>>(a.npair, a.poff, n_ip); ++g_launches;
+  int np = 0;
+  CK(cudaMemcpyAsync(&np, a.poff + n_ip, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  a.npairs = np;
+  if ((rc = tb.get((void**)&a.pair_e, sizeof(int) * (size_t)np)) || (rc = tb.get((void**)&a.pair_ip, sizeof(int) * (size_t)np)) ||
+      (rc = tb.get(&a.slot, sizeof(T) * 12 * (size_t)np * nf)))
+    return rc;
+  k_ip_fill<<<nblk(n_ip, 8), 256, 0, st>>>(m, a); ++g_launches;
+  if (np > 0) {
+    k_ip_adp<POL><<<nblk((long long)np * nf, 64), 64, 0, st>>>(m, a, pol, h->d_qs); ++g_launches;
+  }
+  constexpr int WPB = 4;
+  k_ip_reg<POL, WPB><<<nblk((long long)n_ip * nf, WPB), WPB * 32, 0, st>>>(m, a, pol); ++g_launches;
+  CK(cudaGetLastError());
+  std::vector<T> out(12 * (size_t)n_ip * nf);
+  int err = 0;
+  CK(cudaMemcpyAsync(out.data(), a.out, ob, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&err, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (err != INT_MAX)
+    return fail(MFBEM_EUNSUPPORTED, "internal point " + std::to_string(err - 1) +
+                                        " lies on the boundary away from a node (needs the singular HBIE integration)");
+  T* uo = (T*)u_ip;
+  T* so = (T*)sigma_ip;
+  for (size_t i = 0; i < (size_t)n_ip * nf; ++i) {
+    for (int c = 0; c < 3; ++c) uo[3 * i + c] = out[12 * i + c];
+    for (int c = 0; c < 9; ++c) so[9 * i + c] = out[12 * i + 3 + c];
+  }
+  return 0;
+}
+
+extern "C" int mfbem_internal_points_staela(mfbem_handle* h, double mu, double nu, int32_t n_ip, const double* x_ip,
+                                            const double* u_nodes, const double* t_nodes, double* u_ip,
+                                            double* sigma_ip) {
+  g_err.clear();
+  if (!h || n_ip < 0 || (n_ip > 0 && (!x_ip || !u_nodes || !t_nodes || !u_ip || !sigma_ip)))
+    return fail(MFBEM_EARG, "invalid argument");
+  if (n_ip == 0) return 0;
+  IpStatic pol;
+  pol.k = staela_params(mu, nu);
+  pol.nu = nu;
+  pol.cted1 = -1.0 / (8.0 * kPi * (1.0 - nu));
+  pol.cted2 = 1.0 - 2.0 * nu;
+  pol.ctes1 = mu / (4.0 * kPi * (1.0 - nu));
+  pol.ctes2 = 1.0 - 2.0 * nu;
+  pol.ctes3 = 1.0 - 4.0 * nu;
+  return internal_points_run(h, pol, 1, n_ip, x_ip, u_nodes, t_nodes, u_ip, sigma_ip);
+}
+
+extern "C" int mfbem_internal_points_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
+                                            double omega, int32_t n_ip, const double* x_ip, const double* u_nodes,
+                                            const double* t_nodes, double* u_ip, double* sigma_ip) {
+  g_err.clear();
+  if (!h || !lambda || !mu || n_ip < 0 || (n_ip > 0 && (!x_ip || !u_nodes || !t_nodes || !u_ip || !sigma_ip)))
+    return fail(MFBEM_EARG, "invalid argument");
+  if (n_ip == 0) return 0;
+  TmpBufs tb;
+  HarParD* pd;
+  HarParH* ph;
+  double* dq;
+  int rc;
+  if ((rc = tb.get((void**)&pd, sizeof(HarParD))) || (rc = tb.get((void**)&ph, sizeof(HarParH))) ||
+      (rc = tb.get((void**)&dq, 6 * sizeof(double))))
+    return rc;
+  const double q[6] = {lambda[0], lambda[1], mu[0], mu[1], rho, omega};
+  CK(cudaMemcpyAsync(dq, q, sizeof(q), cudaMemcpyHostToDevice, h->st));
+  k_harpar<<<1, 32, 0, h->st>>>(dq, 1, pd, zexp_thresholds()); ++g_launches;
+  k_harparh<<<1, 32, 0, h->st>>>(dq, 1, ph); ++g_launches;
+  IpHarmonic pol;
+  pol.p = pd;
+  pol.ph = ph;
+  return internal_points_run(h, pol, 1, n_ip, x_ip, u_nodes, t_nodes, u_ip, sigma_ip);
 }
 
 // ---------------------------------------------------------------------------

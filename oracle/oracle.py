@@ -50,6 +50,10 @@ def lib():
         L.orc_assemble_staela.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _dp, _dp, ctypes.c_int,
                                           _lp]
         L.orc_assemble_harela_nu.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 8 + [_dp, _dp, ctypes.c_int, _lp]
+        L.orc_internal_points_staela.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                                 _dp, _dp, _dp, _dp, ctypes.c_int]
+        L.orc_internal_points_harela.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 6 + [ctypes.c_int, _dp, _dp,
+                                                                                          _dp, _dp, ctypes.c_int]
         L.orc_pair_staela.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                       _dp, _dp]
         L.orc_pair_harela.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6 + [_dp, _dp]
@@ -155,6 +159,28 @@ class Problem:
         cls = lib().orc_pair_harela(self._h, ci, e, lam.real, lam.imag, mu.real, mu.imag, float(mat["rho"]),
                                     float(omega), _p(h), _p(g))
         return cls, h, g
+
+    def internal_points(self, xip, u, t, mat=None, omega=None, mu=None, nu=None, nthreads=0):
+        """Displacement [nip,3] and stresses [nip,3,3] (sigma[:, il, kc]) at
+        internal points from nodal u, t [nn,3]; static with mu, nu, harmonic
+        with mat, omega."""
+        xip = np.ascontiguousarray(xip, dtype=np.float64)
+        nip = len(xip)
+        cplx = omega is not None
+        dt = np.complex128 if cplx else np.float64
+        u = np.ascontiguousarray(u, dtype=dt)
+        t = np.ascontiguousarray(t, dtype=dt)
+        out = np.zeros((nip, 4, 3), dtype=dt)
+        if cplx:
+            lam, m = complex(mat["lambda"]), complex(mat["mu"])
+            rc = lib().orc_internal_points_harela(self._h, lam.real, lam.imag, m.real, m.imag, float(mat["rho"]),
+                                                  float(omega), nip, _p(xip), _p(u), _p(t), _p(out), nthreads)
+        else:
+            rc = lib().orc_internal_points_staela(self._h, float(mu), float(nu), nip, _p(xip), _p(u), _p(t), _p(out),
+                                                  nthreads)
+        if rc:
+            raise ValueError(f"internal point {rc - 1} lies on the boundary away from a node")
+        return out[:, 0, :], np.transpose(out[:, 1:, :], (0, 2, 1))
 
     def solution(self, x):
         """Nodal (u, t) from the solved unknown vector: the variable of each

@@ -78,6 +78,9 @@ struct HarPar {
   cplx k1, k2, c1, c2;
   cplx psi[6], chi[6], T1[10], T2[9], T3[9];
   cplx cte_u, cte_t;
+  // d* / s* (HBIE) coefficients
+  cplx S1[11], S2[11], S3[12], S4[10], S5[11];
+  cplx cte_d, cte_s;
 };
 static HarPar harela_parameters(cplx lambda, cplx mu, double rho, double omega) {
   HarPar p;
@@ -134,6 +137,66 @@ static HarPar harela_parameters(cplx lambda, cplx mu, double rho, double omega) 
   p.T3[8] = -6.0 / ik2p2;
   p.cte_u = c_1_4pi / mu;
   p.cte_t = cplx(c_1_4pi, 0.0);
+  // S1..S5 (bem_harela3d.f90:219-279)
+  cplx k1p2 = k1 * k1, q = k1p2 / k2p2, c1p5 = c1p4 * c1, c2p3 = c2p2 * c2;
+  double om3 = om2 * omega;
+  p.S1[0] = 3.0 * (1.0 - 2.0 * r);
+  p.S1[1] = -0.5 * c2p2 / c1p4 * om2;
+  p.S1[2] = k2p2;
+  p.S1[3] = 4.0 * I * k1 * q;
+  p.S1[4] = -7.0 * I * k2;
+  p.S1[5] = 24.0 * q;
+  p.S1[6] = -27.0;
+  p.S1[7] = 60.0 * q / ik1;
+  p.S1[8] = -60.0 / ik2;
+  p.S1[9] = 60.0 * q / ik1p2;
+  p.S1[10] = -60.0 / ik2p2;
+  p.S2[0] = 6.0 * r;
+  p.S2[1] = (0.5 / c2p2 + 1.5 * c2p2 / c1p4 - 1.0 / c1p2) * om2;
+  p.S2[2] = 2.0 * c2p2 / c1p4 * (c1p2 / c2p2 - 2.0) * om2;
+  p.S2[3] = 2.0 * I * c2p2 / c1p3 * (8.0 - 3.0 * c1p2 / c2p2) * omega;
+  p.S2[4] = -4.0 * I * k2;
+  p.S2[5] = 6.0 * r * (6.0 - c1p2 / c2p2);
+  p.S2[6] = -24.0;
+  p.S2[7] = r * 60.0 / ik1;
+  p.S2[8] = -60.0 / ik2;
+  p.S2[9] = 60.0 / ik2p2;
+  p.S2[10] = -60.0 / ik2p2;
+  p.S3[0] = 30.0 * (1.0 - r);
+  p.S3[1] = 1.5 * (1.0 / c2p2 - c2p2 / c1p4) * om2;
+  p.S3[2] = -4.0 * r * k1p2;
+  p.S3[3] = 4.0 * k2p2;
+  p.S3[4] = 40.0 * r * I * k1;
+  p.S3[5] = -40.0 * I * k2;
+  p.S3[6] = 180.0 * r;
+  p.S3[7] = -180.0;
+  p.S3[8] = 420.0 * r / ik1;
+  p.S3[9] = -420.0 / ik2;
+  p.S3[10] = 420.0 / ik2p2;
+  p.S3[11] = -420.0 / ik2p2;
+  p.S4[0] = 2.0 * r;
+  p.S4[1] = 0.5 * (c2p2 / c1p4 + 1.0 / c2p2) * om2;
+  p.S4[2] = -2.0 / 5.0 * (1.0 / c2p3 + 2.0 / 3.0 * c2p2 / c1p5) * I * om3;
+  p.S4[3] = 2.0 * I * k2;
+  p.S4[4] = -4.0 * r;
+  p.S4[5] = 6.0;
+  p.S4[6] = -12.0 * r / ik1;
+  p.S4[7] = 12.0 / ik2;
+  p.S4[8] = -12.0 / ik2p2;
+  p.S4[9] = 12.0 / ik2p2;
+  p.S5[0] = 2.0 * (1.0 - 3.0 * r);
+  p.S5[1] = (-2.0 / c1p2 + 0.5 / c2p2 + 0.5 * c2p2 / c1p4) * om2;
+  p.S5[2] = (8.0 / 3.0 / c1p3 + 4.0 / 15.0 / c2p3 - 1.0 / c1 / c2p2 - 24.0 / 15.0 * c2p2 / c1p5) * I * om3;
+  p.S5[3] = (-4.0 / c1p2 + 1.0 / c2p2 + 4.0 * c2p2 / c1p4) * om2;
+  p.S5[4] = 4.0 * I * (1.0 / c1 - 2.0 * c2p2 / c1p3) * omega;
+  p.S5[5] = 4.0 * (1.0 - 3.0 * r);
+  p.S5[6] = 4.0;
+  p.S5[7] = 12.0 * I * k1 / k2p2;
+  p.S5[8] = -12.0 * I / k2;
+  p.S5[9] = 12.0 / k2p2;
+  p.S5[10] = -12.0 / k2p2;
+  p.cte_d = cplx(c_1_4pi, 0.0);
+  p.cte_s = c_1_4pi * mu;
   return p;
 }
 
@@ -141,6 +204,7 @@ static HarPar harela_parameters(cplx lambda, cplx mu, double rho, double omega) 
 // constants. Static: bem_staela3d.f90:622-633; harmonic: bem_harela3d.f90:654-688.
 struct StaelaK {
   typedef double T;
+  static constexpr int F = 5;  // quasi-singular estimate for 1/r^5 integrands
   double cteu1, cteu2, ctet1, ctet2;
   StaelaK(double mu, double nu) {
     cteu1 = 1.0 / (16.0 * c_pi * mu * (1.0 - nu));
@@ -166,6 +230,7 @@ struct StaelaK {
 };
 struct HarelaK {
   typedef cplx T;
+  static constexpr int F = 5;
   HarPar p;
   explicit HarelaK(const HarPar& pp) : p(pp) {}
   T cu() const { return p.cte_u; }
@@ -217,6 +282,107 @@ struct HarelaK {
         double dk = (il == ik) ? 1.0 : 0.0;
         fu[il][ik] = psi * dk - chi * drdx[il] * drdx[ik];
         ft[il][ik] = TT1 * drdx[il] * drdx[ik] * drdn + TT2 * (drdn * dk + drdx[ik] * n[il]) + TT3 * drdx[il] * n[ik];
+      }
+  }
+};
+
+// HBIE kernels at a point x_i with unit normal n_i, exterior integration.
+// eval() returns s* (integrated with phi^p into m) in the slot of t* and d*
+// (with phi^s into l) in the slot of u*, so ext_pre / ext_st / ext_adp
+// integrate them unchanged: m takes the place of h (constant ct(), sign
+// reversed with the element) and l that of g (constant cu()).
+// Static: bem_staela3d.f90:4376-4446; harmonic: bem_harela3d.f90:2573-2662.
+struct StaelaHK {
+  typedef double T;
+  static constexpr int F = 7;  // quasi-singular estimate for 1/r^7 integrands
+  double nu, cted1, cted2, ctes1, ctes2, ctes3, ni[3];
+  StaelaHK(double mu, double nu_, const double n_i[3]) : nu(nu_) {
+    cted1 = -1.0 / (8.0 * c_pi * (1.0 - nu));
+    cted2 = 1.0 - 2.0 * nu;
+    ctes1 = mu / (4.0 * c_pi * (1.0 - nu));
+    ctes2 = 1.0 - 2.0 * nu;
+    ctes3 = 1.0 - 4.0 * nu;
+    for (int c = 0; c < 3; ++c) ni[c] = n_i[c];
+  }
+  T cu() const { return cted1; }
+  T ct() const { return ctes1; }
+  inline void eval(const double rv[3], const double n[3], T fd[3][3], T fs[3][3]) const {
+    double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    double d1r = 1.0 / r, d1r2 = d1r * d1r, d1r3 = d1r2 * d1r;
+    double drdx[3] = {rv[0] * d1r, rv[1] * d1r, rv[2] * d1r};
+    double drdn = drdx[0] * n[0] + drdx[1] * n[1] + drdx[2] * n[2];
+    double drdni = -(drdx[0] * ni[0] + drdx[1] * ni[1] + drdx[2] * ni[2]);
+    double nni = n[0] * ni[0] + n[1] * ni[1] + n[2] * ni[2];
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        double dk = (il == ik) ? 1.0 : 0.0;
+        fd[il][ik] = d1r2 * ((cted2 * dk + 3.0 * drdx[il] * drdx[ik]) * drdni +
+                             cted2 * (ni[il] * drdx[ik] - ni[ik] * drdx[il]));
+        fs[il][ik] = d1r3 * (3.0 * (5.0 * drdx[il] * drdx[ik] - nu * dk) * drdn * drdni +
+                             3.0 * ctes2 * (drdx[ik] * ni[il] * drdn - drdx[il] * n[ik] * drdni) +
+                             3.0 * nu * (drdx[il] * ni[ik] * drdn - drdx[ik] * n[il] * drdni) +
+                             (3.0 * nu * drdx[il] * drdx[ik] + ctes2 * dk) * nni + ctes2 * n[il] * ni[ik] -
+                             ctes3 * n[ik] * ni[il]);
+      }
+  }
+};
+struct HarelaHK {
+  typedef cplx T;
+  static constexpr int F = 7;
+  HarPar p;
+  double ni[3];
+  HarelaHK(const HarPar& pp, const double n_i[3]) : p(pp) {
+    for (int c = 0; c < 3; ++c) ni[c] = n_i[c];
+  }
+  T cu() const { return p.cte_d; }
+  T ct() const { return p.cte_s; }
+  inline void eval(const double rv[3], const double n[3], T fd[3][3], T fs[3][3]) const {
+    double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    double d1r1 = 1.0 / r, d1r2 = d1r1 * d1r1, d1r3 = d1r2 * d1r1, d1r4 = d1r3 * d1r1, d1r5 = d1r4 * d1r1;
+    double drdx[3] = {rv[0] * d1r1, rv[1] * d1r1, rv[2] * d1r1};
+    double drdn = drdx[0] * n[0] + drdx[1] * n[1] + drdx[2] * n[2];
+    double drdni = -(drdx[0] * ni[0] + drdx[1] * ni[1] + drdx[2] * ni[2]);
+    double nni = n[0] * ni[0] + n[1] * ni[1] + n[2] * ni[2];
+    const cplx I(0.0, 1.0);
+    cplx z[2] = {-I * p.k1 * r, -I * p.k2 * r};
+    cplx E[7][2];
+    zexp_decomposed(2, z, E);
+    for (int j = 0; j < 2; ++j) {
+      E[2][j] = E[2][j] * d1r1;
+      E[3][j] = E[3][j] * d1r2;
+      E[4][j] = E[4][j] * d1r3;
+      E[5][j] = E[5][j] * d1r4;
+      E[6][j] = E[6][j] * d1r5;
+    }
+    cplx TT1 = p.T1[0] * d1r2 + p.T1[1] + p.T1[2] * E[2][0] + p.T1[3] * E[2][1] + p.T1[4] * E[3][0] +
+               p.T1[5] * E[3][1] + p.T1[6] * E[4][0] + p.T1[7] * E[4][1] + p.T1[8] * E[5][0] + p.T1[9] * E[5][1];
+    cplx TT2 = p.T2[0] * d1r2 + p.T2[1] + p.T2[2] * E[2][1] + p.T2[3] * E[3][0] + p.T2[4] * E[3][1] +
+               p.T2[5] * E[4][0] + p.T2[6] * E[4][1] + p.T2[7] * E[5][0] + p.T2[8] * E[5][1];
+    cplx TT3 = p.T3[0] * d1r2 + p.T3[1] + p.T3[2] * E[2][0] + p.T3[3] * E[3][0] + p.T3[4] * E[3][1] +
+               p.T3[5] * E[4][0] + p.T3[6] * E[4][1] + p.T3[7] * E[5][0] + p.T3[8] * E[5][1];
+    cplx S1 = p.S1[0] * d1r3 + p.S1[1] * d1r1 + p.S1[2] * E[2][1] + p.S1[3] * E[3][0] + p.S1[4] * E[3][1] +
+              p.S1[5] * E[4][0] + p.S1[6] * E[4][1] + p.S1[7] * E[5][0] + p.S1[8] * E[5][1] + p.S1[9] * E[6][0] +
+              p.S1[10] * E[6][1];
+    cplx S2 = p.S2[0] * d1r3 + p.S2[1] * d1r1 + p.S2[2] * E[2][0] + p.S2[3] * E[3][0] + p.S2[4] * E[3][1] +
+              p.S2[5] * E[4][0] + p.S2[6] * E[4][1] + p.S2[7] * E[5][0] + p.S2[8] * E[5][1] + p.S2[9] * E[6][0] +
+              p.S2[10] * E[6][1];
+    cplx S3 = p.S3[0] * d1r3 + p.S3[1] * d1r1 + p.S3[2] * E[2][0] + p.S3[3] * E[2][1] + p.S3[4] * E[3][0] +
+              p.S3[5] * E[3][1] + p.S3[6] * E[4][0] + p.S3[7] * E[4][1] + p.S3[8] * E[5][0] + p.S3[9] * E[5][1] +
+              p.S3[10] * E[6][0] + p.S3[11] * E[6][1];
+    cplx S4 = p.S4[0] * d1r3 + p.S4[1] * d1r1 + p.S4[2] + p.S4[3] * E[3][1] + p.S4[4] * E[4][0] +
+              p.S4[5] * E[4][1] + p.S4[6] * E[5][0] + p.S4[7] * E[5][1] + p.S4[8] * E[6][0] + p.S4[9] * E[6][1];
+    cplx S5 = p.S5[0] * d1r3 + p.S5[1] * d1r1 + p.S5[2] + p.S5[3] * E[2][0] + p.S5[4] * E[3][0] +
+              p.S5[5] * E[4][0] + p.S5[6] * E[4][1] + p.S5[7] * E[5][0] + p.S5[8] * E[5][1] + p.S5[9] * E[6][0] +
+              p.S5[10] * E[6][1];
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        double dk = (il == ik) ? 1.0 : 0.0;
+        fd[il][ik] = TT1 * drdx[il] * drdx[ik] * drdni - TT2 * (-drdni * dk + drdx[il] * ni[ik]) -
+                     TT3 * drdx[ik] * ni[il];
+        fs[il][ik] = S1 * (drdx[il] * ni[ik] * drdn - drdx[ik] * n[il] * drdni - dk * drdn * drdni +
+                           drdx[il] * drdx[ik] * nni) +
+                     S2 * (drdx[ik] * ni[il] * drdn - drdx[il] * n[ik] * drdni) +
+                     S3 * drdx[il] * drdx[ik] * drdn * drdni + S4 * (dk * nni + ni[ik] * n[il]) + S5 * n[ik] * ni[il];
       }
   }
 };
@@ -343,7 +509,7 @@ static void ext_adp(const K& k, const Elem& e, bool reverse, double xi_s[4][2], 
     double cl = characteristic_length_quad8(x_s, 1e-12);
     nearest_element_point_quad8(x_s, cl, x_i, barxip, &rmin, &d, &method);
   }
-  int gln_near = qs_n_estimation_telles(2, 5, qsp, d, barxip);
+  int gln_near = qs_n_estimation_telles(2, K::F, qsp, d, barxip);
   bool subdivide = false;
   if (ks == ns) {
     if (gln_near == 0) { gln_near = 30; if (st) st->maxdepth_hits++; }
@@ -642,7 +808,7 @@ static int sbie_auto(const K& k, const Elem& e, bool reverse, const double x_i[3
     sbie_int<K>(k, e, reverse, barxi, out);
     return CLS_SING;
   }
-  int gln_near = qs_n_estimation_standard(2, 5, qsp, d, barxi);
+  int gln_near = qs_n_estimation_standard(2, K::F, qsp, d, barxi);
   int gln = std::max(e.gln_far, gln_near);
   if (gln <= e.ps_gln_max && gln_near > 0) {
     int ps = 0;
@@ -653,6 +819,40 @@ static int sbie_auto(const K& k, const Elem& e, bool reverse, const double x_i[3
   }
   double xi_s[4][2];
   ext_adp<K>(k, e, reverse, xi_s, x_i, qsp, 1, ns, out, st);
+  return CLS_ADP;
+}
+
+// hbie_auto for a point off the element (bem_staela3d.f90:4307-4373 /
+// the harmonic twin): the same classification with the 1/r^7 estimate. A
+// point on the element (d <= 1e-12) would need hbie_int; it returns CLS_SING
+// with zero kernels, and internal points never reach it (see internal_points).
+template <class K>
+static int hbie_auto(const K& k, const Elem& e, bool reverse, const double x_i[3], const QsParams& qsp, int ns,
+                     HG<K>& out) {
+  double r[3] = {e.bc[0] - x_i[0], e.bc[1] - x_i[1], e.bc[2] - x_i[2]};
+  double rmin = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) - e.br;
+  double barxi[2] = {0.0, 0.0}, d;
+  if (rmin > 4.0 * e.br) {
+    d = rmin / e.cl;
+  } else {
+    int method;
+    nearest_element_point_quad8(e.x, e.cl, x_i, barxi, &rmin, &d, &method);
+    if (d <= 1e-12) {
+      out.zero();
+      return CLS_SING;
+    }
+  }
+  int gln_near = qs_n_estimation_standard(2, K::F, qsp, d, barxi);
+  int gln = std::max(e.gln_far, gln_near);
+  if (gln <= e.ps_gln_max && gln_near > 0) {
+    int ps = 0;
+    for (int i = 0; i < e.n_ps; ++i)
+      if (e.ps_gln[i] >= gln) { ps = i; break; }
+    ext_pre<K>(k, ps, e, reverse, x_i, out);
+    return ps;
+  }
+  double xi_s[4][2];
+  ext_adp<K>(k, e, reverse, xi_s, x_i, qsp, 1, ns, out, nullptr);
   return CLS_ADP;
 }
 
@@ -978,6 +1178,75 @@ static int assemble(const Problem& P, const K& k, typename K::T nu, typename K::
   return bad ? -1 : 0;
 }
 
+// Internal points: calculate_internal_points_mechanics_bem_{staela,harela}
+// (src/calculate_internal_points_mechanics_static.f90:188-502,
+// src/calculate_internal_points_mechanics_bem_harela.f90:22-505) for ordinary
+// BE boundaries without symmetry planes, body loads or incident field:
+//   u_il(x_i)      = sum_e sum_kn g(kn,il,ik) t_ik - h(kn,il,ik) u_ik
+//   sigma_il,kc    = sum_e sum_kn l(kn,il,ik) t_ik - m(kn,il,ik) u_ik, n_i = e_kc
+// with sbie_auto / hbie_auto at x_i; a point at a boundary node (distance /
+// csize of the node's first element < 1e-12) takes the node's displacement and
+// zero stresses (calculate_internal_points_mechanics_bem_harela.f90:190-208).
+// out[ip][4][3]: [0] displacement, [1 + kc] sigma(:, kc). Returns the index + 1
+// of the first point that lies on an element away from its nodes, else 0.
+template <class K, class KH, class MKH>
+static int internal_points(const Problem& P, const K& k, MKH mkh, int nip, const double* xip,
+                           const typename K::T* u, const typename K::T* t, typename K::T* out, int nthreads) {
+  typedef typename K::T T;
+  std::vector<int> efirst(P.nn, -1);
+  for (int e = 0; e < P.ne; ++e)
+    for (int kn = 0; kn < 8; ++kn)
+      if (efirst[P.conn[8 * e + kn]] < 0) efirst[P.conn[8 * e + kn]] = e;
+  std::vector<int> on_elem(nip, 0);
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int ip = 0; ip < nip; ++ip) {
+    const double* xi = xip + 3 * (size_t)ip;
+    T acc[4][3];
+    for (int a = 0; a < 4; ++a)
+      for (int c = 0; c < 3; ++c) acc[a][c] = (T)0;
+    int on_node = -1;
+    for (int sn = 0; sn < P.nn; ++sn) {
+      if (efirst[sn] < 0) continue;
+      double rd[3] = {xi[0] - P.X[3 * sn], xi[1] - P.X[3 * sn + 1], xi[2] - P.X[3 * sn + 2]};
+      if (std::sqrt(rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2]) / P.el[efirst[sn]].cl < 1e-12) on_node = sn;
+    }
+    if (on_node < 0) {
+      for (int e = 0; e < P.ne && !on_elem[ip]; ++e) {
+        const int* cn = &P.conn[8 * e];
+        HG<K> hg;
+        if (sbie_auto<K>(k, P.el[e], false, xi, P.qsp, P.ns_max, hg, nullptr) == CLS_SING) {
+          on_elem[ip] = 1;
+          break;
+        }
+        for (int il = 0; il < 3; ++il)
+          for (int ik = 0; ik < 3; ++ik)
+            for (int kn = 0; kn < 8; ++kn)
+              acc[0][il] = acc[0][il] + hg.g[kn][il][ik] * t[3 * cn[kn] + ik] - hg.h[kn][il][ik] * u[3 * cn[kn] + ik];
+        for (int kc = 0; kc < 3; ++kc) {
+          double ni[3] = {0.0, 0.0, 0.0};
+          ni[kc] = 1.0;
+          KH kh = mkh(ni);
+          HG<KH> ml;
+          hbie_auto<KH>(kh, P.el[e], false, xi, P.qsp, P.ns_max, ml);
+          for (int il = 0; il < 3; ++il)
+            for (int ik = 0; ik < 3; ++ik)
+              for (int kn = 0; kn < 8; ++kn)
+                acc[1 + kc][il] =
+                    acc[1 + kc][il] + ml.g[kn][il][ik] * t[3 * cn[kn] + ik] - ml.h[kn][il][ik] * u[3 * cn[kn] + ik];
+        }
+      }
+    } else {
+      for (int c = 0; c < 3; ++c) acc[0][c] = u[3 * on_node + c];
+    }
+    for (int a = 0; a < 4; ++a)
+      for (int c = 0; c < 3; ++c) out[12 * (size_t)ip + 3 * a + c] = acc[a][c];
+  }
+  for (int ip = 0; ip < nip; ++ip)
+    if (on_elem[ip]) return ip + 1;
+  return 0;
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -1067,6 +1336,24 @@ int orc_pair_harela(void* hp, int ci, int e, double lre, double lim, double mre,
   std::memcpy(h, hg.h, sizeof(hg.h));
   std::memcpy(g, hg.g, sizeof(hg.g));
   return cls;
+}
+// Internal points (displacement and stresses), u / t nodal values [nn][3].
+int orc_internal_points_staela(void* hp, double mu, double nu, int nip, const double* xip, const double* u,
+                               const double* t, double* out, int nthreads) {
+  Problem* P = (Problem*)hp;
+  StaelaK k(mu, nu);
+  auto mkh = [&](const double* ni) { return StaelaHK(mu, nu, ni); };
+  return internal_points<StaelaK, StaelaHK>(*P, k, mkh, nip, xip, u, t, out, nthreads);
+}
+int orc_internal_points_harela(void* hp, double lre, double lim, double mre, double mim, double rho, double omega,
+                               int nip, const double* xip, const double* u, const double* t, double* out,
+                               int nthreads) {
+  Problem* P = (Problem*)hp;
+  HarPar par = harela_parameters(cplx(lre, lim), cplx(mre, mim), rho, omega);
+  HarelaK k(par);
+  auto mkh = [&](const double* ni) { return HarelaHK(par, ni); };
+  return internal_points<HarelaK, HarelaHK>(*P, k, mkh, nip, xip, (const cplx*)u, (const cplx*)t, (cplx*)out,
+                                            nthreads);
 }
 // Harmonic parameter block for tests: k1,k2,c1,c2,psi(6),chi(6),T1(10),T2(9),T3(9),cte_u,cte_t (complex)
 void orc_harela_parameters(double lre, double lim, double mre, double mim, double rho, double omega, double* out) {

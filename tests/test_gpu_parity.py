@@ -115,6 +115,27 @@ def test_kat_confined_cube_on_gpu():
     R.close()
 
 
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_kat_harmonic_p_wave_column_on_gpu(oracle, precision):
+    """docs/examples/ME-TH-EL-001 through the device sweep: the closed form to
+    the discretisation error of 4x4 quad8 per face, and the oracle's solution
+    of the same mesh to the parity tolerance."""
+    from test_oracle_kat import _p_wave_column
+    d = M.cube_confined_kat(4)
+    mat = M.viscoelastic(2.4, 0.2, 1.0, 0.02)
+    om = np.array([1.0, 2.0, 5.0])
+    R = BemRegion(d)
+    X = R.sweep_harela(mat, om, precision=precision)
+    P = oracle.Problem(d)
+    for i, w in enumerate(om):
+        u, _ = R.solution(X[i])
+        ue = _p_wave_column(mat, w, d.nodes[:, 0])
+        assert np.abs(u[:, 0] - ue).max() / np.abs(ue).max() < (3e-3 if w > 3 else 2e-4)
+        Ao, bo = P.assemble_harela(mat, w)
+        assert rel(X[i], oracle.lu_solve(Ao, bo)) < (1e-10 if precision == "plain" else 1e-8)
+    R.close()
+
+
 @pytest.mark.parametrize("precision,tol", [("plain", 1e-10), ("mixed", 1e-8)])
 def test_sweep_matches_oracle_solution(oracle, precision, tol):
     d = M.cube_clamped_top_traction(4)
