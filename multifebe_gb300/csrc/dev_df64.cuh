@@ -117,6 +117,8 @@ struct DfConst {
   ff inv[24];       // 1/k (inv[0] unused)
   ff sin_c[9];      // (-1)^k / (2k+1)!, k = 0..8
   ff cos_c[10];     // (-1)^k / (2k)!,   k = 0..9
+  ff zc[16];        // 6! / (6+m)!, m = 0..15: the E_6 series t = sum c_m z^m
+  float zc32[16];   // the same in FP32 (the series tail)
   float ln2[3], pio2[3];
 };
 #ifdef __CUDACC__
@@ -146,6 +148,12 @@ inline DfConst df_constants_host() {
     if (k > 0) g *= (long double)(2 * k - 1) * (long double)(2 * k);
     c.cos_c[k] = split((k & 1 ? -1.0L : 1.0L) / g);
     if (k < 9) c.sin_c[k] = split((k & 1 ? -1.0L : 1.0L) / (g * (long double)(2 * k + 1)));
+  }
+  long double q = 1.0L;
+  for (int m = 0; m < 16; ++m) {
+    if (m > 0) q /= (long double)(6 + m);
+    c.zc[m] = split(q);
+    c.zc32[m] = (float)q;
   }
   split3(0.693147180559945309417232121458176568L, c.ln2);
   split3(1.570796326794896619231321691639751442L, c.pio2);

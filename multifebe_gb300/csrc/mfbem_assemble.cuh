@@ -631,20 +631,43 @@ __device__ __forceinline__ int zexp_nterms_f(const float* t2, float az2) {
   return lo + 1;
 }
 
-// E_2..E_5 of z in double-float: the series tail of numerical.f90:1286-1301 for
-// |z| <= 1 (same number of terms), e^z minus its leading terms above.
+// E_2..E_5 of z in double-float. |z| <= 1: the series of numerical.f90:1286-1301
+// with the same number of terms, E_6 = z^6/6! t, t = sum_{m=0..M} c_m z^m,
+// c_m = 6!/(6+m)!: the terms m <= 6 in double-float (Horner), the tail m >= 7
+// in FP32 -- it is at most 720/13! = 1.2e-7 of t, so its FP32 rounding stays
+// near 1e-14 of t (and 3e-15 of E_5). |z| > 1: e^z minus its leading terms.
 __device__ __forceinline__ void zexp_2to5_ff(const float* t2, cf z, cf& E2, cf& E3, cf& E4, cf& E5) {
   const float az2 = __fmaf_rn(z.re.hi, z.re.hi, __fmul_rn(z.im.hi, z.im.hi));
   cf z2 = cf_mul(z, z), z3 = cf_mul(z2, z), z4 = cf_mul(z3, z);
   if (az2 <= 1.0f) {
-    const int N = zexp_nterms_f(t2, az2) + 6;
-    cf t = cf{ff{1.0f, 0.0f}, ff_zero()};
+    const int M = zexp_nterms_f(t2, az2);
+    const int H = M < 6 ? M : 6;
+    // tail / z^7 in FP32
+    float qr = 0.0f, qi = 0.0f;
+    const float zr = z.re.hi, zi = z.im.hi;
+    if (M >= 7) {
+      qr = c_df.zc32[M];
 #pragma unroll 1
-    for (int k = N; k >= 7; --k) {
-      t = cf_scale(cf_mul(t, z), c_df.inv[k]);
-      t.re = ff_add(t.re, ff{1.0f, 0.0f});
+      for (int m = M - 1; m >= 7; --m) {
+        const float nr = __fmaf_rn(qr, zr, __fmaf_rn(-qi, zi, c_df.zc32[m]));
+        qi = __fmaf_rn(qr, zi, __fmul_rn(qi, zr));
+        qr = nr;
+      }
+    }
+    cf t = cf{c_df.zc[H], ff_zero()};
+#pragma unroll 1
+    for (int m = H - 1; m >= 0; --m) {
+      t = cf_mul(t, z);
+      t.re = ff_add(t.re, c_df.zc[m]);
     }
     cf z5 = cf_mul(z4, z), z6 = cf_mul(z5, z);
+    if (M >= 7) {
+      // z^7 q in FP32, added to the double-float head
+      const float z7r = __fmaf_rn(z6.re.hi, zr, -__fmul_rn(z6.im.hi, zi));
+      const float z7i = __fmaf_rn(z6.re.hi, zi, __fmul_rn(z6.im.hi, zr));
+      t.re = ff_add(t.re, ff{__fmaf_rn(z7r, qr, -__fmul_rn(z7i, qi)), 0.0f});
+      t.im = ff_add(t.im, ff{__fmaf_rn(z7r, qi, __fmul_rn(z7i, qr)), 0.0f});
+    }
     cf e6 = cf_mul(cf_scale(z6, c_df.inv_fact[6]), t);
     E5 = cf_add(e6, cf_scale(z5, c_df.inv_fact[5]));
     E4 = cf_add(E5, cf_scale(z4, c_df.inv_fact[4]));

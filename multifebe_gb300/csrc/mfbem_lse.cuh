@@ -37,10 +37,7 @@ __global__ void __launch_bounds__(128) k_trsv_diag64_h(const S* A, long long str
   S* xg = b + strideb * blockIdx.x;
   extern __shared__ __align__(16) unsigned char smraw[];
   S* D = reinterpret_cast<S*>(smraw);  // D[col * 65 + row] = A(r0 + row, r0 + col)
-  for (int t = threadIdx.x; t < w * 64; t += 128) {
-    const int i = t & 63, j = t >> 6;
-    if (i < w) D[j * 65 + i] = M[(size_t)(r0 + j) * lda + r0 + i];
-  }
+  stage_diag64(M, lda, r0, w, D);
   __syncthreads();
   if (threadIdx.x >= 32) return;
   const int l = threadIdx.x;

@@ -598,6 +598,26 @@ template <> __device__ __forceinline__ double2 shfl_s(double2 v, int src) {
 template <> __device__ __forceinline__ float shfl_s(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 template <> __device__ __forceinline__ double shfl_s(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
+// Stage the w x w diagonal block at (r0, r0) into D[col * 65 + row] with 128
+// threads, eight loads in flight per thread before their stores (the block is
+// usually cold in L2; one load per iteration would serialise on its latency).
+template <typename S>
+__device__ __forceinline__ void stage_diag64(const S* M, int lda, int r0, int w, S* D) {
+  for (int t0 = threadIdx.x; t0 < w * 64; t0 += 128 * 8) {
+    S v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int t = t0 + 128 * u, i = t & 63, j = t >> 6;
+      if (t < w * 64 && i < w) v[u] = M[(size_t)(r0 + j) * lda + r0 + i];
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int t = t0 + 128 * u, i = t & 63, j = t >> 6;
+      if (t < w * 64 && i < w) D[j * 65 + i] = v[u];
+    }
+  }
+}
+
 template <typename S, bool LOWER>
 __global__ void __launch_bounds__(128) k_trsv_diag64(const S* A, long long strideA, int lda, S* b, long long strideb,
                                                      int r0, int w) {
@@ -606,10 +626,7 @@ __global__ void __launch_bounds__(128) k_trsv_diag64(const S* A, long long strid
   S* xg = b + strideb * bidx;
   extern __shared__ __align__(16) unsigned char smraw[];
   S* D = reinterpret_cast<S*>(smraw);  // [col][row], w x w, padded to 65 rows
-  for (int t = threadIdx.x; t < w * 64; t += 128) {
-    const int i = t & 63, j = t >> 6;
-    if (i < w) D[j * 65 + i] = M[(size_t)(r0 + j) * lda + r0 + i];
-  }
+  stage_diag64(M, lda, r0, w, D);
   __syncthreads();
   if (threadIdx.x >= 32) return;
   const int l = threadIdx.x;
@@ -696,6 +713,7 @@ __global__ void k_trsv_update(const S* A, long long strideA, int lda, S* b, long
   int i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= i1) return;
   S acc = Sc<S>::zero();
+#pragma unroll 8
   for (int j = 0; j < w; ++j) acc = Sc<S>::add(acc, Sc<S>::mul(M[(size_t)(r0 + j) * lda + i], xs[j]));
   x[i] = Sc<S>::sub(x[i], acc);
 }
