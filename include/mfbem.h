@@ -173,6 +173,13 @@ int mfbem_internal_points_harela(mfbem_handle* h, const double lambda[2], const 
                                  double omega, int32_t n_ip, const double* x_ip, const double* u_nodes,
                                  const double* t_nodes, double* u_ip, double* sigma_ip);
 
+/* Device memory released with a mesh handle (mfbem_mesh_release) is kept by
+   the library for later handles: buffers of at least 1 MB, up to a quarter of
+   the device memory (environment MFBEM_DEVICE_CACHE_MB overrides the cap; 0
+   disables the cache), with the handles' streams and cuBLAS handles. This
+   returns every cached buffer to the driver. No counterpart in the reference. */
+int mfbem_trim_device_cache(void);
+
 /* Diagnostics of the last mfbem_solve_r / mfbem_solve_c on the calling
    thread, which the reference prints at verbose level 2: rcond (NaN unless
    condition was set with factorize) and per right-hand side the forward-error

@@ -32,7 +32,7 @@ MFBEM_OVERWRITE = 0x2
 ABI_SYMBOLS = [
     "mfbem_mesh_upload", "mfbem_mesh_release", "mfbem_assemble_staela", "mfbem_assemble_harela",
     "mfbem_solve_r", "mfbem_solve_c", "mfbem_solve_report", "mfbem_internal_points_staela",
-    "mfbem_internal_points_harela", "mfbem_sweep_harela", "mfbem_solve_staela", "mfbem_last_stats",
+    "mfbem_internal_points_harela", "mfbem_trim_device_cache", "mfbem_sweep_harela", "mfbem_solve_staela", "mfbem_last_stats",
     "mfbem_last_error", "mfbem_version", "mfbem_solve_c_static",
     "mfbem_qlearn_label", "mfbem_mlp_size", "mfbem_mlp_forward", "mfbem_mlp_loss_grad", "mfbem_mlp_train",
     "mfbem_set_learned_quadrature", "mfbem_sweep_harela_batch",

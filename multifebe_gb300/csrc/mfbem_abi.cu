@@ -13,6 +13,7 @@
 #include <mutex>
 #include <thread>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -61,7 +62,7 @@ struct DevBuf {
 
 struct mfbem_handle {
   DMesh m;
-  std::vector<void*> owned;
+  std::vector<std::pair<void*, size_t>> owned;
   QsCurves* d_qs = nullptr;
   QsCurves* d_q15 = nullptr;
   int ndof = 0, ne = 0, nn = 0;
@@ -81,11 +82,91 @@ struct mfbem_handle {
   double* nodecl = nullptr;
 };
 
+// ---------------------------------------------------------------------------
+// Device memory released with a mesh handle is kept for the next handle: a
+// caller that uploads, sweeps and releases mesh after mesh (or a harmonic
+// driver re-uploading per call) would otherwise pay cudaMalloc / cudaFree of
+// several GB per sweep, and cudaFree synchronises the device. Buffers of at
+// least 1 MB are cached up to a cap (a quarter of the device memory, or
+// MFBEM_DEVICE_CACHE_MB; 0 disables the cache); an allocation takes the
+// smallest cached buffer that fits and is at most twice the request.
+// mfbem_trim_device_cache() returns everything to the driver. Streams and
+// cuBLAS handles of released meshes are reused the same way.
+// ---------------------------------------------------------------------------
+static std::mutex g_pool_mu;
+static std::multimap<size_t, void*> g_pool;
+static size_t g_pool_bytes = 0;
+static long long g_pool_cap = -1;
+static std::vector<std::pair<cudaStream_t, cublasHandle_t>> g_ctx_pool;
+
+static size_t pool_cap() {
+  if (g_pool_cap < 0) {
+    const char* e = getenv("MFBEM_DEVICE_CACHE_MB");
+    if (e) {
+      g_pool_cap = std::max(0LL, atoll(e)) << 20;
+    } else {
+      size_t fr = 0, tot = 0;
+      g_pool_cap = cudaMemGetInfo(&fr, &tot) == cudaSuccess ? (long long)(tot / 4) : 0;
+      cudaGetLastError();
+    }
+  }
+  return (size_t)g_pool_cap;
+}
+// a cached buffer of size in [bytes, 2 bytes], or nullptr; *cap receives its size
+static void* pool_take(size_t bytes, size_t* cap) {
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  auto it = g_pool.lower_bound(bytes);
+  if (it == g_pool.end() || it->first > 2 * bytes) return nullptr;
+  void* p = it->second;
+  *cap = it->first;
+  g_pool_bytes -= it->first;
+  g_pool.erase(it);
+  return p;
+}
+// the caller has synchronised the device with respect to p
+static void pool_give(void* p, size_t bytes) {
+  if (!p) return;
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (bytes >= (1u << 20) && g_pool_bytes + bytes <= pool_cap()) {
+      g_pool.emplace(bytes, p);
+      g_pool_bytes += bytes;
+      return;
+    }
+  }
+  cudaFree(p);
+}
+static cudaError_t pool_malloc(void** p, size_t bytes, size_t* cap) {
+  if (bytes >= (1u << 20) && (*p = pool_take(bytes, cap))) return cudaSuccess;
+  *cap = bytes;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaErrorMemoryAllocation) {
+    // give the cache back to the driver and retry once
+    cudaGetLastError();
+    cudaDeviceSynchronize();
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (auto& kv : g_pool) cudaFree(kv.second);
+    g_pool.clear();
+    g_pool_bytes = 0;
+    e = cudaMalloc(p, bytes);
+  }
+  return e;
+}
+extern "C" int mfbem_trim_device_cache(void) {
+  cudaDeviceSynchronize();
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  for (auto& kv : g_pool) cudaFree(kv.second);
+  g_pool.clear();
+  g_pool_bytes = 0;
+  return 0;
+}
+
 static int dalloc(mfbem_handle* h, void** p, size_t bytes) {
   if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMalloc(p, bytes);
+  size_t cap = 0;
+  cudaError_t e = pool_malloc(p, bytes, &cap);
   if (e != cudaSuccess) return fail(MFBEM_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-  h->owned.push_back(*p);
+  h->owned.emplace_back(*p, cap);
   return 0;
 }
 template <typename T>
@@ -97,12 +178,17 @@ static int dupload(mfbem_handle* h, T** dst, const T* src, size_t n) {
 }
 static int ensure(DevBuf& b, size_t bytes) {
   if (b.bytes >= bytes) return 0;
-  if (b.p) cudaFree(b.p);
+  if (b.p) {
+    // the stream that used it may still run: the cache only takes idle buffers
+    cudaDeviceSynchronize();
+    pool_give(b.p, b.bytes);
+  }
   b.p = nullptr;
   b.bytes = 0;
-  cudaError_t e = cudaMalloc(&b.p, bytes);
+  size_t cap = 0;
+  cudaError_t e = pool_malloc(&b.p, bytes, &cap);
   if (e != cudaSuccess) return fail(MFBEM_ENOMEM, std::string("cudaMalloc(work): ") + cudaGetErrorString(e));
-  b.bytes = bytes;
+  b.bytes = cap;
   return 0;
 }
 
@@ -409,9 +495,19 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   h->stats.points_singular = h->pts_sing;
   h->stats.adaptive_leaves = (int)m.nleaf;
   h->stats.ms_assemble = std::chrono::duration<double, std::milli>(t1 - t0).count();
-  CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
-  if (cublasCreate(&h->blas) != CUBLAS_STATUS_SUCCESS) { mfbem_mesh_release(h); return fail(MFBEM_ECUDA, "cublasCreate"); }
-  cublasSetStream(h->blas, h->st);
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_ctx_pool.empty()) {
+      h->st = g_ctx_pool.back().first;
+      h->blas = g_ctx_pool.back().second;
+      g_ctx_pool.pop_back();
+    }
+  }
+  if (!h->st) {
+    CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    if (cublasCreate(&h->blas) != CUBLAS_STATUS_SUCCESS) { mfbem_mesh_release(h); return fail(MFBEM_ECUDA, "cublasCreate"); }
+    cublasSetStream(h->blas, h->st);
+  }
   *out = h;
   return 0;
 }
@@ -419,12 +515,17 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
 extern "C" int mfbem_mesh_release(mfbem_handle* h) {
   if (!h) return MFBEM_EARG;
   cudaDeviceSynchronize();
-  for (void* p : h->owned) cudaFree(p);
+  for (auto& o : h->owned) pool_give(o.first, o.second);
   for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu, &h->parf,
                     &h->pphi_f, &h->Af, &h->geo_f, &h->gm})
-    if (b->p) cudaFree(b->p);
-  if (h->blas) cublasDestroy(h->blas);
-  if (h->st) cudaStreamDestroy(h->st);
+    pool_give(b->p, b->bytes);
+  if (h->st && h->blas) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    g_ctx_pool.emplace_back(h->st, h->blas);
+  } else {
+    if (h->blas) cublasDestroy(h->blas);
+    if (h->st) cudaStreamDestroy(h->st);
+  }
   delete h;
   return 0;
 }
