@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(NT) k_panel_cluster(S* A, long long strideA, i
   int* xidx = reinterpret_cast<int*>(xval + 2);        // [2]
   __shared__ R sv[NT / 32];
   __shared__ int si[NT / 32];
-  __shared__ int s_p, s_g, s_own;
+  __shared__ int s_p;
   const int mat = blockIdx.x / G;
   const int lane = threadIdx.x & 31, wid = threadIdx.x / 32;
   S* M = A + strideA * mat;
@@ -435,49 +435,60 @@ __global__ void __launch_bounds__(NT) k_panel_cluster(S* A, long long strideA, i
     }
     if (lane == 0) { sv[wid] = best; si[wid] = bi; }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      R b_ = sv[0];
-      int i_ = si[0];
-      for (int w = 1; w < NT / 32; ++w)
-        if (sv[w] > b_ || (sv[w] == b_ && si[w] >= 0 && (i_ < 0 || si[w] < i_))) { b_ = sv[w]; i_ = si[w]; }
-      xval[slot] = b_;
-      xidx[slot] = i_;
-      s_p = i_;
-    }
-    __syncthreads();
-    const int myc = s_p;
-    if ((int)threadIdx.x < kb) {
-      if (myc >= 0) xrow[(slot * 2 + 0) * 32 + threadIdx.x] = pan[(size_t)threadIdx.x * chunk + (myc - r0)];
-      if (jj >= r0 && jj < r1) xrow[(slot * 2 + 1) * 32 + threadIdx.x] = pan[(size_t)threadIdx.x * chunk + (jj - r0)];
+    // the CTA's candidate: warp 0 reduces the warps' (larger |a|, then the
+    // smaller row; no row = -1 loses), then stages it and row jj
+    if (wid == 0) {
+      R v = lane < NT / 32 ? sv[lane] : (R)-1;
+      int ix = lane < NT / 32 ? si[lane] : -1;
+      for (int o = 16; o > 0; o >>= 1) {
+        const R ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, ix, o);
+        if (oi >= 0 && (ix < 0 || ov > v || (ov == v && oi < ix))) { v = ov; ix = oi; }
+      }
+      if (lane == 0) {
+        xval[slot] = v;
+        xidx[slot] = ix;
+      }
+      if (lane < kb) {
+        if (ix >= 0) xrow[(slot * 2 + 0) * 32 + lane] = pan[(size_t)lane * chunk + (ix - r0)];
+        if (jj >= r0 && jj < r1) xrow[(slot * 2 + 1) * 32 + lane] = pan[(size_t)lane * chunk + (jj - r0)];
+      }
     }
     cl.sync();
-    // winner over the cluster's candidates (distributed shared memory)
-    if (threadIdx.x == 0) {
-      R b_ = -1;
-      int i_ = -1, g_ = 0;
-      for (int q = 0; q < G; ++q) {
-        const R v = cl.map_shared_rank(xval, q)[slot];
-        const int ix = cl.map_shared_rank(xidx, q)[slot];
-        if (ix >= 0 && (v > b_ || (v == b_ && ix < i_))) { b_ = v; i_ = ix; g_ = q; }
+    // winner over the cluster's candidates: warp 0 reads the G ranks' slots of
+    // distributed shared memory in parallel (one lane each), reduces with the
+    // same order, fetches the pivot row and interchanges rows p and jj
+    if (wid == 0) {
+      R v = (R)-1;
+      int ix = -1, gq = lane;
+      if (lane < G) {
+        v = cl.map_shared_rank(xval, lane)[slot];
+        ix = cl.map_shared_rank(xidx, lane)[slot];
       }
-      s_p = i_;
-      s_g = g_;
-      s_own = (jj - k) / chunk;  // rank owning row jj
+      for (int o = 16; o > 0; o >>= 1) {
+        const R ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, ix, o);
+        const int og = __shfl_xor_sync(0xffffffffu, gq, o);
+        if (oi >= 0 && (ix < 0 || ov > v || (ov == v && oi < ix))) { v = ov; ix = oi; gq = og; }
+      }
+      const int own = (jj - k) / chunk;  // rank owning row jj
+      if (lane < kb) {
+        const S pr = cl.map_shared_rank(xrow, gq)[(slot * 2 + 0) * 32 + lane];
+        prow[lane] = pr;
+        if (ix != jj) {
+          if (ix >= r0 && ix < r1)
+            pan[(size_t)lane * chunk + (ix - r0)] = cl.map_shared_rank(xrow, own)[(slot * 2 + 1) * 32 + lane];
+          if (jj >= r0 && jj < r1) pan[(size_t)lane * chunk + (jj - r0)] = pr;
+        }
+      }
+      if (lane == 0) s_p = ix;
     }
     __syncthreads();
     const int p = s_p;
-    if ((int)threadIdx.x < kb) prow[threadIdx.x] = cl.map_shared_rank(xrow, s_g)[(slot * 2 + 0) * 32 + threadIdx.x];
-    __syncthreads();
     if (g == 0 && threadIdx.x == 0) {
       piv[jj] = p + 1;
       if (Sc<S>::iszero(prow[j]) && info[mat] == 0) info[mat] = jj + 1;
     }
-    if (p != jj) {
-      if (p >= r0 && p < r1 && (int)threadIdx.x < kb)
-        pan[(size_t)threadIdx.x * chunk + (p - r0)] = cl.map_shared_rank(xrow, s_own)[(slot * 2 + 1) * 32 + threadIdx.x];
-      if (jj >= r0 && jj < r1 && (int)threadIdx.x < kb) pan[(size_t)threadIdx.x * chunk + (jj - r0)] = prow[threadIdx.x];
-    }
-    __syncthreads();
     const S dj = prow[j];
     if (!Sc<S>::iszero(dj)) {
       const S rcp = Sc<S>::rcp(dj);
