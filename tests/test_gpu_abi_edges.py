@@ -117,3 +117,30 @@ def test_upload_rejects_meshes_outside_the_path():
     with pytest.raises(MfbemError) as e:
         BemRegion(d)
     assert e.value.code in (_abi.MFBEM_EUNSUPPORTED, _abi.MFBEM_EARG)
+
+
+def test_released_device_memory_is_reused_safely():
+    """Upload, sweep and release, mesh after mesh of different sizes: the
+    buffers, streams and cuBLAS handles cached from released meshes give the
+    solutions of the first, freshly allocated, handle (a reused buffer with
+    stale contents would show as a large error); trimming the cache
+    returns 0 and a later upload still works."""
+    L = _abi.load()
+    mat = M.viscoelastic(1.0, 0.25, 1.0, 0.05)
+    first = {}
+    for rep in range(2):
+        for n in (3, 4, 3):
+            d = M.cube_clamped_top_traction(n)
+            R = BemRegion(d)
+            om = M.omega_from_a0(np.linspace(0.2, 1.6, 4), mat)
+            X = R.sweep_harela(mat, om, precision="mixed")
+            R.close()
+            if n not in first:
+                first[n] = X
+            else:
+                assert np.abs(X - first[n]).max() <= 1e-12 * np.abs(first[n]).max()
+    assert L.mfbem_trim_device_cache() == 0
+    R = BemRegion(M.cube_clamped_top_traction(3))
+    X = R.sweep_harela(mat, M.omega_from_a0(np.linspace(0.2, 1.6, 4), mat), precision="mixed")
+    R.close()
+    assert np.abs(X - first[3]).max() <= 1e-12 * np.abs(first[3]).max()
