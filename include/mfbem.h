@@ -173,6 +173,22 @@ int mfbem_internal_points_harela(mfbem_handle* h, const double lambda[2], const 
                                  double omega, int32_t n_ip, const double* x_ip, const double* u_nodes,
                                  const double* t_nodes, double* u_ip, double* sigma_ip);
 
+/* Gmsh *.msh 2.2 ASCII reader, host only: the gmsh branch of
+   fbem_mesh%read_from_file (lib/fbem/src/mesh.f90:104-494) with its checks
+   ($MeshFormat 2.2, $PhysicalNames as the parts, element parts = first tag,
+   known element types, unique positive ids). Entities keep the file's order
+   and ids; element nodes are node ids in gmsh order. Returns 0, or -1 with
+   the reason in mfbem_msh_error(). counts = parts, nodes, elements,
+   element-node entries; names: n_parts x name_len bytes, NUL-padded;
+   offsets: [n_elements + 1] into nodes. */
+int mfbem_msh_read(const char* path, void** msh);
+const char* mfbem_msh_error(void);
+int mfbem_msh_sizes(void* msh, int32_t* counts);
+int mfbem_msh_parts(void* msh, int32_t* id, int32_t* dim, char* names, int32_t name_len);
+int mfbem_msh_nodes(void* msh, int32_t* id, double* x);
+int mfbem_msh_elements(void* msh, int32_t* id, int32_t* type, int32_t* part, int32_t* offsets, int32_t* nodes);
+void mfbem_msh_free(void* msh);
+
 /* Device memory released with a mesh handle (mfbem_mesh_release) is kept by
    the library for later handles: buffers of at least 1 MB, up to a quarter of
    the device memory (environment MFBEM_DEVICE_CACHE_MB overrides the cap; 0

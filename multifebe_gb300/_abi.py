@@ -35,7 +35,8 @@ ABI_SYMBOLS = [
     "mfbem_internal_points_harela", "mfbem_trim_device_cache", "mfbem_sweep_harela", "mfbem_solve_staela", "mfbem_last_stats",
     "mfbem_last_error", "mfbem_version", "mfbem_solve_c_static",
     "mfbem_qlearn_label", "mfbem_mlp_size", "mfbem_mlp_forward", "mfbem_mlp_loss_grad", "mfbem_mlp_train",
-    "mfbem_set_learned_quadrature", "mfbem_sweep_harela_batch",
+    "mfbem_set_learned_quadrature", "mfbem_sweep_harela_batch", "mfbem_msh_read", "mfbem_msh_error",
+    "mfbem_msh_sizes", "mfbem_msh_parts", "mfbem_msh_nodes", "mfbem_msh_elements", "mfbem_msh_free",
 ]
 PREP_SYMBOLS = ["mfbem_prep_create", "mfbem_prep_desc", "mfbem_prep_free", "mfbem_prep_dof"]
 
