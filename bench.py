@@ -58,6 +58,11 @@ FP64_NOMINAL_TFLOPS = 1.25
 # 408.1 MB, divided by 2; profiles/k_mixed_cube8x2freq.md). Traffic grows in
 # proportion to the frequencies (one system per frequency).
 REG_TRAFFIC_PER_FREQ = 431.1e6
+# Pipe utilisation of the same launch (ncu --set full, same small case and
+# file): the kernel is bound by instruction issue on the FP32 pipe
+# (double-float arithmetic), not by HBM.
+REG_NCU_PIPES = {"issue_slots_busy_pct": 61.2, "fp32_fma_pipe_pct": 44.3, "fp64_pipe_pct": 3.1,
+                 "source": "profiles/k_mixed_cube8x2freq.md"}
 
 
 def _dist():
@@ -107,7 +112,7 @@ class Clocks:
 
 def cpu_baseline_sample(deck, mat, omega, threads=None):
     """Oracle (reference-equivalent CPU path) assemble + getrf/getrs for one
-    frequency on all host cores. Returns (seconds, cores)."""
+    frequency on all host cores. Returns (seconds, cores, solution)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     cores = threads or os.cpu_count()
@@ -115,8 +120,29 @@ def cpu_baseline_sample(deck, mat, omega, threads=None):
     P = O.Problem(deck)
     t0 = time.perf_counter()
     A, b = P.assemble_harela(mat, omega, nthreads=cores)
-    O.lu_solve(A, b)
-    return time.perf_counter() - t0, cores
+    x = O.lu_solve(A, b, overwrite=True)
+    return time.perf_counter() - t0, cores, x
+
+
+def cpu_sweep_rate(deck, mat, om, samples):
+    """The CPU path's solves/s on a bounded sample of a sweep: one untimed
+    frequency (threads, pages), then `samples` frequencies spread over the
+    sweep, each assembled and solved. The same sampling serves the reference
+    arm and the GPU line's cpu_baseline. Returns (solves/s, cores, seconds)."""
+    cpu_baseline_sample(deck, mat, om[0])
+    idx = [int(round(i * (len(om) - 1) / max(1, samples - 1))) for i in range(samples)] if samples > 1 else [0]
+    ts = []
+    cores = os.cpu_count()
+    for i in idx:
+        t, cores, _ = cpu_baseline_sample(deck, mat, om[i])
+        ts.append(t)
+    return len(ts) / sum(ts), cores, sum(ts)
+
+
+def bench_config(n, nf):
+    """config dict of the headline workload, identical in both arms."""
+    return {"workload": WORKLOAD, "n_dof": n, "frequencies": nf,
+            "l2": "inputs larger than L2 (20 x 192 MB systems per step)"}
 
 
 def run_reference(args):
@@ -125,22 +151,24 @@ def run_reference(args):
         return 0
     from multifebe_gb300 import meshgen as M
     deck, mat, om = M.workload(2)
-    for _ in range(max(1, args.warmup if args.warmup < 2 else 1)):
-        cpu_baseline_sample(deck, mat, om[0])
+    # untimed warm-up frequencies (threads, pages); each a full assemble + solve
+    for i in range(max(1, min(args.warmup, 2))):
+        cpu_baseline_sample(deck, mat, om[i % len(om)])
     ts = []
     cores = os.cpu_count()
     for i in range(args.steps):
-        t, cores = cpu_baseline_sample(deck, mat, om[i % len(om)])
+        t, cores, _ = cpu_baseline_sample(deck, mat, om[i % len(om)])
         ts.append(t)
     tot = sum(ts)
     value = len(ts) / tot
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(ts), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": "one frequency per step", "cores": cores},
+            "config": bench_config(deck.n_dof, len(om)),
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": "assemble + getrf/getrs of one frequency of the sweep per step (oracle restatement "
-                                       "of the Fortran path, OpenMP + OpenBLAS)"},
+                             "sample": "each step assembles and solves (getrf/getrs) one frequency of the sweep, "
+                                       "frequencies taken in turn, after untimed warm-up frequencies (oracle "
+                                       "restatement of the Fortran path, OpenMP + OpenBLAS)"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -234,10 +262,13 @@ def run_gpu(args):
     relerr = max(np.abs(Xm[i] - Xp[i]).max() / np.abs(Xp[i]).max() for i in range(nf))
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "complex128 assembly / complex64 LU + FP64 refinement", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n_dof": n, "frequencies_per_step": nf, "precision": "mixed",
-                       "rel_err_vs_fp64": relerr, "max_backward_error": st["max_backward_error"],
-                       "l2": "inputs larger than L2 (20 x 192 MB systems per step)",
+            "vs_baseline": None,
+            "dtype": "double-float assembly (binary64 x - x_i) into binary64 systems / complex64 LU with 3xTF32 "
+                     "tensor-core updates + FP64 refinement",
+            "data": "synthetic",
+            "config": bench_config(n, nf),
+            "detail": {"precision": "mixed", "rel_err_vs_fp64_gpu": relerr,
+                       "max_backward_error": st["max_backward_error"],
                        "ms_assemble": st["ms_assemble"], "ms_factor": st["ms_factor"], "ms_solve": st["ms_solve"],
                        "ms_regular": st["ms_regular"], "ms_singular": st["ms_singular"],
                        "ms_adaptive": st["ms_adaptive"], "ms_free": st["ms_free"],
@@ -247,6 +278,7 @@ def run_gpu(args):
             "gpu_launches": launches, "clocks": clk,
             "plain_fp64_gpu": {"value": nf / (plain_step / 1e3), "unit": "solves/s", "ms_per_step": plain_step,
                                "ms_factor": sp["ms_factor"], "ms_assemble": sp["ms_assemble"],
+                               "ms_solve": sp["ms_solve"],
                                "speedup_of_mixed": (nf / (per_step_ms / 1e3)) / (nf / (plain_step / 1e3))}}
     line["roofline"] = roofline(st, n, nf)
     if args.precision_form:
@@ -255,11 +287,14 @@ def run_gpu(args):
         line["learned_quadrature"] = learned_quadrature()
     if args.batching:
         line["batching_form"] = batching_form()
-    # cpu baseline: oracle on one frequency (bounded sample)
+    # cpu baseline: the reference arm's sampling on a bounded sample of the sweep
     try:
-        t, cores = cpu_baseline_sample(deck, mat, om[len(om) // 2])
-        line["cpu_baseline"] = {"value": 1.0 / t, "unit": "solves/s", "cores": cores, "kind": "port",
-                                "sample": "assemble + getrf/getrs of one frequency (a0=1.1) on the oracle restatement"}
+        v, cores, secs = cpu_sweep_rate(deck, mat, om, 5)
+        line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
+                                "sample": "5 of the sweep's 20 frequencies spread over a0 0.1..2.0, each "
+                                          "assembled and solved by the oracle restatement (OpenMP + OpenBLAS "
+                                          "getrf/getrs) after one untimed frequency, %.1f s" % secs}
+        line["plain_fp64_gpu"]["speedup_over_cpu"] = line["plain_fp64_gpu"]["value"] / v
     except Exception as ex:  # the oracle must build on the host; report why not
         line["cpu_baseline"] = {"value": None, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"unavailable: {ex}"}
@@ -291,6 +326,7 @@ def roofline(st, n, nf):
             "compute": {"points": pts, "flops_per_point": FLOPS_PER_REGULAR_POINT, "achieved_tflops": tfl,
                         "fp64_nominal_peak_tflops": FP64_NOMINAL_TFLOPS,
                         "frac_of_fp64_nominal": tfl / FP64_NOMINAL_TFLOPS,
+                        "ncu_pipes_of_active_cycles": REG_NCU_PIPES,
                         "note": "SIMT-issue bound (double-float on the FP32 pipe, binary64 only for x - x_i): "
                                 "FP64-equivalent flops above the GPU's whole FP64 rate; HBM and tensor pipes "
                                 "are not the limit of this kernel"}}
@@ -373,29 +409,81 @@ def learned_quadrature():
     return out
 
 
-def precision_form():
-    """The 14883-DOF surface patch at a0=0.5: one mixed solve against one plain
-    FP64 solve on the GPU, and their difference."""
+def _sweep_e2e(R, deck, mat, om, precision, reps):
+    """The public C-ABI from host buffers: mesh upload (H2D) + sweep +
+    solution download (D2H) per repetition. Returns (mean seconds, h2d, d2h)."""
+    from multifebe_gb300 import _abi
+    from multifebe_gb300.bem import _p, PRECISION
+    L = _abi.load()
+    lam = np.array([complex(mat["lambda"]).real, complex(mat["lambda"]).imag])
+    mu = np.array([complex(mat["mu"]).real, complex(mat["mu"]).imag])
+    nu = np.array([complex(mat["nu"]).real, complex(mat["nu"]).imag])
+    omv = np.ascontiguousarray(om, dtype=np.float64)
+    X = np.zeros((len(om), R.n), dtype=np.complex128)
+    ts = []
+    for _ in range(reps):
+        t1 = time.perf_counter()
+        h = ctypes.c_void_p()
+        _abi.check(L.mfbem_mesh_upload(R.desc, ctypes.byref(h)))
+        stt = _abi.Stats()
+        _abi.check(L.mfbem_sweep_harela(h, _p(lam), _p(mu), float(mat["rho"]), _p(nu), len(om), _p(omv),
+                                        PRECISION[precision], 1e-12, _p(X), 0, ctypes.byref(stt)))
+        L.mfbem_mesh_release(h)
+        ts.append(time.perf_counter() - t1)
+    return statistics.mean(ts), _desc_bytes(R.desc.contents, deck), X.nbytes
+
+
+def precision_form(steps=3, warmup=1):
+    """The 14883-DOF surface patch at a0=0.5 (one solve per step).
+    mixed: `steps` device-timed solves after `warmup` untimed ones, and the
+    same through the C-ABI from host buffers (e2e); plain FP64 GPU: one timed
+    solve after an untimed one; CPU: the oracle's assemble + getrf/getrs on
+    all host cores, whose solution is also the FP64 reference of the u and t
+    errors of both GPU paths."""
     from multifebe_gb300 import meshgen as M, BemRegion
     deck, mat, om = M.workload(3)
     R = BemRegion(deck)
-    Xm = R.sweep_harela(mat, om, precision="mixed")
-    Xm = R.sweep_harela(mat, om, precision="mixed")
-    sm = dict(R.last_stats)
+    for _ in range(warmup):
+        R.sweep_harela(mat, om, precision="mixed")
+    tms, st = [], None
+    for _ in range(steps):
+        Xm = R.sweep_harela(mat, om, precision="mixed")
+        st = dict(R.last_stats)
+        tms.append(st["ms_assemble"] + st["ms_factor"] + st["ms_solve"])
+    tm = statistics.mean(tms)
+    e2e_s, h2d, d2h = _sweep_e2e(R, deck, mat, om, "mixed", steps)
+    R.sweep_harela(mat, om, precision="plain")
     Xp = R.sweep_harela(mat, om, precision="plain")
     sp = dict(R.last_stats)
-    R.close()
-    tm = sm["ms_assemble"] + sm["ms_factor"] + sm["ms_solve"]
     tp = sp["ms_assemble"] + sp["ms_factor"] + sp["ms_solve"]
-    return {"workload": WORKLOAD_P, "n_dof": int(Xm.shape[1]),
-            "mixed": {"value": 1e3 / tm, "unit": "solves/s", "ms_assemble": sm["ms_assemble"],
-                      "ms_factor": sm["ms_factor"], "ms_solve": sm["ms_solve"],
-                      "refinement_iterations": sm["refinement_iterations"],
-                      "max_backward_error": sm["max_backward_error"]},
-            "plain_fp64": {"value": 1e3 / tp, "unit": "solves/s", "ms_assemble": sp["ms_assemble"],
-                           "ms_factor": sp["ms_factor"], "ms_solve": sp["ms_solve"]},
-            "speedup_of_mixed": tp / tm,
-            "rel_err_mixed_vs_fp64": float(np.abs(Xm - Xp).max() / np.abs(Xp).max())}
+    out = {"workload": WORKLOAD_P, "n_dof": int(Xm.shape[1]), "steps": steps, "warmup": warmup,
+           "mixed": {"value": 1e3 / tm, "unit": "solves/s", "ms_per_step": tm, "ms_assemble": st["ms_assemble"],
+                     "ms_factor": st["ms_factor"], "ms_solve": st["ms_solve"],
+                     "refinement_iterations": st["refinement_iterations"],
+                     "max_backward_error": st["max_backward_error"],
+                     "e2e": {"value": 1.0 / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                             "d2h_bytes_per_step": d2h}},
+           "plain_fp64_gpu": {"value": 1e3 / tp, "unit": "solves/s", "ms_assemble": sp["ms_assemble"],
+                              "ms_factor": sp["ms_factor"], "ms_solve": sp["ms_solve"]},
+           "speedup_of_mixed": tp / tm,
+           "rel_err_mixed_vs_fp64_gpu": float(np.abs(Xm - Xp).max() / np.abs(Xp).max())}
+    try:
+        t, cores, xo = cpu_baseline_sample(deck, mat, float(om[0]))
+        uo, to = R.solution(xo)
+        errs = {}
+        for name, X in (("mixed", Xm[0]), ("plain_fp64_gpu", Xp[0])):
+            u, tt = R.solution(X)
+            errs[name] = {"u": float(np.abs(u - uo).max() / np.abs(uo).max()),
+                          "t": float(np.abs(tt - to).max() / np.abs(to).max())}
+        out["rel_err_vs_fp64_oracle"] = errs
+        out["cpu_baseline"] = {"value": 1.0 / t, "unit": "solves/s", "cores": cores, "kind": "port",
+                               "sample": "one assemble + getrf/getrs of the patch by the oracle restatement "
+                                         "(OpenMP + OpenBLAS), %.1f s" % t}
+        out["plain_fp64_gpu"]["speedup_over_cpu"] = out["plain_fp64_gpu"]["value"] * t
+    except Exception as ex:
+        out["cpu_baseline"] = {"value": None, "unit": "solves/s", "kind": "port", "sample": f"unavailable: {ex}"}
+    R.close()
+    return out
 
 
 def profile_case(nf):

@@ -12,7 +12,8 @@
 //                  tags, in gmsh order (the reference keeps that order)
 //   $Nodes         ids > 0 and unique; at most 4 words (id and up to three
 //                  coordinates)
-// and element nodes must name declared nodes.
+// element nodes must name declared nodes, and every part holds elements of
+// one dimension (at least one element).
 #include <algorithm>
 #include <cctype>
 #include <cstdint>
@@ -55,6 +56,15 @@ int gmsh_nodes(int type) {
     case 17: return 20;  // hex20
     case 12: return 27;  // hex27
     default: return 0;
+  }
+}
+// dimension of an element of a known gmsh type
+int gmsh_dim(int type) {
+  switch (type) {
+    case 15: return 0;
+    case 1: case 8: case 26: return 1;
+    case 2: case 9: case 3: case 16: case 10: return 2;
+    default: return 3;
   }
 }
 int type_by_name(const std::string& s) {
@@ -182,6 +192,20 @@ bool parse(const std::vector<std::string>& L, Msh& m) {
   }
   for (int32_t v : m.el_nodes)
     if (!node_seen.count(v)) return fail("an element refers to the undeclared node " + std::to_string(v));
+  // each part holds elements of one dimension (mesh.f90:364-372); the
+  // reference reads the dimension of a part's first element, so a part
+  // without elements is refused too
+  for (size_t i = 0; i < m.part_id.size(); ++i) {
+    int dim = -1;
+    for (size_t e = 0; e < m.el_id.size(); ++e) {
+      if (m.el_part[e] != m.part_id[i]) continue;
+      const int d = gmsh_dim(m.el_type[e]);
+      if (dim < 0) dim = d;
+      else if (d != dim)
+        return fail("part " + std::to_string(m.part_id[i]) + " contain elements of different dimensions");
+    }
+    if (dim < 0) return fail("part " + std::to_string(m.part_id[i]) + " contains no elements");
+  }
   return true;
 }
 

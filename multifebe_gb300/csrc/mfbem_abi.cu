@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 #include <chrono>
 #include <cmath>
@@ -35,6 +36,10 @@ static thread_local std::string g_err;
 // kernels of this library launched so far by the calling thread (reported
 // per call in mfbem_stats; per thread so concurrent sweeps count their own)
 static thread_local long long g_launches = 0;
+// iteration limit of the bounded device waits (tcgen05 pipeline mbarriers,
+// cooperative panel barrier); 0 keeps each kernel's own limit. Only the
+// failure-detection test hook mfbem_internal_set_spin_limit changes it.
+static std::atomic<long long> g_spin_limit{0};
 void set_error(const std::string& s) { g_err = s; }
 int fail(int code, const std::string& s) {
   g_err = s;
@@ -55,13 +60,17 @@ using namespace mfb;
     if (s_ != CUBLAS_STATUS_SUCCESS) return fail(MFBEM_ECUDA, std::string(#call) + ": cublas status " + std::to_string((int)s_)); \
   } while (0)
 
+// A device buffer and the device ordinal it was allocated on.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  int dev = -1;
 };
 
 struct mfbem_handle {
   DMesh m;
+  // device ordinal the mesh was uploaded on; every call on the handle needs it current
+  int dev = 0;
   std::vector<std::pair<void*, size_t>> owned;
   QsCurves* d_qs = nullptr;
   QsCurves* d_q15 = nullptr;
@@ -73,6 +82,8 @@ struct mfbem_handle {
   cublasHandle_t blas = nullptr;
   DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, Af, geo_f, gm;
   mfbem_stats stats{};
+  // systems of the last mfbem_sweep_harela call (read back by a test hook)
+  int last_nf = 0;
   long long pts_reg = 0, pts_adp = 0, pts_sing = 0;
   int* d_err = nullptr;
   // internal points: element -> node (0-based), node position and the csize
@@ -94,70 +105,110 @@ struct mfbem_handle {
 // cuBLAS handles of released meshes are reused the same way.
 // ---------------------------------------------------------------------------
 static std::mutex g_pool_mu;
-static std::multimap<size_t, void*> g_pool;
-static size_t g_pool_bytes = 0;
-static long long g_pool_cap = -1;
-static std::vector<std::pair<cudaStream_t, cublasHandle_t>> g_ctx_pool;
+// cached buffers: size -> (device ordinal, pointer); bytes and cap per device
+static std::multimap<size_t, std::pair<int, void*>> g_pool;
+static std::map<int, size_t> g_pool_bytes;
+static std::map<int, long long> g_pool_cap;
+// streams and cuBLAS handles of released meshes: (device, stream, handle)
+static std::vector<std::tuple<int, cudaStream_t, cublasHandle_t>> g_ctx_pool;
 
-static size_t pool_cap() {
-  if (g_pool_cap < 0) {
+static int cur_dev() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return d;
+}
+// runs f with device `dev` current, then restores the caller's device
+template <class F>
+static void on_device(int dev, F f) {
+  const int c = cur_dev();
+  if (c != dev) cudaSetDevice(dev);
+  f();
+  if (c != dev) cudaSetDevice(c);
+}
+// cap of the cache of the current device (set on its first allocation)
+static size_t pool_cap_current(int dev) {
+  auto it = g_pool_cap.find(dev);
+  if (it == g_pool_cap.end()) {
+    long long cap = 0;
     const char* e = getenv("MFBEM_DEVICE_CACHE_MB");
     if (e) {
-      g_pool_cap = std::max(0LL, atoll(e)) << 20;
+      cap = std::max(0LL, atoll(e)) << 20;
     } else {
       size_t fr = 0, tot = 0;
-      g_pool_cap = cudaMemGetInfo(&fr, &tot) == cudaSuccess ? (long long)(tot / 4) : 0;
+      cap = cudaMemGetInfo(&fr, &tot) == cudaSuccess ? (long long)(tot / 4) : 0;
       cudaGetLastError();
     }
+    it = g_pool_cap.emplace(dev, cap).first;
   }
-  return (size_t)g_pool_cap;
+  return (size_t)it->second;
 }
-// a cached buffer of size in [bytes, 2 bytes], or nullptr; *cap receives its size
-static void* pool_take(size_t bytes, size_t* cap) {
+// a cached buffer of device dev of size in [bytes, 2 bytes], or nullptr; *cap receives its size
+static void* pool_take(size_t bytes, int dev, size_t* cap) {
   std::lock_guard<std::mutex> lk(g_pool_mu);
-  auto it = g_pool.lower_bound(bytes);
-  if (it == g_pool.end() || it->first > 2 * bytes) return nullptr;
-  void* p = it->second;
-  *cap = it->first;
-  g_pool_bytes -= it->first;
-  g_pool.erase(it);
-  return p;
+  pool_cap_current(dev);
+  for (auto it = g_pool.lower_bound(bytes); it != g_pool.end() && it->first <= 2 * bytes; ++it) {
+    if (it->second.first != dev) continue;
+    void* p = it->second.second;
+    *cap = it->first;
+    g_pool_bytes[dev] -= it->first;
+    g_pool.erase(it);
+    return p;
+  }
+  return nullptr;
 }
-// the caller has synchronised the device with respect to p
-static void pool_give(void* p, size_t bytes) {
+// p (on device dev) is idle: the caller has synchronised that device
+static void pool_give(void* p, size_t bytes, int dev) {
   if (!p) return;
   {
     std::lock_guard<std::mutex> lk(g_pool_mu);
-    if (bytes >= (1u << 20) && g_pool_bytes + bytes <= pool_cap()) {
-      g_pool.emplace(bytes, p);
-      g_pool_bytes += bytes;
+    auto cap = g_pool_cap.find(dev);
+    if (bytes >= (1u << 20) && cap != g_pool_cap.end() && g_pool_bytes[dev] + bytes <= (size_t)cap->second) {
+      g_pool.emplace(bytes, std::make_pair(dev, p));
+      g_pool_bytes[dev] += bytes;
       return;
     }
   }
-  cudaFree(p);
+  on_device(dev, [&]() { cudaFree(p); });
+}
+// frees the cached buffers of device dev (every device if dev < 0); g_pool_mu held
+static void pool_drop_locked(int dev) {
+  for (auto it = g_pool.begin(); it != g_pool.end();) {
+    if (dev >= 0 && it->second.first != dev) {
+      ++it;
+      continue;
+    }
+    const int d = it->second.first;
+    void* q = it->second.second;
+    on_device(d, [&]() { cudaFree(q); });
+    g_pool_bytes[d] -= it->first;
+    it = g_pool.erase(it);
+  }
 }
 static cudaError_t pool_malloc(void** p, size_t bytes, size_t* cap) {
-  if (bytes >= (1u << 20) && (*p = pool_take(bytes, cap))) return cudaSuccess;
+  const int dev = cur_dev();
+  if (bytes >= (1u << 20) && (*p = pool_take(bytes, dev, cap))) return cudaSuccess;
   *cap = bytes;
   cudaError_t e = cudaMalloc(p, bytes);
   if (e == cudaErrorMemoryAllocation) {
-    // give the cache back to the driver and retry once
+    // give this device's cache back to the driver and retry once
     cudaGetLastError();
     cudaDeviceSynchronize();
     std::lock_guard<std::mutex> lk(g_pool_mu);
-    for (auto& kv : g_pool) cudaFree(kv.second);
-    g_pool.clear();
-    g_pool_bytes = 0;
+    pool_drop_locked(dev);
     e = cudaMalloc(p, bytes);
   }
   return e;
 }
 extern "C" int mfbem_trim_device_cache(void) {
-  cudaDeviceSynchronize();
   std::lock_guard<std::mutex> lk(g_pool_mu);
-  for (auto& kv : g_pool) cudaFree(kv.second);
-  g_pool.clear();
-  g_pool_bytes = 0;
+  std::vector<int> devs;
+  for (auto& kv : g_pool)
+    if (std::find(devs.begin(), devs.end(), kv.second.first) == devs.end()) devs.push_back(kv.second.first);
+  for (int d : devs) on_device(d, []() { cudaDeviceSynchronize(); });
+  pool_drop_locked(-1);
   return 0;
 }
 
@@ -176,12 +227,15 @@ static int dupload(mfbem_handle* h, T** dst, const T* src, size_t n) {
   if (n) CK(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
   return 0;
 }
+// b holds at least `bytes` on the current device (a buffer of another device,
+// or one too small, goes back to its device's cache first)
 static int ensure(DevBuf& b, size_t bytes) {
-  if (b.bytes >= bytes) return 0;
+  const int dev = cur_dev();
+  if (b.p && b.dev == dev && b.bytes >= bytes) return 0;
   if (b.p) {
     // the stream that used it may still run: the cache only takes idle buffers
-    cudaDeviceSynchronize();
-    pool_give(b.p, b.bytes);
+    on_device(b.dev, []() { cudaDeviceSynchronize(); });
+    pool_give(b.p, b.bytes, b.dev);
   }
   b.p = nullptr;
   b.bytes = 0;
@@ -189,6 +243,15 @@ static int ensure(DevBuf& b, size_t bytes) {
   cudaError_t e = pool_malloc(&b.p, bytes, &cap);
   if (e != cudaSuccess) return fail(MFBEM_ENOMEM, std::string("cudaMalloc(work): ") + cudaGetErrorString(e));
   b.bytes = cap;
+  b.dev = dev;
+  return 0;
+}
+// calls on a handle run on the device it was uploaded on
+static int check_dev(const mfbem_handle* h) {
+  const int d = cur_dev();
+  if (d != h->dev)
+    return fail(MFBEM_EARG, "the mesh handle belongs to device " + std::to_string(h->dev) + " but device " +
+                                std::to_string(d) + " is current: make its device current (cudaSetDevice) first");
   return 0;
 }
 
@@ -229,6 +292,7 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   int rc = init_tables();
   if (rc) return rc;
   mfbem_handle* h = new mfbem_handle();
+  h->dev = cur_dev();
   h->ndof = ndof;
   h->ne = ne;
   h->nn = nn;
@@ -497,11 +561,13 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   h->stats.ms_assemble = std::chrono::duration<double, std::milli>(t1 - t0).count();
   {
     std::lock_guard<std::mutex> lk(g_pool_mu);
-    if (!g_ctx_pool.empty()) {
-      h->st = g_ctx_pool.back().first;
-      h->blas = g_ctx_pool.back().second;
-      g_ctx_pool.pop_back();
-    }
+    for (size_t i = g_ctx_pool.size(); i-- > 0;)
+      if (std::get<0>(g_ctx_pool[i]) == h->dev) {
+        h->st = std::get<1>(g_ctx_pool[i]);
+        h->blas = std::get<2>(g_ctx_pool[i]);
+        g_ctx_pool.erase(g_ctx_pool.begin() + i);
+        break;
+      }
   }
   if (!h->st) {
     CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
@@ -514,18 +580,20 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
 
 extern "C" int mfbem_mesh_release(mfbem_handle* h) {
   if (!h) return MFBEM_EARG;
-  cudaDeviceSynchronize();
-  for (auto& o : h->owned) pool_give(o.first, o.second);
-  for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu, &h->parf,
-                    &h->pphi_f, &h->Af, &h->geo_f, &h->gm})
-    pool_give(b->p, b->bytes);
-  if (h->st && h->blas) {
-    std::lock_guard<std::mutex> lk(g_pool_mu);
-    g_ctx_pool.emplace_back(h->st, h->blas);
-  } else {
-    if (h->blas) cublasDestroy(h->blas);
-    if (h->st) cudaStreamDestroy(h->st);
-  }
+  on_device(h->dev, [&]() {
+    cudaDeviceSynchronize();
+    for (auto& o : h->owned) pool_give(o.first, o.second, h->dev);
+    for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu, &h->parf,
+                      &h->pphi_f, &h->Af, &h->geo_f, &h->gm})
+      pool_give(b->p, b->bytes, b->dev);
+    if (h->st && h->blas) {
+      std::lock_guard<std::mutex> lk(g_pool_mu);
+      g_ctx_pool.emplace_back(h->dev, h->st, h->blas);
+    } else {
+      if (h->blas) cublasDestroy(h->blas);
+      if (h->st) cudaStreamDestroy(h->st);
+    }
+  });
   delete h;
   return 0;
 }
@@ -640,6 +708,7 @@ static int assemble_common(mfbem_handle* h, const void* polp, const double* nu_h
                            int flags) {
   const int n = h->ndof;
   if (lda < n) return fail(MFBEM_EARG, "lda < n_dof");
+  if (int rd = check_dev(h)) return rd;
   const size_t es = CPLX ? 16 : 8;
   int rc;
   if ((rc = ensure(h->nu, 2 * sizeof(double)))) return rc;
@@ -657,6 +726,7 @@ static int assemble_common(mfbem_handle* h, const void* polp, const double* nu_h
     }
   } else {
     if ((rc = ensure(h->A, (size_t)n * n * es)) || (rc = ensure(h->b, n * es))) return rc;
+    h->last_nf = 0;  // the sweep systems are overwritten
     dA = (double*)h->A.p;
     db = (double*)h->b.p;
     dlda = n;
@@ -806,6 +876,7 @@ extern "C" int mfbem_internal_points_staela(mfbem_handle* h, double mu, double n
   g_err.clear();
   if (!h || n_ip < 0 || (n_ip > 0 && (!x_ip || !u_nodes || !t_nodes || !u_ip || !sigma_ip)))
     return fail(MFBEM_EARG, "invalid argument");
+  if (int rd = check_dev(h)) return rd;
   if (n_ip == 0) return 0;
   IpStatic pol;
   pol.k = staela_params(mu, nu);
@@ -824,6 +895,7 @@ extern "C" int mfbem_internal_points_harela(mfbem_handle* h, const double lambda
   g_err.clear();
   if (!h || !lambda || !mu || n_ip < 0 || (n_ip > 0 && (!x_ip || !u_nodes || !t_nodes || !u_ip || !sigma_ip)))
     return fail(MFBEM_EARG, "invalid argument");
+  if (int rd = check_dev(h)) return rd;
   if (n_ip == 0) return 0;
   TmpBufs tb;
   HarParD* pd;
@@ -918,7 +990,7 @@ extern "C" int mfbem_internal_tc_cgemm(int32_t m, int32_t n, int32_t k, const fl
     if (staged) {
       dim3 g(nblk(m, TC_BM / 2), nblk(n, TC_BN), 1);
       k_tc_cgemm<<<g, 128, TC_SMEM>>>((const float2*)dA.p, m, 0, (const float2*)dB.p, std::max(k, 1), 0,
-                                      (float2*)dC.p, m, 0, m, n, k, (int*)dE.p);
+                                      (float2*)dC.p, m, 0, m, n, k, (int*)dE.p, g_spin_limit.load());
       ++g_launches;
     } else if ((rc = tc_cgemm_run(0, (const float2*)dA.p, m, 0, (const float2*)dB.p, std::max(k, 1), 0,
                                   (float2*)dC.p, m, 0, m, n, k, 1, ws, (int*)dE.p))) {
@@ -933,6 +1005,32 @@ extern "C" int mfbem_internal_tc_cgemm(int32_t m, int32_t n, int32_t k, const fl
   cleanup();
   if (e != cudaSuccess) return fail(MFBEM_ECUDA, std::string("tc cgemm: ") + cudaGetErrorString(e));
   if (herr) return fail(MFBEM_ETIMEOUT, "tc cgemm: an MMA completion wait timed out");
+  return 0;
+}
+
+// Test hook (not part of the reference interface): sets the iteration limit
+// of the bounded device waits (0 restores each kernel's own), so that a test
+// can make a wait give up and check the error status, the freed resources
+// and the next call. Nothing of the kernels' work is skipped.
+extern "C" int mfbem_internal_set_spin_limit(int64_t iterations) {
+  if (iterations < 0) return fail(MFBEM_EARG, "negative limit");
+  g_spin_limit.store(iterations);
+  return 0;
+}
+
+// Test hook (not part of the reference interface): system f of the handle's
+// last mfbem_sweep_harela call, A (n x n column-major complex128) and b.
+// After a mixed-precision sweep A is the assembled binary64 system (its
+// factors live in the complex64 copy); after a plain sweep A holds the FP64
+// LU factors.
+extern "C" int mfbem_internal_sweep_system(mfbem_handle* h, int32_t f, double* A_out, double* b_out) {
+  g_err.clear();
+  if (!h || !A_out || !b_out || f < 0 || f >= h->last_nf) return fail(MFBEM_EARG, "no such system in the last sweep");
+  if (int rd = check_dev(h)) return rd;
+  const size_t n = (size_t)h->ndof, nn = n * n;
+  CK(cudaMemcpyAsync(A_out, (const double2*)h->A.p + nn * f, sizeof(double2) * nn, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(b_out, (const double2*)h->b.p + n * f, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
   return 0;
 }
 
@@ -1176,6 +1274,7 @@ extern "C" int mfbem_set_learned_quadrature(mfbem_handle* h, const float* w, dou
                                             double kcl, int32_t* n_learned) {
   g_err.clear();
   if (!h || kernel < 0 || kernel > 1) return fail(MFBEM_EARG, "invalid argument");
+  if (int rd = check_dev(h)) return rd;
   DMesh& m = h->m;
   if (n_learned) *n_learned = 0;
   if (m.nadp == 0) return 0;
@@ -1225,6 +1324,7 @@ extern "C" int mfbem_set_learned_quadrature(mfbem_handle* h, const float* w, dou
   if (h->geo_f.p) cudaFree(h->geo_f.p);
   h->geo_f.p = nullptr;
   h->geo_f.bytes = 0;
+  h->geo_f.dev = -1;
   CK(cudaGetLastError());
   CK(cudaDeviceSynchronize());
   if (n_learned && w) {

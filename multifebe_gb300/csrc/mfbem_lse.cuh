@@ -612,22 +612,36 @@ struct SolveCtx {
   cublasHandle_t hb = nullptr;
   DevBuf A, b, ipiv, info, Ao, bc, wv;
 };
-static SolveCtx* g_solve = nullptr;
+// one context per device ordinal (the stream and cuBLAS handle belong to it)
+static std::map<int, SolveCtx*> g_solve;
 static std::mutex g_solve_mu;
 static int solve_ctx(SolveCtx** out) {
   std::lock_guard<std::mutex> lk(g_solve_mu);
-  if (!g_solve) {
-    int nd = 0;
-    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) return fail(MFBEM_ECUDA, "no CUDA device");
+  int nd = 0;
+  if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) return fail(MFBEM_ECUDA, "no CUDA device");
+  const int dev = cur_dev();
+  auto it = g_solve.find(dev);
+  if (it == g_solve.end()) {
     int rc = init_tables();
     if (rc) return rc;
     SolveCtx* c = new SolveCtx();
     CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
     if (cublasCreate(&c->hb) != CUBLAS_STATUS_SUCCESS) return fail(MFBEM_ECUDA, "cublasCreate");
     cublasSetStream(c->hb, c->st);
-    g_solve = c;
+    it = g_solve.emplace(dev, c).first;
   }
-  *out = g_solve;
+  *out = it->second;
+  return 0;
+}
+
+// Pivots handed back by a caller (factorize = 0) must be what getrf leaves:
+// 1-based, row j interchanged with ipiv(j) in [j, n]; any other value would
+// make the row interchanges of the solve read and write outside the vectors.
+static int check_ipiv(int32_t n, const int32_t* ipiv) {
+  for (int32_t j = 0; j < n; ++j)
+    if (ipiv[j] < j + 1 || ipiv[j] > n)
+      return fail(MFBEM_EARG, "ipiv(" + std::to_string(j + 1) + ") = " + std::to_string(ipiv[j]) +
+                                  " is not a pivot of getrf (must lie in [" + std::to_string(j + 1) + ", n])");
   return 0;
 }
 
@@ -643,6 +657,7 @@ static int solve_dropin(int32_t n, double* A, int32_t* ipiv, int32_t aodim, doub
   if (scaling && (!equed || !r || !c)) return fail(MFBEM_EARG, "scaling needs equed, r and c");
   if (scaling && !factorize && *equed != 'N' && *equed != 'R' && *equed != 'C' && *equed != 'B')
     return fail(MFBEM_EARG, "invalid value of equed");
+  if (!factorize && check_ipiv(n, ipiv)) return MFBEM_EARG;
   SolveCtx* cx;
   int rc = solve_ctx(&cx);
   if (rc) return rc;

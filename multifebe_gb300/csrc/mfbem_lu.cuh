@@ -254,7 +254,7 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 template <typename S, int NT>
 __global__ void __launch_bounds__(NT) k_panel_coop(S* A, long long strideA, int lda, int n, int k, int kb, int G,
                                                    int chunk, int b0, int* ipiv, int* info, unsigned* ctr, S* xrow,
-                                                   typename Sc<S>::R* xval, int* xidx, int* err) {
+                                                   typename Sc<S>::R* xval, int* xidx, int* err, long long spin) {
   typedef typename Sc<S>::R R;
   extern __shared__ __align__(16) unsigned char smraw[];
   S* pan = reinterpret_cast<S*>(smraw);  // [kb][chunk]
@@ -316,8 +316,9 @@ __global__ void __launch_bounds__(NT) k_panel_coop(S* A, long long strideA, int 
       const unsigned target = (unsigned)(jj + 1) * (unsigned)G;
       long long it = 0;
       int ok = 1;
+      const long long lim = spin > 0 ? spin : kCoopSpin;
       while (ld_acquire_u32(ctr + mat) < target) {
-        if (++it > kCoopSpin) { ok = 0; atomicExch(err, 1); break; }
+        if (++it > lim) { ok = 0; atomicExch(err, 1); break; }
         __nanosleep(32);
       }
       __threadfence();

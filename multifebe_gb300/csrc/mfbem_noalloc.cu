@@ -96,6 +96,14 @@ extern "C" int mfbem_solve_c_static(int32_t n, double* A, int32_t* ipiv, int32_t
   if ((size_t)n > kMaxN || (size_t)n_rhs > kMaxRhs)
     return mfb::fail(MFBEM_EARG, "mfbem_solve_c_static: n must be <= " + std::to_string(kMaxN) + " and n_rhs <= " +
                                      std::to_string(kMaxRhs) + " (fixed no-allocation working set)");
+  if (!factorize) {
+    // pivots handed back must be getrf's (1-based, ipiv(j) in [j, n]): the
+    // row interchanges of the solve index the vectors with them
+    for (int32_t j = 0; j < n; ++j)
+      if (ipiv[j] < j + 1 || ipiv[j] > n)
+        return mfb::fail(MFBEM_EARG, "ipiv(" + std::to_string(j + 1) + ") = " + std::to_string(ipiv[j]) +
+                                         " is not a pivot of getrf (must lie in [" + std::to_string(j + 1) + ", n])");
+  }
   unsigned char* base = nullptr;
   int rc = scratch_for_current_device(&base);
   if (rc) return rc;

@@ -28,6 +28,12 @@ static int raise_smem_limit(const void* f) {
 // ---------------------------------------------------------------------------
 // GEMM dispatch for the trailing update A22 -= L21 U12 (plain library GEMM)
 // ---------------------------------------------------------------------------
+// ipiv[b][j] = j + 1
+__global__ void k_ipiv_identity(int* ipiv, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) ipiv[(size_t)n * blockIdx.y + j] = j + 1;
+}
+
 // Compute type of the single-precision trailing updates of the mixed LU:
 // 0 SIMT FP32 (cuBLAS), 1 cuBLAS TF32 tensor cores (TF32-accurate factors;
 // refinement in FP64 restores the accuracy and escalates to SIMT FP32 when it
@@ -63,7 +69,8 @@ static int tc_cgemm_run(cudaStream_t st, const float2* A, int lda, long long sA,
   ++g_launches;
   k_tc_prep_b<<<(unsigned)std::min<size_t>((wb + 255) / 256, 152 * 32), 256, 0, st>>>(B, ldb, sB, k, n, nnt, nkc, batch, bhi, blo);
   ++g_launches;
-  k_tc_cgemm_bulk<<<dim3(nmt, nnt, batch), 128, TC_SMEM2, st>>>(ahi, alo, bhi, blo, nmt, nnt, nkc, C, ldc, sC, m, n, err);
+  k_tc_cgemm_bulk<<<dim3(nmt, nnt, batch), 128, TC_SMEM2, st>>>(ahi, alo, bhi, blo, nmt, nnt, nkc, C, ldc, sC, m, n, err,
+                                                                 g_spin_limit.load());
   ++g_launches;
   CK(cudaGetLastError());
   return 0;
@@ -173,6 +180,9 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
   // panel width: the L11 block of the TRSM lives in shared memory (<= 16 KB)
   const int nb = 32;
   CK(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
+  // pivots start as the identity: a panel that gives up on a bounded wait
+  // leaves valid row indices behind for the interchanges that follow
+  k_ipiv_identity<<<dim3(nblk(n, 256), batch), 256, 0, st>>>(ipiv, n); ++g_launches;
   typedef typename Sc<S>::R R;
   const bool tc = g_c32_mode == 3 && std::is_same<S, float2>::value;
   if (tc) {
@@ -263,7 +273,9 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
           const int nbm = std::min(pl.group, batch - b0);
           int Gp = pl.G, ck = chunk, kk = k, kbb = kb, nn_ = n, ldaa = lda, bb0 = b0;
           long long sAA = sA;
-          void* args[] = {&A, &sAA, &ldaa, &nn_, &kk, &kbb, &Gp, &ck, &bb0, &ipiv, &info, &ctr, &xrow, &xval, &xidx, &derr};
+          long long spin = g_spin_limit.load();
+          void* args[] = {&A, &sAA, &ldaa, &nn_, &kk, &kbb, &Gp, &ck, &bb0, &ipiv, &info, &ctr, &xrow, &xval, &xidx, &derr,
+                          &spin};
           std::unique_lock<std::mutex> lk(g_coop_mu, std::defer_lock);
           if (g_concurrent) lk.lock();
           CK(cudaLaunchCooperativeKernel((const void*)k_panel_coop<S, 256>, dim3(pl.G * nbm), dim3(256), args,
@@ -1112,6 +1124,7 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
                                   double rel_tol, double* x_out, int32_t flags, mfbem_stats* stats) {
   g_err.clear();
   if (!h || !lambda || !mu || !nu || !omega || !x_out || n_freq < 1) return fail(MFBEM_EARG, "invalid argument");
+  if (int rd = check_dev(h)) return rd;
   if (precision < 0 || precision > 2) return fail(MFBEM_EARG, "precision must be 0, 1 or 2");
   const int n = h->ndof;
   const long long nn = (long long)n * n;
@@ -1142,6 +1155,7 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   double2* A = (double2*)h->A.p;
   double2* b = (double2*)h->b.p;
   double2* x = (flags & MFBEM_DEVICE_PTRS) ? (double2*)x_out : (double2*)h->x.p;
+  h->last_nf = n_freq;
   // the assembly time covers zeroing the systems too
   cudaEvent_t a0, a1;
   cudaEventCreate(&a0);
@@ -1212,6 +1226,7 @@ extern "C" int mfbem_solve_staela(mfbem_handle* h, double mu, double nu, int32_t
                                   double* x_out, int32_t flags, mfbem_stats* stats) {
   g_err.clear();
   if (!h || !x_out) return fail(MFBEM_EARG, "invalid argument");
+  if (int rd = check_dev(h)) return rd;
   if (precision < 0 || precision > 2) return fail(MFBEM_EARG, "precision must be 0, 1 or 2");
   const int n = h->ndof;
   const long long nn = (long long)n * n;

@@ -56,8 +56,12 @@ __host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
-  for (long long it = 0; it < TC_SPIN; ++it) {
+// Spin limit of the waits on mbarriers: `spin` iterations (<= 0: TC_SPIN).
+// A wait that gives up makes the kernel set its error flag; the waits that
+// then drain the copies and MMAs still in flight use the full TC_SPIN.
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity, long long spin = 0) {
+  const long long lim = spin > 0 ? spin : TC_SPIN;
+  for (long long it = 0; it < lim; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -72,7 +76,7 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
 // C (m x n complex, ldc) -= A (m x k, lda) B (k x n, ldb), batch in blockIdx.z
 __global__ void __launch_bounds__(128, 1) k_tc_cgemm(const float2* A, int lda, long long sA, const float2* B, int ldb,
                                                      long long sB, float2* C, int ldc, long long sC, int m, int n,
-                                                     int k, int* err) {
+                                                     int k, int* err, long long spin) {
   extern __shared__ __align__(1024) unsigned char tsm[];
   unsigned char* Ahi = tsm;
   unsigned char* Alo = tsm + TC_TILE_BYTES;
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm(const float2* A, int lda, l
                    : "memory");
     }
     // the tiles are reused by the next chunk: wait for this chunk's MMAs
-    if (!tc_wait(mb, (uint32_t)phase)) {
+    if (!tc_wait(mb, (uint32_t)phase, spin)) {
       if (t == 0) atomicExch(err, 1);
       s_ok = 0;
     }
@@ -205,8 +209,9 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm(const float2* A, int lda, l
       }
     }
   } else if (!s_ok && threadIdx.x == 0) {
-    // give in-flight MMAs a bounded chance to finish before the TMEM is freed
-    tc_wait(mb, (uint32_t)phase);
+    // the MMAs of the chunk whose wait gave up (phase toggled since): let
+    // them finish (full limit) before the TMEM is freed
+    tc_wait(mb, (uint32_t)(phase ^ 1));
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -310,7 +315,7 @@ __device__ __forceinline__ void tc_expect(uint32_t mbar, uint32_t bytes) {
 __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, const uint32_t* Alo,
                                                           const uint32_t* Bhi, const uint32_t* Blo, int nmt, int nnt,
                                                           int nkc, float2* C, int ldc, long long sC, int m, int n,
-                                                          int* err) {
+                                                          int* err, long long spin) {
   extern __shared__ __align__(1024) unsigned char tsm[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(tsm + 2 * TQ_STAGE_BYTES);  // fb[2], mb[2]
   uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + 2 * TQ_STAGE_BYTES + 32);
@@ -340,7 +345,9 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
   const uint32_t idesc = tc_idesc(TC_BM, TC_BN);
-  int issued = 0;  // chunks whose MMAs were issued
+  int issued = 0;  // chunks whose MMAs were issued (the last commit covers all)
+  int loaded = 0;  // chunks whose bulk copies were issued
+  int landed = 0;  // chunks whose copies were waited for
   if (t == 0) {
     auto load = [&](int kc, int sidx) {
       const uint32_t d = st0 + sidx * TQ_STAGE_BYTES;
@@ -349,6 +356,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
       tc_bulk(d + TQ_TILE_BYTES, Alo + ta0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
       tc_bulk(d + 2 * TQ_TILE_BYTES, Bhi + tb0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
       tc_bulk(d + 3 * TQ_TILE_BYTES, Blo + tb0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
+      loaded = kc + 1;
     };
     bool ok = true;
     if (nkc > 0) load(0, 0);
@@ -356,10 +364,11 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
       const int s = kc & 1;
       if (kc + 1 < nkc) {
         // stage s^1 was read by the MMAs of chunk kc - 1
-        if (kc >= 1 && !tc_wait(mb[s ^ 1], (uint32_t)(((kc - 1) >> 1) & 1))) { ok = false; break; }
+        if (kc >= 1 && !tc_wait(mb[s ^ 1], (uint32_t)(((kc - 1) >> 1) & 1), spin)) { ok = false; break; }
         load(kc + 1, s ^ 1);
       }
-      if (!tc_wait(fb[s], (uint32_t)((kc >> 1) & 1))) { ok = false; break; }
+      if (!tc_wait(fb[s], (uint32_t)((kc >> 1) & 1), spin)) { ok = false; break; }
+      landed = kc + 1;
       const uint32_t ah = st0 + s * TQ_STAGE_BYTES, al = ah + TQ_TILE_BYTES, bh = ah + 2 * TQ_TILE_BYTES,
                      bl = ah + 3 * TQ_TILE_BYTES;
 #pragma unroll
@@ -384,12 +393,14 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
       issued = kc + 1;
     }
     // the last commit covers every earlier MMA
-    if (ok && issued > 0 && !tc_wait(mb[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1))) ok = false;
+    if (ok && issued > 0 && !tc_wait(mb[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1), spin)) ok = false;
     if (!ok) {
       atomicExch(err, 1);
       s_ok = 0;
-      // bounded chance for the copies and MMAs in flight before the TMEM is freed
+      // drain (full limit) before the shared memory and the TMEM are given up:
+      // the MMAs issued so far, then the bulk copies not yet waited for
       if (issued > 0) tc_wait(mb[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1));
+      for (int c = landed; c < loaded; ++c) tc_wait(fb[c & 1], (uint32_t)((c >> 1) & 1));
     }
   }
   __syncthreads();

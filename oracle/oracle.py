@@ -199,11 +199,19 @@ class Problem:
         return u, t
 
 
-def lu_solve(A, b, threads=None):
-    """getrf + getrs (partial pivoting) through scipy's OpenBLAS."""
+def lu_solve(A, b, threads=None, overwrite=False, rcond=False):
+    """getrf + getrs (partial pivoting) through scipy's OpenBLAS. overwrite:
+    factorise A in place (no copy of a large system); rcond: also return
+    LAPACK's ?gecon estimate of the reciprocal one-norm condition number."""
     import scipy.linalg as sl
-    lu, piv = sl.lu_factor(A, overwrite_a=False, check_finite=False)
-    return sl.lu_solve((lu, piv), b, check_finite=False)
+    anorm = float(np.abs(A).sum(axis=0).max()) if rcond else 0.0
+    lu, piv = sl.lu_factor(A, overwrite_a=overwrite, check_finite=False)
+    x = sl.lu_solve((lu, piv), b, check_finite=False)
+    if not rcond:
+        return x
+    con = sl.lapack.zgecon if np.iscomplexobj(lu) else sl.lapack.dgecon
+    rc, info = con(lu, anorm, norm="1")
+    return x, float(rc)
 
 
 def gauss_tables():

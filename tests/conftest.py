@@ -7,7 +7,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-REFERENCE = "/root/reference"
+# sources of the reference (MultiFEBE) for the tests that read its tutorial
+# files; those tests are skipped when the variable is unset
+REFERENCE = os.environ.get("MULTIFEBE_REFERENCE_DIR", "")
 
 
 def pytest_configure(config):
@@ -52,6 +54,6 @@ def oracle():
 
 @pytest.fixture(scope="session")
 def reference_dir():
-    if not os.path.isdir(REFERENCE):
-        pytest.skip("reference sources not present")
+    if not REFERENCE or not os.path.isdir(REFERENCE):
+        pytest.skip("reference sources not present (set MULTIFEBE_REFERENCE_DIR)")
     return REFERENCE

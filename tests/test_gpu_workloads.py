@@ -1,0 +1,140 @@
+"""The benchmark workloads at their own sizes, device against the oracle
+(through the C-ABI sweep, mfbem_sweep_harela / mfbem_sweep_harela_batch).
+
+  cube 8x8 per face, 3462 DOF, all 20 frequencies a0 = 0.1..2.0
+  thin slab 16x16 + 16x1 per face, 5190 DOF, a0 = 0.2 and 1.0
+  cubes n x n per face, n = 5, 6, 7, 10 (1356 .. 5406 DOF), one frequency each
+  surface patch 40x40, 14883 DOF, a0 = 0.5: displacements u and tractions t
+  compared separately
+
+Tolerances (max-norm relative, per frequency): plain FP64 path <= 1e-10
+(<= 1e-12 / rcond on the slab, whose systems are the least well conditioned:
+the FP64 method's own sensitivity, printed beside the measured error); mixed
+path (complex64 LU + FP64 refinement) <= 1e-8. The mixed path's assembled
+binary64 system (double-float evaluation) is compared entry by entry with the
+oracle's system on two small meshes.
+"""
+import numpy as np
+import pytest
+
+from multifebe_gb300 import meshgen as M, BemRegion, sweep_harela_batch
+from multifebe_gb300 import _abi
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _oracle_sweep(oracle, deck, mat, om, rcond=False):
+    P = oracle.Problem(deck)
+    out = []
+    for w in om:
+        A, b = P.assemble_harela(mat, float(w))
+        out.append(oracle.lu_solve(A, b, overwrite=True, rcond=rcond))
+        del A
+    return P, out
+
+
+@pytest.fixture(scope="module")
+def cube8(oracle):
+    deck, mat, om = M.workload(2)
+    P, xs = _oracle_sweep(oracle, deck, mat, om)
+    return deck, mat, om, P, xs
+
+
+@pytest.mark.parametrize("precision,tol", [("plain", 1e-10), ("mixed", 1e-8)])
+def test_cube8_sweep_all_frequencies(cube8, precision, tol):
+    deck, mat, om, P, xs = cube8
+    R = BemRegion(deck)
+    X = R.sweep_harela(mat, om, precision=precision)
+    errs = [rel(X[i], xs[i]) for i in range(len(om))]
+    print(precision, "max rel err over 20 frequencies", max(errs))
+    assert max(errs) < tol, errs
+    for i in (0, len(om) // 2, len(om) - 1):
+        u, t = R.solution(X[i])
+        uo, to = P.solution(xs[i])
+        assert rel(u, uo) < tol and rel(t, to) < tol
+    if precision == "mixed":
+        assert R.last_stats["max_backward_error"] <= 1e-12
+    R.close()
+
+
+@pytest.fixture(scope="module")
+def slab16(oracle):
+    deck, mat, om = M.workload(5)
+    P, xr = _oracle_sweep(oracle, deck, mat, om, rcond=True)
+    return deck, mat, om, P, [x for x, _ in xr], [r for _, r in xr]
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_slab16_sweep(slab16, precision):
+    deck, mat, om, P, xs, rconds = slab16
+    R = BemRegion(deck)
+    X = R.sweep_harela(mat, om, precision=precision)
+    for i in range(len(om)):
+        e = rel(X[i], xs[i])
+        tol = max(1e-10, 1e-12 / rconds[i]) if precision == "plain" else 1e-8
+        print(precision, "a0", [0.2, 1.0][i], "rel err", e, "1/rcond", 1.0 / rconds[i], "tolerance", tol)
+        assert e < tol
+    R.close()
+
+
+def test_cube_sizes_of_the_batch(oracle):
+    """n = 5, 6, 7, 10 in one batched call (mixed) and one by one (plain)."""
+    mat = M.viscoelastic(1.0, 0.25, 1.0, 0.05)
+    sizes = (5, 6, 7, 10)
+    a0 = (0.4, 1.0, 1.4, 0.8)
+    decks = [M.cube_clamped_top_traction(n) for n in sizes]
+    oms = [M.omega_from_a0([a], mat) for a in a0]
+    regions = [BemRegion(d) for d in decks]
+    Xm, stats = sweep_harela_batch(regions, mat, oms, precision="mixed")
+    for d, r, om, xm, st in zip(decks, regions, oms, Xm, stats):
+        _, (xo,) = _oracle_sweep(oracle, d, mat, om)
+        xp = r.sweep_harela(mat, om, precision="plain")
+        ep, em = rel(xp[0], xo), rel(xm[0], xo)
+        print(d.name, d.n_dof, "plain", ep, "mixed", em)
+        assert ep < 1e-10 and em < 1e-8
+        assert st["max_backward_error"] <= 1e-12
+        r.close()
+
+
+def test_surface_patch_u_and_t(oracle):
+    """14883 DOF at a0 = 0.5: u and t of the plain and mixed paths against
+    the oracle's FP64 (complex128 LU) solution."""
+    deck, mat, om = M.workload(3)
+    P, (xo,) = _oracle_sweep(oracle, deck, mat, om)
+    uo, to = P.solution(xo)
+    R = BemRegion(deck)
+    for precision, tol in (("plain", 1e-10), ("mixed", 1e-8)):
+        X = R.sweep_harela(mat, om, precision=precision)
+        u, t = R.solution(X[0])
+        eu, et = rel(u, uo), rel(t, to)
+        print(precision, "u", eu, "t", et)
+        assert eu < tol and et < tol
+    R.close()
+
+
+@pytest.mark.parametrize("name,mk", [("cube4", lambda: M.cube_clamped_top_traction(4)), ("slab4", lambda: M.slab(4, 1))],
+                         ids=["cube4", "slab4"])
+def test_mixed_assembly_matches_oracle_entrywise(oracle, name, mk):
+    import ctypes
+    L = _abi.load()
+    L.mfbem_internal_sweep_system.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+    d = mk()
+    mat = M.viscoelastic(1.0, 0.3, 1.0, 0.05)
+    om = M.omega_from_a0([0.2, 1.5], mat)
+    R = BemRegion(d)
+    P = oracle.Problem(d)
+    R.sweep_harela(mat, om, precision="mixed")
+    n = R.n
+    for f, w in enumerate(om):
+        A = np.zeros((n, n), dtype=np.complex128, order="F")
+        b = np.zeros(n, dtype=np.complex128)
+        _abi.check(L.mfbem_internal_sweep_system(R._h, f, A.ctypes.data, b.ctypes.data))
+        Ao, bo = P.assemble_harela(mat, float(w))
+        ea, eb = rel(A, Ao), rel(b, bo)
+        print(name, f, "A", ea, "b", eb)
+        assert ea < 1e-11 and eb < 1e-11
+    R.close()

@@ -74,3 +74,26 @@ def test_no_device_is_an_error_status_not_a_crash():
     with pytest.raises(_abi.MfbemError) as e:
         BemRegion(M.cube_clamped_top_traction(2))
     assert e.value.code == _abi.MFBEM_ECUDA
+
+
+@pytest.mark.parametrize("entry", ["mfbem_solve_c", "mfbem_solve_r", "mfbem_solve_c_static"])
+def test_reused_factors_with_foreign_pivots_are_refused_before_any_device_work(entry):
+    """factorize = 0 takes the caller's ipiv: values outside getrf's range
+    (ipiv(j) in [j, n], 1-based) are refused on the host, so no kernel ever
+    indexes the vectors with them (checked without a GPU: the call returns
+    before the first CUDA call)."""
+    L = _abi.load()
+    n = 8
+    cplx = entry != "mfbem_solve_r"
+    A = np.asfortranarray(np.eye(n, dtype=np.complex128 if cplx else np.float64))
+    b = np.ones((n, 1), dtype=A.dtype, order="F")
+    for bad in ([1, 2, 3, 4, 5, 6, 7, 9], [0, 2, 3, 4, 5, 6, 7, 8], [2, 1, 3, 4, 5, 6, 7, 8], [1, 2, 3, 4, 5, 6, 7, -3]):
+        ip = np.array(bad, dtype=np.int32)
+        if entry == "mfbem_solve_c_static":
+            rc = L.mfbem_solve_c_static(n, A.ctypes.data_as(_abi._dp), ip.ctypes.data_as(_abi._ip), 1,
+                                        b.ctypes.data_as(_abi._dp), 0)
+        else:
+            rc = getattr(L, entry)(n, A.ctypes.data_as(_abi._dp), ip.ctypes.data_as(_abi._ip), 1, None, None, None,
+                                   None, 1, b.ctypes.data_as(_abi._dp), 0, 0, 0, 0)
+        assert rc == _abi.MFBEM_EARG, bad
+        assert b"is not a pivot of getrf" in L.mfbem_last_error()

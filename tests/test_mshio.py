@@ -91,6 +91,11 @@ def test_refuses_what_the_reference_refuses(tmp_path):
         "unknown type": GOOD_HEAD + NODES + ELEM.replace(" 16 2 ", " 99 2 "),
         "undeclared node": GOOD_HEAD + NODES + ELEM.replace(" 8\n", " 9\n"),
         "zero part id": GOOD_HEAD.replace('2 1 "s"', '2 0 "s"') + NODES + ELEM,
+        # a quad8 and a line3 in the same physical group
+        "mixed dimensions": GOOD_HEAD + NODES + ELEM.replace("$Elements\n1\n", "$Elements\n2\n").replace(
+            "$EndElements", "2 8 2 1 1 1 5 2\n$EndElements"),
+        # a declared part without elements
+        "empty part": GOOD_HEAD.replace('1\n2 1 "s"', '2\n2 1 "s"\n2 2 "e"') + NODES + ELEM,
     }
     for what, text in bad.items():
         with pytest.raises(ValueError):

@@ -49,6 +49,46 @@ def test_static_solve_matches_solve_c_on_two_calls():
         assert _rel(c2, c1) < 1e-10, call
 
 
+def _cudart():
+    import ctypes
+    for name in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            continue
+    pytest.skip("CUDA runtime library not found")
+
+
+def _free_bytes(rt):
+    import ctypes
+    fr, tot = ctypes.c_size_t(), ctypes.c_size_t()
+    assert rt.cudaMemGetInfo(ctypes.byref(fr), ctypes.byref(tot)) == 0
+    return fr.value
+
+
+def test_static_solve_at_its_limits_matches_lapack_and_allocates_nothing():
+    """n = MFBEM_STATIC_MAX_N with MFBEM_STATIC_MAX_RHS right-hand sides (every
+    slot of the array in use) against LAPACK getrf/getrs (scipy), and the
+    device's free memory unchanged by a call that follows a warm-up call."""
+    import scipy.linalg as sl
+    rng = np.random.default_rng(12)
+    n, nrhs = 1024, 4
+    A = np.asfortranarray(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    b = np.asfortranarray(rng.standard_normal((n, nrhs)) + 1j * rng.standard_normal((n, nrhs)))
+    lu, piv = sl.lu_factor(A)
+    x = sl.lu_solve((lu, piv), b)
+    rt = _cudart()
+    A0, b0, ip0 = A.copy(order="F"), b.copy(order="F"), np.zeros(n, dtype=np.int32)
+    assert _static(A0, ip0, b0) == 0, _abi.load().mfbem_last_error()  # warm-up: context, module, symbol address
+    free0 = _free_bytes(rt)
+    A1, b1, ip1 = A.copy(order="F"), b.copy(order="F"), np.zeros(n, dtype=np.int32)
+    assert _static(A1, ip1, b1) == 0, _abi.load().mfbem_last_error()
+    assert _free_bytes(rt) == free0
+    assert np.array_equal(ip1 - 1, piv)
+    assert _rel(A1, lu) < 1e-12
+    assert _rel(b1, x) < 1e-10
+
+
 def test_static_solve_rejects_sizes_beyond_its_array():
     n = 1025
     A = np.asfortranarray(np.eye(n, dtype=np.complex128))
