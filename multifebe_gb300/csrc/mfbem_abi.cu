@@ -30,6 +30,7 @@
 #include "mfbem_internal.cuh"
 #include "mfbem_lu.cuh"
 #include "mfbem_tc.cuh"
+#include "mfbem_oz.cuh"
 
 namespace mfb {
 static thread_local std::string g_err;
@@ -1006,6 +1007,58 @@ extern "C" int mfbem_internal_tc_cgemm(int32_t m, int32_t n, int32_t k, const fl
   if (e != cudaSuccess) return fail(MFBEM_ECUDA, std::string("tc cgemm: ") + cudaGetErrorString(e));
   if (herr) return fail(MFBEM_ETIMEOUT, "tc cgemm: an MMA completion wait timed out");
   return 0;
+}
+
+// Test hook (not part of the reference interface): C -= A B in FP64 for
+// column-major A (m x k), B (k x n), C (m x n), complex (cplx = 1) or real,
+// with the plain LU's trailing-update kernels: mode 0 the Ozaki-scheme
+// tensor-core kernels, 1 the binary64 SIMT kernel.
+extern "C" int mfbem_internal_f64_gemm(int32_t cplx, int32_t m, int32_t n, int32_t k, const double* A,
+                                       const double* B, double* C, int32_t mode) {
+  g_err.clear();
+  if (m <= 0 || n <= 0 || k <= 0 || !A || !B || !C || mode < 0 || mode > 1) return fail(MFBEM_EARG, "invalid argument");
+  const size_t es = cplx ? 16 : 8;
+  DevBuf dA, dB, dC;
+  auto cleanup = [&]() {
+    for (DevBuf* b : {&dA, &dB, &dC})
+      if (b->p) cudaFree(b->p);
+  };
+  int rc;
+  if ((rc = ensure(dA, es * m * k)) || (rc = ensure(dB, es * k * n)) || (rc = ensure(dC, es * m * n))) {
+    cleanup();
+    return rc;
+  }
+  cudaError_t e = cudaMemcpy(dA.p, A, es * m * k, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dB.p, B, es * k * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dC.p, C, es * m * n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cleanup();
+    return fail(MFBEM_ECUDA, std::string("f64 gemm: ") + cudaGetErrorString(e));
+  }
+  if (mode == 0) {
+    if ((rc = oz_err_reset(0)) == 0)
+      rc = cplx ? oz_gemm_run<true>(0, (const double2*)dA.p, m, 0, (const double2*)dB.p, k, 0, (double2*)dC.p, m, 0, m,
+                                    n, k, 1)
+                : oz_gemm_run<false>(0, (const double*)dA.p, m, 0, (const double*)dB.p, k, 0, (double*)dC.p, m, 0, m,
+                                     n, k, 1);
+    if (!rc) rc = oz_err_check(0);
+  } else {
+    if (cplx)
+      k_dgemm_simt<double2><<<dim3(nblk(m, 64), nblk(n, 64), 1), 256>>>((const double2*)dA.p, m, 0,
+                                                                        (const double2*)dB.p, k, 0, (double2*)dC.p, m,
+                                                                        0, m, n, k);
+    else
+      k_dgemm_simt<double><<<dim3(nblk(m, 64), nblk(n, 64), 1), 256>>>((const double*)dA.p, m, 0, (const double*)dB.p,
+                                                                       k, 0, (double*)dC.p, m, 0, m, n, k);
+    ++g_launches;
+    rc = cudaGetLastError() == cudaSuccess ? 0 : fail(MFBEM_ECUDA, "f64 gemm launch");
+  }
+  if (!rc) {
+    e = cudaMemcpy(C, dC.p, es * m * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = fail(MFBEM_ECUDA, std::string("f64 gemm: ") + cudaGetErrorString(e));
+  }
+  cleanup();
+  return rc;
 }
 
 // Test hook (not part of the reference interface): sets the iteration limit

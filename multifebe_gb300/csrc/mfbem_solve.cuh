@@ -75,11 +75,140 @@ static int tc_cgemm_run(cudaStream_t st, const float2* A, int lda, long long sA,
   CK(cudaGetLastError());
   return 0;
 }
+// ---------------------------------------------------------------------------
+// FP64 trailing updates C -= A B of the plain LU (batched, column-major):
+// mode 0 (default) the FP64-accurate Ozaki-scheme kernels on the bf16 tensor
+// cores (mfbem_oz.cuh); mode 1 this library's binary64 SIMT kernel
+// (k_dgemm_simt, FMA on the FP64 pipe). MFBEM_FP64_GEMM=oz|dfma overrides.
+// ---------------------------------------------------------------------------
+static int f64_default() {
+  const char* e = getenv("MFBEM_FP64_GEMM");
+  return (e && std::string(e) == "dfma") ? 1 : 0;
+}
+static thread_local DevBuf g_oz_ws, g_oz_err;
+
+template <bool CPLX>
+static int oz_gemm_run(cudaStream_t st, const typename OzT<CPLX>::S* A, int lda, long long sA,
+                       const typename OzT<CPLX>::S* B, int ldb, long long sB, typename OzT<CPLX>::S* C, int ldc,
+                       long long sC, int m, int n, int k, int batch) {
+  typedef typename OzT<CPLX>::S S;
+  if (m <= 0 || n <= 0 || k <= 0 || batch <= 0) return 0;
+  constexpr int W = CPLX ? 2 : 1;  // real K per complex K
+  const int kmax = OZ_MAXK / W;
+  if (k > kmax) {  // exactness bound of the level accumulators: split K
+    for (int k0 = 0; k0 < k; k0 += kmax) {
+      const int kk = std::min(kmax, k - k0);
+      int rc = oz_gemm_run<CPLX>(st, A + (size_t)k0 * lda, lda, sA, B + k0, ldb, sB, C, ldc, sC, m, n, kk, batch);
+      if (rc) return rc;
+    }
+    return 0;
+  }
+  const int mr = W * m, Kr = W * k;
+  const int nmt = (mr + OZ_BM - 1) / OZ_BM, nnt = (n + OZ_BN - 1) / OZ_BN, nkc = (Kr + OZ_KC - 1) / OZ_KC;
+  const size_t wa = (size_t)batch * nmt * nkc * OZ_S * OZ_TWA, wb = (size_t)batch * nnt * nkc * OZ_S * OZ_TWB;
+  const size_t ne = (size_t)batch * nmt * OZ_BM, nf = (size_t)batch * nnt * OZ_BN;
+  int rc = ensure(g_oz_ws, sizeof(uint32_t) * (wa + wb) + sizeof(int) * (ne + nf) + 256);
+  if (rc) return rc;
+  if (!g_oz_err.p) return fail(MFBEM_ECUDA, "Ozaki GEMM: error flag not set up");
+  if (raise_smem_limit((const void*)k_oz_gemm)) return fail(MFBEM_ECUDA, "shared-memory limit of the Ozaki GEMM");
+  uint32_t* at = (uint32_t*)g_oz_ws.p;
+  uint32_t* bt = at + wa;
+  int* erow = (int*)(bt + wb);
+  int* fcol = erow + ne;
+  k_oz_split_a<CPLX><<<dim3(nmt, batch), 256, 0, st>>>(A, lda, sA, m, k, nmt, nkc, at, erow); ++g_launches;
+  k_oz_split_b<CPLX><<<dim3(nnt, batch), 256, 0, st>>>(B, ldb, sB, k, n, nnt, nkc, bt, fcol); ++g_launches;
+  k_oz_gemm<<<dim3(nmt, nnt, batch), 128, OZ_SMEM, st>>>(at, bt, erow, fcol, nmt, nnt, nkc, (double*)C,
+                                                        (long long)W * ldc, (long long)W * sC, mr, n,
+                                                        (int*)g_oz_err.p, g_spin_limit.load());
+  ++g_launches;
+  CK(cudaGetLastError());
+  return 0;
+}
+// the Ozaki kernels' timeout flag: zeroed before a factorisation, read after it
+static int oz_err_reset(cudaStream_t st) {
+  int rc = ensure(g_oz_err, sizeof(int));
+  if (rc) return rc;
+  CK(cudaMemsetAsync(g_oz_err.p, 0, sizeof(int), st));
+  return 0;
+}
+static int oz_err_check(cudaStream_t st) {
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, g_oz_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (e) return fail(MFBEM_ETIMEOUT, "FP64 trailing update: a tensor-core completion wait timed out");
+  return 0;
+}
+
+// binary64 SIMT update: 64 x 64 tile of C per 256-thread CTA, 4 x 4 outputs
+// per thread, K staged in shared memory 16 at a time
+__device__ __forceinline__ double2 zfma(double2 a, double2 b, double2 c) {
+  return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ double zfma(double a, double b, double c) { return fma(a, b, c); }
+template <typename S>
+__global__ void __launch_bounds__(256) k_dgemm_simt(const S* A, int lda, long long sA, const S* B, int ldb,
+                                                    long long sB, S* C, int ldc, long long sC, int m, int n, int k) {
+  __shared__ S As[16][64 + 1];
+  __shared__ S Bs[16][64 + 1];
+  const int b = blockIdx.z, tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
+  const S* Ab = A + sA * b;
+  const S* Bb = B + sB * b;
+  S acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = Sc<S>::zero();
+  for (int l0 = 0; l0 < k; l0 += 16) {
+    for (int q = threadIdx.x; q < 16 * 64; q += 256) {
+      const int ii = q % 64, ll = q / 64;
+      As[ll][ii] = (i0 + ii < m && l0 + ll < k) ? Ab[(size_t)(l0 + ll) * lda + i0 + ii] : Sc<S>::zero();
+      const int jj = q / 16, lb = q % 16;
+      Bs[lb][jj] = (j0 + jj < n && l0 + lb < k) ? Bb[(size_t)(j0 + jj) * ldb + l0 + lb] : Sc<S>::zero();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int ll = 0; ll < 16; ++ll) {
+      S a[4], bv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = As[ll][tx + 16 * u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) bv[v] = Bs[ll][ty + 16 * v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = zfma(a[u], bv[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+  S* Cb = C + sC * b;
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = i0 + tx + 16 * u, j = j0 + ty + 16 * v;
+      if (i < m && j < n) Cb[(size_t)j * ldc + i] = Sc<S>::sub(Cb[(size_t)j * ldc + i], acc[u][v]);
+    }
+}
+
+template <typename S>
+static int f64_gemm(cudaStream_t st, int m, int n, int k, const S* A, int lda, long long sA, const S* B, int ldb,
+                    long long sB, S* C, int ldc, long long sC, int batch) {
+  if (m <= 0 || n <= 0 || k <= 0) return 0;
+  if (f64_default() == 1) {
+    k_dgemm_simt<S><<<dim3(nblk(m, 64), nblk(n, 64), batch), 256, 0, st>>>(A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k);
+    ++g_launches;
+    CK(cudaGetLastError());
+    return 0;
+  }
+  return oz_gemm_run<std::is_same<S, double2>::value>(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch);
+}
 static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const double* A, int lda, long long sA,
                               const double* B, int ldb, long long sB, double* C, int ldc, long long sC, int batch) {
-  const double al = -1.0, be = 1.0;
-  return cublasDgemmStridedBatched(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, lda, sA, B, ldb, sB, &be, C, ldc,
-                                   sC, batch);
+  cudaStream_t st = nullptr;
+  cublasGetStream(hb, &st);
+  return f64_gemm<double>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch) ? CUBLAS_STATUS_EXECUTION_FAILED
+                                                                                    : CUBLAS_STATUS_SUCCESS;
 }
 static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const float* A, int lda, long long sA,
                               const float* B, int ldb, long long sB, float* C, int ldc, long long sC, int batch) {
@@ -94,9 +223,10 @@ static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const floa
 }
 static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const double2* A, int lda, long long sA,
                               const double2* B, int ldb, long long sB, double2* C, int ldc, long long sC, int batch) {
-  const cuDoubleComplex al = make_cuDoubleComplex(-1.0, 0.0), be = make_cuDoubleComplex(1.0, 0.0);
-  return cublasZgemmStridedBatched(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, (const cuDoubleComplex*)A, lda, sA,
-                                   (const cuDoubleComplex*)B, ldb, sB, &be, (cuDoubleComplex*)C, ldc, sC, batch);
+  cudaStream_t st = nullptr;
+  cublasGetStream(hb, &st);
+  return f64_gemm<double2>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch) ? CUBLAS_STATUS_EXECUTION_FAILED
+                                                                                     : CUBLAS_STATUS_SUCCESS;
 }
 static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const float2* A, int lda, long long sA,
                               const float2* B, int ldb, long long sB, float2* C, int ldc, long long sC, int batch) {
@@ -185,6 +315,11 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
   k_ipiv_identity<<<dim3(nblk(n, 256), batch), 256, 0, st>>>(ipiv, n); ++g_launches;
   typedef typename Sc<S>::R R;
   const bool tc = g_c32_mode == 3 && std::is_same<S, float2>::value;
+  const bool oz = IsF64<S>::v && f64_default() == 0;
+  if (oz) {
+    int rc = oz_err_reset(st);
+    if (rc) return rc;
+  }
   if (tc) {
     int rc = ensure(g_tc_err, sizeof(int));
     if (rc) return rc;
@@ -324,6 +459,10 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
     CK(cudaMemcpyAsync(&e, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (e) return fail(MFBEM_ETIMEOUT, "LU panel: a barrier wait timed out");
+  }
+  if (oz) {
+    int rc = oz_err_check(st);
+    if (rc) return rc;
   }
   if (tc) {
     int e = 0;

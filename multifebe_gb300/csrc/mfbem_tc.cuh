@@ -56,12 +56,26 @@ __host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-// Spin limit of the waits on mbarriers: `spin` iterations (<= 0: TC_SPIN).
-// A wait that gives up makes the kernel set its error flag; the waits that
-// then drain the copies and MMAs still in flight use the full TC_SPIN.
+// Spin limit of the waits on mbarriers: TC_SPIN polls with try_wait (which
+// itself suspends the thread for a short while); a positive `spin` (set only
+// by the failure-detection test hook) instead allows that many non-blocking
+// test_wait polls. A wait that gives up makes the kernel set its error flag;
+// the waits that then drain the copies and MMAs still in flight use the full
+// TC_SPIN.
 __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity, long long spin = 0) {
-  const long long lim = spin > 0 ? spin : TC_SPIN;
-  for (long long it = 0; it < lim; ++it) {
+  if (spin > 0) {
+    for (long long it = 0; it < spin; ++it) {
+      uint32_t done;
+      asm volatile(
+          "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+          : "=r"(done)
+          : "r"(mbar), "r"(parity)
+          : "memory");
+      if (done) return true;
+    }
+    return false;
+  }
+  for (long long it = 0; it < TC_SPIN; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

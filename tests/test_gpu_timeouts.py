@@ -61,6 +61,26 @@ def test_tensor_core_wait_gives_up_then_next_call_is_correct(short_waits, staged
         assert np.abs(C - ref).max() / np.abs(ref).max() < 2e-6
 
 
+def test_fp64_tensor_core_wait_gives_up_then_next_call_is_correct(short_waits):
+    """The Ozaki-scheme kernels of the plain LU's trailing update."""
+    L = short_waits
+    L.mfbem_internal_f64_gemm.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 3 + [ctypes.c_int32]
+    rng = np.random.default_rng(6)
+    m, n, k = 300, 200, 128
+    A = np.asfortranarray(rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k)))
+    B = np.asfortranarray(rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n)))
+    C0 = np.asfortranarray(rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n)))
+    L.mfbem_internal_set_spin_limit(1)
+    C = C0.copy(order="F")
+    assert L.mfbem_internal_f64_gemm(1, m, n, k, A.ctypes.data, B.ctypes.data, C.ctypes.data, 0) == _abi.MFBEM_ETIMEOUT
+    L.mfbem_internal_set_spin_limit(0)
+    for _ in range(2):
+        C = C0.copy(order="F")
+        assert L.mfbem_internal_f64_gemm(1, m, n, k, A.ctypes.data, B.ctypes.data, C.ctypes.data, 0) == 0
+        ref = C0 - A @ B
+        assert np.abs(C - ref).max() / np.abs(ref).max() < 1e-14
+
+
 def test_cooperative_panel_barrier_gives_up_then_next_solve_is_correct(short_waits):
     """n = 3300 complex: the FP64 LU's panel runs as a cooperative grid of
     several CTAs per matrix (its rows exceed the cluster panel's shared memory)."""
