@@ -486,14 +486,14 @@ def precision_form(steps=3, warmup=1):
     return out
 
 
-def profile_case(nf):
+def profile_case(nf, precision="mixed"):
     """Small fixed case for ncu captures: the benchmark mesh, nf frequencies,
-    two mixed-precision sweeps."""
+    two sweeps of the given precision."""
     from multifebe_gb300 import meshgen as M, BemRegion
     deck, mat, om = M.workload(2)
     R = BemRegion(deck)
     for _ in range(2):
-        R.sweep_harela(mat, om[:nf], precision="mixed")
+        R.sweep_harela(mat, om[:nf], precision=precision)
     print(json.dumps(R.last_stats))
     return 0
 
@@ -527,11 +527,13 @@ def main():
                     help="skip the 48-problem batch of uneven meshes")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="profiling helper: run the benchmark mesh for this many frequencies twice, print stats, exit")
+    ap.add_argument("--profile-precision", default="mixed", choices=["mixed", "plain"],
+                    help="precision of the --profile-case sweeps")
     ap.add_argument("--profile-patch", default="", choices=["", "mixed", "plain"],
                     help="profiling helper: one sweep of the 14883-DOF surface patch, print stats, exit")
     args = ap.parse_args()
     if args.profile_case:
-        return profile_case(args.profile_case)
+        return profile_case(args.profile_case, args.profile_precision)
     if args.profile_patch:
         return profile_patch(args.profile_patch)
     if args.impl == "reference":

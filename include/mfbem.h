@@ -192,7 +192,7 @@ void mfbem_msh_free(void* msh);
 /* Device memory released with a mesh handle (mfbem_mesh_release) is kept by
    the library for later handles: buffers of at least 1 MB, up to a quarter of
    the device memory (environment MFBEM_DEVICE_CACHE_MB overrides the cap; 0
-   disables the cache), with the handles' streams and cuBLAS handles. This
+   disables the cache), with the handles' streams. This
    returns every cached buffer to the driver. No counterpart in the reference. */
 int mfbem_trim_device_cache(void);
 
@@ -256,7 +256,7 @@ const char* mfbem_version(void);
    material (lambda[2i], mu[2i], nu[2i] complex, rho[i]), n_freq[i]
    frequencies omega[i][...] and solution array x_out[i] (as
    mfbem_sweep_harela); the sweeps run concurrently on the GPU (one host
-   thread, stream and cuBLAS handle per mesh). stats: [n_mesh] or NULL. */
+   thread and stream per mesh). stats: [n_mesh] or NULL. */
 int mfbem_sweep_harela_batch(int32_t n_mesh, mfbem_handle* const* hs, const double* lambda, const double* mu,
                              const double* rho, const double* nu, const int32_t* n_freq, const double* const* omega,
                              int32_t precision, double rel_tol, double* const* x_out, int32_t flags,

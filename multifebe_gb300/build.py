@@ -74,8 +74,7 @@ def build(force=False, verbose=False):
                 raise RuntimeError("build failed: " + " ".join(cmd[:4]))
             if verbose and (r.stdout or r.stderr):
                 sys.stderr.write(r.stderr)
-    link = [nvcc, ARCH, "-shared", "-o", LIB + ".tmp"] + [os.path.join(OUT, o) for o in jobs] + [
-        "-lcublas", "-lcudart"]
+    link = [nvcc, ARCH, "-shared", "-o", LIB + ".tmp"] + [os.path.join(OUT, o) for o in jobs] + ["-lcudart"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         sys.stderr.write(r.stdout + r.stderr)

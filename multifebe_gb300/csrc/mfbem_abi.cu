@@ -1,7 +1,6 @@
 // C-ABI of the GB300 collocation-BEM library (see include/mfbem.h): handle
 // management, the once-per-mesh device precompute, per-frequency assembly,
 // and the dense solves. Single translation unit for all device code.
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -55,10 +54,11 @@ using namespace mfb;
     cudaError_t e_ = (call);                                                                      \
     if (e_ != cudaSuccess) return fail(MFBEM_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
-#define CKB(call)                                                                                  \
-  do {                                                                                             \
-    cublasStatus_t s_ = (call);                                                                    \
-    if (s_ != CUBLAS_STATUS_SUCCESS) return fail(MFBEM_ECUDA, std::string(#call) + ": cublas status " + std::to_string((int)s_)); \
+// a library routine returning an MFBEM status: pass a failure on
+#define CKG(call)                \
+  do {                           \
+    int rc_ = (call);            \
+    if (rc_) return rc_;         \
   } while (0)
 
 // A device buffer and the device ordinal it was allocated on.
@@ -80,7 +80,6 @@ struct mfbem_handle {
   // once, so later solves factorise with SIMT FP32 updates from the start
   bool tf32_stalled = false;
   cudaStream_t st = nullptr;
-  cublasHandle_t blas = nullptr;
   DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, Af, geo_f, gm;
   mfbem_stats stats{};
   // systems of the last mfbem_sweep_harela call (read back by a test hook)
@@ -103,15 +102,15 @@ struct mfbem_handle {
 // MFBEM_DEVICE_CACHE_MB; 0 disables the cache); an allocation takes the
 // smallest cached buffer that fits and is at most twice the request.
 // mfbem_trim_device_cache() returns everything to the driver. Streams and
-// cuBLAS handles of released meshes are reused the same way.
+// streams of released meshes are reused the same way.
 // ---------------------------------------------------------------------------
 static std::mutex g_pool_mu;
 // cached buffers: size -> (device ordinal, pointer); bytes and cap per device
 static std::multimap<size_t, std::pair<int, void*>> g_pool;
 static std::map<int, size_t> g_pool_bytes;
 static std::map<int, long long> g_pool_cap;
-// streams and cuBLAS handles of released meshes: (device, stream, handle)
-static std::vector<std::tuple<int, cudaStream_t, cublasHandle_t>> g_ctx_pool;
+// streams of released meshes: (device, stream)
+static std::vector<std::pair<int, cudaStream_t>> g_ctx_pool;
 
 static int cur_dev() {
   int d = 0;
@@ -563,18 +562,13 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   {
     std::lock_guard<std::mutex> lk(g_pool_mu);
     for (size_t i = g_ctx_pool.size(); i-- > 0;)
-      if (std::get<0>(g_ctx_pool[i]) == h->dev) {
-        h->st = std::get<1>(g_ctx_pool[i]);
-        h->blas = std::get<2>(g_ctx_pool[i]);
+      if (g_ctx_pool[i].first == h->dev) {
+        h->st = g_ctx_pool[i].second;
         g_ctx_pool.erase(g_ctx_pool.begin() + i);
         break;
       }
   }
-  if (!h->st) {
-    CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
-    if (cublasCreate(&h->blas) != CUBLAS_STATUS_SUCCESS) { mfbem_mesh_release(h); return fail(MFBEM_ECUDA, "cublasCreate"); }
-    cublasSetStream(h->blas, h->st);
-  }
+  if (!h->st) CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
   *out = h;
   return 0;
 }
@@ -587,12 +581,9 @@ extern "C" int mfbem_mesh_release(mfbem_handle* h) {
     for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu, &h->parf,
                       &h->pphi_f, &h->Af, &h->geo_f, &h->gm})
       pool_give(b->p, b->bytes, b->dev);
-    if (h->st && h->blas) {
+    if (h->st) {
       std::lock_guard<std::mutex> lk(g_pool_mu);
-      g_ctx_pool.emplace_back(h->dev, h->st, h->blas);
-    } else {
-      if (h->blas) cublasDestroy(h->blas);
-      if (h->st) cudaStreamDestroy(h->st);
+      g_ctx_pool.emplace_back(h->dev, h->st);
     }
   });
   delete h;
@@ -1044,11 +1035,11 @@ extern "C" int mfbem_internal_f64_gemm(int32_t cplx, int32_t m, int32_t n, int32
     if (!rc) rc = oz_err_check(0);
   } else {
     if (cplx)
-      k_dgemm_simt<double2><<<dim3(nblk(m, 64), nblk(n, 64), 1), 256>>>((const double2*)dA.p, m, 0,
+      k_gemm_simt<double2><<<dim3(nblk(m, 64), nblk(n, 64), 1), 256>>>((const double2*)dA.p, m, 0,
                                                                         (const double2*)dB.p, k, 0, (double2*)dC.p, m,
                                                                         0, m, n, k);
     else
-      k_dgemm_simt<double><<<dim3(nblk(m, 64), nblk(n, 64), 1), 256>>>((const double*)dA.p, m, 0, (const double*)dB.p,
+      k_gemm_simt<double><<<dim3(nblk(m, 64), nblk(n, 64), 1), 256>>>((const double*)dA.p, m, 0, (const double*)dB.p,
                                                                        k, 0, (double*)dC.p, m, 0, m, n, k);
     ++g_launches;
     rc = cudaGetLastError() == cudaSuccess ? 0 : fail(MFBEM_ECUDA, "f64 gemm launch");
@@ -1090,7 +1081,7 @@ extern "C" int mfbem_internal_sweep_system(mfbem_handle* h, int32_t f, double* A
 // ---------------------------------------------------------------------------
 // Batch of harmonic sweeps over meshes of uneven size (no counterpart in the
 // reference): every mesh's sweep runs on its own host thread, stream and
-// cuBLAS handle, so small problems share the GPU instead of running one
+// work buffers, so small problems share the GPU instead of running one
 // after another. Per mesh i: material lambda[2i..], mu[2i..], rho[i],
 // nu[2i..], n_freq[i] frequencies omega[i][...], solutions x_out[i].
 // ---------------------------------------------------------------------------

@@ -405,7 +405,6 @@ __global__ void k_ferr_w(const S* R, double* w, int n, double nzeps, double safe
 // ---------------------------------------------------------------------------
 struct LseWork {
   cudaStream_t st;
-  cublasHandle_t hb;
   double* red;  // device scalars [8]
   int* flag;    // device int [2]
 };
@@ -563,7 +562,7 @@ static int gerfs1(const LseWork& w, const S* Ao, const S* LU, const int* ipiv, i
   int count = 1, rc;
   for (;;) {
     CK(cudaMemcpyAsync(R, B, sizeof(S) * n, cudaMemcpyDeviceToDevice, w.st));
-    CKB(gemv_res(w.hb, n, Ao, n, 0, X, 0, R, 0, 1));
+    if ((rc = gemv_res<S>(w.st, n, Ao, n, 0, X, 0, R, 0, 1))) return rc;
     k_absAx<S><<<dim3(g, ch), 256, 0, w.st>>>(Ao, n, n, X, cpc, part); ++g_launches;
     k_berr<S><<<1, 1024, 0, w.st>>>(R, B, part, ch, n, safe1, safe2, wts, w.red); ++g_launches;
     CK(cudaMemcpyAsync(h, w.red, sizeof(double), cudaMemcpyDeviceToHost, w.st));
@@ -609,10 +608,9 @@ static thread_local LseReport g_lse;
 
 struct SolveCtx {
   cudaStream_t st = nullptr;
-  cublasHandle_t hb = nullptr;
   DevBuf A, b, ipiv, info, Ao, bc, wv;
 };
-// one context per device ordinal (the stream and cuBLAS handle belong to it)
+// one context per device ordinal (the stream belongs to it)
 static std::map<int, SolveCtx*> g_solve;
 static std::mutex g_solve_mu;
 static int solve_ctx(SolveCtx** out) {
@@ -626,8 +624,6 @@ static int solve_ctx(SolveCtx** out) {
     if (rc) return rc;
     SolveCtx* c = new SolveCtx();
     CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
-    if (cublasCreate(&c->hb) != CUBLAS_STATUS_SUCCESS) return fail(MFBEM_ECUDA, "cublasCreate");
-    cublasSetStream(c->hb, c->st);
     it = g_solve.emplace(dev, c).first;
   }
   *out = it->second;
@@ -686,7 +682,7 @@ static int solve_dropin(int32_t n, double* A, int32_t* ipiv, int32_t aodim, doub
   unsigned long long* bits = (unsigned long long*)(part + 64 * (size_t)n);
   int* isgn = (int*)(bits + n);
   double* red = (double*)(((uintptr_t)(isgn + n) + 63) / 64 * 64);
-  LseWork w{st, cx->hb, red, di + 2};
+  LseWork w{st, red, di + 2};
   CK(cudaMemcpyAsync(dA, A, nn * es, cudaMemcpyHostToDevice, st));
   char eq = scaling ? *equed : 'N';
   if (factorize) {
@@ -702,7 +698,7 @@ static int solve_dropin(int32_t n, double* A, int32_t* ipiv, int32_t aodim, doub
       CK(cudaMemcpyAsync(dAo, dA, nn * es, cudaMemcpyDeviceToDevice, st));
       CK(cudaMemcpyAsync(Ao, dAo, nn * es, cudaMemcpyDeviceToHost, st));
     }
-    if ((rc = getrf_batched<S>(cx->hb, st, dA, 0, n, n, 1, dp, di))) return rc;
+    if ((rc = getrf_batched<S>(st, dA, 0, n, n, 1, dp, di))) return rc;
     int info = 0;
     CK(cudaMemcpyAsync(A, dA, nn * es, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(ipiv, dp, sizeof(int) * n, cudaMemcpyDeviceToHost, st));

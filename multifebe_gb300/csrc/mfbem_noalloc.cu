@@ -2,7 +2,7 @@
 // partial pivoting + triangular solves) for callers that cannot allocate device
 // memory. Its whole device working set lives in one file-scope __device__
 // array; the call performs no cudaMalloc / cudaFree and uses no allocating
-// library (no cuBLAS: the trailing update is a kernel of this file).
+// library (the trailing update is a kernel of this file).
 //
 // Limits: n <= MFBEM_STATIC_MAX_N, n_rhs <= MFBEM_STATIC_MAX_RHS. The array
 // (about 16 MiB) is held by every GPU that loads the library until the process

@@ -35,26 +35,27 @@ __global__ void k_ipiv_identity(int* ipiv, int n) {
 }
 
 // Compute type of the single-precision trailing updates of the mixed LU:
-// 0 SIMT FP32 (cuBLAS), 1 cuBLAS TF32 tensor cores (TF32-accurate factors;
+// 0 SIMT FP32 (k_gemm_simt), 1 tcgen05 TF32, one pass (TF32-accurate factors;
 // refinement in FP64 restores the accuracy and escalates to SIMT FP32 when it
-// stalls), 2 cuBLAS's BF16x9 FP32 emulation, 3 this library's tcgen05 3xTF32
-// kernels (FP32-accurate factors at tensor-core speed; complex updates only,
-// real ones use SIMT FP32). Default 3; MFBEM_FP32_GEMM=simt|tf32|bf16x9|tc3 overrides.
+// stalls), 3 tcgen05 3xTF32 (FP32-accurate factors at tensor-core speed).
+// The tensor-core kernels take the complex updates of depth above 32; the
+// real ones and the depth-32 updates inside an outer block run on SIMT FP32.
+// Default 3; MFBEM_FP32_GEMM=simt|tf32|tc3 overrides.
 static thread_local int g_c32_mode = 3;
 static int c32_default() {
   const char* e = getenv("MFBEM_FP32_GEMM");
   const std::string v = e ? e : "tc3";
-  return v == "simt" ? 0 : (v == "bf16x9" ? 2 : (v == "tf32" ? 1 : 3));
+  return v == "simt" ? 0 : (v == "tf32" ? 1 : 3);
 }
-// mode 3: this library's tcgen05 3xTF32 kernels (mfbem_tc.cuh) for the complex
-// trailing updates; their timeout flag and pre-split operand tiles, per host thread
+// modes 1 and 3: the tcgen05 kernels (mfbem_tc.cuh) for the complex trailing
+// updates; their timeout flag and pre-split operand tiles, per host thread
 static thread_local DevBuf g_tc_err, g_tc_ws;
 
 // C -= A B (complex64, batched): split A and B into pre-tiled hi / lo TF32
 // words once, then the bulk-copy / tcgen05 pipeline per 128 x 128 tile of C~.
 static int tc_cgemm_run(cudaStream_t st, const float2* A, int lda, long long sA, const float2* B, int ldb,
                         long long sB, float2* C, int ldc, long long sC, int m, int n, int k, int batch, DevBuf& ws,
-                        int* err) {
+                        int* err, int passes = 3) {
   const int nmt = (m + TC_BM / 2 - 1) / (TC_BM / 2), nnt = (n + TC_BN - 1) / TC_BN, nkc = (k + TQ / 2 - 1) / (TQ / 2);
   if (nmt == 0 || nnt == 0 || nkc == 0) return 0;
   const size_t wa = (size_t)batch * nmt * nkc * TQ_TW, wb = (size_t)batch * nnt * nkc * TQ_TW;
@@ -70,7 +71,74 @@ static int tc_cgemm_run(cudaStream_t st, const float2* A, int lda, long long sA,
   k_tc_prep_b<<<(unsigned)std::min<size_t>((wb + 255) / 256, 152 * 32), 256, 0, st>>>(B, ldb, sB, k, n, nnt, nkc, batch, bhi, blo);
   ++g_launches;
   k_tc_cgemm_bulk<<<dim3(nmt, nnt, batch), 128, TC_SMEM2, st>>>(ahi, alo, bhi, blo, nmt, nnt, nkc, C, ldc, sC, m, n, err,
-                                                                 g_spin_limit.load());
+                                                                 g_spin_limit.load(), passes);
+  ++g_launches;
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// SIMT update C -= A B (any of the four scalar types, batched): a 64 x 64
+// tile of C per 256-thread CTA, 4 x 4 outputs per thread, K staged in shared
+// memory 16 at a time; accumulation in the scalar's own precision (binary64
+// FMA on the FP64 pipe for double / double2).
+__device__ __forceinline__ double2 zfma(double2 a, double2 b, double2 c) {
+  return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ double zfma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float2 zfma(float2 a, float2 b, float2 c) {
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ float zfma(float a, float b, float c) { return fmaf(a, b, c); }
+template <typename S>
+__global__ void __launch_bounds__(256) k_gemm_simt(const S* A, int lda, long long sA, const S* B, int ldb,
+                                                   long long sB, S* C, int ldc, long long sC, int m, int n, int k) {
+  __shared__ S As[16][64 + 1];
+  __shared__ S Bs[16][64 + 1];
+  const int b = blockIdx.z, tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
+  const S* Ab = A + sA * b;
+  const S* Bb = B + sB * b;
+  S acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = Sc<S>::zero();
+  for (int l0 = 0; l0 < k; l0 += 16) {
+    for (int q = threadIdx.x; q < 16 * 64; q += 256) {
+      const int ii = q % 64, ll = q / 64;
+      As[ll][ii] = (i0 + ii < m && l0 + ll < k) ? Ab[(size_t)(l0 + ll) * lda + i0 + ii] : Sc<S>::zero();
+      const int jj = q / 16, lb = q % 16;
+      Bs[lb][jj] = (j0 + jj < n && l0 + lb < k) ? Bb[(size_t)(j0 + jj) * ldb + l0 + lb] : Sc<S>::zero();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int ll = 0; ll < 16; ++ll) {
+      S a[4], bv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = As[ll][tx + 16 * u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) bv[v] = Bs[ll][ty + 16 * v];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = zfma(a[u], bv[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+  S* Cb = C + sC * b;
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = i0 + tx + 16 * u, j = j0 + ty + 16 * v;
+      if (i < m && j < n) Cb[(size_t)j * ldc + i] = Sc<S>::sub(Cb[(size_t)j * ldc + i], acc[u][v]);
+    }
+}
+template <typename S>
+static int gemm_simt(cudaStream_t st, int m, int n, int k, const S* A, int lda, long long sA, const S* B, int ldb,
+                     long long sB, S* C, int ldc, long long sC, int batch) {
+  if (m <= 0 || n <= 0 || k <= 0) return 0;
+  k_gemm_simt<S><<<dim3(nblk(m, 64), nblk(n, 64), batch), 256, 0, st>>>(A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k);
   ++g_launches;
   CK(cudaGetLastError());
   return 0;
@@ -139,115 +207,34 @@ static int oz_err_check(cudaStream_t st) {
   return 0;
 }
 
-// binary64 SIMT update: 64 x 64 tile of C per 256-thread CTA, 4 x 4 outputs
-// per thread, K staged in shared memory 16 at a time
-__device__ __forceinline__ double2 zfma(double2 a, double2 b, double2 c) {
-  return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
-}
-__device__ __forceinline__ double zfma(double a, double b, double c) { return fma(a, b, c); }
-template <typename S>
-__global__ void __launch_bounds__(256) k_dgemm_simt(const S* A, int lda, long long sA, const S* B, int ldb,
-                                                    long long sB, S* C, int ldc, long long sC, int m, int n, int k) {
-  __shared__ S As[16][64 + 1];
-  __shared__ S Bs[16][64 + 1];
-  const int b = blockIdx.z, tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
-  const S* Ab = A + sA * b;
-  const S* Bb = B + sB * b;
-  S acc[4][4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) acc[u][v] = Sc<S>::zero();
-  for (int l0 = 0; l0 < k; l0 += 16) {
-    for (int q = threadIdx.x; q < 16 * 64; q += 256) {
-      const int ii = q % 64, ll = q / 64;
-      As[ll][ii] = (i0 + ii < m && l0 + ll < k) ? Ab[(size_t)(l0 + ll) * lda + i0 + ii] : Sc<S>::zero();
-      const int jj = q / 16, lb = q % 16;
-      Bs[lb][jj] = (j0 + jj < n && l0 + lb < k) ? Bb[(size_t)(j0 + jj) * ldb + l0 + lb] : Sc<S>::zero();
-    }
-    __syncthreads();
-#pragma unroll 4
-    for (int ll = 0; ll < 16; ++ll) {
-      S a[4], bv[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) a[u] = As[ll][tx + 16 * u];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) bv[v] = Bs[ll][ty + 16 * v];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = zfma(a[u], bv[v], acc[u][v]);
-    }
-    __syncthreads();
-  }
-  S* Cb = C + sC * b;
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int i = i0 + tx + 16 * u, j = j0 + ty + 16 * v;
-      if (i < m && j < n) Cb[(size_t)j * ldc + i] = Sc<S>::sub(Cb[(size_t)j * ldc + i], acc[u][v]);
-    }
-}
-
 template <typename S>
 static int f64_gemm(cudaStream_t st, int m, int n, int k, const S* A, int lda, long long sA, const S* B, int ldb,
                     long long sB, S* C, int ldc, long long sC, int batch) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
-  if (f64_default() == 1) {
-    k_dgemm_simt<S><<<dim3(nblk(m, 64), nblk(n, 64), batch), 256, 0, st>>>(A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k);
-    ++g_launches;
-    CK(cudaGetLastError());
-    return 0;
-  }
+  if (f64_default() == 1) return gemm_simt<S>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
   return oz_gemm_run<std::is_same<S, double2>::value>(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch);
 }
-static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const double* A, int lda, long long sA,
-                              const double* B, int ldb, long long sB, double* C, int ldc, long long sC, int batch) {
-  cudaStream_t st = nullptr;
-  cublasGetStream(hb, &st);
-  return f64_gemm<double>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch) ? CUBLAS_STATUS_EXECUTION_FAILED
-                                                                                    : CUBLAS_STATUS_SUCCESS;
+// C -= A B (batched) in the scalar type of the factorisation, as configured
+// above: FP64 (plain LU) or FP32 (mixed LU)
+static int gemm_sb(cudaStream_t st, int m, int n, int k, const double* A, int lda, long long sA, const double* B,
+                   int ldb, long long sB, double* C, int ldc, long long sC, int batch) {
+  return f64_gemm<double>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
 }
-static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const float* A, int lda, long long sA,
-                              const float* B, int ldb, long long sB, float* C, int ldc, long long sC, int batch) {
-  const float al = -1.0f, be = 1.0f;
-  if (g_c32_mode > 0 && g_c32_mode < 3)
-    return cublasGemmStridedBatchedEx(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, CUDA_R_32F, lda, sA, B, CUDA_R_32F,
-                                      ldb, sB, &be, C, CUDA_R_32F, ldc, sC, batch,
-                                      g_c32_mode == 1 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F_EMULATED_16BFX9,
-                                      CUBLAS_GEMM_DEFAULT);
-  return cublasSgemmStridedBatched(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, lda, sA, B, ldb, sB, &be, C, ldc,
-                                   sC, batch);
+static int gemm_sb(cudaStream_t st, int m, int n, int k, const double2* A, int lda, long long sA, const double2* B,
+                   int ldb, long long sB, double2* C, int ldc, long long sC, int batch) {
+  return f64_gemm<double2>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
 }
-static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const double2* A, int lda, long long sA,
-                              const double2* B, int ldb, long long sB, double2* C, int ldc, long long sC, int batch) {
-  cudaStream_t st = nullptr;
-  cublasGetStream(hb, &st);
-  return f64_gemm<double2>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch) ? CUBLAS_STATUS_EXECUTION_FAILED
-                                                                                     : CUBLAS_STATUS_SUCCESS;
+static int gemm_sb(cudaStream_t st, int m, int n, int k, const float* A, int lda, long long sA, const float* B,
+                   int ldb, long long sB, float* C, int ldc, long long sC, int batch) {
+  return gemm_simt<float>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
 }
-static cublasStatus_t gemm_sb(cublasHandle_t hb, int m, int n, int k, const float2* A, int lda, long long sA,
-                              const float2* B, int ldb, long long sB, float2* C, int ldc, long long sC, int batch) {
-  const cuComplex al = make_cuComplex(-1.0f, 0.0f), be = make_cuComplex(1.0f, 0.0f);
+static int gemm_sb(cudaStream_t st, int m, int n, int k, const float2* A, int lda, long long sA, const float2* B,
+                   int ldb, long long sB, float2* C, int ldc, long long sC, int batch) {
   const int mode = g_c32_mode;
-  if (mode == 3 && g_tc_err.p && k > 32) {
-    // the depth-NBO trailing updates on this library's tcgen05 kernels (the
-    // depth-32 updates inside an outer block stay on SIMT FP32 below)
-    cudaStream_t st = nullptr;
-    cublasGetStream(hb, &st);
-    return tc_cgemm_run(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch, g_tc_ws, (int*)g_tc_err.p)
-               ? CUBLAS_STATUS_EXECUTION_FAILED
-               : CUBLAS_STATUS_SUCCESS;
-  }
-  if (mode > 0 && mode < 3)
-    return cublasGemmStridedBatchedEx(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, A, CUDA_C_32F, lda, sA, B, CUDA_C_32F,
-                                      ldb, sB, &be, C, CUDA_C_32F, ldc, sC, batch,
-                                      mode == 1 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F_EMULATED_16BFX9,
-                                      CUBLAS_GEMM_DEFAULT);
-  return cublasCgemmStridedBatched(hb, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &al, (const cuComplex*)A, lda, sA,
-                                   (const cuComplex*)B, ldb, sB, &be, (cuComplex*)C, ldc, sC, batch);
+  if ((mode == 3 || mode == 1) && g_tc_err.p && k > 32)
+    return tc_cgemm_run(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch, g_tc_ws, (int*)g_tc_err.p,
+                        mode == 3 ? 3 : 1);
+  return gemm_simt<float2>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
 }
 
 template <typename S> struct IsF64 { static const bool v = false; };
@@ -305,7 +292,7 @@ static bool coop_plan(int n, int nb, int batch, CoopPlan* pl) {
 
 // Blocked right-looking getrf for a batch of n x n matrices (stride sA).
 template <typename S>
-static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA, int lda, int n, int batch,
+static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, int batch,
                          int* ipiv, int* info, int nbo = 128) {
   // panel width: the L11 block of the TRSM lives in shared memory (<= 16 KB)
   const int nb = 32;
@@ -314,7 +301,7 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
   // leaves valid row indices behind for the interchanges that follow
   k_ipiv_identity<<<dim3(nblk(n, 256), batch), 256, 0, st>>>(ipiv, n); ++g_launches;
   typedef typename Sc<S>::R R;
-  const bool tc = g_c32_mode == 3 && std::is_same<S, float2>::value;
+  const bool tc = (g_c32_mode == 3 || g_c32_mode == 1) && std::is_same<S, float2>::value;
   const bool oz = IsF64<S>::v && f64_default() == 0;
   if (oz) {
     int rc = oz_err_reset(st);
@@ -434,7 +421,7 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
         // inside the outer block: U12 and the update of columns [k+kb, KE)
         const int nc = KE - k - kb;
         k_trsm_cols<S><<<dim3(nblk(nc, trsm_cols<S>()), batch), trsm_cols<S>(), 0, st>>>(A, sA, lda, k, kb, k + kb, KE); ++g_launches;
-        CKB(gemm_sb(hb, n - k - kb, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)(k + kb) * lda, lda,
+        CKG(gemm_sb(st, n - k - kb, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)(k + kb) * lda, lda,
                     sA, A + (k + kb) + (size_t)(k + kb) * lda, lda, sA, batch));
       }
     }
@@ -445,11 +432,11 @@ static int getrf_batched(cublasHandle_t hb, cudaStream_t st, S* A, long long sA,
         const int kb = std::min(nb, KE - k);
         k_trsm_cols<S><<<dim3(nblk(nc, trsm_cols<S>()), batch), trsm_cols<S>(), 0, st>>>(A, sA, lda, k, kb, KE, n); ++g_launches;
         if (k + kb < KE)
-          CKB(gemm_sb(hb, KE - k - kb, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)KE * lda, lda, sA,
+          CKG(gemm_sb(st, KE - k - kb, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)KE * lda, lda, sA,
                       A + (k + kb) + (size_t)KE * lda, lda, sA, batch));
       }
       // trailing update of depth KE - K
-      CKB(gemm_sb(hb, nc, nc, KE - K, A + KE + (size_t)K * lda, lda, sA, A + K + (size_t)KE * lda, lda, sA,
+      CKG(gemm_sb(st, nc, nc, KE - K, A + KE + (size_t)K * lda, lda, sA, A + K + (size_t)KE * lda, lda, sA,
                   A + KE + (size_t)KE * lda, lda, sA, batch));
     }
   }
@@ -502,7 +489,7 @@ __global__ void k_tune_fill(S* A, long long total) {
 static std::mutex g_tune_mu;
 static std::map<std::tuple<int, int, int, int>, int> g_tune;
 template <typename S>
-static int tuned_nbo(cublasHandle_t hb, cudaStream_t st, int n, int batch, int* ipiv, int* info, int* out) {
+static int tuned_nbo(cudaStream_t st, int n, int batch, int* ipiv, int* info, int* out) {
   *out = 128;
   const char* e = getenv("MFBEM_AUTOTUNE");
   if (e && std::string(e) == "0") return 0;
@@ -527,7 +514,7 @@ static int tuned_nbo(cublasHandle_t hb, cudaStream_t st, int n, int batch, int* 
   for (int c = 0; c < 3 && !rc; ++c) {
     k_tune_fill<S><<<152 * 8, 256, 0, st>>>(T, nn * batch); ++g_launches;
     cudaEventRecord(t0, st);
-    rc = getrf_batched<S>(hb, st, T, nn, n, n, batch, ipiv, info, cand[c]);
+    rc = getrf_batched<S>(st, T, nn, n, n, batch, ipiv, info, cand[c]);
     cudaEventRecord(t1, st);
     cudaEventSynchronize(t1);
     float ms = 0.0f;
@@ -773,29 +760,70 @@ __global__ void k_copy_vec(const SD* a, SD* b, long long n) {
     b[i] = a[i];
 }
 
-static cublasStatus_t gemv_res(cublasHandle_t hb, int n, const double* A, int lda, long long sA, const double* x,
-                               long long sx, double* r, long long sr, int batch) {
-  const double al = -1.0, be = 1.0;
-  return cublasDgemvStridedBatched(hb, CUBLAS_OP_N, n, n, &al, A, lda, sA, x, 1, sx, &be, r, 1, sr, batch);
+// ---------------------------------------------------------------------------
+// Batched FP64 GEMV of the refinement: y = y - A x (residual, y holding b on
+// entry) or y = A x, column-major n x n systems. Pass 1: per (row block of
+// 256, column chunk of GV_CH, system) the partial sum over the chunk's
+// columns, one thread per row (coalesced column reads, the chunk of x staged
+// in shared memory, four independent FMA chains); pass 2: the partials of
+// each row added in chunk order, so the result does not depend on scheduling.
+// ---------------------------------------------------------------------------
+constexpr int GV_CH = 256;
+__device__ __forceinline__ double2 vadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double vadd(double a, double b) { return a + b; }
+template <typename S>
+__global__ void __launch_bounds__(256) k_gemv_part(const S* A, long long sA, int lda, int n, const S* x, long long sx,
+                                                   S* part) {
+  __shared__ S xs[GV_CH];
+  const int b = blockIdx.z, c = blockIdx.y, i = blockIdx.x * 256 + threadIdx.x;
+  const int j0 = c * GV_CH, j1 = min(n, j0 + GV_CH);
+  for (int j = j0 + threadIdx.x; j < j1; j += 256) xs[j - j0] = x[sx * b + j];
+  __syncthreads();
+  if (i >= n) return;
+  const S* M = A + sA * b + i;
+  S a0 = Sc<S>::zero(), a1 = a0, a2 = a0, a3 = a0;
+  int j = j0;
+  for (; j + 3 < j1; j += 4) {
+    a0 = zfma(M[(size_t)j * lda], xs[j - j0], a0);
+    a1 = zfma(M[(size_t)(j + 1) * lda], xs[j + 1 - j0], a1);
+    a2 = zfma(M[(size_t)(j + 2) * lda], xs[j + 2 - j0], a2);
+    a3 = zfma(M[(size_t)(j + 3) * lda], xs[j + 3 - j0], a3);
+  }
+  for (; j < j1; ++j) a0 = zfma(M[(size_t)j * lda], xs[j - j0], a0);
+  part[((size_t)b * gridDim.y + c) * n + i] = vadd(vadd(a0, a1), vadd(a2, a3));
 }
-static cublasStatus_t gemv_res(cublasHandle_t hb, int n, const double2* A, int lda, long long sA, const double2* x,
-                               long long sx, double2* r, long long sr, int batch) {
-  const cuDoubleComplex al = make_cuDoubleComplex(-1.0, 0.0), be = make_cuDoubleComplex(1.0, 0.0);
-  return cublasZgemvStridedBatched(hb, CUBLAS_OP_N, n, n, &al, (const cuDoubleComplex*)A, lda, sA,
-                                   (const cuDoubleComplex*)x, 1, sx, &be, (cuDoubleComplex*)r, 1, sr, batch);
+template <typename S>
+__global__ void k_gemv_sum(const S* part, int nch, int n, S* y, long long sy, int residual) {
+  const int b = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  S s = Sc<S>::zero();
+  for (int c = 0; c < nch; ++c) s = vadd(s, part[((size_t)b * nch + c) * n + i]);
+  y[sy * b + i] = residual ? Sc<S>::sub(y[sy * b + i], s) : s;
 }
-
+static thread_local DevBuf g_gv_ws;
+template <typename S>
+static int gemv_run(cudaStream_t st, int n, const S* A, int lda, long long sA, const S* x, long long sx, S* y,
+                    long long sy, int batch, int residual) {
+  const int nch = (n + GV_CH - 1) / GV_CH;
+  int rc = ensure(g_gv_ws, sizeof(S) * (size_t)batch * nch * n);
+  if (rc) return rc;
+  S* part = (S*)g_gv_ws.p;
+  k_gemv_part<S><<<dim3(nblk(n, 256), nch, batch), 256, 0, st>>>(A, sA, lda, n, x, sx, part); ++g_launches;
+  k_gemv_sum<S><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(part, nch, n, y, sy, residual); ++g_launches;
+  CK(cudaGetLastError());
+  return 0;
+}
+// r = r - A x (r holds b on entry)
+template <typename S>
+static int gemv_res(cudaStream_t st, int n, const S* A, int lda, long long sA, const S* x, long long sx, S* r,
+                    long long sr, int batch) {
+  return gemv_run<S>(st, n, A, lda, sA, x, sx, r, sr, batch, 1);
+}
 // y = A x
-static cublasStatus_t gemv_apply(cublasHandle_t hb, int n, const double* A, int lda, long long sA, const double* x,
-                                 long long sx, double* y, long long sy, int batch) {
-  const double al = 1.0, be = 0.0;
-  return cublasDgemvStridedBatched(hb, CUBLAS_OP_N, n, n, &al, A, lda, sA, x, 1, sx, &be, y, 1, sy, batch);
-}
-static cublasStatus_t gemv_apply(cublasHandle_t hb, int n, const double2* A, int lda, long long sA, const double2* x,
-                                 long long sx, double2* y, long long sy, int batch) {
-  const cuDoubleComplex al = make_cuDoubleComplex(1.0, 0.0), be = make_cuDoubleComplex(0.0, 0.0);
-  return cublasZgemvStridedBatched(hb, CUBLAS_OP_N, n, n, &al, (const cuDoubleComplex*)A, lda, sA,
-                                   (const cuDoubleComplex*)x, 1, sx, &be, (cuDoubleComplex*)y, 1, sy, batch);
+template <typename S>
+static int gemv_apply(cudaStream_t st, int n, const S* A, int lda, long long sA, const S* x, long long sx, S* y,
+                      long long sy, int batch) {
+  return gemv_run<S>(st, n, A, lda, sA, x, sx, y, sy, batch, 0);
 }
 
 #include "mfbem_lse.cuh"
@@ -914,8 +942,9 @@ static int residual_check(MixCtx<SD, SF>& c, bool first, bool* all) {
   cudaStream_t st = c.h->st;
   const int n = c.n, batch = c.batch;
   const long long nn = (long long)n * n;
+  int rc;
   k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(c.b, c.r, (long long)n * batch); ++g_launches;
-  if (!first) CKB(gemv_res(c.h->blas, n, c.A, n, nn, c.x, n, c.r, n, batch));
+  if (!first && (rc = gemv_res<SD>(st, n, c.A, n, nn, c.x, n, c.r, n, batch))) return rc;
   k_vecmax<SD><<<batch, 256, 0, st>>>(c.r, n, n, c.nrm, 0, 8); ++g_launches;
   k_vecmax<SD><<<batch, 256, 0, st>>>(c.x, n, n, c.nrm, 1, 8); ++g_launches;
   std::vector<double> hn(8 * (size_t)batch);
@@ -1050,7 +1079,7 @@ static int refine_gmres(MixCtx<SD, SF>& c, int* conv) {
     int j = 0;
     for (; j < m; ++j) {
       // w = M^-1 A V_j
-      CKB(gemv_apply(c.h->blas, n, c.A, n, nn, V + (long long)j * n, sV, c.r, n, batch));
+      if ((rc = gemv_apply<SD>(st, n, c.A, n, nn, V + (long long)j * n, sV, c.r, n, batch))) return rc;
       if ((rc = precond(c, c.r, w))) return rc;
       // classical Gram-Schmidt, twice
       k_bdot<SD><<<dim3(j + 1, batch), 256, 0, st>>>(V, sV, j + 1, w, n, n, hc, m + 1); ++g_launches;
@@ -1148,12 +1177,12 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
   if (precision != 0) {
     g_c32_mode = c32_default();
     if (g_c32_mode == 1 && h->tf32_stalled) g_c32_mode = 0;
-    if ((rc = tuned_nbo<SF>(h->blas, st, n, batch, ipiv, info, &nbo))) return rc;
+    if ((rc = tuned_nbo<SF>(st, n, batch, ipiv, info, &nbo))) return rc;
   }
   cudaEventRecord(e0, st);
   std::vector<int> hinfo(batch);
   if (precision == 0) {
-    if ((rc = getrf_batched<SD>(h->blas, st, A, nn, n, n, batch, ipiv, info))) return rc;
+    if ((rc = getrf_batched<SD>(st, A, nn, n, n, batch, ipiv, info))) return rc;
     cudaEventRecord(e1, st);
     k_copy_vec<SD><<<nblk((long long)n * batch, 256), 256, 0, st>>>(b, x, (long long)n * batch); ++g_launches;
     if ((rc = getrs_batched<SD>(st, A, nn, n, n, ipiv, n, x, n, batch))) return rc;
@@ -1185,7 +1214,7 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     k_demote_rowabs<SD, SF><<<dim3(nblk(n, 256), nblk(n, 128), batch), 256, 0, st>>>(A, c.A32, nn, n, n, rows); ++g_launches;
     k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, c.nrm, 3, 8); ++g_launches;
     k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, c.nrm, 2, 8); ++g_launches;
-    if ((rc = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info, nbo))) return rc;
+    if ((rc = getrf_batched<SF>(st, c.A32, nn, n, n, batch, ipiv, info, nbo))) return rc;
     cudaEventRecord(e1, st);
     CK(cudaMemsetAsync(x, 0, sizeof(SD) * (size_t)n * batch, st));
     // refinement: precision 1, classical refinement until it converges or
@@ -1205,8 +1234,8 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
       ++c.refactor;
       k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, c.A32, nn * batch); ++g_launches;
       int nb2 = 128;
-      int r = tuned_nbo<SF>(h->blas, st, n, batch, ipiv, info, &nb2);
-      if (!r) r = getrf_batched<SF>(h->blas, st, c.A32, nn, n, n, batch, ipiv, info, nb2);
+      int r = tuned_nbo<SF>(st, n, batch, ipiv, info, &nb2);
+      if (!r) r = getrf_batched<SF>(st, c.A32, nn, n, n, batch, ipiv, info, nb2);
       cudaEventRecord(f1, st);
       cudaEventSynchronize(f1);
       float t = 0.0f;
@@ -1219,13 +1248,13 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     };
     if (gm_first) {
       if ((rc = refine_gmres(c, &conv))) return rc;
-      if (!conv && (g_c32_mode == 1 || g_c32_mode == 2)) {
+      if (!conv && g_c32_mode == 1) {
         if ((rc = refactor())) return rc;
         if ((rc = refine_gmres(c, &conv))) return rc;
       }
     } else {
       if ((rc = refine_classical(c, &conv))) return rc;
-      if (!conv && (g_c32_mode == 1 || g_c32_mode == 2)) {
+      if (!conv && g_c32_mode == 1) {
         if ((rc = refactor())) return rc;
         if ((rc = refine_classical(c, &conv))) return rc;
       }

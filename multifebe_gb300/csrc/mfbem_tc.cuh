@@ -321,7 +321,8 @@ __device__ __forceinline__ void tc_expect(uint32_t mbar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
 }
 
-// C -= A B from pre-split tiles: CTA (row tile, column tile, batch); thread 0
+// C -= A B from pre-split tiles (passes 3: the 3xTF32 products; 1: hi x hi
+// only, TF32-accurate); CTA (row tile, column tile, batch); thread 0
 // runs the copy / MMA pipeline (stage s: 4 x 8 KB tiles, "full" barrier fb[s]
 // completed by the bulk copies, "free" barrier mb[s] by the MMA commit), all
 // four warps run the epilogue; 64 KB of shared memory, so three CTAs share an
@@ -329,7 +330,7 @@ __device__ __forceinline__ void tc_expect(uint32_t mbar, uint32_t bytes) {
 __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, const uint32_t* Alo,
                                                           const uint32_t* Bhi, const uint32_t* Blo, int nmt, int nnt,
                                                           int nkc, float2* C, int ldc, long long sC, int m, int n,
-                                                          int* err, long long spin) {
+                                                          int* err, long long spin, int passes) {
   extern __shared__ __align__(1024) unsigned char tsm[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(tsm + 2 * TQ_STAGE_BYTES);  // fb[2], mb[2]
   uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + 2 * TQ_STAGE_BYTES + 32);
@@ -395,12 +396,14 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
                 tmem),
             "l"(dah), "l"(dbh), "r"(idesc), "r"(acc0)
             : "memory");
-        asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(tmem), "l"(dah), "l"(dbl),
-                     "r"(idesc)
-                     : "memory");
-        asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(tmem), "l"(dal), "l"(dbh),
-                     "r"(idesc)
-                     : "memory");
+        if (passes == 3) {
+          asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(tmem), "l"(dah), "l"(dbl),
+                       "r"(idesc)
+                       : "memory");
+          asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;" ::"r"(tmem), "l"(dal), "l"(dbh),
+                       "r"(idesc)
+                       : "memory");
+        }
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb[s])
                    : "memory");

@@ -7,12 +7,14 @@
   surface patch 40x40, 14883 DOF, a0 = 0.5: displacements u and tractions t
   compared separately
 
-Tolerances (max-norm relative, per frequency): plain FP64 path <= 1e-10
-(<= 1e-12 / rcond on the slab, whose systems are the least well conditioned:
-the FP64 method's own sensitivity, printed beside the measured error); mixed
-path (complex64 LU + FP64 refinement) <= 1e-8. The mixed path's assembled
-binary64 system (double-float evaluation) is compared entry by entry with the
-oracle's system on two small meshes.
+Tolerances (max-norm relative, per frequency): plain FP64 path <= 1e-10,
+mixed path (complex64 LU + FP64 refinement) <= 1e-8; on the slab, whose
+systems are ill-conditioned (1/rcond up to about 1e7), both against the oracle
+within max(their bar, 1e-12 / rcond) -- the FP64 method's own sensitivity to
+the ~1e-12 differences of two FP64 assemblies -- and the mixed path within
+1e-8 of the plain path. The mixed path's assembled binary64 system
+(double-float evaluation) is compared entry by entry with the oracle's system
+on two small meshes.
 """
 import numpy as np
 import pytest
@@ -68,16 +70,22 @@ def slab16(oracle):
     return deck, mat, om, P, [x for x, _ in xr], [r for _, r in xr]
 
 
-@pytest.mark.parametrize("precision", ["plain", "mixed"])
-def test_slab16_sweep(slab16, precision):
+def test_slab16_sweep(slab16):
+    """The slab's systems are ill-conditioned (1/rcond about 1e7 at a0 = 0.2):
+    the device and the oracle assemble the same system to about 1e-12, and
+    that difference is amplified in both paths alike. Both paths against the
+    oracle: within max(their bar, 1e-12 / rcond); the mixed path against the
+    plain FP64 GPU path on the same assembled systems: <= 1e-8."""
     deck, mat, om, P, xs, rconds = slab16
     R = BemRegion(deck)
-    X = R.sweep_harela(mat, om, precision=precision)
+    Xp = R.sweep_harela(mat, om, precision="plain")
+    Xm = R.sweep_harela(mat, om, precision="mixed")
     for i in range(len(om)):
-        e = rel(X[i], xs[i])
-        tol = max(1e-10, 1e-12 / rconds[i]) if precision == "plain" else 1e-8
-        print(precision, "a0", [0.2, 1.0][i], "rel err", e, "1/rcond", 1.0 / rconds[i], "tolerance", tol)
-        assert e < tol
+        ep, em, emp = rel(Xp[i], xs[i]), rel(Xm[i], xs[i]), rel(Xm[i], Xp[i])
+        print("a0", [0.2, 1.0][i], "plain", ep, "mixed", em, "mixed vs plain", emp, "1/rcond", 1.0 / rconds[i])
+        assert ep < max(1e-10, 1e-12 / rconds[i])
+        assert em < max(1e-8, 1e-12 / rconds[i])
+        assert emp < 1e-8
     R.close()
 
 
