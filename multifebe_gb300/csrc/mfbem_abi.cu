@@ -80,7 +80,7 @@ struct mfbem_handle {
   // once, so later solves factorise with SIMT FP32 updates from the start
   bool tf32_stalled = false;
   cudaStream_t st = nullptr;
-  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, Af, geo_f, gm;
+  DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, geo_f, gm;
   mfbem_stats stats{};
   // systems of the last mfbem_sweep_harela call (read back by a test hook)
   int last_nf = 0;
@@ -579,7 +579,7 @@ extern "C" int mfbem_mesh_release(mfbem_handle* h) {
     cudaDeviceSynchronize();
     for (auto& o : h->owned) pool_give(o.first, o.second, h->dev);
     for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu, &h->parf,
-                      &h->pphi_f, &h->Af, &h->geo_f, &h->gm})
+                      &h->pphi_f, &h->geo_f, &h->gm})
       pool_give(b->p, b->bytes, b->dev);
     if (h->st) {
       std::lock_guard<std::mutex> lk(g_pool_mu);
@@ -635,7 +635,7 @@ struct AsmTimes {
 template <class POL>
 static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, int nf, double* A, size_t lda,
                            size_t astride, double* b, size_t bstride, AsmTimes* tm = nullptr,
-                           const HarParF* pf = nullptr, const ff* dsf = nullptr, float4* Af = nullptr,
+                           const HarParF* pf = nullptr, const ff* dsf = nullptr, bool mixed = false,
                            const ff* sgf = nullptr, const ff* lgf = nullptr) {
   const DMesh& m = h->m;
   constexpr int WPB = 4;
@@ -645,8 +645,9 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
   if (tm) cudaEventRecord(tm->ev[0], h->st);
   if (m.nreg > 0) {
     if constexpr (std::is_same<POL, PolHarmonic>::value) {
-      if (pf && dsf && Af) {
-        k_mixed<MIX_REG, WPB><<<g, WPB * 32, 0, h->st>>>(m, pf, dsf, nullptr, nf, Af, lda, astride / 2, b, bstride);
+      if (mixed && pf && dsf) {
+        k_mixed<MIX_REG, WPB><<<g, WPB * 32, 0, h->st>>>(m, pf, dsf, nullptr, nf, (double2*)A, lda, astride / 2, b,
+                                                         bstride);
       } else {
         k_reg<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
       }
@@ -657,24 +658,21 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
   }
   if (tm) cudaEventRecord(tm->ev[1], h->st);
   if (m.nadp > 0) {
-    if (Af && lgf) k_mixed<MIX_ADP, WPB><<<g, WPB * 32, 0, h->st>>>(m, pf, dsf, lgf, nf, Af, lda, astride / 2, b, bstride);
+    if (mixed && lgf)
+      k_mixed<MIX_ADP, WPB><<<g, WPB * 32, 0, h->st>>>(m, pf, dsf, lgf, nf, (double2*)A, lda, astride / 2, b, bstride);
     else k_adp<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
     ++g_launches;
   }
   if (tm) cudaEventRecord(tm->ev[2], h->st);
   // the singular kernels keep two combo sets per point: 2 warps per block
   if (m.nsing > 0) {
-    if (Af && sgf) k_mixed<MIX_SING, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pf, dsf, sgf, nf, Af, lda, astride / 2, b, bstride);
+    if (mixed && sgf)
+      k_mixed<MIX_SING, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pf, dsf, sgf, nf, (double2*)A, lda, astride / 2, b, bstride);
     else k_sing<POL, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
     ++g_launches;
   }
   if (tm) cudaEventRecord(tm->ev[3], h->st);
   k_free<POL><<<nblk(nw, 128), 128, 0, h->st>>>(m, pol, d_nu, nf, A, lda, astride, b, bstride, h->d_err); ++g_launches;
-  if (Af) {
-    // mixed: fold the df64 regular-pair sums into the binary64 systems
-    const long long ne_ = (long long)(astride / 2) * nf;
-    k_add_ff<<<152 * 16, 256, 0, h->st>>>((double2*)A, Af, ne_); ++g_launches;
-  }
   if (tm) cudaEventRecord(tm->ev[4], h->st);
   CK(cudaGetLastError());
   return 0;

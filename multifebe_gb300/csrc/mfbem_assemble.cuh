@@ -752,10 +752,12 @@ template <> struct alignas(16) ComboF<true> {
 __device__ __forceinline__ cf cf_sub(cf a, cf b) { return cf_add(a, cf_neg(b)); }
 __device__ __forceinline__ cf cval_f(const ff* dcv_f, int dof) { return cf{dcv_f[2 * (size_t)dof], dcv_f[2 * (size_t)dof + 1]}; }
 // df64 complex entry {re.hi, re.lo, im.hi, im.lo} += v
-__device__ __forceinline__ void addAf(float4* Af, size_t idx, cf v) {
-  float4 a = Af[idx];
-  ff re = ff_add(ff{a.x, a.y}, v.re), im = ff_add(ff{a.z, a.w}, v.im);
-  Af[idx] = make_float4(re.hi, re.lo, im.hi, im.lo);
+// A(idx) += v: the pair's double-float sum rounded once to binary64
+__device__ __forceinline__ void addAc(double2* A, size_t idx, cf v) {
+  double2 a = A[idx];
+  a.x += ff_to(v.re);
+  a.y += ff_to(v.im);
+  A[idx] = a;
 }
 __device__ __forceinline__ void add3(cf bc[3], int i, cf v) {
   if (i == 0) bc[0] = cf_add(bc[0], v);
@@ -764,12 +766,12 @@ __device__ __forceinline__ void add3(cf bc[3], int i, cf v) {
 }
 
 // scale, reverse and scatter this lane's outputs of one pair (the scatter of
-// flush_pair in double-float): A entries into the df64 buffer Af, prescribed
-// values into the lane's b partial sums bc. hp (singular pairs only): static
+// flush_pair in double-float): A entries added to the binary64 system,
+// prescribed values into the lane's b partial sums bc. hp (singular pairs only): static
 // line integrals hli[9] and phi_i[8] of the pair; their CPV part
 // T2[0] hli(il,ik) phi_i(kn) is added to the h outputs.
 __device__ __forceinline__ void flush_pair_ff(const DMesh& m, const HarParF& q, const ff* dcv_f, int dn, int e,
-                                              const cf acc[kAcc], float4* Af, size_t lda, cf bc[3], const ff* hp) {
+                                              const cf acc[kAcc], double2* Ac, size_t lda, cf bc[3], const ff* hp) {
   const int lane = threadIdx.x & 31;
   const bool rev = m.rev[e] != 0;
 #pragma unroll 1
@@ -783,7 +785,7 @@ __device__ __forceinline__ void flush_pair_ff(const DMesh& m, const HarParF& q, 
       cf v = cf_mul(aj, q.cte_t);
       if (rev) v = cf_neg(v);
       const int dof = m.edof[8 * e + kn] + ik;
-      if (m.dct[dof] == 1) addAf(Af, (size_t)dof * lda + 3 * (size_t)dn + il, v);
+      if (m.dct[dof] == 1) addAc(Ac, (size_t)dof * lda + 3 * (size_t)dn + il, v);
       else add3(bc, il, cf_neg(cf_mul(v, cval_f(dcv_f, dof))));
     } else {
       const int qq = o - 72, kn = qq / 6, sidx = qq % 6, il = sym_il(sidx), ik = sym_ik(sidx);
@@ -791,7 +793,7 @@ __device__ __forceinline__ void flush_pair_ff(const DMesh& m, const HarParF& q, 
       for (int t = 0; t < (il == ik ? 1 : 2); ++t) {
         const int r_ = t ? ik : il, c_ = t ? il : ik;
         const int dof = m.edof[8 * e + kn] + c_;
-        if (m.dct[dof] == 0) addAf(Af, (size_t)dof * lda + 3 * (size_t)dn + r_, cf_neg(v));
+        if (m.dct[dof] == 0) addAc(Ac, (size_t)dof * lda + 3 * (size_t)dn + r_, cf_neg(v));
         else add3(bc, r_, cf_mul(v, cval_f(dcv_f, dof)));
       }
     }
@@ -858,15 +860,15 @@ enum MixKind { MIX_REG = 0, MIX_ADP = 1, MIX_SING = 2 };
 
 // Mixed-precision pair kernels (time-harmonic): one warp per (DOF node,
 // frequency), the two-phase scheme of k_reg, all arithmetic after x - x_i in
-// double-float. Af: df64 accumulation buffer with the entry layout of A (entry
-// stride astride_e per frequency), added into the binary64 A by k_add_ff after
-// the other assembly kernels. dsf: df64 copies of phi*J*w [ne][ptot][8], unit
+// double-float; each pair's sums are rounded once to binary64 and added to
+// the system Ac (complex entries, stride astride_e per frequency; the warp
+// owns its node's rows, so no other warp writes them). dsf: df64 copies of phi*J*w [ne][ptot][8], unit
 // normals [ne][ptot][3] and prescribed values [ndof][2]; gf: df64 copy of the
 // frequency-independent point geometry (leaf_geo for adaptive, sing_geo for
 // singular pairs), component-major.
 template <int KIND, int WPB>
 __global__ void __launch_bounds__(WPB * 32, 4) k_mixed(DMesh m, const HarParF* pf, const ff* dsf, const ff* gf, int nf,
-                                                       float4* Af, size_t lda, size_t astride_e, double* b,
+                                                       double2* Ac, size_t lda, size_t astride_e, double* b,
                                                        size_t bstride) {
   constexpr bool SG = KIND == MIX_SING;
   __shared__ ComboF<SG> sm[WPB][32];
@@ -880,7 +882,7 @@ __global__ void __launch_bounds__(WPB * 32, 4) k_mixed(DMesh m, const HarParF* p
   const ff* pphi_f = dsf;
   const ff* pn_f = dsf + 8LL * m.ne * m.ptot;
   const ff* dcv_f = pn_f + 3LL * m.ne * m.ptot;
-  float4* Aff = Af + astride_e * f;
+  double2* Acf = Ac + astride_e * f;
   cf bc[3] = {cf_zero(), cf_zero(), cf_zero()};
   for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
     int s0, s1;
@@ -941,7 +943,7 @@ __global__ void __launch_bounds__(WPB * 32, 4) k_mixed(DMesh m, const HarParF* p
         if (jp != cur) {
           if (cur >= 0) {
             const int e = KIND == MIX_REG ? (m.reg_pair[cur] & 0xFFFFFF) : (KIND == MIX_ADP ? m.adp_e[cur] : m.sing_e[cur]);
-            flush_pair_ff(m, Q, dcv_f, dn, e, acc, Aff, lda, bc, SG ? hps[w] : nullptr);
+            flush_pair_ff(m, Q, dcv_f, dn, e, acc, Acf, lda, bc, SG ? hps[w] : nullptr);
           }
           cur = jp;
           for (int j = 0; j < kAcc; ++j) acc[j] = cf_zero();
@@ -992,17 +994,6 @@ __global__ void __launch_bounds__(WPB * 32, 4) k_mixed(DMesh m, const HarParF* p
       bf[2 * (3 * (size_t)dn + il)] += ff_to(v.re);
       bf[2 * (3 * (size_t)dn + il) + 1] += ff_to(v.im);
     }
-  }
-}
-
-// A += Af (df64 entries to binary64), n complex entries
-__global__ void k_add_ff(double2* A, const float4* Af, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const float4 a = Af[i];
-    double2 x = A[i];
-    x.x += (double)a.x + (double)a.y;
-    x.y += (double)a.z + (double)a.w;
-    A[i] = x;
   }
 }
 

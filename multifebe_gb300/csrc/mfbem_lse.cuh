@@ -683,6 +683,7 @@ static int solve_dropin(int32_t n, double* A, int32_t* ipiv, int32_t aodim, doub
   int* isgn = (int*)(bits + n);
   double* red = (double*)(((uintptr_t)(isgn + n) + 63) / 64 * 64);
   LseWork w{st, red, di + 2};
+  if ((rc = trsv_err_reset(st))) return rc;
   CK(cudaMemcpyAsync(dA, A, nn * es, cudaMemcpyHostToDevice, st));
   char eq = scaling ? *equed : 'N';
   if (factorize) {
@@ -742,7 +743,7 @@ static int solve_dropin(int32_t n, double* A, int32_t* ipiv, int32_t aodim, doub
   }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
-  return 0;
+  return trsv_err_check(st);
 }
 
 extern "C" int mfbem_solve_r(int32_t n, double* A, int32_t* ipiv, int32_t aodim, double* Ao, char* equed, double* r,

@@ -664,6 +664,110 @@ __global__ void __launch_bounds__(128) k_trsv_diag64(const S* A, long long strid
 }
 
 // ---------------------------------------------------------------------------
+// Triangular solve of getrs in one launch per triangle (no counterpart in the
+// reference, which calls ?getrs): the rows are cut in blocks of 64; a CTA takes
+// work items (system, block) in solve order from a global counter, adds the
+// contributions of the blocks already solved as their ready flags appear
+// (L or U read once, 64 contiguous entries per column), solves its 64 x 64
+// diagonal block in one warp (shuffles) and publishes x and its flag. Items are
+// claimed in dependency order, so every block an item waits for is held by a
+// CTA that is already running: no co-residency is needed. Waits on flags are
+// bounded; a wait that gives up sets *err and the CTA publishes its block
+// anyway, so every other wait ends too.
+// LOWER: unit lower L, forward; else upper U with its diagonal, backward.
+// ready[b * nb + blk] must be 0 and *counter 0 on entry. Dynamic shared
+// memory: trsv_sf_smem<S>() bytes.
+// ---------------------------------------------------------------------------
+constexpr long long kTrsvSpin = 1LL << 22;
+template <typename S>
+constexpr size_t trsv_sf_smem() {
+  return sizeof(S) * (64 * 65 + 4 * 64);
+}
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+template <typename S, bool LOWER>
+__global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int lda, int n, S* x, long long sx,
+                                                 int batch, int nb, unsigned* counter, int* ready, int* err,
+                                                 long long spin) {
+  // dynamic shared memory: D [64 x 65] (diagonal block, column-major), part [4][64]
+  extern __shared__ __align__(16) unsigned char sfraw[];
+  S* D = reinterpret_cast<S*>(sfraw);
+  S (*part)[64] = reinterpret_cast<S (*)[64]>(D + 64 * 65);
+  __shared__ int s_item;
+  const int t = threadIdx.x, row = t & 63, grp = t >> 6;
+  const long long lim = spin > 0 ? spin : kTrsvSpin;
+  for (;;) {
+    if (t == 0) s_item = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= nb * batch) break;
+    const int b = item % batch, q = item / batch;
+    const int blk = LOWER ? q : nb - 1 - q;
+    const int r0 = blk * 64, w = min(64, n - r0);
+    const S* M = A + sA * b;
+    S* xb = x + sx * b;
+    // diagonal block into shared memory (used after the contributions)
+    for (int e = t; e < 64 * 64; e += 256) {
+      const int i = e & 63, j = e >> 6;
+      if (i < w && j < w) D[j * 65 + i] = M[(size_t)(r0 + j) * lda + r0 + i];
+    }
+    // contributions of the solved blocks, in the order they were solved
+    S acc = Sc<S>::zero();
+    for (int qq = 0; qq < q; ++qq) {
+      const int jb = LOWER ? qq : nb - 1 - qq;
+      if (t == 0) {
+        long long it = 0;
+        while (ld_acquire_s32(ready + (size_t)b * nb + jb) == 0) {
+          if (++it > lim) {
+            atomicExch(err, 1);
+            break;
+          }
+        }
+      }
+      __syncthreads();
+      const int c0 = jb * 64, wc = min(64, n - c0);
+      if (row < w)
+        for (int c = grp; c < wc; c += 4)
+          acc = Sc<S>::add(acc, Sc<S>::mul(M[(size_t)(c0 + c) * lda + r0 + row], __ldcg(xb + c0 + c)));
+    }
+    part[grp][row] = acc;
+    __syncthreads();
+    if (t < 32) {
+      const int l = t;
+      S x0 = Sc<S>::zero(), x1 = Sc<S>::zero();
+      if (l < w) x0 = Sc<S>::sub(xb[r0 + l], Sc<S>::add(Sc<S>::add(part[0][l], part[1][l]), Sc<S>::add(part[2][l], part[3][l])));
+      if (l + 32 < w)
+        x1 = Sc<S>::sub(xb[r0 + l + 32], Sc<S>::add(Sc<S>::add(part[0][l + 32], part[1][l + 32]),
+                                                    Sc<S>::add(part[2][l + 32], part[3][l + 32])));
+      if (LOWER) {
+        for (int j = 0; j < w; ++j) {
+          const S xj = shfl_s(j < 32 ? x0 : x1, j & 31);
+          if (l > j && l < w) x0 = Sc<S>::sub(x0, Sc<S>::mul(D[j * 65 + l], xj));
+          if (l + 32 > j && l + 32 < w) x1 = Sc<S>::sub(x1, Sc<S>::mul(D[j * 65 + l + 32], xj));
+        }
+      } else {
+        for (int j = w - 1; j >= 0; --j) {
+          if (j < 32) { if (l == j) x0 = Sc<S>::div(x0, D[j * 65 + j]); }
+          else { if (l + 32 == j) x1 = Sc<S>::div(x1, D[j * 65 + j]); }
+          const S xj = shfl_s(j < 32 ? x0 : x1, j & 31);
+          if (l < j) x0 = Sc<S>::sub(x0, Sc<S>::mul(D[j * 65 + l], xj));
+          if (l + 32 < j) x1 = Sc<S>::sub(x1, Sc<S>::mul(D[j * 65 + l + 32], xj));
+        }
+      }
+      if (l < w) xb[r0 + l] = x0;
+      if (l + 32 < w) xb[r0 + l + 32] = x1;
+      __threadfence();
+      __syncwarp();
+      if (l == 0) atomicExch(ready + (size_t)b * nb + blk, 1);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
 // getrs (no transpose) for one right-hand side per matrix, blocked by TB rows:
 //   k_rhs_swap:     apply all interchanges to b (sequential, one thread per matrix)
 //   k_trsv_diag:    solve the TB x TB diagonal block (one CTA per matrix)

@@ -370,7 +370,6 @@ __global__ void __launch_bounds__(128, 1) k_oz_gemm(const uint32_t* At, const ui
         }
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          const int j = nt * OZ_BN + c0 + q;
           // exact integer sum of levels 0..4 in units of 2^-32 (|V| < 2^53)
           const long long i0 = (long long)__float2int_rn(__uint_as_float(v[0][q]));
           const long long i1 = (long long)__float2int_rn(__uint_as_float(v[1][q]) * 0x1p8f);

@@ -38,8 +38,8 @@ __global__ void k_ipiv_identity(int* ipiv, int n) {
 // 0 SIMT FP32 (k_gemm_simt), 1 tcgen05 TF32, one pass (TF32-accurate factors;
 // refinement in FP64 restores the accuracy and escalates to SIMT FP32 when it
 // stalls), 3 tcgen05 3xTF32 (FP32-accurate factors at tensor-core speed).
-// The tensor-core kernels take the complex updates of depth above 32; the
-// real ones and the depth-32 updates inside an outer block run on SIMT FP32.
+// The tensor-core kernels take the complex updates (tc_min_depth below); the
+// real ones run on SIMT FP32.
 // Default 3; MFBEM_FP32_GEMM=simt|tf32|tc3 overrides.
 static thread_local int g_c32_mode = 3;
 static int c32_default() {
@@ -214,6 +214,12 @@ static int f64_gemm(cudaStream_t st, int m, int n, int k, const S* A, int lda, l
   if (f64_default() == 1) return gemm_simt<S>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
   return oz_gemm_run<std::is_same<S, double2>::value>(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch);
 }
+// smallest depth of a complex update that goes to the tensor cores (32: the
+// updates inside an outer block too; MFBEM_TC_MIN_K overrides)
+static int tc_min_depth() {
+  const char* e = getenv("MFBEM_TC_MIN_K");
+  return e ? std::max(1, atoi(e)) : 32;
+}
 // C -= A B (batched) in the scalar type of the factorisation, as configured
 // above: FP64 (plain LU) or FP32 (mixed LU)
 static int gemm_sb(cudaStream_t st, int m, int n, int k, const double* A, int lda, long long sA, const double* B,
@@ -231,7 +237,7 @@ static int gemm_sb(cudaStream_t st, int m, int n, int k, const float* A, int lda
 static int gemm_sb(cudaStream_t st, int m, int n, int k, const float2* A, int lda, long long sA, const float2* B,
                    int ldb, long long sB, float2* C, int ldc, long long sC, int batch) {
   const int mode = g_c32_mode;
-  if ((mode == 3 || mode == 1) && g_tc_err.p && k > 32)
+  if ((mode == 3 || mode == 1) && g_tc_err.p && k >= tc_min_depth())
     return tc_cgemm_run(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch, g_tc_ws, (int*)g_tc_err.p,
                         mode == 3 ? 3 : 1);
   return gemm_simt<float2>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
@@ -581,7 +587,28 @@ __global__ void k_scatter_back(const S* tmp, int n, S* x, long long sx) {
   if (i >= n) return;
   x[sx * bi + i] = tmp[(size_t)n * bi + i];
 }
-static thread_local DevBuf g_rs_ws;
+static thread_local DevBuf g_rs_ws, g_sf_ws, g_sf_err;
+// triangular solves of getrs: one launch per triangle (default) or one pair of
+// launches per 64-row block (MFBEM_TRSV=blocked)
+static bool trsv_sync_free() {
+  const char* e = getenv("MFBEM_TRSV");
+  return !(e && std::string(e) == "blocked");
+}
+// the timeout flag of the one-launch triangular solves: zeroed before a
+// solve (all its getrs calls), read after it
+static int trsv_err_reset(cudaStream_t st) {
+  int rc = ensure(g_sf_err, sizeof(int));
+  if (rc) return rc;
+  CK(cudaMemsetAsync(g_sf_err.p, 0, sizeof(int), st));
+  return 0;
+}
+static int trsv_err_check(cudaStream_t st) {
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, g_sf_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (e) return fail(MFBEM_ETIMEOUT, "triangular solve: a wait on a solved block timed out");
+  return 0;
+}
 
 template <typename S>
 static int getrs_batched(cudaStream_t st, const S* A, long long sA, int lda, int n, const int* ipiv, long long sP,
@@ -606,6 +633,31 @@ static int getrs_batched(cudaStream_t st, const S* A, long long sA, int lda, int
     gathered = true;
   }
   if (!gathered) { k_rhs_swap2<S><<<nblk(batch, 64), 64, 0, st>>>(b, sb, n, ipiv, sP, batch); ++g_launches; }
+  if (trsv_sync_free()) {
+    // one launch per triangle (k_trsv_sf): ready flags [batch][nb] and a counter
+    const int nb = (n + 63) / 64;
+    int rc = ensure(g_sf_ws, sizeof(int) * ((size_t)batch * nb + 1));
+    if (rc) return rc;
+    if (!g_sf_err.p) return fail(MFBEM_ECUDA, "triangular solve: error flag not set up");
+    int* ready = (int*)g_sf_ws.p;
+    unsigned* ctr = (unsigned*)(ready + (size_t)batch * nb);
+    int* err = (int*)g_sf_err.p;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned g = (unsigned)std::max(1, std::min(batch * nb, 2 * nsm));
+    constexpr size_t smem = trsv_sf_smem<S>();
+    if (raise_smem_limit((const void*)k_trsv_sf<S, true>) || raise_smem_limit((const void*)k_trsv_sf<S, false>))
+      return fail(MFBEM_ECUDA, "shared-memory limit of the triangular solve");
+    CK(cudaMemsetAsync(g_sf_ws.p, 0, sizeof(int) * ((size_t)batch * nb + 1), st));
+    k_trsv_sf<S, true><<<g, 256, smem, st>>>(A, sA, lda, n, b, sb, batch, nb, ctr, ready, err, g_spin_limit.load());
+    ++g_launches;
+    CK(cudaMemsetAsync(g_sf_ws.p, 0, sizeof(int) * ((size_t)batch * nb + 1), st));
+    k_trsv_sf<S, false><<<g, 256, smem, st>>>(A, sA, lda, n, b, sb, batch, nb, ctr, ready, err, g_spin_limit.load());
+    ++g_launches;
+    CK(cudaGetLastError());
+    return 0;
+  }
   for (int r0 = 0; r0 < n; r0 += TB) {
     int w = std::min(TB, n - r0);
     k_trsv_diag64<S, true><<<batch, 128, dsm, st>>>(A, sA, lda, b, sb, r0, w); ++g_launches;
@@ -1167,6 +1219,7 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     return rc;
   int* ipiv = (int*)h->ipiv.p;
   int* info = (int*)h->info.p;
+  if ((rc = trsv_err_reset(st))) return rc;
   cudaEvent_t e0, e1, e2;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -1189,6 +1242,7 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     cudaEventRecord(e2, st);
     CK(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if ((rc = trsv_err_check(st))) return rc;
     stats->refinement_iterations = 0;
   } else {
     // FP32 copy of A, factor
@@ -1269,6 +1323,7 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     stats->gmres_iterations += c.inner;
     stats->refactorizations += c.refactor;
     stats->max_backward_error = std::max(stats->max_backward_error, c.maxbe);
+    if ((rc = trsv_err_check(st))) return rc;
     if (!conv) {
       cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
       return fail(MFBEM_ENOCONV, "iterative refinement did not reach the requested backward error");
@@ -1337,7 +1392,6 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   long long l0 = g_launches;
   const HarParF* pf = nullptr;
   const ff* dsf = nullptr;
-  float4* Af = nullptr;
   const ff *sgf = nullptr, *lgf = nullptr;
   if (precision >= 1) {
     // mixed: regular pairs in double-float (df64 datasets made once per mesh:
@@ -1361,14 +1415,12 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
     sgf = ngs ? (const ff*)h->geo_f.p : nullptr;
     lgf = ngl ? (const ff*)h->geo_f.p + ngs : nullptr;
     if ((rc = ensure(h->parf, sizeof(HarParF) * n_freq))) return rc;
-    if ((rc = ensure(h->Af, sizeof(float4) * nn * n_freq))) return rc;
     k_harpar_f<<<nblk(n_freq, 32), 32, 0, h->st>>>(dpar, (HarParF*)h->parf.p, n_freq); ++g_launches;
     pf = (const HarParF*)h->parf.p;
     dsf = (const ff*)h->pphi_f.p;
-    Af = (float4*)h->Af.p;
-    CK(cudaMemsetAsync(Af, 0, sizeof(float4) * nn * n_freq, h->st));
   }
-  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n, &tm, pf, dsf, Af, sgf, lgf)))
+  if ((rc = launch_assembly(h, pol, dnu, n_freq, (double*)A, n, 2 * nn, (double*)b, 2 * (size_t)n, &tm, pf, dsf,
+                            precision >= 1, sgf, lgf)))
     return rc;
   cudaEventRecord(a1, h->st);
   if ((rc = check_err(h))) return rc;
