@@ -260,6 +260,9 @@ def run_gpu(args):
         plain_ms.append(sp["ms_assemble"] + sp["ms_factor"] + sp["ms_solve"])
     plain_step = statistics.mean(plain_ms)
     relerr = max(np.abs(Xm[i] - Xp[i]).max() / np.abs(Xp[i]).max() for i in range(nf))
+    # the plain path with binary64 arithmetic in its trailing updates too
+    # (SIMT FMA on the FP64 pipe instead of the Ozaki-scheme tensor-core GEMM)
+    native = _plain_native(R, mat, om)
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
@@ -279,7 +282,9 @@ def run_gpu(args):
             "plain_fp64_gpu": {"value": nf / (plain_step / 1e3), "unit": "solves/s", "ms_per_step": plain_step,
                                "ms_factor": sp["ms_factor"], "ms_assemble": sp["ms_assemble"],
                                "ms_solve": sp["ms_solve"],
-                               "speedup_of_mixed": (nf / (per_step_ms / 1e3)) / (nf / (plain_step / 1e3))}}
+                               "speedup_of_mixed": (nf / (per_step_ms / 1e3)) / (nf / (plain_step / 1e3)),
+                               "trailing_updates": "FP64-accurate Ozaki scheme on the bf16 tensor cores"},
+            "plain_fp64_gpu_native": dict(native, speedup_of_mixed=native["ms_per_step"] / per_step_ms)}
     line["roofline"] = roofline(st, n, nf)
     if args.precision_form:
         line["precision_form"] = precision_form()
@@ -300,6 +305,28 @@ def run_gpu(args):
                                 "sample": f"unavailable: {ex}"}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def _plain_native(R, mat, om, steps=1):
+    """The plain sweep with MFBEM_FP64_GEMM=dfma: binary64 FMA throughout (the
+    LU's trailing updates on the FP64 pipe). One untimed and `steps` timed sweeps."""
+    old = os.environ.get("MFBEM_FP64_GEMM")
+    os.environ["MFBEM_FP64_GEMM"] = "dfma"
+    try:
+        R.sweep_harela(mat, om, precision="plain")
+        ts = []
+        for _ in range(steps):
+            R.sweep_harela(mat, om, precision="plain")
+            st = R.last_stats
+            ts.append(st["ms_assemble"] + st["ms_factor"] + st["ms_solve"])
+    finally:
+        if old is None:
+            del os.environ["MFBEM_FP64_GEMM"]
+        else:
+            os.environ["MFBEM_FP64_GEMM"] = old
+    t = statistics.mean(ts)
+    return {"value": len(om) / (t / 1e3), "unit": "solves/s", "ms_per_step": t, "ms_factor": st["ms_factor"],
+            "trailing_updates": "binary64 SIMT FMA (own kernel)"}
 
 
 def _peaks():
@@ -367,33 +394,72 @@ def batching_form():
             "max_rel_err_vs_fp64": max(errs), "n_dof": [r_.n for r_ in regions]}
 
 
+def _pair_stats(err, cost, sel):
+    """Quadrature points and log10 relative errors (against the converged
+    integral) of the selected pairs."""
+    e, c = err[sel], cost[sel]
+    return {"pairs": int(sel.sum()), "points": int(c.sum()),
+            "frac_within_1e-7": float((e <= -7.0).mean()) if e.size else None,
+            "log10_err_p50": float(np.median(e)) if e.size else None,
+            "log10_err_p95": float(np.percentile(e, 95)) if e.size else None,
+            "log10_err_max": float(e.max()) if e.size else None}
+
+
 def learned_quadrature():
-    """The thin slab (16x16 + 16x1 quad8 per face, 5190 DOF, a0 0.2 and 1.0):
-    the network is trained on 8000 seeded random pairs labelled on the GPU, then
-    the slab's quasi-singular pairs take the learned rules (log10 tolerance -7).
-    Reported beside the reference adaptive rule: the assembly error against the
-    converged assembly (qsi_relative_error 1e-10) at a0 = 1.0, the adaptive-pair
-    quadrature points and kernel time, and the mixed sweep's solves/s."""
+    """The thin slab (16x16 + 16x1 quad8 per face, 5190 DOF, a0 0.2 and 1.0).
+    The network is trained on 8000 seeded random harmonic pairs (|k| x size in
+    0..0.5, the slab's material) labelled on the GPU. At equal tolerance 1e-7:
+    the reference adaptive rule at qsi_relative_error 1e-7 against the learned
+    rule at log10 tolerance -7 (falling back to that reference rule). Reported:
+    over the slab's own quasi-singular pairs, labelled against their converged
+    integrals (graded depth-9 rule, g = 30), the points and the error
+    distribution -- over all pairs and over the pairs the network changes --;
+    in the device sweep, the adaptive-pair points and kernel time, the
+    assembly error against the converged assembly (qsi_relative_error 1e-10)
+    and the sweep's solves/s."""
     import time as _t
     from multifebe_gb300 import meshgen as M, BemRegion, qlearn as Q
     t0 = _t.perf_counter()
-    e, p, k, kc = Q.random_pairs(8000, seed=21, kernel=0)
+    e, p, k, kc = Q.random_pairs(8000, seed=21, kernel=1)
     F, Y, C, V = Q.label_pairs(e, p, k, kc)
     t1 = _t.perf_counter()
     w = Q.init_weights(2)
     hist = Q.train(w, F, Y, V, steps=3000, batch=2048, lr=2e-3, seed=6)
     t2 = _t.perf_counter()
     deck, mat, om = M.workload(5)
+    # |k2| x element size at the highest frequency (largest slab element size 1/16)
+    k2 = float(om[-1]) / abs(np.sqrt(complex(mat["mu"]) / mat["rho"]))
+    kcl = k2 * (1.0 / 16.0)
+    out = {"workload": "harela slab 1x1x0.02, 16x16 + 16x1 quad8 per face, 5190 complex DOF, a0 0.2 and 1.0",
+           "training": {"pairs": 8000, "kernel": "harmonic", "valid": int(V.sum()), "label_s": t1 - t0,
+                        "train_s": t2 - t1, "steps": 3000, "loss_first": float(hist[:10].mean()),
+                        "loss_last": float(hist[-100:].mean())}}
+    tol = 1e-7
+    ref_c = Q.reference_candidate(tol)
+    R = BemRegion(deck, qsi_relative_error=tol)
+    # the slab's own quasi-singular pairs against their converged integrals
+    el, pts, _ = Q.mesh_adaptive_pairs(R)
+    Fm, Ym, Cm, Vm = Q.label_pairs(el, pts, 1, np.full(len(pts), kcl))
+    pred = Q.forward(w, Fm)
+    ch = Q.choose(pred, Cm, np.log10(tol), fallback=ref_c)
+    idx = np.arange(len(ch))
+    valid = Vm.astype(bool)
+    err_ref, cost_ref = Ym[:, ref_c], Cm[:, ref_c]
+    err_l, cost_l = Ym[idx, ch], Cm[idx, ch]
+    changed = valid & (ch != ref_c)
+    out["mesh_pairs"] = {
+        "adaptive_pairs": int(len(ch)), "labelled_valid": int(valid.sum()),
+        "reference_1e-7": _pair_stats(err_ref, cost_ref, valid),
+        "learned_1e-7": _pair_stats(err_l, cost_l, valid),
+        "changed_pairs": {"reference_1e-7": _pair_stats(err_ref, cost_ref, changed),
+                          "learned_1e-7": _pair_stats(err_l, cost_l, changed)},
+        "reference_1e-6": _pair_stats(Ym[:, Q.REF_DEFAULT], Cm[:, Q.REF_DEFAULT], valid)}
     Rc = BemRegion(deck, qsi_relative_error=1e-10)
     Ac, _ = Rc.build_lse_harela(mat, float(om[-1]))
     Rc.close()
-    R = BemRegion(deck)
-    out = {"workload": "harela slab 1x1x0.02, 16x16 + 16x1 quad8 per face, 5190 complex DOF, a0 0.2 and 1.0",
-           "training": {"pairs": 8000, "valid": int(V.sum()), "label_s": t1 - t0, "train_s": t2 - t1,
-                        "steps": 3000, "loss_first": float(hist[:10].mean()), "loss_last": float(hist[-100:].mean())}}
     scale = float(np.abs(Ac).max())
-    for name, tol in (("reference", None), ("learned", -7.0), ("learned_tol_1e-6.5", -6.5)):
-        nl = R.set_learned_quadrature(w if tol is not None else None, log10_tol=tol or -7.0)
+    for name, wt in (("reference_1e-7", None), ("learned_1e-7", w)):
+        nl = R.set_learned_quadrature(wt, log10_tol=np.log10(tol), kernel=1, kcl=kcl)
         A, _ = R.build_lse_harela(mat, float(om[-1]))
         err = float(np.abs(A - Ac).max() / scale)
         R.sweep_harela(mat, om, precision="mixed")
@@ -401,10 +467,7 @@ def learned_quadrature():
         st = R.last_stats
         out[name] = {"pairs_learned": nl, "points_adaptive": st["points_adaptive"],
                      "ms_adaptive_sweep": st["ms_adaptive"], "assembly_rel_err_vs_converged": err,
-                     "sweep_solves_per_s": len(om) / ((st["ms_assemble"] + st["ms_factor"] + st["ms_solve"]) / 1e3),
-                     "sweep_ms": {k: st[k] for k in ("ms_assemble", "ms_factor", "ms_solve")},
-                     "refinement": {k: st[k] for k in ("refinement_iterations", "gmres_iterations", "refactorizations",
-                                                       "max_backward_error")}}
+                     "sweep_solves_per_s": len(om) / ((st["ms_assemble"] + st["ms_factor"] + st["ms_solve"]) / 1e3)}
     R.close()
     return out
 
@@ -456,6 +519,7 @@ def precision_form(steps=3, warmup=1):
     Xp = R.sweep_harela(mat, om, precision="plain")
     sp = dict(R.last_stats)
     tp = sp["ms_assemble"] + sp["ms_factor"] + sp["ms_solve"]
+    nat = _plain_native(R, mat, om)
     out = {"workload": WORKLOAD_P, "n_dof": int(Xm.shape[1]), "steps": steps, "warmup": warmup,
            "mixed": {"value": 1e3 / tm, "unit": "solves/s", "ms_per_step": tm, "ms_assemble": st["ms_assemble"],
                      "ms_factor": st["ms_factor"], "ms_solve": st["ms_solve"],
@@ -465,6 +529,7 @@ def precision_form(steps=3, warmup=1):
                              "d2h_bytes_per_step": d2h}},
            "plain_fp64_gpu": {"value": 1e3 / tp, "unit": "solves/s", "ms_assemble": sp["ms_assemble"],
                               "ms_factor": sp["ms_factor"], "ms_solve": sp["ms_solve"]},
+           "plain_fp64_gpu_native": dict(nat, speedup_of_mixed=nat["ms_per_step"] / tm),
            "speedup_of_mixed": tp / tm,
            "rel_err_mixed_vs_fp64_gpu": float(np.abs(Xm - Xp).max() / np.abs(Xp).max())}
     try:

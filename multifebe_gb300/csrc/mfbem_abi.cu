@@ -1050,6 +1050,34 @@ extern "C" int mfbem_internal_f64_gemm(int32_t cplx, int32_t m, int32_t n, int32
   return rc;
 }
 
+// Test hook (not part of the reference interface): the quasi-singular
+// (adaptive) pairs of the mesh's classification. *n_pairs receives their
+// number; with xcp and elem given (room for *n_pairs on entry), each pair's
+// collocation point (3 doubles) and 0-based element.
+extern "C" int mfbem_internal_adaptive_pairs(mfbem_handle* h, int32_t* n_pairs, double* xcp, int32_t* elem) {
+  g_err.clear();
+  if (!h || !n_pairs) return fail(MFBEM_EARG, "invalid argument");
+  if (int rd = check_dev(h)) return rd;
+  const int ncp = h->m.ncp, ne = h->m.ne;
+  std::vector<uint8_t> cls((size_t)ncp * ne);
+  std::vector<double> cpx(3 * (size_t)ncp);
+  CK(cudaMemcpy(cls.data(), h->m.cls, cls.size(), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(cpx.data(), h->m.cpx, sizeof(double) * cpx.size(), cudaMemcpyDeviceToHost));
+  const int cap = *n_pairs;
+  int k = 0;
+  for (int c = 0; c < ncp; ++c)
+    for (int e = 0; e < ne; ++e)
+      if (cls[(size_t)c * ne + e] == CLS_ADP) {
+        if (xcp && elem && k < cap) {
+          for (int q = 0; q < 3; ++q) xcp[3 * (size_t)k + q] = cpx[3 * (size_t)c + q];
+          elem[k] = e;
+        }
+        ++k;
+      }
+  *n_pairs = k;
+  return 0;
+}
+
 // Test hook (not part of the reference interface): sets the iteration limit
 // of the bounded device waits (0 restores each kernel's own), so that a test
 // can make a wait give up and check the error status, the freed resources

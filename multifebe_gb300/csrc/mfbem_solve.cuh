@@ -243,6 +243,55 @@ static int gemm_sb(cudaStream_t st, int m, int n, int k, const float2* A, int ld
   return gemm_simt<float2>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
 }
 
+// ---------------------------------------------------------------------------
+// TRSM of the plain LU's row panel, U12 = inv(L11) A12 with L11 the kb x kb
+// unit lower block at (k, k): on the tensor cores as the FP64-accurate update
+// A12 := 0 - (-inv(L11)) A12 (k_trtri_neg, k_take_zero, then the Ozaki GEMM)
+// when the panel row is long; the substitution kernel k_trsm_cols otherwise.
+// ---------------------------------------------------------------------------
+// T[b] = -inv(L11) (column-major, ld 32), one warp per matrix, lane j builds
+// column j of the inverse by forward substitution (L11 staged in shared memory)
+template <typename S>
+__global__ void __launch_bounds__(32) k_trtri_neg(const S* A, long long sA, int lda, int k, int kb, S* T) {
+  __shared__ S L[32 * 33];
+  const int b = blockIdx.x, j = threadIdx.x;
+  const S* M = A + sA * b;
+  for (int t = j; t < kb * kb; t += 32) {
+    const int i = t % kb, c = t / kb;
+    L[c * 33 + i] = M[(size_t)(k + c) * lda + k + i];
+  }
+  __syncwarp();
+  S x[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    S v = Sc<S>::zero();
+    if (i == j) v = Sc<S>::one();
+    else if (i > j && i < kb) {
+#pragma unroll
+      for (int c = 0; c < i; ++c)
+        if (c >= j) v = Sc<S>::sub(v, Sc<S>::mul(L[c * 33 + i], x[c]));
+    }
+    x[i] = v;
+  }
+  S* Tb = T + 1024 * (size_t)b;
+#pragma unroll
+  for (int i = 0; i < 32; ++i) Tb[j * 32 + i] = Sc<S>::sub(Sc<S>::zero(), x[i]);
+}
+// W[b] (kb x nc, ld kb) = A[k:k+kb, c0:c0+nc]; that block of A set to zero
+template <typename S>
+__global__ void k_take_zero(S* A, long long sA, int lda, int k, int kb, int c0, int nc, int batch, S* W) {
+  const long long tot = (long long)batch * nc * kb;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < tot; g += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(g % kb);
+    const long long r = g / kb;
+    const int c = (int)(r % nc), b = (int)(r / nc);
+    S* a = A + sA * b + (size_t)(c0 + c) * lda + k + i;
+    W[g] = *a;
+    *a = Sc<S>::zero();
+  }
+}
+static thread_local DevBuf g_trsm_ws;
+
 template <typename S> struct IsF64 { static const bool v = false; };
 template <> struct IsF64<double> { static const bool v = true; };
 template <> struct IsF64<double2> { static const bool v = true; };
@@ -371,6 +420,29 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
   // one CTA per matrix and panel.
   const bool multi = IsF64<S>::v;
   int G = std::max(1, std::min(64, (n / 128) * 2 / std::max(1, batch) + 1));
+  // U12 of an inner panel: columns [c0, c1) of rows [k, k + kb)
+  auto trsm = [&](int k, int kb, int c0, int c1) -> int {
+    const int nc = c1 - c0;
+    if (nc <= 0) return 0;
+    if constexpr (IsF64<S>::v) {
+      if (oz && nc >= 128) {
+        const size_t tb = sizeof(S) * 1024 * (size_t)batch, wb = sizeof(S) * (size_t)kb * nc * batch;
+        int rc = ensure(g_trsm_ws, tb + wb);
+        if (rc) return rc;
+        S* T = (S*)g_trsm_ws.p;
+        S* W = (S*)((char*)g_trsm_ws.p + tb);
+        k_trtri_neg<S><<<batch, 32, 0, st>>>(A, sA, lda, k, kb, T); ++g_launches;
+        k_take_zero<S><<<(unsigned)std::min<long long>(nblk((long long)batch * nc * kb, 256), 152 * 16), 256, 0, st>>>(
+            A, sA, lda, k, kb, c0, nc, batch, W);
+        ++g_launches;
+        return oz_gemm_run<std::is_same<S, double2>::value>(st, T, 32, 1024, W, kb, (long long)kb * nc,
+                                                            A + k + (size_t)c0 * lda, lda, sA, kb, nc, kb, batch);
+      }
+    }
+    k_trsm_cols<S><<<dim3(nblk(nc, trsm_cols<S>()), batch), trsm_cols<S>(), 0, st>>>(A, sA, lda, k, kb, c0, c1);
+    ++g_launches;
+    return 0;
+  };
   // Two-level blocking: outer blocks of NBO columns are factorised with inner
   // panels of nb columns (updates restricted to the outer block), then one
   // trailing GEMM of depth NBO updates the rest of the matrix.
@@ -426,7 +498,7 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
       if (k + kb < KE) {
         // inside the outer block: U12 and the update of columns [k+kb, KE)
         const int nc = KE - k - kb;
-        k_trsm_cols<S><<<dim3(nblk(nc, trsm_cols<S>()), batch), trsm_cols<S>(), 0, st>>>(A, sA, lda, k, kb, k + kb, KE); ++g_launches;
+        CKG(trsm(k, kb, k + kb, KE));
         CKG(gemm_sb(st, n - k - kb, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)(k + kb) * lda, lda,
                     sA, A + (k + kb) + (size_t)(k + kb) * lda, lda, sA, batch));
       }
@@ -436,7 +508,7 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
       const int nc = n - KE;
       for (int k = K; k < KE; k += nb) {
         const int kb = std::min(nb, KE - k);
-        k_trsm_cols<S><<<dim3(nblk(nc, trsm_cols<S>()), batch), trsm_cols<S>(), 0, st>>>(A, sA, lda, k, kb, KE, n); ++g_launches;
+        CKG(trsm(k, kb, KE, n));
         if (k + kb < KE)
           CKG(gemm_sb(st, KE - k - kb, nc, kb, A + k + kb + (size_t)k * lda, lda, sA, A + k + (size_t)KE * lda, lda, sA,
                       A + (k + kb) + (size_t)KE * lda, lda, sA, batch));

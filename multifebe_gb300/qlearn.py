@@ -171,11 +171,37 @@ def train(w, feats, y, valid=None, steps=3000, batch=1024, lr=2e-3, seed=0):
     return hist
 
 
-def choose(pred, cost, log10_tol):
+def choose(pred, cost, log10_tol, fallback=REF_DEFAULT):
     """Per pair the cheapest candidate (by `cost`, the quadrature points) whose
-    predicted log10 error is <= log10_tol; the method's default rule
-    (REF_DEFAULT) when none qualifies -- the selection the library makes."""
+    predicted log10 error is <= log10_tol; `fallback` (the reference rule at
+    the mesh's qsi_relative_error: candidate 3 for the default 1e-6, 4 for
+    1e-7) when none qualifies -- the selection the library makes."""
     ok = (pred <= log10_tol) & (cost > 0)
     cc = np.where(ok, cost, np.iinfo(np.int32).max)
     c = cc.argmin(1)
-    return np.where(ok.any(1), c, REF_DEFAULT)
+    return np.where(ok.any(1), c, fallback)
+
+
+def reference_candidate(qsi_relative_error):
+    """Candidate index of the reference adaptive rule at a tolerance 10^-(3+c)."""
+    c = int(round(-np.log10(qsi_relative_error))) - 3
+    if not 0 <= c < NT:
+        raise ValueError("no reference-rule candidate for this tolerance")
+    return c
+
+
+def mesh_adaptive_pairs(region):
+    """The quasi-singular (adaptive) pairs of a mesh on the device: element
+    node coordinates [n,8,3] and collocation points [n,3], as label_pairs
+    takes them, and the element index of each pair."""
+    L = _abi.load()
+    if not getattr(L, "_ap_set", False):
+        L.mfbem_internal_adaptive_pairs.argtypes = [_vp, _vp, _vp, _vp]
+        L._ap_set = True
+    n = np.zeros(1, np.int32)
+    check(L.mfbem_internal_adaptive_pairs(region._h, n.ctypes.data, None, None))
+    pts = np.zeros((int(n[0]), 3))
+    el = np.zeros(int(n[0]), np.int32)
+    check(L.mfbem_internal_adaptive_pairs(region._h, n.ctypes.data, pts.ctypes.data, el.ctypes.data))
+    d = region.deck
+    return d.nodes[d.conn[el]], pts, el
