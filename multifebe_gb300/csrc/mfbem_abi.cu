@@ -79,6 +79,9 @@ struct mfbem_handle {
   // mixed solves: TF32 trailing updates stalled the refinement on this mesh
   // once, so later solves factorise with SIMT FP32 updates from the start
   bool tf32_stalled = false;
+  // mixed solves: FP32 factors without row interchanges failed (zero pivot or
+  // stalled refinement) on this mesh once, so later solves pivot from the start
+  bool nopiv_failed = false;
   cudaStream_t st = nullptr;
   DevBuf A, b, A32, x, r, work, ipiv, info, par, nu, parf, pphi_f, geo_f, gm;
   mfbem_stats stats{};

@@ -664,6 +664,83 @@ __global__ void __launch_bounds__(128) k_trsv_diag64(const S* A, long long strid
 }
 
 // ---------------------------------------------------------------------------
+// Inner panel without row interchanges (the mixed path's first attempt; its
+// factors are only a preconditioner for FP64 refinement, which falls back to
+// partial pivoting when it stalls): the kb x kb diagonal block is factorised
+// by one CTA in shared memory, then L21 = A21 inv(U11) row by row. No
+// cross-CTA pivot search per column. A zero or non-finite pivot sets info.
+// ---------------------------------------------------------------------------
+template <typename S>
+__global__ void __launch_bounds__(256) k_diag_lu_nopiv(S* A, long long sA, int lda, int k, int kb, int* info) {
+  __shared__ S D[32 * 33];
+  __shared__ int s_bad;
+  const int b = blockIdx.x, t = threadIdx.x;
+  S* M = A + sA * b;
+  for (int e = t; e < kb * kb; e += 256) {
+    const int i = e % kb, c = e / kb;
+    D[c * 33 + i] = M[(size_t)(k + c) * lda + k + i];
+  }
+  if (t == 0) s_bad = 0;
+  __syncthreads();
+  for (int j = 0; j < kb; ++j) {
+    const S d = D[j * 33 + j];
+    const float m = (float)Sc<S>::abs1(d);
+    if (!(m > 0.0f) || !isfinite(m)) {
+      if (t == 0 && !s_bad) {
+        s_bad = 1;
+        if (info[b] == 0) info[b] = k + j + 1;
+      }
+      break;
+    }
+    const S rcp = Sc<S>::rcp(d);
+    for (int i = j + 1 + t; i < kb; i += 256) D[j * 33 + i] = Sc<S>::mul(D[j * 33 + i], rcp);
+    __syncthreads();
+    const int w = kb - j - 1;
+    for (int e = t; e < w * w; e += 256) {
+      const int i = j + 1 + e % w, c = j + 1 + e / w;
+      D[c * 33 + i] = Sc<S>::sub(D[c * 33 + i], Sc<S>::mul(D[j * 33 + i], D[c * 33 + j]));
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  for (int e = t; e < kb * kb; e += 256) {
+    const int i = e % kb, c = e / kb;
+    M[(size_t)(k + c) * lda + k + i] = D[c * 33 + i];
+  }
+}
+// rows [r0, r1) of columns [k, k + kb): X := X inv(U11), U11 the upper
+// triangle (with its diagonal) of the factorised diagonal block; one thread per row
+template <typename S>
+__global__ void __launch_bounds__(128) k_trsm_runp(S* A, long long sA, int lda, int k, int kb, int r0, int r1) {
+  __shared__ S U[32 * 33];
+  const int b = blockIdx.y, t = threadIdx.x;
+  S* M = A + sA * b;
+  for (int e = t; e < kb * kb; e += 128) {
+    const int i = e % kb, c = e / kb;
+    if (i <= c) U[c * 33 + i] = M[(size_t)(k + c) * lda + k + i];
+  }
+  __syncthreads();
+  const int row = r0 + blockIdx.x * 128 + t;
+  if (row >= r1) return;
+  S x[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j)
+    if (j < kb) x[j] = M[(size_t)(k + j) * lda + row];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    if (j < kb) {
+      S v = x[j];
+#pragma unroll
+      for (int c = 0; c < j; ++c) v = Sc<S>::sub(v, Sc<S>::mul(x[c], U[j * 33 + c]));
+      x[j] = Sc<S>::div(v, U[j * 33 + j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 32; ++j)
+    if (j < kb) M[(size_t)(k + j) * lda + row] = x[j];
+}
+
+// ---------------------------------------------------------------------------
 // Triangular solve of getrs in one launch per triangle (no counterpart in the
 // reference, which calls ?getrs): the rows are cut in blocks of 64; a CTA takes
 // work items (system, block) in solve order from a global counter, adds the

@@ -292,6 +292,18 @@ __global__ void k_take_zero(S* A, long long sA, int lda, int k, int kb, int c0, 
 }
 static thread_local DevBuf g_trsm_ws;
 
+// Row interchanges of the mixed path's FP32 factorisation: none first (the
+// factors only precondition the FP64 refinement; the panel then needs no
+// pivot search across CTAs), partial pivoting when a zero pivot appears or
+// the refinement stalls (the handle remembers it for later solves of the
+// mesh). MFBEM_PIVOT=partial|none overrides. The plain path always pivots.
+static thread_local bool g_nopiv = false;
+static int pivot_default() {
+  const char* e = getenv("MFBEM_PIVOT");
+  if (!e) return -1;
+  return std::string(e) == "none" ? 1 : 0;
+}
+
 template <typename S> struct IsF64 { static const bool v = false; };
 template <> struct IsF64<double> { static const bool v = true; };
 template <> struct IsF64<double2> { static const bool v = true; };
@@ -357,6 +369,8 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
   k_ipiv_identity<<<dim3(nblk(n, 256), batch), 256, 0, st>>>(ipiv, n); ++g_launches;
   typedef typename Sc<S>::R R;
   const bool tc = (g_c32_mode == 3 || g_c32_mode == 1) && std::is_same<S, float2>::value;
+  // single precision only: the mixed path's unpivoted first attempt
+  const bool nopiv = g_nopiv && !IsF64<S>::v;
   const bool oz = IsF64<S>::v && f64_default() == 0;
   if (oz) {
     int rc = oz_err_reset(st);
@@ -451,7 +465,13 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
     const int KE = std::min(n, K + NBO);
     for (int k = K; k < KE; k += nb) {
       const int kb = std::min(nb, KE - k);
-      if (use_cl) {
+      if (nopiv) {
+        k_diag_lu_nopiv<S><<<batch, 256, 0, st>>>(A, sA, lda, k, kb, info); ++g_launches;
+        if (k + kb < n) {
+          k_trsm_runp<S><<<dim3(nblk(n - k - kb, 128), batch), 128, 0, st>>>(A, sA, lda, k, kb, k + kb, n);
+          ++g_launches;
+        }
+      } else if (use_cl) {
         const int chunk = (n - k + GC - 1) / GC;
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute at[1];
@@ -494,7 +514,7 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
         k_panel_cta<S, 512><<<batch, 512, 0, st>>>(A, sA, lda, n, k, kb, ipiv, info); ++g_launches;
       }
       int nout = n - kb;
-      if (nout > 0) { k_laswp<S><<<dim3(nblk(nout, 128), batch), 128, 0, st>>>(A, sA, lda, n, k, kb, ipiv); ++g_launches; }
+      if (nout > 0 && !nopiv) { k_laswp<S><<<dim3(nblk(nout, 128), batch), 128, 0, st>>>(A, sA, lda, n, k, kb, ipiv); ++g_launches; }
       if (k + kb < KE) {
         // inside the outer block: U12 and the update of columns [k+kb, KE)
         const int nc = KE - k - kb;
@@ -822,14 +842,16 @@ __global__ void k_vecmax(const S* v, long long sv, int n, double* out, int slot,
   int b = blockIdx.x;
   const S* x = v + sv * b;
   double m = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, amag(x[i]));
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  // the maximum propagates NaN (fmax would drop it and hide a diverged vector)
+  auto mx = [](double a, double b) { return (b > a || b != b) ? b : a; };
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = mx(m, amag(x[i]));
+  for (int o = 16; o > 0; o >>= 1) m = mx(m, __shfl_xor_sync(0xffffffffu, m, o));
   __shared__ double sm[32];
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x / 32] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)blockDim.x / 32; ++w) m = fmax(m, sm[w]);
-    m = fmax(m, sm[0]);
+    for (int w = 1; w < (int)blockDim.x / 32; ++w) m = mx(m, sm[w]);
+    m = mx(m, sm[0]);
     out[(size_t)nslots * b + slot] = m;
   }
 }
@@ -1048,6 +1070,8 @@ struct MixCtx {
   int* active;
   double tol;
   int it = 0, inner = 0, refactor = 0;
+  // the next residual is b itself (x = 0): at the start and after a restart
+  bool fresh = true;
   double maxbe = 0.0;
   std::vector<double> be;
   // classical refinement: ||d|| / ||x|| of each system's last correction
@@ -1080,11 +1104,13 @@ static int residual_check(MixCtx<SD, SF>& c, bool first, bool* all) {
   std::vector<int> hact(batch);
   c.maxbe = 0.0;
   bool any = false;
+  c.fresh = false;
   for (int bi = 0; bi < batch; ++bi) {
     double be = first ? 1.0 : hn[8 * bi + 0] / (hn[8 * bi + 3] * hn[8 * bi + 1] + hn[8 * bi + 2]);
+    if (!std::isfinite(be)) be = HUGE_VAL;  // non-finite residual or x: not converged
     c.be[bi] = be;
     c.maxbe = std::max(c.maxbe, be);
-    hact[bi] = (be > c.tol || c.dx[bi] > kFwdTol) ? 1 : 0;
+    hact[bi] = (!(be <= c.tol) || c.dx[bi] > kFwdTol) ? 1 : 0;
     any = any || hact[bi];
     c.rprev[bi] = hn[8 * bi + 0];
   }
@@ -1121,12 +1147,14 @@ static int refine_classical(MixCtx<SD, SF>& c, int* conv) {
   *conv = 0;
   for (int it = 0;; ++it) {
     bool all;
-    int rc = residual_check(c, c.it == 0, &all);
+    int rc = residual_check(c, c.fresh, &all);
     if (rc) return rc;
     if (all) { *conv = 1; return 0; }
     bool slow = false;
-    for (int bi = 0; bi < batch; ++bi)
+    for (int bi = 0; bi < batch; ++bi) {
       if (c.be[bi] > c.tol && it >= 2 && c.be[bi] > 0.25 * prev[bi]) slow = true;
+      if (c.be[bi] == HUGE_VAL && it >= 1) return 0;  // diverged (non-finite): give up at once
+    }
     prev = c.be;
     stall = slow ? stall + 1 : 0;
     if (stall >= 2 || it >= 30) return 0;
@@ -1179,7 +1207,7 @@ static int refine_gmres(MixCtx<SD, SF>& c, int* conv) {
   c.dx.assign(batch, 0.0);  // GMRES-IR stops on the backward error alone
   for (int outer = 0; outer < 10; ++outer) {
     bool all;
-    if ((rc = residual_check(c, c.it == 0 && outer == 0, &all))) return rc;
+    if ((rc = residual_check(c, c.fresh, &all))) return rc;
     if (all) { *conv = 1; return 0; }
     ++c.it;
     // z = M^-1 r -> V_0 = z / beta
@@ -1299,10 +1327,13 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
   // mixed: the outer block width of this size class (a first use runs the
   // autotuner, outside the timed factorisation)
   int nbo = 128;
+  g_nopiv = false;
   if (precision != 0) {
     g_c32_mode = c32_default();
     if (g_c32_mode == 1 && h->tf32_stalled) g_c32_mode = 0;
     if ((rc = tuned_nbo<SF>(st, n, batch, ipiv, info, &nbo))) return rc;
+    const int pv = pivot_default();
+    g_nopiv = pv == 1 || (pv < 0 && !h->nopiv_failed);
   }
   cudaEventRecord(e0, st);
   std::vector<int> hinfo(batch);
@@ -1341,6 +1372,20 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     k_vecmax<double><<<batch, 256, 0, st>>>(rows, n, n, c.nrm, 3, 8); ++g_launches;
     k_vecmax<SD><<<batch, 256, 0, st>>>(b, n, n, c.nrm, 2, 8); ++g_launches;
     if ((rc = getrf_batched<SF>(st, c.A32, nn, n, n, batch, ipiv, info, nbo))) return rc;
+    if (g_nopiv) {
+      // a zero or non-finite pivot without interchanges: factorise again with partial pivoting
+      CK(cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * batch, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      bool bad = false;
+      for (int bi = 0; bi < batch; ++bi) bad = bad || hinfo[bi] != 0;
+      if (bad) {
+        g_nopiv = false;
+        h->nopiv_failed = true;
+        ++c.refactor;
+        k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, c.A32, nn * batch); ++g_launches;
+        if ((rc = getrf_batched<SF>(st, c.A32, nn, n, n, batch, ipiv, info, nbo))) return rc;
+      }
+    }
     cudaEventRecord(e1, st);
     CK(cudaMemsetAsync(x, 0, sizeof(SD) * (size_t)n * batch, st));
     // refinement: precision 1, classical refinement until it converges or
@@ -1350,13 +1395,20 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     // again; GMRES-IR last. Precision 2: GMRES-IR first, refactorisation if it fails.
     const bool gm_first = precision == 2 || (getenv("MFBEM_REFINE") && std::string(getenv("MFBEM_REFINE")) == "gmres");
     int conv = 0;
+    // refactorisation after a stall: with partial pivoting if the factors had
+    // none, else with SIMT FP32 updates if they came from single-pass TF32
     auto refactor = [&]() -> int {
       cudaEvent_t f0, f1;
       cudaEventCreate(&f0);
       cudaEventCreate(&f1);
       cudaEventRecord(f0, st);
-      g_c32_mode = 0;
-      h->tf32_stalled = true;
+      if (g_nopiv) {
+        g_nopiv = false;
+        h->nopiv_failed = true;
+      } else {
+        g_c32_mode = 0;
+        h->tf32_stalled = true;
+      }
       ++c.refactor;
       k_demote<SD, SF><<<std::min(nblk(nn * batch, 256), 152u * 32u), 256, 0, st>>>(A, c.A32, nn * batch); ++g_launches;
       int nb2 = 128;
@@ -1372,14 +1424,26 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
       stats->ms_solve -= t;
       return r;
     };
+    auto restart = [&]() -> int {  // refinement from x = 0 after a refactorisation
+      c.fresh = true;
+      c.dx.clear();
+      c.rprev.clear();
+      CK(cudaMemsetAsync(x, 0, sizeof(SD) * (size_t)n * batch, st));
+      return 0;
+    };
     if (gm_first) {
       if ((rc = refine_gmres(c, &conv))) return rc;
-      if (!conv && g_c32_mode == 1) {
-        if ((rc = refactor())) return rc;
+      if (!conv && (g_nopiv || g_c32_mode == 1)) {
+        const bool np = g_nopiv;
+        if ((rc = refactor()) || (np && (rc = restart()))) return rc;
         if ((rc = refine_gmres(c, &conv))) return rc;
       }
     } else {
       if ((rc = refine_classical(c, &conv))) return rc;
+      if (!conv && g_nopiv) {
+        if ((rc = refactor()) || (rc = restart())) return rc;
+        if ((rc = refine_classical(c, &conv))) return rc;
+      }
       if (!conv && g_c32_mode == 1) {
         if ((rc = refactor())) return rc;
         if ((rc = refine_classical(c, &conv))) return rc;

@@ -273,3 +273,26 @@ def test_sweep_batch_of_uneven_meshes(oracle):
     assert rel(X[1][0], oracle.lu_solve(Ao, bo)) < 1e-8
     for r in regions:
         r.close()
+
+
+@pytest.mark.parametrize("pivot", ["none", "partial"])
+@pytest.mark.parametrize("name,mk", [("cube4", lambda: M.cube_clamped_top_traction(4)), ("slab4", lambda: M.slab(4, 1)),
+                                     ("patch8", lambda: M.surface_patch(10.0, 8, 1.0))],
+                         ids=["cube4", "slab4", "patch8"])
+def test_mixed_sweep_pivoting_modes(oracle, monkeypatch, pivot, name, mk):
+    """The mixed path's FP32 factors without row interchanges (the default
+    first attempt: no pivot search across CTAs in the panel) and with partial
+    pivoting both reach the FP64 oracle solution to 1e-8 after refinement."""
+    monkeypatch.setenv("MFBEM_PIVOT", pivot)
+    d = mk()
+    mat = M.viscoelastic(1.0, 0.3, 1.0, 0.05)
+    om = M.omega_from_a0([0.3, 1.2], mat)
+    R = BemRegion(d)
+    P = oracle.Problem(d)
+    X = R.sweep_harela(mat, om, precision="mixed")
+    for i, w in enumerate(om):
+        Ao, bo = P.assemble_harela(mat, w)
+        xo = oracle.lu_solve(Ao, bo)
+        assert rel(X[i], xo) < 1e-8, (pivot, name, i, rel(X[i], xo))
+    assert R.last_stats["max_backward_error"] <= 1e-12
+    R.close()
