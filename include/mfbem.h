@@ -189,6 +189,28 @@ int mfbem_msh_nodes(void* msh, int32_t* id, double* x);
 int mfbem_msh_elements(void* msh, int32_t* id, int32_t* type, int32_t* part, int32_t* offsets, int32_t* nodes);
 void mfbem_msh_free(void* msh);
 
+/* Nodal-solution export (*.nso), host only: the boundary-node records that
+   export_solution_mechanics_{harmonic,static}_nso write for an ordinary
+   boundary of a BE region (src/export_solution_mechanics_harmonic_nso.f90,
+   src/export_solution_mechanics_static_nso.f90), with the Fortran edit
+   descriptors of the export settings (src/read_export.f90:61-70,163-171):
+   integer columns I<int_w>, real columns kind 'E' (Ew.dEe, sci_*) or 'N'
+   (ENw.dEe, eng_*). One record per node in export order: C1 frequency index
+   (0 static), C2 frequency (0 static), C3-C5 region id / 1 / 2, C6-C8
+   boundary id / 1 / 1, C9 node id, C10-C12 coordinates, then u1..u3, t1..t3
+   (harmonic: complex_notation 2 re/im, 1 |z|/arg z, then the zero incident
+   field). values: [n][6] real (static) or [n][6] complex as re/im pairs.
+   header: text written first (NULL: none); append: add to the file.
+   Returns 0, or -1 with the reason in mfbem_nso_error(). */
+int mfbem_nso_write(const char* path, int32_t append, const char* header, int32_t harmonic, int32_t kf, double omega,
+                    int32_t region_id, int32_t n, const int32_t* node_id, const int32_t* boundary_id, const double* x,
+                    const double* values, int32_t int_w, char kind, int32_t w, int32_t d, int32_t e,
+                    int32_t complex_notation);
+const char* mfbem_nso_error(void);
+/* One value under a Fortran edit descriptor ('I' w, 'E' Ew.dEe, 'N'
+   ENw.dEe), right-justified in w characters, NUL-terminated into out. */
+int mfbem_fortran_format(char kind, int32_t w, int32_t d, int32_t e, double v, char* out);
+
 /* Device memory released with a mesh handle (mfbem_mesh_release) is kept by
    the library for later handles: buffers of at least 1 MB, up to a quarter of
    the device memory (environment MFBEM_DEVICE_CACHE_MB overrides the cap; 0

@@ -56,6 +56,8 @@ def build(force=False, verbose=False):
                         "-c", os.path.join(SRC, "host_prep.cpp"), "-o", os.path.join(OUT, "host_prep.o")],
         "host_msh.o": [cxx, "-std=c++17", "-O2", "-fPIC", *inc,
                        "-c", os.path.join(SRC, "host_msh.cpp"), "-o", os.path.join(OUT, "host_msh.o")],
+        "host_nso.o": [cxx, "-std=c++17", "-O2", "-fPIC", *inc,
+                       "-c", os.path.join(SRC, "host_nso.cpp"), "-o", os.path.join(OUT, "host_nso.o")],
         "mfbem_abi.o": [nvcc, ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", *inc,
                         "-Xptxas", "-v" if verbose else "-O3",
                         "-c", os.path.join(SRC, "mfbem_abi.cu"), "-o", os.path.join(OUT, "mfbem_abi.o")],
