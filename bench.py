@@ -447,8 +447,20 @@ def learned_quadrature():
     err_ref, cost_ref = Ym[:, ref_c], Cm[:, ref_c]
     err_l, cost_l = Ym[idx, ch], Cm[idx, ch]
     changed = valid & (ch != ref_c)
+    # the learned rule at equal accuracy: the loosest learned tolerance whose
+    # error distribution over the slab's pairs is no worse than the reference
+    # rule's at 1e-7 (fraction within 1e-7 and 95th percentile)
+    ref_st = _pair_stats(err_ref, cost_ref, valid)
+    eq = None
+    for lt in np.arange(-7.0, -10.01, -0.25):
+        c2 = Q.choose(pred, Cm, lt, fallback=ref_c)
+        st2 = _pair_stats(Ym[idx, c2], Cm[idx, c2], valid)
+        if st2["frac_within_1e-7"] >= ref_st["frac_within_1e-7"] and st2["log10_err_p95"] <= ref_st["log10_err_p95"]:
+            eq = dict(st2, log10_tol=float(lt), points_vs_reference=st2["points"] / ref_st["points"])
+            break
     out["mesh_pairs"] = {
         "adaptive_pairs": int(len(ch)), "labelled_valid": int(valid.sum()),
+        "learned_at_equal_accuracy": eq,
         "reference_1e-7": _pair_stats(err_ref, cost_ref, valid),
         "learned_1e-7": _pair_stats(err_l, cost_l, valid),
         "changed_pairs": {"reference_1e-7": _pair_stats(err_ref, cost_ref, changed),
@@ -458,8 +470,11 @@ def learned_quadrature():
     Ac, _ = Rc.build_lse_harela(mat, float(om[-1]))
     Rc.close()
     scale = float(np.abs(Ac).max())
-    for name, wt in (("reference_1e-7", None), ("learned_1e-7", w)):
-        nl = R.set_learned_quadrature(wt, log10_tol=np.log10(tol), kernel=1, kcl=kcl)
+    runs = [("reference_1e-7", None, np.log10(tol)), ("learned_1e-7", w, np.log10(tol))]
+    if eq is not None:
+        runs.append(("learned_equal_accuracy", w, eq["log10_tol"]))
+    for name, wt, lt in runs:
+        nl = R.set_learned_quadrature(wt, log10_tol=lt, kernel=1, kcl=kcl)
         A, _ = R.build_lse_harela(mat, float(om[-1]))
         err = float(np.abs(A - Ac).max() / scale)
         R.sweep_harela(mat, om, precision="mixed")

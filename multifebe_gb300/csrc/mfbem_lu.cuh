@@ -773,7 +773,7 @@ __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int l
   extern __shared__ __align__(16) unsigned char sfraw[];
   S* D = reinterpret_cast<S*>(sfraw);
   S (*part)[64] = reinterpret_cast<S (*)[64]>(D + 64 * 65);
-  __shared__ int s_item;
+  __shared__ int s_item, s_end;
   const int t = threadIdx.x, row = t & 63, grp = t >> 6;
   const long long lim = spin > 0 ? spin : kTrsvSpin;
   for (;;) {
@@ -791,24 +791,36 @@ __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int l
       const int i = e & 63, j = e >> 6;
       if (i < w && j < w) D[j * 65 + i] = M[(size_t)(r0 + j) * lda + r0 + i];
     }
-    // contributions of the solved blocks, in the order they were solved
+    // contributions of the solved blocks, in the order they were solved:
+    // thread 0 waits for the next one, then takes every later one already
+    // published too, so a CTA that is behind catches up with one barrier
     S acc = Sc<S>::zero();
-    for (int qq = 0; qq < q; ++qq) {
-      const int jb = LOWER ? qq : nb - 1 - qq;
+    for (int done = 0; done < q;) {
       if (t == 0) {
         long long it = 0;
-        while (ld_acquire_s32(ready + (size_t)b * nb + jb) == 0) {
+        const int jb0 = LOWER ? done : nb - 1 - done;
+        while (ld_acquire_s32(ready + (size_t)b * nb + jb0) == 0) {
           if (++it > lim) {
             atomicExch(err, 1);
             break;
           }
+          if (it > 64) __nanosleep(64);
         }
+        int e = done + 1;
+        while (e < q && ld_acquire_s32(ready + (size_t)b * nb + (LOWER ? e : nb - 1 - e)) != 0) ++e;
+        s_end = e;
       }
       __syncthreads();
-      const int c0 = jb * 64, wc = min(64, n - c0);
-      if (row < w)
-        for (int c = grp; c < wc; c += 4)
-          acc = Sc<S>::add(acc, Sc<S>::mul(M[(size_t)(c0 + c) * lda + r0 + row], __ldcg(xb + c0 + c)));
+      const int end = s_end;
+      for (int qq = done; qq < end; ++qq) {
+        const int jb = LOWER ? qq : nb - 1 - qq;
+        const int c0 = jb * 64, wc = min(64, n - c0);
+        if (row < w)
+          for (int c = grp; c < wc; c += 4)
+            acc = Sc<S>::add(acc, Sc<S>::mul(M[(size_t)(c0 + c) * lda + r0 + row], __ldcg(xb + c0 + c)));
+      }
+      done = end;
+      __syncthreads();
     }
     part[grp][row] = acc;
     __syncthreads();

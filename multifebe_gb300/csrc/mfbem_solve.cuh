@@ -249,33 +249,22 @@ static int gemm_sb(cudaStream_t st, int m, int n, int k, const float2* A, int ld
 // A12 := 0 - (-inv(L11)) A12 (k_trtri_neg, k_take_zero, then the Ozaki GEMM)
 // when the panel row is long; the substitution kernel k_trsm_cols otherwise.
 // ---------------------------------------------------------------------------
-// T[b] = -inv(L11) (column-major, ld 32), one warp per matrix, lane j builds
-// column j of the inverse by forward substitution (L11 staged in shared memory)
+// T[b] = -inv(L11) (column-major, ld 32): one warp per (column j, matrix),
+// lane i holding x_i of column j; the forward substitution runs as kb steps
+// of one multiply-add per lane (x_c broadcast by a shuffle), so each lane's
+// dependent chain is kb operations long, and the columns run on separate
+// SMs (binary64 arithmetic is slow on this GPU; long chains of it on one SM
+// were the cost here).
 template <typename S>
 __global__ void __launch_bounds__(32) k_trtri_neg(const S* A, long long sA, int lda, int k, int kb, S* T) {
-  __shared__ S L[32 * 33];
-  const int b = blockIdx.x, j = threadIdx.x;
+  const int j = blockIdx.x, b = blockIdx.y, i = threadIdx.x;
   const S* M = A + sA * b;
-  for (int t = j; t < kb * kb; t += 32) {
-    const int i = t % kb, c = t / kb;
-    L[c * 33 + i] = M[(size_t)(k + c) * lda + k + i];
+  S x = (i == j) ? Sc<S>::one() : Sc<S>::zero();
+  for (int c = j; c < kb - 1; ++c) {
+    const S xc = shfl_s(x, c);
+    if (i > c && i < kb) x = Sc<S>::sub(x, Sc<S>::mul(M[(size_t)(k + c) * lda + k + i], xc));
   }
-  __syncwarp();
-  S x[32];
-#pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    S v = Sc<S>::zero();
-    if (i == j) v = Sc<S>::one();
-    else if (i > j && i < kb) {
-#pragma unroll
-      for (int c = 0; c < i; ++c)
-        if (c >= j) v = Sc<S>::sub(v, Sc<S>::mul(L[c * 33 + i], x[c]));
-    }
-    x[i] = v;
-  }
-  S* Tb = T + 1024 * (size_t)b;
-#pragma unroll
-  for (int i = 0; i < 32; ++i) Tb[j * 32 + i] = Sc<S>::sub(Sc<S>::zero(), x[i]);
+  T[1024 * (size_t)b + j * 32 + i] = Sc<S>::sub(Sc<S>::zero(), x);
 }
 // W[b] (kb x nc, ld kb) = A[k:k+kb, c0:c0+nc]; that block of A set to zero
 template <typename S>
@@ -302,6 +291,12 @@ static int pivot_default() {
   const char* e = getenv("MFBEM_PIVOT");
   if (!e) return -1;
   return std::string(e) == "none" ? 1 : 0;
+}
+
+static int panel_nb_f64() {
+  const char* e = getenv("MFBEM_PANEL_NB");
+  const int v = e ? atoi(e) : 32;
+  return (v == 8 || v == 16) ? v : 32;
 }
 
 template <typename S> struct IsF64 { static const bool v = false; };
@@ -361,8 +356,9 @@ static bool coop_plan(int n, int nb, int batch, CoopPlan* pl) {
 template <typename S>
 static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, int batch,
                          int* ipiv, int* info, int nbo = 128) {
-  // panel width: the L11 block of the TRSM lives in shared memory (<= 16 KB)
-  const int nb = 32;
+  // panel width: the L11 block of the TRSM lives in shared memory (<= 16 KB);
+  // MFBEM_PANEL_NB (8, 16 or 32) overrides for the binary64 factorisations
+  const int nb = IsF64<S>::v ? panel_nb_f64() : 32;
   CK(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
   // pivots start as the identity: a panel that gives up on a bounded wait
   // leaves valid row indices behind for the interchanges that follow
@@ -445,7 +441,7 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
         if (rc) return rc;
         S* T = (S*)g_trsm_ws.p;
         S* W = (S*)((char*)g_trsm_ws.p + tb);
-        k_trtri_neg<S><<<batch, 32, 0, st>>>(A, sA, lda, k, kb, T); ++g_launches;
+        k_trtri_neg<S><<<dim3(32, batch), 32, 0, st>>>(A, sA, lda, k, kb, T); ++g_launches;
         k_take_zero<S><<<(unsigned)std::min<long long>(nblk((long long)batch * nc * kb, 256), 152 * 16), 256, 0, st>>>(
             A, sA, lda, k, kb, c0, nc, batch, W);
         ++g_launches;
@@ -591,7 +587,7 @@ static int tuned_nbo(cudaStream_t st, int n, int batch, int* ipiv, int* info, in
   *out = 128;
   const char* e = getenv("MFBEM_AUTOTUNE");
   if (e && std::string(e) == "0") return 0;
-  const auto key = std::make_tuple((int)sizeof(S), (n + 511) / 512, batch, g_c32_mode);
+  const auto key = std::make_tuple((int)sizeof(S), (n + 511) / 512, batch, g_c32_mode * 2 + (g_nopiv ? 1 : 0));
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
@@ -1331,9 +1327,9 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
   if (precision != 0) {
     g_c32_mode = c32_default();
     if (g_c32_mode == 1 && h->tf32_stalled) g_c32_mode = 0;
-    if ((rc = tuned_nbo<SF>(st, n, batch, ipiv, info, &nbo))) return rc;
     const int pv = pivot_default();
     g_nopiv = pv == 1 || (pv < 0 && !h->nopiv_failed);
+    if ((rc = tuned_nbo<SF>(st, n, batch, ipiv, info, &nbo))) return rc;
   }
   cudaEventRecord(e0, st);
   std::vector<int> hinfo(batch);
