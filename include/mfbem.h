@@ -116,6 +116,23 @@ typedef struct mfbem_stats {
 int mfbem_mesh_upload(const mfbem_mesh_desc* desc, mfbem_handle** out);
 int mfbem_mesh_release(mfbem_handle* h);
 
+/* Region space (region(kr)%space, %halfspace_n, %halfspace_x, %halfspace_bc
+   of src/read_regions.f90:130-200): n = 0 full space (the default), else a
+   half-space whose hyperplane x(|n|) = x has the unit normal sign(n) e_|n|,
+   with bc = 1 (traction-free surface; bc = 0 is MFBEM_EUNSUPPORTED, as the
+   reference stops on it). Both builders then double the free term of
+   collocation points on the hyperplane (build_lse_mechanics_bem_staela.f90:502-513,
+   build_lse_mechanics_bem_harela.f90:688-697); the static builder adds, for
+   n = -3 only (half-space x3 >= x), the complementary kernel of Mindlin's
+   solution to every pair (fbem_bem_staela3d_hsc_sbie_auto,
+   lib/fbem/src/bem_staela3d.f90:9047-9118), so that the free surface needs no
+   elements. The complementary pair lists are built at the next static
+   assembly; a node or collocation point outside the half-space, or an element
+   holding a collocation point of the surface without lying on it, returns
+   MFBEM_EGEOMETRY there (the reference stops). Static internal points of a
+   half-space region are MFBEM_EUNSUPPORTED. */
+int mfbem_set_halfspace(mfbem_handle* h, int32_t n, double x, int32_t bc);
+
 /* build_lse_mechanics_bem_staela: A (n_dof x n_dof, real) and b (n_dof). */
 int mfbem_assemble_staela(mfbem_handle* h, double mu, double nu, double* A, int32_t lda, double* b,
                           int32_t flags);

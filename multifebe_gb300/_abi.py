@@ -37,7 +37,7 @@ ABI_SYMBOLS = [
     "mfbem_qlearn_label", "mfbem_mlp_size", "mfbem_mlp_forward", "mfbem_mlp_loss_grad", "mfbem_mlp_train",
     "mfbem_set_learned_quadrature", "mfbem_sweep_harela_batch", "mfbem_msh_read", "mfbem_msh_error",
     "mfbem_msh_sizes", "mfbem_msh_parts", "mfbem_msh_nodes", "mfbem_msh_elements", "mfbem_msh_free",
-    "mfbem_nso_write", "mfbem_nso_error", "mfbem_fortran_format",
+    "mfbem_nso_write", "mfbem_nso_error", "mfbem_fortran_format", "mfbem_set_halfspace",
 ]
 PREP_SYMBOLS = ["mfbem_prep_create", "mfbem_prep_desc", "mfbem_prep_free", "mfbem_prep_dof"]
 

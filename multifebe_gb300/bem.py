@@ -95,6 +95,14 @@ class BemRegion:
         check(_abi.load().mfbem_last_stats(self._h, ctypes.byref(s)))
         return s.as_dict()
 
+    def set_halfspace(self, n=-3, x=0.0, bc=1):
+        """Region space (src/read_regions.f90:130-200): n = 0 full space, else
+        the half-space with hyperplane normal n (+-1..3), coordinate x and a
+        traction-free surface (bc 1). See mfbem_set_halfspace."""
+        L = _abi.load()
+        L.mfbem_set_halfspace.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_int32]
+        check(L.mfbem_set_halfspace(self._h, int(n), float(x), int(bc)))
+
     # ---------------------------------------------------------------- builders
     def build_lse_staela(self, mu, nu, A=None, b=None):
         n = self.n

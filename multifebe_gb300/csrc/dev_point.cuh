@@ -217,4 +217,87 @@ __device__ __forceinline__ void staela_point(const StaelaP& k, const double rv[3
     }
 }
 
+// Complementary part of Mindlin's fundamental solution for the half-space
+// x3 >= xp with the traction-free surface x3 = xp (fbem_bem_staela3d_hsc_sbie,
+// bem_staela3d.f90:7438-7563), without its constants: fu = 16 pi mu (1 - nu) u,
+// ft = 8 pi (1 - nu) t, [3 * load + component]. Inputs: the horizontal offsets
+// rv1, rv2 of x from x_i, c = x_i3 - xp, z = x3 - xp, and rpz, the vertical
+// offset of x from the image point as the reference forms it (x3 + x_i3). The
+// normal load's cylindrical fields are turned to global axes with
+// cos = rv1 / r, sin = rv2 / r (cos = 1, sin = 0 on the axis r = 0, where
+// the reference's atan2 gives theta = 0).
+__device__ __forceinline__ void hsc_point(double nu, double rv1, double rv2, double c, double z, double rpz,
+                                          const double n[3], double fu[9], double ft[9]) {
+  const double c1 = 1.0 - nu, c2 = 1.0 - 2.0 * nu, c3 = 3.0 - 2.0 * nu, c4 = 3.0 - 4.0 * nu, c5 = 5.0 - 4.0 * nu;
+  const double k12 = 4.0 * c1 * c2;
+  const double a1 = rv1 * rv1, a2 = rv2 * rv2, rh2 = a1 + a2;
+  const double rp = sqrt(rh2 + rpz * rpz);
+  const double rp2 = rp * rp, i1 = 1.0 / rp, i2 = 1.0 / rp2, i3 = i1 * i2, i5 = i3 * i2, i7 = i5 * i2;
+  const double zc = z + c, q = rp + zc, iq = 1.0 / q, b1 = 3.0 * rp + zc;
+  const double K = k12 * i1 * iq * iq;  // 4 c1 c2 / (rp q^2)
+  // tangential loads (l = 0, 1): displacements
+  const double A = c4 * i3 - 6.0 * c * z * i5 - K;
+  const double B = c4 * (z - c) * i3 - 6.0 * c * z * zc * i5 + k12 * i1 * iq;
+  const double rv[2] = {rv1, rv2}, aa[2] = {a1, a2};
+  for (int l = 0; l < 2; ++l) {
+    const double a = rv[l], b = rv[1 - l], al = aa[l], bl = aa[1 - l];
+    fu[3 * l + l] = i1 + c4 * al * i3 + 2.0 * c * z * i3 * (1.0 - 3.0 * al * i2) + k12 * iq * (1.0 - al * i1 * iq);
+    fu[3 * l + 1 - l] = rv1 * rv2 * A;
+    fu[3 * l + 2] = a * B;
+    // stresses of the load along l: along (l), across (m) and vertical (3)
+    const double sll = a * (c2 * c5 * i3 - 3.0 * c4 * al * i5 - K * (3.0 - al * b1 * i2 * iq) +
+                            6.0 * c * i5 * (3.0 * c - c3 * zc + 5.0 * al * z * i2));
+    const double smm = a * (c2 * c4 * i3 - 3.0 * c4 * bl * i5 - K * (1.0 - bl * b1 * i2 * iq) +
+                            6.0 * c * i5 * (c - c2 * zc + 5.0 * bl * z * i2));
+    const double s33 = a * (-c2 * i3 - 3.0 * c4 * zc * zc * i5 + 6.0 * c * i5 * (c + c2 * zc + 5.0 * z * zc * zc * i2));
+    const double sm3 = rv1 * rv2 * (-3.0 * c4 * zc * i5 + 6.0 * c * i5 * (c2 + 5.0 * z * zc * i2));
+    const double sl3 = c2 * (z - c) * i3 - 3.0 * c4 * al * zc * i5 - 6.0 * c * i5 * (z * zc - c2 * al - 5.0 * al * z * zc * i2);
+    const double slm = b * (c2 * i3 - 3.0 * c4 * al * i5 - K * (1.0 - al * b1 * i2 * iq) - 6.0 * c * z * i5 * (1.0 - 5.0 * al * i2));
+    const double nl = n[l], nm = n[1 - l], n3 = n[2];
+    ft[3 * l + l] = sll * nl + slm * nm + sl3 * n3;
+    ft[3 * l + 1 - l] = slm * nl + smm * nm + sm3 * n3;
+    ft[3 * l + 2] = sl3 * nl + sm3 * nm + s33 * n3;
+  }
+  // normal load (l = 2)
+  const double V = c4 * (z - c) * i3 - k12 * i1 * iq + 6.0 * c * z * zc * i5;
+  fu[6] = rv1 * V;
+  fu[7] = rv2 * V;
+  fu[8] = (8.0 * c1 * c1 - c4) * i1 + (c4 * zc * zc - 2.0 * c * z) * i3 + 6.0 * c * z * zc * zc * i5;
+  const double srr = -c2 * (z + 7.0 * c) * i3 + k12 * i1 * iq +
+                     (6.0 * c * c2 * zc * zc - 6.0 * c * c * zc - 3.0 * c4 * rh2 * (z - c)) * i5 - 30.0 * c * rh2 * z * zc * i7;
+  const double stt = c2 * (c4 * zc - 6.0 * c) * i3 - k12 * i1 * iq + 6.0 * c2 * c * zc * zc * i5 - 6.0 * c * c * zc * i5;
+  const double s33 = c2 * (z - c) * i3 - (3.0 * c4 * z * zc * zc - 3.0 * c * zc * (5.0 * z - c)) * i5 - 30.0 * c * z * zc * zc * zc * i7;
+  const double E = c2 * i3 - (3.0 * c4 * z * zc - 3.0 * c * (3.0 * z + c)) * i5 - 30.0 * c * z * zc * zc * i7;
+  double cc = 1.0, ss = 0.0, cs = 0.0;
+  if (rh2 > 0.0) {
+    const double ir2 = 1.0 / rh2;
+    cc = a1 * ir2;
+    ss = a2 * ir2;
+    cs = rv1 * rv2 * ir2;
+  }
+  const double sxx = cc * srr + ss * stt, syy = ss * srr + cc * stt, sxy = cs * (srr - stt);
+  const double sxz = rv1 * E, syz = rv2 * E;
+  ft[6] = sxx * n[0] + sxy * n[1] + sxz * n[2];
+  ft[7] = sxy * n[0] + syy * n[1] + syz * n[2];
+  ft[8] = sxz * n[0] + syz * n[1] + s33 * n[2];
+}
+
+// The complementary displacement kernel on the free surface itself, as the
+// singular integration of fbem_bem_staela3d_hsc_sbie_int integrates it
+// (bem_staela3d.f90:8815-8829), times 16 pi mu (1 - nu): r = |x - x_i|,
+// dr = (x - x_i) / r, z = x3 - xp.
+__device__ __forceinline__ void hsc_surface_g(double nu, double r, const double dr[3], double z, double fu[9]) {
+  const double a = 3.0 - 4.0 * nu, b = 4.0 * (1.0 - nu) * (1.0 - 2.0 * nu), d1r = 1.0 / r;
+  const double is = 1.0 / (r + z);
+  fu[0] = d1r + a * dr[0] * dr[0] * d1r + b * is * (1.0 - dr[0] * dr[0] * r * is);
+  fu[1] = a * dr[0] * dr[1] * d1r - b * dr[0] * dr[1] * r * is * is;
+  fu[2] = a * dr[0] * dr[2] * d1r + b * dr[0] * is;
+  fu[3] = fu[1];
+  fu[4] = d1r + a * dr[1] * dr[1] * d1r + b * is * (1.0 - dr[1] * dr[1] * r * is);
+  fu[5] = a * dr[1] * dr[2] * d1r + b * dr[1] * is;
+  fu[6] = a * dr[0] * dr[2] * d1r - b * dr[0] * is;
+  fu[7] = a * dr[1] * dr[2] * d1r - b * dr[1] * is;
+  fu[8] = (8.0 * (1.0 - nu) * (1.0 - nu) - a) * d1r + a * dr[2] * dr[2] * d1r;
+}
+
 }  // namespace mfb

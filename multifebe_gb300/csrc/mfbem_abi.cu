@@ -94,6 +94,15 @@ struct mfbem_handle {
   int* enode = nullptr;
   double* nodex = nullptr;
   double* nodecl = nullptr;
+  // half-space region (mfbem_set_halfspace): hyperplane normal (0: full
+  // space), coordinate; pair lists of the complementary kernel classified on
+  // the images of the collocation points (built at the first static assembly)
+  int hs_n = 0;
+  double hs_x = 0.0;
+  bool hs_built = false;
+  DMesh mh;
+  double* hs_c = nullptr;  // [ncp] x_i3 - hs_x
+  long long hs_pts[3] = {0, 0, 0};
 };
 
 // ---------------------------------------------------------------------------
@@ -276,6 +285,106 @@ static inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) 
 extern "C" const char* mfbem_last_error(void) { return g_err.c_str(); }
 extern "C" const char* mfbem_version(void) { return "mfbem-gb300 0.1 sm_103a"; }
 
+// Classification of every (collocation point, element) pair of m and the
+// pair lists, adaptive subdivision leaves and singular layouts built from it
+// (m.cpx: the points the pairs are classified on); hoists the adaptive and
+// singular point geometry when it fits. pts: regular / adaptive / singular
+// quadrature points.
+static int build_pairs(mfbem_handle* h, DMesh& m, long long pts[3]) {
+  const int ncp = m.ncp, ne = m.ne;
+  int rc;
+  if ((rc = dalloc(h, (void**)&m.cls, (size_t)ncp * ne))) return rc;
+  k_classify<<<std::min(nblk((long long)ncp * ne, 256), 152u * 16u), 256>>>(m, h->d_qs); ++g_launches;
+  // counts and list offsets
+  int *nreg, *nadp, *nsing;
+  long long* npts;
+  if ((rc = dalloc(h, (void**)&nreg, sizeof(int) * ncp)) || (rc = dalloc(h, (void**)&nadp, sizeof(int) * ncp)) ||
+      (rc = dalloc(h, (void**)&nsing, sizeof(int) * ncp)) || (rc = dalloc(h, (void**)&npts, sizeof(long long) * ncp)) ||
+      (rc = dalloc(h, (void**)&m.reg_start, sizeof(int) * (ncp + 1))) ||
+      (rc = dalloc(h, (void**)&m.adp_start, sizeof(int) * (ncp + 1))) ||
+      (rc = dalloc(h, (void**)&m.sing_start, sizeof(int) * (ncp + 1)))) {
+    return rc;
+  }
+  long long* pts_base;
+  if ((rc = dalloc(h, (void**)&pts_base, sizeof(long long) * (ncp + 1)))) return rc;
+  k_count<<<nblk(ncp, 8), 256>>>(m, nreg, nadp, nsing, npts); ++g_launches;
+  k_scan<int, int><<<1, 1024>>>(nreg, m.reg_start, ncp); ++g_launches;
+  k_scan<int, int><<<1, 1024>>>(nadp, m.adp_start, ncp); ++g_launches;
+  k_scan<int, int><<<1, 1024>>>(nsing, m.sing_start, ncp); ++g_launches;
+  k_scan<long long, long long><<<1, 1024>>>(npts, pts_base, ncp); ++g_launches;
+  CK(cudaGetLastError());
+  int tot[3];
+  long long totp;
+  CK(cudaMemcpy(&tot[0], m.reg_start + ncp, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&tot[1], m.adp_start + ncp, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&tot[2], m.sing_start + ncp, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&totp, pts_base + ncp, sizeof(long long), cudaMemcpyDeviceToHost));
+  m.nreg = tot[0];
+  m.nadp = tot[1];
+  m.nsing = tot[2];
+  int *adp_cp, *sing_cp;
+  if ((rc = dalloc(h, (void**)&m.reg_pair, sizeof(int) * (m.nreg + 1))) ||
+      (rc = dalloc(h, (void**)&m.reg_pt, sizeof(long long) * (m.nreg + 1))) ||
+      (rc = dalloc(h, (void**)&m.adp_e, sizeof(int) * (m.nadp + 1))) ||
+      (rc = dalloc(h, (void**)&adp_cp, sizeof(int) * (m.nadp + 1))) ||
+      (rc = dalloc(h, (void**)&m.sing_e, sizeof(int) * (m.nsing + 1))) ||
+      (rc = dalloc(h, (void**)&sing_cp, sizeof(int) * (m.nsing + 1)))) {
+    return rc;
+  }
+  k_fill<<<nblk(ncp, 8), 256>>>(m, pts_base, adp_cp, sing_cp); ++g_launches;
+  CK(cudaMemcpy(m.reg_pt + m.nreg, &totp, sizeof(long long), cudaMemcpyHostToDevice));
+  pts[0] = totp;
+  // adaptive subdivision leaves
+  int* nl;
+  if ((rc = dalloc(h, (void**)&nl, sizeof(int) * (m.nadp + 1))) ||
+      (rc = dalloc(h, (void**)&m.adp_leaf, sizeof(int) * (m.nadp + 1)))) {
+    return rc;
+  }
+  if (m.nadp > 0) k_adp_count<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, adp_cp, nl); ++g_launches;
+  k_scan<int, int><<<1, 1024>>>(nl, m.adp_leaf, (int)m.nadp); ++g_launches;
+  int nleaf = 0;
+  CK(cudaMemcpy(&nleaf, m.adp_leaf + m.nadp, sizeof(int), cudaMemcpyDeviceToHost));
+  m.nleaf = nleaf;
+  long long* lpts;
+  if ((rc = dalloc(h, (void**)&m.leaf, sizeof(double) * LEAF_D * (m.nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&m.leaf_gln, sizeof(int) * (m.nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&m.leaf_pair, sizeof(int) * (m.nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&m.leaf_pt, sizeof(long long) * (m.nleaf + 1))) ||
+      (rc = dalloc(h, (void**)&lpts, sizeof(long long) * (m.nleaf + 1)))) {
+    return rc;
+  }
+  if (m.nadp > 0) k_adp_fill<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, adp_cp); ++g_launches;
+  if (m.nleaf > 0) k_leaf_points<<<nblk(m.nleaf, 256), 256>>>(m, lpts); ++g_launches;
+  k_scan<long long, long long><<<1, 1024>>>(lpts, m.leaf_pt, (int)m.nleaf); ++g_launches;
+  CK(cudaMemcpy(&pts[1], m.leaf_pt + m.nleaf, sizeof(long long), cudaMemcpyDeviceToHost));
+  // singular pairs
+  long long* spts;
+  if ((rc = dalloc(h, (void**)&m.sing_d, sizeof(double) * SING_D * (m.nsing + 1))) ||
+      (rc = dalloc(h, (void**)&m.sing_i, sizeof(int) * SING_I * (m.nsing + 1))) ||
+      (rc = dalloc(h, (void**)&m.sing_pt, sizeof(long long) * (m.nsing + 1))) ||
+      (rc = dalloc(h, (void**)&spts, sizeof(long long) * (m.nsing + 1)))) {
+    return rc;
+  }
+  if (m.nsing > 0) k_sing_prep<<<nblk(m.nsing, 64), 64>>>(m, h->d_q15, sing_cp, spts); ++g_launches;
+  k_scan<long long, long long><<<1, 1024>>>(spts, m.sing_pt, (int)m.nsing); ++g_launches;
+  CK(cudaMemcpy(&pts[2], m.sing_pt + m.nsing, sizeof(long long), cudaMemcpyDeviceToHost));
+  // hoist the singular / adaptive point geometry out of the frequency loop when
+  // it fits a modest share of the device (22 / 14 doubles per point)
+  m.adp_cp = adp_cp;
+  m.nsing_pts = pts[2];
+  m.nleaf_pts = pts[1];
+  const size_t geo_budget = (size_t)8 << 30;
+  if (m.nsing_pts > 0 && (size_t)m.nsing_pts * 22 * sizeof(double) <= geo_budget) {
+    if ((rc = dalloc(h, (void**)&m.sing_geo, (size_t)m.nsing_pts * 22 * sizeof(double)))) return rc;
+    k_sing_geo<<<nblk(m.nsing_pts, 128), 128>>>(m); ++g_launches;
+  }
+  if (m.nleaf_pts > 0 && (size_t)m.nleaf_pts * 14 * sizeof(double) <= geo_budget) {
+    if ((rc = dalloc(h, (void**)&m.leaf_geo, (size_t)m.nleaf_pts * 14 * sizeof(double)))) return rc;
+    k_leaf_geo<<<nblk(m.nleaf_pts, 128), 128>>>(m); ++g_launches;
+  }
+  return 0;
+}
+
 // ---------------------------------------------------------------------------
 // upload + once-per-mesh precompute
 // ---------------------------------------------------------------------------
@@ -301,6 +410,7 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   h->nn = nn;
   DMesh& m = h->m;
   std::memset(&m, 0, sizeof(m));
+  m.hs_ax = -1;
   m.ne = ne;
   m.ndn = nn;
   m.ndof = ndof;
@@ -448,7 +558,6 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
       (rc = dalloc(h, (void**)&m.px, 3 * sizeof(double) * (size_t)ne * m.ptot)) ||
       (rc = dalloc(h, (void**)&m.pn, 3 * sizeof(double) * (size_t)ne * m.ptot)) ||
       (rc = dalloc(h, (void**)&m.pphi, 8 * sizeof(double) * (size_t)ne * m.ptot)) ||
-      (rc = dalloc(h, (void**)&m.cls, (size_t)ncp * ne)) ||
       (rc = dalloc(h, (void**)&m.ft, sizeof(double) * FT_D * (size_t)ncp)) ||
       (rc = dalloc(h, (void**)&m.ft_ok, sizeof(int) * (size_t)ncp)) ||
       (rc = dalloc(h, (void**)&h->d_err, sizeof(int)))) {
@@ -457,100 +566,12 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   }
   auto t0 = std::chrono::steady_clock::now();
   k_datasets<<<ne, 128>>>(m); ++g_launches;
-  k_classify<<<std::min(nblk((long long)ncp * ne, 256), 152u * 16u), 256>>>(m, h->d_qs); ++g_launches;
-  // counts and list offsets
-  int *nreg, *nadp, *nsing;
-  long long* npts;
-  if ((rc = dalloc(h, (void**)&nreg, sizeof(int) * ncp)) || (rc = dalloc(h, (void**)&nadp, sizeof(int) * ncp)) ||
-      (rc = dalloc(h, (void**)&nsing, sizeof(int) * ncp)) || (rc = dalloc(h, (void**)&npts, sizeof(long long) * ncp)) ||
-      (rc = dalloc(h, (void**)&m.reg_start, sizeof(int) * (ncp + 1))) ||
-      (rc = dalloc(h, (void**)&m.adp_start, sizeof(int) * (ncp + 1))) ||
-      (rc = dalloc(h, (void**)&m.sing_start, sizeof(int) * (ncp + 1)))) {
-    mfbem_mesh_release(h);
-    return rc;
-  }
-  long long* pts_base;
-  if ((rc = dalloc(h, (void**)&pts_base, sizeof(long long) * (ncp + 1)))) { mfbem_mesh_release(h); return rc; }
-  k_count<<<nblk(ncp, 8), 256>>>(m, nreg, nadp, nsing, npts); ++g_launches;
-  k_scan<int, int><<<1, 1024>>>(nreg, m.reg_start, ncp); ++g_launches;
-  k_scan<int, int><<<1, 1024>>>(nadp, m.adp_start, ncp); ++g_launches;
-  k_scan<int, int><<<1, 1024>>>(nsing, m.sing_start, ncp); ++g_launches;
-  k_scan<long long, long long><<<1, 1024>>>(npts, pts_base, ncp); ++g_launches;
-  CK(cudaGetLastError());
-  int tot[3];
-  long long totp;
-  CK(cudaMemcpy(&tot[0], m.reg_start + ncp, sizeof(int), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(&tot[1], m.adp_start + ncp, sizeof(int), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(&tot[2], m.sing_start + ncp, sizeof(int), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(&totp, pts_base + ncp, sizeof(long long), cudaMemcpyDeviceToHost));
-  m.nreg = tot[0];
-  m.nadp = tot[1];
-  m.nsing = tot[2];
-  int *adp_cp, *sing_cp;
-  if ((rc = dalloc(h, (void**)&m.reg_pair, sizeof(int) * (m.nreg + 1))) ||
-      (rc = dalloc(h, (void**)&m.reg_pt, sizeof(long long) * (m.nreg + 1))) ||
-      (rc = dalloc(h, (void**)&m.adp_e, sizeof(int) * (m.nadp + 1))) ||
-      (rc = dalloc(h, (void**)&adp_cp, sizeof(int) * (m.nadp + 1))) ||
-      (rc = dalloc(h, (void**)&m.sing_e, sizeof(int) * (m.nsing + 1))) ||
-      (rc = dalloc(h, (void**)&sing_cp, sizeof(int) * (m.nsing + 1)))) {
-    mfbem_mesh_release(h);
-    return rc;
-  }
-  k_fill<<<nblk(ncp, 8), 256>>>(m, pts_base, adp_cp, sing_cp); ++g_launches;
-  CK(cudaMemcpy(m.reg_pt + m.nreg, &totp, sizeof(long long), cudaMemcpyHostToDevice));
-  h->pts_reg = totp;
-  // adaptive subdivision leaves
-  int* nl;
-  if ((rc = dalloc(h, (void**)&nl, sizeof(int) * (m.nadp + 1))) ||
-      (rc = dalloc(h, (void**)&m.adp_leaf, sizeof(int) * (m.nadp + 1)))) {
-    mfbem_mesh_release(h);
-    return rc;
-  }
-  if (m.nadp > 0) k_adp_count<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, adp_cp, nl); ++g_launches;
-  k_scan<int, int><<<1, 1024>>>(nl, m.adp_leaf, (int)m.nadp); ++g_launches;
-  int nleaf = 0;
-  CK(cudaMemcpy(&nleaf, m.adp_leaf + m.nadp, sizeof(int), cudaMemcpyDeviceToHost));
-  m.nleaf = nleaf;
-  long long* lpts;
-  if ((rc = dalloc(h, (void**)&m.leaf, sizeof(double) * LEAF_D * (m.nleaf + 1))) ||
-      (rc = dalloc(h, (void**)&m.leaf_gln, sizeof(int) * (m.nleaf + 1))) ||
-      (rc = dalloc(h, (void**)&m.leaf_pair, sizeof(int) * (m.nleaf + 1))) ||
-      (rc = dalloc(h, (void**)&m.leaf_pt, sizeof(long long) * (m.nleaf + 1))) ||
-      (rc = dalloc(h, (void**)&lpts, sizeof(long long) * (m.nleaf + 1)))) {
-    mfbem_mesh_release(h);
-    return rc;
-  }
-  if (m.nadp > 0) k_adp_fill<<<nblk(m.nadp, 64), 64>>>(m, h->d_qs, adp_cp); ++g_launches;
-  if (m.nleaf > 0) k_leaf_points<<<nblk(m.nleaf, 256), 256>>>(m, lpts); ++g_launches;
-  k_scan<long long, long long><<<1, 1024>>>(lpts, m.leaf_pt, (int)m.nleaf); ++g_launches;
-  CK(cudaMemcpy(&h->pts_adp, m.leaf_pt + m.nleaf, sizeof(long long), cudaMemcpyDeviceToHost));
-  // singular pairs
-  long long* spts;
-  if ((rc = dalloc(h, (void**)&m.sing_d, sizeof(double) * SING_D * (m.nsing + 1))) ||
-      (rc = dalloc(h, (void**)&m.sing_i, sizeof(int) * SING_I * (m.nsing + 1))) ||
-      (rc = dalloc(h, (void**)&m.sing_pt, sizeof(long long) * (m.nsing + 1))) ||
-      (rc = dalloc(h, (void**)&spts, sizeof(long long) * (m.nsing + 1)))) {
-    mfbem_mesh_release(h);
-    return rc;
-  }
-  if (m.nsing > 0) k_sing_prep<<<nblk(m.nsing, 64), 64>>>(m, h->d_q15, sing_cp, spts); ++g_launches;
-  k_scan<long long, long long><<<1, 1024>>>(spts, m.sing_pt, (int)m.nsing); ++g_launches;
-  CK(cudaMemcpy(&h->pts_sing, m.sing_pt + m.nsing, sizeof(long long), cudaMemcpyDeviceToHost));
+  long long pts[3] = {0, 0, 0};
+  if ((rc = build_pairs(h, m, pts))) { mfbem_mesh_release(h); return rc; }
+  h->pts_reg = pts[0];
+  h->pts_adp = pts[1];
+  h->pts_sing = pts[2];
   k_ft_prep<<<nblk(ncp, 128), 128>>>(m); ++g_launches;
-  // hoist the singular / adaptive point geometry out of the frequency loop when
-  // it fits a modest share of the device (22 / 14 doubles per point)
-  m.adp_cp = adp_cp;
-  m.nsing_pts = h->pts_sing;
-  m.nleaf_pts = h->pts_adp;
-  const size_t geo_budget = (size_t)8 << 30;
-  if (m.nsing_pts > 0 && (size_t)m.nsing_pts * 22 * sizeof(double) <= geo_budget) {
-    if ((rc = dalloc(h, (void**)&m.sing_geo, (size_t)m.nsing_pts * 22 * sizeof(double)))) { mfbem_mesh_release(h); return rc; }
-    k_sing_geo<<<nblk(m.nsing_pts, 128), 128>>>(m); ++g_launches;
-  }
-  if (m.nleaf_pts > 0 && (size_t)m.nleaf_pts * 14 * sizeof(double) <= geo_budget) {
-    if ((rc = dalloc(h, (void**)&m.leaf_geo, (size_t)m.nleaf_pts * 14 * sizeof(double)))) { mfbem_mesh_release(h); return rc; }
-    k_leaf_geo<<<nblk(m.nleaf_pts, 128), 128>>>(m); ++g_launches;
-  }
   CK(cudaGetLastError());
   CK(cudaDeviceSynchronize());
   auto t1 = std::chrono::steady_clock::now();
@@ -593,6 +614,37 @@ extern "C" int mfbem_mesh_release(mfbem_handle* h) {
   return 0;
 }
 
+extern "C" int mfbem_set_halfspace(mfbem_handle* h, int32_t n, double x, int32_t bc) {
+  g_err.clear();
+  if (!h) return fail(MFBEM_EARG, "null argument");
+  if (n < -3 || n > 3) return fail(MFBEM_EARG, "half-space hyperplane normal must be in -3..3 (0: full space)");
+  if (n != 0 && bc != 1)
+    return fail(MFBEM_EUNSUPPORTED, "only the traction-free half-space surface (bc = 1) is available");
+  if (!std::isfinite(x)) return fail(MFBEM_EARG, "half-space hyperplane coordinate must be finite");
+  if (n != h->hs_n || x != h->hs_x) h->hs_built = false;
+  h->hs_n = n;
+  h->hs_x = x;
+  h->m.hs_ax = n == 0 ? -1 : std::abs(n) - 1;
+  h->m.hs_x = x;
+  return 0;
+}
+
+// Test hook: pair counts of the half-space complementary kernel (regular,
+// adaptive, singular pairs, adaptive leaves; regular, adaptive, singular
+// points), after the first static assembly of a half-space region.
+extern "C" int mfbem_internal_hs_counts(mfbem_handle* h, long long* out) {
+  if (!h || !out) return fail(MFBEM_EARG, "null argument");
+  if (!h->hs_built) return fail(MFBEM_EARG, "no half-space pair lists built");
+  out[0] = h->mh.nreg;
+  out[1] = h->mh.nadp;
+  out[2] = h->mh.nsing;
+  out[3] = h->mh.nleaf;
+  out[4] = h->hs_pts[0];
+  out[5] = h->hs_pts[1];
+  out[6] = h->hs_pts[2];
+  return 0;
+}
+
 extern "C" int mfbem_last_stats(mfbem_handle* h, mfbem_stats* s) {
   if (!h || !s) return fail(MFBEM_EARG, "null argument");
   *s = h->stats;
@@ -610,6 +662,40 @@ __global__ void k_harpar(const double* in /*nf x {lre,lim,mre,mim,rho,omega}*/, 
   HarParD p = harela_params(mk(q[0], q[1]), mk(q[2], q[3]), q[4], q[5]);
   p.steps = steps;
   out[f] = p;
+}
+
+// Pair lists of the half-space complementary kernel (static builder, plane
+// x3 = hs_x): the collocation points' images classified against every element
+// like the full-space pairs, once per mesh and hyperplane.
+static int hs_prepare_static(mfbem_handle* h) {
+  if (h->hs_n == 0 || h->hs_built) return 0;
+  if (h->hs_n != -3)
+    return fail(MFBEM_EUNSUPPORTED, "the static half-space kernel needs the hyperplane normal n = -3");
+  const DMesh& m = h->m;
+  DMesh& mh = h->mh;
+  mh = m;
+  mh.cls = nullptr;
+  mh.sing_geo = nullptr;
+  mh.leaf_geo = nullptr;
+  int rc;
+  double* img;
+  if ((rc = dalloc(h, (void**)&img, 3 * sizeof(double) * (size_t)m.ncp)) ||
+      (rc = dalloc(h, (void**)&h->hs_c, sizeof(double) * (size_t)m.ncp)))
+    return rc;
+  CK(cudaDeviceSynchronize());
+  k_hs_image<<<nblk(m.ncp, 128), 128>>>(m.cpx, m.ncp, h->hs_x, img, h->hs_c); ++g_launches;
+  mh.cpx = img;
+  if ((rc = build_pairs(h, mh, h->hs_pts))) return rc;
+  CK(cudaMemset(h->d_err, 0, sizeof(int)));
+  k_hs_check<<<nblk(8LL * m.ne + m.ncp + mh.nsing, 256), 256>>>(mh, h->hs_c, h->hs_x, h->d_err); ++g_launches;
+  int e = 0;
+  CK(cudaMemcpy(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaDeviceSynchronize());
+  if (e & 1) return fail(MFBEM_EGEOMETRY, "a node or collocation point lies outside the half-space");
+  if (e & 2)
+    return fail(MFBEM_EGEOMETRY, "an element holding a collocation point of the free surface does not lie on it");
+  h->hs_built = true;
+  return 0;
 }
 
 // Assembly kernels in a fixed order (regular, adaptive, singular, free terms);
@@ -644,6 +730,22 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
   constexpr int WPB = 4;
   long long nw = (long long)m.ndn * nf;
   unsigned g = nblk(nw, WPB);
+  // static half-space region: the complementary kernel's pairs follow each
+  // full-space stage and add into the same rows
+  constexpr bool kStatic = std::is_same<POL, PolStatic>::value;
+  const bool hs = kStatic && h->hs_built && h->hs_n == -3;
+  const DMesh& mh = h->mh;
+  PolHsc ph{};
+  PolHscSing phs{};
+  if constexpr (kStatic) {
+    ph.k = pol.k;
+    ph.c = h->hs_c;
+    ph.xp = h->hs_x;
+    ph.nu = pol.nu;
+    phs.k = pol.k;
+    phs.c = h->hs_c;
+    phs.nu = pol.nu;
+  }
   CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
   if (tm) cudaEventRecord(tm->ev[0], h->st);
   if (m.nreg > 0) {
@@ -659,12 +761,24 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
     }
     ++g_launches;
   }
+  if constexpr (kStatic) {
+    if (hs && mh.nreg > 0) {
+      k_reg<PolHsc, WPB><<<g, WPB * 32, 0, h->st>>>(mh, ph, nf, A, lda, astride, b, bstride);
+      ++g_launches;
+    }
+  }
   if (tm) cudaEventRecord(tm->ev[1], h->st);
   if (m.nadp > 0) {
     if (mixed && lgf)
       k_mixed<MIX_ADP, WPB><<<g, WPB * 32, 0, h->st>>>(m, pf, dsf, lgf, nf, (double2*)A, lda, astride / 2, b, bstride);
     else k_adp<POL, WPB><<<g, WPB * 32, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
     ++g_launches;
+  }
+  if constexpr (kStatic) {
+    if (hs && mh.nadp > 0) {
+      k_adp<PolHsc, WPB><<<g, WPB * 32, 0, h->st>>>(mh, ph, nf, A, lda, astride, b, bstride);
+      ++g_launches;
+    }
   }
   if (tm) cudaEventRecord(tm->ev[2], h->st);
   // the singular kernels keep two combo sets per point: 2 warps per block
@@ -673,6 +787,12 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
       k_mixed<MIX_SING, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pf, dsf, sgf, nf, (double2*)A, lda, astride / 2, b, bstride);
     else k_sing<POL, 2><<<nblk(nw, 2), 64, 0, h->st>>>(m, pol, nf, A, lda, astride, b, bstride);
     ++g_launches;
+  }
+  if constexpr (kStatic) {
+    if (hs && mh.nsing > 0) {
+      k_sing<PolHscSing, 2><<<nblk(nw, 2), 64, 0, h->st>>>(mh, phs, nf, A, lda, astride, b, bstride);
+      ++g_launches;
+    }
   }
   if (tm) cudaEventRecord(tm->ev[3], h->st);
   k_free<POL><<<nblk(nw, 128), 128, 0, h->st>>>(m, pol, d_nu, nf, A, lda, astride, b, bstride, h->d_err); ++g_launches;
@@ -760,8 +880,11 @@ extern "C" int mfbem_assemble_staela(mfbem_handle* h, double mu, double nu, doub
                                      int32_t flags) {
   g_err.clear();
   if (!h || !A || !b) return fail(MFBEM_EARG, "null argument");
+  if (int rd = check_dev(h)) return rd;
+  if (int rc = hs_prepare_static(h)) return rc;
   PolStatic pol;
   pol.k = staela_params(mu, nu);
+  pol.nu = nu;
   double nuv[2] = {nu, 0.0};
   return assemble_common<false>(h, &pol, nuv, A, lda, b, flags);
 }
@@ -870,6 +993,8 @@ extern "C" int mfbem_internal_points_staela(mfbem_handle* h, double mu, double n
   if (!h || n_ip < 0 || (n_ip > 0 && (!x_ip || !u_nodes || !t_nodes || !u_ip || !sigma_ip)))
     return fail(MFBEM_EARG, "invalid argument");
   if (int rd = check_dev(h)) return rd;
+  if (h->hs_n != 0)
+    return fail(MFBEM_EUNSUPPORTED, "internal points of a static half-space region are not available");
   if (n_ip == 0) return 0;
   IpStatic pol;
   pol.k = staela_params(mu, nu);

@@ -44,15 +44,17 @@ __device__ __forceinline__ void addA(double* A, size_t idx, cd v) {
 // Kernel family policies -----------------------------------------------------
 struct PolStatic {
   typedef double T;
+  static constexpr int NG = 6;  // independent components of g per node (u* symmetric)
   StaelaP k;
+  double nu = 0.0;
   __device__ T cte_t(int) const { return k.ctet1; }
   __device__ T cte_u(int) const { return k.cteu1; }
   __device__ T cpv(int) const { return k.ctet2; }  // coefficient of the CPV/line-integral part
-  __device__ void point(int, const double rv[3], const double n[3], T fu[9], T ft[9]) const {
+  __device__ void point(int, int, const double rv[3], const double n[3], T fu[9], T ft[9]) const {
     staela_point(k, rv, n, fu, ft);
   }
   // singular (interior) integration: regular parts and the CPV integrand
-  __device__ void point_sing(int, const double rv[3], const double n[3], T fu[9], T ft[9], T fc[9]) const {
+  __device__ void point_sing(int, int, const double rv[3], const double n[3], T fu[9], T ft[9], T fc[9]) const {
     double r = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
     double d1r = 1.0 / r, d1r2 = d1r * d1r;
     double dr[3] = {rv[0] * d1r, rv[1] * d1r, rv[2] * d1r};
@@ -68,14 +70,15 @@ struct PolStatic {
 };
 struct PolHarmonic {
   typedef cd T;
+  static constexpr int NG = 6;
   const HarParD* p;  // one parameter block per frequency
   __device__ T cte_t(int f) const { return p[f].cte_t; }
   __device__ T cte_u(int f) const { return p[f].cte_u; }
   __device__ T cpv(int f) const { return p[f].T2[0]; }
-  __device__ void point(int f, const double rv[3], const double n[3], T fu[9], T ft[9]) const {
+  __device__ void point(int f, int, const double rv[3], const double n[3], T fu[9], T ft[9]) const {
     harela_point(p[f], rv, n, fu, ft);
   }
-  __device__ void point_sing(int f, const double rv[3], const double n[3], T fu[9], T ft[9], T fc[9]) const {
+  __device__ void point_sing(int f, int, const double rv[3], const double n[3], T fu[9], T ft[9], T fc[9]) const {
     const HarParD& q = p[f];
     double r = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
     cd psi, chi, TT1, TT2, TT3;
@@ -101,27 +104,80 @@ struct PolHarmonic {
   }
 };
 
+// Half-space complementary kernel (static, traction-free surface x3 = xp):
+// the pair lists of these policies are classified on the images of the
+// collocation points, so rv = x - image; c[cp] = x_i3 - xp of the original
+// point. u* of this kernel is not symmetric: all nine g components are kept.
+struct PolHsc {
+  typedef double T;
+  static constexpr int NG = 9;
+  StaelaP k;
+  const double* c;  // [ncp]
+  double xp, nu;
+  __device__ T cte_t(int) const { return -k.ctet1; }  // 1 / (8 pi (1 - nu))
+  __device__ T cte_u(int) const { return k.cteu1; }   // 1 / (16 pi mu (1 - nu))
+  __device__ T cpv(int) const { return 0.0; }
+  __device__ void point(int, int cp, const double rv[3], const double n[3], T fu[9], T ft[9]) const {
+    const double ci = c[cp];
+    // z = x3 - xp; the image's vertical offset as x3 + x_i3 (reflection in x3 = 0)
+    hsc_point(nu, rv[0], rv[1], ci, rv[2] - ci, rv[2] + 2.0 * xp, n, fu, ft);
+  }
+};
+// Singular pairs of the complementary kernel (collocation point and element on
+// the free surface): h is minus the full-space singular h (CPV and line
+// integrals included), g the surface restriction of the complementary
+// displacement kernel on the same polar rule. rv = x - x_i here.
+struct PolHscSing {
+  typedef double T;
+  static constexpr int NG = 9;
+  StaelaP k;
+  const double* c;
+  double nu;
+  __device__ T cte_t(int) const { return k.ctet1; }
+  __device__ T cte_u(int) const { return k.cteu1; }
+  __device__ T cpv(int) const { return -k.ctet2; }
+  __device__ void point_sing(int, int cp, const double rv[3], const double n[3], T fu[9], T ft[9], T fc[9]) const {
+    double r = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    double d1r = 1.0 / r, d1r2 = d1r * d1r;
+    double dr[3] = {rv[0] * d1r, rv[1] * d1r, rv[2] * d1r};
+    double drdn = dr[0] * n[0] + dr[1] * n[1] + dr[2] * n[2];
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        double dk = (il == ik) ? 1.0 : 0.0;
+        ft[3 * il + ik] = -(d1r2 * drdn * (k.ctet2 * dk + 3.0 * dr[il] * dr[ik]));
+        fc[3 * il + ik] = -(d1r2 * k.ctet2 * (n[il] * dr[ik] - n[ik] * dr[il]));
+      }
+    hsc_surface_g(nu, r, dr, rv[2] + c[cp], fu);
+  }
+};
+
 // Outputs of one pair handled by the lanes of a warp: o = lane + 32 j, j < 4.
 // o < 72: h(kn, il, ik), kn = o / 9; o >= 72: g(kn, s) with s one of the six
 // (il <= ik) components (u* is symmetric, so g(kn, il, ik) = g(kn, ik, il)).
 constexpr int kOut = 120;
 constexpr int kAcc = 4;
+// outputs and accumulators per lane for NG g components per node
+template <int NG> struct GOut {
+  static constexpr int out = 72 + 8 * NG;
+  static constexpr int acc = (out + 31) / 32;
+};
 __device__ __forceinline__ int sym_il(int s) { return s < 3 ? 0 : (s < 5 ? 1 : 2); }
 __device__ __forceinline__ int sym_ik(int s) { return s < 3 ? s : (s < 5 ? s - 2 : 2); }
 
 // Shared flush: scale, reverse, scatter one pair's outputs of this lane set.
 template <class POL>
 __device__ __forceinline__ void flush_pair(const DMesh& m, const POL& pol, int f, int dn, int e,
-                                           typename POL::T acc[kAcc], double* A, size_t lda, size_t astride,
+                                           typename POL::T* acc, double* A, size_t lda, size_t astride,
                                            double* b, size_t bstride, const double* hli_phi /* or null */) {
   typedef typename POL::T T;
+  constexpr int NG = POL::NG;
   const int lane = threadIdx.x & 31;
   T bc[3] = {VT<T>::zero(), VT<T>::zero(), VT<T>::zero()};
   const bool rev = m.rev[e] != 0;
   double* Af = A + astride * f;
-  for (int j = 0; j < kAcc; ++j) {
+  for (int j = 0; j < GOut<NG>::acc; ++j) {
     int o = lane + 32 * j;
-    if (o >= kOut) break;
+    if (o >= GOut<NG>::out) break;
     T v = acc[j];
     if (o < 72) {
       int kn = o / 9, il = (o % 9) / 3, ik = o % 3;
@@ -133,9 +189,10 @@ __device__ __forceinline__ void flush_pair(const DMesh& m, const POL& pol, int f
       if (m.dct[dof] == 1) addA(Af, (size_t)dof * lda + row, v);
       else bc[il] = bc[il] - v * cval(m.dcv, dof, v);
     } else {
-      int q = o - 72, kn = q / 6, sidx = q % 6, il = sym_il(sidx), ik = sym_ik(sidx);
+      int q = o - 72, kn = q / NG, sidx = q % NG;
+      int il = NG == 6 ? sym_il(sidx) : sidx / 3, ik = NG == 6 ? sym_ik(sidx) : sidx % 3;
       v = v * pol.cte_u(f);
-      for (int t = 0; t < (il == ik ? 1 : 2); ++t) {
+      for (int t = 0; t < (il == ik || NG == 9 ? 1 : 2); ++t) {
         int r_ = t ? ik : il, c_ = t ? il : ik;
         int dof = m.edof[8 * e + kn] + c_;
         size_t row = 3 * (size_t)dn + r_;
@@ -153,22 +210,26 @@ __device__ __forceinline__ void flush_pair(const DMesh& m, const POL& pol, int f
   __syncwarp();
 }
 
-template <typename T>
+template <typename T, int NG = 6>
 struct alignas(16) Combo {
-  T fu[6], ft[9];
+  T fu[NG], ft[9];
   double w[8];
   int pair;
 };
-template <typename T>
+template <typename T, int NG = 6>
 struct alignas(16) ComboS {
-  T fu[6], ft[9], fc[9];
+  T fu[NG], ft[9], fc[9];
   double w[8], wd[8];
   int pair;
 };
-// keep the six independent components of the symmetric u*
-template <typename T>
-__device__ __forceinline__ void store_u6(T* dst, const T fu[9]) {
-  dst[0] = fu[0]; dst[1] = fu[1]; dst[2] = fu[2]; dst[3] = fu[4]; dst[4] = fu[5]; dst[5] = fu[8];
+// keep the NG independent components of u* (six of a symmetric one)
+template <int NG, typename T>
+__device__ __forceinline__ void store_u(T* dst, const T fu[9]) {
+  if (NG == 6) {
+    dst[0] = fu[0]; dst[1] = fu[1]; dst[2] = fu[2]; dst[3] = fu[4]; dst[4] = fu[5]; dst[5] = fu[8];
+  } else {
+    for (int q = 0; q < 9; ++q) dst[q] = fu[q];
+  }
 }
 
 __device__ __forceinline__ int find_le(const long long* a, int lo, int hi, long long v) {
@@ -181,21 +242,21 @@ __device__ __forceinline__ int find_le(const long long* a, int lo, int hi, long 
   return lo;
 }
 
-template <typename T>
-__device__ __forceinline__ void accumulate(T acc[kAcc], const T* fu6, const T* ft, const double* w) {
+template <int NG, typename T>
+__device__ __forceinline__ void accumulate(T* acc, const T* fug, const T* ft, const double* w) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int j = 0; j < kAcc; ++j) {
+  for (int j = 0; j < GOut<NG>::acc; ++j) {
     int o = lane + 32 * j;
-    if (o < kOut) {
+    if (o < GOut<NG>::out) {
       T v;
       int kn;
       if (o < 72) {
         kn = o / 9;
         v = ft[o % 9];
       } else {
-        kn = (o - 72) / 6;
-        v = fu6[(o - 72) % 6];
+        kn = (o - 72) / NG;
+        v = fug[(o - 72) % NG];
       }
       acc[j] = acc[j] + v * w[kn];
     }
@@ -207,20 +268,21 @@ template <class POL, int WPB>
 __global__ void __launch_bounds__(WPB * 32) k_reg(DMesh m, POL pol, int nf, double* A, size_t lda, size_t astride,
                                                   double* b, size_t bstride) {
   typedef typename POL::T T;
-  __shared__ Combo<T> sm[WPB][32];
+  constexpr int NG = POL::NG, NA = GOut<NG>::acc;
+  __shared__ Combo<T, NG> sm[WPB][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x / 32;
   const long long gw = blockIdx.x * (long long)WPB + w;
   if (gw >= (long long)m.ndn * nf) return;
   const int dn = (int)(gw % m.ndn), f = (int)(gw / m.ndn);
-  Combo<T>* S = sm[w];
+  Combo<T, NG>* S = sm[w];
   for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
     const int s0 = m.reg_start[cp], s1 = m.reg_start[cp + 1];
     if (s0 == s1) continue;
     const double* xi = m.cpx + 3 * (size_t)cp;
     const long long P0 = m.reg_pt[s0], Q = m.reg_pt[s1] - P0;
     int cur = -1;
-    T acc[kAcc];
-    for (int j = 0; j < kAcc; ++j) acc[j] = VT<T>::zero();
+    T acc[NA];
+    for (int j = 0; j < NA; ++j) acc[j] = VT<T>::zero();
     for (long long base = 0; base < Q; base += 32) {
       long long c = base + lane;
       if (c < Q) {
@@ -231,8 +293,8 @@ __global__ void __launch_bounds__(WPB * 32) k_reg(DMesh m, POL pol, int nf, doub
         double rv[3] = {m.px[3 * pt] - xi[0], m.px[3 * pt + 1] - xi[1], m.px[3 * pt + 2] - xi[2]};
         double n[3] = {m.pn[3 * pt], m.pn[3 * pt + 1], m.pn[3 * pt + 2]};
         T fu9[9];
-        pol.point(f, rv, n, fu9, S[lane].ft);
-        store_u6(S[lane].fu, fu9);
+        pol.point(f, cp, rv, n, fu9, S[lane].ft);
+        store_u<NG>(S[lane].fu, fu9);
         for (int k = 0; k < 8; ++k) S[lane].w[k] = m.pphi[8 * pt + k];
         S[lane].pair = jp;
       }
@@ -243,9 +305,9 @@ __global__ void __launch_bounds__(WPB * 32) k_reg(DMesh m, POL pol, int nf, doub
         if (jp != cur) {
           if (cur >= 0) flush_pair(m, pol, f, dn, m.reg_pair[cur] & 0xFFFFFF, acc, A, lda, astride, b, bstride, nullptr);
           cur = jp;
-          for (int j = 0; j < kAcc; ++j) acc[j] = VT<T>::zero();
+          for (int j = 0; j < NA; ++j) acc[j] = VT<T>::zero();
         }
-        accumulate(acc, S[t].fu, S[t].ft, S[t].w);
+        accumulate<NG>(acc, S[t].fu, S[t].ft, S[t].w);
       }
       __syncwarp();
     }
@@ -297,12 +359,13 @@ template <class POL, int WPB>
 __global__ void __launch_bounds__(WPB * 32) k_adp(DMesh m, POL pol, int nf, double* A, size_t lda, size_t astride,
                                                   double* b, size_t bstride) {
   typedef typename POL::T T;
-  __shared__ Combo<T> sm[WPB][32];
+  constexpr int NG = POL::NG, NA = GOut<NG>::acc;
+  __shared__ Combo<T, NG> sm[WPB][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x / 32;
   const long long gw = blockIdx.x * (long long)WPB + w;
   if (gw >= (long long)m.ndn * nf) return;
   const int dn = (int)(gw % m.ndn), f = (int)(gw / m.ndn);
-  Combo<T>* S = sm[w];
+  Combo<T, NG>* S = sm[w];
   for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
     const int a0 = m.adp_start[cp], a1 = m.adp_start[cp + 1];
     if (a0 == a1) continue;
@@ -310,8 +373,8 @@ __global__ void __launch_bounds__(WPB * 32) k_adp(DMesh m, POL pol, int nf, doub
     const double* xi = m.cpx + 3 * (size_t)cp;
     const long long P0 = m.leaf_pt[l0], Q = m.leaf_pt[l1] - P0;
     int cur = -1;
-    T acc[kAcc];
-    for (int j = 0; j < kAcc; ++j) acc[j] = VT<T>::zero();
+    T acc[NA];
+    for (int j = 0; j < NA; ++j) acc[j] = VT<T>::zero();
     for (long long base = 0; base < Q; base += 32) {
       long long c = base + lane;
       if (c < Q) {
@@ -323,15 +386,15 @@ __global__ void __launch_bounds__(WPB * 32) k_adp(DMesh m, POL pol, int nf, doub
           double rv[3] = {G[g], G[np + g], G[2 * np + g]};
           double n[3] = {G[3 * np + g], G[4 * np + g], G[5 * np + g]};
           T fu9[9];
-          pol.point(f, rv, n, fu9, S[lane].ft);
-          store_u6(S[lane].fu, fu9);
+          pol.point(f, cp, rv, n, fu9, S[lane].ft);
+          store_u<NG>(S[lane].fu, fu9);
           for (int q = 0; q < 8; ++q) S[lane].w[q] = G[(6 + q) * np + g];
         } else {
           double rv[3], n[3], w[8];
           leaf_point(m, l, a, (int)(P0 + c - m.leaf_pt[l]), xi, rv, n, w);
           T fu9[9];
-          pol.point(f, rv, n, fu9, S[lane].ft);
-          store_u6(S[lane].fu, fu9);
+          pol.point(f, cp, rv, n, fu9, S[lane].ft);
+          store_u<NG>(S[lane].fu, fu9);
           for (int q = 0; q < 8; ++q) S[lane].w[q] = w[q];
         }
         S[lane].pair = a;
@@ -343,9 +406,9 @@ __global__ void __launch_bounds__(WPB * 32) k_adp(DMesh m, POL pol, int nf, doub
         if (a != cur) {
           if (cur >= 0) flush_pair(m, pol, f, dn, m.adp_e[cur], acc, A, lda, astride, b, bstride, nullptr);
           cur = a;
-          for (int j = 0; j < kAcc; ++j) acc[j] = VT<T>::zero();
+          for (int j = 0; j < NA; ++j) acc[j] = VT<T>::zero();
         }
-        accumulate(acc, S[t].fu, S[t].ft, S[t].w);
+        accumulate<NG>(acc, S[t].fu, S[t].ft, S[t].w);
       }
       __syncwarp();
     }
@@ -428,20 +491,21 @@ template <class POL, int WPB>
 __global__ void __launch_bounds__(WPB * 32) k_sing(DMesh m, POL pol, int nf, double* A, size_t lda, size_t astride,
                                                    double* b, size_t bstride) {
   typedef typename POL::T T;
-  __shared__ ComboS<T> sm[WPB][32];
+  constexpr int NG = POL::NG, NA = GOut<NG>::acc;
+  __shared__ ComboS<T, NG> sm[WPB][32];
   __shared__ double hp[WPB][17];  // hli[9], phi_i[8] of the pair being flushed
   const int lane = threadIdx.x & 31, w = threadIdx.x / 32;
   const long long gw = blockIdx.x * (long long)WPB + w;
   if (gw >= (long long)m.ndn * nf) return;
   const int dn = (int)(gw % m.ndn), f = (int)(gw / m.ndn);
-  ComboS<T>* S = sm[w];
+  ComboS<T, NG>* S = sm[w];
   for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
     const int q0 = m.sing_start[cp], q1 = m.sing_start[cp + 1];
     if (q0 == q1) continue;
     const long long P0 = m.sing_pt[q0], Q = m.sing_pt[q1] - P0;
     int cur = -1;
-    T acc[kAcc], acd[kAcc];
-    for (int j = 0; j < kAcc; ++j) acc[j] = acd[j] = VT<T>::zero();
+    T acc[NA], acd[NA];
+    for (int j = 0; j < NA; ++j) acc[j] = acd[j] = VT<T>::zero();
     for (long long base = 0; base < Q; base += 32) {
       long long c = base + lane;
       if (c < Q) {
@@ -460,8 +524,8 @@ __global__ void __launch_bounds__(WPB * 32) k_sing(DMesh m, POL pol, int nf, dou
           sing_point(m, q, (int)(P0 + c - m.sing_pt[q]), rv, n, S[lane].w, S[lane].wd);
         }
         T fu9[9];
-        pol.point_sing(f, rv, n, fu9, S[lane].ft, S[lane].fc);
-        store_u6(S[lane].fu, fu9);
+        pol.point_sing(f, cp, rv, n, fu9, S[lane].ft, S[lane].fc);
+        store_u<NG>(S[lane].fu, fu9);
         S[lane].pair = q;
       }
       __syncwarp();
@@ -470,18 +534,18 @@ __global__ void __launch_bounds__(WPB * 32) k_sing(DMesh m, POL pol, int nf, dou
         int q = S[t].pair;
         if (q != cur) {
           if (cur >= 0) {
-            for (int j = 0; j < kAcc; ++j) acc[j] = acc[j] + acd[j];
+            for (int j = 0; j < NA; ++j) acc[j] = acc[j] + acd[j];
             flush_pair(m, pol, f, dn, m.sing_e[cur], acc, A, lda, astride, b, bstride, hp[w]);
           }
           cur = q;
-          for (int j = 0; j < kAcc; ++j) acc[j] = acd[j] = VT<T>::zero();
+          for (int j = 0; j < NA; ++j) acc[j] = acd[j] = VT<T>::zero();
           if (lane < 17) {
             const double* D = m.sing_d + (size_t)q * SING_D;
             hp[w][lane] = lane < 9 ? D[13 + lane] : D[5 + lane - 9];
           }
           __syncwarp();
         }
-        accumulate(acc, S[t].fu, S[t].ft, S[t].w);
+        accumulate<NG>(acc, S[t].fu, S[t].ft, S[t].w);
         // CPV integrand with (phi - phi_i): h outputs only
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
@@ -495,7 +559,7 @@ __global__ void __launch_bounds__(WPB * 32) k_sing(DMesh m, POL pol, int nf, dou
       __syncwarp();
     }
     if (cur >= 0) {
-      for (int j = 0; j < kAcc; ++j) acc[j] = acc[j] + acd[j];
+      for (int j = 0; j < NA; ++j) acc[j] = acc[j] + acd[j];
       flush_pair(m, pol, f, dn, m.sing_e[cur], acc, A, lda, astride, b, bstride, hp[w]);
     }
   }
@@ -524,6 +588,11 @@ __global__ void k_free(DMesh m, POL pol, const double* nu /* complex, per freque
   T bc[3] = {z, z, z};
   for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
     int e = m.cp_elem[cp], kn0 = m.cp_kn[cp];
+    // half-space: a collocation point on the traction-free surface takes twice
+    // its free term (build_lse_mechanics_bem_staela.f90:502-513,
+    // build_lse_mechanics_bem_harela.f90:688-697)
+    const double two =
+        (m.hs_ax >= 0 && m.cpx[3 * (size_t)cp + m.hs_ax] - m.hs_x <= 1e-12 / m.cl[e]) ? 2.0 : 1.0;
     if (m.cp_kind[cp] == 0) {
       if (!m.ft_ok[cp]) { atomicExch(err, 1); continue; }
       const double* F = m.ft + (size_t)cp * FT_D;
@@ -534,6 +603,7 @@ __global__ void k_free(DMesh m, POL pol, const double* nu /* complex, per freque
         for (int ik = 0; ik < 3; ++ik) {
           T C = q * F[1 + 3 * il + ik];
           if (il == ik) C = C + F[0];
+          C = C * two;
           int dof = m.edof[8 * e + kn0] + ik;
           if (m.dct[dof] == 1) addA(Af, (size_t)dof * lda + row, C);
           else bc[il] = bc[il] - C * cval(m.dcv, dof, z);
@@ -545,7 +615,7 @@ __global__ void k_free(DMesh m, POL pol, const double* nu /* complex, per freque
       for (int kn = 0; kn < 8; ++kn)
         for (int il = 0; il < 3; ++il) {
           size_t row = 3 * (size_t)dn + il;
-          T v = fr(0.5 * phi[kn], z);
+          T v = fr(0.5 * phi[kn] * two, z);
           int dof = m.edof[8 * e + kn] + il;
           if (m.dct[dof] == 1) addA(Af, (size_t)dof * lda + row, v);
           else bc[il] = bc[il] - v * cval(m.dcv, dof, z);

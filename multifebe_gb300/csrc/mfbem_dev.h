@@ -85,6 +85,10 @@ struct DMesh {
   double* ft;            // [ncp][FT_D]
   int* ft_ok;            // [ncp] 1 ok, 0 invalid configuration
   long long nreg, nadp, nleaf, nsing;
+  // half-space region with a traction-free surface x[hs_ax] = hs_x (free
+  // terms of collocation points on it doubled); hs_ax = -1: full space
+  int hs_ax;
+  double hs_x;
 };
 
 }  // namespace mfb

@@ -526,4 +526,35 @@ __global__ void k_ft_prep(DMesh m) {
   m.ft_ok[cp] = 1;
 }
 
+// ---------------------------------------------------------------- half-space
+// Images of the collocation points in the free surface x3 = xp, on which the
+// complementary kernel's pairs are classified (fbem_bem_staela3d_hsc_sbie_auto,
+// bem_staela3d.f90:9074-9075), and c = x_i3 - xp of the points themselves.
+__global__ void k_hs_image(const double* cpx, int ncp, double xp, double* img, double* c) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncp) return;
+  img[3 * (size_t)i] = cpx[3 * (size_t)i];
+  img[3 * (size_t)i + 1] = cpx[3 * (size_t)i + 1];
+  img[3 * (size_t)i + 2] = 2.0 * xp - cpx[3 * (size_t)i + 2];
+  c[i] = cpx[3 * (size_t)i + 2] - xp;
+}
+// Configurations the reference stops on (bem_staela3d.f90:7466-7476,8700-8705):
+// bit 0, an element node or collocation point outside the half-space; bit 1,
+// an element holding a collocation point of the free surface (a singular pair
+// of the complementary kernel) that does not lie on the surface.
+__global__ void k_hs_check(DMesh mh, const double* c, double xp, int* err) {
+  const long long n1 = 8LL * mh.ne, n2 = n1 + mh.ncp, n3 = n2 + mh.nsing;
+  long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (id >= n3) return;
+  if (id < n1) {
+    if (mh.ex[3 * id + 2] < xp) atomicOr(err, 1);
+  } else if (id < n2) {
+    if (c[id - n1] < 0.0) atomicOr(err, 1);
+  } else {
+    const int e = mh.sing_e[id - n2];
+    for (int k = 0; k < 8; ++k)
+      if (fabs(mh.ex[24 * (size_t)e + 3 * k + 2] - xp) > 1e-12) atomicOr(err, 2);
+  }
+}
+
 }  // namespace mfb

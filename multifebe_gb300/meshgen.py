@@ -191,6 +191,90 @@ def surface_patch(half=10.0, n=40, load_half=1.0, traction=(0.0, 0.0, -1.0)):
 
 
 # ----------------------------------------------------------------------------
+# Half-space decks: the region x3 >= 0 with the traction-free surface x3 = 0
+# (outward normal -e3, the only plane the static complementary kernel takes).
+# Element normals point out of the soil.
+# ----------------------------------------------------------------------------
+
+_Q8_REVERSE = [0, 3, 2, 1, 7, 6, 5, 4]  # same element, opposite normal
+
+
+def halfspace_footing(a=1.0, n=8, p=1.0):
+    """Loaded square [-a,a]^2 on the surface x3 = 0 of the half-space x3 >= 0,
+    n x n quad8, uniform pressure p (traction (0, 0, p) on the soil, pushing
+    into it) on every node; the rest of the surface is free and not meshed.
+    Love's closed form for the settlement of the centre:
+    8 ln(1 + sqrt 2) p a (1 - nu^2) / (pi E)."""
+    h = 2.0 * a / n
+    key_to_node = {}
+    coords = []
+    conn = []
+    for b in range(n):
+        for c in range(n):
+            p1 = np.array([2 * c, 2 * b, 0])
+            el = []
+            # xi1 along +x2, xi2 along +x1: T1 x T2 = -e3
+            for q in _quad8_from_corner(p1, np.array([0, 2, 0]), np.array([2, 0, 0])):
+                key = (int(q[0]), int(q[1]))
+                if key not in key_to_node:
+                    key_to_node[key] = len(coords)
+                    coords.append([-a + 0.5 * h * q[0], -a + 0.5 * h * q[1], 0.0])
+                el.append(key_to_node[key])
+            conn.append(el)
+    nodes = np.array(coords, dtype=np.float64)
+    nn = len(nodes)
+    ctype = np.ones((nn, 3), dtype=np.int32)
+    cvalue = np.zeros((nn, 3), dtype=np.complex128)
+    cvalue[:, 2] = p
+    return Deck(f"hs_footing{n}", nodes, np.array(conn, dtype=np.int32), ctype, cvalue,
+                np.zeros(len(conn), dtype=np.int32))
+
+
+def _compact(nodes, conn):
+    used = np.unique(conn)
+    remap = -np.ones(len(nodes), dtype=np.int64)
+    remap[used] = np.arange(len(used))
+    return nodes[used], remap[conn].astype(np.int32)
+
+
+def halfspace_excavation(a=0.5, depth=0.5, n=4, p=1.0):
+    """Open box [-a,a]^2 x [0,depth] cut into the half-space x3 >= 0: its
+    bottom and four walls (no lid; the rim lies on the free surface and its
+    nodes get SBIE-MCA), normals into the box. Pressure p on the bottom
+    (traction (0, 0, p)), walls traction-free."""
+    d = box((2 * a, 2 * a, depth), (n, n, n), split_faces=False, name="hs_excavation")
+    keep = d.boundary_of_element != 0  # drop the face x3 = 0
+    conn = d.conn[keep][:, _Q8_REVERSE]
+    nodes = d.nodes - np.array([a, a, 0.0])
+    nodes, conn = _compact(nodes, conn)
+    nn = len(nodes)
+    ctype = np.ones((nn, 3), dtype=np.int32)
+    cvalue = np.zeros((nn, 3), dtype=np.complex128)
+    bottom = np.abs(nodes[:, 2] - depth) <= 1e-12
+    cvalue[bottom, 2] = p
+    return Deck(f"hs_excavation{n}", nodes, conn, ctype, cvalue, d.boundary_of_element[keep])
+
+
+def halfspace_cavity(a=0.25, top=0.2, n=3, p=1.0):
+    """Closed cubic cavity [-a,a]^2 x [top, top+2a] buried in the half-space
+    x3 >= 0, normals into the cavity, traction (0, 0, p) on every node."""
+    d = box((2 * a, 2 * a, 2 * a), (n, n, n), split_faces=False, name="hs_cavity")
+    conn = d.conn[:, _Q8_REVERSE].astype(np.int32)
+    nodes = d.nodes - np.array([a, a, -top])
+    nn = len(nodes)
+    ctype = np.ones((nn, 3), dtype=np.int32)
+    cvalue = np.zeros((nn, 3), dtype=np.complex128)
+    cvalue[:, 2] = p
+    return Deck(f"hs_cavity{n}", nodes, conn, ctype, cvalue, d.boundary_of_element)
+
+
+def love_square_centre(a, p, E, nu):
+    """Settlement of the centre of a uniformly loaded square 2a x 2a on an
+    elastic half-space (Love; four corners of a x a squares)."""
+    return 8.0 * np.log(1.0 + np.sqrt(2.0)) * p * a * (1.0 - nu ** 2) / (np.pi * E)
+
+
+# ----------------------------------------------------------------------------
 # Materials
 # ----------------------------------------------------------------------------
 

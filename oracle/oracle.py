@@ -64,6 +64,10 @@ def lib():
         L.orc_zexp.argtypes = [ctypes.c_double, ctypes.c_double, _dp]
         L.orc_nearest_quad8.argtypes = [_dp, ctypes.c_double, _dp, _dp, _dp, _dp, _ip]
         L.orc_freeterm.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp]
+        L.orc_problem_set_halfspace.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        L.orc_hsc_point.argtypes = [ctypes.c_double] * 3 + [_dp] * 5
+        L.orc_pair_hsc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                   _dp, _dp]
         _lib = L
     return _lib
 
@@ -122,22 +126,43 @@ class Problem:
         lib().orc_colloc(self._h, _p(x), _p(info, _ip))
         return x, info
 
+    def set_halfspace(self, n=-3, x=0.0, bc=1):
+        """Half-space region (read_regions.f90:130-200): hyperplane normal n,
+        coordinate x, traction-free surface (bc 1). The static builder adds the
+        complementary kernel (n = -3 only) and both builders double the free
+        term of collocation points on the surface."""
+        if lib().orc_problem_set_halfspace(self._h, int(n), float(x), int(bc)) != 0:
+            raise ValueError("half-space: n in -3..3 and bc = 1 only")
+
+    _ERR = {-1: "invalid normals/tangents configuration at a free-term node",
+            -2: "a point lies outside the half-space",
+            -3: "an element containing a collocation point on the free surface does not lie on it",
+            -4: "the static half-space kernel needs the hyperplane normal n = -3"}
+
     def assemble_staela(self, mu, nu, nthreads=0):
         n = self.n
         A = np.zeros((n, n), dtype=np.float64, order="F")
         b = np.zeros(n, dtype=np.float64)
-        st = np.zeros(6, dtype=np.int64)
+        st = np.zeros(8, dtype=np.int64)
         rc = lib().orc_assemble_staela(self._h, mu, nu, _p(A), _p(b), nthreads, _p(st, _lp))
         if rc != 0:
-            raise RuntimeError("oracle: invalid normals/tangents configuration at a free-term node")
+            raise RuntimeError("oracle: " + self._ERR.get(rc, str(rc)))
         self.stats = st
         return A, b
+
+    def pair_hsc(self, ci, e, mu, nu):
+        h = np.zeros((8, 3, 3))
+        g = np.zeros((8, 3, 3))
+        cls = lib().orc_pair_hsc(self._h, ci, e, mu, nu, _p(h), _p(g))
+        if cls < 0:
+            raise RuntimeError("oracle: " + self._ERR.get(cls, str(cls)))
+        return cls, h, g
 
     def assemble_harela(self, mat, omega, nthreads=0):
         n = self.n
         A = np.zeros((n, n), dtype=np.complex128, order="F")
         b = np.zeros(n, dtype=np.complex128)
-        st = np.zeros(6, dtype=np.int64)
+        st = np.zeros(8, dtype=np.int64)
         lam, mu, nu = complex(mat["lambda"]), complex(mat["mu"]), complex(mat["nu"])
         rc = lib().orc_assemble_harela_nu(self._h, lam.real, lam.imag, mu.real, mu.imag, float(mat["rho"]),
                                           float(omega), nu.real, nu.imag, _p(A), _p(b), nthreads, _p(st, _lp))
@@ -212,6 +237,17 @@ def lu_solve(A, b, threads=None, overwrite=False, rcond=False):
     con = sl.lapack.zgecon if np.iscomplexobj(lu) else sl.lapack.dgecon
     rc, info = con(lu, anorm, norm="1")
     return x, float(rc)
+
+
+def hsc_point(mu, nu, xp, x_i, x, n):
+    """Complementary half-space kernel at one point: u, t [3, 3] (load, component)."""
+    u = np.zeros((3, 3))
+    t = np.zeros((3, 3))
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (x_i, x, n)]
+    rc = lib().orc_hsc_point(mu, nu, xp, *[_p(v) for v in a], _p(u), _p(t))
+    if rc:
+        raise ValueError("point outside the half-space")
+    return u, t
 
 
 def gauss_tables():

@@ -6,6 +6,7 @@
 #include <cstring>
 #include <map>
 #include <algorithm>
+#include <type_traits>
 #include <omp.h>
 
 namespace orc {
@@ -205,8 +206,8 @@ static HarPar harela_parameters(cplx lambda, cplx mu, double rho, double omega) 
 struct StaelaK {
   typedef double T;
   static constexpr int F = 5;  // quasi-singular estimate for 1/r^5 integrands
-  double cteu1, cteu2, ctet1, ctet2;
-  StaelaK(double mu, double nu) {
+  double cteu1, cteu2, ctet1, ctet2, mu, nu;
+  StaelaK(double mu_, double nu_) : mu(mu_), nu(nu_) {
     cteu1 = 1.0 / (16.0 * c_pi * mu * (1.0 - nu));
     cteu2 = 3.0 - 4.0 * nu;
     ctet1 = -1.0 / (8.0 * c_pi * (1.0 - nu));
@@ -387,6 +388,16 @@ struct HarelaHK {
   }
 };
 
+// Kernel at the integration point x for the collocation point x_i: the
+// full-space kernels depend on x - x_i only; the half-space complementary
+// kernel (HscK, below) overloads this with the absolute coordinates.
+template <class K>
+inline void kernel_at(const K& k, const double x[3], const double x_i[3], const double n[3],
+                      typename K::T fu[3][3], typename K::T ft[3][3]) {
+  double rv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] - x_i[2]};
+  k.eval(rv, n, fu, ft);
+}
+
 template <class K>
 struct HG {
   typename K::T h[8][3][3], g[8][3][3];
@@ -406,9 +417,8 @@ static void ext_pre(const K& k, int ps, const Elem& e, bool reverse, const doubl
     const double* x = &e.px[kt * 3];
     const double* n = &e.pn[kt * 3];
     const double* pj = &e.pphijw[kt * 8];
-    double rv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] - x_i[2]};
     typename K::T fu[3][3], ft[3][3];
-    k.eval(rv, n, fu, ft);
+    kernel_at(k, x, x_i, n, fu, ft);
     for (int il = 0; il < 3; ++il)
       for (int ik = 0; ik < 3; ++ik)
         for (int a = 0; a < 8; ++a) {
@@ -465,12 +475,11 @@ static void ext_st(const K& k, const Elem& e, bool reverse, const double xi_s[4]
                      T1[0] * T2[1] - T1[1] * T2[0]};
       double jg = std::sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
       double n[3] = {N[0] / jg, N[1] / jg, N[2] / jg};
-      double rv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] - x_i[2]};
       double jw = jg * js * jt1 * jt2 * w1 * w2;
       double pj[8];
       for (int q = 0; q < 8; ++q) pj[q] = phi[q] * jw;
       typename K::T fu[3][3], ft[3][3];
-      k.eval(rv, n, fu, ft);
+      kernel_at(k, x, x_i, n, fu, ft);
       for (int il = 0; il < 3; ++il)
         for (int ik = 0; ik < 3; ++ik)
           for (int a = 0; a < 8; ++a) {
@@ -493,7 +502,11 @@ struct AdpStats { long leaves = 0, points = 0, maxdepth_hits = 0; };
 // sbie_ext_adp: bem_staela3d.f90:973-1096 / bem_harela3d.f90:1050-1172
 template <class K>
 static void ext_adp(const K& k, const Elem& e, bool reverse, double xi_s[4][2], const double x_i[3],
-                    const QsParams& qsp, int ks, int ns, HG<K>& acc, AdpStats* st) {
+                    const QsParams& qsp, int ks, int ns, HG<K>& acc, AdpStats* st, const double* x_near = nullptr) {
+  // x_near: the point whose nearest element point drives the subdivision (the
+  // collocation point, or its image for the half-space complementary kernel,
+  // bem_staela3d.f90:8411-8412)
+  const double* xn = x_near ? x_near : x_i;
   double barxip[2], rmin, d;
   int method;
   if (ks == 1) {
@@ -502,12 +515,12 @@ static void ext_adp(const K& k, const Elem& e, bool reverse, double xi_s[4][2], 
     xi_s[1][0] = 1;  xi_s[1][1] = -1;
     xi_s[2][0] = 1;  xi_s[2][1] = 1;
     xi_s[3][0] = -1; xi_s[3][1] = 1;
-    nearest_element_point_quad8(e.x, e.cl, x_i, barxip, &rmin, &d, &method);
+    nearest_element_point_quad8(e.x, e.cl, xn, barxip, &rmin, &d, &method);
   } else {
     double x_s[8][3];
     subdivision_coords_quad8(e.x, xi_s, x_s);
     double cl = characteristic_length_quad8(x_s, 1e-12);
-    nearest_element_point_quad8(x_s, cl, x_i, barxip, &rmin, &d, &method);
+    nearest_element_point_quad8(x_s, cl, xn, barxip, &rmin, &d, &method);
   }
   int gln_near = qs_n_estimation_telles(2, K::F, qsp, d, barxip);
   bool subdivide = false;
@@ -523,19 +536,19 @@ static void ext_adp(const K& k, const Elem& e, bool reverse, double xi_s[4][2], 
     for (int q = 0; q < 2; ++q) {
       t[0][q] = xi_s[0][q]; t[1][q] = 0.5 * (xi_s[0][q] + xi_s[1][q]); t[2][q] = c[q]; t[3][q] = 0.5 * (xi_s[0][q] + xi_s[3][q]);
     }
-    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st);
+    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st, x_near);
     for (int q = 0; q < 2; ++q) {
       t[0][q] = 0.5 * (xi_s[0][q] + xi_s[1][q]); t[1][q] = xi_s[1][q]; t[2][q] = 0.5 * (xi_s[1][q] + xi_s[2][q]); t[3][q] = c[q];
     }
-    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st);
+    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st, x_near);
     for (int q = 0; q < 2; ++q) {
       t[0][q] = c[q]; t[1][q] = 0.5 * (xi_s[1][q] + xi_s[2][q]); t[2][q] = xi_s[2][q]; t[3][q] = 0.5 * (xi_s[2][q] + xi_s[3][q]);
     }
-    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st);
+    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st, x_near);
     for (int q = 0; q < 2; ++q) {
       t[0][q] = 0.5 * (xi_s[0][q] + xi_s[3][q]); t[1][q] = c[q]; t[2][q] = 0.5 * (xi_s[2][q] + xi_s[3][q]); t[3][q] = xi_s[3][q];
     }
-    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st);
+    ext_adp(k, e, reverse, t, x_i, qsp, ks + 1, ns, acc, st, x_near);
   } else {
     double barr = telles_barr_any(d);
     int gln = std::max(gln_near, e.gln_far);
@@ -683,7 +696,7 @@ static void polar_loop(const Elem& e, const double xi_i[2], const double x_i[3],
         double n[3] = {N[0] / jg, N[1] / jg, N[2] / jg};
         double rv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] - x_i[2]};
         double jw = jg * rho * jtp * wa * wr;
-        fn(rv, n, phi, jw);
+        fn(x, rv, n, phi, jw);
       }
     }
   }
@@ -700,7 +713,7 @@ void sbie_int<StaelaK>(const StaelaK& k, const Elem& e, bool reverse, const doub
   for (int q = 0; q < 8; ++q)
     for (int c = 0; c < 3; ++c) x_i[c] = x_i[c] + phii[q] * e.x[q][c];
   int nsub, st[8];
-  auto fn = [&](const double rv[3], const double n[3], const double phi[8], double jw) {
+  auto fn = [&](const double*, const double rv[3], const double n[3], const double phi[8], double jw) {
     double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
     double d1r = 1.0 / r, d1r2 = d1r * d1r;
     double drdx[3] = {rv[0] * d1r, rv[1] * d1r, rv[2] * d1r};
@@ -745,7 +758,7 @@ void sbie_int<HarelaK>(const HarelaK& k, const Elem& e, bool reverse, const doub
     for (int c = 0; c < 3; ++c) x_i[c] = x_i[c] + phii[q] * e.x[q][c];
   int nsub, st[8];
   const HarPar& p = k.p;
-  auto fn = [&](const double rv[3], const double n[3], const double phi[8], double jw) {
+  auto fn = [&](const double*, const double rv[3], const double n[3], const double phi[8], double jw) {
     double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
     cplx psi, chi, TT1, TT2, TT3;
     double dr1, dr2;
@@ -857,6 +870,208 @@ static int hbie_auto(const K& k, const Elem& e, bool reverse, const double x_i[3
 }
 
 // ---------------------------------------------------------------------------
+// Half-space complementary kernel (static): the part of Mindlin's fundamental
+// solution for the half-space x3 >= xp with a traction-free surface x3 = xp
+// (outward unit normal (0, 0, -1)) that is added to Kelvin's full-space
+// solution. fbem_bem_staela3d_hsc_sbie, bem_staela3d.f90:7438-7563, with its
+// constants applied per point. As written there, the image point is
+// (x_i1, x_i2, -x_i3) (the reflection in x3 = 0) while c and z are measured
+// from x3 = xp: both agree for the plane x3 = 0. u[il][ik], t[il][ik]: load
+// direction il, observed component ik.
+// ---------------------------------------------------------------------------
+static thread_local int g_hs_err = 0;  // 1: a point below the free surface; 2: a singular element off it
+
+struct HscK {
+  typedef double T;
+  static constexpr int F = 5;
+  double mu, nu, xp;
+  HscK(double mu_, double nu_, double xp_) : mu(mu_), nu(nu_), xp(xp_) {}
+  double cu() const { return 1.0; }
+  double ct() const { return 1.0; }
+  void eval_at(const double x[3], const double x_i[3], const double n[3], double u[3][3], double t[3][3]) const {
+    if (x_i[2] < xp || x[2] < xp) g_hs_err = 1;
+    const double c1 = 1.0 - nu, c2 = 1.0 - 2.0 * nu, c3 = 3.0 - 2.0 * nu, c4 = 3.0 - 4.0 * nu, c5 = 5.0 - 4.0 * nu;
+    const double c = x_i[2] - xp, z = x[2] - xp;
+    const double rv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] - x_i[2]};
+    const double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1]);
+    const double rpv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] + x_i[2]};
+    const double rp = std::sqrt(rpv[0] * rpv[0] + rpv[1] * rpv[1] + rpv[2] * rpv[2]);
+    const double rp2 = rp * rp, rp3 = rp2 * rp, rp5 = rp3 * rp2, rp7 = rp5 * rp2;
+    const double zc = z + c, q = rp + z + c;
+    const double r1 = rv[0] * rv[0], r2 = rv[1] * rv[1];
+    // load along the normal, local cylindrical axes (r, theta, x3)
+    double un[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, sn[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    un[2][0] = r * (c4 * (z - c) / rp3 - 4.0 * c1 * c2 / rp / q + 6.0 * c * z * zc / rp5);
+    un[2][2] = (8.0 * (c1 * c1) - c4) / rp + (c4 * (zc * zc) - 2.0 * c * z) / rp3 + 6.0 * c * z * (zc * zc) / rp5;
+    sn[0][0] = -c2 * (z + 7.0 * c) / rp3 + 4.0 * c1 * c2 / rp / q +
+               (6.0 * c * c2 * (zc * zc) - 6.0 * (c * c) * zc - 3.0 * c4 * (r * r) * (z - c)) / rp5 -
+               30.0 * c * (r * r) * z * zc / rp7;
+    sn[0][2] = r * (c2 / rp3 - (3.0 * c4 * z * zc - 3.0 * c * (3.0 * z + c)) / rp5 - 30.0 * c * z * (zc * zc) / rp7);
+    sn[2][0] = sn[0][2];
+    sn[1][1] = c2 * (c4 * zc - 6.0 * c) / rp3 - 4.0 * c1 * c2 / rp / q + 6.0 * c2 * c * (zc * zc) / rp5 -
+               6.0 * (c * c) * zc / rp5;
+    sn[2][2] = c2 * (z - c) / rp3 - (3.0 * c4 * z * (zc * zc) - 3.0 * c * zc * (5.0 * z - c)) / rp5 -
+               30.0 * c * z * (zc * zc * zc) / rp7;
+    // to global axes: L (.) L^T with L the rotation by theta about x3
+    const double th = std::atan2(x[1] - x_i[1], x[0] - x_i[0]);
+    const double L[3][3] = {{std::cos(th), -std::sin(th), 0.0}, {std::sin(th), std::cos(th), 0.0}, {0.0, 0.0, 1.0}};
+    auto rot = [&](double a[3][3]) {
+      double tmp[3][3], out[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double v = 0.0;
+          for (int k = 0; k < 3; ++k) v = v + a[i][k] * L[j][k];
+          tmp[i][j] = v;
+        }
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double v = 0.0;
+          for (int k = 0; k < 3; ++k) v = v + L[i][k] * tmp[k][j];
+          out[i][j] = v;
+        }
+      std::memcpy(a, out, sizeof(out));
+    };
+    rot(un);
+    rot(sn);
+    // loads tangent to the surface, global axes
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) u[i][j] = 0.0;
+    const double q2 = q * q;
+    u[0][0] = 1.0 / rp + c4 * r1 / rp3 + 2.0 * c * z / rp3 * (1.0 - 3.0 * r1 / rp2) + 4.0 * c1 * c2 / q * (1.0 - r1 / rp / q);
+    u[0][1] = rv[0] * rv[1] * (c4 / rp3 - 6.0 * c * z / rp5 - 4.0 * c1 * c2 / rp / q2);
+    u[0][2] = rv[0] * (c4 * (z - c) / rp3 - 6.0 * c * z * zc / rp5 + 4.0 * c1 * c2 / rp / q);
+    u[1][0] = rv[0] * rv[1] * (c4 / rp3 - 6.0 * c * z / rp5 - 4.0 * c1 * c2 / rp / q2);
+    u[1][1] = 1.0 / rp + c4 * r2 / rp3 + 2.0 * c * z / rp3 * (1.0 - 3.0 * r2 / rp2) + 4.0 * c1 * c2 / q * (1.0 - r2 / rp / q);
+    u[1][2] = rv[1] * (c4 * (z - c) / rp3 - 6.0 * c * z * zc / rp5 + 4.0 * c1 * c2 / rp / q);
+    double sg[3][3][3];  // sg[i][j][k]: stress ij of the load along k
+    std::memset(sg, 0, sizeof(sg));
+    const double b1 = 3.0 * rp + z + c;
+    sg[0][0][0] = rv[0] * (c2 * c5 / rp3 - 3.0 * c4 * r1 / rp5 - 4.0 * c1 * c2 / rp / q2 * (3.0 - r1 * b1 / rp2 / q) +
+                           6.0 * c / rp5 * (3.0 * c - c3 * zc + 5.0 * r1 * z / rp2));
+    sg[1][1][0] = rv[0] * (c2 * c4 / rp3 - 3.0 * c4 * r2 / rp5 - 4.0 * c1 * c2 / rp / q2 * (1.0 - r2 * b1 / rp2 / q) +
+                           6.0 * c / rp5 * (c - c2 * zc + 5.0 * r2 * z / rp2));
+    sg[2][2][0] = rv[0] * (-c2 / rp3 - 3.0 * c4 * (zc * zc) / rp5 + 6.0 * c / rp5 * (c + c2 * zc + 5.0 * z * (zc * zc) / rp2));
+    sg[1][2][0] = rv[0] * rv[1] * (-3.0 * c4 * zc / rp5 + 6.0 * c / rp5 * (c2 + 5.0 * z * zc / rp2));
+    sg[2][0][0] = c2 * (z - c) / rp3 - 3.0 * c4 * r1 * zc / rp5 - 6.0 * c / rp5 * (z * zc - c2 * r1 - 5.0 * r1 * z * zc / rp2);
+    sg[0][1][0] = rv[1] * (c2 / rp3 - 3.0 * c4 * r1 / rp5 - 4.0 * c1 * c2 / rp / q2 * (1.0 - r1 * b1 / rp2 / q) -
+                           6.0 * c * z / rp5 * (1.0 - 5.0 * r1 / rp2));
+    sg[2][1][0] = sg[1][2][0];
+    sg[0][2][0] = sg[2][0][0];
+    sg[1][0][0] = sg[0][1][0];
+    sg[0][0][1] = rv[1] * (c2 * c4 / rp3 - 3.0 * c4 * r1 / rp5 - 4.0 * c1 * c2 / rp / q2 * (1.0 - r1 * b1 / rp2 / q) +
+                           6.0 * c / rp5 * (c - c2 * zc + 5.0 * r1 * z / rp2));
+    sg[1][1][1] = rv[1] * (c2 * c5 / rp3 - 3.0 * c4 * r2 / rp5 - 4.0 * c1 * c2 / rp / q2 * (3.0 - r2 * b1 / rp2 / q) +
+                           6.0 * c / rp5 * (3.0 * c - c3 * zc + 5.0 * r2 * z / rp2));
+    sg[2][2][1] = rv[1] * (-c2 / rp3 - 3.0 * c4 * (zc * zc) / rp5 + 6.0 * c / rp5 * (c + c2 * zc + 5.0 * z * (zc * zc) / rp2));
+    sg[0][2][1] = rv[0] * rv[1] * (-3.0 * c4 * zc / rp5 + 6.0 * c / rp5 * (c2 + 5.0 * z * zc / rp2));
+    sg[2][1][1] = c2 * (z - c) / rp3 - 3.0 * c4 * r2 * zc / rp5 - 6.0 * c / rp5 * (z * zc - c2 * r2 - 5.0 * r2 * z * zc / rp2);
+    sg[1][0][1] = rv[0] * (c2 / rp3 - 3.0 * c4 * r2 / rp5 - 4.0 * c1 * c2 / rp / q2 * (1.0 - r2 * b1 / rp2 / q) -
+                           6.0 * c * z / rp5 * (1.0 - 5.0 * r2 / rp2));
+    sg[2][0][1] = sg[0][2][1];
+    sg[1][2][1] = sg[2][1][1];
+    sg[0][1][1] = sg[1][0][1];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) sg[i][j][2] = sn[i][j];
+    const double cu_ = 16.0 * c_pi * c1 * mu, cs_ = 8.0 * c_pi * c1;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) u[i][j] = (u[i][j] + un[i][j]) / cu_;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) sg[i][j][k] = sg[i][j][k] / cs_;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) t[i][j] = sg[j][0][i] * n[0] + sg[j][1][i] * n[1] + sg[j][2][i] * n[2];
+  }
+};
+inline void kernel_at(const HscK& k, const double x[3], const double x_i[3], const double n[3], double fu[3][3],
+                      double ft[3][3]) {
+  k.eval_at(x, x_i, n, fu, ft);
+}
+
+// fbem_bem_staela3d_hsc_sbie_int (bem_staela3d.f90:8624-8833): element on the
+// free surface containing the collocation point. h is minus the full-space h
+// (the complete traction kernel vanishes on the free surface); g integrates
+// the complementary displacement kernel restricted to the surface with the
+// same polar rule as the full-space singular integration.
+static void hsc_int(const StaelaK& kf, const HscK& k, const Elem& e, bool reverse, const double xi_i[2], HG<HscK>& out) {
+  out.zero();
+  for (int q = 0; q < 8; ++q)
+    if (std::fabs(e.x[q][2] - k.xp) > 1e-12) g_hs_err = 2;
+  HG<StaelaK> full;
+  sbie_int<StaelaK>(kf, e, reverse, xi_i, full);
+  for (int a = 0; a < 8; ++a)
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) out.h[a][il][ik] = -full.h[a][il][ik];
+  double phii[8];
+  phi_quad8(xi_i, phii);
+  double x_i[3] = {0, 0, 0};
+  for (int q = 0; q < 8; ++q)
+    for (int c = 0; c < 3; ++c) x_i[c] = x_i[c] + phii[q] * e.x[q][c];
+  const double nu = k.nu, xp = k.xp;
+  auto fn = [&](const double* x, const double rv[3], const double*, const double phi[8], double jw) {
+    double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    double d1r = 1.0 / r;
+    double dr[3] = {rv[0] * d1r, rv[1] * d1r, rv[2] * d1r};
+    const double a = 3.0 - 4.0 * nu, b = 4.0 * (1.0 - nu) * (1.0 - 2.0 * nu), s = r + x[2] - xp;
+    double gk[3][3];
+    gk[0][0] = d1r + a * (dr[0] * dr[0]) * d1r + b / s * (1.0 - (dr[0] * dr[0]) * r / s);
+    gk[0][1] = a * dr[0] * dr[1] * d1r - b * dr[0] * dr[1] * r / (s * s);
+    gk[0][2] = a * dr[0] * dr[2] * d1r + b * dr[0] / s;
+    gk[1][0] = a * dr[0] * dr[1] * d1r - b * dr[0] * dr[1] * r / (s * s);
+    gk[1][1] = d1r + a * (dr[1] * dr[1]) * d1r + b / s * (1.0 - (dr[1] * dr[1]) * r / s);
+    gk[1][2] = a * dr[1] * dr[2] * d1r + b * dr[1] / s;
+    gk[2][0] = a * dr[0] * dr[2] * d1r - b * dr[0] / s;
+    gk[2][1] = a * dr[1] * dr[2] * d1r - b * dr[1] / s;
+    gk[2][2] = (8.0 * ((1.0 - nu) * (1.0 - nu)) - a) * d1r + a * (dr[2] * dr[2]) * d1r;
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik)
+        for (int q = 0; q < 8; ++q) out.g[q][il][ik] = out.g[q][il][ik] + gk[il][ik] * (phi[q] * jw);
+  };
+  int nsub, st[8];
+  polar_loop<HscK>(e, xi_i, x_i, fn, &nsub, st);
+  const double cg = 16.0 * c_pi * k.mu * (1.0 - nu);
+  for (int q = 0; q < 8; ++q)
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) out.g[q][il][ik] = out.g[q][il][ik] / cg;
+}
+
+// fbem_bem_staela3d_hsc_sbie_auto (bem_staela3d.f90:9047-9118): sbie_auto's
+// classification on the image of the collocation point in the free surface,
+// the kernel evaluated at the collocation point itself.
+static int hsc_auto(const StaelaK& kf, const HscK& k, const Elem& e, bool reverse, const double x_i[3],
+                    const QsParams& qsp, int ns, HG<HscK>& out, AdpStats* st) {
+  const double xq[3] = {x_i[0], x_i[1], 2.0 * k.xp - x_i[2]};
+  double r[3] = {e.bc[0] - xq[0], e.bc[1] - xq[1], e.bc[2] - xq[2]};
+  double rmin = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) - e.br;
+  double barxi[2], d;
+  int delta;
+  if (rmin > 4.0 * e.br) {
+    delta = 0;
+    barxi[0] = barxi[1] = 0.0;
+    d = rmin / e.cl;
+  } else {
+    int method;
+    nearest_element_point_quad8(e.x, e.cl, xq, barxi, &rmin, &d, &method);
+    delta = (d <= 1e-12) ? 1 : 0;
+  }
+  if (delta == 1) {
+    hsc_int(kf, k, e, reverse, barxi, out);
+    return CLS_SING;
+  }
+  int gln_near = qs_n_estimation_standard(2, HscK::F, qsp, d, barxi);
+  int gln = std::max(e.gln_far, gln_near);
+  if (gln <= e.ps_gln_max && gln_near > 0) {
+    int ps = 0;
+    for (int i = 0; i < e.n_ps; ++i)
+      if (e.ps_gln[i] >= gln) { ps = i; break; }
+    ext_pre<HscK>(k, ps, e, reverse, x_i, out);
+    return ps;
+  }
+  double xi_s[4][2];
+  ext_adp<HscK>(k, e, reverse, xi_s, x_i, qsp, 1, ns, out, st, xq);
+  return CLS_ADP;
+}
+
+// ---------------------------------------------------------------------------
 // Free term: V. Mantic's formula, bem_staela3d.f90:228-405 (real nu) and
 // bem_harela3d.f90:365-542 (complex nu): identical algorithm.
 // Returns false when the normals/tangents configuration is invalid (the
@@ -963,6 +1178,11 @@ struct Problem {
   std::vector<Colloc> cps;
   std::vector<std::vector<int>> node_cps;        // collocation points per node
   int ndof;
+  // region space (read_regions.f90:130-200): hs_n = 0 full space, else the
+  // half-space with hyperplane normal hs_n (+-1..3), coordinate hs_x and
+  // boundary condition hs_bc (1: traction-free surface)
+  int hs_n = 0, hs_bc = 1;
+  double hs_x = 0.0;
 };
 
 static void build(Problem& P) {
@@ -1128,6 +1348,16 @@ static bool free_terms_for_node(const Problem& P, int s, typename K::T nu, typen
       for (int il = 0; il < 3; ++il)
         for (int a = 0; a < 8; ++a) hg.h[a][il][il] = hg.h[a][il][il] + 0.5 * pphi[a];
     }
+    // half-space with a traction-free surface: a collocation point on the
+    // surface takes twice the free term (build_lse_mechanics_bem_staela.f90:502-513,
+    // build_lse_mechanics_bem_harela.f90:688-697)
+    if (P.hs_n != 0) {
+      const int ax = std::abs(P.hs_n) - 1;
+      if (cp.x[ax] - P.hs_x <= 1e-12 / P.el[cp.elem].cl && P.hs_bc == 1)
+        for (int a = 0; a < 8; ++a)
+          for (int il = 0; il < 3; ++il)
+            for (int ik = 0; ik < 3; ++ik) hg.h[a][il][ik] = 2.0 * hg.h[a][il][ik];
+    }
     scatter<T>(P, cp.elem, hg.h, hg.g, rowbuf, brow);
   }
   return true;
@@ -1140,10 +1370,13 @@ static int assemble(const Problem& P, const K& k, typename K::T nu, typename K::
   const int n = P.ndof;
   int nord = (int)P.node_order.size();
   int bad = 0;
-  long s_leaves = 0, s_points = 0, s_maxd = 0, s_sing = 0, s_adp = 0, s_pre = 0;
+  long s_leaves = 0, s_points = 0, s_maxd = 0, s_sing = 0, s_adp = 0, s_pre = 0, s_hsing = 0, s_hadp = 0;
+  int hs_err = 0;
   if (nthreads > 0) omp_set_num_threads(nthreads);
-#pragma omp parallel reduction(+ : bad, s_leaves, s_points, s_maxd, s_sing, s_adp, s_pre)
+#pragma omp parallel reduction(+ : bad, s_leaves, s_points, s_maxd, s_sing, s_adp, s_pre, s_hsing, s_hadp) \
+    reduction(max : hs_err)
   {
+    g_hs_err = 0;
     std::vector<T> rowbuf(3 * (size_t)n);
     AdpStats st;
 #pragma omp for schedule(dynamic, 1)
@@ -1158,6 +1391,23 @@ static int assemble(const Problem& P, const K& k, typename K::T nu, typename K::
           if (cls == CLS_SING) s_sing++;
           else if (cls == CLS_ADP) s_adp++;
           else s_pre++;
+          if constexpr (std::is_same<K, StaelaK>::value) {
+            // half-space region: h, g of the complementary kernel added to the
+            // full-space ones (build_lse_mechanics_bem_staela.f90:861-875)
+            if (P.hs_n != 0) {
+              HscK kh(k.mu, k.nu, P.hs_x);
+              HG<HscK> hp;
+              int c2 = hsc_auto(k, kh, P.el[e], false, P.cps[ci].x, P.qsp, P.ns_max, hp, &st);
+              if (c2 == CLS_SING) s_hsing++;
+              else if (c2 == CLS_ADP) s_hadp++;
+              for (int a = 0; a < 8; ++a)
+                for (int il = 0; il < 3; ++il)
+                  for (int ik = 0; ik < 3; ++ik) {
+                    hg.h[a][il][ik] = hg.h[a][il][ik] + hp.h[a][il][ik];
+                    hg.g[a][il][ik] = hg.g[a][il][ik] + hp.g[a][il][ik];
+                  }
+            }
+          }
           scatter<T>(P, e, hg.h, hg.g, rowbuf.data(), brow);
         }
       }
@@ -1171,10 +1421,13 @@ static int assemble(const Problem& P, const K& k, typename K::T nu, typename K::
     s_leaves += st.leaves;
     s_points += st.points;
     s_maxd += st.maxdepth_hits;
+    hs_err = std::max(hs_err, g_hs_err);
   }
   if (stats) {
     stats[0] = s_pre; stats[1] = s_adp; stats[2] = s_sing; stats[3] = s_leaves; stats[4] = s_points; stats[5] = s_maxd;
+    stats[6] = s_hadp; stats[7] = s_hsing;
   }
+  if (hs_err) return -1 - hs_err;
   return bad ? -1 : 0;
 }
 
@@ -1304,8 +1557,45 @@ void orc_node_geometry(void* h, double* n_gn, double* tbp, double* tbm, char* in
   std::memcpy(in_boundary, P->in_boundary.data(), P->in_boundary.size());
 }
 
+// Region space: n = 0 full space, else the half-space normal (+-1..3), its
+// hyperplane coordinate and boundary condition (1 traction-free). The static
+// complementary kernel exists for n = -3 only (bem_staela3d.f90:7466-7468);
+// the harmonic builder applies the free-term rule alone.
+int orc_problem_set_halfspace(void* h, int n, double x, int bc) {
+  Problem* P = (Problem*)h;
+  if (n < -3 || n > 3 || bc != 1) return -1;
+  P->hs_n = n;
+  P->hs_x = x;
+  P->hs_bc = bc;
+  return 0;
+}
+// One point of the complementary kernel (u, t [3][3]: load, component).
+int orc_hsc_point(double mu, double nu, double xp, const double* x_i, const double* x, const double* n, double* u,
+                  double* t) {
+  HscK k(mu, nu, xp);
+  g_hs_err = 0;
+  double uu[3][3], tt[3][3];
+  k.eval_at(x, x_i, n, uu, tt);
+  std::memcpy(u, uu, sizeof(uu));
+  std::memcpy(t, tt, sizeof(tt));
+  return g_hs_err;
+}
+// One (collocation point, element) pair of the complementary kernel.
+int orc_pair_hsc(void* hp, int ci, int e, double mu, double nu, double* h, double* g) {
+  Problem* P = (Problem*)hp;
+  StaelaK kf(mu, nu);
+  HscK k(mu, nu, P->hs_x);
+  HG<HscK> hg;
+  g_hs_err = 0;
+  int cls = hsc_auto(kf, k, P->el[e], false, P->cps[ci].x, P->qsp, P->ns_max, hg, nullptr);
+  std::memcpy(h, hg.h, sizeof(hg.h));
+  std::memcpy(g, hg.g, sizeof(hg.g));
+  return g_hs_err ? -1 - g_hs_err : cls;
+}
+
 int orc_assemble_staela(void* h, double mu, double nu, double* A, double* b, int nthreads, long* stats) {
   Problem* P = (Problem*)h;
+  if (P->hs_n != 0 && P->hs_n != -3) return -4;
   StaelaK k(mu, nu);
   return assemble<StaelaK>(*P, k, nu, A, b, nthreads, stats);
 }
