@@ -14,8 +14,10 @@ host buffers: mesh upload (H2D) + sweep + solution download (D2H) every step.
 Beside the headline: the plain FP64 GPU path on the same sweep
 (plain_fp64_gpu), the 14883-DOF surface patch with mixed vs plain FP64
 (precision_form), the learned quadrature on the thin slab (learned_quadrature),
-48 uneven problems in one batched call (batching_form), the roofline of the
-dominant kernel and the CPU oracle timed on the host cores.
+48 uneven problems in one batched call (batching_form), the static cube
+(870 DOF), the thin slab (5190 DOF) and a half-space footing with their CPU
+arms (configs_form), the roofline of the dominant kernel and the CPU oracle
+timed on the host cores.
 
 --impl reference times the reference-equivalent CPU path (the oracle: OpenMP
 assembly on all host cores + OpenBLAS getrf/getrs) on one frequency per step.
@@ -292,6 +294,8 @@ def run_gpu(args):
         line["learned_quadrature"] = learned_quadrature()
     if args.batching:
         line["batching_form"] = batching_form()
+    if args.configs:
+        line["configs_form"] = configs_form()
     # cpu baseline: the reference arm's sampling on a bounded sample of the sweep
     try:
         v, cores, secs = cpu_sweep_rate(deck, mat, om, 5)
@@ -566,6 +570,112 @@ def precision_form(steps=3, warmup=1):
     return out
 
 
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    return O
+
+
+def configs_form():
+    """The other benchmark configurations, each with its CPU arm (the oracle
+    on all host cores) and the error of the GPU solutions against the
+    oracle's FP64 solution:
+      cfg 1: staela cube 4x4 per face (870 real DOF), plain and mixed;
+      cfg 5: harela thin slab (5190 complex DOF), both frequencies, plain and
+             mixed sweeps;
+      half-space footing: staela, 8x8 quad8 loaded square on the surface of a
+             half-space (complementary kernel), plain, with Love's closed form."""
+    from multifebe_gb300 import meshgen as M, BemRegion
+    O = _oracle()
+    cores = os.cpu_count()
+    out = {}
+
+    def rel(a, b):
+        return float(np.abs(a - b).max() / np.abs(b).max())
+
+    def static_case(deck, mat, hs, reps):
+        R = BemRegion(deck)
+        if hs:
+            R.set_halfspace(-3, 0.0, 1)
+        res = {}
+        xs = {}
+        for prec in ("plain", "mixed"):
+            R.solve_staela(mat["mu"], mat["nu"], precision=prec)  # warm-up
+            ms = []
+            for _ in range(reps):
+                xs[prec] = R.solve_staela(mat["mu"], mat["nu"], precision=prec)
+                st = R.last_stats
+                ms.append(st["ms_assemble"] + st["ms_factor"] + st["ms_solve"])
+            res[prec] = {"value": 1e3 / statistics.mean(ms), "unit": "solves/s", "ms_per_solve": statistics.mean(ms),
+                         "ms_assemble": st["ms_assemble"], "ms_factor": st["ms_factor"], "ms_solve": st["ms_solve"]}
+        P = O.Problem(deck)
+        if hs:
+            P.set_halfspace(-3, 0.0, 1)
+        P.assemble_staela(mat["mu"], mat["nu"], nthreads=cores)  # warm-up
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            A, b = P.assemble_staela(mat["mu"], mat["nu"], nthreads=cores)
+            xo = O.lu_solve(A, b, overwrite=True)
+            ts.append(time.perf_counter() - t0)
+        res["cpu_baseline"] = {"value": 1.0 / statistics.mean(ts), "unit": "solves/s", "cores": cores, "kind": "port",
+                               "sample": "3 assemble + getrf/getrs of the oracle after one untimed assembly"}
+        for prec in ("plain", "mixed"):
+            res[prec]["rel_err_vs_fp64_oracle"] = rel(xs[prec], xo)
+            res[prec]["speedup_over_cpu"] = res[prec]["value"] / res["cpu_baseline"]["value"]
+        R.close()
+        return res, xs, P
+
+    deck, mat, _ = M.workload(1)
+    out["cfg1_staela_cube4"], _, _ = static_case(deck, mat, False, 20)
+    out["cfg1_staela_cube4"]["n_dof"] = deck.n_dof
+
+    deck = M.halfspace_footing(1.0, 8, 1.0)
+    mat = M.elastic(1.0, 0.25)
+    res, xs, P = static_case(deck, mat, True, 10)
+    u, _ = P.solution(xs["plain"])
+    c = int(np.argmin(np.linalg.norm(deck.nodes, axis=1)))
+    w = M.love_square_centre(1.0, 1.0, 1.0, 0.25)
+    res["love_centre_settlement"] = {"gpu": float(u[c, 2]), "closed_form": w, "rel_err": abs(u[c, 2] - w) / w}
+    res["n_dof"] = deck.n_dof
+    out["halfspace_footing_8x8"] = res
+
+    deck, mat, om = M.workload(5)
+    R = BemRegion(deck)
+    res = {"n_dof": deck.n_dof, "frequencies": len(om)}
+    X = {}
+    for prec in ("plain", "mixed"):
+        R.sweep_harela(mat, om, precision=prec)  # warm-up
+        ms = []
+        for _ in range(3):
+            X[prec] = R.sweep_harela(mat, om, precision=prec)
+            st = R.last_stats
+            ms.append(st["ms_assemble"] + st["ms_factor"] + st["ms_solve"])
+        res[prec] = {"value": len(om) / (statistics.mean(ms) / 1e3), "unit": "solves/s",
+                     "ms_per_sweep": statistics.mean(ms), "ms_assemble": st["ms_assemble"],
+                     "ms_factor": st["ms_factor"], "ms_solve": st["ms_solve"]}
+    R.close()
+    P = O.Problem(deck)
+    ts, errs = [], {"plain": 0.0, "mixed": 0.0}
+    for i, wv in enumerate(om):
+        t0 = time.perf_counter()
+        A, b = P.assemble_harela(mat, float(wv), nthreads=cores)
+        xo = O.lu_solve(A, b, overwrite=True)
+        ts.append(time.perf_counter() - t0)
+        del A
+        for prec in errs:
+            errs[prec] = max(errs[prec], rel(X[prec][i], xo))
+    res["cpu_baseline"] = {"value": len(ts) / sum(ts), "unit": "solves/s", "cores": cores, "kind": "port",
+                           "sample": "both frequencies assembled and solved by the oracle (first includes warm-up)"}
+    for prec in errs:
+        res[prec]["rel_err_vs_fp64_oracle"] = errs[prec]
+        res[prec]["speedup_over_cpu"] = res[prec]["value"] / res["cpu_baseline"]["value"]
+    res["note"] = ("the slab's systems are ill-conditioned (1/rcond ~1e7 at a0 = 0.2): both GPU paths differ "
+                   "from the oracle by the conditioning times ~1e-12 assembly differences")
+    out["cfg5_harela_slab16"] = res
+    return out
+
+
 def profile_case(nf, precision="mixed"):
     """Small fixed case for ncu captures: the benchmark mesh, nf frequencies,
     two sweeps of the given precision."""
@@ -605,6 +715,8 @@ def main():
                     help="skip the learned-quadrature measurement on the thin slab")
     ap.add_argument("--no-batching", dest="batching", action="store_false",
                     help="skip the 48-problem batch of uneven meshes")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="skip configurations 1 and 5 and the half-space footing")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="profiling helper: run the benchmark mesh for this many frequencies twice, print stats, exit")
     ap.add_argument("--profile-precision", default="mixed", choices=["mixed", "plain"],

@@ -758,7 +758,7 @@ __global__ void __launch_bounds__(128) k_trsm_runp(S* A, long long sA, int lda, 
 constexpr long long kTrsvSpin = 1LL << 22;
 template <typename S>
 constexpr size_t trsv_sf_smem() {
-  return sizeof(S) * (64 * 65 + 4 * 64);
+  return sizeof(S) * (64 * 65 + 4 * 64 + 64);
 }
 __device__ __forceinline__ int ld_acquire_s32(const int* p) {
   int v;
@@ -769,10 +769,12 @@ template <typename S, bool LOWER>
 __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int lda, int n, S* x, long long sx,
                                                  int batch, int nb, unsigned* counter, int* ready, int* err,
                                                  long long spin) {
-  // dynamic shared memory: D [64 x 65] (diagonal block, column-major), part [4][64]
+  // dynamic shared memory: D [64 x 65] (diagonal block, column-major), part [4][64],
+  // xs [64] (the solved block being applied)
   extern __shared__ __align__(16) unsigned char sfraw[];
   S* D = reinterpret_cast<S*>(sfraw);
   S (*part)[64] = reinterpret_cast<S (*)[64]>(D + 64 * 65);
+  S* xs = D + 64 * 65 + 4 * 64;
   __shared__ int s_item, s_end;
   const int t = threadIdx.x, row = t & 63, grp = t >> 6;
   const long long lim = spin > 0 ? spin : kTrsvSpin;
@@ -786,6 +788,21 @@ __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int l
     const int r0 = blk * 64, w = min(64, n - r0);
     const S* M = A + sA * b;
     S* xb = x + sx * b;
+    // this thread's 16 entries (row, columns grp + 4i) of the next solved
+    // block's tile: loaded before that block is published (the factors do not
+    // depend on it), so applying a newly solved block costs one load of its
+    // 64 values and 16 FMAs
+    S mreg[16];
+    auto load_tile = [&](int qq) {
+      const int jb = LOWER ? qq : nb - 1 - qq;
+      const int c0 = jb * 64, wc = min(64, n - c0);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int c = grp + 4 * i;
+        mreg[i] = (row < w && c < wc) ? M[(size_t)(c0 + c) * lda + r0 + row] : Sc<S>::zero();
+      }
+    };
+    if (q > 0) load_tile(0);
     // diagonal block into shared memory (used after the contributions)
     for (int e = t; e < 64 * 64; e += 256) {
       const int i = e & 63, j = e >> 6;
@@ -815,12 +832,14 @@ __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int l
       for (int qq = done; qq < end; ++qq) {
         const int jb = LOWER ? qq : nb - 1 - qq;
         const int c0 = jb * 64, wc = min(64, n - c0);
-        if (row < w)
-          for (int c = grp; c < wc; c += 4)
-            acc = Sc<S>::add(acc, Sc<S>::mul(M[(size_t)(c0 + c) * lda + r0 + row], __ldcg(xb + c0 + c)));
+        if (t < 64) xs[t] = t < wc ? __ldcg(xb + c0 + t) : Sc<S>::zero();
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) acc = Sc<S>::add(acc, Sc<S>::mul(mreg[i], xs[grp + 4 * i]));
+        __syncthreads();
+        if (qq + 1 < q) load_tile(qq + 1);
       }
       done = end;
-      __syncthreads();
     }
     part[grp][row] = acc;
     __syncthreads();

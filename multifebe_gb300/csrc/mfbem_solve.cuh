@@ -1349,8 +1349,12 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     stats->refinement_iterations = 0;
   } else {
     // FP32 copy of A, factor
+    // work: d32 [batch][n] (SF), then, from a 256-byte boundary (a real FP32
+    // vector of odd length would leave the doubles misaligned), nrm [batch][8],
+    // rows [batch][n] (double), active [batch] (int)
+    const size_t off_nrm = (sizeof(SF) * (size_t)n * batch + 255) / 256 * 256;
     if ((rc = ensure(h->A32, sizeof(SF) * nn * batch)) || (rc = ensure(h->r, sizeof(SD) * (size_t)n * batch)) ||
-        (rc = ensure(h->work, sizeof(SF) * (size_t)n * batch + sizeof(double) * ((size_t)n * batch + 8 * batch) + 4 * batch)))
+        (rc = ensure(h->work, off_nrm + sizeof(double) * ((size_t)n * batch + 8 * batch) + 4 * batch)))
       return rc;
     MixCtx<SD, SF> c;
     c.h = h;
@@ -1363,7 +1367,7 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     c.x = x;
     c.r = (SD*)h->r.p;
     c.d32 = (SF*)h->work.p;
-    c.nrm = (double*)((char*)h->work.p + sizeof(SF) * (size_t)n * batch);  // [batch][8]: |r|,|x|,|b|,|A|,precond scale
+    c.nrm = (double*)((char*)h->work.p + off_nrm);  // [batch][8]: |r|,|x|,|b|,|A|,precond scale
     double* rows = c.nrm + 8 * batch;
     c.active = (int*)(rows + (size_t)n * batch);
     c.tol = tol;

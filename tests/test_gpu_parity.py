@@ -153,8 +153,13 @@ def test_sweep_matches_oracle_solution(oracle, precision, tol):
     R.close()
 
 
-def test_static_solve_mixed_matches_plain():
-    d = M.cube_clamped_top_traction(4)
+@pytest.mark.parametrize("name,mk", [("cube4", lambda: M.cube_clamped_top_traction(4)),
+                                     ("footing6", lambda: M.halfspace_footing(1.0, 6, 1.0))],
+                         ids=["cube4", "footing6-odd-n"])
+def test_static_solve_mixed_matches_plain(name, mk):
+    """footing6: 399 unknowns, an odd length for the FP32 work vectors of the
+    real mixed path (the doubles after them stay aligned)."""
+    d = mk()
     R = BemRegion(d)
     mat = M.elastic(1.0, 0.25)
     xp = R.solve_staela(mat["mu"], mat["nu"], precision="plain")
