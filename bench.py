@@ -462,9 +462,36 @@ def learned_quadrature():
         if st2["frac_within_1e-7"] >= ref_st["frac_within_1e-7"] and st2["log10_err_p95"] <= ref_st["log10_err_p95"]:
             eq = dict(st2, log10_tol=float(lt), points_vs_reference=st2["points"] / ref_st["points"])
             break
+    # accuracy / cost curves over the slab's pairs: the reference rule at
+    # qsi_relative_error 1e-6 .. 1e-9 and the learned rule at log10 tolerance
+    # -7 .. -10; then, for each reference setting, the cheapest learned
+    # tolerance whose worst pair error and 95th percentile are no larger
+    ref_curve = []
+    for c in range(Q.REF_DEFAULT, min(Q.REF_DEFAULT + 4, Cm.shape[1])):
+        st_c = _pair_stats(Ym[:, c], Cm[:, c], valid)
+        ref_curve.append(dict(st_c, qsi_relative_error=10.0 ** -(3 + c)))
+    learned_curve = []
+    for lt in np.arange(-7.0, -10.01, -0.25):
+        c2 = Q.choose(pred, Cm, lt, fallback=ref_c)
+        learned_curve.append(dict(_pair_stats(Ym[idx, c2], Cm[idx, c2], valid), log10_tol=float(lt)))
+    at_equal = []
+    for rc_ in ref_curve:
+        best = None
+        for lc in learned_curve:
+            if lc["log10_err_max"] <= rc_["log10_err_max"] and lc["log10_err_p95"] <= rc_["log10_err_p95"]:
+                if best is None or lc["points"] < best["points"]:
+                    best = lc
+        at_equal.append({"reference_qsi": rc_["qsi_relative_error"], "reference_points": rc_["points"],
+                         "reference_log10_err_max": rc_["log10_err_max"],
+                         "learned_log10_tol": best["log10_tol"] if best else None,
+                         "learned_points": best["points"] if best else None,
+                         "learned_log10_err_max": best["log10_err_max"] if best else None,
+                         "points_vs_reference": (best["points"] / rc_["points"]) if best else None})
     out["mesh_pairs"] = {
         "adaptive_pairs": int(len(ch)), "labelled_valid": int(valid.sum()),
         "learned_at_equal_accuracy": eq,
+        "reference_curve": ref_curve, "learned_curve": learned_curve,
+        "learned_vs_reference_at_equal_worst_error": at_equal,
         "reference_1e-7": _pair_stats(err_ref, cost_ref, valid),
         "learned_1e-7": _pair_stats(err_l, cost_l, valid),
         "changed_pairs": {"reference_1e-7": _pair_stats(err_ref, cost_ref, changed),
@@ -698,6 +725,18 @@ def profile_patch(precision):
     return 0
 
 
+def profile_static(precision):
+    """ncu case for the static cube (870 DOF): three solves of the given
+    precision (the first loads the kernels)."""
+    from multifebe_gb300 import meshgen as M, BemRegion
+    deck, mat, _ = M.workload(1)
+    R = BemRegion(deck)
+    for _ in range(3):
+        R.solve_staela(mat["mu"], mat["nu"], precision=precision)
+    print(json.dumps(R.last_stats))
+    return 0
+
+
 def _desc_bytes(d, deck):
     ne, nn = deck.n_elements, deck.n_nodes
     return int(ne * (24 + 1 + 4 + 24 + 24 + 16 + 24) * 8 + ne * (8 + 1 + 1) * 4 + nn * (3 + 6 + 3 + 1) * 4 + nn * 6 * 8)
@@ -723,7 +762,11 @@ def main():
                     help="precision of the --profile-case sweeps")
     ap.add_argument("--profile-patch", default="", choices=["", "mixed", "plain"],
                     help="profiling helper: one sweep of the 14883-DOF surface patch, print stats, exit")
+    ap.add_argument("--profile-static", default="", choices=["", "mixed", "plain"],
+                    help="profiling helper: three static solves of the 870-DOF cube, print stats, exit")
     args = ap.parse_args()
+    if args.profile_static:
+        return profile_static(args.profile_static)
     if args.profile_case:
         return profile_case(args.profile_case, args.profile_precision)
     if args.profile_patch:
