@@ -29,7 +29,7 @@
 // 2 x 2 blocks [[re, -im], [im, re]] and B~, C~ the complex arrays viewed as
 // real (as in the TF32 kernel of mfbem_tc.cuh).
 //
-// Kernels: k_oz_split_a / k_oz_split_b compute the scales and write the slices
+// Kernels: k_oz_split (row tiles of A, column tiles of B) computes the scales and writes the slices
 // pre-tiled in the canonical K-major no-swizzle UMMA layout (8-row x 16-byte
 // core matrices), all seven slices of a (tile, K chunk) contiguous, so the
 // GEMM streams one bulk copy of A slices and one of B slices per chunk into a
@@ -104,6 +104,31 @@ __device__ __forceinline__ uint32_t oz_pack(int d0, int d1, int p) {
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
+// Exact conversions to binary64 built with integer instructions: GB300
+// executes about two binary64 operations per cycle per SM, so the epilogue
+// keeps its two FMAs on the FP64 pipe and forms their operands on the
+// integer pipe. |V| < 2^53: the value is representable, no rounding.
+__device__ __forceinline__ double oz_i64_to_f64(long long V) {
+  if (V == 0) return 0.0;
+  const unsigned long long sg = V < 0 ? 0x8000000000000000ULL : 0ULL;
+  const unsigned long long u = V < 0 ? (unsigned long long)(-V) : (unsigned long long)V;
+  const int e = 63 - __clzll(u);  // leading bit, 0..52
+  if (e > 52) return (double)V;   // outside the bound: the hardware conversion
+  const unsigned long long m = u << (52 - e);
+  return __longlong_as_double((long long)(sg | ((unsigned long long)(e + 1023) << 52) | (m & 0xFFFFFFFFFFFFFULL)));
+}
+// binary32 -> binary64 (exact for normal values; zero and subnormal binary32
+// inputs give zero, inf / NaN the hardware conversion)
+__device__ __forceinline__ double oz_f32_to_f64(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned ex = (u >> 23) & 0xFFu;
+  if (ex == 0u) return 0.0;
+  if (ex == 0xFFu) return (double)x;
+  return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                          ((unsigned long long)(ex + 896u) << 52) |
+                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+
 template <bool CPLX> struct OzT;
 template <> struct OzT<true> { typedef double2 S; };
 template <> struct OzT<false> { typedef double S; };
@@ -116,12 +141,12 @@ __device__ __forceinline__ double oz_absmax(double v) { return fabs(v); }
 // slices of every K chunk. Output: tiles [batch][mt][kc][slice][word],
 // exponents erow[batch][nmt * OZ_BM].
 template <bool CPLX>
-__global__ void __launch_bounds__(256) k_oz_split_a(const typename OzT<CPLX>::S* A, int lda, long long sA, int m,
-                                                    int k, int nmt, int nkc, uint32_t* tiles, int* erow) {
+__device__ __forceinline__ void oz_split_a_tile(const typename OzT<CPLX>::S* A, int lda, long long sA, int m, int k,
+                                                int nmt, int nkc, uint32_t* tiles, int* erow, int mt, int b) {
   typedef typename OzT<CPLX>::S S;
   __shared__ double smax[4][OZ_BM];
   __shared__ int se[OZ_BM];
-  const int mt = blockIdx.x, b = blockIdx.y, t = threadIdx.x;
+  const int t = threadIdx.x;
   const S* Ab = A + sA * b;
   // rows of the source matrix in this tile: 64 complex or 128 real
   constexpr int RS = CPLX ? OZ_BM / 2 : OZ_BM;
@@ -188,11 +213,11 @@ __global__ void __launch_bounds__(256) k_oz_split_a(const typename OzT<CPLX>::S*
 // rows of B. One CTA (256 threads) per (column tile, batch). Output: tiles
 // [batch][nt][kc][slice][word], exponents fcol[batch][nnt * OZ_BN].
 template <bool CPLX>
-__global__ void __launch_bounds__(256) k_oz_split_b(const typename OzT<CPLX>::S* B, int ldb, long long sB, int k,
-                                                    int n, int nnt, int nkc, uint32_t* tiles, int* fcol) {
+__device__ __forceinline__ void oz_split_b_tile(const typename OzT<CPLX>::S* B, int ldb, long long sB, int k, int n,
+                                                int nnt, int nkc, uint32_t* tiles, int* fcol, int nt, int b) {
   typedef typename OzT<CPLX>::S S;
   __shared__ int sf[OZ_BN];
-  const int nt = blockIdx.x, b = blockIdx.y, t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const S* Bb = B + sB * b;
   const int j0 = nt * OZ_BN;
   // column scales: a warp per column, lanes along K
@@ -231,6 +256,17 @@ __global__ void __launch_bounds__(256) k_oz_split_b(const typename OzT<CPLX>::S*
       for (int p = 0; p < OZ_S; ++p) dst[(size_t)p * OZ_TWB + w] = oz_pack(d0[p], d1[p], p);
     }
   }
+}
+
+// Both operands' slices in one launch: blocks [0, nmt) split row tiles of A,
+// blocks [nmt, nmt + nnt) column tiles of B (blockIdx.y: the matrix).
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_oz_split(const typename OzT<CPLX>::S* A, int lda, long long sA, int m,
+                                                  const typename OzT<CPLX>::S* B, int ldb, long long sB, int n, int k,
+                                                  int nmt, int nnt, int nkc, uint32_t* at, int* erow, uint32_t* bt,
+                                                  int* fcol) {
+  if ((int)blockIdx.x < nmt) oz_split_a_tile<CPLX>(A, lda, sA, m, k, nmt, nkc, at, erow, blockIdx.x, blockIdx.y);
+  else oz_split_b_tile<CPLX>(B, ldb, sB, k, n, nnt, nkc, bt, fcol, blockIdx.x - nmt, blockIdx.y);
 }
 
 __device__ __forceinline__ uint64_t oz_desc(uint32_t addr) {
@@ -377,7 +413,7 @@ __global__ void __launch_bounds__(128, 1) k_oz_gemm(const uint32_t* At, const ui
           const long long i3 = (long long)__float2int_rn(__uint_as_float(v[3][q]) * 0x1p24f);
           const long long i4 = (long long)__float2int_rn(__uint_as_float(v[4][q]) * 0x1p32f);
           const long long V = (i0 << 32) + (i1 << 24) + (i2 << 16) + (i3 << 8) + i4;
-          const double sum = fma((double)V, 0x1p-32, (double)__uint_as_float(v[5][q]));
+          const double sum = fma(oz_i64_to_f64(V), 0x1p-32, oz_f32_to_f64(__uint_as_float(v[5][q])));
           int s = er + sfc[c0 + q] - 14;
           s = s < -1022 ? -1022 : (s > 1023 ? 1023 : s);
           const double scale = __hiloint2double((s + 1023) << 20, 0);

@@ -183,8 +183,9 @@ static int oz_gemm_run(cudaStream_t st, const typename OzT<CPLX>::S* A, int lda,
   uint32_t* bt = at + wa;
   int* erow = (int*)(bt + wb);
   int* fcol = erow + ne;
-  k_oz_split_a<CPLX><<<dim3(nmt, batch), 256, 0, st>>>(A, lda, sA, m, k, nmt, nkc, at, erow); ++g_launches;
-  k_oz_split_b<CPLX><<<dim3(nnt, batch), 256, 0, st>>>(B, ldb, sB, k, n, nnt, nkc, bt, fcol); ++g_launches;
+  k_oz_split<CPLX><<<dim3(nmt + nnt, batch), 256, 0, st>>>(A, lda, sA, m, B, ldb, sB, n, k, nmt, nnt, nkc, at, erow,
+                                                            bt, fcol);
+  ++g_launches;
   k_oz_gemm<<<dim3(nmt, nnt, batch), 128, OZ_SMEM, st>>>(at, bt, erow, fcol, nmt, nnt, nkc, (double*)C,
                                                         (long long)W * ldc, (long long)W * sC, mr, n,
                                                         (int*)g_oz_err.p, g_spin_limit.load());
