@@ -56,14 +56,15 @@ FLOPS_PER_REGULAR_POINT = 1280
 # formulation of the same kernel could at best run at this rate
 FP64_NOMINAL_TFLOPS = 1.25
 # DRAM bytes per frequency of that kernel from ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum of one launch of the 2-frequency profile case, 454.1 +
-# 408.1 MB, divided by 2; profiles/k_mixed_cube8x2freq.md). Traffic grows in
+# dram__bytes_write.sum of one launch of the 2-frequency profile case, 454.5 +
+# 393.5 MB, divided by 2; profiles/k_mixed_cube8x2freq.md): A written once
+# and read back once (the flush adds into the zeroed system). Traffic grows in
 # proportion to the frequencies (one system per frequency).
-REG_TRAFFIC_PER_FREQ = 431.1e6
+REG_TRAFFIC_PER_FREQ = 424.0e6
 # Pipe utilisation of the same launch (ncu --set full, same small case and
 # file): the kernel is bound by instruction issue on the FP32 pipe
 # (double-float arithmetic), not by HBM.
-REG_NCU_PIPES = {"issue_slots_busy_pct": 61.2, "fp32_fma_pipe_pct": 44.3, "fp64_pipe_pct": 3.1,
+REG_NCU_PIPES = {"issue_slots_busy_pct": 60.0, "fp32_fma_pipe_pct": 42.5, "fp64_pipe_pct": 21.6,
                  "source": "profiles/k_mixed_cube8x2freq.md"}
 
 

@@ -765,6 +765,30 @@ __device__ __forceinline__ int ld_acquire_s32(const int* p) {
   asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+// Loads of the factors issued where they stand in the program: the
+// prefetch of the next solved block's tile must leave before the wait on
+// that block's flag (a plain load may be scheduled next to its first use,
+// behind the wait). The factors are read-only during the solve.
+__device__ __forceinline__ float ld_pinned(const float* p) {
+  float v;
+  asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double ld_pinned(const double* p) {
+  double v;
+  asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float2 ld_pinned(const float2* p) {
+  float2 v;
+  asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double2 ld_pinned(const double2* p) {
+  double2 v;
+  asm volatile("ld.global.nc.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+  return v;
+}
 template <typename S, bool LOWER>
 __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int lda, int n, S* x, long long sx,
                                                  int batch, int nb, unsigned* counter, int* ready, int* err,
@@ -799,7 +823,7 @@ __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int l
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const int c = grp + 4 * i;
-        mreg[i] = (row < w && c < wc) ? M[(size_t)(c0 + c) * lda + r0 + row] : Sc<S>::zero();
+        mreg[i] = (row < w && c < wc) ? ld_pinned(M + (size_t)(c0 + c) * lda + r0 + row) : Sc<S>::zero();
       }
     };
     if (q > 0) load_tile(0);

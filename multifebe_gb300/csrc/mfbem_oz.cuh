@@ -104,31 +104,6 @@ __device__ __forceinline__ uint32_t oz_pack(int d0, int d1, int p) {
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
-// Exact conversions to binary64 built with integer instructions: GB300
-// executes about two binary64 operations per cycle per SM, so the epilogue
-// keeps its two FMAs on the FP64 pipe and forms their operands on the
-// integer pipe. |V| < 2^53: the value is representable, no rounding.
-__device__ __forceinline__ double oz_i64_to_f64(long long V) {
-  if (V == 0) return 0.0;
-  const unsigned long long sg = V < 0 ? 0x8000000000000000ULL : 0ULL;
-  const unsigned long long u = V < 0 ? (unsigned long long)(-V) : (unsigned long long)V;
-  const int e = 63 - __clzll(u);  // leading bit, 0..52
-  if (e > 52) return (double)V;   // outside the bound: the hardware conversion
-  const unsigned long long m = u << (52 - e);
-  return __longlong_as_double((long long)(sg | ((unsigned long long)(e + 1023) << 52) | (m & 0xFFFFFFFFFFFFFULL)));
-}
-// binary32 -> binary64 (exact for normal values; zero and subnormal binary32
-// inputs give zero, inf / NaN the hardware conversion)
-__device__ __forceinline__ double oz_f32_to_f64(float x) {
-  const unsigned u = __float_as_uint(x);
-  const unsigned ex = (u >> 23) & 0xFFu;
-  if (ex == 0u) return 0.0;
-  if (ex == 0xFFu) return (double)x;
-  return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
-                                          ((unsigned long long)(ex + 896u) << 52) |
-                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
-}
-
 template <bool CPLX> struct OzT;
 template <> struct OzT<true> { typedef double2 S; };
 template <> struct OzT<false> { typedef double S; };
@@ -413,7 +388,7 @@ __global__ void __launch_bounds__(128, 1) k_oz_gemm(const uint32_t* At, const ui
           const long long i3 = (long long)__float2int_rn(__uint_as_float(v[3][q]) * 0x1p24f);
           const long long i4 = (long long)__float2int_rn(__uint_as_float(v[4][q]) * 0x1p32f);
           const long long V = (i0 << 32) + (i1 << 24) + (i2 << 16) + (i3 << 8) + i4;
-          const double sum = fma(oz_i64_to_f64(V), 0x1p-32, oz_f32_to_f64(__uint_as_float(v[5][q])));
+          const double sum = fma((double)V, 0x1p-32, (double)__uint_as_float(v[5][q]));
           int s = er + sfc[c0 + q] - 14;
           s = s < -1022 ? -1022 : (s > 1023 ? 1023 : s);
           const double scale = __hiloint2double((s + 1023) << 20, 0);
