@@ -475,6 +475,14 @@ def learned_quadrature():
     for lt in np.arange(-7.0, -10.01, -0.25):
         c2 = Q.choose(pred, Cm, lt, fallback=ref_c)
         learned_curve.append(dict(_pair_stats(Ym[idx, c2], Cm[idx, c2], valid), log10_tol=float(lt)))
+    # the same selection with the true labels instead of the network's
+    # predictions: the cheapest candidate per pair whose converged-integral
+    # error meets the tolerance -- the best any predictor of this candidate
+    # set can do
+    label_curve = []
+    for lt in np.arange(-6.0, -9.01, -0.25):
+        c3 = Q.choose(Ym, Cm, lt, fallback=ref_c)
+        label_curve.append(dict(_pair_stats(Ym[idx, c3], Cm[idx, c3], valid), log10_tol=float(lt)))
     at_equal = []
     for rc_ in ref_curve:
         best = None
@@ -482,7 +490,12 @@ def learned_quadrature():
             if lc["log10_err_max"] <= rc_["log10_err_max"] and lc["log10_err_p95"] <= rc_["log10_err_p95"]:
                 if best is None or lc["points"] < best["points"]:
                     best = lc
+        bl = None
+        for lc in label_curve:
+            if lc["log10_err_max"] <= rc_["log10_err_max"] and (bl is None or lc["points"] < bl["points"]):
+                bl = lc
         at_equal.append({"reference_qsi": rc_["qsi_relative_error"], "reference_points": rc_["points"],
+                         "true_label_choice_points": bl["points"] if bl else None,
                          "reference_log10_err_max": rc_["log10_err_max"],
                          "learned_log10_tol": best["log10_tol"] if best else None,
                          "learned_points": best["points"] if best else None,
@@ -491,7 +504,7 @@ def learned_quadrature():
     out["mesh_pairs"] = {
         "adaptive_pairs": int(len(ch)), "labelled_valid": int(valid.sum()),
         "learned_at_equal_accuracy": eq,
-        "reference_curve": ref_curve, "learned_curve": learned_curve,
+        "reference_curve": ref_curve, "learned_curve": learned_curve, "true_label_curve": label_curve,
         "learned_vs_reference_at_equal_worst_error": at_equal,
         "reference_1e-7": _pair_stats(err_ref, cost_ref, valid),
         "learned_1e-7": _pair_stats(err_l, cost_l, valid),
@@ -704,24 +717,38 @@ def configs_form():
     return out
 
 
+def _profiler(on):
+    """cuProfilerStart / cuProfilerStop (driver API): with `ncu
+    --profile-from-start off` only the launches between the two are captured."""
+    lib = ctypes.CDLL("libcuda.so.1")
+    return (lib.cuProfilerStart if on else lib.cuProfilerStop)()
+
+
 def profile_case(nf, precision="mixed"):
     """Small fixed case for ncu captures: the benchmark mesh, nf frequencies,
-    two sweeps of the given precision."""
+    two sweeps of the given precision (the second one between
+    cuProfilerStart / cuProfilerStop)."""
     from multifebe_gb300 import meshgen as M, BemRegion
     deck, mat, om = M.workload(2)
     R = BemRegion(deck)
-    for _ in range(2):
-        R.sweep_harela(mat, om[:nf], precision=precision)
+    R.sweep_harela(mat, om[:nf], precision=precision)
+    _profiler(True)
+    R.sweep_harela(mat, om[:nf], precision=precision)
+    _profiler(False)
     print(json.dumps(R.last_stats))
     return 0
 
 
 def profile_patch(precision):
-    """ncu case for the 14883-DOF surface patch: one sweep at a0=0.5."""
+    """ncu case for the 14883-DOF surface patch: two sweeps at a0=0.5, the
+    second between cuProfilerStart / cuProfilerStop."""
     from multifebe_gb300 import meshgen as M, BemRegion
     deck, mat, om = M.workload(3)
     R = BemRegion(deck)
     R.sweep_harela(mat, om, precision=precision)
+    _profiler(True)
+    R.sweep_harela(mat, om, precision=precision)
+    _profiler(False)
     print(json.dumps(R.last_stats))
     return 0
 

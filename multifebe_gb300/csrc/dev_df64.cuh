@@ -10,7 +10,6 @@
 // accuracy target is absolute with respect to the summands.
 #pragma once
 #include <cuda_runtime.h>
-#include "dev_cvt.cuh"
 
 namespace mfb {
 
@@ -26,7 +25,7 @@ __device__ __forceinline__ ff ff_from(double x) {
   float l = __double2float_rn(x - (double)h);
   return ff{h, l};
 }
-__device__ __forceinline__ double ff_to(ff a) { return f32_to_f64_exact(a.hi) + f32_to_f64_exact(a.lo); }
+__device__ __forceinline__ double ff_to(ff a) { return (double)a.hi + (double)a.lo; }
 __device__ __forceinline__ ff ff_zero() { return ff{0.0f, 0.0f}; }
 
 // a + b

@@ -208,11 +208,18 @@ static int oz_err_check(cudaStream_t st) {
   return 0;
 }
 
+// Below this many real multiply-adds an update goes to the binary64 SIMT
+// kernel even in mode 0: the Ozaki path's fixed cost (operand split, TMEM
+// allocation, binary64 epilogue; about 30-40 µs) exceeds the SIMT kernel's
+// time there (small static systems, the depth-16 updates inside an outer block).
+constexpr double kOzMinMacs = 16777216.0;  // 2^24
 template <typename S>
 static int f64_gemm(cudaStream_t st, int m, int n, int k, const S* A, int lda, long long sA, const S* B, int ldb,
                     long long sB, S* C, int ldc, long long sC, int batch) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
-  if (f64_default() == 1) return gemm_simt<S>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
+  const double macs = (double)m * n * k * batch * (std::is_same<S, double2>::value ? 4.0 : 1.0);
+  if (f64_default() == 1 || macs < kOzMinMacs)
+    return gemm_simt<S>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
   return oz_gemm_run<std::is_same<S, double2>::value>(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch);
 }
 // smallest depth of a complex update that goes to the tensor cores (32: the
@@ -440,7 +447,8 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
     const int nc = c1 - c0;
     if (nc <= 0) return 0;
     if constexpr (IsF64<S>::v) {
-      if (oz && nc >= 128) {
+      const double macs = (double)kb * kb * nc * batch * (std::is_same<S, double2>::value ? 4.0 : 1.0);
+      if (oz && nc >= 128 && macs >= kOzMinMacs / 4) {
         const size_t tb = sizeof(S) * 1024 * (size_t)batch, wb = sizeof(S) * (size_t)kb * nc * batch;
         int rc = ensure(g_trsm_ws, tb + wb);
         if (rc) return rc;
