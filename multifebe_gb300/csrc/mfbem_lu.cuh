@@ -758,7 +758,7 @@ __global__ void __launch_bounds__(128) k_trsm_runp(S* A, long long sA, int lda, 
 constexpr long long kTrsvSpin = 1LL << 22;
 template <typename S>
 constexpr size_t trsv_sf_smem() {
-  return sizeof(S) * (64 * 65 + 4 * 64 + 64);
+  return sizeof(S) * (64 * 65 + 4 * 64 + 64 + 64);
 }
 __device__ __forceinline__ int ld_acquire_s32(const int* p) {
   int v;
@@ -794,11 +794,13 @@ __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int l
                                                  int batch, int nb, unsigned* counter, int* ready, int* err,
                                                  long long spin) {
   // dynamic shared memory: D [64 x 65] (diagonal block, column-major), part [4][64],
-  // xs [64] (the solved block being applied)
+  // xs [64] (the solved block being applied), rinv [64] (reciprocals of U's
+  // diagonal, formed before the wait so that no division lies on the chain)
   extern __shared__ __align__(16) unsigned char sfraw[];
   S* D = reinterpret_cast<S*>(sfraw);
   S (*part)[64] = reinterpret_cast<S (*)[64]>(D + 64 * 65);
   S* xs = D + 64 * 65 + 4 * 64;
+  S* rinv = xs + 64;
   __shared__ int s_item, s_end;
   const int t = threadIdx.x, row = t & 63, grp = t >> 6;
   const long long lim = spin > 0 ? spin : kTrsvSpin;
@@ -832,6 +834,7 @@ __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int l
       const int i = e & 63, j = e >> 6;
       if (i < w && j < w) D[j * 65 + i] = M[(size_t)(r0 + j) * lda + r0 + i];
     }
+    if (!LOWER && t < w) rinv[t] = Sc<S>::rcp(M[(size_t)(r0 + t) * lda + r0 + t]);
     // contributions of the solved blocks, in the order they were solved:
     // thread 0 waits for the next one, then takes every later one already
     // published too, so a CTA that is behind catches up with one barrier
@@ -882,8 +885,8 @@ __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int l
         }
       } else {
         for (int j = w - 1; j >= 0; --j) {
-          if (j < 32) { if (l == j) x0 = Sc<S>::div(x0, D[j * 65 + j]); }
-          else { if (l + 32 == j) x1 = Sc<S>::div(x1, D[j * 65 + j]); }
+          if (j < 32) { if (l == j) x0 = Sc<S>::mul(x0, rinv[j]); }
+          else { if (l + 32 == j) x1 = Sc<S>::mul(x1, rinv[j]); }
           const S xj = shfl_s(j < 32 ? x0 : x1, j & 31);
           if (l < j) x0 = Sc<S>::sub(x0, Sc<S>::mul(D[j * 65 + l], xj));
           if (l + 32 < j) x1 = Sc<S>::sub(x1, Sc<S>::mul(D[j * 65 + l + 32], xj));
