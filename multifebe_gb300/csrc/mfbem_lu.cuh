@@ -584,9 +584,23 @@ __global__ void __launch_bounds__(trsm_cols<S>()) k_trsm_cols(S* A, long long st
   const int c = threadIdx.x;
   if (c < ncol) {
     S* x = T + c * 33;
-    for (int jj = 0; jj < w; ++jj) {
-      const S xj = x[jj];
-      for (int i = jj + 1; i < w; ++i) x[i] = Sc<S>::sub(x[i], Sc<S>::mul(L[jj * w + i], xj));
+    if (w == 32) {
+      // full panel width: the column in registers, the substitution unrolled
+      // (L read from shared memory as a broadcast, no read-modify-write of x)
+      S xr[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) xr[i] = x[i];
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj)
+#pragma unroll
+        for (int i = jj + 1; i < 32; ++i) xr[i] = Sc<S>::sub(xr[i], Sc<S>::mul(L[jj * 32 + i], xr[jj]));
+#pragma unroll
+      for (int i = 0; i < 32; ++i) x[i] = xr[i];
+    } else {
+      for (int jj = 0; jj < w; ++jj) {
+        const S xj = x[jj];
+        for (int i = jj + 1; i < w; ++i) x[i] = Sc<S>::sub(x[i], Sc<S>::mul(L[jj * w + i], xj));
+      }
     }
   }
   __syncthreads();
@@ -708,17 +722,55 @@ __global__ void __launch_bounds__(256) k_diag_lu_nopiv(S* A, long long sA, int l
     M[(size_t)(k + c) * lda + k + i] = D[c * 33 + i];
   }
 }
+// The same factorisation by one warp with the block in registers: lane i
+// holds row i, the pivot row's entries reach the other lanes by shuffles, so
+// no block-wide barrier lies between two columns (the kernel is on the
+// factorisation's critical path once per inner panel).
+template <typename S>
+__global__ void __launch_bounds__(32) k_diag_lu_nopiv_warp(S* A, long long sA, int lda, int k, int kb, int* info) {
+  const int b = blockIdx.x, i = threadIdx.x;
+  S* M = A + sA * b;
+  S a[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) a[c] = (i < kb && c < kb) ? M[(size_t)(k + c) * lda + k + i] : Sc<S>::zero();
+  bool bad = false;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    if (j < kb && !bad) {
+      const S d = shfl_s(a[j], j);
+      const float m = (float)Sc<S>::abs1(d);
+      if (!(m > 0.0f) || !isfinite(m)) {
+        bad = true;
+        if (i == 0 && info[b] == 0) info[b] = k + j + 1;
+      } else {
+        const S rcp = Sc<S>::rcp(d);
+        const S l = Sc<S>::mul(a[j], rcp);
+        if (i > j) a[j] = l;
+#pragma unroll
+        for (int c = j + 1; c < 32; ++c) {
+          const S u = shfl_s(a[c], j);
+          if (i > j) a[c] = Sc<S>::sub(a[c], Sc<S>::mul(l, u));
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 32; ++c)
+    if (i < kb && c < kb) M[(size_t)(k + c) * lda + k + i] = a[c];
+}
 // rows [r0, r1) of columns [k, k + kb): X := X inv(U11), U11 the upper
 // triangle (with its diagonal) of the factorised diagonal block; one thread per row
 template <typename S>
 __global__ void __launch_bounds__(128) k_trsm_runp(S* A, long long sA, int lda, int k, int kb, int r0, int r1) {
   __shared__ S U[32 * 33];
+  __shared__ S ur[32];  // reciprocals of U11's diagonal: the row chains multiply, no division
   const int b = blockIdx.y, t = threadIdx.x;
   S* M = A + sA * b;
   for (int e = t; e < kb * kb; e += 128) {
     const int i = e % kb, c = e / kb;
     if (i <= c) U[c * 33 + i] = M[(size_t)(k + c) * lda + k + i];
   }
+  if (t < kb) ur[t] = Sc<S>::rcp(M[(size_t)(k + t) * lda + k + t]);
   __syncthreads();
   const int row = r0 + blockIdx.x * 128 + t;
   if (row >= r1) return;
@@ -732,7 +784,7 @@ __global__ void __launch_bounds__(128) k_trsm_runp(S* A, long long sA, int lda, 
       S v = x[j];
 #pragma unroll
       for (int c = 0; c < j; ++c) v = Sc<S>::sub(v, Sc<S>::mul(x[c], U[j * 33 + c]));
-      x[j] = Sc<S>::div(v, U[j * 33 + j]);
+      x[j] = Sc<S>::mul(v, ur[j]);
     }
   }
 #pragma unroll
