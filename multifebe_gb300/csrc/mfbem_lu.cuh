@@ -722,42 +722,6 @@ __global__ void __launch_bounds__(256) k_diag_lu_nopiv(S* A, long long sA, int l
     M[(size_t)(k + c) * lda + k + i] = D[c * 33 + i];
   }
 }
-// The same factorisation by one warp with the block in registers: lane i
-// holds row i, the pivot row's entries reach the other lanes by shuffles, so
-// no block-wide barrier lies between two columns (the kernel is on the
-// factorisation's critical path once per inner panel).
-template <typename S>
-__global__ void __launch_bounds__(32) k_diag_lu_nopiv_warp(S* A, long long sA, int lda, int k, int kb, int* info) {
-  const int b = blockIdx.x, i = threadIdx.x;
-  S* M = A + sA * b;
-  S a[32];
-#pragma unroll
-  for (int c = 0; c < 32; ++c) a[c] = (i < kb && c < kb) ? M[(size_t)(k + c) * lda + k + i] : Sc<S>::zero();
-  bool bad = false;
-#pragma unroll
-  for (int j = 0; j < 32; ++j) {
-    if (j < kb && !bad) {
-      const S d = shfl_s(a[j], j);
-      const float m = (float)Sc<S>::abs1(d);
-      if (!(m > 0.0f) || !isfinite(m)) {
-        bad = true;
-        if (i == 0 && info[b] == 0) info[b] = k + j + 1;
-      } else {
-        const S rcp = Sc<S>::rcp(d);
-        const S l = Sc<S>::mul(a[j], rcp);
-        if (i > j) a[j] = l;
-#pragma unroll
-        for (int c = j + 1; c < 32; ++c) {
-          const S u = shfl_s(a[c], j);
-          if (i > j) a[c] = Sc<S>::sub(a[c], Sc<S>::mul(l, u));
-        }
-      }
-    }
-  }
-#pragma unroll
-  for (int c = 0; c < 32; ++c)
-    if (i < kb && c < kb) M[(size_t)(k + c) * lda + k + i] = a[c];
-}
 // rows [r0, r1) of columns [k, k + kb): X := X inv(U11), U11 the upper
 // triangle (with its diagonal) of the factorised diagonal block; one thread per row
 template <typename S>

@@ -475,7 +475,7 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
     for (int k = K; k < KE; k += nb) {
       const int kb = std::min(nb, KE - k);
       if (nopiv) {
-        k_diag_lu_nopiv_warp<S><<<batch, 32, 0, st>>>(A, sA, lda, k, kb, info); ++g_launches;
+        k_diag_lu_nopiv<S><<<batch, 256, 0, st>>>(A, sA, lda, k, kb, info); ++g_launches;
         if (k + kb < n) {
           k_trsm_runp<S><<<dim3(nblk(n - k - kb, 128), batch), 128, 0, st>>>(A, sA, lda, k, kb, k + kb, n);
           ++g_launches;
