@@ -222,11 +222,14 @@ static int f64_gemm(cudaStream_t st, int m, int n, int k, const S* A, int lda, l
     return gemm_simt<S>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
   return oz_gemm_run<std::is_same<S, double2>::value>(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch);
 }
-// smallest depth of a complex update that goes to the tensor cores (32: the
-// updates inside an outer block too; MFBEM_TC_MIN_K overrides)
-static int tc_min_depth() {
+// smallest depth of a complex update that goes to the tensor cores: 32 (the
+// updates inside an outer block too) for a batch of systems, 64 for a single
+// system, whose depth-32 updates ran faster on the SIMT kernel (88.8 against
+// 91.4 ms for the factorisation of one 14883-row system); MFBEM_TC_MIN_K
+// overrides
+static int tc_min_depth(int batch) {
   const char* e = getenv("MFBEM_TC_MIN_K");
-  return e ? std::max(1, atoi(e)) : 32;
+  return e ? std::max(1, atoi(e)) : (batch > 1 ? 32 : 64);
 }
 // C -= A B (batched) in the scalar type of the factorisation, as configured
 // above: FP64 (plain LU) or FP32 (mixed LU)
@@ -245,7 +248,7 @@ static int gemm_sb(cudaStream_t st, int m, int n, int k, const float* A, int lda
 static int gemm_sb(cudaStream_t st, int m, int n, int k, const float2* A, int lda, long long sA, const float2* B,
                    int ldb, long long sB, float2* C, int ldc, long long sC, int batch) {
   const int mode = g_c32_mode;
-  if ((mode == 3 || mode == 1) && g_tc_err.p && k >= tc_min_depth())
+  if ((mode == 3 || mode == 1) && g_tc_err.p && k >= tc_min_depth(batch))
     return tc_cgemm_run(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch, g_tc_ws, (int*)g_tc_err.p,
                         mode == 3 ? 3 : 1);
   return gemm_simt<float2>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);

@@ -68,6 +68,12 @@ def lib():
         L.orc_hsc_point.argtypes = [ctypes.c_double] * 3 + [_dp] * 5
         L.orc_pair_hsc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    _dp, _dp]
+        L.orc_problem_set_formulation.argtypes = [ctypes.c_void_p, _ip, _dp, _dp]
+        L.orc_colloc_normals.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_pair_hbie_staela.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_double, _dp, _dp]
+        L.orc_pair_hbie_harela.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6 + \
+            [_dp, _dp]
         _lib = L
     return _lib
 
@@ -137,13 +143,54 @@ class Problem:
     _ERR = {-1: "invalid normals/tangents configuration at a free-term node",
             -2: "a point lies outside the half-space",
             -3: "an element containing a collocation point on the free surface does not lie on it",
-            -4: "the static half-space kernel needs the hyperplane normal n = -3"}
+            -4: "the static half-space kernel needs the hyperplane normal n = -3",
+            -5: "HBIE formulations in a half-space region are not available",
+            -6: "the HBIE cannot be collocated at an element edge"}
+
+    FORMULATIONS = {"sbie": 0, "hbie": 1, "dual_bm": 2}
+
+    def set_formulation(self, form, alpha=None, delta=None):
+        """BEM formulation of every node (src/read_bem_formulation_selected_nodes.f90):
+        form is one name of FORMULATIONS for all nodes or an array of codes per
+        node (0 default SBIE, 1 'hbie', 2 'dual_bm_same'); alpha (Burton &
+        Miller weight) and delta (HBIE point offset, default 0.22540333) per
+        node or scalar. Rebuilds the collocation points."""
+        nn = self.deck.n_nodes
+        f = np.full(nn, self.FORMULATIONS[form], dtype=np.int32) if isinstance(form, str) else \
+            np.ascontiguousarray(form, dtype=np.int32)
+        a = np.ascontiguousarray(np.broadcast_to(1.0 if alpha is None else alpha, (nn,)), dtype=np.float64)
+        dl = np.ascontiguousarray(np.broadcast_to(0.22540333 if delta is None else delta, (nn,)), dtype=np.float64)
+        if lib().orc_problem_set_formulation(self._h, _p(f, _ip), _p(a), _p(dl)) != 0:
+            raise ValueError("formulation codes must be 0, 1 or 2")
+
+    def colloc_normals(self):
+        m = lib().orc_n_colloc(self._h)
+        nrm = np.zeros((m, 3))
+        lib().orc_colloc_normals(self._h, _p(nrm))
+        return nrm
+
+    def pair_hbie(self, ci, e, mu=None, nu=None, mat=None, omega=None):
+        """HBIE kernels (m, l [8, 3, 3]) of collocation point ci against element
+        e: static with mu, nu, harmonic with mat, omega."""
+        cplx = omega is not None
+        dt = np.complex128 if cplx else np.float64
+        m = np.zeros((8, 3, 3), dtype=dt)
+        l = np.zeros((8, 3, 3), dtype=dt)
+        if cplx:
+            lam, mu_ = complex(mat["lambda"]), complex(mat["mu"])
+            cls = lib().orc_pair_hbie_harela(self._h, ci, e, lam.real, lam.imag, mu_.real, mu_.imag,
+                                             float(mat["rho"]), float(omega), _p(m), _p(l))
+        else:
+            cls = lib().orc_pair_hbie_staela(self._h, ci, e, float(mu), float(nu), _p(m), _p(l))
+        if cls < 0:
+            raise RuntimeError("oracle: " + self._ERR.get(cls, str(cls)))
+        return cls, m, l
 
     def assemble_staela(self, mu, nu, nthreads=0):
         n = self.n
         A = np.zeros((n, n), dtype=np.float64, order="F")
         b = np.zeros(n, dtype=np.float64)
-        st = np.zeros(8, dtype=np.int64)
+        st = np.zeros(12, dtype=np.int64)
         rc = lib().orc_assemble_staela(self._h, mu, nu, _p(A), _p(b), nthreads, _p(st, _lp))
         if rc != 0:
             raise RuntimeError("oracle: " + self._ERR.get(rc, str(rc)))
@@ -162,12 +209,12 @@ class Problem:
         n = self.n
         A = np.zeros((n, n), dtype=np.complex128, order="F")
         b = np.zeros(n, dtype=np.complex128)
-        st = np.zeros(8, dtype=np.int64)
+        st = np.zeros(12, dtype=np.int64)
         lam, mu, nu = complex(mat["lambda"]), complex(mat["mu"]), complex(mat["nu"])
         rc = lib().orc_assemble_harela_nu(self._h, lam.real, lam.imag, mu.real, mu.imag, float(mat["rho"]),
                                           float(omega), nu.real, nu.imag, _p(A), _p(b), nthreads, _p(st, _lp))
         if rc != 0:
-            raise RuntimeError("oracle: invalid normals/tangents configuration at a free-term node")
+            raise RuntimeError("oracle: " + self._ERR.get(rc, str(rc)))
         self.stats = st
         return A, b
 

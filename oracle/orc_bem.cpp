@@ -835,13 +835,427 @@ static int sbie_auto(const K& k, const Elem& e, bool reverse, const double x_i[3
   return CLS_ADP;
 }
 
-// hbie_auto for a point off the element (bem_staela3d.f90:4307-4373 /
-// the harmonic twin): the same classification with the 1/r^7 estimate. A
-// point on the element (d <= 1e-12) would need hbie_int; it returns CLS_SING
-// with zero kernels, and internal points never reach it (see internal_points).
+// ---------------------------------------------------------------------------
+// HBIE interior integration: the collocation point lies inside the element
+// (never at an edge: the HBIE is collocated at non-nodal points). Polar
+// integration of the regularised integrands around xi_i plus line integrals
+// over the four edges for the parts reduced by Stokes' theorem.
+// Static: fbem_bem_staela3d_hbie_int (bem_staela3d.f90:4918-5353);
+// harmonic: fbem_bem_harela3d_hbie_int (bem_harela3d.f90:3169-3630).
+// HG<K>.h receives m (integrated with phi^p), HG<K>.g receives l (phi^s).
+// ---------------------------------------------------------------------------
+static thread_local int g_hbie_err = 0;  // 1: an HBIE collocation point at an element edge
+
+struct HbieLi {
+  double lli[3][3], mli1, mli2[3], mli3[3][3], mli4[3], mli5[3][3][3];
+  void zero() { std::memset(this, 0, sizeof(*this)); }
+};
+
+// fbem_bem_staela3d_hbie_int_li (bem_staela3d.f90:5356-5578): all line
+// integrals of one line3 edge, adaptive Telles + bisection, 1/r^2 estimate
+static void hbie_int_li(const double xn[3][3], double xi_s[2], const double x_i[3], const double n_i[3], int ngp_min,
+                        const QsParams& qsp, int ks, int ns, HbieLi& L) {
+  double x_s[3][3];
+  if (ks == 1) {
+    xi_s[0] = -1.0;
+    xi_s[1] = 1.0;
+    std::memcpy(x_s, xn, sizeof(x_s));
+  } else {
+    subdivision_coords_line3(xn, xi_s, x_s);
+  }
+  double cl = characteristic_length_line3(x_s, 1e-12);
+  double barxip, rmin, d;
+  int method;
+  nearest_element_point_line3(x_s, cl, x_i, &barxip, &rmin, &d, &method);
+  int gln_near = qs_n_estimation_telles(1, 2, qsp, d, &barxip);
+  bool subdivide = false;
+  if (ks == ns) {
+    if (gln_near == 0) gln_near = 30;
+  } else if (gln_near == 0) {
+    subdivide = true;
+  }
+  if (subdivide) {
+    double t[2];
+    t[0] = xi_s[0]; t[1] = 0.5 * (xi_s[0] + xi_s[1]);
+    hbie_int_li(xn, t, x_i, n_i, ngp_min, qsp, ks + 1, ns, L);
+    t[0] = 0.5 * (xi_s[0] + xi_s[1]); t[1] = xi_s[1];
+    hbie_int_li(xn, t, x_i, n_i, ngp_min, qsp, ks + 1, ns, L);
+    return;
+  }
+  HbieLi T;
+  T.zero();
+  int gln = std::max(gln_near, ngp_min);
+  Telles tp = telles11(barxip, telles_barr_any(d));
+  for (int kip = 1; kip <= gln; ++kip) {
+    double gm = gl11_xi(kip, gln), w = gl11_w(kip, gln);
+    double xip, jt;
+    telles_xi_jac(tp, gm, xip, jt);
+    double xi = 0.5 * (1.0 - xip) * xi_s[0] + 0.5 * (1.0 + xip) * xi_s[1];
+    double js = 0.5 * (xi_s[1] - xi_s[0]);
+    double phi[3], dphi[3];
+    phi_line3(xi, phi);
+    dphi_line3(xi, dphi);
+    double x[3] = {0, 0, 0}, Tg[3] = {0, 0, 0};
+    for (int q = 0; q < 3; ++q)
+      for (int c = 0; c < 3; ++c) {
+        x[c] = x[c] + phi[q] * xn[q][c];
+        Tg[c] = Tg[c] + dphi[q] * xn[q][c];
+      }
+    double jg = std::sqrt(Tg[0] * Tg[0] + Tg[1] * Tg[1] + Tg[2] * Tg[2]);
+    double t[3] = {Tg[0] / jg, Tg[1] / jg, Tg[2] / jg};
+    double rv[3] = {x[0] - x_i[0], x[1] - x_i[1], x[2] - x_i[2]};
+    double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    double dr1 = 1.0 / r, dr3 = 1.0 / (r * r * r);
+    double drdx[3] = {rv[0] * dr1, rv[1] * dr1, rv[2] * dr1};
+    double jw = jg * js * jt * w;
+    T.lli[0][1] = T.lli[0][1] - dr1 * t[2] * jw;
+    T.lli[0][2] = T.lli[0][2] + dr1 * t[1] * jw;
+    T.lli[1][2] = T.lli[1][2] - dr1 * t[0] * jw;
+    double rxni[3] = {rv[1] * n_i[2] - rv[2] * n_i[1], rv[2] * n_i[0] - rv[0] * n_i[2], rv[0] * n_i[1] - rv[1] * n_i[0]};
+    double rxnit = rxni[0] * t[0] + rxni[1] * t[1] + rxni[2] * t[2];
+    T.mli1 = T.mli1 + dr3 * rxnit * jw;
+    for (int a = 0; a < 3; ++a)
+      for (int b = a; b < 3; ++b) T.mli3[a][b] = T.mli3[a][b] + dr3 * rxnit * drdx[a] * drdx[b] * jw;
+    for (int ik = 0; ik < 3; ++ik) {
+      double ek[3] = {0, 0, 0};
+      ek[ik] = 1.0;
+      double ekxni[3] = {ek[1] * n_i[2] - ek[2] * n_i[1], ek[2] * n_i[0] - ek[0] * n_i[2],
+                         ek[0] * n_i[1] - ek[1] * n_i[0]};
+      double ekxnit = ekxni[0] * t[0] + ekxni[1] * t[1] + ekxni[2] * t[2];
+      double rxek[3] = {rv[1] * ek[2] - rv[2] * ek[1], rv[2] * ek[0] - rv[0] * ek[2], rv[0] * ek[1] - rv[1] * ek[0]};
+      double rxekt = rxek[0] * t[0] + rxek[1] * t[1] + rxek[2] * t[2];
+      T.mli2[ik] = T.mli2[ik] + dr1 * ekxnit * jw;
+      T.mli4[ik] = T.mli4[ik] + dr3 * rxekt * jw;
+      for (int a = 0; a < 3; ++a)
+        for (int b = a; b < 3; ++b) T.mli5[a][b][ik] = T.mli5[a][b][ik] + dr1 * ekxnit * drdx[a] * drdx[b] * jw;
+    }
+  }
+  T.lli[1][0] = -T.lli[0][1];
+  T.lli[2][0] = -T.lli[0][2];
+  T.lli[2][1] = -T.lli[1][2];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < a; ++b) {
+      T.mli3[a][b] = T.mli3[b][a];
+      for (int k = 0; k < 3; ++k) T.mli5[a][b][k] = T.mli5[b][a][k];
+    }
+  for (int a = 0; a < 3; ++a) {
+    L.mli2[a] = L.mli2[a] + T.mli2[a];
+    L.mli4[a] = L.mli4[a] + T.mli4[a];
+    for (int b = 0; b < 3; ++b) {
+      L.lli[a][b] = L.lli[a][b] + T.lli[a][b];
+      L.mli3[a][b] = L.mli3[a][b] + T.mli3[a][b];
+      for (int k = 0; k < 3; ++k) L.mli5[a][b][k] = L.mli5[a][b][k] + T.mli5[a][b][k];
+    }
+  }
+  L.mli1 = L.mli1 + T.mli1;
+}
+
+// Collocation point data of the interior integration: x_i, the unit normal
+// n_i, phi(xi_i) and psi_i, the shape functions' tangential gradient at xi_i
+// in the orthogonal frame v1 = t1, v2 = n_i x t1 (bem_staela3d.f90:5022-5118).
+struct HbieAt {
+  double x_i[3], n_i[3], phi_i[8], psi_i[8][3];
+};
+static void hbie_at(const Elem& e, const double xi_i[2], HbieAt& a) {
+  double d1[8], d2[8];
+  phi_quad8(xi_i, a.phi_i);
+  dphi_quad8(xi_i, d1, d2);
+  double T1[3] = {0, 0, 0}, T2[3] = {0, 0, 0};
+  for (int c = 0; c < 3; ++c) a.x_i[c] = 0.0;
+  for (int q = 0; q < 8; ++q)
+    for (int c = 0; c < 3; ++c) {
+      a.x_i[c] = a.x_i[c] + a.phi_i[q] * e.x[q][c];
+      T1[c] = T1[c] + d1[q] * e.x[q][c];
+      T2[c] = T2[c] + d2[q] * e.x[q][c];
+    }
+  double N[3] = {T1[1] * T2[2] - T1[2] * T2[1], T1[2] * T2[0] - T1[0] * T2[2], T1[0] * T2[1] - T1[1] * T2[0]};
+  double jg = std::sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+  for (int c = 0; c < 3; ++c) a.n_i[c] = N[c] / jg;
+  double jxi1 = std::sqrt(T1[0] * T1[0] + T1[1] * T1[1] + T1[2] * T1[2]);
+  double jxi2 = std::sqrt(T2[0] * T2[0] + T2[1] * T2[1] + T2[2] * T2[2]);
+  double t1[3] = {T1[0] / jxi1, T1[1] / jxi1, T1[2] / jxi1}, t2[3] = {T2[0] / jxi2, T2[1] / jxi2, T2[2] / jxi2};
+  const double* ni = a.n_i;
+  double v1[3] = {t1[0], t1[1], t1[2]};
+  double v2[3] = {ni[1] * t1[2] - ni[2] * t1[1], ni[2] * t1[0] - ni[0] * t1[2], ni[0] * t1[1] - ni[1] * t1[0]};
+  double M11 = 1.0, M12 = v1[0] * t2[0] + v1[1] * t2[1] + v1[2] * t2[2], M21 = 0.0,
+         M22 = v2[0] * t2[0] + v2[1] * t2[1] + v2[2] * t2[2];
+  double det = M11 * M22 - M12 * M21;
+  double x11 = M22 / (jxi1 * det), x12 = -M12 / (jxi1 * det), x21 = -M21 / (jxi2 * det), x22 = M11 / (jxi2 * det);
+  for (int k = 0; k < 8; ++k)
+    for (int c = 0; c < 3; ++c)
+      a.psi_i[k][c] = (d1[k] * x11 + d2[k] * x21) * v1[c] + (d1[k] * x12 + d2[k] * x22) * v2[c];
+}
+
+static void hbie_edges(const Elem& e, const HbieAt& a, HbieLi& L) {
+  L.zero();
+  QsParams qsp;
+  qs_calculate_parameters(1e-15, qsp);
+  for (int ke = 0; ke < 4; ++ke) {
+    double xe[3][3];
+    for (int q = 0; q < 3; ++q)
+      for (int c = 0; c < 3; ++c) xe[q][c] = e.x[quad8_edge_node[ke][q]][c];
+    double xs[2];
+    hbie_int_li(xe, xs, a.x_i, a.n_i, 5, qsp, 1, 16, L);
+  }
+}
+
+static void hbie_int(const StaelaHK& k, const Elem& e, bool reverse, const double xi_i[2], HG<StaelaHK>& out) {
+  out.zero();
+  if (check_xi1xi2_edge_quad(xi_i)) {
+    g_hbie_err = 1;
+    return;
+  }
+  HbieAt a;
+  hbie_at(e, xi_i, a);
+  const double nu = k.nu, cted2 = k.cted2, ctes2 = k.ctes2, ctes3 = k.ctes3;
+  const double* ni = a.n_i;
+  int nsub, st[8];
+  auto fn = [&](const double*, const double rv[3], const double n[3], const double phi[8], double jw) {
+    double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    double d1r = 1.0 / r, d1r2 = d1r * d1r, d1r3 = d1r2 * d1r;
+    double drdx[3] = {rv[0] * d1r, rv[1] * d1r, rv[2] * d1r};
+    double drdn = drdx[0] * n[0] + drdx[1] * n[1] + drdx[2] * n[2];
+    double drdni = -(drdx[0] * ni[0] + drdx[1] * ni[1] + drdx[2] * ni[2]);
+    double nni = n[0] * ni[0] + n[1] * ni[1] + n[2] * ni[2];
+    double pj[8], reg[8], psn[8];
+    for (int q = 0; q < 8; ++q) {
+      pj[q] = phi[q] * jw;
+      reg[q] = phi[q] - a.phi_i[q] - a.psi_i[q][0] * rv[0] - a.psi_i[q][1] * rv[1] - a.psi_i[q][2] * rv[2];
+      psn[q] = a.psi_i[q][0] * n[0] + a.psi_i[q][1] * n[1] + a.psi_i[q][2] * n[2];
+    }
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        double dk = (il == ik) ? 1.0 : 0.0;
+        // L1
+        double fd = d1r2 * ((cted2 * dk + 3.0 * drdx[il] * drdx[ik]) * drdni +
+                            cted2 * ((ni[il] - n[il]) * drdx[ik] - (ni[ik] - n[ik]) * drdx[il]));
+        for (int q = 0; q < 8; ++q) out.g[q][il][ik] = out.g[q][il][ik] + fd * pj[q];
+        // L21
+        if (il != ik) {
+          fd = d1r2 * cted2 * (n[il] * drdx[ik] - n[ik] * drdx[il]);
+          for (int q = 0; q < 8; ++q) out.g[q][il][ik] = out.g[q][il][ik] + fd * (phi[q] - a.phi_i[q]) * jw;
+        }
+        // M1
+        double fs = 3.0 * d1r3 * drdn * drdni * (5.0 * drdx[il] * drdx[ik] - nu * dk);
+        for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + fs * pj[q];
+        if (il == ik) {
+          // M21, M221, M231
+          fs = ctes2 * d1r3 * nni;
+          for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + fs * reg[q] * jw;
+          fs = -ctes2 * 3.0 * d1r3 * drdn * drdni;
+          for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + a.phi_i[q] * fs * jw;
+          fs = -ctes2 * d1r2 * drdni;
+          for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + fs * psn[q] * jw;
+        }
+        // M31
+        fs = d1r3 * (3.0 * ctes2 * (drdx[ik] * ni[il] * drdn - drdx[il] * n[ik] * drdni) +
+                     3.0 * nu * (drdx[il] * ni[ik] * drdn - drdx[ik] * n[il] * drdni) +
+                     3.0 * nu * drdx[il] * drdx[ik] * nni + ctes2 * ni[ik] * n[il] - ctes3 * ni[il] * n[ik]);
+        for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + fs * reg[q] * jw;
+        // M321
+        fs = d1r3 * (-15.0 * nu * drdx[il] * drdx[ik] * drdn * drdni +
+                     3.0 * nu * drdx[ik] * (ni[il] * drdn - n[il] * drdni) +
+                     3.0 * ctes2 * drdx[il] * (ni[ik] * drdn - n[ik] * drdni));
+        for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + a.phi_i[q] * fs * jw;
+        // M331
+        for (int ij = 0; ij < 3; ++ij) {
+          double djk = (ij == ik) ? 1.0 : 0.0;
+          fs = d1r2 * (drdx[ij] * (3.0 * ctes2 * (drdx[ik] * ni[il] * drdn - drdx[il] * n[ik] * drdni) +
+                                   3.0 * nu * (drdx[il] * ni[ik] * drdn - drdx[ik] * n[il] * drdni) -
+                                   3.0 * nu * drdx[il] * n[ik] * drdni) -
+                       ((1.0 - 3.0 * nu) * ni[il] * drdx[ij] + nu * ni[ij] * drdx[il]) * (n[ik] - ni[ik] * nni) +
+                       ctes2 * ni[ik] * drdx[ij] * (n[il] - ni[il] * nni) -
+                       nu * (dk + ni[il] * ni[ik]) * n[ij] * drdni - nu * (djk - ni[ij] * ni[ik]) * n[il] * drdni);
+          for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + a.psi_i[q][ij] * fs * jw;
+        }
+      }
+  };
+  polar_loop<StaelaHK>(e, xi_i, a.x_i, fn, &nsub, st);
+  HbieLi L;
+  hbie_edges(e, a, L);
+  for (int il = 0; il < 3; ++il)
+    for (int ik = 0; ik < 3; ++ik) {
+      double dk = (il == ik) ? 1.0 : 0.0;
+      for (int q = 0; q < 8; ++q) {
+        const double ph = a.phi_i[q];
+        const double* ps = a.psi_i[q];
+        out.g[q][il][ik] = out.g[q][il][ik] + ph * cted2 * L.lli[il][ik];  // L22
+        double v = out.h[q][il][ik];
+        if (il == ik) {
+          v = v + ph * ctes2 * L.mli1;                                  // M222
+          for (int ij = 0; ij < 3; ++ij) v = v + ps[ij] * ctes2 * L.mli2[ij];  // M232
+        }
+        v = v + ph * 3.0 * nu * L.mli3[il][ik];          // M322
+        v = v + ph * ctes2 * ni[ik] * L.mli4[il];        // M323
+        v = v - ph * ctes3 * ni[il] * L.mli4[ik];        // M324
+        for (int ij = 0; ij < 3; ++ij) {
+          double djk = (ij == ik) ? 1.0 : 0.0;
+          v = v + ps[ij] * nu * L.mli5[ij][il][ik];                               // M332
+          v = v + ps[ij] * nu * (dk + ni[il] * ni[ik]) * L.mli2[ij];              // M333
+          v = v + ps[ij] * nu * (djk - ni[ij] * ni[ik]) * L.mli2[il];             // M334
+        }
+        out.h[q][il][ik] = v;
+      }
+    }
+  for (int q = 0; q < 8; ++q)
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        out.h[q][il][ik] = k.ctes1 * out.h[q][il][ik];
+        out.g[q][il][ik] = k.cted1 * out.g[q][il][ik];
+        if (reverse) out.g[q][il][ik] = -out.g[q][il][ik];
+      }
+}
+
+static void hbie_int(const HarelaHK& k, const Elem& e, bool reverse, const double xi_i[2], HG<HarelaHK>& out) {
+  out.zero();
+  if (check_xi1xi2_edge_quad(xi_i)) {
+    g_hbie_err = 1;
+    return;
+  }
+  HbieAt a;
+  hbie_at(e, xi_i, a);
+  const HarPar& p = k.p;
+  const double* ni = a.n_i;
+  const cplx I(0.0, 1.0);
+  const cplx S1o3 = p.S1[0] / 3.0;
+  int nsub, st[8];
+  auto fn = [&](const double*, const double rv[3], const double n[3], const double phi[8], double jw) {
+    double r = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+    double dr1 = 1.0 / r, dr2 = dr1 * dr1, dr3 = dr2 * dr1, dr4 = dr3 * dr1, dr5 = dr4 * dr1;
+    double drdx[3] = {rv[0] * dr1, rv[1] * dr1, rv[2] * dr1};
+    double drdn = drdx[0] * n[0] + drdx[1] * n[1] + drdx[2] * n[2];
+    double drdni = -(drdx[0] * ni[0] + drdx[1] * ni[1] + drdx[2] * ni[2]);
+    double nni = n[0] * ni[0] + n[1] * ni[1] + n[2] * ni[2];
+    double pj[8], reg[8], psn[8];
+    for (int q = 0; q < 8; ++q) {
+      pj[q] = phi[q] * jw;
+      reg[q] = phi[q] - a.phi_i[q] - a.psi_i[q][0] * rv[0] - a.psi_i[q][1] * rv[1] - a.psi_i[q][2] * rv[2];
+      psn[q] = a.psi_i[q][0] * n[0] + a.psi_i[q][1] * n[1] + a.psi_i[q][2] * n[2];
+    }
+    cplx z[2] = {-I * p.k1 * r, -I * p.k2 * r};
+    cplx E[7][2];
+    zexp_decomposed(2, z, E);
+    for (int j = 0; j < 2; ++j) {
+      E[2][j] = E[2][j] * dr1;
+      E[3][j] = E[3][j] * dr2;
+      E[4][j] = E[4][j] * dr3;
+      E[5][j] = E[5][j] * dr4;
+      E[6][j] = E[6][j] * dr5;
+    }
+    // regular parts only (the 1/r^2 and 1/r^3 terms are regularised below)
+    cplx TT1 = p.T1[1] + p.T1[2] * E[2][0] + p.T1[3] * E[2][1] + p.T1[4] * E[3][0] + p.T1[5] * E[3][1] +
+               p.T1[6] * E[4][0] + p.T1[7] * E[4][1] + p.T1[8] * E[5][0] + p.T1[9] * E[5][1];
+    cplx TT2 = p.T2[1] + p.T2[2] * E[2][1] + p.T2[3] * E[3][0] + p.T2[4] * E[3][1] + p.T2[5] * E[4][0] +
+               p.T2[6] * E[4][1] + p.T2[7] * E[5][0] + p.T2[8] * E[5][1];
+    cplx TT3 = p.T3[1] + p.T3[2] * E[2][0] + p.T3[3] * E[3][0] + p.T3[4] * E[3][1] + p.T3[5] * E[4][0] +
+               p.T3[6] * E[4][1] + p.T3[7] * E[5][0] + p.T3[8] * E[5][1];
+    cplx S1 = p.S1[1] * dr1 + p.S1[2] * E[2][1] + p.S1[3] * E[3][0] + p.S1[4] * E[3][1] + p.S1[5] * E[4][0] +
+              p.S1[6] * E[4][1] + p.S1[7] * E[5][0] + p.S1[8] * E[5][1] + p.S1[9] * E[6][0] + p.S1[10] * E[6][1];
+    cplx S2 = p.S2[1] * dr1 + p.S2[2] * E[2][0] + p.S2[3] * E[3][0] + p.S2[4] * E[3][1] + p.S2[5] * E[4][0] +
+              p.S2[6] * E[4][1] + p.S2[7] * E[5][0] + p.S2[8] * E[5][1] + p.S2[9] * E[6][0] + p.S2[10] * E[6][1];
+    cplx S3 = p.S3[1] * dr1 + p.S3[2] * E[2][0] + p.S3[3] * E[2][1] + p.S3[4] * E[3][0] + p.S3[5] * E[3][1] +
+              p.S3[6] * E[4][0] + p.S3[7] * E[4][1] + p.S3[8] * E[5][0] + p.S3[9] * E[5][1] + p.S3[10] * E[6][0] +
+              p.S3[11] * E[6][1];
+    cplx S4 = p.S4[1] * dr1 + p.S4[2] + p.S4[3] * E[3][1] + p.S4[4] * E[4][0] + p.S4[5] * E[4][1] +
+              p.S4[6] * E[5][0] + p.S4[7] * E[5][1] + p.S4[8] * E[6][0] + p.S4[9] * E[6][1];
+    cplx S5 = p.S5[1] * dr1 + p.S5[2] + p.S5[3] * E[2][0] + p.S5[4] * E[3][0] + p.S5[5] * E[4][0] +
+              p.S5[6] * E[4][1] + p.S5[7] * E[5][0] + p.S5[8] * E[5][1] + p.S5[9] * E[6][0] + p.S5[10] * E[6][1];
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        double dk = (il == ik) ? 1.0 : 0.0;
+        cplx fd = (TT1 + p.T1[0] * dr2) * drdx[il] * drdx[ik] * drdni + (TT2 + p.T2[0] * dr2) * dk * drdni -
+                  TT2 * drdx[il] * ni[ik] - TT3 * drdx[ik] * ni[il] +
+                  p.T2[0] * dr2 * ((ni[il] - n[il]) * drdx[ik] - (ni[ik] - n[ik]) * drdx[il]);
+        cplx fs = S1 * (drdx[il] * ni[ik] * drdn - drdx[ik] * n[il] * drdni - dk * drdn * drdni +
+                        drdx[il] * drdx[ik] * nni) +
+                  S2 * (drdx[ik] * ni[il] * drdn - drdx[il] * n[ik] * drdni) + S3 * drdx[il] * drdx[ik] * drdn * drdni +
+                  S4 * (dk * nni + ni[ik] * n[il]) + S5 * n[ik] * ni[il] - dk * p.S1[0] * dr3 * drdn * drdni +
+                  p.S3[0] * dr3 * drdx[il] * drdx[ik] * drdn * drdni;
+        for (int q = 0; q < 8; ++q) {
+          out.h[q][il][ik] = out.h[q][il][ik] + fs * pj[q];
+          out.g[q][il][ik] = out.g[q][il][ik] + fd * pj[q];
+        }
+        // L21
+        if (il != ik) {
+          fd = p.T2[0] * dr2 * (n[il] * drdx[ik] - n[ik] * drdx[il]);
+          for (int q = 0; q < 8; ++q) out.g[q][il][ik] = out.g[q][il][ik] + fd * (phi[q] - a.phi_i[q]) * jw;
+        }
+        if (il == ik) {
+          // M21, M221, M231
+          fs = p.S4[0] * dr3 * nni;
+          for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + fs * reg[q] * jw;
+          fs = -p.S4[0] * 3.0 * dr3 * drdn * drdni;
+          for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + a.phi_i[q] * fs * jw;
+          fs = -p.S4[0] * dr2 * drdni;
+          for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + fs * psn[q] * jw;
+        }
+        // M31
+        fs = dr3 * (p.S2[0] * (drdx[ik] * ni[il] * drdn - drdx[il] * n[ik] * drdni) +
+                    p.S1[0] * (drdx[il] * ni[ik] * drdn - drdx[ik] * n[il] * drdni) +
+                    p.S1[0] * drdx[il] * drdx[ik] * nni + p.S4[0] * ni[ik] * n[il] + p.S5[0] * ni[il] * n[ik]);
+        for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + fs * reg[q] * jw;
+        // M321
+        fs = dr3 * (-5.0 * p.S1[0] * drdx[il] * drdx[ik] * drdn * drdni +
+                    p.S1[0] * drdx[ik] * (ni[il] * drdn - n[il] * drdni) +
+                    p.S2[0] * drdx[il] * (ni[ik] * drdn - n[ik] * drdni));
+        for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + a.phi_i[q] * fs * jw;
+        // M331
+        for (int ij = 0; ij < 3; ++ij) {
+          double djk = (ij == ik) ? 1.0 : 0.0;
+          fs = dr2 * (drdx[ij] * (p.S2[0] * (drdx[ik] * ni[il] * drdn - drdx[il] * n[ik] * drdni) +
+                                  p.S1[0] * (drdx[il] * ni[ik] * drdn - drdx[ik] * n[il] * drdni) -
+                                  p.S1[0] * drdx[il] * n[ik] * drdni) -
+                      ((S1o3 - p.S5[0]) * ni[il] * drdx[ij] + S1o3 * ni[ij] * drdx[il]) * (n[ik] - ni[ik] * nni) +
+                      p.S4[0] * ni[ik] * drdx[ij] * (n[il] - ni[il] * nni) -
+                      S1o3 * (dk + ni[il] * ni[ik]) * n[ij] * drdni - S1o3 * (djk - ni[ij] * ni[ik]) * n[il] * drdni);
+          for (int q = 0; q < 8; ++q) out.h[q][il][ik] = out.h[q][il][ik] + a.psi_i[q][ij] * fs * jw;
+        }
+      }
+  };
+  polar_loop<HarelaHK>(e, xi_i, a.x_i, fn, &nsub, st);
+  HbieLi L;
+  hbie_edges(e, a, L);
+  for (int il = 0; il < 3; ++il)
+    for (int ik = 0; ik < 3; ++ik) {
+      double dk = (il == ik) ? 1.0 : 0.0;
+      for (int q = 0; q < 8; ++q) {
+        const double ph = a.phi_i[q];
+        const double* ps = a.psi_i[q];
+        out.g[q][il][ik] = out.g[q][il][ik] + ph * p.T2[0] * L.lli[il][ik];  // L22
+        cplx v = out.h[q][il][ik];
+        if (il == ik) {
+          v = v + ph * p.S4[0] * L.mli1;                                     // M222
+          for (int ij = 0; ij < 3; ++ij) v = v + ps[ij] * p.S4[0] * L.mli2[ij];  // M232
+        }
+        v = v + ph * p.S1[0] * L.mli3[il][ik];          // M322
+        v = v + ph * p.S4[0] * ni[ik] * L.mli4[il];     // M323
+        v = v + ph * p.S5[0] * ni[il] * L.mli4[ik];     // M324
+        for (int ij = 0; ij < 3; ++ij) {
+          double djk = (ij == ik) ? 1.0 : 0.0;
+          v = v + ps[ij] * S1o3 * L.mli5[ij][il][ik];                    // M332
+          v = v + ps[ij] * S1o3 * (dk + ni[il] * ni[ik]) * L.mli2[ij];   // M333
+          v = v + ps[ij] * S1o3 * (djk - ni[ij] * ni[ik]) * L.mli2[il];  // M334
+        }
+        out.h[q][il][ik] = v;
+      }
+    }
+  for (int q = 0; q < 8; ++q)
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) {
+        out.h[q][il][ik] = p.cte_s * out.h[q][il][ik];
+        out.g[q][il][ik] = p.cte_d * out.g[q][il][ik];
+        if (reverse) out.g[q][il][ik] = -out.g[q][il][ik];
+      }
+}
+
+// hbie_auto (bem_staela3d.f90:4307-4373 / bem_harela3d.f90:3632-3697): the
+// classification of sbie_auto with the 1/r^7 estimate. A point on the element
+// (d <= 1e-12) takes the interior integration when `interior` is set (HBIE
+// collocation on the boundary); internal points pass false and get zero
+// kernels with CLS_SING, which they report.
 template <class K>
 static int hbie_auto(const K& k, const Elem& e, bool reverse, const double x_i[3], const QsParams& qsp, int ns,
-                     HG<K>& out) {
+                     HG<K>& out, bool interior = false, AdpStats* st = nullptr) {
   double r[3] = {e.bc[0] - x_i[0], e.bc[1] - x_i[1], e.bc[2] - x_i[2]};
   double rmin = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) - e.br;
   double barxi[2] = {0.0, 0.0}, d;
@@ -851,7 +1265,8 @@ static int hbie_auto(const K& k, const Elem& e, bool reverse, const double x_i[3
     int method;
     nearest_element_point_quad8(e.x, e.cl, x_i, barxi, &rmin, &d, &method);
     if (d <= 1e-12) {
-      out.zero();
+      if (interior) hbie_int(k, e, reverse, barxi, out);
+      else out.zero();
       return CLS_SING;
     }
   }
@@ -865,7 +1280,44 @@ static int hbie_auto(const K& k, const Elem& e, bool reverse, const double x_i[3
     return ps;
   }
   double xi_s[4][2];
-  ext_adp<K>(k, e, reverse, xi_s, x_i, qsp, 1, ns, out, nullptr);
+  ext_adp<K>(k, e, reverse, xi_s, x_i, qsp, 1, ns, out, st);
+  return CLS_ADP;
+}
+
+// fbem_bem_harela3d_shbie_auto (bem_harela3d.f90:4888-4957): SBIE and HBIE
+// kernels at one collocation point, classified once with the HBIE's 1/r^7
+// estimate: interior integration of both, one precalculated rule for both
+// (shbie_ext_pre, bem_harela3d.f90:4781-4886), or each kernel's own adaptive
+// subdivision.
+static int shbie_auto(const HarelaK& k, const HarelaHK& kh, const Elem& e, bool reverse, const double x_i[3],
+                      const QsParams& qsp, int ns, HG<HarelaK>& hg, HG<HarelaHK>& ml, AdpStats* st) {
+  double r[3] = {e.bc[0] - x_i[0], e.bc[1] - x_i[1], e.bc[2] - x_i[2]};
+  double rmin = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) - e.br;
+  double barxi[2] = {0.0, 0.0}, d;
+  if (rmin > 4.0 * e.br) {
+    d = rmin / e.cl;
+  } else {
+    int method;
+    nearest_element_point_quad8(e.x, e.cl, x_i, barxi, &rmin, &d, &method);
+    if (d <= 1e-12) {
+      sbie_int<HarelaK>(k, e, reverse, barxi, hg);
+      hbie_int(kh, e, reverse, barxi, ml);
+      return CLS_SING;
+    }
+  }
+  int gln_near = qs_n_estimation_standard(2, HarelaHK::F, qsp, d, barxi);
+  int gln = std::max(e.gln_far, gln_near);
+  if (gln <= e.ps_gln_max && gln_near > 0) {
+    int ps = 0;
+    for (int i = 0; i < e.n_ps; ++i)
+      if (e.ps_gln[i] >= gln) { ps = i; break; }
+    ext_pre<HarelaK>(k, ps, e, reverse, x_i, hg);
+    ext_pre<HarelaHK>(kh, ps, e, reverse, x_i, ml);
+    return ps;
+  }
+  double xi_s[4][2];
+  ext_adp<HarelaK>(k, e, reverse, xi_s, x_i, qsp, 1, ns, hg, st);
+  ext_adp<HarelaHK>(kh, e, reverse, xi_s, x_i, qsp, 1, ns, ml, st);
   return CLS_ADP;
 }
 
@@ -1153,9 +1605,10 @@ static bool freeterm(int ne, const double* n, const double* t, double tol, T nu,
 struct Colloc {
   double x[3];
   int node;     // collocation node (rows)
-  int kind;     // 0 SBIE (nodal), 1 SBIE MCA
+  int kind;     // 0 SBIE (nodal), 1 SBIE MCA, 2 HBIE, 3 SBIE + HBIE (Burton & Miller) at one point
   int elem, kn; // element/local node it was taken from
   double xi[2];
+  double n[3];  // unit normal at xi (HBIE kinds)
 };
 
 struct Problem {
@@ -1183,6 +1636,14 @@ struct Problem {
   // boundary condition hs_bc (1: traction-free surface)
   int hs_n = 0, hs_bc = 1;
   double hs_x = 0.0;
+  // BEM formulation per node (src/read_bem_formulation_selected_nodes.f90:
+  // 70-260, ordinary boundary of continuous elements): 0 the default SBIE
+  // (assign_default_bem_formulation.f90:76-93), 1 'hbie' (HBIE alone at
+  // non-nodal points), 2 'dual_bm_same' (SBIE and HBIE at the same non-nodal
+  // point, Burton & Miller combination with weight alpha); delta_hbie moves
+  // the point into each element of the node
+  std::vector<int> form;
+  std::vector<double> alpha, delta_hbie;
 };
 
 static void build(Problem& P) {
@@ -1264,7 +1725,20 @@ static void build(Problem& P) {
       for (int c = 0; c < 3; ++c) P.dof[3 * s + c] = row++;
     }
   P.ndof = row;
-  // collocation points in the collocation loop order (build_lse_mechanics_bem_staela.f90:761-1034)
+  P.form.assign(nn, 0);
+  P.alpha.assign(nn, 1.0);
+  P.delta_hbie.assign(nn, 0.22540333);
+}
+
+// Collocation points in the collocation loop order
+// (build_lse_mechanics_bem_staela.f90:761-1034): per element and local node,
+// the node's nodal SBIE point (once), SBIE-MCA point or HBIE point. HBIE
+// points: xi moved from the element edge by delta_hbie
+// (src/build_data_at_collocation_points.f90:148-160) and the unit normal there
+// (:368-376).
+static void build_colloc(Problem& P) {
+  const int nn = P.nn, ne = P.ne;
+  P.cps.clear();
   std::vector<char> coll(nn, 0);
   P.node_cps.assign(nn, {});
   for (int e = 0; e < ne; ++e)
@@ -1272,8 +1746,24 @@ static void build(Problem& P) {
       int s = P.conn[8 * e + k];
       Colloc cp;
       cp.node = s; cp.elem = e; cp.kn = k;
+      cp.n[0] = cp.n[1] = cp.n[2] = 0.0;
       double xi[2] = {quad8_xi_nodes[k][0], quad8_xi_nodes[k][1]};
-      if (!P.in_boundary[s]) {
+      if (P.form[s] != 0) {
+        double dl = P.delta_hbie[s];
+        if (check_xi1xi2_edge_quad(xi)) { xi[0] = xi[0] * (1.0 - dl); xi[1] = xi[1] * (1.0 - dl); }
+        cp.kind = P.form[s] == 1 ? 2 : 3;
+        double d1[8], d2[8];
+        dphi_quad8(xi, d1, d2);
+        double T1[3] = {0, 0, 0}, T2[3] = {0, 0, 0};
+        for (int q = 0; q < 8; ++q)
+          for (int c = 0; c < 3; ++c) {
+            T1[c] = T1[c] + d1[q] * P.el[e].x[q][c];
+            T2[c] = T2[c] + d2[q] * P.el[e].x[q][c];
+          }
+        double N[3] = {T1[1] * T2[2] - T1[2] * T2[1], T1[2] * T2[0] - T1[0] * T2[2], T1[0] * T2[1] - T1[1] * T2[0]};
+        double jn = std::sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+        for (int c = 0; c < 3; ++c) cp.n[c] = N[c] / jn;
+      } else if (!P.in_boundary[s]) {
         if (coll[s]) continue;
         coll[s] = 1;
         cp.kind = 0;
@@ -1322,7 +1812,8 @@ static void scatter(const Problem& P, int e, const T h[8][3][3], const T g[8][3]
 // Free-term contribution for collocation node s (first element of the
 // collocation order carries it), build_lse_mechanics_bem_staela.f90:152-549.
 template <class K>
-static bool free_terms_for_node(const Problem& P, int s, typename K::T nu, typename K::T* rowbuf, typename K::T* brow) {
+static bool free_terms_for_node(const Problem& P, int s, typename K::T nu, typename K::T beta, typename K::T* rowbuf,
+                                typename K::T* brow) {
   typedef typename K::T T;
   for (int ci : P.node_cps[s]) {
     const Colloc& cp = P.cps[ci];
@@ -1345,8 +1836,18 @@ static bool free_terms_for_node(const Problem& P, int s, typename K::T nu, typen
     } else {
       double pphi[8];
       phi_quad8(cp.xi, pphi);
-      for (int il = 0; il < 3; ++il)
-        for (int a = 0; a < 8; ++a) hg.h[a][il][il] = hg.h[a][il][il] + 0.5 * pphi[a];
+      // SBIE at a non-nodal point: 1/2 phi(xi_i) on h; HBIE: -1/2 phi(xi_i) on
+      // l, which is g ('hbie', dual = 0) or weighted by beta into g (Burton &
+      // Miller) (build_lse_mechanics_bem_staela.f90:181-211,440-489,
+      // build_lse_mechanics_bem_harela.f90:316-360,598-681)
+      if (cp.kind != 2)
+        for (int il = 0; il < 3; ++il)
+          for (int a = 0; a < 8; ++a) hg.h[a][il][il] = hg.h[a][il][il] + 0.5 * pphi[a];
+      if (cp.kind >= 2) {
+        const T w = cp.kind == 2 ? (T)1.0 : beta * P.alpha[s];
+        for (int il = 0; il < 3; ++il)
+          for (int a = 0; a < 8; ++a) hg.g[a][il][il] = hg.g[a][il][il] + w * (-0.5 * pphi[a]);
+      }
     }
     // half-space with a traction-free surface: a collocation point on the
     // surface takes twice the free term (build_lse_mechanics_bem_staela.f90:502-513,
@@ -1363,22 +1864,42 @@ static bool free_terms_for_node(const Problem& P, int s, typename K::T nu, typen
   return true;
 }
 
-template <class K>
-static int assemble(const Problem& P, const K& k, typename K::T nu, typename K::T* A, typename K::T* b, int nthreads,
-                    long* stats) {
+// The region builder's collocation loop for one BE region. mkh(n_i) makes the
+// HBIE kernel at a point with unit normal n_i; bm is the Burton & Miller
+// factor besides the node's alpha: 1 static (h + alpha m,
+// build_lse_mechanics_bem_staela.f90:835-841), i / c2 harmonic with c2 the
+// complex S-wave speed (h + alpha i / c2 m, build_lse_mechanics_bem_harela.f90:
+// 1174-1181). stats: [0..2] SBIE precalculated / adaptive / singular pairs,
+// [3] adaptive leaves, [4] their points, [5] maximum-depth hits, [6..7]
+// complementary adaptive / singular pairs, [8..10] HBIE precalculated /
+// adaptive / singular pairs.
+template <class K, class KH, class MKH>
+static int assemble(const Problem& P, const K& k, MKH mkh, typename K::T bm, typename K::T nu, typename K::T* A,
+                    typename K::T* b, int nthreads, long* stats) {
   typedef typename K::T T;
+  constexpr bool kHarmonic = std::is_same<K, HarelaK>::value;
   const int n = P.ndof;
   int nord = (int)P.node_order.size();
   int bad = 0;
+  bool has_hbie = false;
+  for (int f : P.form) has_hbie = has_hbie || f != 0;
+  if (has_hbie && P.hs_n != 0) return -5;
   long s_leaves = 0, s_points = 0, s_maxd = 0, s_sing = 0, s_adp = 0, s_pre = 0, s_hsing = 0, s_hadp = 0;
-  int hs_err = 0;
+  long s_bpre = 0, s_badp = 0, s_bsing = 0;
+  int hs_err = 0, hb_err = 0;
   if (nthreads > 0) omp_set_num_threads(nthreads);
-#pragma omp parallel reduction(+ : bad, s_leaves, s_points, s_maxd, s_sing, s_adp, s_pre, s_hsing, s_hadp) \
-    reduction(max : hs_err)
+#pragma omp parallel reduction(+ : bad, s_leaves, s_points, s_maxd, s_sing, s_adp, s_pre, s_hsing, s_hadp, s_bpre, \
+                               s_badp, s_bsing) reduction(max : hs_err, hb_err)
   {
     g_hs_err = 0;
+    g_hbie_err = 0;
     std::vector<T> rowbuf(3 * (size_t)n);
     AdpStats st;
+    auto count = [&](int cls, long& sing, long& adp, long& pre) {
+      if (cls == CLS_SING) sing++;
+      else if (cls == CLS_ADP) adp++;
+      else pre++;
+    };
 #pragma omp for schedule(dynamic, 1)
     for (int oi = 0; oi < nord; ++oi) {
       int s = P.node_order[oi];
@@ -1386,32 +1907,58 @@ static int assemble(const Problem& P, const K& k, typename K::T nu, typename K::
       T brow[3] = {(T)0, (T)0, (T)0};
       for (int e = 0; e < P.ne; ++e) {
         for (int ci : P.node_cps[s]) {
+          const Colloc& cp = P.cps[ci];
           HG<K> hg;
-          int cls = sbie_auto<K>(k, P.el[e], false, P.cps[ci].x, P.qsp, P.ns_max, hg, &st);
-          if (cls == CLS_SING) s_sing++;
-          else if (cls == CLS_ADP) s_adp++;
-          else s_pre++;
-          if constexpr (std::is_same<K, StaelaK>::value) {
-            // half-space region: h, g of the complementary kernel added to the
-            // full-space ones (build_lse_mechanics_bem_staela.f90:861-875)
-            if (P.hs_n != 0) {
-              HscK kh(k.mu, k.nu, P.hs_x);
-              HG<HscK> hp;
-              int c2 = hsc_auto(k, kh, P.el[e], false, P.cps[ci].x, P.qsp, P.ns_max, hp, &st);
-              if (c2 == CLS_SING) s_hsing++;
-              else if (c2 == CLS_ADP) s_hadp++;
-              for (int a = 0; a < 8; ++a)
-                for (int il = 0; il < 3; ++il)
-                  for (int ik = 0; ik < 3; ++ik) {
-                    hg.h[a][il][ik] = hg.h[a][il][ik] + hp.h[a][il][ik];
-                    hg.g[a][il][ik] = hg.g[a][il][ik] + hp.g[a][il][ik];
-                  }
+          if (cp.kind <= 1) {
+            count(sbie_auto<K>(k, P.el[e], false, cp.x, P.qsp, P.ns_max, hg, &st), s_sing, s_adp, s_pre);
+            if constexpr (std::is_same<K, StaelaK>::value) {
+              // half-space region: h, g of the complementary kernel added to the
+              // full-space ones (build_lse_mechanics_bem_staela.f90:861-875)
+              if (P.hs_n != 0) {
+                HscK kc(k.mu, k.nu, P.hs_x);
+                HG<HscK> hp;
+                int c2 = hsc_auto(k, kc, P.el[e], false, cp.x, P.qsp, P.ns_max, hp, &st);
+                if (c2 == CLS_SING) s_hsing++;
+                else if (c2 == CLS_ADP) s_hadp++;
+                for (int a = 0; a < 8; ++a)
+                  for (int il = 0; il < 3; ++il)
+                    for (int ik = 0; ik < 3; ++ik) {
+                      hg.h[a][il][ik] = hg.h[a][il][ik] + hp.h[a][il][ik];
+                      hg.g[a][il][ik] = hg.g[a][il][ik] + hp.g[a][il][ik];
+                    }
+              }
             }
+          } else {
+            KH kh = mkh(cp.n);
+            HG<KH> ml;
+            T w = (T)1.0;
+            if (cp.kind == 2) {
+              // 'hbie': h = m, g = l
+              count(hbie_auto<KH>(kh, P.el[e], false, cp.x, P.qsp, P.ns_max, ml, true, &st), s_bsing, s_badp, s_bpre);
+              hg.zero();
+            } else {
+              w = bm * P.alpha[s];
+              if constexpr (kHarmonic) {
+                int c = shbie_auto(k, kh, P.el[e], false, cp.x, P.qsp, P.ns_max, hg, ml, &st);
+                count(c, s_sing, s_adp, s_pre);
+                count(c, s_bsing, s_badp, s_bpre);
+              } else {
+                count(sbie_auto<K>(k, P.el[e], false, cp.x, P.qsp, P.ns_max, hg, &st), s_sing, s_adp, s_pre);
+                count(hbie_auto<KH>(kh, P.el[e], false, cp.x, P.qsp, P.ns_max, ml, true, &st), s_bsing, s_badp,
+                      s_bpre);
+              }
+            }
+            for (int a = 0; a < 8; ++a)
+              for (int il = 0; il < 3; ++il)
+                for (int ik = 0; ik < 3; ++ik) {
+                  hg.h[a][il][ik] = hg.h[a][il][ik] + w * ml.h[a][il][ik];
+                  hg.g[a][il][ik] = hg.g[a][il][ik] + w * ml.g[a][il][ik];
+                }
           }
           scatter<T>(P, e, hg.h, hg.g, rowbuf.data(), brow);
         }
       }
-      if (!free_terms_for_node<K>(P, s, nu, rowbuf.data(), brow)) bad++;
+      if (!free_terms_for_node<K>(P, s, nu, bm, rowbuf.data(), brow)) bad++;
       for (int il = 0; il < 3; ++il) {
         int r = P.dof[3 * s + il];
         for (int c = 0; c < n; ++c) A[(size_t)c * n + r] = A[(size_t)c * n + r] + rowbuf[(size_t)il * n + c];
@@ -1422,12 +1969,15 @@ static int assemble(const Problem& P, const K& k, typename K::T nu, typename K::
     s_points += st.points;
     s_maxd += st.maxdepth_hits;
     hs_err = std::max(hs_err, g_hs_err);
+    hb_err = std::max(hb_err, g_hbie_err);
   }
   if (stats) {
     stats[0] = s_pre; stats[1] = s_adp; stats[2] = s_sing; stats[3] = s_leaves; stats[4] = s_points; stats[5] = s_maxd;
     stats[6] = s_hadp; stats[7] = s_hsing;
+    stats[8] = s_bpre; stats[9] = s_badp; stats[10] = s_bsing;
   }
   if (hs_err) return -1 - hs_err;
+  if (hb_err) return -6;
   return bad ? -1 : 0;
 }
 
@@ -1519,7 +2069,53 @@ void* orc_problem_new(int nn, const double* X, int ne, const int* conn, const in
   for (int i = 0; i < n_ps; ++i) P->ps_gln[i] = ps_gln[i];
   qs_calculate_parameters(qsi_re, P->qsp);
   build(*P);
+  build_colloc(*P);
   return P;
+}
+// BEM formulation per node (0 default SBIE, 1 'hbie', 2 'dual_bm_same'),
+// alpha and delta_hbie per node (null: 1 and 0.22540333, the quadratic
+// default of read_bem_formulation_selected_nodes.f90:43); rebuilds the
+// collocation points. Returns -1 for a formulation code out of range.
+int orc_problem_set_formulation(void* h, const int* form, const double* alpha, const double* delta) {
+  Problem* P = (Problem*)h;
+  for (int s = 0; s < P->nn; ++s)
+    if (form[s] < 0 || form[s] > 2) return -1;
+  for (int s = 0; s < P->nn; ++s) {
+    P->form[s] = form[s];
+    P->alpha[s] = alpha ? alpha[s] : 1.0;
+    P->delta_hbie[s] = delta ? delta[s] : 0.22540333;
+  }
+  build_colloc(*P);
+  return 0;
+}
+// unit normals of the collocation points (zero for SBIE points)
+void orc_colloc_normals(void* h, double* n /*3*ncp*/) {
+  Problem* P = (Problem*)h;
+  for (size_t i = 0; i < P->cps.size(); ++i)
+    for (int c = 0; c < 3; ++c) n[3 * i + c] = P->cps[i].n[c];
+}
+// One (collocation point, element) pair of the HBIE kernels at the point's
+// normal (m, l laid out [kn][il][ik]), interior integration included.
+int orc_pair_hbie_staela(void* hp, int ci, int e, double mu, double nu, double* m, double* l) {
+  Problem* P = (Problem*)hp;
+  StaelaHK k(mu, nu, P->cps[ci].n);
+  HG<StaelaHK> ml;
+  g_hbie_err = 0;
+  int cls = hbie_auto<StaelaHK>(k, P->el[e], false, P->cps[ci].x, P->qsp, P->ns_max, ml, true);
+  std::memcpy(m, ml.h, sizeof(ml.h));
+  std::memcpy(l, ml.g, sizeof(ml.g));
+  return g_hbie_err ? -6 : cls;
+}
+int orc_pair_hbie_harela(void* hp, int ci, int e, double lre, double lim, double mre, double mim, double rho,
+                         double omega, double* m, double* l) {
+  Problem* P = (Problem*)hp;
+  HarelaHK k(harela_parameters(cplx(lre, lim), cplx(mre, mim), rho, omega), P->cps[ci].n);
+  HG<HarelaHK> ml;
+  g_hbie_err = 0;
+  int cls = hbie_auto<HarelaHK>(k, P->el[e], false, P->cps[ci].x, P->qsp, P->ns_max, ml, true);
+  std::memcpy(m, ml.h, sizeof(ml.h));
+  std::memcpy(l, ml.g, sizeof(ml.g));
+  return g_hbie_err ? -6 : cls;
 }
 void orc_problem_free(void* h) { delete (Problem*)h; }
 int orc_n_dof(void* h) { return ((Problem*)h)->ndof; }
@@ -1597,14 +2193,18 @@ int orc_assemble_staela(void* h, double mu, double nu, double* A, double* b, int
   Problem* P = (Problem*)h;
   if (P->hs_n != 0 && P->hs_n != -3) return -4;
   StaelaK k(mu, nu);
-  return assemble<StaelaK>(*P, k, nu, A, b, nthreads, stats);
+  auto mkh = [&](const double* ni) { return StaelaHK(mu, nu, ni); };
+  return assemble<StaelaK, StaelaHK>(*P, k, mkh, 1.0, nu, A, b, nthreads, stats);
 }
 // Harmonic assembly; nu is the region's complex-typed Poisson ratio (property_c(3)).
 int orc_assemble_harela_nu(void* h, double lre, double lim, double mre, double mim, double rho, double omega,
                            double nure, double nuim, double* A, double* b, int nthreads, long* stats) {
   Problem* P = (Problem*)h;
-  HarelaK k(harela_parameters(cplx(lre, lim), cplx(mre, mim), rho, omega));
-  return assemble<HarelaK>(*P, k, cplx(nure, nuim), (cplx*)A, (cplx*)b, nthreads, stats);
+  HarPar par = harela_parameters(cplx(lre, lim), cplx(mre, mim), rho, omega);
+  HarelaK k(par);
+  auto mkh = [&](const double* ni) { return HarelaHK(par, ni); };
+  return assemble<HarelaK, HarelaHK>(*P, k, mkh, cplx(0.0, 1.0) / par.c2, cplx(nure, nuim), (cplx*)A, (cplx*)b,
+                                     nthreads, stats);
 }
 
 // One (collocation point, element) pair; h,g laid out [kn][il][ik].
