@@ -116,6 +116,40 @@ typedef struct mfbem_stats {
 int mfbem_mesh_upload(const mfbem_mesh_desc* desc, mfbem_handle** out);
 int mfbem_mesh_release(mfbem_handle* h);
 
+/* HBIE collocation on the boundary: the node(sn)%hbie / %dual /
+   %dual_is_common / %alpha and element(se)%xi_i_hbie / %x_i_hbie / %n_i_hbie
+   members the reference sets from the [bem formulation over boundaries]
+   section (src/read_bem_formulation_selected_nodes.f90:70-260) and
+   src/build_data_at_collocation_points.f90:148-160,368-376, for ordinary
+   boundaries of continuous elements. Per node, (hbie, dual, dual_is_common):
+     (0, 0, 0)  the SBIE of the mesh descriptor: nodal, or MCA by its sbie flag;
+     (1, 0, 0)  'hbie': the HBIE alone, collocated at x_i_hbie in every
+                element of the node (h = m, g = l);
+     (1, 1, 1)  'dual_bm_same': SBIE and HBIE at the same points x_i_hbie,
+                Burton & Miller: h + beta m, g + beta l with beta = alpha in
+                the static builder (build_lse_mechanics_bem_staela.f90:835-841)
+                and alpha i / c2 in the harmonic one, c2 = sqrt(mu / rho) the
+                complex S-wave speed (build_lse_mechanics_bem_harela.f90:1174-1181).
+   Other combinations (crack-like boundaries, 'dual_bm_mixed') return
+   MFBEM_EUNSUPPORTED. The HBIE points are classified as hbie_auto does
+   (lib/fbem/src/bem_staela3d.f90:4307-4373, 1/r^7 estimate); the element
+   holding a point takes the interior (hypersingular) integration
+   (bem_staela3d.f90:4918-5353, bem_harela3d.f90:3169-3630); the SBIE part of
+   a Burton & Miller point is classified like sbie_auto by the static builder
+   and like shbie_auto (bem_harela3d.f90:4888-4957) by the harmonic one. The
+   n_i_hbie of an element whose reversion flag is set is reversed on upload.
+   A half-space region with HBIE points is MFBEM_EUNSUPPORTED. */
+typedef struct mfbem_dual_desc {
+  const int32_t* hbie;           /* [n_nodes] */
+  const int32_t* dual;           /* [n_nodes] */
+  const int32_t* dual_is_common; /* [n_nodes] */
+  const double* alpha;           /* [n_nodes] */
+  const double* xi_i_hbie;       /* [n_elements][8][2] */
+  const double* x_i_hbie;        /* [n_elements][8][3] */
+  const double* n_i_hbie;        /* [n_elements][8][3] */
+} mfbem_dual_desc;
+int mfbem_mesh_upload_dual(const mfbem_mesh_desc* desc, const mfbem_dual_desc* dual, mfbem_handle** out);
+
 /* Region space (region(kr)%space, %halfspace_n, %halfspace_x, %halfspace_bc
    of src/read_regions.f90:130-200): n = 0 full space (the default), else a
    half-space whose hyperplane x(|n|) = x has the unit normal sign(n) e_|n|,

@@ -37,9 +37,10 @@ ABI_SYMBOLS = [
     "mfbem_qlearn_label", "mfbem_mlp_size", "mfbem_mlp_forward", "mfbem_mlp_loss_grad", "mfbem_mlp_train",
     "mfbem_set_learned_quadrature", "mfbem_sweep_harela_batch", "mfbem_msh_read", "mfbem_msh_error",
     "mfbem_msh_sizes", "mfbem_msh_parts", "mfbem_msh_nodes", "mfbem_msh_elements", "mfbem_msh_free",
-    "mfbem_nso_write", "mfbem_nso_error", "mfbem_fortran_format", "mfbem_set_halfspace",
+    "mfbem_nso_write", "mfbem_nso_error", "mfbem_fortran_format", "mfbem_set_halfspace", "mfbem_mesh_upload_dual",
 ]
-PREP_SYMBOLS = ["mfbem_prep_create", "mfbem_prep_desc", "mfbem_prep_free", "mfbem_prep_dof"]
+PREP_SYMBOLS = ["mfbem_prep_create", "mfbem_prep_desc", "mfbem_prep_free", "mfbem_prep_dof",
+                "mfbem_prep_set_formulation", "mfbem_prep_dual"]
 
 
 class MeshDesc(ctypes.Structure):
@@ -52,6 +53,11 @@ class MeshDesc(ctypes.Structure):
         ("qsi_relative_error", c_double), ("qsi_ns_max", c_int32), ("n_precalsets", c_int32),
         ("precalset_gln", _ip), ("geometric_tolerance", c_double),
     ]
+
+
+class DualDesc(ctypes.Structure):
+    _fields_ = [("hbie", _ip), ("dual", _ip), ("dual_is_common", _ip), ("alpha", _dp), ("xi_i_hbie", _dp),
+                ("x_i_hbie", _dp), ("n_i_hbie", _dp)]
 
 
 class Stats(ctypes.Structure):
@@ -111,6 +117,10 @@ def load():
     L.mfbem_prep_desc.argtypes = [vp]
     L.mfbem_prep_free.argtypes = [vp]
     L.mfbem_prep_dof.argtypes = [vp, _ip, _ip]
+    L.mfbem_prep_set_formulation.argtypes = [vp, _ip, _dp, _dp]
+    L.mfbem_prep_dual.restype = ctypes.POINTER(DualDesc)
+    L.mfbem_prep_dual.argtypes = [vp]
+    L.mfbem_mesh_upload_dual.argtypes = [ctypes.POINTER(MeshDesc), ctypes.POINTER(DualDesc), ctypes.POINTER(vp)]
     _lib = L
     return L
 

@@ -37,9 +37,17 @@ def _p(a, t=_dp):
 
 
 class BemRegion:
-    """One BE region (ordinary boundaries, continuous quad8) on the GPU."""
+    """One BE region (ordinary boundaries, continuous quad8) on the GPU.
 
-    def __init__(self, deck, **settings):
+    formulation: None / 'sbie' (the default SBIE with MCA at mesh-boundary
+    nodes), 'hbie' or 'dual_bm' ('dual_bm_same': Burton & Miller with weight
+    alpha), for every node or as an array of codes per node (0, 1, 2); delta
+    moves the HBIE points into the elements (default 0.22540333). See
+    mfbem_mesh_upload_dual."""
+
+    FORMULATIONS = {"sbie": 0, "hbie": 1, "dual_bm": 2}
+
+    def __init__(self, deck, formulation=None, alpha=None, delta=None, **settings):
         s = dict(DEFAULT_SETTINGS)
         s.update(settings)
         self.deck = deck
@@ -57,7 +65,17 @@ class BemRegion:
         self.desc = L.mfbem_prep_desc(self._prep)
         self.n = int(self.desc.contents.n_dof)
         self._h = ctypes.c_void_p()
-        check(L.mfbem_mesh_upload(self.desc, ctypes.byref(self._h)))
+        if formulation is None:
+            check(L.mfbem_mesh_upload(self.desc, ctypes.byref(self._h)))
+            return
+        nn = deck.n_nodes
+        f = np.full(nn, self.FORMULATIONS[formulation], dtype=np.int32) if isinstance(formulation, str) else \
+            np.ascontiguousarray(formulation, dtype=np.int32)
+        a = np.ascontiguousarray(np.broadcast_to(1.0 if alpha is None else alpha, (nn,)), dtype=np.float64)
+        dl = np.ascontiguousarray(np.broadcast_to(0.22540333 if delta is None else delta, (nn,)), dtype=np.float64)
+        if L.mfbem_prep_set_formulation(self._prep, _p(f, _ip), _p(a), _p(dl)) != 0:
+            raise ValueError("formulation codes must be 0, 1 or 2")
+        check(L.mfbem_mesh_upload_dual(self.desc, L.mfbem_prep_dual(self._prep), ctypes.byref(self._h)))
 
     def close(self):
         L = _abi.load()

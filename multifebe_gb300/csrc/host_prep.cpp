@@ -97,6 +97,11 @@ struct mfbem_prep {
   std::vector<double> x_gn, csize, bball, n_gn, tbp_gn, cvalue, xi_mca, x_mca, X;
   std::vector<int32_t> element_node, n_phi, reversion, row, col, ctype, sbie, gln;
   std::vector<int32_t> dof, order;
+  // HBIE formulations (mfbem_prep_set_formulation)
+  mfbem_dual_desc dual;
+  bool has_dual = false;
+  std::vector<int32_t> hbie, dualv, common;
+  std::vector<double> alpha, xi_hbie, x_hbie, n_hbie;
 };
 
 extern "C" mfbem_prep* mfbem_prep_create(int32_t nn, const double* X, int32_t ne, const int32_t* conn,
@@ -231,6 +236,64 @@ extern "C" mfbem_prep* mfbem_prep_create(int32_t nn, const double* X, int32_t ne
   d.geometric_tolerance = geo_tol;
   return P;
 }
+
+// BEM formulation per node, as src/read_bem_formulation_selected_nodes.f90:
+// 70-260 sets it for an ordinary boundary of continuous elements: form 0 SBIE
+// (the default of assign_default_bem_formulation.f90), 1 'hbie', 2
+// 'dual_bm_same' with weight alpha; delta moves the HBIE point of each element
+// node into the element (fbem_move_xi1xi2_from_edge, the quadratic default
+// 0.22540333 when delta <= 0). The points and unit normals there follow
+// src/build_data_at_collocation_points.f90:148-160,368-376. Returns -1 for a
+// code out of range.
+extern "C" int mfbem_prep_set_formulation(mfbem_prep* P, const int32_t* form, const double* alpha,
+                                          const double* delta) {
+  const int nn = P->nn, ne = P->ne;
+  for (int s = 0; s < nn; ++s)
+    if (form[s] < 0 || form[s] > 2) return -1;
+  P->hbie.assign(nn, 0);
+  P->dualv.assign(nn, 0);
+  P->common.assign(nn, 0);
+  P->alpha.assign(nn, 1.0);
+  for (int s = 0; s < nn; ++s) {
+    P->hbie[s] = form[s] != 0;
+    P->dualv[s] = form[s] == 2;
+    P->common[s] = form[s] == 2;
+    if (alpha) P->alpha[s] = alpha[s];
+  }
+  P->xi_hbie.assign(16 * (size_t)ne, 0.0);
+  P->x_hbie.assign(24 * (size_t)ne, 0.0);
+  P->n_hbie.assign(24 * (size_t)ne, 0.0);
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 8; ++k) {
+      const int s = P->element_node[8 * e + k] - 1;
+      if (form[s] == 0) continue;
+      const double dl = (delta && delta[s] > 0.0) ? delta[s] : 0.22540333;
+      double x1 = q8xi(k, 0), x2 = q8xi(k, 1);
+      if (on_quad_edge(x1, x2)) { x1 = x1 * (1.0 - dl); x2 = x2 * (1.0 - dl); }
+      const double* x = &P->x_gn[24 * (size_t)e];
+      double xp[3], T1[3], T2[3], phi[8], N[3];
+      geom_q8(x, x1, x2, xp, T1, T2, phi);
+      cross3(T1, T2, N);
+      const double jn = norm3(N);
+      P->xi_hbie[16 * (size_t)e + 2 * k] = x1;
+      P->xi_hbie[16 * (size_t)e + 2 * k + 1] = x2;
+      for (int c = 0; c < 3; ++c) {
+        P->x_hbie[24 * (size_t)e + 3 * k + c] = xp[c];
+        P->n_hbie[24 * (size_t)e + 3 * k + c] = N[c] / jn;
+      }
+    }
+  mfbem_dual_desc& d = P->dual;
+  d.hbie = P->hbie.data();
+  d.dual = P->dualv.data();
+  d.dual_is_common = P->common.data();
+  d.alpha = P->alpha.data();
+  d.xi_i_hbie = P->xi_hbie.data();
+  d.x_i_hbie = P->x_hbie.data();
+  d.n_i_hbie = P->n_hbie.data();
+  P->has_dual = true;
+  return 0;
+}
+extern "C" const mfbem_dual_desc* mfbem_prep_dual(const mfbem_prep* p) { return p->has_dual ? &p->dual : nullptr; }
 
 extern "C" const mfbem_mesh_desc* mfbem_prep_desc(const mfbem_prep* p) { return &p->desc; }
 extern "C" void mfbem_prep_free(mfbem_prep* p) { delete p; }

@@ -27,6 +27,7 @@
 #include "mfbem_precompute.cuh"
 #include "mfbem_assemble.cuh"
 #include "mfbem_internal.cuh"
+#include "mfbem_hbie.cuh"
 #include "mfbem_lu.cuh"
 #include "mfbem_tc.cuh"
 #include "mfbem_oz.cuh"
@@ -103,6 +104,16 @@ struct mfbem_handle {
   DMesh mh;
   double* hs_c = nullptr;  // [ncp] x_i3 - hs_x
   long long hs_pts[3] = {0, 0, 0};
+  // HBIE collocation (mfbem_mesh_upload_dual): mb, the view of the HBIE
+  // points with their pair lists (1/r^7 classification), built at upload;
+  // ms[0] / ms[1], the SBIE part of the Burton & Miller points classified
+  // like sbie_auto (static) / shbie_auto (harmonic), built at the first
+  // assembly of each kind from ms_base (points only)
+  bool has_hbie = false, has_bm = false;
+  DMesh mb, ms_base, ms[2];
+  bool ms_built[2] = {false, false};
+  long long mb_pts[3] = {0, 0, 0}, ms_pts[2][3] = {{0, 0, 0}, {0, 0, 0}};
+  DevBuf parh;  // HarParH per frequency of the last harmonic assembly
 };
 
 // ---------------------------------------------------------------------------
@@ -366,6 +377,11 @@ static int build_pairs(mfbem_handle* h, DMesh& m, long long pts[3]) {
     return rc;
   }
   if (m.nsing > 0) k_sing_prep<<<nblk(m.nsing, 64), 64>>>(m, h->d_q15, sing_cp, spts); ++g_launches;
+  if (m.hbie) {
+    // HBIE view: n_i, psi_i and the edge line integrals of every singular pair
+    if ((rc = dalloc(h, (void**)&m.hsing_x, sizeof(double) * HSING_X * (m.nsing + 1)))) return rc;
+    if (m.nsing > 0) { k_hsing_prep<<<nblk(m.nsing, 64), 64>>>(m, h->d_q15); ++g_launches; }
+  }
   k_scan<long long, long long><<<1, 1024>>>(spts, m.sing_pt, (int)m.nsing); ++g_launches;
   CK(cudaMemcpy(&pts[2], m.sing_pt + m.nsing, sizeof(long long), cudaMemcpyDeviceToHost));
   // hoist the singular / adaptive point geometry out of the frequency loop when
@@ -388,7 +404,71 @@ static int build_pairs(mfbem_handle* h, DMesh& m, long long pts[3]) {
 // ---------------------------------------------------------------------------
 // upload + once-per-mesh precompute
 // ---------------------------------------------------------------------------
-extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
+// Collocation points of one view, sorted by DOF-order node (stable: the
+// builders' collocation order within a node), uploaded into v's point arrays.
+struct HostCP {
+  double x[3], xi[2], n[3], alpha;
+  int dn, kind, e, kn;
+};
+static int upload_points(mfbem_handle* h, std::vector<HostCP>& cps, int nn, DMesh& v) {
+  std::stable_sort(cps.begin(), cps.end(), [](const HostCP& a, const HostCP& b) { return a.dn < b.dn; });
+  const int ncp = (int)cps.size();
+  std::vector<int> dn_cp(nn + 1, 0), cp_dn(ncp), cp_kind(ncp), cp_e(ncp), cp_kn(ncp);
+  std::vector<double> cpx(3 * (size_t)ncp), cpxi(2 * (size_t)ncp), cpn(3 * (size_t)ncp), cpa(ncp);
+  for (int i = 0; i < ncp; ++i) {
+    const HostCP& c = cps[i];
+    dn_cp[c.dn + 1]++;
+    for (int q = 0; q < 3; ++q) {
+      cpx[3 * i + q] = c.x[q];
+      cpn[3 * i + q] = c.n[q];
+    }
+    cpxi[2 * i] = c.xi[0];
+    cpxi[2 * i + 1] = c.xi[1];
+    cp_dn[i] = c.dn;
+    cp_kind[i] = c.kind;
+    cp_e[i] = c.e;
+    cp_kn[i] = c.kn;
+    cpa[i] = c.alpha;
+  }
+  for (int i = 0; i < nn; ++i) dn_cp[i + 1] += dn_cp[i];
+  double *dx, *dxi, *dnrm, *da;
+  int *ddn, *dk, *de, *dkn, *ddc;
+  int rc;
+  if ((rc = dupload(h, &dx, cpx.data(), cpx.size())) || (rc = dupload(h, &dxi, cpxi.data(), cpxi.size())) ||
+      (rc = dupload(h, &dnrm, cpn.data(), cpn.size())) || (rc = dupload(h, &da, cpa.data(), cpa.size())) ||
+      (rc = dupload(h, &ddn, cp_dn.data(), cp_dn.size())) || (rc = dupload(h, &dk, cp_kind.data(), cp_kind.size())) ||
+      (rc = dupload(h, &de, cp_e.data(), cp_e.size())) || (rc = dupload(h, &dkn, cp_kn.data(), cp_kn.size())) ||
+      (rc = dupload(h, &ddc, dn_cp.data(), dn_cp.size())))
+    return rc;
+  v.ncp = ncp;
+  v.cpx = dx;
+  v.cp_xi = dxi;
+  v.cp_n = dnrm;
+  v.cp_alpha = da;
+  v.cp_dn = ddn;
+  v.cp_kind = dk;
+  v.cp_elem = de;
+  v.cp_kn = dkn;
+  v.dn_cp = ddc;
+  v.inc_start = nullptr;
+  v.inc_el = nullptr;
+  v.cls = nullptr;
+  v.sing_geo = nullptr;
+  v.leaf_geo = nullptr;
+  v.hsing_x = nullptr;
+  v.ft = nullptr;
+  v.ft_ok = nullptr;
+  return 0;
+}
+
+static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mfbem_handle** out);
+extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) { return upload_impl(d, nullptr, out); }
+extern "C" int mfbem_mesh_upload_dual(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mfbem_handle** out) {
+  if (!dual) return fail(MFBEM_EARG, "null dual descriptor");
+  return upload_impl(d, dual, out);
+}
+
+static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mfbem_handle** out) {
   g_err.clear();
   if (!d || !out) return fail(MFBEM_EARG, "null argument");
   *out = nullptr;
@@ -411,6 +491,7 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   DMesh& m = h->m;
   std::memset(&m, 0, sizeof(m));
   m.hs_ax = -1;
+  m.fcls = m.fadp = 5;
   m.ne = ne;
   m.ndn = nn;
   m.ndof = ndof;
@@ -461,13 +542,39 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
       dcv[2 * dof] = d->cvalue[6 * s + 2 * k];
       dcv[2 * dof + 1] = d->cvalue[6 * s + 2 * k + 1];
     }
-  // collocation points in the builders' collocation order
+  // formulation per node: 0 SBIE, 1 HBIE alone, 2 Burton & Miller (dual desc)
+  std::vector<int> form(nn, 0);
+  if (dual) {
+    if (!dual->hbie || !dual->dual || !dual->dual_is_common || !dual->alpha || !dual->xi_i_hbie || !dual->x_i_hbie ||
+        !dual->n_i_hbie) {
+      delete h;
+      return fail(MFBEM_EARG, "null member of the dual descriptor");
+    }
+    for (int s = 0; s < nn; ++s) {
+      const int hb = dual->hbie[s], du = dual->dual[s], co = dual->dual_is_common[s];
+      if (hb == 0 && du == 0 && co == 0) form[s] = 0;
+      else if (hb == 1 && du == 0 && co == 0) form[s] = 1;
+      else if (hb == 1 && du == 1 && co == 1) form[s] = 2;
+      else {
+        delete h;
+        return fail(MFBEM_EUNSUPPORTED, "node " + std::to_string(s + 1) +
+                                            ": only SBIE, 'hbie' and 'dual_bm_same' formulations are available");
+      }
+      if (form[s] == 2 && !std::isfinite(dual->alpha[s])) {
+        delete h;
+        return fail(MFBEM_EARG, "Burton & Miller alpha must be finite");
+      }
+    }
+  }
+  // collocation points in the builders' collocation order (SBIE view: nodes
+  // with the SBIE formulation only)
   struct CP { double x[3], xi[2]; int dn, kind, e, kn; };
   std::vector<CP> cps;
   std::vector<char> col(nn, 0);
   for (int e = 0; e < ne; ++e)
     for (int k = 0; k < 8; ++k) {
       int s = d->element_node[8 * e + k] - 1;
+      if (form[s] != 0) continue;
       CP c;
       c.dn = dn_of[s];
       c.e = e;
@@ -572,6 +679,49 @@ extern "C" int mfbem_mesh_upload(const mfbem_mesh_desc* d, mfbem_handle** out) {
   h->pts_adp = pts[1];
   h->pts_sing = pts[2];
   k_ft_prep<<<nblk(ncp, 128), 128>>>(m); ++g_launches;
+  // HBIE view and the Burton & Miller points' SBIE part
+  if (dual) {
+    std::vector<HostCP> hb, bm;
+    for (int e = 0; e < ne; ++e)
+      for (int k = 0; k < 8; ++k) {
+        const int s = d->element_node[8 * e + k] - 1;
+        if (form[s] == 0) continue;
+        HostCP c;
+        const double sg = rev[e] ? -1.0 : 1.0;
+        for (int q = 0; q < 3; ++q) {
+          c.x[q] = dual->x_i_hbie[24 * (size_t)e + 3 * k + q];
+          c.n[q] = sg * dual->n_i_hbie[24 * (size_t)e + 3 * k + q];
+        }
+        c.xi[0] = dual->xi_i_hbie[16 * (size_t)e + 2 * k];
+        c.xi[1] = dual->xi_i_hbie[16 * (size_t)e + 2 * k + 1];
+        if (on_quad_edge(c.xi[0], c.xi[1])) {
+          mfbem_mesh_release(h);
+          return fail(MFBEM_EARG, "the HBIE cannot be collocated at an element edge (xi_i_hbie on the edge)");
+        }
+        c.alpha = form[s] == 2 ? dual->alpha[s] : 1.0;
+        c.dn = dn_of[s];
+        c.kind = form[s] == 1 ? 2 : 3;
+        c.e = e;
+        c.kn = k;
+        hb.push_back(c);
+        if (form[s] == 2) {
+          c.kind = 1;
+          bm.push_back(c);
+        }
+      }
+    h->has_hbie = true;
+    h->has_bm = !bm.empty();
+    h->mb = m;
+    if ((rc = upload_points(h, hb, nn, h->mb))) { mfbem_mesh_release(h); return rc; }
+    h->mb.fcls = h->mb.fadp = 7;
+    h->mb.hbie = 1;
+    if ((rc = build_pairs(h, h->mb, h->mb_pts))) { mfbem_mesh_release(h); return rc; }
+    if (h->has_bm) {
+      h->ms_base = m;
+      if ((rc = upload_points(h, bm, nn, h->ms_base))) { mfbem_mesh_release(h); return rc; }
+      h->ms_base.fadp = 5;
+    }
+  }
   CK(cudaGetLastError());
   CK(cudaDeviceSynchronize());
   auto t1 = std::chrono::steady_clock::now();
@@ -603,7 +753,7 @@ extern "C" int mfbem_mesh_release(mfbem_handle* h) {
     cudaDeviceSynchronize();
     for (auto& o : h->owned) pool_give(o.first, o.second, h->dev);
     for (DevBuf* b : {&h->A, &h->b, &h->A32, &h->x, &h->r, &h->work, &h->ipiv, &h->info, &h->par, &h->nu, &h->parf,
-                      &h->pphi_f, &h->geo_f, &h->gm})
+                      &h->pphi_f, &h->geo_f, &h->gm, &h->parh})
       pool_give(b->p, b->bytes, b->dev);
     if (h->st) {
       std::lock_guard<std::mutex> lk(g_pool_mu);
@@ -617,6 +767,8 @@ extern "C" int mfbem_mesh_release(mfbem_handle* h) {
 extern "C" int mfbem_set_halfspace(mfbem_handle* h, int32_t n, double x, int32_t bc) {
   g_err.clear();
   if (!h) return fail(MFBEM_EARG, "null argument");
+  if (n != 0 && h->has_hbie)
+    return fail(MFBEM_EUNSUPPORTED, "HBIE formulations in a half-space region are not available");
   if (n < -3 || n > 3) return fail(MFBEM_EARG, "half-space hyperplane normal must be in -3..3 (0: full space)");
   if (n != 0 && bc != 1)
     return fail(MFBEM_EUNSUPPORTED, "only the traction-free half-space surface (bc = 1) is available");
@@ -698,6 +850,44 @@ static int hs_prepare_static(mfbem_handle* h) {
   return 0;
 }
 
+// Pair lists of the Burton & Miller points' SBIE part for the static (0) or
+// harmonic (1) builder: sbie_auto's classification (1/r^5 estimate) or
+// shbie_auto's (the HBIE's 1/r^7 estimate, bem_harela3d.f90:4888-4957); both
+// subdivide adaptive pairs with the SBIE's own estimate. Built once per kind.
+static int bm_prepare(mfbem_handle* h, int kind) {
+  if (!h->has_bm || h->ms_built[kind]) return 0;
+  CK(cudaDeviceSynchronize());
+  DMesh& v = h->ms[kind];
+  v = h->ms_base;
+  v.fcls = kind ? 7 : 5;
+  v.fadp = 5;
+  int rc = build_pairs(h, v, h->ms_pts[kind]);
+  if (rc) return rc;
+  CK(cudaDeviceSynchronize());
+  h->ms_built[kind] = true;
+  return 0;
+}
+
+// Test hook: pair counts of the HBIE view (regular, adaptive, singular pairs,
+// adaptive leaves; regular, adaptive, singular points), then those of the
+// Burton & Miller SBIE view of the static and the harmonic builder (zeros
+// until built).
+extern "C" int mfbem_internal_hbie_counts(mfbem_handle* h, long long* out) {
+  if (!h || !out) return fail(MFBEM_EARG, "null argument");
+  if (!h->has_hbie) return fail(MFBEM_EARG, "no HBIE collocation points");
+  const DMesh* v[3] = {&h->mb, &h->ms[0], &h->ms[1]};
+  const long long* p[3] = {h->mb_pts, h->ms_pts[0], h->ms_pts[1]};
+  for (int i = 0; i < 3; ++i) {
+    const bool b = i == 0 || h->ms_built[i - 1];
+    out[7 * i + 0] = b ? v[i]->nreg : 0;
+    out[7 * i + 1] = b ? v[i]->nadp : 0;
+    out[7 * i + 2] = b ? v[i]->nsing : 0;
+    out[7 * i + 3] = b ? v[i]->nleaf : 0;
+    for (int j = 0; j < 3; ++j) out[7 * i + 4 + j] = b ? p[i][j] : 0;
+  }
+  return 0;
+}
+
 // Assembly kernels in a fixed order (regular, adaptive, singular, free terms);
 // per-kernel device times are recorded with events on the library's stream.
 struct AsmTimes {
@@ -735,6 +925,33 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
   constexpr bool kStatic = std::is_same<POL, PolStatic>::value;
   const bool hs = kStatic && h->hs_built && h->hs_n == -3;
   const DMesh& mh = h->mh;
+  // HBIE points (their own view) and the SBIE part of the Burton & Miller
+  // points (the view of this builder's classification)
+  const bool hb = h->has_hbie;
+  const bool bm = h->has_bm && h->ms_built[kStatic ? 0 : 1];
+  if (h->has_bm && !bm) return fail(MFBEM_EARG, "Burton & Miller pair lists not prepared");
+  const DMesh& mb = h->mb;
+  const DMesh& msv = h->ms[kStatic ? 0 : 1];
+  typedef typename std::conditional<kStatic, PolHbieStatic, PolHbieHarmonic>::type PolH;
+  typedef typename std::conditional<kStatic, HsStatic, HsHarmonic>::type HsK;
+  PolH phb{};
+  HsK hsk{};
+  if (hb) {
+    if constexpr (kStatic) {
+      phb = hbie_static_policy(pol.mu, pol.nu);
+      hsk.nu = phb.nu; hsk.cted1 = phb.cted1; hsk.cted2 = phb.cted2;
+      hsk.ctes1 = phb.ctes1; hsk.ctes2 = phb.ctes2; hsk.ctes3 = phb.ctes3;
+    } else {
+      if (!pol.ph) return fail(MFBEM_EARG, "HBIE points need the d* / s* parameters");
+      phb.p = pol.p;
+      phb.ph = pol.ph;
+      hsk.p = pol.p;
+      hsk.ph = pol.ph;
+    }
+    phb.cpn = mb.cp_n;
+    phb.cpa = mb.cp_alpha;
+    phb.cpk = mb.cp_kind;
+  }
   PolHsc ph{};
   PolHscSing phs{};
   if constexpr (kStatic) {
@@ -767,6 +984,14 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
       ++g_launches;
     }
   }
+  if (bm && msv.nreg > 0) {
+    k_reg<POL, WPB><<<g, WPB * 32, 0, h->st>>>(msv, pol, nf, A, lda, astride, b, bstride);
+    ++g_launches;
+  }
+  if (hb && mb.nreg > 0) {
+    k_reg<PolH, WPB><<<g, WPB * 32, 0, h->st>>>(mb, phb, nf, A, lda, astride, b, bstride);
+    ++g_launches;
+  }
   if (tm) cudaEventRecord(tm->ev[1], h->st);
   if (m.nadp > 0) {
     if (mixed && lgf)
@@ -779,6 +1004,14 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
       k_adp<PolHsc, WPB><<<g, WPB * 32, 0, h->st>>>(mh, ph, nf, A, lda, astride, b, bstride);
       ++g_launches;
     }
+  }
+  if (bm && msv.nadp > 0) {
+    k_adp<POL, WPB><<<g, WPB * 32, 0, h->st>>>(msv, pol, nf, A, lda, astride, b, bstride);
+    ++g_launches;
+  }
+  if (hb && mb.nadp > 0) {
+    k_adp<PolH, WPB><<<g, WPB * 32, 0, h->st>>>(mb, phb, nf, A, lda, astride, b, bstride);
+    ++g_launches;
   }
   if (tm) cudaEventRecord(tm->ev[2], h->st);
   // the singular kernels keep two combo sets per point: 2 warps per block
@@ -794,8 +1027,22 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
       ++g_launches;
     }
   }
+  if (bm && msv.nsing > 0) {
+    k_sing<POL, 2><<<nblk(nw, 2), 64, 0, h->st>>>(msv, pol, nf, A, lda, astride, b, bstride);
+    ++g_launches;
+  }
+  if (hb && mb.nsing > 0) {
+    k_hsing<HsK><<<(unsigned)nw, 32, 0, h->st>>>(mb, hsk, nf, A, lda, astride, b, bstride);
+    ++g_launches;
+  }
   if (tm) cudaEventRecord(tm->ev[3], h->st);
   k_free<POL><<<nblk(nw, 128), 128, 0, h->st>>>(m, pol, d_nu, nf, A, lda, astride, b, bstride, h->d_err); ++g_launches;
+  if (hb) {
+    const HarParH* pph = nullptr;
+    if constexpr (!kStatic) pph = pol.ph;
+    k_hfree<typename POL::T><<<nblk(nw, 128), 128, 0, h->st>>>(mb, pph, nf, A, lda, astride, b, bstride);
+    ++g_launches;
+  }
   if (tm) cudaEventRecord(tm->ev[4], h->st);
   CK(cudaGetLastError());
   return 0;
@@ -882,11 +1129,25 @@ extern "C" int mfbem_assemble_staela(mfbem_handle* h, double mu, double nu, doub
   if (!h || !A || !b) return fail(MFBEM_EARG, "null argument");
   if (int rd = check_dev(h)) return rd;
   if (int rc = hs_prepare_static(h)) return rc;
+  if (int rc = bm_prepare(h, 0)) return rc;
   PolStatic pol;
   pol.k = staela_params(mu, nu);
   pol.nu = nu;
+  pol.mu = mu;
   double nuv[2] = {nu, 0.0};
   return assemble_common<false>(h, &pol, nuv, A, lda, b, flags);
+}
+
+// d* / s* parameters per frequency (HarParH) from q [nf][6] (lambda, mu, rho,
+// omega), for the HBIE points of a harmonic assembly
+static int hbie_params(mfbem_handle* h, const double* dq, int nf, const HarParH** out) {
+  *out = nullptr;
+  if (!h->has_hbie) return 0;
+  int rc;
+  if ((rc = ensure(h->parh, sizeof(HarParH) * nf))) return rc;
+  k_harparh<<<nblk(nf, 32), 32, 0, h->st>>>(dq, nf, (HarParH*)h->parh.p); ++g_launches;
+  *out = (const HarParH*)h->parh.p;
+  return 0;
 }
 
 extern "C" int mfbem_assemble_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
@@ -900,8 +1161,10 @@ extern "C" int mfbem_assemble_harela(mfbem_handle* h, const double lambda[2], co
   double* dq = (double*)((char*)h->par.p + sizeof(HarParD));
   CK(cudaMemcpyAsync(dq, q, sizeof(q), cudaMemcpyHostToDevice, h->st));
   k_harpar<<<1, 32, 0, h->st>>>(dq, 1, (HarParD*)h->par.p, zexp_thresholds()); ++g_launches;
+  if ((rc = bm_prepare(h, 1))) return rc;
   PolHarmonic pol;
   pol.p = (const HarParD*)h->par.p;
+  if ((rc = hbie_params(h, dq, 1, &pol.ph))) return rc;
   return assemble_common<true>(h, &pol, nu, A, lda, b, flags);
 }
 

@@ -46,7 +46,7 @@ struct PolStatic {
   typedef double T;
   static constexpr int NG = 6;  // independent components of g per node (u* symmetric)
   StaelaP k;
-  double nu = 0.0;
+  double nu = 0.0, mu = 0.0;
   __device__ T cte_t(int) const { return k.ctet1; }
   __device__ T cte_u(int) const { return k.cteu1; }
   __device__ T cpv(int) const { return k.ctet2; }  // coefficient of the CPV/line-integral part
@@ -68,10 +68,12 @@ struct PolStatic {
       }
   }
 };
+struct HarParH;
 struct PolHarmonic {
   typedef cd T;
   static constexpr int NG = 6;
   const HarParD* p;  // one parameter block per frequency
+  const HarParH* ph = nullptr;  // d* / s* parameters per frequency (HBIE points only)
   __device__ T cte_t(int f) const { return p[f].cte_t; }
   __device__ T cte_u(int f) const { return p[f].cte_u; }
   __device__ T cpv(int f) const { return p[f].T2[0]; }

@@ -26,6 +26,10 @@ constexpr int LEAF_D = 16;  // xs[4][2], telles1 {a,b,c,d}, telles2 {a,b,c,d}
 constexpr int SING_D = 56;  // xi_i[2], x_i[3], phi_i[8], hli[9], th[8][2], thp[8][2], pad
 constexpr int SING_I = 28;  // nsub, st[8], ngp_theta[8], off[9] (combo offsets), total, pad
 constexpr int FT_D = 10;    // cp (solid-angle part) and sum_b[3][3] of the free term
+// HBIE singular pairs: n_i[3], psi_i[8][3], then the edge line integrals
+// lli[3][3], mli1, mli2[3], mli3[3][3], mli4[3], mli5[3][3][3]
+constexpr int HSING_X = 80;
+constexpr int HX_N = 0, HX_PSI = 3, HX_LLI = 27, HX_M1 = 36, HX_M2 = 37, HX_M3 = 40, HX_M4 = 49, HX_M5 = 52;
 
 struct DMesh {
   int ne, ndn, ncp, ndof, nps, ptot, ns_max;
@@ -89,6 +93,17 @@ struct DMesh {
   // terms of collocation points on it doubled); hs_ax = -1: full space
   int hs_ax;
   double hs_x;
+  // quasi-singular estimate order of the pair classification (5: SBIE, 7:
+  // HBIE and the shared SBIE/HBIE classification of shbie_auto) and of the
+  // adaptive subdivision (5 SBIE, 7 HBIE)
+  int fcls, fadp;
+  // HBIE view: collocation points carry the unit normal n_i and the Burton &
+  // Miller weight alpha (cp_kind 2: HBIE alone, 3: Burton & Miller); the
+  // singular pairs keep their HSING_X extras
+  int hbie;
+  const double* cp_n;
+  const double* cp_alpha;
+  double* hsing_x;
 };
 
 }  // namespace mfb

@@ -24,9 +24,10 @@
 namespace mfb {
 
 // d* / s* coefficients of fbem_bem_harela3d_calculate_parameters (bem_harela3d.f90:219-283)
+// (ic2 = i / c2, the Burton & Miller factor of the harmonic builder)
 struct HarParH {
   cd S1[11], S2[11], S3[12], S4[10], S5[11];
-  cd cte_d, cte_s;
+  cd cte_d, cte_s, ic2;
 };
 __host__ __device__ inline HarParH harela_hbie_params(cd lambda, cd mu, double rho, double omega) {
   HarParH p;
@@ -95,6 +96,7 @@ __host__ __device__ inline HarParH harela_hbie_params(cd lambda, cd mu, double r
   p.S5[10] = -12.0 / k2p2;
   p.cte_d = mk(k1_4Pi);
   p.cte_s = k1_4Pi * mu;
+  p.ic2 = I / c2;
   return p;
 }
 

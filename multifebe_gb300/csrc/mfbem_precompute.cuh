@@ -58,7 +58,7 @@ __global__ void k_classify(DMesh m, const QsCurves* __restrict__ qs) {
     if (sing) {
       c = CLS_SING;
     } else {
-      int gn = qs_estimate(*qs, 2, 5, d, bx, false);
+      int gn = qs_estimate(*qs, 2, m.fcls, d, bx, false);
       int gln = max(m.gln_far[e], gn);
       if (gln <= m.ps_gln_max && gn > 0) {
         int ps = 0;
@@ -191,7 +191,7 @@ __device__ int adp_traverse(const DMesh& m, const QsCurves& qs, int e, const dou
       double cl = clen_q8(xsub, 1e-12);
       nearest_q8(xsub, cl, xi, bx, &rmin, &d, &method);
     }
-    int gn = qs_estimate(qs, 2, 5, d, bx, true);
+    int gn = qs_estimate(qs, 2, m.fadp, d, bx, true);
     bool sub = false;
     if (nd.ks == m.ns_max) {
       if (gn == 0) gn = 30;
@@ -447,6 +447,148 @@ __global__ void k_sing_prep(DMesh m, const QsCurves* q15, const int* sing_cp, lo
   }
   I[25] = off;
   npts[q] = off;
+}
+
+// ---------------------------------------------------------------- HBIE singular pairs
+// All line integrals of the HBIE interior integration over one line3 edge,
+// adaptive Telles + bisection with the 1/r^2 estimate
+// (fbem_bem_staela3d_hbie_int_li, bem_staela3d.f90:5356-5578). L: lli[3][3],
+// mli1, mli2[3], mli3[3][3], mli4[3], mli5[3][3][3] (HX_* offsets - HX_LLI).
+__device__ void hbie_line_integrals(const double* xe, const double* xi_, const double* ni, const QsCurves& q15,
+                                    double* L) {
+  struct It {
+    double s0, s1;
+    int ks;
+  };
+  It st[20];
+  int top = 0;
+  st[top++] = It{-1.0, 1.0, 1};
+  while (top > 0) {
+    It it = st[--top];
+    double xs[9];
+    if (it.ks == 1) {
+      for (int j = 0; j < 9; ++j) xs[j] = xe[j];
+    } else {
+      subdiv_l3(xe, it.s0, it.s1, xs);
+    }
+    double cl = length_l3(xs, 1e-12);
+    double bx, rmin, d;
+    int method;
+    nearest_l3(xs, cl, xi_, &bx, &rmin, &d, &method);
+    int gn = qs_estimate(q15, 1, 2, d, &bx, true);
+    bool sub = false;
+    if (it.ks == 16) {
+      if (gn == 0) gn = 30;
+    } else if (gn == 0) {
+      sub = true;
+    }
+    if (sub && top + 2 <= 20) {
+      double mid = 0.5 * (it.s0 + it.s1);
+      st[top++] = It{mid, it.s1, it.ks + 1};
+      st[top++] = It{it.s0, mid, it.ks + 1};
+      continue;
+    }
+    int gln = max(gn, 5);
+    Telles t = telles11(bx, telles_barr(d));
+    double T[52];
+    for (int j = 0; j < 52; ++j) T[j] = 0.0;
+    for (int k = 1; k <= gln; ++k) {
+      double xip, jt;
+      telles_map(t, gl11x(k, gln), xip, jt);
+      double w = gl11w(k, gln);
+      double xi = 0.5 * (1.0 - xip) * it.s0 + 0.5 * (1.0 + xip) * it.s1;
+      double js = 0.5 * (it.s1 - it.s0);
+      double ph[3], dp[3];
+      phi_l3<double>(xi, ph);
+      dphi_l3<double>(xi, dp);
+      double xp[3] = {0, 0, 0}, Tg[3] = {0, 0, 0};
+      for (int q = 0; q < 3; ++q)
+        for (int c = 0; c < 3; ++c) {
+          xp[c] = xp[c] + ph[q] * xe[3 * q + c];
+          Tg[c] = Tg[c] + dp[q] * xe[3 * q + c];
+        }
+      double jg = norm3(Tg);
+      double tt[3] = {Tg[0] / jg, Tg[1] / jg, Tg[2] / jg};
+      double rv[3] = {xp[0] - xi_[0], xp[1] - xi_[1], xp[2] - xi_[2]};
+      double r = norm3(rv);
+      double dr1 = 1.0 / r, dr3 = 1.0 / (r * r * r);
+      double dr[3] = {rv[0] * dr1, rv[1] * dr1, rv[2] * dr1};
+      double jw = jg * js * jt * w;
+      T[1] = T[1] - dr1 * tt[2] * jw;
+      T[2] = T[2] + dr1 * tt[1] * jw;
+      T[5] = T[5] - dr1 * tt[0] * jw;
+      double rxni[3] = {rv[1] * ni[2] - rv[2] * ni[1], rv[2] * ni[0] - rv[0] * ni[2], rv[0] * ni[1] - rv[1] * ni[0]};
+      double rxnit = rxni[0] * tt[0] + rxni[1] * tt[1] + rxni[2] * tt[2];
+      T[9] = T[9] + dr3 * rxnit * jw;
+      for (int a = 0; a < 3; ++a)
+        for (int b = a; b < 3; ++b) T[13 + 3 * a + b] = T[13 + 3 * a + b] + dr3 * rxnit * dr[a] * dr[b] * jw;
+      for (int ik = 0; ik < 3; ++ik) {
+        // (e_k x n_i).t and (r x e_k).t
+        const int i1 = (ik + 1) % 3, i2 = (ik + 2) % 3;
+        double ekxnit = ni[i1] * tt[i2] - ni[i2] * tt[i1];
+        double rxekt = rv[i2] * tt[i1] - rv[i1] * tt[i2];
+        T[10 + ik] = T[10 + ik] + dr1 * ekxnit * jw;
+        T[22 + ik] = T[22 + ik] + dr3 * rxekt * jw;
+        for (int a = 0; a < 3; ++a)
+          for (int b = a; b < 3; ++b)
+            T[25 + 9 * a + 3 * b + ik] = T[25 + 9 * a + 3 * b + ik] + dr1 * ekxnit * dr[a] * dr[b] * jw;
+      }
+    }
+    T[3] = -T[1];
+    T[6] = -T[2];
+    T[7] = -T[5];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < a; ++b) {
+        T[13 + 3 * a + b] = T[13 + 3 * b + a];
+        for (int k = 0; k < 3; ++k) T[25 + 9 * a + 3 * b + k] = T[25 + 9 * b + 3 * a + k];
+      }
+    for (int j = 0; j < 52; ++j) L[j] += T[j];
+  }
+}
+
+// Extras of the HBIE singular pairs (after k_sing_prep has laid out the polar
+// rule and x_i): the unit normal n_i and psi_i, the shape functions'
+// tangential gradient in the orthogonal frame v1 = t1, v2 = n_i x t1 at xi_i
+// (bem_staela3d.f90:5022-5118), and the line integrals of all four edges.
+__global__ void k_hsing_prep(DMesh m, const QsCurves* q15) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= m.nsing) return;
+  const int e = m.sing_e[q];
+  const double* x = m.ex + 24 * (size_t)e;
+  const double* D = m.sing_d + (size_t)q * SING_D;
+  double* X = m.hsing_x + (size_t)q * HSING_X;
+  double d1[8], d2[8];
+  dphi_q8<double>(D[0], D[1], d1, d2);
+  double T1[3] = {0, 0, 0}, T2[3] = {0, 0, 0};
+  for (int k = 0; k < 8; ++k)
+    for (int c = 0; c < 3; ++c) {
+      T1[c] = T1[c] + d1[k] * x[3 * k + c];
+      T2[c] = T2[c] + d2[k] * x[3 * k + c];
+    }
+  double N[3];
+  cross3(T1, T2, N);
+  double jg = norm3(N);
+  double ni[3] = {N[0] / jg, N[1] / jg, N[2] / jg};
+  double j1 = norm3(T1), j2 = norm3(T2);
+  double t1[3] = {T1[0] / j1, T1[1] / j1, T1[2] / j1}, t2[3] = {T2[0] / j2, T2[1] / j2, T2[2] / j2};
+  double v2[3];
+  cross3(ni, t1, v2);
+  double M12 = t1[0] * t2[0] + t1[1] * t2[1] + t1[2] * t2[2], M22 = v2[0] * t2[0] + v2[1] * t2[1] + v2[2] * t2[2];
+  double det = M22;  // M11 = 1, M21 = 0
+  double x11 = M22 / (j1 * det), x12 = -M12 / (j1 * det), x21 = 0.0 / (j2 * det), x22 = 1.0 / (j2 * det);
+  for (int c = 0; c < 3; ++c) X[HX_N + c] = ni[c];
+  for (int k = 0; k < 8; ++k)
+    for (int c = 0; c < 3; ++c)
+      X[HX_PSI + 3 * k + c] = (d1[k] * x11 + d2[k] * x21) * t1[c] + (d1[k] * x12 + d2[k] * x22) * v2[c];
+  double L[52];
+  for (int j = 0; j < 52; ++j) L[j] = 0.0;
+  for (int ke = 0; ke < 4; ++ke) {
+    double xe[9];
+    for (int n = 0; n < 3; ++n)
+      for (int c = 0; c < 3; ++c) xe[3 * n + c] = x[3 * q8edge(ke, n) + c];
+    hbie_line_integrals(xe, D + 2, ni, *q15, L);
+  }
+  for (int j = 0; j < 52; ++j) X[HX_LLI + j] = L[j];
 }
 
 // ---------------------------------------------------------------- free terms

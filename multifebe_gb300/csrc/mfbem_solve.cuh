@@ -1538,8 +1538,10 @@ extern "C" int mfbem_sweep_harela(mfbem_handle* h, const double lambda[2], const
   cudaEventRecord(a0, h->st);
   CK(cudaMemsetAsync(A, 0, sizeof(double2) * nn * n_freq, h->st));
   CK(cudaMemsetAsync(b, 0, sizeof(double2) * (size_t)n * n_freq, h->st));
+  if ((rc = bm_prepare(h, 1))) return rc;
   PolHarmonic pol;
   pol.p = dpar;
+  if ((rc = hbie_params(h, dq, n_freq, &pol.ph))) return rc;
   AsmTimes tm;
   long long l0 = g_launches;
   const HarParF* pf = nullptr;
@@ -1620,9 +1622,11 @@ extern "C" int mfbem_solve_staela(mfbem_handle* h, double mu, double nu, int32_t
   CK(cudaMemsetAsync(A, 0, sizeof(double) * nn, h->st));
   CK(cudaMemsetAsync(b, 0, sizeof(double) * n, h->st));
   if ((rc = hs_prepare_static(h))) return rc;
+  if ((rc = bm_prepare(h, 0))) return rc;
   PolStatic pol;
   pol.k = staela_params(mu, nu);
   pol.nu = nu;
+  pol.mu = mu;
   AsmTimes tm;
   long long l0 = g_launches;
   if ((rc = launch_assembly(h, pol, (const double*)h->nu.p, 1, A, n, 0, b, 0, &tm))) return rc;

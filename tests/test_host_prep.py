@@ -57,6 +57,41 @@ def test_prep_matches_oracle_bit_exact(oracle, deck):
         L.mfbem_prep_free(pp)
 
 
+@pytest.mark.parametrize("form", ["hbie", "dual_bm"])
+def test_prep_hbie_points_match_oracle(oracle, form):
+    """HBIE points and their unit normals (src/build_data_at_collocation_points.f90:
+    148-160,368-376) and the node members of the dual descriptor."""
+    deck = M.cube_confined_kat(2)
+    L, pp, keep = _prep(deck)
+    try:
+        nn, ne = deck.n_nodes, deck.n_elements
+        code = {"hbie": 1, "dual_bm": 2}[form]
+        f = np.full(nn, code, dtype=np.int32)
+        f[::5] = 0  # a few nodes keep the SBIE
+        a = np.linspace(0.5, 1.5, nn)
+        dl = np.full(nn, 0.3)
+        assert L.mfbem_prep_set_formulation(pp, f.ctypes.data_as(_abi._ip), a.ctypes.data_as(_abi._dp),
+                                            dl.ctypes.data_as(_abi._dp)) == 0
+        dd = L.mfbem_prep_dual(pp).contents
+        hb = np.ctypeslib.as_array(dd.hbie, shape=(nn,))
+        du = np.ctypeslib.as_array(dd.dual, shape=(nn,))
+        co = np.ctypeslib.as_array(dd.dual_is_common, shape=(nn,))
+        assert np.array_equal(hb, f != 0) and np.array_equal(du, f == 2) and np.array_equal(co, f == 2)
+        xh = np.ctypeslib.as_array(dd.x_i_hbie, shape=(24 * ne,)).reshape(ne, 8, 3)
+        nh = np.ctypeslib.as_array(dd.n_i_hbie, shape=(24 * ne,)).reshape(ne, 8, 3)
+        P = oracle.Problem(deck)
+        P.set_formulation(f, alpha=a, delta=dl)
+        x, info = P.colloc()
+        nrm = P.colloc_normals()
+        sel = np.nonzero(info[:, 1] >= 2)[0]
+        assert len(sel) == np.isin(deck.conn, np.nonzero(f)[0]).sum()
+        for i in sel:
+            assert np.abs(xh[info[i, 2], info[i, 3]] - x[i]).max() <= 1e-15
+            assert np.abs(nh[info[i, 2], info[i, 3]] - nrm[i]).max() <= 1e-15
+    finally:
+        L.mfbem_prep_free(pp)
+
+
 def test_library_exports_every_declared_symbol():
     L = _abi.load()
     hdr = open(os.path.join(ROOT, "include", "mfbem.h")).read()
