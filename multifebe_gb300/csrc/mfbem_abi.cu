@@ -305,7 +305,8 @@ static int build_pairs(mfbem_handle* h, DMesh& m, long long pts[3]) {
   const int ncp = m.ncp, ne = m.ne;
   int rc;
   if ((rc = dalloc(h, (void**)&m.cls, (size_t)ncp * ne))) return rc;
-  k_classify<<<std::min(nblk((long long)ncp * ne, 256), 152u * 16u), 256>>>(m, h->d_qs); ++g_launches;
+  // a view may hold no points (every node of the region on another formulation)
+  if (ncp > 0) { k_classify<<<std::min(nblk((long long)ncp * ne, 256), 152u * 16u), 256>>>(m, h->d_qs); ++g_launches; }
   // counts and list offsets
   int *nreg, *nadp, *nsing;
   long long* npts;
@@ -318,7 +319,7 @@ static int build_pairs(mfbem_handle* h, DMesh& m, long long pts[3]) {
   }
   long long* pts_base;
   if ((rc = dalloc(h, (void**)&pts_base, sizeof(long long) * (ncp + 1)))) return rc;
-  k_count<<<nblk(ncp, 8), 256>>>(m, nreg, nadp, nsing, npts); ++g_launches;
+  if (ncp > 0) { k_count<<<nblk(ncp, 8), 256>>>(m, nreg, nadp, nsing, npts); ++g_launches; }
   k_scan<int, int><<<1, 1024>>>(nreg, m.reg_start, ncp); ++g_launches;
   k_scan<int, int><<<1, 1024>>>(nadp, m.adp_start, ncp); ++g_launches;
   k_scan<int, int><<<1, 1024>>>(nsing, m.sing_start, ncp); ++g_launches;
@@ -342,7 +343,7 @@ static int build_pairs(mfbem_handle* h, DMesh& m, long long pts[3]) {
       (rc = dalloc(h, (void**)&sing_cp, sizeof(int) * (m.nsing + 1)))) {
     return rc;
   }
-  k_fill<<<nblk(ncp, 8), 256>>>(m, pts_base, adp_cp, sing_cp); ++g_launches;
+  if (ncp > 0) { k_fill<<<nblk(ncp, 8), 256>>>(m, pts_base, adp_cp, sing_cp); ++g_launches; }
   CK(cudaMemcpy(m.reg_pt + m.nreg, &totp, sizeof(long long), cudaMemcpyHostToDevice));
   pts[0] = totp;
   // adaptive subdivision leaves
@@ -678,7 +679,7 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
   h->pts_reg = pts[0];
   h->pts_adp = pts[1];
   h->pts_sing = pts[2];
-  k_ft_prep<<<nblk(ncp, 128), 128>>>(m); ++g_launches;
+  if (ncp > 0) { k_ft_prep<<<nblk(ncp, 128), 128>>>(m); ++g_launches; }
   // HBIE view and the Burton & Miller points' SBIE part
   if (dual) {
     std::vector<HostCP> hb, bm;
