@@ -625,7 +625,11 @@ def configs_form():
       cfg 5: harela thin slab (5190 complex DOF), both frequencies, plain and
              mixed sweeps;
       half-space footing: staela, 8x8 quad8 loaded square on the surface of a
-             half-space (complementary kernel), plain, with Love's closed form."""
+             half-space (complementary kernel), plain, with Love's closed form;
+      Burton & Miller cube: the cube 8x8 of the headline with the
+             'dual_bm_same' formulation (SBIE + i/c2 HBIE at the 3072 HBIE
+             points), four frequencies, plain and mixed sweeps, the oracle on
+             one of them."""
     from multifebe_gb300 import meshgen as M, BemRegion
     O = _oracle()
     cores = os.cpu_count()
@@ -714,6 +718,37 @@ def configs_form():
     res["note"] = ("the slab's systems are ill-conditioned (1/rcond ~1e7 at a0 = 0.2): both GPU paths differ "
                    "from the oracle by the conditioning times ~1e-12 assembly differences")
     out["cfg5_harela_slab16"] = res
+
+    deck, mat, _ = M.workload(2)
+    om = M.omega_from_a0(np.array([0.5, 1.0, 1.5, 2.0]), mat)
+    R = BemRegion(deck, formulation="dual_bm")
+    res = {"n_dof": deck.n_dof, "frequencies": len(om), "formulation": "dual_bm_same, alpha 1"}
+    X = {}
+    for prec in ("plain", "mixed"):
+        R.sweep_harela(mat, om[:1], precision=prec)  # warm-up
+        ms = []
+        for _ in range(2):
+            X[prec] = R.sweep_harela(mat, om, precision=prec)
+            st = R.last_stats
+            ms.append(st["ms_assemble"] + st["ms_factor"] + st["ms_solve"])
+        res[prec] = {"value": len(om) / (statistics.mean(ms) / 1e3), "unit": "solves/s",
+                     "ms_per_sweep": statistics.mean(ms), "ms_assemble": st["ms_assemble"],
+                     "ms_regular": st["ms_regular"], "ms_adaptive": st["ms_adaptive"],
+                     "ms_singular": st["ms_singular"], "ms_factor": st["ms_factor"], "ms_solve": st["ms_solve"]}
+    R.close()
+    P = O.Problem(deck)
+    P.set_formulation("dual_bm")
+    t0 = time.perf_counter()
+    A, b = P.assemble_harela(mat, float(om[-1]), nthreads=cores)
+    xo = O.lu_solve(A, b, overwrite=True)
+    t = time.perf_counter() - t0
+    del A
+    res["cpu_baseline"] = {"value": 1.0 / t, "unit": "solves/s", "cores": cores, "kind": "port",
+                           "sample": "one frequency (a0 = 2.0) assembled and solved by the oracle"}
+    for prec in ("plain", "mixed"):
+        res[prec]["rel_err_vs_fp64_oracle"] = rel(X[prec][-1], xo)
+        res[prec]["speedup_over_cpu"] = res[prec]["value"] / res["cpu_baseline"]["value"]
+    out["burton_miller_cube8"] = res
     return out
 
 

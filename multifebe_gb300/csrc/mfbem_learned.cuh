@@ -479,6 +479,7 @@ __global__ void __launch_bounds__(WPB * 32) k_ql_label(int n, const double* ex, 
   fm.cl = cl;
   fm.gln_far = gln_far;
   fm.ns_max = ns_max;
+  fm.fcls = fm.fadp = 5;  // SBIE kernels: the 1/r^5 estimate
   double* lbuf = scratch + (size_t)s * QL_MAXREF * LEAF_D;
   for (int r = 0; r < QL_NT; ++r) {
     int cnt = 0;
