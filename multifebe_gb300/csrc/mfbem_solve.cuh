@@ -61,7 +61,15 @@ static int tc_cgemm_run(cudaStream_t st, const float2* A, int lda, long long sA,
   const size_t wa = (size_t)batch * nmt * nkc * TQ_TW, wb = (size_t)batch * nnt * nkc * TQ_TW;
   int rc = ensure(ws, sizeof(uint32_t) * 2 * (wa + wb));
   if (rc) return rc;
-  if (raise_smem_limit((const void*)k_tc_cgemm_bulk)) return fail(MFBEM_ECUDA, "shared-memory limit of the tcgen05 GEMM");
+  // column tiles of 256 (M 128 x N 256 MMAs, two CTAs per SM) unless the
+  // update is narrower; MFBEM_TC_BN=128 selects the 128-column tiles
+  static const int bn_env = [] {
+    const char* e = getenv("MFBEM_TC_BN");
+    return e ? atoi(e) : 256;
+  }();
+  const bool wide = bn_env != 128 && nnt > 1;
+  if (raise_smem_limit(wide ? (const void*)k_tc_cgemm_bulk<2> : (const void*)k_tc_cgemm_bulk<1>))
+    return fail(MFBEM_ECUDA, "shared-memory limit of the tcgen05 GEMM");
   uint32_t* ahi = (uint32_t*)ws.p;
   uint32_t* alo = ahi + wa;
   uint32_t* bhi = alo + wa;
@@ -70,8 +78,12 @@ static int tc_cgemm_run(cudaStream_t st, const float2* A, int lda, long long sA,
   ++g_launches;
   k_tc_prep_b<<<(unsigned)std::min<size_t>((wb + 255) / 256, 152 * 32), 256, 0, st>>>(B, ldb, sB, k, n, nnt, nkc, batch, bhi, blo);
   ++g_launches;
-  k_tc_cgemm_bulk<<<dim3(nmt, nnt, batch), 128, TC_SMEM2, st>>>(ahi, alo, bhi, blo, nmt, nnt, nkc, C, ldc, sC, m, n, err,
-                                                                 g_spin_limit.load(), passes);
+  if (wide)
+    k_tc_cgemm_bulk<2><<<dim3(nmt, (nnt + 1) / 2, batch), 128, tc_smem_bulk<2>(), st>>>(
+        ahi, alo, bhi, blo, nmt, nnt, nkc, C, ldc, sC, m, n, err, g_spin_limit.load(), passes);
+  else
+    k_tc_cgemm_bulk<1><<<dim3(nmt, nnt, batch), 128, tc_smem_bulk<1>(), st>>>(ahi, alo, bhi, blo, nmt, nnt, nkc, C, ldc,
+                                                                           sC, m, n, err, g_spin_limit.load(), passes);
   ++g_launches;
   CK(cudaGetLastError());
   return 0;

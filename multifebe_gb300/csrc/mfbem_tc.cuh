@@ -247,9 +247,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm(const float2* A, int lda, l
 constexpr int TQ = 16;
 constexpr int TQ_TW = TC_BM * TQ;                  // words per tile (2048)
 constexpr int TQ_TILE_BYTES = TQ_TW * 4;           // 8 KB
-constexpr int TQ_STAGE_BYTES = 4 * TQ_TILE_BYTES;  // A hi/lo, B hi/lo
 constexpr int TQ_SBO = TQ / 4 * 128;               // 512 B
-constexpr int TC_SMEM2 = 2 * TQ_STAGE_BYTES + 64;
 
 __device__ __forceinline__ uint64_t tq_desc(uint32_t addr) {
   uint64_t d = 0;
@@ -322,23 +320,35 @@ __device__ __forceinline__ void tc_expect(uint32_t mbar, uint32_t bytes) {
 }
 
 // C -= A B from pre-split tiles (passes 3: the 3xTF32 products; 1: hi x hi
-// only, TF32-accurate); CTA (row tile, column tile, batch); thread 0
-// runs the copy / MMA pipeline (stage s: 4 x 8 KB tiles, "full" barrier fb[s]
-// completed by the bulk copies, "free" barrier mb[s] by the MMA commit), all
-// four warps run the epilogue; 64 KB of shared memory, so three CTAs share an
-// SM and one's epilogue overlaps another's MMAs.
+// only, TF32-accurate); CTA (row tile, column tile of NH x 128 columns,
+// batch); thread 0 runs the copy / MMA pipeline (stage s: the A hi / lo tiles
+// and NH B hi / lo tiles of 8 KB, "full" barrier fb[s] completed by the bulk
+// copies, "free" barrier mb[s] by the MMA commit), all four warps run the
+// epilogue. NH = 1: 64 KB of shared memory, three CTAs per SM; NH = 2: one
+// M 128 x N 256 MMA per K step (half the shared-memory operand traffic per
+// multiply-add of two N 128 MMAs, whose A is read twice), 96 KB and two CTAs
+// per SM (2 x 256 TMEM columns). Either way one CTA's epilogue overlaps
+// another's MMAs. The B tiles of one column tile's two halves are adjacent
+// 128-row blocks of the K-major layout (row group g at g x 512 B), so the
+// 256-row operand is the two pre-split tiles copied back to back; a missing
+// second half (n <= 128 in the last tile) is not copied and its columns,
+// which only feed outputs j >= n, are never stored.
+template <int NH>
 __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, const uint32_t* Alo,
                                                           const uint32_t* Bhi, const uint32_t* Blo, int nmt, int nnt,
                                                           int nkc, float2* C, int ldc, long long sC, int m, int n,
                                                           int* err, long long spin, int passes) {
+  constexpr int SB = (2 + 2 * NH) * TQ_TILE_BYTES;  // stage bytes
+  constexpr int BN = TC_BN * NH;                     // columns per CTA (TMEM columns)
   extern __shared__ __align__(1024) unsigned char tsm[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(tsm + 2 * TQ_STAGE_BYTES);  // fb[2], mb[2]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + 2 * TQ_STAGE_BYTES + 32);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tsm + 2 * SB);  // fb[2], mb[2]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + 2 * SB + 32);
   __shared__ int s_ok;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int mt = blockIdx.x, nt = blockIdx.y, bz = blockIdx.z;
+  const int nh = min(NH, nnt - nt * NH);  // B halves present
   const size_t ta0 = ((size_t)bz * nmt + mt) * nkc * TQ_TW;  // first A tile of this row tile
-  const size_t tb0 = ((size_t)bz * nnt + nt) * nkc * TQ_TW;
+  const size_t tb0 = ((size_t)bz * nnt + (size_t)nt * NH) * nkc * TQ_TW;
   const uint32_t fb[2] = {smem_u32(bars), smem_u32(bars + 1)}, mb[2] = {smem_u32(bars + 2), smem_u32(bars + 3)};
   const uint32_t st0 = smem_u32(tsm);
   if (t == 0) {
@@ -350,8 +360,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
     s_ok = 1;
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
-                 "r"(TC_BN)
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(BN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -359,18 +368,21 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
-  const uint32_t idesc = tc_idesc(TC_BM, TC_BN);
+  const uint32_t idesc = tc_idesc(TC_BM, BN);
   int issued = 0;  // chunks whose MMAs were issued (the last commit covers all)
   int loaded = 0;  // chunks whose bulk copies were issued
   int landed = 0;  // chunks whose copies were waited for
   if (t == 0) {
     auto load = [&](int kc, int sidx) {
-      const uint32_t d = st0 + sidx * TQ_STAGE_BYTES;
-      tc_expect(fb[sidx], (uint32_t)TQ_STAGE_BYTES);
+      const uint32_t d = st0 + sidx * SB;
+      tc_expect(fb[sidx], (uint32_t)((2 + 2 * nh) * TQ_TILE_BYTES));
       tc_bulk(d, Ahi + ta0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
       tc_bulk(d + TQ_TILE_BYTES, Alo + ta0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
-      tc_bulk(d + 2 * TQ_TILE_BYTES, Bhi + tb0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
-      tc_bulk(d + 3 * TQ_TILE_BYTES, Blo + tb0 + (size_t)kc * TQ_TW, TQ_TILE_BYTES, fb[sidx]);
+      for (int h = 0; h < nh; ++h) {
+        const size_t tb = tb0 + ((size_t)h * nkc + kc) * TQ_TW;
+        tc_bulk(d + (2 + h) * TQ_TILE_BYTES, Bhi + tb, TQ_TILE_BYTES, fb[sidx]);
+        tc_bulk(d + (2 + NH + h) * TQ_TILE_BYTES, Blo + tb, TQ_TILE_BYTES, fb[sidx]);
+      }
       loaded = kc + 1;
     };
     bool ok = true;
@@ -384,8 +396,8 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
       }
       if (!tc_wait(fb[s], (uint32_t)((kc >> 1) & 1), spin)) { ok = false; break; }
       landed = kc + 1;
-      const uint32_t ah = st0 + s * TQ_STAGE_BYTES, al = ah + TQ_TILE_BYTES, bh = ah + 2 * TQ_TILE_BYTES,
-                     bl = ah + 3 * TQ_TILE_BYTES;
+      const uint32_t ah = st0 + s * SB, al = ah + TQ_TILE_BYTES, bh = ah + 2 * TQ_TILE_BYTES,
+                     bl = ah + (2 + NH) * TQ_TILE_BYTES;
 #pragma unroll
       for (int ks = 0; ks < TQ / 8; ++ks) {
         const uint32_t ko = ks * 256;  // 8 tf32 = two core matrices along K
@@ -426,7 +438,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
     const int r = 32 * warp + lane;
     const int i = mt * (TC_BM / 2) + (r >> 1), comp = r & 1;
     float2* Cb = C + sC * bz;
-    for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+    for (int c0 = 0; c0 < nh * TC_BN; c0 += 32) {
       uint32_t v[32];
       const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
       asm volatile(
@@ -446,12 +458,12 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
         float cv[32];
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
-          const int j = nt * TC_BN + c0 + q;
+          const int j = nt * BN + c0 + q;
           cv[q] = j < n ? cr[2 * ((size_t)j * ldc + i) + comp] : 0.0f;
         }
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
-          const int j = nt * TC_BN + c0 + q;
+          const int j = nt * BN + c0 + q;
           if (j < n) cr[2 * ((size_t)j * ldc + i) + comp] = cv[q] - __uint_as_float(v[q]);
         }
       }
@@ -460,7 +472,11 @@ __global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, c
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+}
+template <int NH>
+constexpr int tc_smem_bulk() {
+  return 2 * (2 + 2 * NH) * TQ_TILE_BYTES + 64;
 }
 
 }  // namespace mfb

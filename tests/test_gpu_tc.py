@@ -23,7 +23,8 @@ def _tc(C, A, B, staged=0):
 
 
 @pytest.mark.parametrize("staged", [0, 1], ids=["bulk", "staged"])
-@pytest.mark.parametrize("m,n,k", [(64, 128, 16), (100, 70, 40), (300, 260, 128), (513, 129, 33), (64, 16, 1)])
+@pytest.mark.parametrize("m,n,k", [(64, 128, 16), (100, 70, 40), (300, 260, 128), (513, 129, 33), (64, 16, 1),
+                                   (257, 600, 70)])
 def test_tc_cgemm_matches_fp64_reference(m, n, k, staged):
     rng = np.random.default_rng(m * 7 + n * 3 + k)
     A = (rng.normal(size=(m, k)) + 1j * rng.normal(size=(m, k))).astype(np.complex64)
