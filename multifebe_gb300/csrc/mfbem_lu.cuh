@@ -680,61 +680,64 @@ __global__ void __launch_bounds__(128) k_trsv_diag64(const S* A, long long strid
 // ---------------------------------------------------------------------------
 // Inner panel without row interchanges (the mixed path's first attempt; its
 // factors are only a preconditioner for FP64 refinement, which falls back to
-// partial pivoting when it stalls): the kb x kb diagonal block is factorised
-// by one CTA in shared memory, then L21 = A21 inv(U11) row by row. No
-// cross-CTA pivot search per column. A zero or non-finite pivot sets info.
+// partial pivoting when it stalls), one launch: every CTA factorises the
+// kb x kb diagonal block in shared memory (the same operations in the same
+// order, so every copy is bitwise the one written back), takes the
+// reciprocals of U11's diagonal, then solves its 128 rows of
+// L21 = A21 inv(U11), one thread per row. No cross-CTA pivot search per
+// column and no launch between the diagonal block and its rows (a separate
+// diagonal kernel cost one dependent launch per 32 columns). The factorised
+// block goes back in place only after every CTA has read the original: each
+// CTA takes a ticket from cnt[b] after its load, and the last one writes and
+// resets the counter (zero on entry, zero on exit). A zero or non-finite
+// pivot sets info and leaves the rows as they are.
+// Grid: (max(1, ceil((r1 - r0) / 128)), batch).
 // ---------------------------------------------------------------------------
 template <typename S>
-__global__ void __launch_bounds__(256) k_diag_lu_nopiv(S* A, long long sA, int lda, int k, int kb, int* info) {
+__global__ void __launch_bounds__(128) k_panel_nopiv(S* A, long long sA, int lda, int k, int kb, int r0, int r1,
+                                                     int* info, int* cnt) {
   __shared__ S D[32 * 33];
-  __shared__ int s_bad;
-  const int b = blockIdx.x, t = threadIdx.x;
+  __shared__ S ur[32];  // reciprocals of U11's diagonal: the row chains multiply, no division
+  __shared__ int s_bad, s_last;
+  const int b = blockIdx.y, t = threadIdx.x;
   S* M = A + sA * b;
-  for (int e = t; e < kb * kb; e += 256) {
+  for (int e = t; e < kb * kb; e += 128) {
     const int i = e % kb, c = e / kb;
     D[c * 33 + i] = M[(size_t)(k + c) * lda + k + i];
   }
   if (t == 0) s_bad = 0;
   __syncthreads();
+  if (t == 0) s_last = atomicAdd(cnt + b, 1) == (int)gridDim.x - 1;
   for (int j = 0; j < kb; ++j) {
     const S d = D[j * 33 + j];
     const float m = (float)Sc<S>::abs1(d);
     if (!(m > 0.0f) || !isfinite(m)) {
-      if (t == 0 && !s_bad) {
+      if (t == 0) {
         s_bad = 1;
-        if (info[b] == 0) info[b] = k + j + 1;
+        if (s_last && info[b] == 0) info[b] = k + j + 1;
       }
       break;
     }
     const S rcp = Sc<S>::rcp(d);
-    for (int i = j + 1 + t; i < kb; i += 256) D[j * 33 + i] = Sc<S>::mul(D[j * 33 + i], rcp);
+    for (int i = j + 1 + t; i < kb; i += 128) D[j * 33 + i] = Sc<S>::mul(D[j * 33 + i], rcp);
     __syncthreads();
     const int w = kb - j - 1;
-    for (int e = t; e < w * w; e += 256) {
+    for (int e = t; e < w * w; e += 128) {
       const int i = j + 1 + e % w, c = j + 1 + e / w;
       D[c * 33 + i] = Sc<S>::sub(D[c * 33 + i], Sc<S>::mul(D[j * 33 + i], D[c * 33 + j]));
     }
     __syncthreads();
   }
   __syncthreads();
-  for (int e = t; e < kb * kb; e += 256) {
-    const int i = e % kb, c = e / kb;
-    M[(size_t)(k + c) * lda + k + i] = D[c * 33 + i];
+  if (s_last) {
+    for (int e = t; e < kb * kb; e += 128) {
+      const int i = e % kb, c = e / kb;
+      M[(size_t)(k + c) * lda + k + i] = D[c * 33 + i];
+    }
+    if (t == 0) cnt[b] = 0;
   }
-}
-// rows [r0, r1) of columns [k, k + kb): X := X inv(U11), U11 the upper
-// triangle (with its diagonal) of the factorised diagonal block; one thread per row
-template <typename S>
-__global__ void __launch_bounds__(128) k_trsm_runp(S* A, long long sA, int lda, int k, int kb, int r0, int r1) {
-  __shared__ S U[32 * 33];
-  __shared__ S ur[32];  // reciprocals of U11's diagonal: the row chains multiply, no division
-  const int b = blockIdx.y, t = threadIdx.x;
-  S* M = A + sA * b;
-  for (int e = t; e < kb * kb; e += 128) {
-    const int i = e % kb, c = e / kb;
-    if (i <= c) U[c * 33 + i] = M[(size_t)(k + c) * lda + k + i];
-  }
-  if (t < kb) ur[t] = Sc<S>::rcp(M[(size_t)(k + t) * lda + k + t]);
+  if (s_bad) return;
+  if (t < kb) ur[t] = Sc<S>::rcp(D[t * 33 + t]);
   __syncthreads();
   const int row = r0 + blockIdx.x * 128 + t;
   if (row >= r1) return;
@@ -747,7 +750,7 @@ __global__ void __launch_bounds__(128) k_trsm_runp(S* A, long long sA, int lda, 
     if (j < kb) {
       S v = x[j];
 #pragma unroll
-      for (int c = 0; c < j; ++c) v = Sc<S>::sub(v, Sc<S>::mul(x[c], U[j * 33 + c]));
+      for (int c = 0; c < j; ++c) v = Sc<S>::sub(v, Sc<S>::mul(x[c], D[j * 33 + c]));
       x[j] = Sc<S>::mul(v, ur[j]);
     }
   }

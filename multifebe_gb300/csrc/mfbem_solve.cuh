@@ -332,7 +332,7 @@ template <> struct IsF64<double2> { static const bool v = true; };
 
 // Workspace of the cooperative panel (barrier counters, candidate exchange,
 // error flag); per host thread, so concurrent sweeps do not share it
-static thread_local DevBuf g_lu_ws;
+static thread_local DevBuf g_lu_ws, g_pn_ws;
 // Concurrent sweeps (mfbem_sweep_harela_batch): a cooperative panel launch
 // waits on its own CTAs only, and two of them sharing the SMs could each hold
 // part of the machine; so under concurrency the panels run one at a time
@@ -394,6 +394,13 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
   const bool tc = (g_c32_mode == 3 || g_c32_mode == 1) && std::is_same<S, float2>::value;
   // single precision only: the mixed path's unpivoted first attempt
   const bool nopiv = g_nopiv && !IsF64<S>::v;
+  int* pn_cnt = nullptr;  // tickets of k_panel_nopiv, one per matrix
+  if (nopiv) {
+    int rc = ensure(g_pn_ws, sizeof(int) * batch);
+    if (rc) return rc;
+    pn_cnt = (int*)g_pn_ws.p;
+    CK(cudaMemsetAsync(pn_cnt, 0, sizeof(int) * batch, st));
+  }
   const bool oz = IsF64<S>::v && f64_default() == 0;
   if (oz) {
     int rc = oz_err_reset(st);
@@ -490,11 +497,9 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
     for (int k = K; k < KE; k += nb) {
       const int kb = std::min(nb, KE - k);
       if (nopiv) {
-        k_diag_lu_nopiv<S><<<batch, 256, 0, st>>>(A, sA, lda, k, kb, info); ++g_launches;
-        if (k + kb < n) {
-          k_trsm_runp<S><<<dim3(nblk(n - k - kb, 128), batch), 128, 0, st>>>(A, sA, lda, k, kb, k + kb, n);
-          ++g_launches;
-        }
+        const unsigned gr = std::max(1u, nblk(n - k - kb, 128));
+        k_panel_nopiv<S><<<dim3(gr, batch), 128, 0, st>>>(A, sA, lda, k, kb, k + kb, n, info, pn_cnt);
+        ++g_launches;
       } else if (use_cl) {
         const int chunk = (n - k + GC - 1) / GC;
         cudaLaunchConfig_t cfg = {};
@@ -726,9 +731,11 @@ static int trsv_err_check(cudaStream_t st) {
   return 0;
 }
 
+// no_interchanges: the factors come from the unpivoted factorisation (ipiv is
+// the identity), so the permutation step is skipped
 template <typename S>
 static int getrs_batched(cudaStream_t st, const S* A, long long sA, int lda, int n, const int* ipiv, long long sP,
-                         S* b, long long sb, int batch) {
+                         S* b, long long sb, int batch, bool no_interchanges = false) {
   // diagonal blocks of TB rows solved by one warp (k_trsv_diag64), the rows
   // below / above updated by a GEMV over the solved block
   const int TB = 64;
@@ -736,8 +743,8 @@ static int getrs_batched(cudaStream_t st, const S* A, long long sA, int lda, int
   if (raise_smem_limit((const void*)k_trsv_diag64<S, true>) || raise_smem_limit((const void*)k_trsv_diag64<S, false>))
     return fail(MFBEM_ECUDA, "shared-memory limit of the triangular solve");
   const size_t psm = (size_t)n * sizeof(int);
-  bool gathered = false;
-  if (psm <= 200 * 1024) {
+  bool gathered = no_interchanges;
+  if (!gathered && psm <= 200 * 1024) {
     int rc = ensure(g_rs_ws, (size_t)batch * n * (sizeof(int) + sizeof(S)) + 256);
     if (rc) return rc;
     if (psm > 48 * 1024 && raise_smem_limit((const void*)k_perm)) return fail(MFBEM_ECUDA, "shared-memory limit of the row permutation");
@@ -1152,7 +1159,7 @@ static int precond(MixCtx<SD, SF>& c, const SD* u, SD* out) {
   const long long nn = (long long)n * n;
   k_vecmax<SD><<<batch, 256, 0, st>>>(u, n, n, c.nrm, 4, 8); ++g_launches;
   k_scale_demote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(u, n, c.d32, n, n, c.nrm, 8, 4); ++g_launches;
-  int rc = getrs_batched<SF>(st, c.A32, nn, n, n, c.ipiv, n, c.d32, n, batch);
+  int rc = getrs_batched<SF>(st, c.A32, nn, n, n, c.ipiv, n, c.d32, n, batch, g_nopiv);
   if (rc) return rc;
   k_promote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(c.d32, n, out, n, n, c.nrm, 8, 4); ++g_launches;
   return 0;
@@ -1183,7 +1190,7 @@ static int refine_classical(MixCtx<SD, SF>& c, int* conv) {
     stall = slow ? stall + 1 : 0;
     if (stall >= 2 || it >= 30) return 0;
     k_scale_demote<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(c.r, n, c.d32, n, n, c.nrm, 8, 0); ++g_launches;
-    if ((rc = getrs_batched<SF>(st, c.A32, nn, n, n, c.ipiv, n, c.d32, n, batch))) return rc;
+    if ((rc = getrs_batched<SF>(st, c.A32, nn, n, n, c.ipiv, n, c.d32, n, batch, g_nopiv))) return rc;
     k_update<SD, SF><<<dim3(nblk(n, 256), batch), 256, 0, st>>>(c.x, n, c.d32, n, n, c.nrm, 8, 0, c.active); ++g_launches;
     // size of this correction relative to the updated x (for the forward criterion)
     k_vecmax<SF><<<batch, 256, 0, st>>>(c.d32, n, n, c.nrm, 5, 8); ++g_launches;
