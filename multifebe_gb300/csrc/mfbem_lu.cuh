@@ -848,12 +848,20 @@ __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int l
       }
     };
     if (q > 0) load_tile(0);
-    // diagonal block into shared memory (used after the contributions)
+    // diagonal block into shared memory (used after the contributions); the
+    // upper triangle's rows scaled by the reciprocals of U's diagonal, so
+    // that the substitution chain below carries no multiplication by them
+    if (!LOWER) {
+      if (t < w) rinv[t] = Sc<S>::rcp(M[(size_t)(r0 + t) * lda + r0 + t]);
+      __syncthreads();
+    }
     for (int e = t; e < 64 * 64; e += 256) {
       const int i = e & 63, j = e >> 6;
-      if (i < w && j < w) D[j * 65 + i] = M[(size_t)(r0 + j) * lda + r0 + i];
+      if (i < w && j < w) {
+        const S v = M[(size_t)(r0 + j) * lda + r0 + i];
+        D[j * 65 + i] = LOWER ? v : Sc<S>::mul(v, rinv[i]);
+      }
     }
-    if (!LOWER && t < w) rinv[t] = Sc<S>::rcp(M[(size_t)(r0 + t) * lda + r0 + t]);
     // contributions of the solved blocks, in the order they were solved:
     // thread 0 waits for the next one, then takes every later one already
     // published too, so a CTA that is behind catches up with one barrier
@@ -903,9 +911,10 @@ __global__ void __launch_bounds__(256) k_trsv_sf(const S* A, long long sA, int l
           if (l + 32 > j && l + 32 < w) x1 = Sc<S>::sub(x1, Sc<S>::mul(D[j * 65 + l + 32], xj));
         }
       } else {
+        // rows pre-scaled: x_l = y_l / u_ll - sum_{j > l} (u_lj / u_ll) x_j
+        if (l < w) x0 = Sc<S>::mul(x0, rinv[l]);
+        if (l + 32 < w) x1 = Sc<S>::mul(x1, rinv[l + 32]);
         for (int j = w - 1; j >= 0; --j) {
-          if (j < 32) { if (l == j) x0 = Sc<S>::mul(x0, rinv[j]); }
-          else { if (l + 32 == j) x1 = Sc<S>::mul(x1, rinv[j]); }
           const S xj = shfl_s(j < 32 ? x0 : x1, j & 31);
           if (l < j) x0 = Sc<S>::sub(x0, Sc<S>::mul(D[j * 65 + l], xj));
           if (l + 32 < j) x1 = Sc<S>::sub(x1, Sc<S>::mul(D[j * 65 + l + 32], xj));
