@@ -1105,13 +1105,19 @@ struct MixCtx {
   bool fresh = true;
   double maxbe = 0.0;
   std::vector<double> be;
-  // classical refinement: ||d|| / ||x|| of each system's last correction
-  // (infinity norms; +inf before the first), and ||r|| it was scaled by
-  std::vector<double> dx, rprev;
+  // classical refinement: the estimated forward error of each system relative
+  // to x (+inf before the first correction), the last correction's
+  // ||d|| / ||x|| (infinity norms) and ||r|| it was scaled by
+  std::vector<double> dx, dxraw, rprev;
 };
-// forward criterion of the classical refinement: the last correction is at
-// most this fraction of x (with the backward-error test it bounds the forward
-// error on ill-conditioned systems, where a small backward error alone does not)
+// forward criterion of the classical refinement: the estimated remaining error
+// is at most this fraction of x (with the backward-error test it bounds the
+// forward error on ill-conditioned systems, where a small backward error alone
+// does not). The estimate is the last correction's size, times rho / (1 - rho)
+// once two corrections give its contraction rho = ||d_k|| / ||d_k-1|| < 1/2:
+// the error left after d_k is about rho ||d_k|| (Higham, Accuracy and
+// Stability of Numerical Algorithms, 2nd ed., section 12.1), so a third
+// correction whose only purpose would be to show a tiny size is not needed.
 constexpr double kFwdTol = 1e-10;
 
 // r = b - A x, backward errors ||r|| / (||A|| ||x|| + ||b||) (infinity norms);
@@ -1198,9 +1204,16 @@ static int refine_classical(MixCtx<SD, SF>& c, int* conv) {
     std::vector<double> hn(8 * (size_t)batch);
     CK(cudaMemcpyAsync(hn.data(), c.nrm, sizeof(double) * 8 * batch, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if ((int)c.dxraw.size() != batch) c.dxraw.assign(batch, 1e300);
     for (int bi = 0; bi < batch; ++bi)
-      if (c.be[bi] > c.tol || c.dx[bi] > kFwdTol)
-        c.dx[bi] = c.rprev[bi] * hn[8 * bi + 5] / std::max(hn[8 * bi + 6], 1e-300);
+      if (c.be[bi] > c.tol || c.dx[bi] > kFwdTol) {
+        const double raw = c.rprev[bi] * hn[8 * bi + 5] / std::max(hn[8 * bi + 6], 1e-300);
+        const double prev = c.dxraw[bi];
+        c.dxraw[bi] = raw;
+        double est = raw;
+        if (prev < 1e300 && prev > 0.0 && raw / prev < 0.5) est = raw / prev / (1.0 - raw / prev) * raw;
+        c.dx[bi] = est;
+      }
     ++c.it;
   }
 }
@@ -1462,6 +1475,7 @@ static int solve_batch(mfbem_handle* h, SD* A, int n, int batch, const SD* b, SD
     auto restart = [&]() -> int {  // refinement from x = 0 after a refactorisation
       c.fresh = true;
       c.dx.clear();
+      c.dxraw.clear();
       c.rprev.clear();
       CK(cudaMemsetAsync(x, 0, sizeof(SD) * (size_t)n * batch, st));
       return 0;

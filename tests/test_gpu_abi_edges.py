@@ -85,10 +85,13 @@ def test_one_frequency_sweep_matches_the_multi_frequency_sweep():
     R = BemRegion(d)
     mat = M.viscoelastic(1.0, 0.25, 1.0, 0.05)
     om = M.omega_from_a0(np.linspace(0.1, 2.0, 6), mat)
-    for prec in ("plain", "mixed"):
+    # plain: the same FP64 factorisation either way; mixed: each run's FP32
+    # factors (blocked per batch size) differ, and the refinement stops once
+    # the estimated forward error is below 1e-10
+    for prec, tol in (("plain", 1e-11), ("mixed", 1e-9)):
         X = R.sweep_harela(mat, om, precision=prec)
         x3 = R.sweep_harela(mat, om[3:4], precision=prec)
-        assert np.abs(x3[0] - X[3]).max() / np.abs(X[3]).max() < 1e-11
+        assert np.abs(x3[0] - X[3]).max() / np.abs(X[3]).max() < tol
     R.close()
 
 
