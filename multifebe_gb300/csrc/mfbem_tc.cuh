@@ -333,8 +333,9 @@ __device__ __forceinline__ void tc_expect(uint32_t mbar, uint32_t bytes) {
 // 256-row operand is the two pre-split tiles copied back to back; a missing
 // second half (n <= 128 in the last tile) is not copied and its columns,
 // which only feed outputs j >= n, are never stored.
+// (NH = 1: registers capped for three CTAs per SM, the shared-memory limit)
 template <int NH>
-__global__ void __launch_bounds__(128, 1) k_tc_cgemm_bulk(const uint32_t* Ahi, const uint32_t* Alo,
+__global__ void __launch_bounds__(128, NH == 1 ? 3 : 2) k_tc_cgemm_bulk(const uint32_t* Ahi, const uint32_t* Alo,
                                                           const uint32_t* Bhi, const uint32_t* Blo, int nmt, int nnt,
                                                           int nkc, float2* C, int ldc, long long sC, int m, int n,
                                                           int* err, long long spin, int passes) {
