@@ -225,12 +225,24 @@ static int oz_err_check(cudaStream_t st) {
 // allocation, binary64 epilogue; about 30-40 µs) exceeds the SIMT kernel's
 // time there (small static systems, the depth-16 updates inside an outer block).
 constexpr double kOzMinMacs = 16777216.0;  // 2^24
+// smallest update depth taken by the Ozaki scheme (MFBEM_OZ_MIN_K; 0, the
+// default: any depth above the size threshold). Sending the depth-16 and
+// depth-32 updates to the binary64 SIMT kernel instead made the plain
+// factorisation slower (20 cube systems 232.8 -> 317 ms, the 14883-row patch
+// 676 -> 795 ms at depth < 33).
+static int oz_min_depth() {
+  static const int v = [] {
+    const char* e = getenv("MFBEM_OZ_MIN_K");
+    return e ? std::max(0, atoi(e)) : 0;
+  }();
+  return v;
+}
 template <typename S>
 static int f64_gemm(cudaStream_t st, int m, int n, int k, const S* A, int lda, long long sA, const S* B, int ldb,
                     long long sB, S* C, int ldc, long long sC, int batch) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
   const double macs = (double)m * n * k * batch * (std::is_same<S, double2>::value ? 4.0 : 1.0);
-  if (f64_default() == 1 || macs < kOzMinMacs)
+  if (f64_default() == 1 || macs < kOzMinMacs || k < oz_min_depth())
     return gemm_simt<S>(st, m, n, k, A, lda, sA, B, ldb, sB, C, ldc, sC, batch);
   return oz_gemm_run<std::is_same<S, double2>::value>(st, A, lda, sA, B, ldb, sB, C, ldc, sC, m, n, k, batch);
 }
@@ -470,7 +482,7 @@ static int getrf_batched(cudaStream_t st, S* A, long long sA, int lda, int n, in
     if (nc <= 0) return 0;
     if constexpr (IsF64<S>::v) {
       const double macs = (double)kb * kb * nc * batch * (std::is_same<S, double2>::value ? 4.0 : 1.0);
-      if (oz && nc >= 128 && macs >= kOzMinMacs / 4) {
+      if (oz && nc >= 128 && macs >= kOzMinMacs / 4 && kb >= oz_min_depth()) {
         const size_t tb = sizeof(S) * 1024 * (size_t)batch, wb = sizeof(S) * (size_t)kb * nc * batch;
         int rc = ensure(g_trsm_ws, tb + wb);
         if (rc) return rc;
