@@ -130,8 +130,25 @@ int mfbem_mesh_release(mfbem_handle* h);
                 the static builder (build_lse_mechanics_bem_staela.f90:835-841)
                 and alpha i / c2 in the harmonic one, c2 = sqrt(mu / rho) the
                 complex S-wave speed (build_lse_mechanics_bem_harela.f90:1174-1181).
-   Other combinations (crack-like boundaries, 'dual_bm_mixed') return
-   MFBEM_EUNSUPPORTED. The HBIE points are classified as hbie_auto does
+     (1, 2, 1)  a node of a crack-like boundary (fbem_dual_boundary,
+                src/assign_default_bem_formulation.f90:94-128): the SBIE and
+                the HBIE at the same points x_i_hbie, each its own equation.
+   Other combinations ('dual_bm_mixed') return MFBEM_EUNSUPPORTED.
+   Crack-like boundaries (boundary class cracklike, src/read_boundaries.f90:
+   105; dual BEM): crack_el marks their elements (NULL: none), whose nodes
+   belong to no ordinary element and carry two faces, face 1 with the
+   element normal and face 2 with the reversed one; ctype2 / cvalue2 are
+   node(sn)%ctype(k,2) / %cvalue(k,1,2) of face 2. A crack node takes six
+   rows r..r+5 in the reference's order: row(k,1) = r + 2(k-1) its SBIE,
+   row(k,2) = row(k,1) + 1 its HBIE, face 1's unknown of direction k in
+   column row(k,1) (the mesh descriptor's row / col) and face 2's in
+   row(k,1) + 1 (src/build_auxiliary_variables_mechanics_static.f90:146-207);
+   n_dof = 3 n_nodes + 3 (crack nodes). Face 2 takes -h, g, -m, l of the
+   element (src/build_lse_mechanics_bem_staela.f90:883-887); the SBIE
+   equation takes 1/2 phi(xi_i) on both faces' u, the HBIE -1/2 phi(xi_i) on
+   face 1's t and +1/2 phi(xi_i) on face 2's (staela.f90:195-204,
+   build_lse_mechanics_bem_harela.f90:344-360). Internal points of such a
+   region are MFBEM_EUNSUPPORTED. The HBIE points are classified as hbie_auto does
    (lib/fbem/src/bem_staela3d.f90:4307-4373, 1/r^7 estimate); the element
    holding a point takes the interior (hypersingular) integration
    (bem_staela3d.f90:4918-5353, bem_harela3d.f90:3169-3630); the SBIE part of
@@ -147,6 +164,9 @@ typedef struct mfbem_dual_desc {
   const double* xi_i_hbie;       /* [n_elements][8][2] */
   const double* x_i_hbie;        /* [n_elements][8][3] */
   const double* n_i_hbie;        /* [n_elements][8][3] */
+  const int32_t* crack_el;       /* [n_elements] 0/1, may be NULL (no crack-like boundary) */
+  const int32_t* ctype2;         /* [n_nodes][3] face 2 (read for crack nodes) */
+  const double* cvalue2;         /* [n_nodes][3][2] face 2 */
 } mfbem_dual_desc;
 int mfbem_mesh_upload_dual(const mfbem_mesh_desc* desc, const mfbem_dual_desc* dual, mfbem_handle** out);
 

@@ -40,7 +40,7 @@ ABI_SYMBOLS = [
     "mfbem_nso_write", "mfbem_nso_error", "mfbem_fortran_format", "mfbem_set_halfspace", "mfbem_mesh_upload_dual",
 ]
 PREP_SYMBOLS = ["mfbem_prep_create", "mfbem_prep_desc", "mfbem_prep_free", "mfbem_prep_dof",
-                "mfbem_prep_set_formulation", "mfbem_prep_dual"]
+                "mfbem_prep_set_formulation", "mfbem_prep_set_crack", "mfbem_prep_dof2", "mfbem_prep_dual"]
 
 
 class MeshDesc(ctypes.Structure):
@@ -57,7 +57,7 @@ class MeshDesc(ctypes.Structure):
 
 class DualDesc(ctypes.Structure):
     _fields_ = [("hbie", _ip), ("dual", _ip), ("dual_is_common", _ip), ("alpha", _dp), ("xi_i_hbie", _dp),
-                ("x_i_hbie", _dp), ("n_i_hbie", _dp)]
+                ("x_i_hbie", _dp), ("n_i_hbie", _dp), ("crack_el", _ip), ("ctype2", _ip), ("cvalue2", _dp)]
 
 
 class Stats(ctypes.Structure):
@@ -118,6 +118,8 @@ def load():
     L.mfbem_prep_free.argtypes = [vp]
     L.mfbem_prep_dof.argtypes = [vp, _ip, _ip]
     L.mfbem_prep_set_formulation.argtypes = [vp, _ip, _dp, _dp]
+    L.mfbem_prep_set_crack.argtypes = [vp, _ip, _ip, _dp]
+    L.mfbem_prep_dof2.argtypes = [vp, _ip]
     L.mfbem_prep_dual.restype = ctypes.POINTER(DualDesc)
     L.mfbem_prep_dual.argtypes = [vp]
     L.mfbem_mesh_upload_dual.argtypes = [ctypes.POINTER(MeshDesc), ctypes.POINTER(DualDesc), ctypes.POINTER(vp)]

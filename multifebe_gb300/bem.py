@@ -42,12 +42,14 @@ class BemRegion:
     formulation: None / 'sbie' (the default SBIE with MCA at mesh-boundary
     nodes), 'hbie' or 'dual_bm' ('dual_bm_same': Burton & Miller with weight
     alpha), for every node or as an array of codes per node (0, 1, 2); delta
-    moves the HBIE points into the elements (default 0.22540333). See
-    mfbem_mesh_upload_dual."""
+    moves the HBIE points into the elements (default 0.22540333). crack:
+    (crack_el [ne] bool, ctype2 [nn, 3], cvalue2 [nn, 3]) marks the elements
+    of crack-like boundaries (dual BEM) and gives face 2's conditions; the
+    deck's ctype / cvalue are face 1's. See mfbem_mesh_upload_dual."""
 
     FORMULATIONS = {"sbie": 0, "hbie": 1, "dual_bm": 2}
 
-    def __init__(self, deck, formulation=None, alpha=None, delta=None, **settings):
+    def __init__(self, deck, formulation=None, alpha=None, delta=None, crack=None, **settings):
         s = dict(DEFAULT_SETTINGS)
         s.update(settings)
         self.deck = deck
@@ -63,18 +65,33 @@ class BemRegion:
                                          s["qsi_ns_max"], len(self._gl), _p(self._gl, _ip),
                                          s["geometric_tolerance"])
         self.desc = L.mfbem_prep_desc(self._prep)
-        self.n = int(self.desc.contents.n_dof)
         self._h = ctypes.c_void_p()
-        if formulation is None:
+        self.crack = None
+        if formulation is None and crack is None:
+            self.n = int(self.desc.contents.n_dof)
             check(L.mfbem_mesh_upload(self.desc, ctypes.byref(self._h)))
             return
         nn = deck.n_nodes
+        if formulation is None:
+            formulation = "sbie"
         f = np.full(nn, self.FORMULATIONS[formulation], dtype=np.int32) if isinstance(formulation, str) else \
             np.ascontiguousarray(formulation, dtype=np.int32)
         a = np.ascontiguousarray(np.broadcast_to(1.0 if alpha is None else alpha, (nn,)), dtype=np.float64)
         dl = np.ascontiguousarray(np.broadcast_to(0.22540333 if delta is None else delta, (nn,)), dtype=np.float64)
         if L.mfbem_prep_set_formulation(self._prep, _p(f, _ip), _p(a), _p(dl)) != 0:
             raise ValueError("formulation codes must be 0, 1 or 2")
+        if crack is not None:
+            ce = np.ascontiguousarray(np.asarray(crack[0], dtype=bool), dtype=np.int32)
+            ct2 = np.ascontiguousarray(crack[1], dtype=np.int32)
+            cv2 = np.ascontiguousarray(crack[2], dtype=np.complex128)
+            rc = L.mfbem_prep_set_crack(self._prep, _p(ce, _ip), _p(ct2, _ip), _p(cv2.view(np.float64)))
+            if rc == -1:
+                raise ValueError("a node of a crack-like element also belongs to an ordinary element")
+            if rc != 0:
+                raise ValueError("ctype2 must be 0 or 1")
+            self.crack = (ce.astype(bool), ct2, cv2)
+            self._crack_keep = (ce, ct2, cv2)
+        self.n = int(self.desc.contents.n_dof)
         check(L.mfbem_mesh_upload_dual(self.desc, L.mfbem_prep_dual(self._prep), ctypes.byref(self._h)))
 
     def close(self):
@@ -228,6 +245,26 @@ class BemRegion:
         u[~known_u] = vals[~known_u]
         t[known_u] = vals[known_u]
         return u, t
+
+    def solution_faces(self, x):
+        """(u1, t1, u2, t2) [n_nodes, 3] of a region with crack-like
+        boundaries: face 1 of every node (solution()) and face 2 of the crack
+        nodes (zero elsewhere)."""
+        u1, t1 = self.solution(x)
+        ce, ct2, cv2 = self.crack
+        nn = self.deck.n_nodes
+        d2 = np.zeros(3 * nn, dtype=np.int32)
+        _abi.load().mfbem_prep_dof2(self._prep, _p(d2, _ip))
+        d2 = d2.reshape(nn, 3)
+        cplx = np.iscomplexobj(x)
+        cv = cv2 if cplx else cv2.real
+        on = d2 >= 0
+        known_u = on & (ct2 == 0)
+        known_t = on & (ct2 == 1)
+        vals = np.where(on, x[np.maximum(d2, 0)], 0)
+        u2 = np.where(known_u, cv, np.where(known_t, vals, 0)).astype(u1.dtype)
+        t2 = np.where(known_t, cv, np.where(known_u, vals, 0)).astype(u1.dtype)
+        return u1, t1, u2, t2
 
 
 class LseState:

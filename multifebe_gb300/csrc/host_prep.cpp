@@ -6,7 +6,7 @@
 //   - mesh-boundary nodes and default formulations
 //     (lib/fbem/src/data_structures.f90:1433-1495, src/assign_default_bem_formulation.f90:76-93);
 //   - MCA collocation points (src/build_data_at_collocation_points.f90:125-147,174-223);
-//   - DOF numbering (src/build_auxiliary_variables_mechanics_static.f90:60-140).
+//   - DOF numbering (src/build_auxiliary_variables_mechanics_static.f90:60-207).
 // The results are the inputs of mfbem_mesh_upload; none of it runs per frequency.
 #include "mfbem_host.h"
 
@@ -97,12 +97,117 @@ struct mfbem_prep {
   std::vector<double> x_gn, csize, bball, n_gn, tbp_gn, cvalue, xi_mca, x_mca, X;
   std::vector<int32_t> element_node, n_phi, reversion, row, col, ctype, sbie, gln;
   std::vector<int32_t> dof, order;
-  // HBIE formulations (mfbem_prep_set_formulation)
+  // HBIE formulations (mfbem_prep_set_formulation) and crack-like boundaries
+  // (mfbem_prep_set_crack)
   mfbem_dual_desc dual;
   bool has_dual = false;
-  std::vector<int32_t> hbie, dualv, common;
-  std::vector<double> alpha, xi_hbie, x_hbie, n_hbie;
+  std::vector<int32_t> form, hbie, dualv, common;
+  std::vector<double> alpha, delta, xi_hbie, x_hbie, n_hbie;
+  std::vector<int32_t> crack_el, crack_node, ctype2, dof2;
+  std::vector<double> cvalue2;
 };
+
+namespace {
+
+// DOF numbering, src/build_auxiliary_variables_mechanics_static.f90:60-207:
+// nodes in order of first appearance over the elements; an ordinary node
+// takes rows r, r+1, r+2 (col = row of the unknown of each direction); a
+// crack-like node r..r+5 with row(k,1) = r + 2(k-1) (SBIE), row(k,2) =
+// row(k,1) + 1 (HBIE) and face 2's unknown in column row(k,1) + 1.
+void number_dofs(mfbem_prep* P) {
+  const int nn = P->nn, ne = P->ne;
+  const bool ck = !P->crack_node.empty();
+  P->row.assign(3 * (size_t)nn, 0);
+  P->col.assign(6 * (size_t)nn, 0);
+  P->dof.assign(3 * (size_t)nn, -1);
+  P->dof2.assign(3 * (size_t)nn, -1);
+  P->order.clear();
+  std::vector<char> used(nn, 0);
+  int r = 1;
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 8; ++k) {
+      const int s = P->element_node[8 * e + k] - 1;
+      if (used[s]) continue;
+      used[s] = 1;
+      P->order.push_back(s);
+      const int w = (ck && P->crack_node[s]) ? 2 : 1;
+      for (int c = 0; c < 3; ++c) {
+        const int rc = r + w * c;
+        P->row[3 * (size_t)s + c] = rc;
+        if (P->ctype[3 * (size_t)s + c] == 0) P->col[6 * (size_t)s + 3 + c] = rc;
+        else P->col[6 * (size_t)s + c] = rc;
+        P->dof[3 * (size_t)s + c] = rc - 1;
+        if (w == 2) P->dof2[3 * (size_t)s + c] = rc;
+      }
+      r += 3 * w;
+    }
+  P->desc.n_dof = r - 1;
+  P->desc.row = P->row.data();
+  P->desc.col = P->col.data();
+}
+
+// The dual descriptor from the formulation codes and the crack-like
+// boundaries: HBIE points of every node with an HBIE, xi moved from the
+// element edge by delta (fbem_move_xi1xi2_from_edge; quadratic default
+// 0.22540333, assign_default_bem_formulation.f90:42) and the unit normal
+// there (src/build_data_at_collocation_points.f90:148-160,368-376).
+void rebuild_dual(mfbem_prep* P) {
+  const int nn = P->nn, ne = P->ne;
+  if (P->form.empty()) P->form.assign(nn, 0);
+  if (P->alpha.empty()) P->alpha.assign(nn, 1.0);
+  if (P->delta.empty()) P->delta.assign(nn, 0.0);
+  const bool ck = !P->crack_node.empty();
+  P->hbie.assign(nn, 0);
+  P->dualv.assign(nn, 0);
+  P->common.assign(nn, 0);
+  for (int s = 0; s < nn; ++s) {
+    if (ck && P->crack_node[s]) {
+      P->hbie[s] = 1;
+      P->dualv[s] = 2;
+      P->common[s] = 1;
+      continue;
+    }
+    P->hbie[s] = P->form[s] != 0;
+    P->dualv[s] = P->form[s] == 2;
+    P->common[s] = P->form[s] == 2;
+  }
+  P->xi_hbie.assign(16 * (size_t)ne, 0.0);
+  P->x_hbie.assign(24 * (size_t)ne, 0.0);
+  P->n_hbie.assign(24 * (size_t)ne, 0.0);
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 8; ++k) {
+      const int s = P->element_node[8 * e + k] - 1;
+      if (!P->hbie[s]) continue;
+      const double dl = P->delta[s] > 0.0 ? P->delta[s] : 0.22540333;
+      double x1 = q8xi(k, 0), x2 = q8xi(k, 1);
+      if (on_quad_edge(x1, x2)) { x1 = x1 * (1.0 - dl); x2 = x2 * (1.0 - dl); }
+      const double* x = &P->x_gn[24 * (size_t)e];
+      double xp[3], T1[3], T2[3], phi[8], N[3];
+      geom_q8(x, x1, x2, xp, T1, T2, phi);
+      cross3(T1, T2, N);
+      const double jn = norm3(N);
+      P->xi_hbie[16 * (size_t)e + 2 * k] = x1;
+      P->xi_hbie[16 * (size_t)e + 2 * k + 1] = x2;
+      for (int c = 0; c < 3; ++c) {
+        P->x_hbie[24 * (size_t)e + 3 * k + c] = xp[c];
+        P->n_hbie[24 * (size_t)e + 3 * k + c] = N[c] / jn;
+      }
+    }
+  mfbem_dual_desc& d = P->dual;
+  d.hbie = P->hbie.data();
+  d.dual = P->dualv.data();
+  d.dual_is_common = P->common.data();
+  d.alpha = P->alpha.data();
+  d.xi_i_hbie = P->xi_hbie.data();
+  d.x_i_hbie = P->x_hbie.data();
+  d.n_i_hbie = P->n_hbie.data();
+  d.crack_el = ck ? P->crack_el.data() : nullptr;
+  d.ctype2 = ck ? P->ctype2.data() : nullptr;
+  d.cvalue2 = ck ? P->cvalue2.data() : nullptr;
+  P->has_dual = true;
+}
+
+}  // namespace
 
 extern "C" mfbem_prep* mfbem_prep_create(int32_t nn, const double* X, int32_t ne, const int32_t* conn,
                                          const int32_t* ctype, const double* cvalue, double qsi_re, int32_t ns_max,
@@ -187,33 +292,13 @@ extern "C" mfbem_prep* mfbem_prep_create(int32_t nn, const double* X, int32_t ne
         for (int c = 0; c < 3; ++c) xp[c] = xp[c] + phi[q] * P->x_gn[24 * (size_t)e + 3 * q + c];
       for (int c = 0; c < 3; ++c) P->x_mca[24 * (size_t)e + 3 * k + c] = xp[c];
     }
-  // DOF numbering: node-wise, first appearance over elements
-  P->row.assign(3 * (size_t)nn, 0);
-  P->col.assign(6 * (size_t)nn, 0);
   P->ctype.assign(ctype, ctype + 3 * (size_t)nn);
   P->cvalue.assign(cvalue, cvalue + 6 * (size_t)nn);
-  P->dof.assign(3 * (size_t)nn, -1);
-  std::vector<char> used(nn, 0);
-  int r = 1;
-  for (int e = 0; e < ne; ++e)
-    for (int k = 0; k < 8; ++k) {
-      int s = conn[8 * e + k];
-      if (used[s]) continue;
-      used[s] = 1;
-      P->order.push_back(s);
-      for (int c = 0; c < 3; ++c) {
-        P->row[3 * (size_t)s + c] = r;
-        if (ctype[3 * (size_t)s + c] == 0) P->col[6 * (size_t)s + 3 + c] = r;
-        else P->col[6 * (size_t)s + c] = r;
-        P->dof[3 * (size_t)s + c] = r - 1;
-        ++r;
-      }
-    }
+  number_dofs(P);
   P->gln.assign(ps_gln, ps_gln + n_ps);
   mfbem_mesh_desc& d = P->desc;
   d.n_nodes = nn;
   d.n_elements = ne;
-  d.n_dof = r - 1;
   d.x_gn = P->x_gn.data();
   d.element_node = P->element_node.data();
   d.csize = P->csize.data();
@@ -222,8 +307,6 @@ extern "C" mfbem_prep* mfbem_prep_create(int32_t nn, const double* X, int32_t ne
   d.reversion = P->reversion.data();
   d.n_gn = P->n_gn.data();
   d.tbp_gn = P->tbp_gn.data();
-  d.row = P->row.data();
-  d.col = P->col.data();
   d.ctype = P->ctype.data();
   d.cvalue = P->cvalue.data();
   d.sbie = P->sbie.data();
@@ -241,56 +324,50 @@ extern "C" mfbem_prep* mfbem_prep_create(int32_t nn, const double* X, int32_t ne
 // 70-260 sets it for an ordinary boundary of continuous elements: form 0 SBIE
 // (the default of assign_default_bem_formulation.f90), 1 'hbie', 2
 // 'dual_bm_same' with weight alpha; delta moves the HBIE point of each element
-// node into the element (fbem_move_xi1xi2_from_edge, the quadratic default
-// 0.22540333 when delta <= 0). The points and unit normals there follow
-// src/build_data_at_collocation_points.f90:148-160,368-376. Returns -1 for a
-// code out of range.
+// node into the element (the quadratic default 0.22540333 when delta <= 0).
+// Returns -1 for a code out of range.
 extern "C" int mfbem_prep_set_formulation(mfbem_prep* P, const int32_t* form, const double* alpha,
                                           const double* delta) {
-  const int nn = P->nn, ne = P->ne;
+  const int nn = P->nn;
   for (int s = 0; s < nn; ++s)
     if (form[s] < 0 || form[s] > 2) return -1;
-  P->hbie.assign(nn, 0);
-  P->dualv.assign(nn, 0);
-  P->common.assign(nn, 0);
+  P->form.assign(form, form + nn);
   P->alpha.assign(nn, 1.0);
+  P->delta.assign(nn, 0.0);
   for (int s = 0; s < nn; ++s) {
-    P->hbie[s] = form[s] != 0;
-    P->dualv[s] = form[s] == 2;
-    P->common[s] = form[s] == 2;
     if (alpha) P->alpha[s] = alpha[s];
+    if (delta) P->delta[s] = delta[s];
   }
-  P->xi_hbie.assign(16 * (size_t)ne, 0.0);
-  P->x_hbie.assign(24 * (size_t)ne, 0.0);
-  P->n_hbie.assign(24 * (size_t)ne, 0.0);
+  rebuild_dual(P);
+  return 0;
+}
+
+// Crack-like boundary (dual BEM): crack_el [ne] marks its elements, ctype2 /
+// cvalue2 [nn][3] the conditions of face 2 (read for its nodes). Renumbers
+// the DOF (six per crack node) and sets its nodes' formulation
+// (src/assign_default_bem_formulation.f90:94-128; delta of their points as
+// given to mfbem_prep_set_formulation, else the quadratic default).
+// Returns -1 if a node of a crack-like element also belongs to an ordinary
+// one, -2 for a ctype2 other than 0 / 1.
+extern "C" int mfbem_prep_set_crack(mfbem_prep* P, const int32_t* crack_el, const int32_t* ctype2,
+                                    const double* cvalue2) {
+  const int nn = P->nn, ne = P->ne;
+  std::vector<int32_t> cn(nn, 0), on(nn, 0);
   for (int e = 0; e < ne; ++e)
-    for (int k = 0; k < 8; ++k) {
-      const int s = P->element_node[8 * e + k] - 1;
-      if (form[s] == 0) continue;
-      const double dl = (delta && delta[s] > 0.0) ? delta[s] : 0.22540333;
-      double x1 = q8xi(k, 0), x2 = q8xi(k, 1);
-      if (on_quad_edge(x1, x2)) { x1 = x1 * (1.0 - dl); x2 = x2 * (1.0 - dl); }
-      const double* x = &P->x_gn[24 * (size_t)e];
-      double xp[3], T1[3], T2[3], phi[8], N[3];
-      geom_q8(x, x1, x2, xp, T1, T2, phi);
-      cross3(T1, T2, N);
-      const double jn = norm3(N);
-      P->xi_hbie[16 * (size_t)e + 2 * k] = x1;
-      P->xi_hbie[16 * (size_t)e + 2 * k + 1] = x2;
-      for (int c = 0; c < 3; ++c) {
-        P->x_hbie[24 * (size_t)e + 3 * k + c] = xp[c];
-        P->n_hbie[24 * (size_t)e + 3 * k + c] = N[c] / jn;
-      }
-    }
-  mfbem_dual_desc& d = P->dual;
-  d.hbie = P->hbie.data();
-  d.dual = P->dualv.data();
-  d.dual_is_common = P->common.data();
-  d.alpha = P->alpha.data();
-  d.xi_i_hbie = P->xi_hbie.data();
-  d.x_i_hbie = P->x_hbie.data();
-  d.n_i_hbie = P->n_hbie.data();
-  P->has_dual = true;
+    for (int k = 0; k < 8; ++k) (crack_el[e] ? cn : on)[P->element_node[8 * e + k] - 1] = 1;
+  for (int s = 0; s < nn; ++s) {
+    if (cn[s] && on[s]) return -1;
+    if (cn[s])
+      for (int c = 0; c < 3; ++c)
+        if (ctype2[3 * s + c] != 0 && ctype2[3 * s + c] != 1) return -2;
+  }
+  P->crack_el.assign(ne, 0);
+  for (int e = 0; e < ne; ++e) P->crack_el[e] = crack_el[e] ? 1 : 0;
+  P->crack_node = cn;
+  P->ctype2.assign(ctype2, ctype2 + 3 * (size_t)nn);
+  P->cvalue2.assign(cvalue2, cvalue2 + 6 * (size_t)nn);
+  number_dofs(P);
+  rebuild_dual(P);
   return 0;
 }
 extern "C" const mfbem_dual_desc* mfbem_prep_dual(const mfbem_prep* p) { return p->has_dual ? &p->dual : nullptr; }
@@ -300,6 +377,9 @@ extern "C" void mfbem_prep_free(mfbem_prep* p) { delete p; }
 extern "C" void mfbem_prep_dof(const mfbem_prep* p, int32_t* dof, int32_t* order) {
   for (size_t i = 0; i < p->dof.size(); ++i) dof[i] = p->dof[i];
   for (size_t i = 0; i < p->order.size(); ++i) order[i] = p->order[i];
+}
+extern "C" void mfbem_prep_dof2(const mfbem_prep* p, int32_t* dof2) {
+  for (size_t i = 0; i < p->dof2.size(); ++i) dof2[i] = p->dof2[i];
 }
 
 // element far-field order (phijac_ngp) for callers outside this file

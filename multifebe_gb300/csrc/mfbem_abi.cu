@@ -109,7 +109,7 @@ struct mfbem_handle {
   // ms[0] / ms[1], the SBIE part of the Burton & Miller points classified
   // like sbie_auto (static) / shbie_auto (harmonic), built at the first
   // assembly of each kind from ms_base (points only)
-  bool has_hbie = false, has_bm = false;
+  bool has_hbie = false, has_bm = false, has_crack = false;
   DMesh mb, ms_base, ms[2];
   bool ms_built[2] = {false, false};
   long long mb_pts[3] = {0, 0, 0}, ms_pts[2][3] = {{0, 0, 0}, {0, 0, 0}};
@@ -476,7 +476,29 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
   int dev_count = 0;
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) return fail(MFBEM_ECUDA, "no CUDA device");
   const int nn = d->n_nodes, ne = d->n_elements, ndof = d->n_dof;
-  if (nn <= 0 || ne <= 0 || ndof != 3 * nn) return fail(MFBEM_EARG, "n_dof must be 3*n_nodes for one BE region");
+  if (nn <= 0 || ne <= 0) return fail(MFBEM_EARG, "empty mesh");
+  // crack-like boundaries: their elements and nodes (a node of one carries
+  // both faces' unknowns and equations, six rows)
+  std::vector<char> ckn(nn, 0);
+  int ncrack = 0;
+  if (dual && dual->crack_el) {
+    if (!dual->ctype2 || !dual->cvalue2) return fail(MFBEM_EARG, "crack_el needs ctype2 and cvalue2");
+    std::vector<char> ordn(nn, 0);
+    for (int e = 0; e < ne; ++e)
+      for (int k = 0; k < 8; ++k) {
+        const int s = d->element_node[8 * e + k] - 1;
+        if (s < 0 || s >= nn) return fail(MFBEM_EARG, "element_node out of range");
+        (dual->crack_el[e] ? ckn : ordn)[s] = 1;
+      }
+    for (int s = 0; s < nn; ++s) {
+      if (ckn[s] && ordn[s])
+        return fail(MFBEM_EUNSUPPORTED, "node " + std::to_string(s + 1) +
+                                            " belongs to a crack-like and an ordinary element");
+      ncrack += ckn[s];
+    }
+  }
+  if (ndof != 3 * nn + 3 * ncrack)
+    return fail(MFBEM_EARG, "n_dof must be 3 per node (6 per crack-like node) for one BE region");
   if (d->n_precalsets < 1 || d->n_precalsets > 16) return fail(MFBEM_EARG, "n_precalsets out of range [1,16]");
   if (d->qsi_ns_max < 1 || d->qsi_ns_max > 17) return fail(MFBEM_EUNSUPPORTED, "qsi_ns_max must be in [1,17]");
   for (int i = 0; i < d->n_precalsets; ++i)
@@ -507,21 +529,34 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
     m.ps_gln_max = std::max(m.ps_gln_max, d->precalset_gln[i]);
   }
   m.geo_tol = d->geometric_tolerance;
-  // --- host bookkeeping (topology only)
-  std::vector<int> dn_of(nn, -1);
-  for (int s = 0; s < nn; ++s) {
-    int r1 = d->row[3 * s];
-    if (r1 < 1 || (r1 - 1) % 3 != 0 || d->row[3 * s + 1] != r1 + 1 || d->row[3 * s + 2] != r1 + 2 || r1 + 2 > ndof) {
+  // --- host bookkeeping (topology only). DOF-order nodes ("dnodes") follow
+  // the rows: an ordinary node takes rows r, r+1, r+2 with col == row; a node
+  // of a crack-like boundary rows r..r+5, row(k,1) = r + 2(k-1) (SBIE),
+  // row(k,2) = row(k,1) + 1 (HBIE) and face f's column of direction k at
+  // row(k,1) + f - 1 (build_auxiliary_variables_mechanics_static.f90:146-207).
+  std::vector<int> dn_of(nn, -1), rb(nn, 0), by_row(nn);
+  for (int s = 0; s < nn; ++s) by_row[s] = s;
+  std::stable_sort(by_row.begin(), by_row.end(), [&](int a, int b) { return d->row[3 * a] < d->row[3 * b]; });
+  for (int i = 0, next = 1; i < nn; ++i) {
+    const int s = by_row[i], r1 = d->row[3 * s], w = ckn[s] ? 2 : 1;
+    if (r1 != next || d->row[3 * s + 1] != r1 + w || d->row[3 * s + 2] != r1 + 2 * w) {
       delete h;
-      return fail(MFBEM_EARG, "node rows must be node-wise consecutive triples");
+      return fail(MFBEM_EARG, ckn[s] ? "the rows of a crack-like node must be r, r+2, r+4 after the previous node's"
+                                     : "node rows must be node-wise consecutive triples");
     }
-    dn_of[s] = (r1 - 1) / 3;
+    next = r1 + 3 * w;
+    dn_of[s] = i;
+    rb[s] = r1 - 1;
     for (int k = 0; k < 3; ++k) {
       int ct = d->ctype[3 * s + k];
       int c = ct == 0 ? d->col[6 * s + 3 + k] : d->col[6 * s + k];
-      if ((ct != 0 && ct != 1) || c != r1 + k) {
+      if ((ct != 0 && ct != 1) || c != r1 + w * k) {
         delete h;
-        return fail(MFBEM_EUNSUPPORTED, "only ctype 0/1 with col == row (ordinary BE boundary) is supported");
+        return fail(MFBEM_EUNSUPPORTED, "only ctype 0/1 with col == row (BE boundary) is supported");
+      }
+      if (ckn[s] && dual->ctype2[3 * s + k] != 0 && dual->ctype2[3 * s + k] != 1) {
+        delete h;
+        return fail(MFBEM_EUNSUPPORTED, "ctype2 must be 0 or 1");
       }
     }
   }
@@ -530,19 +565,26 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
     for (int k = 0; k < 8; ++k) {
       int s = d->element_node[8 * e + k] - 1;
       if (s < 0 || s >= nn) { delete h; return fail(MFBEM_EARG, "element_node out of range"); }
-      edof[8 * e + k] = 3 * dn_of[s];
+      edof[8 * e + k] = rb[s];
     }
     if (d->reversion) rev[e] = d->reversion[e] ? 1 : 0;
+    if (ncrack && dual->crack_el[e]) {
+      if (rev[e]) { delete h; return fail(MFBEM_EUNSUPPORTED, "a crack-like element cannot be reversed"); }
+      rev[e] = 2;
+    }
   }
   std::vector<int> dct(ndof);
   std::vector<double> dcv(2 * (size_t)ndof);
   for (int s = 0; s < nn; ++s)
-    for (int k = 0; k < 3; ++k) {
-      int dof = 3 * dn_of[s] + k;
-      dct[dof] = d->ctype[3 * s + k];
-      dcv[2 * dof] = d->cvalue[6 * s + 2 * k];
-      dcv[2 * dof + 1] = d->cvalue[6 * s + 2 * k + 1];
-    }
+    for (int k = 0; k < 3; ++k)
+      for (int f = 0; f <= (int)ckn[s]; ++f) {
+        const int dof = rb[s] + (ckn[s] ? 2 * k + f : k);
+        const int* ct = f ? dual->ctype2 : d->ctype;
+        const double* cv = f ? dual->cvalue2 : d->cvalue;
+        dct[dof] = ct[3 * s + k];
+        dcv[2 * dof] = cv[6 * s + 2 * k];
+        dcv[2 * dof + 1] = cv[6 * s + 2 * k + 1];
+      }
   // formulation per node: 0 SBIE, 1 HBIE alone, 2 Burton & Miller (dual desc)
   std::vector<int> form(nn, 0);
   if (dual) {
@@ -553,6 +595,17 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
     }
     for (int s = 0; s < nn; ++s) {
       const int hb = dual->hbie[s], du = dual->dual[s], co = dual->dual_is_common[s];
+      if (ckn[s]) {
+        // crack-like node: SBIE and HBIE at the same points, each its own
+        // equation (fbem_dual_boundary, assign_default_bem_formulation.f90:94-128)
+        if (hb != 1 || du != 2 || co != 1) {
+          delete h;
+          return fail(MFBEM_EARG, "node " + std::to_string(s + 1) +
+                                      " of a crack-like boundary needs (hbie, dual, dual_is_common) = (1, 2, 1)");
+        }
+        form[s] = 3;
+        continue;
+      }
       if (hb == 0 && du == 0 && co == 0) form[s] = 0;
       else if (hb == 1 && du == 0 && co == 0) form[s] = 1;
       else if (hb == 1 && du == 1 && co == 1) form[s] = 2;
@@ -661,6 +714,22 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
   m.dct = dctd; m.dcv = dcvd; m.cpx = cpxd; m.cp_xi = cpxid; m.cp_dn = cpdn; m.cp_kind = cpk;
   m.cp_elem = cpe; m.cp_kn = cpkn; m.dn_cp = dncp; m.inc_start = incs; m.inc_el = ince;
   m.n_gn = ngn; m.tbp_gn = tbp;
+  // rows of each dnode's equations when crack-like nodes break the 3 dn + il
+  // layout: SBIE rows (this view and the SBIE part) and HBIE rows
+  int* dn_rb_h = nullptr;
+  if (ncrack) {
+    std::vector<int> rs(nn), rh(nn);
+    for (int s = 0; s < nn; ++s) {
+      rs[dn_of[s]] = (rb[s] << 1) | ckn[s];
+      rh[dn_of[s]] = ((rb[s] + ckn[s]) << 1) | ckn[s];
+    }
+    int* dn_rb_s = nullptr;
+    if ((rc = dupload(h, &dn_rb_s, rs.data(), rs.size())) || (rc = dupload(h, &dn_rb_h, rh.data(), rh.size()))) {
+      mfbem_mesh_release(h);
+      return rc;
+    }
+    m.dn_rb = dn_rb_s;
+  }
   QsCurves q = qs_curves(d->qsi_relative_error), q15 = qs_curves(1e-15);
   if ((rc = dupload(h, &h->d_qs, &q, 1)) || (rc = dupload(h, &h->d_q15, &q15, 1)) ||
       (rc = dalloc(h, (void**)&m.px, 3 * sizeof(double) * (size_t)ne * m.ptot)) ||
@@ -688,7 +757,7 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
         const int s = d->element_node[8 * e + k] - 1;
         if (form[s] == 0) continue;
         HostCP c;
-        const double sg = rev[e] ? -1.0 : 1.0;
+        const double sg = (rev[e] & 1) ? -1.0 : 1.0;
         for (int q = 0; q < 3; ++q) {
           c.x[q] = dual->x_i_hbie[24 * (size_t)e + 3 * k + q];
           c.n[q] = sg * dual->n_i_hbie[24 * (size_t)e + 3 * k + q];
@@ -701,18 +770,21 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
         }
         c.alpha = form[s] == 2 ? dual->alpha[s] : 1.0;
         c.dn = dn_of[s];
-        c.kind = form[s] == 1 ? 2 : 3;
+        c.kind = form[s] == 1 ? 2 : (form[s] == 2 ? 3 : 4);
         c.e = e;
         c.kn = k;
         hb.push_back(c);
-        if (form[s] == 2) {
+        if (form[s] >= 2) {
+          // the SBIE part (Burton & Miller) or equation (crack-like node)
           c.kind = 1;
           bm.push_back(c);
         }
       }
     h->has_hbie = true;
     h->has_bm = !bm.empty();
+    h->has_crack = ncrack > 0;
     h->mb = m;
+    if (ncrack) h->mb.dn_rb = dn_rb_h;
     if ((rc = upload_points(h, hb, nn, h->mb))) { mfbem_mesh_release(h); return rc; }
     h->mb.fcls = h->mb.fadp = 7;
     h->mb.hbie = 1;
@@ -920,6 +992,9 @@ static int launch_assembly(mfbem_handle* h, const POL& pol, const double* d_nu, 
   const DMesh& m = h->m;
   constexpr int WPB = 4;
   long long nw = (long long)m.ndn * nf;
+  // the double-float kernels write rows 3 dn + il: a region with crack-like
+  // boundaries (six rows per crack node) assembles in binary64 only
+  if (h->has_crack) mixed = false;
   unsigned g = nblk(nw, WPB);
   // static half-space region: the complementary kernel's pairs follow each
   // full-space stage and add into the same rows
@@ -1191,6 +1266,8 @@ template <class POL>
 static int internal_points_run(mfbem_handle* h, const POL& pol, int nf, int32_t n_ip, const double* x_ip,
                                const double* u_nodes, const double* t_nodes, double* u_ip, double* sigma_ip) {
   typedef typename POL::T T;
+  if (h->has_crack)
+    return fail(MFBEM_EUNSUPPORTED, "internal points of a region with crack-like boundaries are not available");
   const DMesh& m = h->m;
   const int nn = h->nn, ne = h->ne;
   TmpBufs tb;

@@ -175,7 +175,11 @@ __device__ __forceinline__ void flush_pair(const DMesh& m, const POL& pol, int f
   constexpr int NG = POL::NG;
   const int lane = threadIdx.x & 31;
   T bc[3] = {VT<T>::zero(), VT<T>::zero(), VT<T>::zero()};
-  const bool rev = m.rev[e] != 0;
+  const int rv = m.rev[e];
+  const bool rev = (rv & 1) != 0;
+  // crack-like element: face 2 (reversed normal) takes -h and g at the next
+  // column (build_lse_mechanics_bem_staela.f90:883-887)
+  const int ck = rv >> 1;
   double* Af = A + astride * f;
   for (int j = 0; j < GOut<NG>::acc; ++j) {
     int o = lane + 32 * j;
@@ -186,20 +190,24 @@ __device__ __forceinline__ void flush_pair(const DMesh& m, const POL& pol, int f
       if (hli_phi) v = v + hli_phi[9 + kn] * pol.cpv(f) * hli_phi[3 * il + ik];
       v = v * pol.cte_t(f);
       if (rev) v = -v;
-      int dof = m.edof[8 * e + kn] + ik;
-      size_t row = 3 * (size_t)dn + il;
-      if (m.dct[dof] == 1) addA(Af, (size_t)dof * lda + row, v);
-      else bc[il] = bc[il] - v * cval(m.dcv, dof, v);
+      const size_t row = dn_row(m, dn, il);
+      for (int fc = 0; fc <= ck; ++fc, v = -v) {
+        const int dof = m.edof[8 * e + kn] + (ik << ck) + fc;
+        if (m.dct[dof] == 1) addA(Af, (size_t)dof * lda + row, v);
+        else bc[il] = bc[il] - v * cval(m.dcv, dof, v);
+      }
     } else {
       int q = o - 72, kn = q / NG, sidx = q % NG;
       int il = NG == 6 ? sym_il(sidx) : sidx / 3, ik = NG == 6 ? sym_ik(sidx) : sidx % 3;
       v = v * pol.cte_u(f);
       for (int t = 0; t < (il == ik || NG == 9 ? 1 : 2); ++t) {
         int r_ = t ? ik : il, c_ = t ? il : ik;
-        int dof = m.edof[8 * e + kn] + c_;
-        size_t row = 3 * (size_t)dn + r_;
-        if (m.dct[dof] == 0) addA(Af, (size_t)dof * lda + row, -v);
-        else bc[r_] = bc[r_] + v * cval(m.dcv, dof, v);
+        const size_t row = dn_row(m, dn, r_);
+        for (int fc = 0; fc <= ck; ++fc) {
+          const int dof = m.edof[8 * e + kn] + (c_ << ck) + fc;
+          if (m.dct[dof] == 0) addA(Af, (size_t)dof * lda + row, -v);
+          else bc[r_] = bc[r_] + v * cval(m.dcv, dof, v);
+        }
       }
     }
   }
@@ -207,7 +215,7 @@ __device__ __forceinline__ void flush_pair(const DMesh& m, const POL& pol, int f
     for (int o = 16; o > 0; o >>= 1) bc[il] = bc[il] + shfl_x(bc[il], o);
   if (lane == 0) {
     double* bf = b + bstride * f;
-    for (int il = 0; il < 3; ++il) addA(bf, 3 * (size_t)dn + il, bc[il]);
+    for (int il = 0; il < 3; ++il) addA(bf, dn_row(m, dn, il), bc[il]);
   }
   __syncwarp();
 }
@@ -584,6 +592,7 @@ __global__ void k_free(DMesh m, POL pol, const double* nu /* complex, per freque
   long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (id >= (long long)m.ndn * nf) return;
   int dn = (int)(id % m.ndn), f = (int)(id / m.ndn);
+  if (m.dn_cp[dn] == m.dn_cp[dn + 1]) return;
   double* Af = A + astride * f;
   double* bf = b + bstride * f;
   const T z = VT<T>::zero();
@@ -601,7 +610,7 @@ __global__ void k_free(DMesh m, POL pol, const double* nu /* complex, per freque
       T onemnu = one_minus(nu + 2 * f, z);
       T q = -1.0 / ((8.0 * kPi) * onemnu);
       for (int il = 0; il < 3; ++il) {
-        size_t row = 3 * (size_t)dn + il;
+        const size_t row = dn_row(m, dn, il);
         for (int ik = 0; ik < 3; ++ik) {
           T C = q * F[1 + 3 * il + ik];
           if (il == ik) C = C + F[0];
@@ -616,7 +625,7 @@ __global__ void k_free(DMesh m, POL pol, const double* nu /* complex, per freque
       phi_q8<double>(m.cp_xi[2 * cp], m.cp_xi[2 * cp + 1], phi);
       for (int kn = 0; kn < 8; ++kn)
         for (int il = 0; il < 3; ++il) {
-          size_t row = 3 * (size_t)dn + il;
+          const size_t row = dn_row(m, dn, il);
           T v = fr(0.5 * phi[kn] * two, z);
           int dof = m.edof[8 * e + kn] + il;
           if (m.dct[dof] == 1) addA(Af, (size_t)dof * lda + row, v);
@@ -624,7 +633,7 @@ __global__ void k_free(DMesh m, POL pol, const double* nu /* complex, per freque
         }
     }
   }
-  for (int il = 0; il < 3; ++il) addA(bf, 3 * (size_t)dn + il, bc[il]);
+  for (int il = 0; il < 3; ++il) addA(bf, dn_row(m, dn, il), bc[il]);
 }
 
 // ============================================================================
@@ -838,14 +847,15 @@ __device__ __forceinline__ void add3(cf bc[3], int i, cf v) {
 }
 
 // scale, reverse and scatter this lane's outputs of one pair (the scatter of
-// flush_pair in double-float): A entries added to the binary64 system,
+// flush_pair in double-float; rows 3 dn + il: never used on a region with
+// crack-like boundaries): A entries added to the binary64 system,
 // prescribed values into the lane's b partial sums bc. hp (singular pairs only): static
 // line integrals hli[9] and phi_i[8] of the pair; their CPV part
 // T2[0] hli(il,ik) phi_i(kn) is added to the h outputs.
 __device__ __forceinline__ void flush_pair_ff(const DMesh& m, const HarParF& q, const ff* dcv_f, int dn, int e,
                                               const cf acc[kAcc], double2* Ac, size_t lda, cf bc[3], const ff* hp) {
   const int lane = threadIdx.x & 31;
-  const bool rev = m.rev[e] != 0;
+  const bool rev = (m.rev[e] & 1) != 0;
 #pragma unroll 1
   for (int j = 0; j < kAcc; ++j) {
     const int o = lane + 32 * j;

@@ -3,7 +3,10 @@
 //
 // HBM layout (all arrays structure-of-arrays, 0-based):
 //   elements   ex[ne][8][3], cl, gln_far, ball[ne][4], rev, edof[ne][8]
-//              (DOF index of direction 1 of each element node = row base)
+//              (DOF index of direction 1 of each element node = row base;
+//              rev bit 0: reversed, bit 1: element of a crack-like boundary,
+//              whose nodes interleave both faces: face f, direction c at
+//              edof + 2 c + f)
 //   DOFs       dct[ndof] (0 u known / 1 t known), dcv[ndof] complex value
 //   colloc.    points sorted by DOF-order node ("dnode"): cpx[ncp][3], cp_dn,
 //              cp_kind (0 nodal SBIE / 1 SBIE-MCA), cp_elem, cp_kn, cp_xi[2];
@@ -104,6 +107,19 @@ struct DMesh {
   const double* cp_n;
   const double* cp_alpha;
   double* hsing_x;
+  // rows of each dnode's equations in a region with crack-like boundaries
+  // (null: 3 dn + il): (row base << 1) | s, rows base + (il << s); a crack
+  // node's SBIE rows are r, r+2, r+4 and its HBIE rows r+1, r+3, r+5
+  // (build_auxiliary_variables_mechanics_static.f90:146-207)
+  const int* dn_rb;
 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ size_t dn_row(const DMesh& m, int dn, int il) {
+  if (!m.dn_rb) return 3 * (size_t)dn + il;
+  const int v = m.dn_rb[dn];
+  return (size_t)(v >> 1) + ((size_t)il << (v & 1));
+}
+#endif
 
 }  // namespace mfb

@@ -279,20 +279,26 @@ __device__ __forceinline__ void hsing_point(const HS& hs, int f, const HsCoef<ty
 }
 
 // Scatter one HBIE singular pair (final m, l of this lane's outputs) into A, b.
+// On a crack-like element face 2 takes -m and l at the next column.
 template <typename T>
 __device__ __forceinline__ void hsing_scatter(const DMesh& m, int dn, int e, int o, T v, double* Af, size_t lda, T bc[3]) {
+  const int ck = m.rev[e] >> 1;
   if (o < 72) {
     const int kn = o / 9, il = (o % 9) / 3, ik = o % 3;
-    const int dof = m.edof[8 * e + kn] + ik;
-    const size_t row = 3 * (size_t)dn + il;
-    if (m.dct[dof] == 1) addA(Af, (size_t)dof * lda + row, v);
-    else bc[il] = bc[il] - v * cval(m.dcv, dof, v);
+    const size_t row = dn_row(m, dn, il);
+    for (int fc = 0; fc <= ck; ++fc, v = -v) {
+      const int dof = m.edof[8 * e + kn] + (ik << ck) + fc;
+      if (m.dct[dof] == 1) addA(Af, (size_t)dof * lda + row, v);
+      else bc[il] = bc[il] - v * cval(m.dcv, dof, v);
+    }
   } else {
     const int q = o - 72, kn = q / 9, il = (q % 9) / 3, ik = q % 3;
-    const int dof = m.edof[8 * e + kn] + ik;
-    const size_t row = 3 * (size_t)dn + il;
-    if (m.dct[dof] == 0) addA(Af, (size_t)dof * lda + row, -v);
-    else bc[il] = bc[il] + v * cval(m.dcv, dof, v);
+    const size_t row = dn_row(m, dn, il);
+    for (int fc = 0; fc <= ck; ++fc) {
+      const int dof = m.edof[8 * e + kn] + (ik << ck) + fc;
+      if (m.dct[dof] == 0) addA(Af, (size_t)dof * lda + row, -v);
+      else bc[il] = bc[il] + v * cval(m.dcv, dof, v);
+    }
   }
 }
 
@@ -351,7 +357,7 @@ __global__ void __launch_bounds__(32) k_hsing(DMesh m, HS hs, int nf, double* A,
       }
       __syncwarp();
       const int e = m.sing_e[qp];
-      const bool rev = m.rev[e] != 0;
+      const bool rev = (m.rev[e] & 1) != 0;
       const T cs = k.cte_s * beta, cl = k.cte_d * beta;
       T bc[3] = {z, z, z};
       for (int j = 0; j < NA; ++j) {
@@ -375,7 +381,7 @@ __global__ void __launch_bounds__(32) k_hsing(DMesh m, HS hs, int nf, double* A,
         for (int o = 16; o > 0; o >>= 1) bc[il] = bc[il] + shfl_x(bc[il], o);
       if (lane == 0) {
         double* bf = b + bstride * f;
-        for (int il = 0; il < 3; ++il) addA(bf, 3 * (size_t)dn + il, bc[il]);
+        for (int il = 0; il < 3; ++il) addA(bf, dn_row(m, dn, il), bc[il]);
       }
       __syncwarp();
     };
@@ -442,20 +448,44 @@ __global__ void __launch_bounds__(32) k_hsing(DMesh m, HS hs, int nf, double* A,
 // Free terms of the HBIE view's points (build_lse_mechanics_bem_staela.f90:
 // 181-211,459-489, build_lse_mechanics_bem_harela.f90:316-360,629-681): -1/2
 // phi(xi_i) on l (taken as g: weight 1 for HBIE alone, beta for Burton &
-// Miller) and, for Burton & Miller, the SBIE's 1/2 phi(xi_i) on h. One thread
-// per (dnode, frequency).
+// Miller) and, for Burton & Miller, the SBIE's 1/2 phi(xi_i) on h. A point of
+// a crack-like boundary (cp_kind 4, dual BEM) carries both equations of its
+// node: the SBIE (rows one below the HBIE's) takes 1/2 phi(xi_i) on both
+// faces' u, the HBIE -1/2 phi(xi_i) on face 1's t and +1/2 phi(xi_i) on face
+// 2's t (staela.f90:195-204). One thread per (dnode, frequency).
 template <typename T>
 __global__ void k_hfree(DMesh m, const HarParH* ph, int nf, double* A, size_t lda, size_t astride, double* b,
                         size_t bstride) {
   const long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (id >= (long long)m.ndn * nf) return;
   const int dn = (int)(id % m.ndn), f = (int)(id / m.ndn);
+  if (m.dn_cp[dn] == m.dn_cp[dn + 1]) return;
   double* Af = A + astride * f;
   double* bf = b + bstride * f;
   const T z = VT<T>::zero();
-  T bc[3] = {z, z, z};
+  T bc[3] = {z, z, z}, bs[3] = {z, z, z};
+  bool crack = false;
   for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
     const int e = m.cp_elem[cp];
+    if (m.cp_kind[cp] == 4) {
+      crack = true;
+      double phi[8];
+      phi_q8<double>(m.cp_xi[2 * cp], m.cp_xi[2 * cp + 1], phi);
+      for (int kn = 0; kn < 8; ++kn)
+        for (int il = 0; il < 3; ++il) {
+          const size_t row = dn_row(m, dn, il);
+          for (int fc = 0; fc < 2; ++fc) {
+            const int dof = m.edof[8 * e + kn] + 2 * il + fc;
+            const T v = z + 0.5 * phi[kn];
+            if (m.dct[dof] == 1) addA(Af, (size_t)dof * lda + row - 1, v);
+            else bs[il] = bs[il] - v * cval(m.dcv, dof, z);
+            const T g = z + (fc ? 0.5 : -0.5) * phi[kn];
+            if (m.dct[dof] == 0) addA(Af, (size_t)dof * lda + row, -g);
+            else bc[il] = bc[il] + g * cval(m.dcv, dof, z);
+          }
+        }
+      continue;
+    }
     const bool bm = m.cp_kind[cp] == 3;
     T beta = z + 1.0;
     if (bm) {
@@ -466,7 +496,7 @@ __global__ void k_hfree(DMesh m, const HarParH* ph, int nf, double* A, size_t ld
     phi_q8<double>(m.cp_xi[2 * cp], m.cp_xi[2 * cp + 1], phi);
     for (int kn = 0; kn < 8; ++kn)
       for (int il = 0; il < 3; ++il) {
-        const size_t row = 3 * (size_t)dn + il;
+        const size_t row = dn_row(m, dn, il);
         const int dof = m.edof[8 * e + kn] + il;
         if (bm) {
           const T v = z + 0.5 * phi[kn];
@@ -478,7 +508,10 @@ __global__ void k_hfree(DMesh m, const HarParH* ph, int nf, double* A, size_t ld
         else bc[il] = bc[il] + g * cval(m.dcv, dof, z);
       }
   }
-  for (int il = 0; il < 3; ++il) addA(bf, 3 * (size_t)dn + il, bc[il]);
+  for (int il = 0; il < 3; ++il) {
+    addA(bf, dn_row(m, dn, il), bc[il]);
+    if (crack) addA(bf, dn_row(m, dn, il) - 1, bs[il]);
+  }
 }
 
 }  // namespace mfb

@@ -40,5 +40,12 @@ void mfbem_prep_dof(const mfbem_prep* p, int32_t* dof, int32_t* order);
    mfbem_prep_dual then returns the descriptor for mfbem_mesh_upload_dual
    (NULL before). */
 int mfbem_prep_set_formulation(mfbem_prep* p, const int32_t* form, const double* alpha, const double* delta);
+/* crack-like boundary: crack_el [ne] 0/1, face 2 conditions ctype2 [nn][3],
+   cvalue2 [nn][3][2]; renumbers the DOF (mfbem_prep_desc's n_dof, row, col)
+   and makes the dual descriptor. -1: a crack node in an ordinary element,
+   -2: ctype2 out of range. */
+int mfbem_prep_set_crack(mfbem_prep* p, const int32_t* crack_el, const int32_t* ctype2, const double* cvalue2);
+/* face 2's DOF [nn][3] (0-based, -1 off crack-like boundaries) */
+void mfbem_prep_dof2(const mfbem_prep* p, int32_t* dof2);
 const mfbem_dual_desc* mfbem_prep_dual(const mfbem_prep* p);
 }

@@ -418,7 +418,7 @@ __global__ void k_ip_adp(DMesh m, IpArgs a, POL pol, const QsCurves* __restrict_
       tn[3 * kn + c] = tv[3 * s + c];
     }
   }
-  const double rs = m.rev[e] ? -1.0 : 1.0;
+  const double rs = (m.rev[e] & 1) ? -1.0 : 1.0;
   T du[3], sg[3][3];
   for (int c = 0; c < 3; ++c) {
     du[c] = VT<T>::zero();
@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(WPB * 32) k_ip_reg(DMesh m, IpArgs a, POL pol)
       nv[w][j] = j < 24 ? uv[3 * s + c] : tv[3 * s + c];
     }
     __syncwarp();
-    const double rs = m.rev[e] ? -1.0 : 1.0;
+    const double rs = (m.rev[e] & 1) ? -1.0 : 1.0;
 #pragma unroll 1
     for (int h = 0; h < 2; ++h) {
       const uint8_t c = h ? ch : cs;

@@ -268,6 +268,92 @@ def halfspace_cavity(a=0.25, top=0.2, n=3, p=1.0):
     return Deck(f"hs_cavity{n}", nodes, conn, ctype, cvalue, d.boundary_of_element)
 
 
+def penny_crack(a=1.0, m=2, k=2, p=1.0):
+    """Penny-shaped crack of radius a in the plane z = 0 of a full space,
+    quad8, an O-grid: an m x m central square of half-width a/2 and four
+    blocks of m x k elements out to the circle (mid-side nodes on the mapped
+    curves). Element normals +z. Both faces loaded by the crack pressure p:
+    face 1 (outward normal +z) t = -p e_z, face 2 t = +p e_z. Returns the
+    deck (face 1 conditions) and (crack_el, ctype2, cvalue2).
+    Sneddon's opening: u2_z - u1_z = 8 (1 - nu^2) p / (pi E) sqrt(a^2 - r^2)."""
+    s0 = 0.5 * a
+
+    def central(u, v):
+        return np.array([s0 * u, s0 * v, 0.0])
+
+    def outer(t, rho, rot):
+        p0 = np.array([s0, s0 * t])
+        th = t * np.pi / 4.0
+        p1 = a * np.array([np.cos(th), np.sin(th)])
+        q = (1.0 - rho) * p0 + rho * p1
+        c, sn = np.cos(rot), np.sin(rot)
+        return np.array([c * q[0] - sn * q[1], sn * q[0] + c * q[1], 0.0])
+
+    loc = [(-1, -1), (1, -1), (1, 1), (-1, 1), (0, -1), (1, 0), (0, 1), (-1, 0)]
+    elems = []
+    for i in range(m):
+        for j in range(m):
+            u0, v0 = -1 + 2 * i / m, -1 + 2 * j / m
+            elems.append([central(u0 + (1 + xi) / m, v0 + (1 + eta) / m) for xi, eta in loc])
+    for b in range(4):
+        rot = b * np.pi / 2.0
+        for i in range(m):
+            for j in range(k):
+                t0, r0 = -1 + 2 * i / m, j / k
+                # local xi along rho, eta along t (orientation fixed below)
+                elems.append([outer(t0 + (1 + eta) / m, r0 + (1 + xi) / (2 * k), rot) for xi, eta in loc])
+    coords, conn, index = [], [], {}
+    for el in elems:
+        row = []
+        for x in el:
+            key = tuple(np.round(x, 12))
+            if key not in index:
+                index[key] = len(coords)
+                coords.append(x)
+            row.append(index[key])
+        conn.append(row)
+    nodes = np.array(coords)
+    conn = np.array(conn, dtype=np.int32)
+    # orientation: +z normals (counter-clockwise corners)
+    for e in range(len(conn)):
+        c = nodes[conn[e, :4]]
+        if np.cross(c[1] - c[0], c[3] - c[0])[2] < 0:
+            conn[e] = conn[e][[0, 3, 2, 1, 7, 6, 5, 4]]
+    nn = len(nodes)
+    ctype = np.ones((nn, 3), dtype=np.int32)
+    cvalue = np.zeros((nn, 3), dtype=np.complex128)
+    cvalue[:, 2] = -p
+    cvalue2 = np.zeros((nn, 3), dtype=np.complex128)
+    cvalue2[:, 2] = p
+    d = Deck(f"penny{m}x{k}", nodes, conn, ctype, cvalue, np.zeros(len(conn), dtype=np.int32))
+    return d, (np.ones(len(conn), dtype=bool), np.ones((nn, 3), dtype=np.int32), cvalue2)
+
+
+def penny_crack_in_box(a=1.0, m=2, k=1, half=2.0, nb=2, p=1.0):
+    """The pressurised penny crack of penny_crack inside a clamped cube
+    [-half, half]^3 (nb x nb quad8 per face, u = 0): one region with a
+    crack-like and an ordinary boundary. The crack's elements come first, so
+    the ordinary nodes' rows follow the six-row crack nodes."""
+    dc, (ce, ct2, cv2) = penny_crack(a, m, k, p)
+    db = box((2 * half,) * 3, (nb, nb, nb), split_faces=False)
+    nodes = np.vstack([dc.nodes, db.nodes - half])
+    conn = np.vstack([dc.conn, db.conn + dc.n_nodes]).astype(np.int32)
+    nb_n = db.n_nodes
+    ctype = np.vstack([dc.ctype, np.zeros((nb_n, 3), dtype=np.int32)])
+    cvalue = np.vstack([dc.cvalue, np.zeros((nb_n, 3), dtype=np.complex128)])
+    ct2 = np.vstack([ct2, np.ones((nb_n, 3), dtype=np.int32)])
+    cv2 = np.vstack([cv2, np.zeros((nb_n, 3), dtype=np.complex128)])
+    ce = np.concatenate([ce, np.zeros(db.n_elements, dtype=bool)])
+    d = Deck(f"penny{m}x{k}_box{nb}", nodes, conn, ctype, cvalue,
+             np.concatenate([np.zeros(dc.n_elements, np.int32), 1 + db.boundary_of_element]))
+    return d, (ce, ct2, cv2)
+
+
+def sneddon_opening(r, a, p, E, nu):
+    """Opening of a pressurised penny crack (Sneddon 1946)."""
+    return 8.0 * (1.0 - nu ** 2) * p / (np.pi * E) * np.sqrt(np.maximum(a * a - r * r, 0.0))
+
+
 def love_square_centre(a, p, E, nu):
     """Settlement of the centre of a uniformly loaded square 2a x 2a on an
     elastic half-space (Love; four corners of a x a squares)."""

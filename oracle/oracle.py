@@ -69,6 +69,8 @@ def lib():
         L.orc_pair_hsc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    _dp, _dp]
         L.orc_problem_set_formulation.argtypes = [ctypes.c_void_p, _ip, _dp, _dp]
+        L.orc_problem_set_crack.argtypes = [ctypes.c_void_p, ctypes.c_char_p, _ip, _dp]
+        L.orc_dof2_map.argtypes = [ctypes.c_void_p, _ip]
         L.orc_colloc_normals.argtypes = [ctypes.c_void_p, _dp]
         L.orc_pair_hbie_staela.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_double, _dp, _dp]
@@ -162,6 +164,43 @@ class Problem:
         dl = np.ascontiguousarray(np.broadcast_to(0.22540333 if delta is None else delta, (nn,)), dtype=np.float64)
         if lib().orc_problem_set_formulation(self._h, _p(f, _ip), _p(a), _p(dl)) != 0:
             raise ValueError("formulation codes must be 0, 1 or 2")
+
+    def set_crack(self, crack_el, ctype2, cvalue2):
+        """Crack-like boundary (dual BEM): crack_el [ne] bool marks its
+        elements; ctype2, cvalue2 [nn, 3] the boundary conditions of face 2
+        (face 1: the deck's ctype / cvalue). Renumbers the DOF."""
+        ce = np.ascontiguousarray(np.asarray(crack_el, dtype=bool).astype(np.int8))
+        ct = np.ascontiguousarray(ctype2, dtype=np.int32)
+        cv = np.ascontiguousarray(cvalue2, dtype=np.complex128).view(np.float64)
+        if lib().orc_problem_set_crack(self._h, ce.ctypes.data_as(ctypes.c_char_p), _p(ct, _ip), _p(cv)) != 0:
+            raise ValueError("a crack node also belongs to an ordinary element")
+        self.n = lib().orc_n_dof(self._h)
+        self._crack = (np.asarray(crack_el, dtype=bool), ct.copy(), np.asarray(cvalue2, dtype=np.complex128).copy())
+
+    def dof2_map(self):
+        nn = self.deck.n_nodes
+        d = np.zeros(3 * nn, dtype=np.int32)
+        lib().orc_dof2_map(self._h, _p(d, _ip))
+        return d.reshape(nn, 3)
+
+    def solution_faces(self, x):
+        """(u1, t1, u2, t2) [nn, 3]: face 1 of every node, face 2 of the crack
+        nodes (zero elsewhere)."""
+        u1, t1 = self.solution(x)
+        ce, ct2, cv2 = self._crack
+        d2 = self.dof2_map()
+        u2 = np.zeros_like(u1)
+        t2 = np.zeros_like(t1)
+        nodes = np.unique(self.deck.conn[ce])
+        for s in nodes:
+            for c in range(3):
+                v = x[d2[s, c]]
+                kv = cv2[s, c] if np.iscomplexobj(x) else cv2[s, c].real
+                if ct2[s, c] == 0:
+                    u2[s, c], t2[s, c] = kv, v
+                else:
+                    u2[s, c], t2[s, c] = v, kv
+        return u1, t1, u2, t2
 
     def colloc_normals(self):
         m = lib().orc_n_colloc(self._h)

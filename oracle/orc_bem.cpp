@@ -1644,6 +1644,13 @@ struct Problem {
   // the point into each element of the node
   std::vector<int> form;
   std::vector<double> alpha, delta_hbie;
+  // crack-like boundary (src/read_boundaries.f90:105): its elements, and
+  // their nodes with two faces (build_auxiliary_variables_mechanics_static.f90:
+  // 150-181): face 2's boundary conditions and DOF (dof2: the face-2 column,
+  // equal to the row of the node's second (HBIE) equation)
+  std::vector<char> crack_el, crack;
+  std::vector<int> ctype2, dof2;
+  std::vector<cplx> cvalue2;
 };
 
 static void build(Problem& P) {
@@ -1712,8 +1719,24 @@ static void build(Problem& P) {
         P.tbm_gn[(8 * e + k) * 3 + c] = vb;
       }
     }
-  // DOF numbering, build_auxiliary_variables_mechanics_static.f90:60-140
+  P.form.assign(nn, 0);
+  P.alpha.assign(nn, 1.0);
+  P.delta_hbie.assign(nn, 0.22540333);
+  P.crack_el.assign(ne, 0);
+  P.crack.assign(nn, 0);
+  P.ctype2.assign(3 * nn, 1);
+  P.cvalue2.assign(3 * nn, cplx(0.0, 0.0));
+}
+
+// DOF numbering, build_auxiliary_variables_mechanics_static.f90:60-181: nodes
+// in element order (first appearance); an ordinary node takes rows / columns
+// r, r+1, r+2; a node of a crack-like boundary r..r+5 with row(k, eq) =
+// r + 2k + eq - 1 and col(k, face) = r + 2k + face - 1.
+static void build_dofs(Problem& P) {
+  const int nn = P.nn, ne = P.ne;
   P.dof.assign(3 * nn, -1);
+  P.dof2.assign(3 * nn, -1);
+  P.node_order.clear();
   std::vector<char> used(nn, 0);
   int row = 0;
   for (int e = 0; e < ne; ++e)
@@ -1722,12 +1745,17 @@ static void build(Problem& P) {
       if (used[s]) continue;
       used[s] = 1;
       P.node_order.push_back(s);
-      for (int c = 0; c < 3; ++c) P.dof[3 * s + c] = row++;
+      if (P.crack[s]) {
+        for (int c = 0; c < 3; ++c) {
+          P.dof[3 * s + c] = row + 2 * c;
+          P.dof2[3 * s + c] = row + 2 * c + 1;
+        }
+        row += 6;
+      } else {
+        for (int c = 0; c < 3; ++c) P.dof[3 * s + c] = row++;
+      }
     }
   P.ndof = row;
-  P.form.assign(nn, 0);
-  P.alpha.assign(nn, 1.0);
-  P.delta_hbie.assign(nn, 0.22540333);
 }
 
 // Collocation points in the collocation loop order
@@ -1748,10 +1776,12 @@ static void build_colloc(Problem& P) {
       cp.node = s; cp.elem = e; cp.kn = k;
       cp.n[0] = cp.n[1] = cp.n[2] = 0.0;
       double xi[2] = {quad8_xi_nodes[k][0], quad8_xi_nodes[k][1]};
-      if (P.form[s] != 0) {
+      if (P.form[s] != 0 || P.crack[s]) {
+        // crack-like nodes: SBIE and HBIE at the same MCA point, each its own
+        // equation (dual BEM, assign_default_bem_formulation.f90:94-128)
         double dl = P.delta_hbie[s];
         if (check_xi1xi2_edge_quad(xi)) { xi[0] = xi[0] * (1.0 - dl); xi[1] = xi[1] * (1.0 - dl); }
-        cp.kind = P.form[s] == 1 ? 2 : 3;
+        cp.kind = P.crack[s] ? 4 : (P.form[s] == 1 ? 2 : 3);
         double d1[8], d2[8];
         dphi_quad8(xi, d1, d2);
         double T1[3] = {0, 0, 0}, T2[3] = {0, 0, 0};
@@ -1785,40 +1815,89 @@ static void build_colloc(Problem& P) {
     }
 }
 
-// Scatter one (collocation node, integration element) block into the row
-// buffer of that node: assemble_bem_staela_equation.f90:69-98 and
-// assemble_bem_harela_equation.f90:78-113 (ordinary BE boundary).
+// Scatter one (collocation point, integration element) block into the row
+// buffer of one equation of the point's node: assemble_bem_staela_equation.f90:
+// 69-124 and assemble_bem_harela_equation.f90:78-150. Face 1 of the element's
+// nodes takes (hp, gp); on a crack-like element face 2 takes (hm, gm) too.
 template <typename T>
-static void scatter(const Problem& P, int e, const T h[8][3][3], const T g[8][3][3], T* rowbuf /*3*ndof*/,
-                    T* brow /*3*/) {
+static void scatter4(const Problem& P, int e, const T hp[8][3][3], const T gp[8][3][3], const T hm[8][3][3],
+                     const T gm[8][3][3], T* rowbuf /*3*ndof*/, T* brow /*3*/) {
+  auto val = [](const cplx& v) -> T {
+    if constexpr (std::is_same<T, double>::value) return v.real();
+    else return v;
+  };
+  const bool ck = P.crack_el[e] != 0;
   for (int il = 0; il < 3; ++il)
     for (int ik = 0; ik < 3; ++ik)
       for (int kn = 0; kn < 8; ++kn) {
         int s = P.conn[8 * e + kn];
         int col = P.dof[3 * s + ik];
-        T cv = (T)0;
-        if constexpr (std::is_same<T, double>::value) cv = P.cvalue[3 * s + ik].real();
-        else cv = P.cvalue[3 * s + ik];
+        T cv = val(P.cvalue[3 * s + ik]);
         if (P.ctype[3 * s + ik] == 0) {
-          rowbuf[il * P.ndof + col] = rowbuf[il * P.ndof + col] - g[kn][il][ik];
-          brow[il] = brow[il] - h[kn][il][ik] * cv;
+          rowbuf[il * P.ndof + col] = rowbuf[il * P.ndof + col] - gp[kn][il][ik];
+          brow[il] = brow[il] - hp[kn][il][ik] * cv;
         } else {
-          rowbuf[il * P.ndof + col] = rowbuf[il * P.ndof + col] + h[kn][il][ik];
-          brow[il] = brow[il] + g[kn][il][ik] * cv;
+          rowbuf[il * P.ndof + col] = rowbuf[il * P.ndof + col] + hp[kn][il][ik];
+          brow[il] = brow[il] + gp[kn][il][ik] * cv;
+        }
+        if (ck) {
+          int col2 = P.dof2[3 * s + ik];
+          T cv2 = val(P.cvalue2[3 * s + ik]);
+          if (P.ctype2[3 * s + ik] == 0) {
+            rowbuf[il * P.ndof + col2] = rowbuf[il * P.ndof + col2] - gm[kn][il][ik];
+            brow[il] = brow[il] - hm[kn][il][ik] * cv2;
+          } else {
+            rowbuf[il * P.ndof + col2] = rowbuf[il * P.ndof + col2] + hm[kn][il][ik];
+            brow[il] = brow[il] + gm[kn][il][ik] * cv2;
+          }
         }
       }
+}
+// integration kernels: face 2 of a crack-like element sees the reversed
+// normal, hm = -h, gm = g (build_lse_mechanics_bem_staela.f90:883-887)
+template <typename T>
+static void scatter(const Problem& P, int e, const T h[8][3][3], const T g[8][3][3], T* rowbuf, T* brow) {
+  if (!P.crack_el[e]) {
+    scatter4<T>(P, e, h, g, h, g, rowbuf, brow);
+    return;
+  }
+  T hm[8][3][3];
+  for (int a = 0; a < 8; ++a)
+    for (int il = 0; il < 3; ++il)
+      for (int ik = 0; ik < 3; ++ik) hm[a][il][ik] = -h[a][il][ik];
+  scatter4<T>(P, e, h, g, hm, g, rowbuf, brow);
 }
 
 // Free-term contribution for collocation node s (first element of the
 // collocation order carries it), build_lse_mechanics_bem_staela.f90:152-549.
 template <class K>
 static bool free_terms_for_node(const Problem& P, int s, typename K::T nu, typename K::T beta, typename K::T* rowbuf,
-                                typename K::T* brow) {
+                                typename K::T* brow, typename K::T* rowbuf2, typename K::T* brow2) {
   typedef typename K::T T;
   for (int ci : P.node_cps[s]) {
     const Colloc& cp = P.cps[ci];
     HG<K> hg;
     hg.zero();
+    if (cp.kind == 4) {
+      // crack-like point (dual BEM): SBIE equation 1/2 phi on both faces' u,
+      // HBIE equation -1/2 phi on face 1's t, +1/2 phi on face 2's t
+      // (build_lse_mechanics_bem_staela.f90:181-204)
+      double pphi[8];
+      phi_quad8(cp.xi, pphi);
+      HG<K> z, l1, l2;
+      z.zero();
+      l1.zero();
+      l2.zero();
+      for (int il = 0; il < 3; ++il)
+        for (int a = 0; a < 8; ++a) {
+          hg.h[a][il][il] = 0.5 * pphi[a];
+          l1.g[a][il][il] = -0.5 * pphi[a];
+          l2.g[a][il][il] = 0.5 * pphi[a];
+        }
+      scatter4<T>(P, cp.elem, hg.h, z.g, hg.h, z.g, rowbuf, brow);
+      scatter4<T>(P, cp.elem, z.h, l1.g, z.h, l2.g, rowbuf2, brow2);
+      continue;
+    }
     if (cp.kind == 0) {
       int nce = (int)P.node_el[s].size();
       std::vector<double> nset(3 * nce), tset(3 * nce);
@@ -1883,6 +1962,7 @@ static int assemble(const Problem& P, const K& k, MKH mkh, typename K::T bm, typ
   int bad = 0;
   bool has_hbie = false;
   for (int f : P.form) has_hbie = has_hbie || f != 0;
+  for (char c : P.crack) has_hbie = has_hbie || c != 0;
   if (has_hbie && P.hs_n != 0) return -5;
   long s_leaves = 0, s_points = 0, s_maxd = 0, s_sing = 0, s_adp = 0, s_pre = 0, s_hsing = 0, s_hadp = 0;
   long s_bpre = 0, s_badp = 0, s_bsing = 0;
@@ -1893,7 +1973,7 @@ static int assemble(const Problem& P, const K& k, MKH mkh, typename K::T bm, typ
   {
     g_hs_err = 0;
     g_hbie_err = 0;
-    std::vector<T> rowbuf(3 * (size_t)n);
+    std::vector<T> rowbuf(3 * (size_t)n), rowbuf2;
     AdpStats st;
     auto count = [&](int cls, long& sing, long& adp, long& pre) {
       if (cls == CLS_SING) sing++;
@@ -1904,11 +1984,30 @@ static int assemble(const Problem& P, const K& k, MKH mkh, typename K::T bm, typ
     for (int oi = 0; oi < nord; ++oi) {
       int s = P.node_order[oi];
       std::fill(rowbuf.begin(), rowbuf.end(), (T)0);
-      T brow[3] = {(T)0, (T)0, (T)0};
+      if (P.crack[s]) rowbuf2.assign(3 * (size_t)n, (T)0);
+      T brow[3] = {(T)0, (T)0, (T)0}, brow2[3] = {(T)0, (T)0, (T)0};
       for (int e = 0; e < P.ne; ++e) {
         for (int ci : P.node_cps[s]) {
           const Colloc& cp = P.cps[ci];
           HG<K> hg;
+          if (cp.kind == 4) {
+            // dual BEM: the SBIE into the node's first equation, the HBIE into
+            // its second, each with both faces of a crack-like element
+            // (build_lse_mechanics_bem_staela.f90:783-830,1000-1010)
+            KH kh = mkh(cp.n);
+            HG<KH> ml;
+            if constexpr (kHarmonic) {
+              int c = shbie_auto(k, kh, P.el[e], false, cp.x, P.qsp, P.ns_max, hg, ml, &st);
+              count(c, s_sing, s_adp, s_pre);
+              count(c, s_bsing, s_badp, s_bpre);
+            } else {
+              count(sbie_auto<K>(k, P.el[e], false, cp.x, P.qsp, P.ns_max, hg, &st), s_sing, s_adp, s_pre);
+              count(hbie_auto<KH>(kh, P.el[e], false, cp.x, P.qsp, P.ns_max, ml, true, &st), s_bsing, s_badp, s_bpre);
+            }
+            scatter<T>(P, e, hg.h, hg.g, rowbuf.data(), brow);
+            scatter<T>(P, e, ml.h, ml.g, rowbuf2.data(), brow2);
+            continue;
+          }
           if (cp.kind <= 1) {
             count(sbie_auto<K>(k, P.el[e], false, cp.x, P.qsp, P.ns_max, hg, &st), s_sing, s_adp, s_pre);
             if constexpr (std::is_same<K, StaelaK>::value) {
@@ -1958,11 +2057,16 @@ static int assemble(const Problem& P, const K& k, MKH mkh, typename K::T bm, typ
           scatter<T>(P, e, hg.h, hg.g, rowbuf.data(), brow);
         }
       }
-      if (!free_terms_for_node<K>(P, s, nu, bm, rowbuf.data(), brow)) bad++;
+      if (!free_terms_for_node<K>(P, s, nu, bm, rowbuf.data(), brow, rowbuf2.data(), brow2)) bad++;
       for (int il = 0; il < 3; ++il) {
         int r = P.dof[3 * s + il];
         for (int c = 0; c < n; ++c) A[(size_t)c * n + r] = A[(size_t)c * n + r] + rowbuf[(size_t)il * n + c];
         b[r] = b[r] + brow[il];
+        if (P.crack[s]) {
+          int r2 = P.dof2[3 * s + il];
+          for (int c = 0; c < n; ++c) A[(size_t)c * n + r2] = A[(size_t)c * n + r2] + rowbuf2[(size_t)il * n + c];
+          b[r2] = b[r2] + brow2[il];
+        }
       }
     }
     s_leaves += st.leaves;
@@ -2069,8 +2173,36 @@ void* orc_problem_new(int nn, const double* X, int ne, const int* conn, const in
   for (int i = 0; i < n_ps; ++i) P->ps_gln[i] = ps_gln[i];
   qs_calculate_parameters(qsi_re, P->qsp);
   build(*P);
+  build_dofs(*P);
   build_colloc(*P);
   return P;
+}
+// Crack-like boundary: crack_el [ne] marks its elements (their nodes get two
+// faces), ctype2 [nn][3] and cvalue2 [nn][3] (complex) the boundary conditions
+// of face 2 (face 1: the problem's ctype / cvalue). Renumbers the DOF and
+// rebuilds the collocation points. Returns -1 if a crack node also belongs
+// to an ordinary element (a node lies in one boundary, data_structures.f90:
+// 1433-1452).
+int orc_problem_set_crack(void* h, const char* crack_el, const int* ctype2, const double* cvalue2) {
+  Problem* P = (Problem*)h;
+  std::vector<char> cn(P->nn, 0), on(P->nn, 0);
+  for (int e = 0; e < P->ne; ++e)
+    for (int k = 0; k < 8; ++k) (crack_el[e] ? cn : on)[P->conn[8 * e + k]] = 1;
+  for (int s = 0; s < P->nn; ++s)
+    if (cn[s] && on[s]) return -1;
+  P->crack_el.assign(crack_el, crack_el + P->ne);
+  P->crack = cn;
+  for (int i = 0; i < 3 * P->nn; ++i) {
+    P->ctype2[i] = ctype2[i];
+    P->cvalue2[i] = cplx(cvalue2[2 * i], cvalue2[2 * i + 1]);
+  }
+  build_dofs(*P);
+  build_colloc(*P);
+  return 0;
+}
+void orc_dof2_map(void* h, int* dof2 /*3*nn*/) {
+  Problem* P = (Problem*)h;
+  for (int i = 0; i < 3 * P->nn; ++i) dof2[i] = P->dof2[i];
 }
 // BEM formulation per node (0 default SBIE, 1 'hbie', 2 'dual_bm_same'),
 // alpha and delta_hbie per node (null: 1 and 0.22540333, the quadratic

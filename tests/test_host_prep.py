@@ -92,6 +92,58 @@ def test_prep_hbie_points_match_oracle(oracle, form):
         L.mfbem_prep_free(pp)
 
 
+@pytest.mark.parametrize("mk", [lambda: M.penny_crack(1.0, 2, 2, 1.0), lambda: M.penny_crack_in_box(1.0, 2, 1, 2.0, 2)],
+                         ids=["penny", "penny_in_box"])
+def test_prep_crack_matches_oracle(oracle, mk):
+    """Crack-like boundaries: the six-row DOF layout of the crack nodes
+    (src/build_auxiliary_variables_mechanics_static.f90:146-207), their
+    (hbie, dual, dual_is_common) = (1, 2, 1) and points, as the oracle's."""
+    deck, (ce, ct2, cv2) = mk()
+    L, pp, keep = _prep(deck)
+    try:
+        nn, ne = deck.n_nodes, deck.n_elements
+        cei = np.ascontiguousarray(ce, dtype=np.int32)
+        ct2 = np.ascontiguousarray(ct2, dtype=np.int32)
+        cv2 = np.ascontiguousarray(cv2, dtype=np.complex128)
+        assert L.mfbem_prep_set_crack(pp, cei.ctypes.data_as(_abi._ip), ct2.ctypes.data_as(_abi._ip),
+                                      cv2.view(np.float64).ctypes.data_as(_abi._dp)) == 0
+        P = oracle.Problem(deck)
+        P.set_crack(ce, ct2, cv2)
+        desc = L.mfbem_prep_desc(pp).contents
+        assert desc.n_dof == P.n == 3 * nn + 3 * len(np.unique(deck.conn[ce]))
+        dof = np.zeros(3 * nn, dtype=np.int32)
+        order = np.zeros(nn, dtype=np.int32)
+        dof2 = np.zeros(3 * nn, dtype=np.int32)
+        L.mfbem_prep_dof(pp, dof.ctypes.data_as(_abi._ip), order.ctypes.data_as(_abi._ip))
+        L.mfbem_prep_dof2(pp, dof2.ctypes.data_as(_abi._ip))
+        odof, oorder = P.dof_map()
+        assert np.array_equal(dof.reshape(-1, 3), odof) and np.array_equal(order, oorder)
+        assert np.array_equal(dof2.reshape(-1, 3), P.dof2_map())
+        row = np.ctypeslib.as_array(desc.row, shape=(3 * nn,)).reshape(-1, 3)
+        assert np.array_equal(row - 1, odof)
+        dd = L.mfbem_prep_dual(pp).contents
+        cn = np.zeros(nn, bool)
+        cn[np.unique(deck.conn[ce])] = True
+        hb = np.ctypeslib.as_array(dd.hbie, shape=(nn,))
+        du = np.ctypeslib.as_array(dd.dual, shape=(nn,))
+        co = np.ctypeslib.as_array(dd.dual_is_common, shape=(nn,))
+        assert np.array_equal(hb, cn) and np.array_equal(du, 2 * cn) and np.array_equal(co, cn)
+        assert np.array_equal(np.ctypeslib.as_array(dd.crack_el, shape=(ne,)), cei)
+        x, info = P.colloc()
+        xh = np.ctypeslib.as_array(dd.x_i_hbie, shape=(24 * ne,)).reshape(ne, 8, 3)
+        sel = np.nonzero(info[:, 1] == 4)[0]
+        assert len(sel) == 8 * ce.sum()
+        for i in sel:
+            assert np.abs(xh[info[i, 2], info[i, 3]] - x[i]).max() <= 1e-15
+        # a crack node in an ordinary element is refused
+        bad = cei.copy()
+        bad[0] = 0
+        assert L.mfbem_prep_set_crack(pp, bad.ctypes.data_as(_abi._ip), ct2.ctypes.data_as(_abi._ip),
+                                      cv2.view(np.float64).ctypes.data_as(_abi._dp)) == -1
+    finally:
+        L.mfbem_prep_free(pp)
+
+
 def test_library_exports_every_declared_symbol():
     L = _abi.load()
     hdr = open(os.path.join(ROOT, "include", "mfbem.h")).read()
