@@ -806,10 +806,11 @@ __device__ __forceinline__ void harela_point_ff(const HarParF& q, const ff rv[3]
     const ff dri = sel3(dr, il), drk = sel3(dr, ik), ni = sel3(n, il), nk = sel3(n, ik);
     const ff rr = ff_mul(dri, drk);
     const ff s1 = il == ik ? ff_add(ff_mul(drk, ni), drdn) : ff_mul(drk, ni);
-    cf t = cf_scale(T1, ff_mul(rr, drdn));
-    t = cf_fma_r(T2, s1, t);
-    t = cf_fma_r(T3, ff_mul(dri, nk), t);
-    ft[c] = t;
+    cf t = cf_zero();
+    acc_cmac_r(t, T1, ff_mul(rr, drdn));
+    acc_cmac_r(t, T2, s1);
+    acc_cmac_r(t, T3, ff_mul(dri, nk));
+    ft[c] = cf_norm(t);
     if (ik >= il) {
       cf u = cf_neg(cf_scale(chi, rr));
       if (il == ik) u = cf_add(u, psi);
@@ -1043,13 +1044,14 @@ __global__ void __launch_bounds__(WPB * 32, 4) k_mixed(DMesh m, const HarParF* p
           for (int j = 0; j < kAcc; ++j) {
             const int o = lane + 32 * j;
             if (o < kOut) {
+              // compensated accumulation (lo unnormalised until the flush)
               if (o < 72) {
                 const int kn = o / 9, cc = o % 9;
-                acc[j] = cf_fma_r(S[t].ft[cc], S[t].w[kn], acc[j]);
-                if constexpr (SG) acc[j] = cf_fma_r(S[t].fc[cc], S[t].wd[kn], acc[j]);
+                acc_cmac_r(acc[j], S[t].ft[cc], S[t].w[kn]);
+                if constexpr (SG) acc_cmac_r(acc[j], S[t].fc[cc], S[t].wd[kn]);
               } else {
                 const int kn = (o - 72) / 6;
-                acc[j] = cf_fma_r(S[t].fu[(o - 72) % 6], S[t].w[kn], acc[j]);
+                acc_cmac_r(acc[j], S[t].fu[(o - 72) % 6], S[t].w[kn]);
               }
             }
           }
