@@ -967,6 +967,17 @@ __global__ void __launch_bounds__(WPB * 32, 4) k_mixed(DMesh m, const HarParF* p
   const ff* dcv_f = pn_f + 3LL * m.ne * m.ptot;
   double2* Acf = Ac + astride_e * f;
   cf bc[3] = {cf_zero(), cf_zero(), cf_zero()};
+  // this lane's output slots: byte offset of its kernel value in the point's
+  // ComboF (t* or u* component) << 4 | element node; -1 past the 120 outputs.
+  // One path for both kinds, so no slot diverges between t* and u* lanes.
+  int slot[kAcc];
+#pragma unroll
+  for (int j = 0; j < kAcc; ++j) {
+    const int o = lane + 32 * j;
+    if (o < 72) slot[j] = (int)((offsetof(ComboF<SG>, ft) + sizeof(cf) * (o % 9)) << 4) | (o / 9);
+    else if (o < kOut) slot[j] = (int)((offsetof(ComboF<SG>, fu) + sizeof(cf) * ((o - 72) % 6)) << 4) | ((o - 72) / 6);
+    else slot[j] = -1;
+  }
   for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
     int s0, s1;
     const long long* pts;
@@ -1040,18 +1051,17 @@ __global__ void __launch_bounds__(WPB * 32, 4) k_mixed(DMesh m, const HarParF* p
           }
         }
         if (t < nt) {
+          const char* St = reinterpret_cast<const char*>(&S[t]);
 #pragma unroll
           for (int j = 0; j < kAcc; ++j) {
-            const int o = lane + 32 * j;
-            if (o < kOut) {
+            const int sl = slot[j];
+            if (sl >= 0) {
               // compensated accumulation (lo unnormalised until the flush)
-              if (o < 72) {
-                const int kn = o / 9, cc = o % 9;
-                acc_cmac_r(acc[j], S[t].ft[cc], S[t].w[kn]);
-                if constexpr (SG) acc_cmac_r(acc[j], S[t].fc[cc], S[t].wd[kn]);
-              } else {
-                const int kn = (o - 72) / 6;
-                acc_cmac_r(acc[j], S[t].fu[(o - 72) % 6], S[t].w[kn]);
+              const int kn = sl & 15;
+              acc_cmac_r(acc[j], *reinterpret_cast<const cf*>(St + (sl >> 4)), S[t].w[kn]);
+              if constexpr (SG) {
+                const int o = lane + 32 * j;
+                if (o < 72) acc_cmac_r(acc[j], S[t].fc[o % 9], S[t].wd[kn]);
               }
             }
           }

@@ -260,18 +260,22 @@ def test_static_solve_gmres_refinement(oracle):
 
 def test_sweep_batch_of_uneven_meshes(oracle):
     """Sweeps of meshes of different size in one call (concurrent on the GPU)
-    agree with each mesh's plain FP64 sweep to 1e-8 (mixed precision), and the
-    cube's with the FP64 oracle."""
+    agree with each mesh's plain FP64 sweep to max(1e-8, 1e-14 / rcond) (mixed
+    precision: double-float pair sums, entries within about 1e-14 of the
+    binary64 assembly; the thin slab's 1/rcond reaches 6.7e6), and the cube's
+    with the FP64 oracle."""
     from multifebe_gb300 import sweep_harela_batch
     decks = [M.cube_clamped_top_traction(2), M.cube_clamped_top_traction(3), M.slab(3, 1)]
     mat = M.viscoelastic(1.0, 0.25, 1.0, 0.05)
     oms = [M.omega_from_a0([0.3, 1.1], mat), M.omega_from_a0([0.5], mat), M.omega_from_a0([0.2, 0.9, 1.4], mat)]
     regions = [BemRegion(d) for d in decks]
     X, stats = sweep_harela_batch(regions, mat, oms, precision="mixed")
-    for r, om, x, st in zip(regions, oms, X, stats):
+    for d, r, om, x, st in zip(decks, regions, oms, X, stats):
         xp = r.sweep_harela(mat, om, precision="plain")
+        Po = oracle.Problem(d)
         for i in range(len(om)):
-            assert rel(x[i], xp[i]) < 1e-8
+            _, rc = oracle.lu_solve(*Po.assemble_harela(mat, om[i]), rcond=True)
+            assert rel(x[i], xp[i]) < max(1e-8, 1e-14 / rc), (d.name, i, rel(x[i], xp[i]), 1.0 / rc)
         assert st["max_backward_error"] <= 1e-12
     P = oracle.Problem(decks[1])
     Ao, bo = P.assemble_harela(mat, oms[1][0])

@@ -11,10 +11,10 @@ Tolerances (max-norm relative, per frequency): plain FP64 path <= 1e-10,
 mixed path (complex64 LU + FP64 refinement) <= 1e-8; on the slab, whose
 systems are ill-conditioned (1/rcond up to about 1e7), both against the oracle
 within max(their bar, 1e-12 / rcond) -- the FP64 method's own sensitivity to
-the ~1e-12 differences of two FP64 assemblies -- and the mixed path within
-1e-8 of the plain path. The mixed path's assembled binary64 system
-(double-float evaluation) is compared entry by entry with the oracle's system
-on two small meshes.
+the ~1e-12 differences of two FP64 assemblies -- and the mixed path
+(double-float pair sums) within max(1e-8, 1e-14 / rcond) of the plain path.
+The mixed path's assembled binary64 system (double-float evaluation) is
+compared entry by entry with the oracle's system on two small meshes.
 """
 import numpy as np
 import pytest
@@ -74,8 +74,10 @@ def test_slab16_sweep(slab16):
     """The slab's systems are ill-conditioned (1/rcond about 1e7 at a0 = 0.2):
     the device and the oracle assemble the same system to about 1e-12, and
     that difference is amplified in both paths alike. Both paths against the
-    oracle: within max(their bar, 1e-12 / rcond); the mixed path against the
-    plain FP64 GPU path on the same assembled systems: <= 1e-8."""
+    oracle: within max(their bar, 1e-12 / rcond). The mixed path evaluates the
+    pairs in double-float (entries within about 1e-14 of the binary64
+    assembly), so against the plain FP64 GPU path: within
+    max(1e-8, 1e-14 / rcond)."""
     deck, mat, om, P, xs, rconds = slab16
     R = BemRegion(deck)
     Xp = R.sweep_harela(mat, om, precision="plain")
@@ -85,7 +87,7 @@ def test_slab16_sweep(slab16):
         print("a0", [0.2, 1.0][i], "plain", ep, "mixed", em, "mixed vs plain", emp, "1/rcond", 1.0 / rconds[i])
         assert ep < max(1e-10, 1e-12 / rconds[i])
         assert em < max(1e-8, 1e-12 / rconds[i])
-        assert emp < 1e-8
+        assert emp < max(1e-8, 1e-14 / rconds[i])
     R.close()
 
 
