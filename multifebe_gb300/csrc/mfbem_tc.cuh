@@ -8,14 +8,20 @@
 //   B~ (2k x n)  = B viewed as real (same memory)
 //   A~ (2m x 2k) : A~(2i,2l) = re a_il, A~(2i+1,2l) = im a_il,
 //                  A~(2i,2l+1) = -im a_il, A~(2i+1,2l+1) = re a_il
-// so C~ -= A~ B~ is C -= A B. A CTA (4 warps) computes a 128 x 128 tile of C~
-// (64 complex rows x 128 columns): per chunk of 32 real K it stages A~ and B~
-// (hi and lo parts) in shared memory in the canonical K-major layout without
-// swizzle (8-row x 16-byte core matrices, 128 B apart along K, 1024 B apart
-// along M/N), thread 0 issues 4 K-steps x 3 products of
-// tcgen05.mma.cta_group::1.kind::tf32 (M 128, N 128, K 8) into a 128-column
-// TMEM accumulator and commits to an mbarrier; after the last chunk every
-// warp reads its 32 TMEM lanes (tcgen05.ld 32x32b) and subtracts from C.
+// so C~ -= A~ B~ is C -= A B. Operand tiles live in shared memory in the
+// canonical K-major layout without swizzle (8-row x 16-byte core matrices,
+// 128 B apart along K, 1024 B apart along M/N); one thread issues
+// tcgen05.mma.cta_group::1.kind::tf32 (K 8) into a TMEM accumulator and
+// commits to an mbarrier; every warp then reads its 32 TMEM lanes
+// (tcgen05.ld 32x32b) and subtracts from C. Two kernels:
+//   k_tc_cgemm         each CTA splits and stages its own 128 x 128 tile's
+//                      operands (kept as the self-contained variant the
+//                      tests compare against);
+//   k_tc_cgemm_bulk<NH> the LU's trailing update: operands split once into
+//                      tf32 hi / lo tiles by k_tc_prep_a / k_tc_prep_b, copied
+//                      by cp.async.bulk into a two-stage pipeline; NH = 2 runs
+//                      one M 128 x N 256 MMA per K step (two 128-column
+//                      halves in 256 TMEM columns, two CTAs per SM).
 // Every wait is bounded: on a timeout the kernel sets *err, waits (bounded)
 // for its MMAs, frees its TMEM and returns.
 #pragma once
