@@ -130,10 +130,19 @@ int mfbem_mesh_release(mfbem_handle* h);
                 the static builder (build_lse_mechanics_bem_staela.f90:835-841)
                 and alpha i / c2 in the harmonic one, c2 = sqrt(mu / rho) the
                 complex S-wave speed (build_lse_mechanics_bem_harela.f90:1174-1181).
+     (1, 1, 0)  'dual_bm_mixed': the node's SBIE at its own point (nodal, or
+                MCA by its sbie flag at x_i_sbie_mca) plus beta times the
+                HBIE at the points x_i_hbie of its elements, integrated on
+                their own (sbie_auto and hbie_auto in both builders,
+                src/read_bem_formulation_selected_nodes.f90:243-295). The
+                reference's non-common branch keeps a nodal SBIE's h of the
+                node's first element for its later ones (the rows it
+                assembles are not this weighted sum); the library assembles
+                the weighted sum;
      (1, 2, 1)  a node of a crack-like boundary (fbem_dual_boundary,
                 src/assign_default_bem_formulation.f90:94-128): the SBIE and
                 the HBIE at the same points x_i_hbie, each its own equation.
-   Other combinations ('dual_bm_mixed') return MFBEM_EUNSUPPORTED.
+   Other combinations return MFBEM_EUNSUPPORTED.
    Crack-like boundaries (boundary class cracklike, src/read_boundaries.f90:
    105; dual BEM): crack_el marks their elements (NULL: none), whose nodes
    belong to no ordinary element and carry two faces, face 1 with the

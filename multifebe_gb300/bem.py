@@ -40,14 +40,15 @@ class BemRegion:
     """One BE region (ordinary boundaries, continuous quad8) on the GPU.
 
     formulation: None / 'sbie' (the default SBIE with MCA at mesh-boundary
-    nodes), 'hbie' or 'dual_bm' ('dual_bm_same': Burton & Miller with weight
-    alpha), for every node or as an array of codes per node (0, 1, 2); delta
+    nodes), 'hbie', 'dual_bm' ('dual_bm_same': Burton & Miller with weight
+    alpha at common points) or 'dual_bm_mixed' (the SBIE at its own nodal or
+    MCA point), for every node or as an array of codes per node (0..3); delta
     moves the HBIE points into the elements (default 0.22540333). crack:
     (crack_el [ne] bool, ctype2 [nn, 3], cvalue2 [nn, 3]) marks the elements
     of crack-like boundaries (dual BEM) and gives face 2's conditions; the
     deck's ctype / cvalue are face 1's. See mfbem_mesh_upload_dual."""
 
-    FORMULATIONS = {"sbie": 0, "hbie": 1, "dual_bm": 2}
+    FORMULATIONS = {"sbie": 0, "hbie": 1, "dual_bm": 2, "dual_bm_mixed": 3}
 
     def __init__(self, deck, formulation=None, alpha=None, delta=None, crack=None, **settings):
         s = dict(DEFAULT_SETTINGS)
@@ -79,7 +80,7 @@ class BemRegion:
         a = np.ascontiguousarray(np.broadcast_to(1.0 if alpha is None else alpha, (nn,)), dtype=np.float64)
         dl = np.ascontiguousarray(np.broadcast_to(0.22540333 if delta is None else delta, (nn,)), dtype=np.float64)
         if L.mfbem_prep_set_formulation(self._prep, _p(f, _ip), _p(a), _p(dl)) != 0:
-            raise ValueError("formulation codes must be 0, 1 or 2")
+            raise ValueError("formulation codes must be 0, 1, 2 or 3")
         if crack is not None:
             ce = np.ascontiguousarray(np.asarray(crack[0], dtype=bool), dtype=np.int32)
             ct2 = np.ascontiguousarray(crack[1], dtype=np.int32)

@@ -109,6 +109,29 @@ struct mfbem_prep {
 
 namespace {
 
+// MCA collocation points of the mesh-boundary nodes: xi moved from the edge by
+// 0.05 (assign_default_bem_formulation.f90:39,85-92), or by the quadratic
+// default 0.22540333 for a 'dual_bm_mixed' node
+// (read_bem_formulation_selected_nodes.f90:273-294).
+void mca_points(mfbem_prep* P) {
+  for (int e = 0; e < P->ne; ++e)
+    for (int k = 0; k < 8; ++k) {
+      const int s = P->element_node[8 * e + k] - 1;
+      if (!P->sbie[s]) continue;
+      const double dl = (!P->form.empty() && P->form[s] == 3) ? 0.22540333 : 0.05;
+      double x1 = q8xi(k, 0), x2 = q8xi(k, 1);
+      if (on_quad_edge(x1, x2)) { x1 = x1 * (1.0 - dl); x2 = x2 * (1.0 - dl); }
+      P->xi_mca[16 * (size_t)e + 2 * k] = x1;
+      P->xi_mca[16 * (size_t)e + 2 * k + 1] = x2;
+      double phi[8];
+      phi_q8<double>(x1, x2, phi);
+      double xp[3] = {0, 0, 0};
+      for (int q = 0; q < 8; ++q)
+        for (int c = 0; c < 3; ++c) xp[c] = xp[c] + phi[q] * P->x_gn[24 * (size_t)e + 3 * q + c];
+      for (int c = 0; c < 3; ++c) P->x_mca[24 * (size_t)e + 3 * k + c] = xp[c];
+    }
+}
+
 // DOF numbering, src/build_auxiliary_variables_mechanics_static.f90:60-207:
 // nodes in order of first appearance over the elements; an ordinary node
 // takes rows r, r+1, r+2 (col = row of the unknown of each direction); a
@@ -168,7 +191,7 @@ void rebuild_dual(mfbem_prep* P) {
       continue;
     }
     P->hbie[s] = P->form[s] != 0;
-    P->dualv[s] = P->form[s] == 2;
+    P->dualv[s] = P->form[s] >= 2;
     P->common[s] = P->form[s] == 2;
   }
   P->xi_hbie.assign(16 * (size_t)ne, 0.0);
@@ -276,22 +299,7 @@ extern "C" mfbem_prep* mfbem_prep_create(int32_t nn, const double* X, int32_t ne
     }
   P->sbie.assign(nn, 0);
   for (int s = 0; s < nn; ++s) P->sbie[s] = inb[s] ? 1 : 0;
-  // MCA collocation points, delta = 0.05 (assign_default_bem_formulation.f90:39,85-92)
-  for (int e = 0; e < ne; ++e)
-    for (int k = 0; k < 8; ++k) {
-      int s = conn[8 * e + k];
-      if (!inb[s]) continue;
-      double x1 = q8xi(k, 0), x2 = q8xi(k, 1);
-      if (on_quad_edge(x1, x2)) { x1 = x1 * (1.0 - 0.05); x2 = x2 * (1.0 - 0.05); }
-      P->xi_mca[16 * (size_t)e + 2 * k] = x1;
-      P->xi_mca[16 * (size_t)e + 2 * k + 1] = x2;
-      double phi[8];
-      phi_q8<double>(x1, x2, phi);
-      double xp[3] = {0, 0, 0};
-      for (int q = 0; q < 8; ++q)
-        for (int c = 0; c < 3; ++c) xp[c] = xp[c] + phi[q] * P->x_gn[24 * (size_t)e + 3 * q + c];
-      for (int c = 0; c < 3; ++c) P->x_mca[24 * (size_t)e + 3 * k + c] = xp[c];
-    }
+  mca_points(P);
   P->ctype.assign(ctype, ctype + 3 * (size_t)nn);
   P->cvalue.assign(cvalue, cvalue + 6 * (size_t)nn);
   number_dofs(P);
@@ -321,16 +329,16 @@ extern "C" mfbem_prep* mfbem_prep_create(int32_t nn, const double* X, int32_t ne
 }
 
 // BEM formulation per node, as src/read_bem_formulation_selected_nodes.f90:
-// 70-260 sets it for an ordinary boundary of continuous elements: form 0 SBIE
+// 70-295 sets it for an ordinary boundary of continuous elements: form 0 SBIE
 // (the default of assign_default_bem_formulation.f90), 1 'hbie', 2
-// 'dual_bm_same' with weight alpha; delta moves the HBIE point of each element
-// node into the element (the quadratic default 0.22540333 when delta <= 0).
-// Returns -1 for a code out of range.
+// 'dual_bm_same', 3 'dual_bm_mixed' (both with weight alpha); delta moves the
+// HBIE point of each element node into the element (the quadratic default
+// 0.22540333 when delta <= 0). Returns -1 for a code out of range.
 extern "C" int mfbem_prep_set_formulation(mfbem_prep* P, const int32_t* form, const double* alpha,
                                           const double* delta) {
   const int nn = P->nn;
   for (int s = 0; s < nn; ++s)
-    if (form[s] < 0 || form[s] > 2) return -1;
+    if (form[s] < 0 || form[s] > 3) return -1;
   P->form.assign(form, form + nn);
   P->alpha.assign(nn, 1.0);
   P->delta.assign(nn, 0.0);
@@ -338,6 +346,7 @@ extern "C" int mfbem_prep_set_formulation(mfbem_prep* P, const int32_t* form, co
     if (alpha) P->alpha[s] = alpha[s];
     if (delta) P->delta[s] = delta[s];
   }
+  mca_points(P);
   rebuild_dual(P);
   return 0;
 }

@@ -585,7 +585,8 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
         dcv[2 * dof] = cv[6 * s + 2 * k];
         dcv[2 * dof + 1] = cv[6 * s + 2 * k + 1];
       }
-  // formulation per node: 0 SBIE, 1 HBIE alone, 2 Burton & Miller (dual desc)
+  // formulation per node: 0 SBIE, 1 HBIE alone, 2 Burton & Miller at common points,
+  // 3 crack-like node (dual BEM), 4 Burton & Miller with the SBIE at its own point
   std::vector<int> form(nn, 0);
   if (dual) {
     if (!dual->hbie || !dual->dual || !dual->dual_is_common || !dual->alpha || !dual->xi_i_hbie || !dual->x_i_hbie ||
@@ -609,12 +610,13 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
       if (hb == 0 && du == 0 && co == 0) form[s] = 0;
       else if (hb == 1 && du == 0 && co == 0) form[s] = 1;
       else if (hb == 1 && du == 1 && co == 1) form[s] = 2;
+      else if (hb == 1 && du == 1 && co == 0) form[s] = 4;
       else {
         delete h;
         return fail(MFBEM_EUNSUPPORTED, "node " + std::to_string(s + 1) +
-                                            ": only SBIE, 'hbie' and 'dual_bm_same' formulations are available");
+                                            ": only SBIE, 'hbie', 'dual_bm_same' and 'dual_bm_mixed' formulations are available");
       }
-      if (form[s] == 2 && !std::isfinite(dual->alpha[s])) {
+      if ((form[s] == 2 || form[s] == 4) && !std::isfinite(dual->alpha[s])) {
         delete h;
         return fail(MFBEM_EARG, "Burton & Miller alpha must be finite");
       }
@@ -628,7 +630,7 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
   for (int e = 0; e < ne; ++e)
     for (int k = 0; k < 8; ++k) {
       int s = d->element_node[8 * e + k] - 1;
-      if (form[s] != 0) continue;
+      if (form[s] != 0 && form[s] != 4) continue;  // 'dual_bm_mixed': SBIE here, HBIE in its view
       CP c;
       c.dn = dn_of[s];
       c.e = e;
@@ -768,13 +770,13 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
           mfbem_mesh_release(h);
           return fail(MFBEM_EARG, "the HBIE cannot be collocated at an element edge (xi_i_hbie on the edge)");
         }
-        c.alpha = form[s] == 2 ? dual->alpha[s] : 1.0;
+        c.alpha = (form[s] == 2 || form[s] == 4) ? dual->alpha[s] : 1.0;
         c.dn = dn_of[s];
-        c.kind = form[s] == 1 ? 2 : (form[s] == 2 ? 3 : 4);
+        c.kind = form[s] == 1 ? 2 : (form[s] == 2 ? 3 : (form[s] == 3 ? 4 : 5));
         c.e = e;
         c.kn = k;
         hb.push_back(c);
-        if (form[s] >= 2) {
+        if (form[s] == 2 || form[s] == 3) {
           // the SBIE part (Burton & Miller) or equation (crack-like node)
           c.kind = 1;
           bm.push_back(c);

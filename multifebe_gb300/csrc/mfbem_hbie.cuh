@@ -13,14 +13,22 @@
 //   free terms                k_hfree (-1/2 phi(xi_i) on l, and 1/2 phi(xi_i)
 //                             on h for Burton & Miller).
 // Each point's equation is h = m, g = l ('hbie'), or adds beta (m, l) to the
-// SBIE at the same point (Burton & Miller): beta = alpha in the static
-// builder (build_lse_mechanics_bem_staela.f90:835-841), alpha i / c2 in the
-// harmonic one (build_lse_mechanics_bem_harela.f90:1174-1181, c2 the complex
-// S-wave speed). beta is folded into the integrands here, so the rows of both
-// views simply add into A and b.
+// SBIE at the same point (Burton & Miller, 'dual_bm_same') or to the node's
+// SBIE at its own nodal / MCA point ('dual_bm_mixed', whose SBIE points sit in
+// the SBIE view): beta = alpha in the static builder
+// (build_lse_mechanics_bem_staela.f90:835-841), alpha i / c2 in the harmonic
+// one (build_lse_mechanics_bem_harela.f90:1174-1181, c2 the complex S-wave
+// speed). beta is folded into the integrands here, so the rows of both views
+// simply add into A and b. Crack-like nodes put their HBIE in rows of their
+// own (k_hfree and the scatter).
 #pragma once
 
 namespace mfb {
+
+// HBIE points weighted by the Burton & Miller factor beta alpha: kind 3
+// ('dual_bm_same') and 5 ('dual_bm_mixed'); kinds 2 ('hbie') and 4
+// (crack-like node) take weight 1.
+__host__ __device__ __forceinline__ bool hbie_weighted(int kind) { return kind == 3 || kind == 5; }
 
 // d* (fd, integrated into l) and s* (fs, into m) at one point for the
 // collocation normal ni, without their constants.
@@ -117,13 +125,13 @@ struct PolHbieStatic {
   double nu, cted1, cted2, ctes1, ctes2, ctes3;
   const double* cpn;    // [ncp][3] collocation normals
   const double* cpa;    // [ncp] Burton & Miller alpha
-  const int* cpk;       // [ncp] 2 HBIE alone, 3 Burton & Miller
+  const int* cpk;       // [ncp] kind: 2 HBIE alone, 3 Burton & Miller, 4 crack-like, 5 'dual_bm_mixed'
   __device__ T cte_t(int) const { return ctes1; }
   __device__ T cte_u(int) const { return cted1; }
   __device__ T cpv(int) const { return 0.0; }
   __device__ void point(int, int cp, const double rv[3], const double n[3], T fu[9], T ft[9]) const {
     hbie_point_s(nu, cted2, ctes2, ctes3, rv, n, cpn + 3 * (size_t)cp, fu, ft);
-    if (cpk[cp] == 3) {
+    if (hbie_weighted(cpk[cp])) {
       const double b = cpa[cp];
 #pragma unroll
       for (int q = 0; q < 9; ++q) {
@@ -146,7 +154,7 @@ struct PolHbieHarmonic {
   __device__ T cpv(int) const { return mk(0.0); }
   __device__ void point(int f, int cp, const double rv[3], const double n[3], T fu[9], T ft[9]) const {
     hbie_point_h(p[f], ph[f], rv, n, cpn + 3 * (size_t)cp, fu, ft);
-    if (cpk[cp] == 3) {
+    if (hbie_weighted(cpk[cp])) {
       const cd b = cpa[cp] * ph[f].ic2;
 #pragma unroll
       for (int q = 0; q < 9; ++q) {
@@ -324,7 +332,7 @@ __global__ void __launch_bounds__(32) k_hsing(DMesh m, HS hs, int nf, double* A,
   for (int cp = m.dn_cp[dn]; cp < m.dn_cp[dn + 1]; ++cp) {
     const int q0 = m.sing_start[cp], q1 = m.sing_start[cp + 1];
     if (q0 == q1) continue;
-    const T beta = m.cp_kind[cp] == 3 ? k.bm * m.cp_alpha[cp] : VT<T>::zero() + 1.0;
+    const T beta = hbie_weighted(m.cp_kind[cp]) ? k.bm * m.cp_alpha[cp] : VT<T>::zero() + 1.0;
     const long long P0 = m.sing_pt[q0], Q = m.sing_pt[q1] - P0;
     int cur = -1;
     T acc[NA], as0 = z, as1 = z;
@@ -486,9 +494,11 @@ __global__ void k_hfree(DMesh m, const HarParH* ph, int nf, double* A, size_t ld
         }
       continue;
     }
+    // Burton & Miller: the SBIE's 1/2 phi(xi_i) on h here too ('dual_bm_same';
+    // 'dual_bm_mixed' has it at its own SBIE point in the SBIE view)
     const bool bm = m.cp_kind[cp] == 3;
     T beta = z + 1.0;
-    if (bm) {
+    if (hbie_weighted(m.cp_kind[cp])) {
       if constexpr (std::is_same<T, cd>::value) beta = ph[f].ic2 * m.cp_alpha[cp];
       else beta = z + m.cp_alpha[cp];
     }

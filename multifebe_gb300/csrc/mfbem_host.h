@@ -35,7 +35,7 @@ const mfbem_mesh_desc* mfbem_prep_desc(const mfbem_prep* p);
 void mfbem_prep_free(mfbem_prep* p);
 /* diagnostic copies: dof [nn][3] 0-based (row-1); node order [nn] */
 void mfbem_prep_dof(const mfbem_prep* p, int32_t* dof, int32_t* order);
-/* BEM formulation per node (0 SBIE, 1 'hbie', 2 'dual_bm_same'), Burton &
+/* BEM formulation per node (0 SBIE, 1 'hbie', 2 'dual_bm_same', 3 'dual_bm_mixed'), Burton &
    Miller alpha and HBIE point offset delta per node (NULL: 1 and 0.22540333);
    mfbem_prep_dual then returns the descriptor for mfbem_mesh_upload_dual
    (NULL before). */

@@ -149,12 +149,13 @@ class Problem:
             -5: "HBIE formulations in a half-space region are not available",
             -6: "the HBIE cannot be collocated at an element edge"}
 
-    FORMULATIONS = {"sbie": 0, "hbie": 1, "dual_bm": 2}
+    FORMULATIONS = {"sbie": 0, "hbie": 1, "dual_bm": 2, "dual_bm_mixed": 3}
 
     def set_formulation(self, form, alpha=None, delta=None):
         """BEM formulation of every node (src/read_bem_formulation_selected_nodes.f90):
         form is one name of FORMULATIONS for all nodes or an array of codes per
-        node (0 default SBIE, 1 'hbie', 2 'dual_bm_same'); alpha (Burton &
+        node (0 default SBIE, 1 'hbie', 2 'dual_bm_same', 3 'dual_bm_mixed');
+        alpha (Burton &
         Miller weight) and delta (HBIE point offset, default 0.22540333) per
         node or scalar. Rebuilds the collocation points."""
         nn = self.deck.n_nodes
@@ -163,7 +164,7 @@ class Problem:
         a = np.ascontiguousarray(np.broadcast_to(1.0 if alpha is None else alpha, (nn,)), dtype=np.float64)
         dl = np.ascontiguousarray(np.broadcast_to(0.22540333 if delta is None else delta, (nn,)), dtype=np.float64)
         if lib().orc_problem_set_formulation(self._h, _p(f, _ip), _p(a), _p(dl)) != 0:
-            raise ValueError("formulation codes must be 0, 1 or 2")
+            raise ValueError("formulation codes must be 0, 1, 2 or 3")
 
     def set_crack(self, crack_el, ctype2, cvalue2):
         """Crack-like boundary (dual BEM): crack_el [ne] bool marks its

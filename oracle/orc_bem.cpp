@@ -1605,7 +1605,9 @@ static bool freeterm(int ne, const double* n, const double* t, double tol, T nu,
 struct Colloc {
   double x[3];
   int node;     // collocation node (rows)
-  int kind;     // 0 SBIE (nodal), 1 SBIE MCA, 2 HBIE, 3 SBIE + HBIE (Burton & Miller) at one point
+  int kind;     // 0 SBIE (nodal), 1 SBIE MCA, 2 HBIE, 3 SBIE + HBIE (Burton & Miller) at one point,
+                // 4 SBIE and HBIE of a crack-like node, 5 the HBIE part of 'dual_bm_mixed'
+                // (beta alpha HBIE at its own point; the node's SBIE at its kind 0 / 1 point)
   int elem, kn; // element/local node it was taken from
   double xi[2];
   double n[3];  // unit normal at xi (HBIE kinds)
@@ -1764,6 +1766,31 @@ static void build_dofs(Problem& P) {
 // points: xi moved from the element edge by delta_hbie
 // (src/build_data_at_collocation_points.f90:148-160) and the unit normal there
 // (:368-376).
+// HBIE point of element e's local node k: xi moved from the edge by dl
+// (fbem_move_xi1xi2_from_edge), x there and the element's unit normal.
+static void hbie_point(const Problem& P, int e, int k, double dl, Colloc& cp) {
+  double xi[2] = {quad8_xi_nodes[k][0], quad8_xi_nodes[k][1]};
+  if (check_xi1xi2_edge_quad(xi)) { xi[0] = xi[0] * (1.0 - dl); xi[1] = xi[1] * (1.0 - dl); }
+  double d1[8], d2[8], phi[8];
+  dphi_quad8(xi, d1, d2);
+  phi_quad8(xi, phi);
+  double T1[3] = {0, 0, 0}, T2[3] = {0, 0, 0}, x[3] = {0, 0, 0};
+  for (int q = 0; q < 8; ++q)
+    for (int c = 0; c < 3; ++c) {
+      T1[c] = T1[c] + d1[q] * P.el[e].x[q][c];
+      T2[c] = T2[c] + d2[q] * P.el[e].x[q][c];
+      x[c] = x[c] + phi[q] * P.el[e].x[q][c];
+    }
+  double N[3] = {T1[1] * T2[2] - T1[2] * T2[1], T1[2] * T2[0] - T1[0] * T2[2], T1[0] * T2[1] - T1[1] * T2[0]};
+  double jn = std::sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+  for (int c = 0; c < 3; ++c) {
+    cp.n[c] = N[c] / jn;
+    cp.x[c] = x[c];
+  }
+  cp.xi[0] = xi[0];
+  cp.xi[1] = xi[1];
+}
+
 static void build_colloc(Problem& P) {
   const int nn = P.nn, ne = P.ne;
   P.cps.clear();
@@ -1776,7 +1803,17 @@ static void build_colloc(Problem& P) {
       cp.node = s; cp.elem = e; cp.kn = k;
       cp.n[0] = cp.n[1] = cp.n[2] = 0.0;
       double xi[2] = {quad8_xi_nodes[k][0], quad8_xi_nodes[k][1]};
-      if (P.form[s] != 0 || P.crack[s]) {
+      if (P.form[s] == 3 && !P.crack[s]) {
+        // 'dual_bm_mixed': the HBIE at its own point of this element (kind 5,
+        // weight beta alpha), the SBIE at the node's usual point below
+        // (src/read_bem_formulation_selected_nodes.f90:243-295)
+        Colloc hb = cp;
+        hb.kind = 5;
+        hbie_point(P, e, k, P.delta_hbie[s], hb);
+        P.node_cps[s].push_back((int)P.cps.size());
+        P.cps.push_back(hb);
+      }
+      if ((P.form[s] != 0 && P.form[s] != 3) || P.crack[s]) {
         // crack-like nodes: SBIE and HBIE at the same MCA point, each its own
         // equation (dual BEM, assign_default_bem_formulation.f90:94-128)
         double dl = P.delta_hbie[s];
@@ -1919,7 +1956,7 @@ static bool free_terms_for_node(const Problem& P, int s, typename K::T nu, typen
       // l, which is g ('hbie', dual = 0) or weighted by beta into g (Burton &
       // Miller) (build_lse_mechanics_bem_staela.f90:181-211,440-489,
       // build_lse_mechanics_bem_harela.f90:316-360,598-681)
-      if (cp.kind != 2)
+      if (cp.kind != 2 && cp.kind != 5)
         for (int il = 0; il < 3; ++il)
           for (int a = 0; a < 8; ++a) hg.h[a][il][il] = hg.h[a][il][il] + 0.5 * pphi[a];
       if (cp.kind >= 2) {
@@ -2031,7 +2068,15 @@ static int assemble(const Problem& P, const K& k, MKH mkh, typename K::T bm, typ
             KH kh = mkh(cp.n);
             HG<KH> ml;
             T w = (T)1.0;
-            if (cp.kind == 2) {
+            if (cp.kind == 5) {
+              // 'dual_bm_mixed': the HBIE alone at its own point, weighted by
+              // beta alpha (separate hbie_auto in both builders,
+              // build_lse_mechanics_bem_staela.f90:938-997,
+              // build_lse_mechanics_bem_harela.f90:1244-1284)
+              count(hbie_auto<KH>(kh, P.el[e], false, cp.x, P.qsp, P.ns_max, ml, true, &st), s_bsing, s_badp, s_bpre);
+              hg.zero();
+              w = bm * P.alpha[s];
+            } else if (cp.kind == 2) {
               // 'hbie': h = m, g = l
               count(hbie_auto<KH>(kh, P.el[e], false, cp.x, P.qsp, P.ns_max, ml, true, &st), s_bsing, s_badp, s_bpre);
               hg.zero();
@@ -2211,11 +2256,16 @@ void orc_dof2_map(void* h, int* dof2 /*3*nn*/) {
 int orc_problem_set_formulation(void* h, const int* form, const double* alpha, const double* delta) {
   Problem* P = (Problem*)h;
   for (int s = 0; s < P->nn; ++s)
-    if (form[s] < 0 || form[s] > 2) return -1;
+    if (form[s] < 0 || form[s] > 3) return -1;
   for (int s = 0; s < P->nn; ++s) {
     P->form[s] = form[s];
     P->alpha[s] = alpha ? alpha[s] : 1.0;
     P->delta_hbie[s] = delta ? delta[s] : 0.22540333;
+    // 'dual_bm_mixed' on the mesh boundary: the SBIE's MCA point moves by the
+    // quadratic default 0.22540333 instead of the boundary default 0.05
+    // (read_bem_formulation_selected_nodes.f90:273-294)
+    if (P->in_boundary[s])
+      for (auto& pr : P->node_el[s]) P->delta_mca[8 * pr.first + pr.second] = form[s] == 3 ? 0.22540333 : 0.05;
   }
   build_colloc(*P);
   return 0;

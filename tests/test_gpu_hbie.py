@@ -1,5 +1,6 @@
-"""HBIE collocation on the boundary ('hbie' and 'dual_bm_same' formulations)
-on the device against the oracle, through the C-ABI (mfbem_mesh_upload_dual).
+"""HBIE collocation on the boundary ('hbie', 'dual_bm_same' and
+'dual_bm_mixed' formulations) on the device against the oracle, through the
+C-ABI (mfbem_mesh_upload_dual).
 
 The oracle restates the builders' HBIE branches (build_lse_mechanics_bem_staela.f90:
 783-842,938-997, build_lse_mechanics_bem_harela.f90:1144-1284), hbie_auto /
@@ -37,9 +38,11 @@ def hbie_counts(R):
 
 
 def mixed_codes(d):
-    """Per-node codes: SBIE, 'hbie' and Burton & Miller nodes in one region."""
+    """Per-node codes: SBIE, 'hbie', 'dual_bm_same' and 'dual_bm_mixed' nodes
+    in one region."""
     f = np.full(d.n_nodes, 2, dtype=np.int32)
     f[d.nodes[:, 2] > 0.99] = 1
+    f[d.nodes[:, 1] < 0.01] = 3
     f[d.nodes[:, 0] < 0.01] = 0
     return f
 
@@ -70,7 +73,7 @@ def tol_of(sens, floor):
 
 DECKS = [("cube2", lambda: M.cube_clamped_top_traction(2)), ("kat2", lambda: M.cube_confined_kat(2)),
          ("patch", lambda: M.surface_patch(2.0, 4, 1.0))]
-FORMS = ["hbie", "dual_bm", "codes"]
+FORMS = ["hbie", "dual_bm", "dual_bm_mixed", "codes"]
 
 
 def form_of(name, d):
@@ -140,7 +143,7 @@ def test_static_solve_burton_miller(oracle, precision, tol):
 
 
 @pytest.mark.parametrize("precision,tol", [("plain", 1e-10), ("mixed", 1e-8)])
-@pytest.mark.parametrize("form", ["hbie", "dual_bm"])
+@pytest.mark.parametrize("form", ["hbie", "dual_bm", "dual_bm_mixed"])
 def test_harmonic_sweep(oracle, form, precision, tol):
     """ME-TH-EL-001 column: the sweep's solutions equal the oracle's LU
     solutions and converge to the closed form like the oracle's."""
@@ -163,11 +166,11 @@ def test_hbie_errors():
         R.set_halfspace(-3, 0.0, 1)
     assert e.value.code == _abi.MFBEM_EUNSUPPORTED
     R.close()
-    # a combination outside the three formulations ('dual_bm_mixed')
+    # a combination outside the formulations (dual without the HBIE)
     R0 = BemRegion(d)
     L = _abi.load()
     nn, ne = d.n_nodes, d.n_elements
-    keep = [np.ones(nn, np.int32), np.ones(nn, np.int32), np.zeros(nn, np.int32), np.ones(nn),
+    keep = [np.zeros(nn, np.int32), np.ones(nn, np.int32), np.ones(nn, np.int32), np.ones(nn),
             np.zeros(16 * ne), np.zeros(24 * ne), np.zeros(24 * ne)]
     dd = _abi.DualDesc(*[k.ctypes.data_as(_abi._ip if k.dtype == np.int32 else _abi._dp) for k in keep])
     h = ctypes.c_void_p()

@@ -57,15 +57,16 @@ def test_prep_matches_oracle_bit_exact(oracle, deck):
         L.mfbem_prep_free(pp)
 
 
-@pytest.mark.parametrize("form", ["hbie", "dual_bm"])
+@pytest.mark.parametrize("form", ["hbie", "dual_bm", "dual_bm_mixed"])
 def test_prep_hbie_points_match_oracle(oracle, form):
     """HBIE points and their unit normals (src/build_data_at_collocation_points.f90:
-    148-160,368-376) and the node members of the dual descriptor."""
+    148-160,368-376), the node members of the dual descriptor and the MCA
+    points ('dual_bm_mixed' moves them by 0.22540333)."""
     deck = M.cube_confined_kat(2)
     L, pp, keep = _prep(deck)
     try:
         nn, ne = deck.n_nodes, deck.n_elements
-        code = {"hbie": 1, "dual_bm": 2}[form]
+        code = {"hbie": 1, "dual_bm": 2, "dual_bm_mixed": 3}[form]
         f = np.full(nn, code, dtype=np.int32)
         f[::5] = 0  # a few nodes keep the SBIE
         a = np.linspace(0.5, 1.5, nn)
@@ -76,7 +77,7 @@ def test_prep_hbie_points_match_oracle(oracle, form):
         hb = np.ctypeslib.as_array(dd.hbie, shape=(nn,))
         du = np.ctypeslib.as_array(dd.dual, shape=(nn,))
         co = np.ctypeslib.as_array(dd.dual_is_common, shape=(nn,))
-        assert np.array_equal(hb, f != 0) and np.array_equal(du, f == 2) and np.array_equal(co, f == 2)
+        assert np.array_equal(hb, f != 0) and np.array_equal(du, f >= 2) and np.array_equal(co, f == 2)
         xh = np.ctypeslib.as_array(dd.x_i_hbie, shape=(24 * ne,)).reshape(ne, 8, 3)
         nh = np.ctypeslib.as_array(dd.n_i_hbie, shape=(24 * ne,)).reshape(ne, 8, 3)
         P = oracle.Problem(deck)
@@ -88,6 +89,12 @@ def test_prep_hbie_points_match_oracle(oracle, form):
         for i in sel:
             assert np.abs(xh[info[i, 2], info[i, 3]] - x[i]).max() <= 1e-15
             assert np.abs(nh[info[i, 2], info[i, 3]] - nrm[i]).max() <= 1e-15
+        desc = L.mfbem_prep_desc(pp).contents
+        xm = np.ctypeslib.as_array(desc.x_i_sbie_mca, shape=(24 * ne,)).reshape(ne, 8, 3)
+        mca = np.nonzero(info[:, 1] == 1)[0]
+        assert len(mca) > 0
+        for i in mca:
+            assert np.array_equal(xm[info[i, 2], info[i, 3]], x[i])
     finally:
         L.mfbem_prep_free(pp)
 

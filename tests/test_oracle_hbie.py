@@ -13,9 +13,9 @@ and shbie_auto (:4888-4957) against identities and closed forms:
   - the harmonic kernels tend to the static ones as omega -> 0;
   - a plane P wave satisfies the harmonic identity to the discretisation
     error, which shrinks with the mesh;
-  - the builders with 'dual_bm_same' and 'hbie' formulations reproduce the
-    closed forms of docs/examples/ME-ST-EL-002 (confined cube, exact linear
-    field) and ME-TH-EL-001 (P-wave column).
+  - the builders with 'dual_bm_same', 'hbie' and 'dual_bm_mixed'
+    formulations reproduce the closed forms of docs/examples/ME-ST-EL-002
+    (confined cube, exact linear field) and ME-TH-EL-001 (P-wave column).
 """
 import numpy as np
 import pytest
@@ -122,7 +122,7 @@ def test_plane_wave_identity_converges(oracle):
     assert errs[0] < 5e-3 and errs[1] < 1e-3 and errs[1] < errs[0] / 3, errs
 
 
-@pytest.mark.parametrize("form", ["dual_bm", "hbie"])
+@pytest.mark.parametrize("form", ["dual_bm", "hbie", "dual_bm_mixed"])
 def test_confined_cube_static(oracle, form):
     """ME-ST-EL-002 through the static builder: Burton & Miller (alpha = 1,
     build_lse_mechanics_bem_staela.f90:835-841) and HBIE alone."""
@@ -139,7 +139,7 @@ def test_confined_cube_static(oracle, form):
     assert P.stats[10] == 8 * d.n_elements
 
 
-@pytest.mark.parametrize("form", ["dual_bm", "hbie"])
+@pytest.mark.parametrize("form", ["dual_bm", "hbie", "dual_bm_mixed"])
 def test_p_wave_column_harmonic(oracle, form):
     """ME-TH-EL-001 through the harmonic builder (Burton & Miller weight
     alpha i / c2, build_lse_mechanics_bem_harela.f90:1174-1181)."""
@@ -184,11 +184,60 @@ def test_burton_miller_is_the_weighted_sum(oracle):
     assert np.abs(b1 - (b0 + alpha * bh)).max() < 1e-13 * max(np.abs(b1).max(), 1.0)
 
 
+@pytest.mark.parametrize("harmonic", [False, True])
+def test_dual_bm_mixed_is_the_weighted_sum(oracle, harmonic):
+    """'dual_bm_mixed' (src/read_bem_formulation_selected_nodes.f90:243-295):
+    the node's SBIE at its own point (nodal, or MCA on the mesh boundary) plus
+    beta alpha times the HBIE at the HBIE points of its elements, each
+    integrated on its own (sbie_auto, hbie_auto), so the system is the SBIE
+    system plus beta alpha times the 'hbie' system. The reference's
+    non-common branch keeps the SBIE's h of a nodal point for the node's
+    later elements; the oracle and the library assemble the weighted sum.
+    (One closed boundary: every SBIE point nodal, as in the 'sbie' system.)"""
+    d = M.box((1.0, 1.0, 1.0), (2, 2, 2), split_faces=False)
+    d.ctype[d.nodes[:, 2] < 1e-12] = 0
+    d.cvalue[d.nodes[:, 2] < 1e-12] = (0.1, -0.2, 0.3)
+    d.cvalue[d.nodes[:, 2] > 1 - 1e-12] = (0.0, 0.0, -1.0)
+    alpha = 0.7
+    sysd = {}
+    for form in ("dual_bm_mixed", "hbie", "sbie"):
+        P = oracle.Problem(d)
+        P.set_formulation(form, alpha=alpha)
+        if harmonic:
+            mat = M.viscoelastic(2.4, 0.2, 1.0, 0.02)
+            sysd[form] = P.assemble_harela(mat, 2.0)
+        else:
+            sysd[form] = P.assemble_staela(MU, NU)
+    beta = alpha * 1j / np.sqrt(mat["mu"] / mat["rho"]) if harmonic else alpha
+    (A1, b1), (Ah, bh), (A0, b0) = sysd["dual_bm_mixed"], sysd["hbie"], sysd["sbie"]
+    assert np.abs(A1 - (A0 + beta * Ah)).max() < 1e-14 * np.abs(A1).max()
+    assert np.abs(b1 - (b0 + beta * bh)).max() < 1e-14 * max(np.abs(b1).max(), 1.0)
+
+
+def test_dual_bm_mixed_points(oracle):
+    """'dual_bm_mixed' collocation points: one HBIE point per element of the
+    node (delta_hbie) and the SBIE at the node (nodal) or, on a mesh boundary,
+    at MCA points moved by the quadratic default 0.22540333
+    (read_bem_formulation_selected_nodes.f90:243-295)."""
+    d = M.cube_confined_kat(1)  # six boundaries: every node on a mesh boundary
+    P = oracle.Problem(d)
+    P.set_formulation("dual_bm_mixed", delta=0.3)
+    x, info = P.colloc()
+    kinds = info[:, 1]
+    assert (kinds == 5).sum() == 8 * d.n_elements and (kinds == 1).sum() == 8 * d.n_elements
+    assert (kinds == 0).sum() == 0
+    on_x1 = np.all(np.abs(d.nodes[d.conn[info[:, 2]]][:, :, 0] - 1.0) < 1e-12, axis=1)
+    yz = {k: set(map(tuple, np.round(x[on_x1 & (kinds == k)][:, 1:], 10))) for k in (1, 5)}
+    c1, c5 = 0.5 * 0.22540333, 0.5 * 0.3
+    assert (c1, c1) in yz[1] and (1 - c1, 1 - c1) in yz[1]
+    assert (c5, c5) in yz[5] and (1 - c5, 1 - c5) in yz[5]
+
+
 def test_formulation_errors(oracle):
     d = M.halfspace_footing(1.0, 2, 1.0)
     P = oracle.Problem(d)
     with pytest.raises(ValueError):
-        P.set_formulation(np.full(d.n_nodes, 3))
+        P.set_formulation(np.full(d.n_nodes, 4))
     P.set_formulation("dual_bm")
     P.set_halfspace(-3, 0.0, 1)
     with pytest.raises(RuntimeError, match="half-space"):
