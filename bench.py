@@ -56,15 +56,15 @@ FLOPS_PER_REGULAR_POINT = 1280
 # formulation of the same kernel could at best run at this rate
 FP64_NOMINAL_TFLOPS = 1.25
 # DRAM bytes per frequency of that kernel from ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum of one launch of the 2-frequency profile case, 454.5 +
-# 393.5 MB, divided by 2; profiles/k_mixed_cube8x2freq.md): A written once
+# dram__bytes_write.sum of one launch of the 2-frequency profile case, 453.4 +
+# 392.9 MB, divided by 2; profiles/k_mixed_cube8x2freq.md): A written once
 # and read back once (the flush adds into the zeroed system). Traffic grows in
 # proportion to the frequencies (one system per frequency).
-REG_TRAFFIC_PER_FREQ = 424.0e6
+REG_TRAFFIC_PER_FREQ = 423.2e6
 # Pipe utilisation of the same launch (ncu --set full, same small case and
 # file): the kernel is bound by instruction issue on the FP32 pipe
 # (double-float arithmetic), not by HBM.
-REG_NCU_PIPES = {"issue_slots_busy_pct": 60.0, "fp32_fma_pipe_pct": 42.5, "fp64_pipe_pct": 21.6,
+REG_NCU_PIPES = {"issue_slots_busy_pct": 61.4, "fp32_fma_pipe_pct": 40.0, "fp64_pipe_pct": 26.3,
                  "source": "profiles/k_mixed_cube8x2freq.md"}
 
 
