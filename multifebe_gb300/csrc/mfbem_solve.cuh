@@ -74,9 +74,10 @@ static int tc_cgemm_run(cudaStream_t st, const float2* A, int lda, long long sA,
   uint32_t* alo = ahi + wa;
   uint32_t* bhi = alo + wa;
   uint32_t* blo = bhi + wb;
-  k_tc_prep_a<<<(unsigned)std::min<size_t>((wa + 255) / 256, 152 * 32), 256, 0, st>>>(A, lda, sA, m, k, nmt, nkc, batch, ahi, alo);
+  // one block per tile (wa / TQ_TW and wb / TQ_TW tiles)
+  k_tc_prep_a<<<(unsigned)(wa / TQ_TW), 256, 0, st>>>(A, lda, sA, m, k, nmt, nkc, batch, ahi, alo);
   ++g_launches;
-  k_tc_prep_b<<<(unsigned)std::min<size_t>((wb + 255) / 256, 152 * 32), 256, 0, st>>>(B, ldb, sB, k, n, nnt, nkc, batch, bhi, blo);
+  k_tc_prep_b<<<(unsigned)(wb / TQ_TW), 256, 0, st>>>(B, ldb, sB, k, n, nnt, nkc, batch, bhi, blo);
   ++g_launches;
   if (wide)
     k_tc_cgemm_bulk<2><<<dim3(nmt, (nnt + 1) / 2, batch), 128, tc_smem_bulk<2>(), st>>>(

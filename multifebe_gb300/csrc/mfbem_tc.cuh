@@ -271,48 +271,45 @@ __device__ __forceinline__ void tq_rk(int w, int& r, int& kk) {
   kk = (cm % (TQ / 4)) * 4 + (w & 3);
 }
 
-// A~ tiles: [batch][row tile][K chunk][word]
-__global__ void k_tc_prep_a(const float2* A, int lda, long long sA, int m, int k, int nmt, int nkc, int batch,
-                            uint32_t* hi, uint32_t* lo) {
-  const long long total = (long long)batch * nmt * nkc * TQ_TW;
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
-    const int w = (int)(g % TQ_TW);
-    long long tl = g / TQ_TW;
-    const int kc = (int)(tl % nkc);
-    tl /= nkc;
-    const int mt = (int)(tl % nmt);
-    const int b = (int)(tl / nmt);
+// A~ tiles: [batch][row tile][K chunk][word]. One 256-thread block per tile
+// (blockIdx.x = (b * nmt + mt) * nkc + kc), eight words per thread: the tile
+// coordinates are decoded once per block, not per word.
+__global__ void __launch_bounds__(256) k_tc_prep_a(const float2* A, int lda, long long sA, int m, int k, int nmt,
+                                                   int nkc, int batch, uint32_t* hi, uint32_t* lo) {
+  const int kc = (int)(blockIdx.x % nkc), tl = (int)(blockIdx.x / nkc), mt = tl % nmt, b = tl / nmt;
+  const float2* Ab = A + sA * b;
+  const size_t g0 = (size_t)blockIdx.x * TQ_TW;
+#pragma unroll 2
+  for (int w = threadIdx.x; w < TQ_TW; w += 256) {
     int r, kk;
     tq_rk(w, r, kk);
     const int i = mt * (TC_BM / 2) + (r >> 1), l = kc * (TQ / 2) + (kk >> 1);
     float2 a = make_float2(0.0f, 0.0f);
-    if (i < m && l < k) a = A[sA * b + (size_t)l * lda + i];
+    if (i < m && l < k) a = Ab[(size_t)l * lda + i];
     const float v = (kk & 1) ? ((r & 1) ? a.x : -a.y) : ((r & 1) ? a.y : a.x);
     const uint32_t h = f2tf32(v);
-    hi[g] = h;
-    lo[g] = f2tf32(v - __uint_as_float(h));
+    hi[g0 + w] = h;
+    lo[g0 + w] = f2tf32(v - __uint_as_float(h));
   }
 }
-// B~ tiles: [batch][column tile][K chunk][word]; element (jj, kk) is component kk&1 of b(l, j)
-__global__ void k_tc_prep_b(const float2* B, int ldb, long long sB, int k, int n, int nnt, int nkc, int batch,
-                            uint32_t* hi, uint32_t* lo) {
-  const long long total = (long long)batch * nnt * nkc * TQ_TW;
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
-    const int w = (int)(g % TQ_TW);
-    long long tl = g / TQ_TW;
-    const int kc = (int)(tl % nkc);
-    tl /= nkc;
-    const int nt = (int)(tl % nnt);
-    const int b = (int)(tl / nnt);
+// B~ tiles: [batch][column tile][K chunk][word]; element (jj, kk) is component
+// kk&1 of b(l, j). One block per tile as k_tc_prep_a.
+__global__ void __launch_bounds__(256) k_tc_prep_b(const float2* B, int ldb, long long sB, int k, int n, int nnt,
+                                                   int nkc, int batch, uint32_t* hi, uint32_t* lo) {
+  const int kc = (int)(blockIdx.x % nkc), tl = (int)(blockIdx.x / nkc), nt = tl % nnt, b = tl / nnt;
+  const float2* Bb = B + sB * b;
+  const size_t g0 = (size_t)blockIdx.x * TQ_TW;
+#pragma unroll 2
+  for (int w = threadIdx.x; w < TQ_TW; w += 256) {
     int jj, kk;
     tq_rk(w, jj, kk);
     const int j = nt * TC_BN + jj, l = kc * (TQ / 2) + (kk >> 1);
     float2 bv = make_float2(0.0f, 0.0f);
-    if (l < k && j < n) bv = B[sB * b + (size_t)j * ldb + l];
+    if (l < k && j < n) bv = Bb[(size_t)j * ldb + l];
     const float v = (kk & 1) ? bv.y : bv.x;
     const uint32_t h = f2tf32(v);
-    hi[g] = h;
-    lo[g] = f2tf32(v - __uint_as_float(h));
+    hi[g0 + w] = h;
+    lo[g0 + w] = f2tf32(v - __uint_as_float(h));
   }
 }
 
