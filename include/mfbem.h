@@ -157,7 +157,8 @@ int mfbem_mesh_release(mfbem_handle* h);
    equation takes 1/2 phi(xi_i) on both faces' u, the HBIE -1/2 phi(xi_i) on
    face 1's t and +1/2 phi(xi_i) on face 2's (staela.f90:195-204,
    build_lse_mechanics_bem_harela.f90:344-360). Internal points of such a
-   region are MFBEM_EUNSUPPORTED. The HBIE points are classified as hbie_auto does
+   region: mfbem_internal_points_faces_staela / _harela.
+   The HBIE points are classified as hbie_auto does
    (lib/fbem/src/bem_staela3d.f90:4307-4373, 1/r^7 estimate); the element
    holding a point takes the interior (hypersingular) integration
    (bem_staela3d.f90:4918-5353, bem_harela3d.f90:3169-3630); the SBIE part of
@@ -252,6 +253,20 @@ int mfbem_internal_points_staela(mfbem_handle* h, double mu, double nu, int32_t 
 int mfbem_internal_points_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
                                  double omega, int32_t n_ip, const double* x_ip, const double* u_nodes,
                                  const double* t_nodes, double* u_ip, double* sigma_ip);
+/* The same for a region with crack-like boundaries: u2_nodes, t2_nodes
+   [n_nodes][3] hold face 2's solution (node%value(:, 2); read for the crack
+   nodes), which the reference integrates with the reversed element
+   (calculate_internal_points_mechanics_static.f90:320-354,431-465,
+   calculate_internal_points_mechanics_bem_harela.f90:343-470). The two
+   functions above return MFBEM_EUNSUPPORTED on such a region; a point at a
+   crack node (where the faces' values differ) returns MFBEM_EUNSUPPORTED. */
+int mfbem_internal_points_faces_staela(mfbem_handle* h, double mu, double nu, int32_t n_ip, const double* x_ip,
+                                       const double* u_nodes, const double* t_nodes, const double* u2_nodes,
+                                       const double* t2_nodes, double* u_ip, double* sigma_ip);
+int mfbem_internal_points_faces_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
+                                       double omega, int32_t n_ip, const double* x_ip, const double* u_nodes,
+                                       const double* t_nodes, const double* u2_nodes, const double* t2_nodes,
+                                       double* u_ip, double* sigma_ip);
 
 /* Gmsh *.msh 2.2 ASCII reader, host only: the gmsh branch of
    fbem_mesh%read_from_file (lib/fbem/src/mesh.f90:104-494) with its checks

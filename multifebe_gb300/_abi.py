@@ -38,6 +38,7 @@ ABI_SYMBOLS = [
     "mfbem_set_learned_quadrature", "mfbem_sweep_harela_batch", "mfbem_msh_read", "mfbem_msh_error",
     "mfbem_msh_sizes", "mfbem_msh_parts", "mfbem_msh_nodes", "mfbem_msh_elements", "mfbem_msh_free",
     "mfbem_nso_write", "mfbem_nso_error", "mfbem_fortran_format", "mfbem_set_halfspace", "mfbem_mesh_upload_dual",
+    "mfbem_internal_points_faces_staela", "mfbem_internal_points_faces_harela",
 ]
 PREP_SYMBOLS = ["mfbem_prep_create", "mfbem_prep_desc", "mfbem_prep_free", "mfbem_prep_dof",
                 "mfbem_prep_set_formulation", "mfbem_prep_set_crack", "mfbem_prep_dof2", "mfbem_prep_dual"]
@@ -104,6 +105,10 @@ def load():
     L.mfbem_solve_report.argtypes = [_dp, c_int32, _dp, _dp]
     L.mfbem_internal_points_staela.argtypes = [vp, c_double, c_double, c_int32, _dp, _dp, _dp, _dp, _dp]
     L.mfbem_internal_points_harela.argtypes = [vp, _dp, _dp, c_double, c_double, c_int32, _dp, _dp, _dp, _dp, _dp]
+    L.mfbem_internal_points_faces_staela.argtypes = [vp, c_double, c_double, c_int32, _dp, _dp, _dp, _dp, _dp, _dp,
+                                                     _dp]
+    L.mfbem_internal_points_faces_harela.argtypes = [vp, _dp, _dp, c_double, c_double, c_int32, _dp, _dp, _dp, _dp,
+                                                     _dp, _dp, _dp]
     L.mfbem_sweep_harela.argtypes = [vp, _dp, _dp, c_double, _dp, c_int32, _dp, c_int32, c_double, _dp, c_int32,
                                      ctypes.POINTER(Stats)]
     L.mfbem_solve_staela.argtypes = [vp, c_double, c_double, c_int32, c_double, _dp, c_int32, ctypes.POINTER(Stats)]

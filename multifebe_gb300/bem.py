@@ -206,11 +206,13 @@ class BemRegion:
         self.last_stats = st.as_dict()
         return x
 
-    def internal_points(self, xip, u, t, mat=None, omega=None, mu=None, nu=None):
+    def internal_points(self, xip, u, t, mat=None, omega=None, mu=None, nu=None, u2=None, t2=None):
         """calculate_internal_points_mechanics_bem_{staela,harela}: displacement
         [nip, 3] and stress tensor [nip, 3, 3] (sigma[:, il, kc]) at points
         inside the region from the nodal solution u, t [n_nodes, 3] (as
-        solution() returns it). Static with mu, nu; harmonic with mat, omega."""
+        solution() returns it; with crack-like boundaries also face 2's u2,
+        t2, as solution_faces() returns them). Static with mu, nu; harmonic
+        with mat, omega."""
         L = _abi.load()
         xip = np.ascontiguousarray(xip, dtype=np.float64).reshape(-1, 3)
         nip = len(xip)
@@ -219,13 +221,26 @@ class BemRegion:
         u = np.ascontiguousarray(u, dtype=dt)
         t = np.ascontiguousarray(t, dtype=dt)
         assert u.shape == (self.deck.n_nodes, 3) and t.shape == u.shape
+        faces = u2 is not None
+        if faces:
+            u2 = np.ascontiguousarray(u2, dtype=dt)
+            t2 = np.ascontiguousarray(t2, dtype=dt)
+            assert u2.shape == u.shape and t2.shape == u.shape
         ui = np.zeros((nip, 3), dtype=dt)
         si = np.zeros((nip, 3, 3), dtype=dt)  # [ip][kc][il], as value_c(il, kc)
         if cplx:
             lam = np.array([complex(mat["lambda"]).real, complex(mat["lambda"]).imag])
             m = np.array([complex(mat["mu"]).real, complex(mat["mu"]).imag])
-            check(L.mfbem_internal_points_harela(self._h, _p(lam), _p(m), float(mat["rho"]), float(omega), nip,
-                                                 _p(xip), _p(u), _p(t), _p(ui), _p(si)))
+            if faces:
+                check(L.mfbem_internal_points_faces_harela(self._h, _p(lam), _p(m), float(mat["rho"]), float(omega),
+                                                           nip, _p(xip), _p(u), _p(t), _p(u2), _p(t2), _p(ui),
+                                                           _p(si)))
+            else:
+                check(L.mfbem_internal_points_harela(self._h, _p(lam), _p(m), float(mat["rho"]), float(omega), nip,
+                                                     _p(xip), _p(u), _p(t), _p(ui), _p(si)))
+        elif faces:
+            check(L.mfbem_internal_points_faces_staela(self._h, float(mu), float(nu), nip, _p(xip), _p(u), _p(t),
+                                                       _p(u2), _p(t2), _p(ui), _p(si)))
         else:
             check(L.mfbem_internal_points_staela(self._h, float(mu), float(nu), nip, _p(xip), _p(u), _p(t), _p(ui),
                                                  _p(si)))

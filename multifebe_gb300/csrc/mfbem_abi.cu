@@ -110,6 +110,7 @@ struct mfbem_handle {
   // like sbie_auto (static) / shbie_auto (harmonic), built at the first
   // assembly of each kind from ms_base (points only)
   bool has_hbie = false, has_bm = false, has_crack = false;
+  std::vector<char> crack_node;  // [nn] node of a crack-like boundary
   DMesh mb, ms_base, ms[2];
   bool ms_built[2] = {false, false};
   long long mb_pts[3] = {0, 0, 0}, ms_pts[2][3] = {{0, 0, 0}, {0, 0, 0}};
@@ -785,6 +786,7 @@ static int upload_impl(const mfbem_mesh_desc* d, const mfbem_dual_desc* dual, mf
     h->has_hbie = true;
     h->has_bm = !bm.empty();
     h->has_crack = ncrack > 0;
+    if (ncrack) h->crack_node = ckn;
     h->mb = m;
     if (ncrack) h->mb.dn_rb = dn_rb_h;
     if ((rc = upload_points(h, hb, nn, h->mb))) { mfbem_mesh_release(h); return rc; }
@@ -1266,12 +1268,34 @@ struct TmpBufs {
 
 template <class POL>
 static int internal_points_run(mfbem_handle* h, const POL& pol, int nf, int32_t n_ip, const double* x_ip,
-                               const double* u_nodes, const double* t_nodes, double* u_ip, double* sigma_ip) {
+                               const double* u_nodes, const double* t_nodes, const double* u2_nodes,
+                               const double* t2_nodes, double* u_ip, double* sigma_ip) {
   typedef typename POL::T T;
-  if (h->has_crack)
-    return fail(MFBEM_EUNSUPPORTED, "internal points of a region with crack-like boundaries are not available");
   const DMesh& m = h->m;
   const int nn = h->nn, ne = h->ne;
+  // crack-like boundaries: face 2 sees -h and g of the element, so
+  // g t1 - h u1 + g t2 + h u2 = g (t1 + t2) - h (u1 - u2) per node
+  // (calculate_internal_points_mechanics_static.f90:320-354, 431-465)
+  std::vector<T> ueff, teff;
+  if (h->has_crack) {
+    if (!u2_nodes || !t2_nodes)
+      return fail(MFBEM_EUNSUPPORTED, "a region with crack-like boundaries needs both faces' solution "
+                                      "(mfbem_internal_points_faces_staela / _harela)");
+    const T* u1 = (const T*)u_nodes;
+    const T* t1 = (const T*)t_nodes;
+    const T* u2 = (const T*)u2_nodes;
+    const T* t2 = (const T*)t2_nodes;
+    ueff.assign(u1, u1 + 3 * (size_t)nn);
+    teff.assign(t1, t1 + 3 * (size_t)nn);
+    for (int s = 0; s < nn; ++s)
+      if (h->crack_node[s])
+        for (int c = 0; c < 3; ++c) {
+          ueff[3 * s + c] = u1[3 * s + c] - u2[3 * s + c];
+          teff[3 * s + c] = t1[3 * s + c] + t2[3 * s + c];
+        }
+    u_nodes = (const double*)ueff.data();
+    t_nodes = (const double*)teff.data();
+  }
   TmpBufs tb;
   IpArgs a{};
   a.nip = n_ip;
@@ -1313,13 +1337,19 @@ static int internal_points_run(mfbem_handle* h, const POL& pol, int nf, int32_t 
   k_ip_reg<POL, WPB><<<nblk((long long)n_ip * nf, WPB), WPB * 32, 0, st>>>(m, a, pol); ++g_launches;
   CK(cudaGetLastError());
   std::vector<T> out(12 * (size_t)n_ip * nf);
+  std::vector<int> onn(h->has_crack ? n_ip : 0);
   int err = 0;
   CK(cudaMemcpyAsync(out.data(), a.out, ob, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&err, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (h->has_crack) CK(cudaMemcpyAsync(onn.data(), a.onnode, sizeof(int) * (size_t)n_ip, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (err != INT_MAX)
     return fail(MFBEM_EUNSUPPORTED, "internal point " + std::to_string(err - 1) +
                                         " lies on the boundary away from a node (needs the singular HBIE integration)");
+  for (int ip = 0; ip < (int)onn.size(); ++ip)
+    if (onn[ip] >= 0 && h->crack_node[onn[ip]])
+      return fail(MFBEM_EUNSUPPORTED, "internal point " + std::to_string(ip) +
+                                          " lies at a node of a crack-like boundary (two faces)");
   T* uo = (T*)u_ip;
   T* so = (T*)sigma_ip;
   for (size_t i = 0; i < (size_t)n_ip * nf; ++i) {
@@ -1329,9 +1359,9 @@ static int internal_points_run(mfbem_handle* h, const POL& pol, int nf, int32_t 
   return 0;
 }
 
-extern "C" int mfbem_internal_points_staela(mfbem_handle* h, double mu, double nu, int32_t n_ip, const double* x_ip,
-                                            const double* u_nodes, const double* t_nodes, double* u_ip,
-                                            double* sigma_ip) {
+static int internal_points_staela(mfbem_handle* h, double mu, double nu, int32_t n_ip, const double* x_ip,
+                                  const double* u_nodes, const double* t_nodes, const double* u2_nodes,
+                                  const double* t2_nodes, double* u_ip, double* sigma_ip) {
   g_err.clear();
   if (!h || n_ip < 0 || (n_ip > 0 && (!x_ip || !u_nodes || !t_nodes || !u_ip || !sigma_ip)))
     return fail(MFBEM_EARG, "invalid argument");
@@ -1347,12 +1377,25 @@ extern "C" int mfbem_internal_points_staela(mfbem_handle* h, double mu, double n
   pol.ctes1 = mu / (4.0 * kPi * (1.0 - nu));
   pol.ctes2 = 1.0 - 2.0 * nu;
   pol.ctes3 = 1.0 - 4.0 * nu;
-  return internal_points_run(h, pol, 1, n_ip, x_ip, u_nodes, t_nodes, u_ip, sigma_ip);
+  return internal_points_run(h, pol, 1, n_ip, x_ip, u_nodes, t_nodes, u2_nodes, t2_nodes, u_ip, sigma_ip);
+}
+extern "C" int mfbem_internal_points_staela(mfbem_handle* h, double mu, double nu, int32_t n_ip, const double* x_ip,
+                                            const double* u_nodes, const double* t_nodes, double* u_ip,
+                                            double* sigma_ip) {
+  return internal_points_staela(h, mu, nu, n_ip, x_ip, u_nodes, t_nodes, nullptr, nullptr, u_ip, sigma_ip);
+}
+extern "C" int mfbem_internal_points_faces_staela(mfbem_handle* h, double mu, double nu, int32_t n_ip,
+                                                  const double* x_ip, const double* u_nodes, const double* t_nodes,
+                                                  const double* u2_nodes, const double* t2_nodes, double* u_ip,
+                                                  double* sigma_ip) {
+  if (n_ip > 0 && (!u2_nodes || !t2_nodes)) return fail(MFBEM_EARG, "invalid argument");
+  return internal_points_staela(h, mu, nu, n_ip, x_ip, u_nodes, t_nodes, u2_nodes, t2_nodes, u_ip, sigma_ip);
 }
 
-extern "C" int mfbem_internal_points_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
-                                            double omega, int32_t n_ip, const double* x_ip, const double* u_nodes,
-                                            const double* t_nodes, double* u_ip, double* sigma_ip) {
+static int internal_points_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
+                                  double omega, int32_t n_ip, const double* x_ip, const double* u_nodes,
+                                  const double* t_nodes, const double* u2_nodes, const double* t2_nodes, double* u_ip,
+                                  double* sigma_ip) {
   g_err.clear();
   if (!h || !lambda || !mu || n_ip < 0 || (n_ip > 0 && (!x_ip || !u_nodes || !t_nodes || !u_ip || !sigma_ip)))
     return fail(MFBEM_EARG, "invalid argument");
@@ -1373,7 +1416,22 @@ extern "C" int mfbem_internal_points_harela(mfbem_handle* h, const double lambda
   IpHarmonic pol;
   pol.p = pd;
   pol.ph = ph;
-  return internal_points_run(h, pol, 1, n_ip, x_ip, u_nodes, t_nodes, u_ip, sigma_ip);
+  return internal_points_run(h, pol, 1, n_ip, x_ip, u_nodes, t_nodes, u2_nodes, t2_nodes, u_ip, sigma_ip);
+}
+extern "C" int mfbem_internal_points_harela(mfbem_handle* h, const double lambda[2], const double mu[2], double rho,
+                                            double omega, int32_t n_ip, const double* x_ip, const double* u_nodes,
+                                            const double* t_nodes, double* u_ip, double* sigma_ip) {
+  return internal_points_harela(h, lambda, mu, rho, omega, n_ip, x_ip, u_nodes, t_nodes, nullptr, nullptr, u_ip,
+                                sigma_ip);
+}
+extern "C" int mfbem_internal_points_faces_harela(mfbem_handle* h, const double lambda[2], const double mu[2],
+                                                  double rho, double omega, int32_t n_ip, const double* x_ip,
+                                                  const double* u_nodes, const double* t_nodes,
+                                                  const double* u2_nodes, const double* t2_nodes, double* u_ip,
+                                                  double* sigma_ip) {
+  if (n_ip > 0 && (!u2_nodes || !t2_nodes)) return fail(MFBEM_EARG, "invalid argument");
+  return internal_points_harela(h, lambda, mu, rho, omega, n_ip, x_ip, u_nodes, t_nodes, u2_nodes, t2_nodes, u_ip,
+                                sigma_ip);
 }
 
 // ---------------------------------------------------------------------------

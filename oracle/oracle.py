@@ -51,9 +51,10 @@ def lib():
                                           _lp]
         L.orc_assemble_harela_nu.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 8 + [_dp, _dp, ctypes.c_int, _lp]
         L.orc_internal_points_staela.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
-                                                 _dp, _dp, _dp, _dp, ctypes.c_int]
+                                                 _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int]
         L.orc_internal_points_harela.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 6 + [ctypes.c_int, _dp, _dp,
-                                                                                          _dp, _dp, ctypes.c_int]
+                                                                                          _dp, _dp, _dp, _dp,
+                                                                                          ctypes.c_int]
         L.orc_pair_staela.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                       _dp, _dp]
         L.orc_pair_harela.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6 + [_dp, _dp]
@@ -81,7 +82,7 @@ def lib():
 
 
 def _p(a, t=_dp):
-    return a.ctypes.data_as(t)
+    return None if a is None else a.ctypes.data_as(t)
 
 
 # settings defaults, src/read_settings.f90:86,101,143-145,164
@@ -272,26 +273,31 @@ class Problem:
                                     float(omega), _p(h), _p(g))
         return cls, h, g
 
-    def internal_points(self, xip, u, t, mat=None, omega=None, mu=None, nu=None, nthreads=0):
+    def internal_points(self, xip, u, t, mat=None, omega=None, mu=None, nu=None, nthreads=0, u2=None, t2=None):
         """Displacement [nip,3] and stresses [nip,3,3] (sigma[:, il, kc]) at
-        internal points from nodal u, t [nn,3]; static with mu, nu, harmonic
-        with mat, omega."""
+        internal points from nodal u, t [nn,3] (and face 2's u2, t2 with
+        crack-like boundaries); static with mu, nu, harmonic with mat, omega."""
         xip = np.ascontiguousarray(xip, dtype=np.float64)
         nip = len(xip)
         cplx = omega is not None
         dt = np.complex128 if cplx else np.float64
         u = np.ascontiguousarray(u, dtype=dt)
         t = np.ascontiguousarray(t, dtype=dt)
+        if u2 is not None:
+            u2 = np.ascontiguousarray(u2, dtype=dt)
+            t2 = np.ascontiguousarray(t2, dtype=dt)
         out = np.zeros((nip, 4, 3), dtype=dt)
         if cplx:
             lam, m = complex(mat["lambda"]), complex(mat["mu"])
             rc = lib().orc_internal_points_harela(self._h, lam.real, lam.imag, m.real, m.imag, float(mat["rho"]),
-                                                  float(omega), nip, _p(xip), _p(u), _p(t), _p(out), nthreads)
-        else:
-            rc = lib().orc_internal_points_staela(self._h, float(mu), float(nu), nip, _p(xip), _p(u), _p(t), _p(out),
+                                                  float(omega), nip, _p(xip), _p(u), _p(t), _p(u2), _p(t2), _p(out),
                                                   nthreads)
+        else:
+            rc = lib().orc_internal_points_staela(self._h, float(mu), float(nu), nip, _p(xip), _p(u), _p(t), _p(u2),
+                                                  _p(t2), _p(out), nthreads)
         if rc:
-            raise ValueError(f"internal point {rc - 1} lies on the boundary away from a node")
+            raise ValueError(f"internal point {rc - 1} lies on the boundary (on an element away from its nodes, "
+                             "or at a node of a crack-like boundary)")
         return out[:, 0, :], np.transpose(out[:, 1:, :], (0, 2, 1))
 
     def solution(self, x):

@@ -2139,11 +2139,16 @@ static int assemble(const Problem& P, const K& k, MKH mkh, typename K::T bm, typ
 // with sbie_auto / hbie_auto at x_i; a point at a boundary node (distance /
 // csize of the node's first element < 1e-12) takes the node's displacement and
 // zero stresses (calculate_internal_points_mechanics_bem_harela.f90:190-208).
+// A crack-like element adds face 2's terms with its reversed kernels, + g t2
+// + h u2 and + l t2 + m u2 (calculate_internal_points_mechanics_static.f90:
+// 320-354,431-465); u2, t2 [nn][3] (null without cracks).
 // out[ip][4][3]: [0] displacement, [1 + kc] sigma(:, kc). Returns the index + 1
-// of the first point that lies on an element away from its nodes, else 0.
+// of the first point that lies on an element away from its nodes or at a
+// node of a crack-like boundary, else 0.
 template <class K, class KH, class MKH>
 static int internal_points(const Problem& P, const K& k, MKH mkh, int nip, const double* xip,
-                           const typename K::T* u, const typename K::T* t, typename K::T* out, int nthreads) {
+                           const typename K::T* u, const typename K::T* t, const typename K::T* u2,
+                           const typename K::T* t2, typename K::T* out, int nthreads) {
   typedef typename K::T T;
   std::vector<int> efirst(P.nn, -1);
   for (int e = 0; e < P.ne; ++e)
@@ -2171,10 +2176,15 @@ static int internal_points(const Problem& P, const K& k, MKH mkh, int nip, const
           on_elem[ip] = 1;
           break;
         }
+        const bool ck = P.crack_el[e] != 0 && u2 && t2;
         for (int il = 0; il < 3; ++il)
           for (int ik = 0; ik < 3; ++ik)
-            for (int kn = 0; kn < 8; ++kn)
+            for (int kn = 0; kn < 8; ++kn) {
               acc[0][il] = acc[0][il] + hg.g[kn][il][ik] * t[3 * cn[kn] + ik] - hg.h[kn][il][ik] * u[3 * cn[kn] + ik];
+              if (ck)
+                acc[0][il] = acc[0][il] + hg.g[kn][il][ik] * t2[3 * cn[kn] + ik] +
+                             hg.h[kn][il][ik] * u2[3 * cn[kn] + ik];
+            }
         for (int kc = 0; kc < 3; ++kc) {
           double ni[3] = {0.0, 0.0, 0.0};
           ni[kc] = 1.0;
@@ -2183,11 +2193,17 @@ static int internal_points(const Problem& P, const K& k, MKH mkh, int nip, const
           hbie_auto<KH>(kh, P.el[e], false, xi, P.qsp, P.ns_max, ml);
           for (int il = 0; il < 3; ++il)
             for (int ik = 0; ik < 3; ++ik)
-              for (int kn = 0; kn < 8; ++kn)
+              for (int kn = 0; kn < 8; ++kn) {
                 acc[1 + kc][il] =
                     acc[1 + kc][il] + ml.g[kn][il][ik] * t[3 * cn[kn] + ik] - ml.h[kn][il][ik] * u[3 * cn[kn] + ik];
+                if (ck)
+                  acc[1 + kc][il] = acc[1 + kc][il] + ml.g[kn][il][ik] * t2[3 * cn[kn] + ik] +
+                                    ml.h[kn][il][ik] * u2[3 * cn[kn] + ik];
+              }
         }
       }
+    } else if (P.crack[on_node]) {
+      on_elem[ip] = 1;
     } else {
       for (int c = 0; c < 3; ++c) acc[0][c] = u[3 * on_node + c];
     }
@@ -2411,21 +2427,21 @@ int orc_pair_harela(void* hp, int ci, int e, double lre, double lim, double mre,
 }
 // Internal points (displacement and stresses), u / t nodal values [nn][3].
 int orc_internal_points_staela(void* hp, double mu, double nu, int nip, const double* xip, const double* u,
-                               const double* t, double* out, int nthreads) {
+                               const double* t, const double* u2, const double* t2, double* out, int nthreads) {
   Problem* P = (Problem*)hp;
   StaelaK k(mu, nu);
   auto mkh = [&](const double* ni) { return StaelaHK(mu, nu, ni); };
-  return internal_points<StaelaK, StaelaHK>(*P, k, mkh, nip, xip, u, t, out, nthreads);
+  return internal_points<StaelaK, StaelaHK>(*P, k, mkh, nip, xip, u, t, u2, t2, out, nthreads);
 }
 int orc_internal_points_harela(void* hp, double lre, double lim, double mre, double mim, double rho, double omega,
-                               int nip, const double* xip, const double* u, const double* t, double* out,
-                               int nthreads) {
+                               int nip, const double* xip, const double* u, const double* t, const double* u2,
+                               const double* t2, double* out, int nthreads) {
   Problem* P = (Problem*)hp;
   HarPar par = harela_parameters(cplx(lre, lim), cplx(mre, mim), rho, omega);
   HarelaK k(par);
   auto mkh = [&](const double* ni) { return HarelaHK(par, ni); };
-  return internal_points<HarelaK, HarelaHK>(*P, k, mkh, nip, xip, (const cplx*)u, (const cplx*)t, (cplx*)out,
-                                            nthreads);
+  return internal_points<HarelaK, HarelaHK>(*P, k, mkh, nip, xip, (const cplx*)u, (const cplx*)t, (const cplx*)u2,
+                                            (const cplx*)t2, (cplx*)out, nthreads);
 }
 // Harmonic parameter block for tests: k1,k2,c1,c2,psi(6),chi(6),T1(10),T2(9),T3(9),cte_u,cte_t (complex)
 void orc_harela_parameters(double lre, double lim, double mre, double mim, double rho, double omega, double* out) {

@@ -132,11 +132,6 @@ def test_crack_errors():
     with pytest.raises(MfbemError) as e:
         R.set_halfspace(-3, -1.0, 1)
     assert e.value.code == _abi.MFBEM_EUNSUPPORTED
-    mat = M.elastic(1.0, 0.25)
-    u = np.zeros((d.n_nodes, 3))
-    with pytest.raises(MfbemError) as e:
-        R.internal_points(np.array([[0.0, 0.0, 0.5]]), u, u, mu=mat["mu"], nu=mat["nu"])
-    assert e.value.code == _abi.MFBEM_EUNSUPPORTED
     # a crack node whose formulation flags are not the dual BEM's
     L = _abi.load()
     dd = L.mfbem_prep_dual(R._prep).contents
@@ -154,3 +149,39 @@ def test_crack_errors():
     ce[0] = False
     with pytest.raises(ValueError):
         BemRegion(d, crack=(ce, crack[1], crack[2]))
+
+
+@pytest.mark.parametrize("harmonic", [False, True])
+def test_internal_points_with_both_faces(oracle, harmonic):
+    """mfbem_internal_points_faces_*: face 2 integrated with the reversed
+    element (calculate_internal_points_mechanics_static.f90:320-354,431-465),
+    device against the oracle (<= 1e-10, max-norm relative) inside the cube
+    around the crack, near it and far from it; the single-face entry points and
+    a point at a crack node are refused."""
+    d, crack = M.penny_crack_in_box(1.0, 2, 1, 2.0, 2)
+    P = oracle.Problem(d)
+    P.set_crack(*crack)
+    R = BemRegion(d, crack=crack)
+    xp = np.array([[0.3, 0.2, 0.4], [-0.5, 0.1, -0.3], [1.2, 0.0, 0.1], [0.0, 0.0, 0.05], [0.1, -1.5, 1.5]])
+    if harmonic:
+        mat = M.viscoelastic(1.0, 0.25, 1.0, 0.05)
+        om = 0.8
+        x = R.sweep_harela(mat, [om], precision="plain")[0]
+        kw = dict(mat=mat, omega=om)
+    else:
+        mat = M.elastic(1.0, 0.25)
+        x = R.solve_staela(mat["mu"], mat["nu"], precision="plain")
+        kw = dict(mu=mat["mu"], nu=mat["nu"])
+    u1, t1, u2, t2 = R.solution_faces(x)
+    ud, sd = R.internal_points(xp, u1, t1, u2=u2, t2=t2, **kw)
+    uo, so = P.internal_points(xp, u1, t1, u2=u2, t2=t2, **kw)
+    print("harmonic" if harmonic else "static", "u", rel(ud, uo), "sigma", rel(sd, so))
+    assert rel(ud, uo) <= 1e-10 and rel(sd, so) <= 1e-10
+    with pytest.raises(MfbemError) as e:
+        R.internal_points(xp, u1, t1, **kw)
+    assert e.value.code == _abi.MFBEM_EUNSUPPORTED
+    c = np.nonzero(crack[0])[0][0]
+    with pytest.raises(MfbemError) as e:
+        R.internal_points(d.nodes[d.conn[c, :1]], u1, t1, u2=u2, t2=t2, **kw)
+    assert e.value.code == _abi.MFBEM_EUNSUPPORTED
+    R.close()

@@ -108,3 +108,29 @@ def test_crack_errors(oracle):
     P.set_halfspace(-3, -1.0, 1)
     with pytest.raises(RuntimeError, match="half-space"):
         P.assemble_staela(0.4, 0.25)
+
+
+def test_internal_points_of_a_cracked_region(oracle):
+    """Internal points with both faces' solution (calculate_internal_points_
+    mechanics_static.f90:320-354,431-465): approaching the crack from either
+    side the displacement tends to that face's, sigma_zz to the pressure, and
+    the field is mirror-symmetric; face 1 alone gives nothing of the sort."""
+    d, P = crack_problem(oracle, 2, 3, 2)
+    mat = M.elastic(E, NU)
+    x = oracle.lu_solve(*P.assemble_staela(mat["mu"], mat["nu"]))
+    u1, t1, u2, t2 = P.solution_faces(x)
+    c = np.argmin(np.linalg.norm(d.nodes, axis=1))
+    z = np.array([0.02, 0.3, 1.0])
+    xp = np.stack([np.zeros(3), np.zeros(3), z], 1)
+    up, sp = P.internal_points(xp, u1, t1, mu=mat["mu"], nu=mat["nu"], u2=u2, t2=t2)
+    um, sm = P.internal_points(-xp, u1, t1, mu=mat["mu"], nu=mat["nu"], u2=u2, t2=t2)
+    assert abs(up[0, 2] - u2[c, 2]) < 0.02 * u2[c, 2] and abs(um[0, 2] - u1[c, 2]) < 0.02 * u2[c, 2]
+    assert abs(sp[0, 2, 2] + 1.0) < 0.03
+    assert np.allclose(up[:, 2], -um[:, 2], rtol=1e-12, atol=0) and np.allclose(sp[:, 2, 2], sm[:, 2, 2], rtol=1e-12)
+    assert np.abs(sp[:, :2, 2]).max() < 1e-12 and np.abs(up[:, :2]).max() < 1e-12
+    assert np.all(np.diff(up[:, 2]) < 0)  # the opening decays away from the crack
+    u0, _ = P.internal_points(xp[:1], u1, t1, mu=mat["mu"], nu=mat["nu"])
+    assert abs(u0[0, 2] - u2[c, 2]) > 0.5 * u2[c, 2]
+    # a point at a crack node has no single value
+    with pytest.raises(ValueError):
+        P.internal_points(d.nodes[c:c + 1], u1, t1, mu=mat["mu"], nu=mat["nu"], u2=u2, t2=t2)
