@@ -67,6 +67,8 @@ def lib():
         L.orc_freeterm.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp]
         L.orc_problem_set_halfspace.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int]
         L.orc_hsc_point.argtypes = [ctypes.c_double] * 3 + [_dp] * 5
+        L.orc_hsc_hbie_point.argtypes = [ctypes.c_double] * 3 + [_dp] * 6
+        L.orc_hsc_sigma_ad.argtypes = [ctypes.c_double] * 3 + [_dp] * 3
         L.orc_pair_hsc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    _dp, _dp]
         L.orc_problem_set_formulation.argtypes = [ctypes.c_void_p, _ip, _dp, _dp]
@@ -295,6 +297,10 @@ class Problem:
         else:
             rc = lib().orc_internal_points_staela(self._h, float(mu), float(nu), nip, _p(xip), _p(u), _p(t), _p(u2),
                                                   _p(t2), _p(out), nthreads)
+        if rc == -7:
+            raise RuntimeError("half-space internal points: normal -3 and a traction-free surface only")
+        if rc == -8:
+            raise RuntimeError("half-space internal points: a point lies outside the half-space")
         if rc:
             raise ValueError(f"internal point {rc - 1} lies on the boundary (on an element away from its nodes, "
                              "or at a node of a crack-like boundary)")
@@ -341,6 +347,24 @@ def hsc_point(mu, nu, xp, x_i, x, n):
     if rc:
         raise ValueError("point outside the half-space")
     return u, t
+
+
+def hsc_hbie_point(mu, nu, xp, x_i, n_i, x, n):
+    """Complementary half-space HBIE kernels at one point: d, s [3, 3]."""
+    d = np.zeros((3, 3))
+    s = np.zeros((3, 3))
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (x_i, n_i, x, n)]
+    if lib().orc_hsc_hbie_point(mu, nu, xp, *[_p(v) for v in a], _p(d), _p(s)):
+        raise ValueError("point outside the half-space")
+    return d, s
+
+
+def hsc_sigma_ad(mu, nu, xp, x_i, x):
+    """Complementary stress sigma[l, k, j] (load l) from the differentiated u*."""
+    sig = np.zeros((3, 3, 3))
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (x_i, x)]
+    lib().orc_hsc_sigma_ad(mu, nu, xp, *[_p(v) for v in a], _p(sig))
+    return sig
 
 
 def gauss_tables():

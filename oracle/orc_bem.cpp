@@ -1439,6 +1439,169 @@ inline void kernel_at(const HscK& k, const double x[3], const double x_i[3], con
   k.eval_at(x, x_i, n, fu, ft);
 }
 
+// ---------------------------------------------------------------------------
+// Complementary HBIE kernels d*, s* of the half-space (static) at an internal
+// point: fbem_bem_staela3d_hsc_hbie (bem_staela3d.f90:10882-11102) builds them
+// from the first and mixed second derivatives of the complementary u* with
+// respect to the field point x and the source point x_i. Here those
+// derivatives come from forward-mode differentiation (a jet carrying the value,
+// the gradients in x and x_i and the mixed Hessian block) of u* written in
+// Cartesian form, then the same steps: sigma* = C : grad_x u*, its x_i
+// derivative, d*_lkp / s*_lkp = C applied to the x_i gradients, contracted with
+// n_i. z and z_i are measured from the plane x3 = xp, R the distance to the
+// image (x_i1, x_i2, 2 xp - x_i3).
+// ---------------------------------------------------------------------------
+struct Jet {
+  double v, gx[3], gi[3], H[3][3];  // value, d/dx, d/dx_i, d2/(dx_j dx_i_p)
+};
+static inline Jet jconst(double c) {
+  Jet r{};
+  r.v = c;
+  return r;
+}
+static inline Jet operator+(const Jet& a, const Jet& b) {
+  Jet r;
+  r.v = a.v + b.v;
+  for (int j = 0; j < 3; ++j) {
+    r.gx[j] = a.gx[j] + b.gx[j];
+    r.gi[j] = a.gi[j] + b.gi[j];
+    for (int p = 0; p < 3; ++p) r.H[j][p] = a.H[j][p] + b.H[j][p];
+  }
+  return r;
+}
+static inline Jet operator*(double c, const Jet& a) {
+  Jet r;
+  r.v = c * a.v;
+  for (int j = 0; j < 3; ++j) {
+    r.gx[j] = c * a.gx[j];
+    r.gi[j] = c * a.gi[j];
+    for (int p = 0; p < 3; ++p) r.H[j][p] = c * a.H[j][p];
+  }
+  return r;
+}
+static inline Jet operator-(const Jet& a, const Jet& b) { return a + (-1.0) * b; }
+static inline Jet operator+(const Jet& a, double c) { Jet r = a; r.v = r.v + c; return r; }
+static inline Jet operator*(const Jet& a, const Jet& b) {
+  Jet r;
+  r.v = a.v * b.v;
+  for (int j = 0; j < 3; ++j) {
+    r.gx[j] = a.v * b.gx[j] + a.gx[j] * b.v;
+    r.gi[j] = a.v * b.gi[j] + a.gi[j] * b.v;
+  }
+  for (int j = 0; j < 3; ++j)
+    for (int p = 0; p < 3; ++p)
+      r.H[j][p] = a.v * b.H[j][p] + a.H[j][p] * b.v + a.gx[j] * b.gi[p] + a.gi[p] * b.gx[j];
+  return r;
+}
+// g(a) for a scalar function with derivatives d1 = g'(a.v), d2 = g''(a.v)
+static inline Jet jchain(const Jet& a, double g, double d1, double d2) {
+  Jet r;
+  r.v = g;
+  for (int j = 0; j < 3; ++j) {
+    r.gx[j] = d1 * a.gx[j];
+    r.gi[j] = d1 * a.gi[j];
+  }
+  for (int j = 0; j < 3; ++j)
+    for (int p = 0; p < 3; ++p) r.H[j][p] = d1 * a.H[j][p] + d2 * a.gx[j] * a.gi[p];
+  return r;
+}
+static inline Jet jinv(const Jet& a) { const double q = 1.0 / a.v; return jchain(a, q, -q * q, 2.0 * q * q * q); }
+static inline Jet jsqrt(const Jet& a) {
+  const double s = std::sqrt(a.v);
+  return jchain(a, s, 0.5 / s, -0.25 / (s * a.v));
+}
+
+// Complementary u*[l][k] (load direction l, component k, without the factor
+// 1 / (16 pi mu (1 - nu))) in Cartesian form: the tangential-load rows of
+// hsc_sbie (bem_staela3d.f90:7438-7563) and the normal-load row with the
+// radial component r F written as (x - x_i) F.
+static void hsc_u_jets(double nu, const Jet x[3], const Jet xi[3], double xp, Jet u[3][3]) {
+  const double c1 = 1.0 - nu, c2 = 1.0 - 2.0 * nu, c4 = 3.0 - 4.0 * nu;
+  const Jet rx = x[0] - xi[0], ry = x[1] - xi[1];
+  const Jet z = x[2] + (-xp), c = xi[2] + (-xp), zc = z + c;
+  const Jet rp = jsqrt(rx * rx + ry * ry + zc * zc);
+  const Jet irp = jinv(rp), irp2 = irp * irp, irp3 = irp2 * irp, irp5 = irp3 * irp2;
+  const Jet q = rp + zc, iq = jinv(q), iq2 = iq * iq;
+  const Jet cz = c * z;
+  const double k12 = 4.0 * c1 * c2;
+  const Jet rr[2] = {rx, ry};
+  for (int a = 0; a < 2; ++a) {
+    const Jet ra2 = rr[a] * rr[a];
+    u[a][a] = irp + (c4 * ra2) * irp3 + (2.0 * cz) * irp3 * (jconst(1.0) - (3.0 * ra2) * irp2) +
+              (k12 * iq) * (jconst(1.0) - ra2 * irp * iq);
+    u[a][2] = rr[a] * ((c4 * (z - c)) * irp3 - (6.0 * cz * zc) * irp5 + (k12 * irp) * iq);
+    u[2][a] = rr[a] * ((c4 * (z - c)) * irp3 - (k12 * irp) * iq + (6.0 * cz * zc) * irp5);
+  }
+  u[0][1] = rx * ry * (c4 * irp3 - (6.0 * cz) * irp5 - (k12 * irp) * iq2);
+  u[1][0] = u[0][1];
+  u[2][2] = (8.0 * c1 * c1 - c4) * irp + (c4 * zc * zc - 2.0 * cz) * irp3 + (6.0 * cz * zc * zc) * irp5;
+}
+
+struct HscHK {
+  typedef double T;
+  static constexpr int F = 7;
+  double mu, nu, xp, ni[3];
+  HscHK(double mu_, double nu_, double xp_, const double n_i[3]) : mu(mu_), nu(nu_), xp(xp_) {
+    for (int c = 0; c < 3; ++c) ni[c] = n_i[c];
+  }
+  double cu() const { return 1.0; }
+  double ct() const { return 1.0; }
+  // fd = d*, fs = s* (load direction il, component ik), constants included
+  void eval_at(const double xq[3], const double x_i[3], const double n[3], double fd[3][3], double fs[3][3]) const {
+    if (x_i[2] < xp || xq[2] < xp) g_hs_err = 1;
+    Jet x[3], xi[3];
+    for (int c = 0; c < 3; ++c) {
+      x[c] = jconst(xq[c]);
+      x[c].gx[c] = 1.0;
+      xi[c] = jconst(x_i[c]);
+      xi[c].gi[c] = 1.0;
+    }
+    Jet u[3][3];
+    hsc_u_jets(nu, x, xi, xp, u);
+    const double Ku = 1.0 / (16.0 * c_pi * mu * (1.0 - nu)), lam = 2.0 * mu * nu / (1.0 - 2.0 * nu);
+    // d/dx_i of t* = sigma*(x) n with sigma*_{l,kj} = lam d_kj div u_l + mu (u_lk,j + u_lj,k)
+    double dt[3][3][3];  // dt[l][k][p]
+    for (int l = 0; l < 3; ++l)
+      for (int k = 0; k < 3; ++k)
+        for (int p = 0; p < 3; ++p) {
+          double div = 0.0;
+          for (int m = 0; m < 3; ++m) div = div + u[l][m].H[m][p];
+          double v = 0.0;
+          for (int j = 0; j < 3; ++j) {
+            double sg = mu * (u[l][k].H[j][p] + u[l][j].H[k][p]);
+            if (j == k) sg = sg + lam * div;
+            v = v + sg * n[j];
+          }
+          dt[l][k][p] = Ku * v;
+        }
+    for (int l = 0; l < 3; ++l)
+      for (int k = 0; k < 3; ++k) {
+        double dv = 0.0, sv = 0.0;
+        for (int p = 0; p < 3; ++p) {
+          double dl = mu * Ku * (u[l][k].gi[p] + u[p][k].gi[l]);
+          double sl = mu * (dt[l][k][p] + dt[p][k][l]);
+          if (l == p) {
+            double tr = 0.0, ts = 0.0;
+            for (int j = 0; j < 3; ++j) {
+              tr = tr + u[j][k].gi[j];
+              ts = ts + dt[j][k][j];
+            }
+            dl = dl + lam * Ku * tr;
+            sl = sl + lam * ts;
+          }
+          dv = dv + dl * ni[p];
+          sv = sv + sl * ni[p];
+        }
+        fd[l][k] = dv;
+        fs[l][k] = sv;
+      }
+  }
+};
+inline void kernel_at(const HscHK& k, const double x[3], const double x_i[3], const double n[3], double fu[3][3],
+                      double ft[3][3]) {
+  k.eval_at(x, x_i, n, fu, ft);
+}
+
 // fbem_bem_staela3d_hsc_sbie_int (bem_staela3d.f90:8624-8833): element on the
 // free surface containing the collocation point. h is minus the full-space h
 // (the complete traction kernel vanishes on the free surface); g integrates
@@ -1520,6 +1683,42 @@ static int hsc_auto(const StaelaK& kf, const HscK& k, const Elem& e, bool revers
   }
   double xi_s[4][2];
   ext_adp<HscK>(k, e, reverse, xi_s, x_i, qsp, 1, ns, out, st, xq);
+  return CLS_ADP;
+}
+
+// fbem_bem_staela3d_hsc_hbie_auto (bem_staela3d.f90:11573-11645): hbie_auto's
+// classification (1/r^7 estimate) on the image of the point; a point on an
+// element of the free surface (image on the element) cannot be integrated
+// (the reference stops): g_hs_err = 2.
+static int hsc_hbie_auto(const HscHK& k, const Elem& e, bool reverse, const double x_i[3], const QsParams& qsp,
+                         int ns, HG<HscHK>& out, AdpStats* st) {
+  const double xq[3] = {x_i[0], x_i[1], 2.0 * k.xp - x_i[2]};
+  double r[3] = {e.bc[0] - xq[0], e.bc[1] - xq[1], e.bc[2] - xq[2]};
+  double rmin = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) - e.br;
+  double barxi[2], d;
+  if (rmin > 4.0 * e.br) {
+    barxi[0] = barxi[1] = 0.0;
+    d = rmin / e.cl;
+  } else {
+    int method;
+    nearest_element_point_quad8(e.x, e.cl, xq, barxi, &rmin, &d, &method);
+    if (d <= 1e-12) {
+      g_hs_err = 2;
+      out.zero();
+      return CLS_SING;
+    }
+  }
+  int gln_near = qs_n_estimation_standard(2, HscHK::F, qsp, d, barxi);
+  int gln = std::max(e.gln_far, gln_near);
+  if (gln <= e.ps_gln_max && gln_near > 0) {
+    int ps = 0;
+    for (int i = 0; i < e.n_ps; ++i)
+      if (e.ps_gln[i] >= gln) { ps = i; break; }
+    ext_pre<HscHK>(k, ps, e, reverse, x_i, out);
+    return ps;
+  }
+  double xi_s[4][2];
+  ext_adp<HscHK>(k, e, reverse, xi_s, x_i, qsp, 1, ns, out, st, xq);
   return CLS_ADP;
 }
 
@@ -2177,6 +2376,22 @@ static int internal_points(const Problem& P, const K& k, MKH mkh, int nip, const
           break;
         }
         const bool ck = P.crack_el[e] != 0 && u2 && t2;
+        if constexpr (std::is_same<K, StaelaK>::value) {
+          // half-space: the complementary kernels added to the full-space
+          // ones (calculate_internal_points_mechanics_static.f90:288-310,
+          // 401-418): hsc_sbie_auto for u, hsc_hbie_auto for sigma
+          if (P.hs_n != 0) {
+            HscK kc(k.mu, k.nu, P.hs_x);
+            HG<HscK> hp;
+            hsc_auto(k, kc, P.el[e], false, xi, P.qsp, P.ns_max, hp, nullptr);
+            for (int a = 0; a < 8; ++a)
+              for (int il = 0; il < 3; ++il)
+                for (int ik = 0; ik < 3; ++ik) {
+                  hg.h[a][il][ik] = hg.h[a][il][ik] + hp.h[a][il][ik];
+                  hg.g[a][il][ik] = hg.g[a][il][ik] + hp.g[a][il][ik];
+                }
+          }
+        }
         for (int il = 0; il < 3; ++il)
           for (int ik = 0; ik < 3; ++ik)
             for (int kn = 0; kn < 8; ++kn) {
@@ -2191,6 +2406,19 @@ static int internal_points(const Problem& P, const K& k, MKH mkh, int nip, const
           KH kh = mkh(ni);
           HG<KH> ml;
           hbie_auto<KH>(kh, P.el[e], false, xi, P.qsp, P.ns_max, ml);
+          if constexpr (std::is_same<K, StaelaK>::value) {
+            if (P.hs_n != 0) {
+              HscHK kc(k.mu, k.nu, P.hs_x, ni);
+              HG<HscHK> mp;
+              hsc_hbie_auto(kc, P.el[e], false, xi, P.qsp, P.ns_max, mp, nullptr);
+              for (int a = 0; a < 8; ++a)
+                for (int il = 0; il < 3; ++il)
+                  for (int ik = 0; ik < 3; ++ik) {
+                    ml.h[a][il][ik] = ml.h[a][il][ik] + mp.h[a][il][ik];
+                    ml.g[a][il][ik] = ml.g[a][il][ik] + mp.g[a][il][ik];
+                  }
+            }
+          }
           for (int il = 0; il < 3; ++il)
             for (int ik = 0; ik < 3; ++ik)
               for (int kn = 0; kn < 8; ++kn) {
@@ -2429,6 +2657,13 @@ int orc_pair_harela(void* hp, int ci, int e, double lre, double lim, double mre,
 int orc_internal_points_staela(void* hp, double mu, double nu, int nip, const double* xip, const double* u,
                                const double* t, const double* u2, const double* t2, double* out, int nthreads) {
   Problem* P = (Problem*)hp;
+  if (P->hs_n != 0) {
+    // the complementary kernels exist for the half-space x3 >= xp only
+    // (fbem_bem_staela3d_hsc_hbie: np = -3); points must lie in it
+    if (P->hs_n != -3 || P->hs_bc != 1) return -7;
+    for (int ip = 0; ip < nip; ++ip)
+      if (xip[3 * ip + 2] < P->hs_x) return -8;
+  }
   StaelaK k(mu, nu);
   auto mkh = [&](const double* ni) { return StaelaHK(mu, nu, ni); };
   return internal_points<StaelaK, StaelaHK>(*P, k, mkh, nip, xip, u, t, u2, t2, out, nthreads);
@@ -2442,6 +2677,37 @@ int orc_internal_points_harela(void* hp, double lre, double lim, double mre, dou
   auto mkh = [&](const double* ni) { return HarelaHK(par, ni); };
   return internal_points<HarelaK, HarelaHK>(*P, k, mkh, nip, xip, (const cplx*)u, (const cplx*)t, (const cplx*)u2,
                                             (const cplx*)t2, (cplx*)out, nthreads);
+}
+// Complementary HBIE kernels at one point (d, s [3][3]: load il, component
+// ik) and the complementary stress sigma[l][k][j] = sigma*_{l,kj} from the
+// derivatives of the Cartesian u* (test hooks for the pinning).
+int orc_hsc_hbie_point(double mu, double nu, double xp, const double* x_i, const double* n_i, const double* x,
+                       const double* n, double* d, double* s) {
+  g_hs_err = 0;
+  HscHK k(mu, nu, xp, n_i);
+  double fd[3][3], fs[3][3];
+  k.eval_at(x, x_i, n, fd, fs);
+  std::memcpy(d, fd, sizeof(fd));
+  std::memcpy(s, fs, sizeof(fs));
+  return g_hs_err;
+}
+void orc_hsc_sigma_ad(double mu, double nu, double xp, const double* x_i, const double* xq, double* sig) {
+  Jet x[3], xi[3];
+  for (int c = 0; c < 3; ++c) {
+    x[c] = jconst(xq[c]);
+    x[c].gx[c] = 1.0;
+    xi[c] = jconst(x_i[c]);
+    xi[c].gi[c] = 1.0;
+  }
+  Jet u[3][3];
+  hsc_u_jets(nu, x, xi, xp, u);
+  const double Ku = 1.0 / (16.0 * c_pi * mu * (1.0 - nu)), lam = 2.0 * mu * nu / (1.0 - 2.0 * nu);
+  for (int l = 0; l < 3; ++l) {
+    const double div = u[l][0].gx[0] + u[l][1].gx[1] + u[l][2].gx[2];
+    for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 3; ++j)
+        sig[9 * l + 3 * k + j] = Ku * ((j == k ? lam * div : 0.0) + mu * (u[l][k].gx[j] + u[l][j].gx[k]));
+  }
 }
 // Harmonic parameter block for tests: k1,k2,c1,c2,psi(6),chi(6),T1(10),T2(9),T3(9),cte_u,cte_t (complex)
 void orc_harela_parameters(double lre, double lim, double mre, double mim, double rho, double omega, double* out) {

@@ -128,3 +128,47 @@ def test_static_kernel_needs_the_x3_normal(oracle):
     P.set_halfspace(3, 0.0, 1)
     with pytest.raises(RuntimeError, match="n = -3"):
         P.assemble_staela(0.4, 0.25)
+
+
+def test_complementary_stress_from_the_differentiated_displacement(oracle):
+    """The Cartesian complementary u* differentiated in x (jets) gives the
+    closed-form complementary stress of hsc_sbie (bem_staela3d.f90:7438-7563)
+    used by the builder: the basis of the d*, s* kernels of hsc_hbie."""
+    mu, nu = 0.4, 0.25
+    rng = np.random.default_rng(1)
+    worst = 0.0
+    for _ in range(20):
+        xi = rng.uniform([-1, -1, 0.05], [1, 1, 1.5])
+        x = rng.uniform([-1, -1, 0.0], [1, 1, 1.5])
+        sig = oracle.hsc_sigma_ad(mu, nu, 0.0, xi, x)
+        for j in range(3):
+            n = np.zeros(3)
+            n[j] = 1.0
+            _, t = oracle.hsc_point(mu, nu, 0.0, xi, x, n)
+            worst = max(worst, np.abs(t - sig[:, :, j]).max() / np.abs(sig).max())
+    assert worst < 1e-13, worst
+
+
+def test_internal_stresses_under_a_loaded_square(oracle):
+    """Static internal points of a half-space region (the complementary
+    kernels hsc_sbie_auto / hsc_hbie_auto, calculate_internal_points_
+    mechanics_static.f90:288-310,401-418): the vertical stress below the
+    centre of a uniformly loaded square 2a x 2a is Holl's closed form
+    -(2p/pi) [atan(a^2 / (z R)) + 2 a^2 z / (R (a^2 + z^2))], R^2 = 2a^2 + z^2,
+    to the quadrature tolerance; the shear stresses vanish on the axis."""
+    a, p = 1.0, 1.0
+    mat = M.elastic(1.0, 0.25)
+    d = M.halfspace_footing(a, 4, p)
+    P = oracle.Problem(d)
+    P.set_halfspace(-3, 0.0, 1)
+    u, t = P.solution(oracle.lu_solve(*P.assemble_staela(mat["mu"], mat["nu"])))
+    zs = np.array([0.25, 0.5, 1.0, 2.0])
+    xip = np.stack([np.zeros(4), np.zeros(4), zs], 1)
+    ui, si = P.internal_points(xip, u, t, mu=mat["mu"], nu=mat["nu"])
+    R = np.sqrt(2 * a * a + zs ** 2)
+    holl = -(2 * p / np.pi) * (np.arctan(a * a / (zs * R)) + (a * a * zs / R) * (2.0 / (a * a + zs ** 2)))
+    assert np.abs(si[:, 2, 2] - holl).max() < 1e-6 * np.abs(holl).max()
+    assert np.abs(si[:, 0, 2]).max() < 1e-12 and np.abs(si[:, 1, 2]).max() < 1e-12
+    assert np.all(np.diff(ui[:, 2]) < 0)
+    with pytest.raises(RuntimeError, match="outside"):
+        P.internal_points(np.array([[0.0, 0.0, -0.1]]), u, t, mu=mat["mu"], nu=mat["nu"])
