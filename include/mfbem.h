@@ -194,7 +194,11 @@ int mfbem_mesh_upload_dual(const mfbem_mesh_desc* desc, const mfbem_dual_desc* d
    assembly; a node or collocation point outside the half-space, or an element
    holding a collocation point of the surface without lying on it, returns
    MFBEM_EGEOMETRY there (the reference stops). Static internal points of a
-   half-space region are MFBEM_EUNSUPPORTED. */
+   half-space region (n = -3) add the complementary kernels from each point's
+   image (fbem_bem_staela3d_hsc_sbie_auto / _hsc_hbie_auto,
+   src/calculate_internal_points_mechanics_static.f90:288-310,401-418); a
+   point outside the half-space returns MFBEM_EGEOMETRY, one on the free
+   surface on an element MFBEM_EUNSUPPORTED (the reference stops). */
 int mfbem_set_halfspace(mfbem_handle* h, int32_t n, double x, int32_t bc);
 
 /* build_lse_mechanics_bem_staela: A (n_dof x n_dof, real) and b (n_dof). */

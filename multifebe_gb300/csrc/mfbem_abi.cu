@@ -1266,13 +1266,58 @@ struct TmpBufs {
   }
 };
 
+// One pass of the internal points: classification, quasi-singular pair
+// lists, adaptive and precalculated integration; out [nf][nip][12].
+template <class POL>
+static int ip_pass(mfbem_handle* h, IpArgs a, const POL& pol, TmpBufs& tb, std::vector<typename POL::T>& out) {
+  typedef typename POL::T T;
+  const DMesh& m = h->m;
+  const int n_ip = a.nip, ne = h->ne, nf = a.nf;
+  const size_t ob = sizeof(T) * 12 * (size_t)n_ip * nf;
+  int rc;
+  if ((rc = tb.get((void**)&a.cls_s, (size_t)n_ip * ne)) || (rc = tb.get((void**)&a.cls_h, (size_t)n_ip * ne)) ||
+      (rc = tb.get((void**)&a.npair, sizeof(int) * n_ip)) || (rc = tb.get((void**)&a.poff, sizeof(int) * (n_ip + 1))) ||
+      (rc = tb.get((void**)&a.err, sizeof(int))) || (rc = tb.get(&a.out, ob)))
+    return rc;
+  cudaStream_t st = h->st;
+  const int big = INT_MAX;
+  CK(cudaMemcpyAsync(a.err, &big, sizeof(int), cudaMemcpyHostToDevice, st));
+  k_ip_classify<<<std::min(nblk((long long)n_ip * ne, 256), 152u * 16u), 256, 0, st>>>(m, a, h->d_qs); ++g_launches;
+  k_ip_count<<<nblk(n_ip, 8), 256, 0, st>>>(m, a); ++g_launches;
+  k_scan<int, int><<<1, 1024, 0, st>>>(a.npair, a.poff, n_ip); ++g_launches;
+  int np = 0;
+  CK(cudaMemcpyAsync(&np, a.poff + n_ip, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  a.npairs = np;
+  if ((rc = tb.get((void**)&a.pair_e, sizeof(int) * (size_t)np)) || (rc = tb.get((void**)&a.pair_ip, sizeof(int) * (size_t)np)) ||
+      (rc = tb.get(&a.slot, sizeof(T) * 12 * (size_t)np * nf)))
+    return rc;
+  k_ip_fill<<<nblk(n_ip, 8), 256, 0, st>>>(m, a); ++g_launches;
+  if (np > 0) {
+    k_ip_adp<POL><<<nblk((long long)np * nf, 64), 64, 0, st>>>(m, a, pol, h->d_qs); ++g_launches;
+  }
+  constexpr int WPB = 4;
+  k_ip_reg<POL, WPB><<<nblk((long long)n_ip * nf, WPB), WPB * 32, 0, st>>>(m, a, pol); ++g_launches;
+  CK(cudaGetLastError());
+  out.assign(12 * (size_t)n_ip * nf, T{});
+  int err = 0;
+  CK(cudaMemcpyAsync(out.data(), a.out, ob, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&err, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (err != INT_MAX)
+    return fail(MFBEM_EUNSUPPORTED, "internal point " + std::to_string(err - 1) +
+                                        (a.image ? " lies on the free surface of the half-space on an element"
+                                                 : " lies on the boundary away from a node (needs the singular HBIE "
+                                                   "integration)"));
+  return 0;
+}
+
 template <class POL>
 static int internal_points_run(mfbem_handle* h, const POL& pol, int nf, int32_t n_ip, const double* x_ip,
                                const double* u_nodes, const double* t_nodes, const double* u2_nodes,
                                const double* t2_nodes, double* u_ip, double* sigma_ip) {
   typedef typename POL::T T;
-  const DMesh& m = h->m;
-  const int nn = h->nn, ne = h->ne;
+  const int nn = h->nn;
   // crack-like boundaries: face 2 sees -h and g of the element, so
   // g t1 - h u1 + g t2 + h u2 = g (t1 + t2) - h (u1 - u2) per node
   // (calculate_internal_points_mechanics_static.f90:320-354, 431-465)
@@ -1304,52 +1349,42 @@ static int internal_points_run(mfbem_handle* h, const POL& pol, int nf, int32_t 
   a.enode = h->enode;
   a.nodex = h->nodex;
   a.nodecl = h->nodecl;
-  const size_t vb = sizeof(T) * 3 * (size_t)nn * nf, ob = sizeof(T) * 12 * (size_t)n_ip * nf;
+  const size_t vb = sizeof(T) * 3 * (size_t)nn * nf;
   int rc;
   if ((rc = tb.get((void**)&a.xip, sizeof(double) * 3 * (size_t)n_ip)) || (rc = tb.get((void**)&a.uval, vb)) ||
-      (rc = tb.get((void**)&a.tval, vb)) || (rc = tb.get((void**)&a.cls_s, (size_t)n_ip * ne)) ||
-      (rc = tb.get((void**)&a.cls_h, (size_t)n_ip * ne)) || (rc = tb.get((void**)&a.onnode, sizeof(int) * n_ip)) ||
-      (rc = tb.get((void**)&a.npair, sizeof(int) * n_ip)) || (rc = tb.get((void**)&a.poff, sizeof(int) * (n_ip + 1))) ||
-      (rc = tb.get((void**)&a.err, sizeof(int))) || (rc = tb.get(&a.out, ob)))
+      (rc = tb.get((void**)&a.tval, vb)) || (rc = tb.get((void**)&a.onnode, sizeof(int) * n_ip)))
     return rc;
   cudaStream_t st = h->st;
   CK(cudaMemcpyAsync((void*)a.xip, x_ip, sizeof(double) * 3 * (size_t)n_ip, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync((void*)a.uval, u_nodes, vb, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync((void*)a.tval, t_nodes, vb, cudaMemcpyHostToDevice, st));
-  const int big = INT_MAX;
-  CK(cudaMemcpyAsync(a.err, &big, sizeof(int), cudaMemcpyHostToDevice, st));
   k_ip_onnode<<<nblk(n_ip, 128), 128, 0, st>>>(a); ++g_launches;
-  k_ip_classify<<<std::min(nblk((long long)n_ip * ne, 256), 152u * 16u), 256, 0, st>>>(m, a, h->d_qs); ++g_launches;
-  k_ip_count<<<nblk(n_ip, 8), 256, 0, st>>>(m, a); ++g_launches;
-  k_scan<int, int><<<1, 1024, 0, st>>>(a.npair, a.poff, n_ip); ++g_launches;
-  int np = 0;
-  CK(cudaMemcpyAsync(&np, a.poff + n_ip, sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  a.npairs = np;
-  if ((rc = tb.get((void**)&a.pair_e, sizeof(int) * (size_t)np)) || (rc = tb.get((void**)&a.pair_ip, sizeof(int) * (size_t)np)) ||
-      (rc = tb.get(&a.slot, sizeof(T) * 12 * (size_t)np * nf)))
-    return rc;
-  k_ip_fill<<<nblk(n_ip, 8), 256, 0, st>>>(m, a); ++g_launches;
-  if (np > 0) {
-    k_ip_adp<POL><<<nblk((long long)np * nf, 64), 64, 0, st>>>(m, a, pol, h->d_qs); ++g_launches;
+  std::vector<T> out;
+  if ((rc = ip_pass(h, a, pol, tb, out))) return rc;
+  // static half-space: the complementary kernels from the points' images
+  if constexpr (std::is_same<POL, IpStatic>::value) {
+    if (h->hs_n == -3) {
+      IpArgs ai = a;
+      ai.image = 1;
+      ai.hs_xp = h->hs_x;
+      IpHsc ph;
+      ph.mu = pol.mu;
+      ph.nu = pol.nu;
+      ph.xp = h->hs_x;
+      std::vector<T> out2;
+      if ((rc = ip_pass(h, ai, ph, tb, out2))) return rc;
+      for (size_t i = 0; i < out.size(); ++i) out[i] = out[i] + out2[i];
+    }
   }
-  constexpr int WPB = 4;
-  k_ip_reg<POL, WPB><<<nblk((long long)n_ip * nf, WPB), WPB * 32, 0, st>>>(m, a, pol); ++g_launches;
-  CK(cudaGetLastError());
-  std::vector<T> out(12 * (size_t)n_ip * nf);
-  std::vector<int> onn(h->has_crack ? n_ip : 0);
-  int err = 0;
-  CK(cudaMemcpyAsync(out.data(), a.out, ob, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(&err, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));
-  if (h->has_crack) CK(cudaMemcpyAsync(onn.data(), a.onnode, sizeof(int) * (size_t)n_ip, cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  if (err != INT_MAX)
-    return fail(MFBEM_EUNSUPPORTED, "internal point " + std::to_string(err - 1) +
-                                        " lies on the boundary away from a node (needs the singular HBIE integration)");
-  for (int ip = 0; ip < (int)onn.size(); ++ip)
-    if (onn[ip] >= 0 && h->crack_node[onn[ip]])
-      return fail(MFBEM_EUNSUPPORTED, "internal point " + std::to_string(ip) +
-                                          " lies at a node of a crack-like boundary (two faces)");
+  if (h->has_crack) {
+    std::vector<int> onn(n_ip);
+    CK(cudaMemcpyAsync(onn.data(), a.onnode, sizeof(int) * (size_t)n_ip, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int ip = 0; ip < n_ip; ++ip)
+      if (onn[ip] >= 0 && h->crack_node[onn[ip]])
+        return fail(MFBEM_EUNSUPPORTED, "internal point " + std::to_string(ip) +
+                                            " lies at a node of a crack-like boundary (two faces)");
+  }
   T* uo = (T*)u_ip;
   T* so = (T*)sigma_ip;
   for (size_t i = 0; i < (size_t)n_ip * nf; ++i) {
@@ -1366,12 +1401,20 @@ static int internal_points_staela(mfbem_handle* h, double mu, double nu, int32_t
   if (!h || n_ip < 0 || (n_ip > 0 && (!x_ip || !u_nodes || !t_nodes || !u_ip || !sigma_ip)))
     return fail(MFBEM_EARG, "invalid argument");
   if (int rd = check_dev(h)) return rd;
-  if (h->hs_n != 0)
-    return fail(MFBEM_EUNSUPPORTED, "internal points of a static half-space region are not available");
+  if (h->hs_n != 0) {
+    // the complementary kernels exist for the half-space x3 >= xp only
+    // (fbem_bem_staela3d_hsc_sbie / _hsc_hbie: np = -3)
+    if (h->hs_n != -3)
+      return fail(MFBEM_EUNSUPPORTED, "static half-space internal points need the normal n = -3");
+    for (int ip = 0; ip < n_ip; ++ip)
+      if (x_ip[3 * (size_t)ip + 2] < h->hs_x)
+        return fail(MFBEM_EGEOMETRY, "internal point " + std::to_string(ip) + " lies outside the half-space");
+  }
   if (n_ip == 0) return 0;
   IpStatic pol;
   pol.k = staela_params(mu, nu);
   pol.nu = nu;
+  pol.mu = mu;
   pol.cted1 = -1.0 / (8.0 * kPi * (1.0 - nu));
   pol.cted2 = 1.0 - 2.0 * nu;
   pol.ctes1 = mu / (4.0 * kPi * (1.0 - nu));

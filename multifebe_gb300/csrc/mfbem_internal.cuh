@@ -128,8 +128,8 @@ __device__ __forceinline__ void zexp_2to6(const ZexpSteps& steps, cd z, cd E[7])
 struct IpStatic {
   typedef double T;
   StaelaP k;
-  double nu, cted1, cted2, ctes1, ctes2, ctes3;
-  __device__ void sbie(int, const double rv[3], const double n[3], const T ut[3], const T uu[3], double rs,
+  double nu, cted1, cted2, ctes1, ctes2, ctes3, mu = 0.0;
+  __device__ void sbie(int, const double*, const double rv[3], const double n[3], const T ut[3], const T uu[3], double rs,
                        T du[3]) const {
     double fu[9], ft[9];
     staela_point(k, rv, n, fu, ft);
@@ -144,7 +144,7 @@ struct IpStatic {
       du[il] += k.cteu1 * g - rs * k.ctet1 * h;
     }
   }
-  __device__ void hbie(int, const double rv[3], const double n[3], const T ut[3], const T uu[3], double rs,
+  __device__ void hbie(int, const double*, const double rv[3], const double n[3], const T ut[3], const T uu[3], double rs,
                        T sg[3][3]) const {
     const double r = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
     const double d1r = 1.0 / r, d1r2 = d1r * d1r, d1r3 = d1r2 * d1r;
@@ -178,7 +178,7 @@ struct IpHarmonic {
   typedef cd T;
   const HarParD* p;
   const HarParH* ph;
-  __device__ void sbie(int f, const double rv[3], const double n[3], const T ut[3], const T uu[3], double rs,
+  __device__ void sbie(int f, const double*, const double rv[3], const double n[3], const T ut[3], const T uu[3], double rs,
                        T du[3]) const {
     cd fu[9], ft[9];
     harela_point(p[f], rv, n, fu, ft);
@@ -193,7 +193,7 @@ struct IpHarmonic {
       du[il] = du[il] + p[f].cte_u * g - (rs * p[f].cte_t) * h;
     }
   }
-  __device__ void hbie(int f, const double rv[3], const double n[3], const T ut[3], const T uu[3], double rs,
+  __device__ void hbie(int f, const double*, const double rv[3], const double n[3], const T ut[3], const T uu[3], double rs,
                        T sg[3][3]) const {
     const HarParD& q = p[f];
     const HarParH& s = ph[f];
@@ -250,6 +250,184 @@ struct IpHarmonic {
   }
 };
 
+// Half-space (static, x3 >= xp, traction-free surface): the complementary
+// kernels added at internal points (calculate_internal_points_mechanics_static.f90:
+// 288-310,401-418). rv is measured from the image of the point (the pairs are
+// classified on it, as fbem_bem_staela3d_hsc_sbie_auto / _hsc_hbie_auto do);
+// xi is the point. u*, t*: hsc_point (fbem_bem_staela3d_hsc_sbie). d*, s*
+// (fbem_bem_staela3d_hsc_hbie, bem_staela3d.f90:10882-11102): built from the
+// first and mixed second derivatives of the complementary u* in x and x_i,
+// here by forward-mode differentiation of u* in Cartesian form (HJet: value,
+// the gradients in x and x_i and the mixed Hessian block).
+struct HJet {
+  double v, gx[3], gi[3], H[3][3];
+};
+__device__ __forceinline__ HJet hj_const(double c) {
+  HJet r;
+  r.v = c;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    r.gx[j] = r.gi[j] = 0.0;
+#pragma unroll
+    for (int p = 0; p < 3; ++p) r.H[j][p] = 0.0;
+  }
+  return r;
+}
+__device__ __forceinline__ HJet hj_axpy(double a, const HJet& x, const HJet& y) {  // a x + y
+  HJet r;
+  r.v = a * x.v + y.v;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    r.gx[j] = a * x.gx[j] + y.gx[j];
+    r.gi[j] = a * x.gi[j] + y.gi[j];
+#pragma unroll
+    for (int p = 0; p < 3; ++p) r.H[j][p] = a * x.H[j][p] + y.H[j][p];
+  }
+  return r;
+}
+__device__ __forceinline__ HJet hj_add(const HJet& x, const HJet& y) { return hj_axpy(1.0, x, y); }
+__device__ __forceinline__ HJet hj_sub(const HJet& x, const HJet& y) { return hj_axpy(-1.0, y, x); }
+__device__ __forceinline__ HJet hj_scale(double a, const HJet& x) { return hj_axpy(a, x, hj_const(0.0)); }
+__device__ __forceinline__ HJet hj_mul(const HJet& a, const HJet& b) {
+  HJet r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    r.gx[j] = a.v * b.gx[j] + a.gx[j] * b.v;
+    r.gi[j] = a.v * b.gi[j] + a.gi[j] * b.v;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int p = 0; p < 3; ++p) r.H[j][p] = a.v * b.H[j][p] + a.H[j][p] * b.v + a.gx[j] * b.gi[p] + a.gi[p] * b.gx[j];
+  return r;
+}
+__device__ __forceinline__ HJet hj_chain(const HJet& a, double g, double d1, double d2) {
+  HJet r;
+  r.v = g;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    r.gx[j] = d1 * a.gx[j];
+    r.gi[j] = d1 * a.gi[j];
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int p = 0; p < 3; ++p) r.H[j][p] = d1 * a.H[j][p] + d2 * a.gx[j] * a.gi[p];
+  return r;
+}
+__device__ __forceinline__ HJet hj_inv(const HJet& a) {
+  const double q = 1.0 / a.v;
+  return hj_chain(a, q, -q * q, 2.0 * q * q * q);
+}
+__device__ __forceinline__ HJet hj_sqrt(const HJet& a) {
+  const double s = sqrt(a.v);
+  return hj_chain(a, s, 0.5 / s, -0.25 / (s * a.v));
+}
+// complementary u*[l][k] without 1 / (16 pi mu (1 - nu)); x, xi seeded jets
+__device__ void hsc_u_jets(double nu, const HJet x[3], const HJet xi[3], double xp, HJet u[3][3]) {
+  const double c1 = 1.0 - nu, c2 = 1.0 - 2.0 * nu, c4 = 3.0 - 4.0 * nu, k12 = 4.0 * c1 * c2;
+  const HJet rx = hj_sub(x[0], xi[0]), ry = hj_sub(x[1], xi[1]);
+  const HJet z = hj_axpy(1.0, x[2], hj_const(-xp)), c = hj_axpy(1.0, xi[2], hj_const(-xp)), zc = hj_add(z, c);
+  const HJet rp = hj_sqrt(hj_add(hj_add(hj_mul(rx, rx), hj_mul(ry, ry)), hj_mul(zc, zc)));
+  const HJet irp = hj_inv(rp), irp2 = hj_mul(irp, irp), irp3 = hj_mul(irp2, irp), irp5 = hj_mul(irp3, irp2);
+  const HJet iq = hj_inv(hj_add(rp, zc)), iq2 = hj_mul(iq, iq);
+  const HJet cz = hj_mul(c, z), zmc = hj_sub(z, c);
+  const HJet one = hj_const(1.0);
+  const HJet irpiq = hj_mul(irp, iq);
+  // shared radial factors of the tangential / normal loads
+  const HJet tA = hj_sub(hj_scale(c4, hj_mul(zmc, irp3)), hj_scale(6.0, hj_mul(hj_mul(cz, zc), irp5)));
+  const HJet Bt = hj_axpy(k12, irpiq, tA);   // load tangential, component 3
+  const HJet Bn = hj_axpy(-k12, irpiq, hj_axpy(12.0, hj_mul(hj_mul(cz, zc), irp5), tA));  // normal load, components 1, 2
+#pragma unroll 1
+  for (int a = 0; a < 2; ++a) {
+    const HJet ra = a ? ry : rx, ra2 = hj_mul(ra, ra);
+    HJet v = hj_add(irp, hj_scale(c4, hj_mul(ra2, irp3)));
+    v = hj_add(v, hj_mul(hj_scale(2.0, hj_mul(cz, irp3)), hj_axpy(-3.0, hj_mul(ra2, irp2), one)));
+    v = hj_add(v, hj_mul(hj_scale(k12, iq), hj_sub(one, hj_mul(ra2, irpiq))));
+    u[a][a] = v;
+    u[a][2] = hj_mul(ra, Bt);
+    u[2][a] = hj_mul(ra, Bn);
+  }
+  u[0][1] = hj_mul(hj_mul(rx, ry), hj_sub(hj_sub(hj_scale(c4, irp3), hj_scale(6.0, hj_mul(cz, irp5))),
+                                          hj_scale(k12, hj_mul(irp, iq2))));
+  u[1][0] = u[0][1];
+  const HJet zc2 = hj_mul(zc, zc);
+  u[2][2] = hj_add(hj_add(hj_scale(8.0 * c1 * c1 - c4, irp), hj_mul(hj_sub(hj_scale(c4, zc2), hj_scale(2.0, cz)), irp3)),
+                   hj_scale(6.0, hj_mul(hj_mul(cz, zc2), irp5)));
+}
+struct IpHsc {
+  typedef double T;
+  double mu, nu, xp;
+  __device__ void sbie(int, const double* xi, const double rv[3], const double n[3], const T ut[3], const T uu[3],
+                       double rs, T du[3]) const {
+    const double c = xi[2] - xp;
+    double fu[9], ft[9];
+    hsc_point(nu, rv[0], rv[1], c, rv[2] - c, rv[2] + 2.0 * xp, n, fu, ft);
+    const double cu = 1.0 / (16.0 * kPi * mu * (1.0 - nu)), ct = 1.0 / (8.0 * kPi * (1.0 - nu));
+#pragma unroll
+    for (int il = 0; il < 3; ++il) {
+      double g = 0.0, h = 0.0;
+#pragma unroll
+      for (int ik = 0; ik < 3; ++ik) {
+        g += fu[3 * il + ik] * ut[ik];
+        h += ft[3 * il + ik] * uu[ik];
+      }
+      du[il] += cu * g - rs * ct * h;
+    }
+  }
+  __device__ void hbie(int, const double* xi, const double rv[3], const double n[3], const T ut[3], const T uu[3],
+                       double rs, T sg[3][3]) const {
+    // x = image + rv
+    const double xq[3] = {xi[0] + rv[0], xi[1] + rv[1], 2.0 * xp - xi[2] + rv[2]};
+    HJet xj[3], ij[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      xj[c] = hj_const(xq[c]);
+      xj[c].gx[c] = 1.0;
+      ij[c] = hj_const(xi[c]);
+      ij[c].gi[c] = 1.0;
+    }
+    HJet u[3][3];
+    hsc_u_jets(nu, xj, ij, xp, u);
+    const double Ku = 1.0 / (16.0 * kPi * mu * (1.0 - nu)), lam = 2.0 * mu * nu / (1.0 - 2.0 * nu);
+    // x_i derivative of t* = sigma*(x) n, sigma*_{l,kj} = lam d_kj div u_l + mu (u_lk,j + u_lj,k)
+    double dt[3][3][3];
+#pragma unroll 1
+    for (int l = 0; l < 3; ++l)
+#pragma unroll 1
+      for (int k = 0; k < 3; ++k)
+#pragma unroll 1
+        for (int p = 0; p < 3; ++p) {
+          const double div = u[l][0].H[0][p] + u[l][1].H[1][p] + u[l][2].H[2][p];
+          double v = 0.0;
+          for (int j = 0; j < 3; ++j) {
+            double sj = mu * (u[l][k].H[j][p] + u[l][j].H[k][p]);
+            if (j == k) sj += lam * div;
+            v += sj * n[j];
+          }
+          dt[l][k][p] = Ku * v;
+        }
+    // d*_lkp, s*_lkp contracted with n_i = e_kc: sg(:, kc) += d ut - rs s uu
+#pragma unroll 1
+    for (int kc = 0; kc < 3; ++kc)
+#pragma unroll 1
+      for (int l = 0; l < 3; ++l) {
+        double acc = 0.0;
+        for (int k = 0; k < 3; ++k) {
+          double dl = mu * Ku * (u[l][k].gi[kc] + u[kc][k].gi[l]);
+          double sl = mu * (dt[l][k][kc] + dt[kc][k][l]);
+          if (l == kc) {
+            dl += lam * Ku * (u[0][k].gi[0] + u[1][k].gi[1] + u[2][k].gi[2]);
+            sl += lam * (dt[0][k][0] + dt[1][k][1] + dt[2][k][2]);
+          }
+          acc += dl * ut[k] - rs * sl * uu[k];
+        }
+        sg[l][kc] += acc;
+      }
+  }
+};
+
 // q: [nf][6] = lambda (re, im), mu (re, im), rho, omega
 __global__ void k_harparh(const double* q, int nf, HarParH* out) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -279,7 +457,17 @@ struct IpArgs {
   void* slot;            // [nf][npairs][12] T
   int npairs;
   void* out;             // [nf][nip][12] T: u(3), then sigma(:, kc) for kc = 0..2
+  // image pass of a half-space region: pairs classified and integrated from
+  // the image (x_i1, x_i2, 2 xp - x_i3) of each point; points at a node add 0
+  int image;
+  double hs_xp;
 };
+// the point the pair geometry is measured from: the point, or its image
+__device__ __forceinline__ void ip_ref(const IpArgs& a, const double* xi, double xr[3]) {
+  xr[0] = xi[0];
+  xr[1] = xi[1];
+  xr[2] = a.image ? 2.0 * a.hs_xp - xi[2] : xi[2];
+}
 
 // point at a node: the last node (in node order) within 1e-12 csize
 __global__ void k_ip_onnode(IpArgs a) {
@@ -301,7 +489,8 @@ __global__ void k_ip_classify(DMesh m, IpArgs a, const QsCurves* __restrict__ qs
   for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < total;
        id += (long long)gridDim.x * blockDim.x) {
     const int ip = (int)(id / m.ne), e = (int)(id % m.ne);
-    const double* xi = a.xip + 3 * (size_t)ip;
+    double xi[3];
+    ip_ref(a, a.xip + 3 * (size_t)ip, xi);
     const double* b = m.ball + 4 * (size_t)e;
     const double r0 = b[0] - xi[0], r1 = b[1] - xi[1], r2 = b[2] - xi[2];
     double rmin = sqrt(r0 * r0 + r1 * r1 + r2 * r2) - b[3];
@@ -407,6 +596,8 @@ __global__ void k_ip_adp(DMesh m, IpArgs a, POL pol, const QsCurves* __restrict_
   const int pr = (int)(id % a.npairs), f = (int)(id / a.npairs);
   const int ip = a.pair_ip[pr], e = a.pair_e[pr];
   const double* xi = a.xip + 3 * (size_t)ip;
+  double xr[3];
+  ip_ref(a, xi, xr);
   const double* x = m.ex + 24 * (size_t)e;
   const T* uv = (const T*)a.uval + (size_t)f * a.nn * 3;
   const T* tv = (const T*)a.tval + (size_t)f * a.nn * 3;
@@ -440,11 +631,11 @@ __global__ void k_ip_adp(DMesh m, IpArgs a, POL pol, const QsCurves* __restrict_
       double bx[2], rmin, d;
       int method;
       if (nd.ks == 1) {
-        nearest_q8(x, m.cl[e], xi, bx, &rmin, &d, &method);
+        nearest_q8(x, m.cl[e], xr, bx, &rmin, &d, &method);
       } else {
         double xsub[24];
         subdiv_q8(x, nd.xs, xsub);
-        nearest_q8(xsub, clen_q8(xsub, 1e-12), xi, bx, &rmin, &d, &method);
+        nearest_q8(xsub, clen_q8(xsub, 1e-12), xr, bx, &rmin, &d, &method);
       }
       int gn = qs_estimate(*qs, 2, F, d, bx, true);
       bool sub = false;
@@ -496,14 +687,14 @@ __global__ void k_ip_adp(DMesh m, IpArgs a, POL pol, const QsCurves* __restrict_
           cross3(T1, T2, N);
           const double jg = norm3(N);
           const double n[3] = {N[0] / jg, N[1] / jg, N[2] / jg};
-          const double rv[3] = {xq[0] - xi[0], xq[1] - xi[1], xq[2] - xi[2]};
+          const double rv[3] = {xq[0] - xr[0], xq[1] - xr[1], xq[2] - xr[2]};
           const double jw = jg * js * jt1 * jt2 * gl11w(k1, g) * gl11w(k2, g);
           double w[8];
           for (int qq = 0; qq < 8; ++qq) w[qq] = phi[qq] * jw;
           T uu[3], ut[3];
           ip_weights<T>(un, tn, w, uu, ut);
-          if (h) pol.hbie(f, rv, n, ut, uu, rs, sg);
-          else pol.sbie(f, rv, n, ut, uu, rs, du);
+          if (h) pol.hbie(f, xi, rv, n, ut, uu, rs, sg);
+          else pol.sbie(f, xi, rv, n, ut, uu, rs, du);
         }
       }
     }
@@ -531,10 +722,12 @@ __global__ void __launch_bounds__(WPB * 32) k_ip_reg(DMesh m, IpArgs a, POL pol)
   const T* tv = (const T*)a.tval + (size_t)f * a.nn * 3;
   const int on = a.onnode[ip];
   if (on >= 0) {
-    if (lane < 12) o[lane] = lane < 3 ? uv[3 * on + lane] : VT<T>::zero();
+    if (lane < 12) o[lane] = (lane < 3 && !a.image) ? uv[3 * on + lane] : VT<T>::zero();
     return;
   }
   const double* xi = a.xip + 3 * (size_t)ip;
+  double xr[3];
+  ip_ref(a, xi, xr);
   T du[3], sg[3][3];
   for (int c = 0; c < 3; ++c) {
     du[c] = VT<T>::zero();
@@ -559,14 +752,14 @@ __global__ void __launch_bounds__(WPB * 32) k_ip_reg(DMesh m, IpArgs a, POL pol)
       const int P = m.ps_gln[c] * m.ps_gln[c];
       for (int k = lane; k < P; k += 32) {
         const size_t pt = (size_t)e * m.ptot + m.ps_off[c] + k;
-        const double rv[3] = {m.px[3 * pt] - xi[0], m.px[3 * pt + 1] - xi[1], m.px[3 * pt + 2] - xi[2]};
+        const double rv[3] = {m.px[3 * pt] - xr[0], m.px[3 * pt + 1] - xr[1], m.px[3 * pt + 2] - xr[2]};
         const double n[3] = {m.pn[3 * pt], m.pn[3 * pt + 1], m.pn[3 * pt + 2]};
         double wq[8];
         for (int q = 0; q < 8; ++q) wq[q] = m.pphi[8 * pt + q];
         T uu[3], ut[3];
         ip_weights<T>(nv[w], nv[w] + 24, wq, uu, ut);
-        if (h) pol.hbie(f, rv, n, ut, uu, rs, sg);
-        else pol.sbie(f, rv, n, ut, uu, rs, du);
+        if (h) pol.hbie(f, xi, rv, n, ut, uu, rs, sg);
+        else pol.sbie(f, xi, rv, n, ut, uu, rs, du);
       }
     }
   }

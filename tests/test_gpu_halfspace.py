@@ -113,3 +113,34 @@ def test_halfspace_geometry_errors():
     R.set_halfspace(0, 0.0, 1)
     R.build_lse_staela(mat["mu"], mat["nu"])
     R.close()
+
+
+def test_static_internal_points_of_a_half_space(oracle):
+    """Static internal points of a half-space region: the complementary
+    kernels (hsc_sbie_auto, hsc_hbie_auto) added from the points' images
+    (calculate_internal_points_mechanics_static.f90:288-310,401-418), device
+    against the oracle (<= 1e-10) and Holl's vertical stress below the centre
+    of the loaded square (quadrature tolerance); a point above the free surface
+    is refused."""
+    a, p = 1.0, 1.0
+    d = M.halfspace_footing(a, 4, p)
+    mat = M.elastic(1.0, 0.25)
+    P = oracle.Problem(d)
+    P.set_halfspace(-3, 0.0, 1)
+    R = BemRegion(d)
+    R.set_halfspace(-3, 0.0, 1)
+    u, t = R.solution(R.solve_staela(mat["mu"], mat["nu"], precision="plain"))
+    zs = np.array([0.25, 0.5, 1.0, 2.0])
+    xip = np.concatenate([np.stack([np.zeros(4), np.zeros(4), zs], 1),
+                          np.array([[0.7, -0.4, 0.3], [1.5, 1.2, 0.05], [-2.0, 0.5, 1.0]])])
+    ud, sd = R.internal_points(xip, u, t, mu=mat["mu"], nu=mat["nu"])
+    uo, so = P.internal_points(xip, u, t, mu=mat["mu"], nu=mat["nu"])
+    print("u", rel(ud, uo), "sigma", rel(sd, so))
+    assert rel(ud, uo) <= 1e-10 and rel(sd, so) <= 1e-10
+    R2 = np.sqrt(2 * a * a + zs ** 2)
+    holl = -(2 * p / np.pi) * (np.arctan(a * a / (zs * R2)) + (a * a * zs / R2) * (2.0 / (a * a + zs ** 2)))
+    assert np.abs(sd[:4, 2, 2] - holl).max() < 1e-6 * np.abs(holl).max()
+    with pytest.raises(MfbemError) as e:
+        R.internal_points(np.array([[0.0, 0.0, -0.1]]), u, t, mu=mat["mu"], nu=mat["nu"])
+    assert e.value.code == _abi.MFBEM_EGEOMETRY
+    R.close()
