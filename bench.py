@@ -633,6 +633,8 @@ def configs_form():
              mixed sweeps;
       half-space footing: staela, 8x8 quad8 loaded square on the surface of a
              half-space (complementary kernel), plain, with Love's closed form;
+      penny crack in a cube: staela, a crack-like boundary (dual BEM, six
+             rows per crack node) inside a clamped cube, plain and mixed;
       Burton & Miller cube: the cube 8x8 of the headline with the
              'dual_bm_same' formulation (SBIE + i/c2 HBIE at the 3072 HBIE
              points), four frequencies, plain and mixed sweeps, the oracle on
@@ -645,8 +647,8 @@ def configs_form():
     def rel(a, b):
         return float(np.abs(a - b).max() / np.abs(b).max())
 
-    def static_case(deck, mat, hs, reps):
-        R = BemRegion(deck)
+    def static_case(deck, mat, hs, reps, crack=None):
+        R = BemRegion(deck, crack=crack)
         if hs:
             R.set_halfspace(-3, 0.0, 1)
         res = {}
@@ -663,6 +665,8 @@ def configs_form():
         P = O.Problem(deck)
         if hs:
             P.set_halfspace(-3, 0.0, 1)
+        if crack is not None:
+            P.set_crack(*crack)
         P.assemble_staela(mat["mu"], mat["nu"], nthreads=cores)  # warm-up
         ts = []
         for _ in range(3):
@@ -691,6 +695,17 @@ def configs_form():
     res["love_centre_settlement"] = {"gpu": float(u[c, 2]), "closed_form": w, "rel_err": abs(u[c, 2] - w) / w}
     res["n_dof"] = deck.n_dof
     out["halfspace_footing_8x8"] = res
+
+    # crack-like boundary (dual BEM): pressurised penny crack inside a clamped
+    # cube 8 x 8 x 8 (crack 4 x 4 + 4 x (4 x 3) quad8, cube 4 x 4 per face)
+    deck, crack = M.penny_crack_in_box(1.0, 4, 3, 4.0, 4)
+    res, xs, P = static_case(deck, mat, False, 10, crack=crack)
+    u1, _, u2, _ = P.solution_faces(xs["plain"])
+    c = int(np.argmin(np.linalg.norm(deck.nodes, axis=1)))
+    res["n_dof"] = P.n
+    res["opening_at_centre"] = {"gpu": float(u2[c, 2] - u1[c, 2]),
+                                "sneddon_full_space": float(M.sneddon_opening(0.0, 1.0, 1.0, 1.0, 0.25))}
+    out["penny_crack_in_cube"] = res
 
     deck, mat, om = M.workload(5)
     R = BemRegion(deck)
